@@ -1,0 +1,245 @@
+"""ctypes bindings for the CPU oracle (test infrastructure only).
+
+Two checkers live under ``oracle/``:
+
+* ``build/libmhd_oracle.so`` -- the plain-C restatement ``mhd_oracle.c`` of
+  ppkMHD's MUSCL-Hancock + HLLD + CT step (built by ``make -C oracle``);
+* ``_ref/libppkmhd_ref{64,32}.so`` -- the reference's own functor sources
+  compiled against the Kokkos-API shim (built by ``oracle/build_ref.sh``
+  where the reference tree is present).
+
+Only tests, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
+import this module.  Arrays cross the boundary as numpy float64 arrays in the
+layout of the library being called: the C oracle uses LayoutLeft
+(``[var][k][j][i]``), the compiled reference uses LayoutRight
+(``[i][j][k][var]``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "build", "libmhd_oracle.so")
+REF_SO = {64: os.path.join(HERE, "_ref", "libppkmhd_ref64.so"),
+          32: os.path.join(HERE, "_ref", "libppkmhd_ref32.so")}
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+class OrcParams(ctypes.Structure):
+    """Mirror of ``orc_params`` in mhd_oracle.h."""
+
+    _fields_ = [
+        ("dim", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+        ("ghost", ctypes.c_int), ("isize", ctypes.c_int), ("jsize", ctypes.c_int),
+        ("ksize", ctypes.c_int),
+        ("xmin", ctypes.c_double), ("xmax", ctypes.c_double), ("ymin", ctypes.c_double),
+        ("ymax", ctypes.c_double), ("zmin", ctypes.c_double), ("zmax", ctypes.c_double),
+        ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
+        ("gamma0", ctypes.c_double), ("cfl", ctypes.c_double), ("slope_type", ctypes.c_double),
+        ("smallr", ctypes.c_double), ("smallc", ctypes.c_double), ("smallp", ctypes.c_double),
+        ("cIso", ctypes.c_double),
+        ("riemann", ctypes.c_int), ("version", ctypes.c_int), ("bc", ctypes.c_int * 6),
+        ("tEnd", ctypes.c_double), ("tCurrent", ctypes.c_double), ("nStepmax", ctypes.c_int),
+        ("ot_kt", ctypes.c_double), ("problem_is_ot", ctypes.c_int),
+    ]
+
+
+def build_oracle() -> None:
+    """Compile the C restatement (gcc, seconds)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_SO):
+            build_oracle()
+        L = ctypes.CDLL(ORACLE_SO)
+        L.orc_params_from_ini.argtypes = [ctypes.c_char_p, ctypes.POINTER(OrcParams)]
+        L.orc_params_from_ini.restype = ctypes.c_int
+        L.orc_create.argtypes = [ctypes.POINTER(OrcParams), ctypes.c_int]
+        L.orc_create.restype = ctypes.c_void_p
+        L.orc_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_set_state.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_get_state.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_run.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_run.restype = ctypes.c_int
+        L.orc_time.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.POINTER(ctypes.c_int)]
+        L.orc_nelem.argtypes = [ctypes.POINTER(OrcParams)]
+        L.orc_nelem.restype = ctypes.c_int64
+        L.orc_init_orszag_tang.argtypes = [ctypes.POINTER(OrcParams), _dp]
+        L.orc_make_boundaries.argtypes = [ctypes.POINTER(OrcParams), _dp]
+        L.orc_riemann.argtypes = [ctypes.POINTER(OrcParams), _dp, _dp, _dp]
+        L.orc_compute_emf.argtypes = [ctypes.POINTER(OrcParams), ctypes.c_int, _dp]
+        L.orc_compute_emf.restype = ctypes.c_double
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def params_from_ini(ini_text: str) -> OrcParams:
+    p = OrcParams()
+    rc = lib().orc_params_from_ini(ini_text.encode(), ctypes.byref(p))
+    if rc != 0:
+        raise ValueError("oracle: unsupported solver_name in .ini")
+    return p
+
+
+def state_shape(p: OrcParams):
+    """LayoutLeft numpy shape [var][k][j][i] (2D: [var][j][i])."""
+    if p.dim == 2:
+        return (8, p.jsize, p.isize)
+    return (8, p.ksize, p.jsize, p.isize)
+
+
+class OracleSolver:
+    """The C restatement driven like the reference solver (ctor + main loop)."""
+
+    def __init__(self, ini_text: str, nthreads: int = 1):
+        self.p = params_from_ini(ini_text)
+        self.h = lib().orc_create(ctypes.byref(self.p), int(nthreads))
+
+    def close(self):
+        if self.h:
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_state(self, U: np.ndarray):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        assert U.shape == state_shape(self.p)
+        lib().orc_set_state(self.h, _ptr(U))
+
+    def get_state(self) -> np.ndarray:
+        U = np.empty(state_shape(self.p), dtype=np.float64)
+        lib().orc_get_state(self.h, _ptr(U))
+        return U
+
+    def run(self, n: int) -> int:
+        return lib().orc_run(self.h, int(n))
+
+    def time(self):
+        t, dt, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        lib().orc_time(self.h, ctypes.byref(t), ctypes.byref(dt), ctypes.byref(it))
+        return t.value, dt.value, it.value
+
+
+def orszag_tang(p: OrcParams) -> np.ndarray:
+    U = np.zeros(state_shape(p), dtype=np.float64)
+    lib().orc_init_orszag_tang(ctypes.byref(p), _ptr(U))
+    return U
+
+
+def riemann(p: OrcParams, qL, qR) -> np.ndarray:
+    l = np.ascontiguousarray(qL, dtype=np.float64)
+    r = np.ascontiguousarray(qR, dtype=np.float64)
+    f = np.zeros(8)
+    lib().orc_riemann(ctypes.byref(p), _ptr(l), _ptr(r), _ptr(f))
+    return f
+
+
+def compute_emf(p: OrcParams, emf_dir: int, q_edge) -> float:
+    q = np.ascontiguousarray(q_edge, dtype=np.float64).reshape(4, 8)
+    return float(lib().orc_compute_emf(ctypes.byref(p), int(emf_dir), _ptr(q)))
+
+
+# ---------------------------------------------------------------- reference
+
+def ref_available(bits: int = 64) -> bool:
+    return os.path.exists(REF_SO[bits])
+
+
+class RefSolver:
+    """The reference's own functors (compiled via the Kokkos-API shim)."""
+
+    def __init__(self, ini_text: str, bits: int = 64):
+        L = ctypes.CDLL(REF_SO[bits])
+        self.real = np.float64 if bits == 64 else np.float32
+        L.ref_create.argtypes = [ctypes.c_char_p]
+        L.ref_create.restype = ctypes.c_void_p
+        L.ref_destroy.argtypes = [ctypes.c_void_p]
+        L.ref_sizes.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+        L.ref_get_state.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.ref_set_state.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.ref_run.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.ref_run.restype = ctypes.c_int
+        L.ref_time.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.POINTER(ctypes.c_int)]
+        self.L = L
+        self.h = L.ref_create(ini_text.encode())
+        if not self.h:
+            raise ValueError("reference: unsupported solver_name")
+        sz = (ctypes.c_int * 6)()
+        L.ref_sizes(self.h, sz)
+        self.isize, self.jsize, self.ksize, self.nbvar, self.dim, self.ghost = list(sz)
+
+    def close(self):
+        if self.h:
+            self.L.ref_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _right_shape(self):
+        if self.dim == 2:
+            return (self.isize, self.jsize, self.nbvar)
+        return (self.isize, self.jsize, self.ksize, self.nbvar)
+
+    def get_state(self) -> np.ndarray:
+        """Returned in LayoutLeft [var][k][j][i] (float64)."""
+        U = np.empty(self._right_shape(), dtype=self.real)
+        self.L.ref_get_state(self.h, U.ctypes.data_as(ctypes.c_void_p))
+        return np.ascontiguousarray(U.T, dtype=np.float64)
+
+    def set_state(self, U_left: np.ndarray):
+        U = np.ascontiguousarray(np.asarray(U_left).T, dtype=self.real)
+        assert U.shape == self._right_shape()
+        self.L.ref_set_state(self.h, U.ctypes.data_as(ctypes.c_void_p))
+
+    def run(self, n: int) -> int:
+        return self.L.ref_run(self.h, int(n))
+
+    def time(self):
+        t, dt, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        self.L.ref_time(self.h, ctypes.byref(t), ctypes.byref(dt), ctypes.byref(it))
+        return t.value, dt.value, it.value
+
+
+def ref_probe_lib(bits: int = 64):
+    L = ctypes.CDLL(REF_SO[bits])
+    real = ctypes.c_double if bits == 64 else ctypes.c_float
+    rp = ctypes.POINTER(real)
+    L.ref_riemann.argtypes = [ctypes.c_char_p, rp, rp, rp]
+    L.ref_compute_emf.argtypes = [ctypes.c_char_p, ctypes.c_int, rp]
+    L.ref_compute_emf.restype = real
+    L.ref_params.argtypes = [ctypes.c_char_p, _dp]
+    return L
+
+
+def interior(U: np.ndarray, ghost: int = 3) -> np.ndarray:
+    g = ghost
+    if U.ndim == 3:
+        return U[:, g:-g, g:-g]
+    return U[:, g:-g, g:-g, g:-g]
+
+
+def rel_l1(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """Per-variable relative L1 error sum|a-b| / sum|b| over the interior."""
+    ax = tuple(range(1, a.ndim))
+    num = np.abs(a - b).sum(axis=ax)
+    den = np.abs(b).sum(axis=ax)
+    return num / np.where(den > 0, den, 1.0)
