@@ -1,0 +1,379 @@
+"""Benchmark of the MUSCL-Hancock + HLLD + CT MHD step on GB300.
+
+Default workload: 3D Orszag-Tang 256^3 (periodic, HLLD, CFL 0.8, gamma0 5/3
+float-rounded as the reference's ConfigMap does, seeded 1e-3 uniform velocity
+perturbation), FP64 plain path.  A "step" is one full iteration of the solver
+(boundaries, primitives, CFL dt, slopes, half step, HLLD fluxes, CT EMFs,
+update).  Metric: interior cell-updates per second.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--workload ot3d_256_fp64|ot3d_256_fp32|ot2d_256_fp64]
+
+One JSON line is printed by rank 0.  Multi-GPU runs (torchrun) are independent
+replicas of the workload, one per GPU ("replicas only": the path has no
+exchange step on one problem per GPU).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+WORKLOADS = {
+    # name: (dim, n, precision, label)
+    "ot3d_256_fp64": (3, 256, 64, "3D Orszag-Tang 256^3, FP64 plain MUSCL-Hancock+HLLD+CT"),
+    "ot3d_256_fp32": (3, 256, 32, "3D Orszag-Tang 256^3, FP32 plain MUSCL-Hancock+HLLD+CT"),
+    "ot2d_256_fp64": (2, 256, 64, "2D Orszag-Tang 256^2, FP64 plain MUSCL-Hancock+HLLD+CT"),
+}
+
+
+def ot_ini(dim: int, n: int, precision: int) -> str:
+    lines = ["[run]", f"solver_name=MHD_Muscl_{dim}D", "tEnd=1000.0", "nStepmax=100000000",
+             "nOutput=0", "[mesh]", f"nx={n}", f"ny={n}"]
+    if dim == 3:
+        lines.append(f"nz={n}")
+    for f in ("xmin", "xmax", "ymin", "ymax", "zmin", "zmax")[: 2 * dim]:
+        lines.append(f"boundary_type_{f}=3")
+    lines += ["[hydro]", "gamma0=1.6666666666666667", "cfl=0.8", "slope_type=2",
+              "problem=orszag_tang", "riemann=hlld", "smallr=1e-8", "smallc=1e-8",
+              "[OTHER]", "implementationVersion=2", "[gb300]", f"precision={precision}"]
+    return "\n".join(lines) + "\n"
+
+
+def perturbed_ot_state(U: np.ndarray, seed: int = 1234, amp: float = 1e-3) -> np.ndarray:
+    """Seeded uniform(-amp, amp) velocity perturbation of every cell, density
+    kept, total energy recomputed with the perturbed kinetic energy."""
+    rng = np.random.default_rng(seed)
+    U = U.astype(np.float64, copy=True)
+    rho = U[0]
+    ekin_old = 0.5 * (U[2] ** 2 + U[3] ** 2 + U[4] ** 2) / rho
+    for v in (2, 3, 4):
+        U[v] += rho * rng.uniform(-amp, amp, size=rho.shape)
+    ekin_new = 0.5 * (U[2] ** 2 + U[3] ** 2 + U[4] ** 2) / rho
+    U[1] += ekin_new - ekin_old
+    return U
+
+
+# ---------------------------------------------------------------- clocks
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- helpers
+
+def load_peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def emit(obj):
+    print(json.dumps(obj), flush=True)
+
+
+# ---------------------------------------------------------------- CPU side
+
+def cpu_baseline_run(dim: int, n: int, steps: int, warmup: int, nthreads: int):
+    """The oracle port of the reference step (oracle/mhd_oracle.c) on the host
+    cores: same workload, full grid, `steps` timed iterations."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+
+    oracle_py.build_oracle()
+    ini = ot_ini(dim, n, 64)
+    s = oracle_py.OracleSolver(ini, nthreads=nthreads)
+    if dim == 3:
+        s.set_state(perturbed_ot_state(s.get_state()))
+    if warmup:
+        s.run(warmup)
+    t0 = time.perf_counter()
+    s.run(steps)
+    el = time.perf_counter() - t0
+    s.close()
+    cells = n ** dim
+    return cells * steps / el, el
+
+
+# ---------------------------------------------------------------- GPU side
+
+def run_gb300(args):
+    world, rank, local = dist_setup()
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import ppkmhd_gb300 as m
+
+    dim, n, precision, label = WORKLOADS[args.workload]
+    ini = ot_ini(dim, n, precision)
+    p = m.params_from_ini(ini)
+    p.device = local
+    s = m.MHDSolver(p)
+    s.init_problem()
+    U0 = s.get_state()
+    if dim == 3:
+        s.set_state(perturbed_ot_state(U0).astype(s.real))
+        U0 = s.get_state()
+    interior_cells, ghost_cells = s.cell_counts()
+    state_bytes = U0.nbytes
+    real_bytes = 8 if precision == 64 else 4
+
+    # warm-up (device-resident, graph replay)
+    s.run_timed(max(args.warmup, 3))
+
+    # ---- timed region: device-resident state, CUDA events on the library stream
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms = s.run_timed(args.steps)
+    torch.cuda.synchronize()
+    t_sec = ms / 1e3
+    if world > 1:
+        tt = torch.tensor([t_sec], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_sec = float(tt.item())
+    value = world * interior_cells * args.steps / t_sec
+
+    # ---- per-kernel timing of one iteration (events around every launch)
+    prof = {}
+    for _ in range(3):
+        for name, kms in s.profile_step():
+            prof.setdefault(name, []).append(kms)
+    prof = {k: float(np.median(v)) for k, v in prof.items()}
+    step_ms = sum(prof.values())
+    dom = max(prof, key=prof.get)
+
+    # ---- end to end through the host-buffer ABI call (H2D + step + D2H per step)
+    e2e_steps = max(2, min(args.steps, 10))
+    h_in = torch.empty(U0.size, dtype=torch.float64 if precision == 64 else torch.float32,
+                       pin_memory=True)
+    h_out = torch.empty_like(h_in, pin_memory=True)
+    h_in.numpy()[:] = U0.reshape(-1)
+    s.step_host_ptr(h_in.data_ptr(), h_out.data_ptr())  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for q in range(e2e_steps):
+        a, b = (h_in, h_out) if q % 2 == 0 else (h_out, h_in)
+        s.step_host_ptr(a.data_ptr(), b.data_ptr())
+    e2e_sec = time.perf_counter() - t0
+    e2e_value = world * interior_cells * e2e_steps / e2e_sec
+
+    hbm_peak, peak_kind = load_peaks()
+    alg_bytes_per_cell = 16 * real_bytes
+    achieved = alg_bytes_per_cell * interior_cells / (prof[dom] / 1e3) / 1e9
+    step_achieved = alg_bytes_per_cell * interior_cells / (step_ms / 1e3) / 1e9
+    traffic = load_profile_traffic(args.workload, dom)
+
+    # FP32 companion figure for the same workload (device-resident)
+    variants = {}
+    if args.workload == "ot3d_256_fp64" and not args.no_variants:
+        p32 = m.params_from_ini(ot_ini(dim, n, 32))
+        p32.device = local
+        s32 = m.MHDSolver(p32)
+        s32.set_state(U0.astype(np.float32))
+        s32.run_timed(3)
+        ms32 = s32.run_timed(args.steps)
+        variants["fp32"] = {"value": interior_cells * args.steps / (ms32 / 1e3),
+                            "ms_per_step": ms32 / args.steps, "dtype": "f32",
+                            "note": "FP32 storage and arithmetic, FP64 dt/sums/div B"}
+        s32.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        v, el = cpu_baseline_run(dim, n, steps=args.cpu_steps, warmup=1, nthreads=nthreads)
+        cpu = {"value": v, "unit": "cell-updates/s", "cores": nthreads, "kind": "port",
+               "sample": f"{args.cpu_steps} steps of the same {n}^{dim} grid after 1 warm-up "
+                         f"step, oracle/mhd_oracle.c with {nthreads} OpenMP threads "
+                         f"({el:.1f} s timed)"}
+
+    if rank == 0:
+        out = {
+            "metric": "MHD cell-updates/s (interior cells), plain MUSCL-Hancock+HLLD+CT step",
+            "value": value,
+            "unit": "cell-updates/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": max(args.warmup, 3),
+            "ms_per_step": t_sec * 1e3 / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64" if precision == 64 else "f32",
+            "data": "synthetic: Orszag-Tang initial condition"
+                    + (" + seeded 1e-3 velocity perturbation" if dim == 3 else ""),
+            "config": {"workload": label, "grid": [n] * dim, "cells": interior_cells,
+                       "cells_with_ghosts": ghost_cells, "state_bytes": state_bytes,
+                       "l2": "inputs larger than L2 (state %.2f GB per array)" % (state_bytes / 1e9),
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "kernels_per_step": s.launches_per_step(),
+                       "per_kernel_ms": prof},
+            "e2e": {"value": e2e_value, "unit": "cell-updates/s",
+                    "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes,
+                    "steps": e2e_steps,
+                    "call": "mhd_step_host (pinned host buffers, copies inside the timed region)"},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+                         "peak_source": f"hbm_gbs of {peak_kind}",
+                         "algorithmic_bytes_per_cell": alg_bytes_per_cell,
+                         "step_achieved": step_achieved,
+                         "step_frac": step_achieved / hbm_peak},
+            "clocks": clk.summary(),
+            "gpu_launches": s.launches_per_step() * args.steps,
+            "cpu_baseline": cpu,
+            "variants": variants,
+        }
+        emit(out)
+    s.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def load_profile_traffic(workload: str, kernel: str):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (profiles/*.json), or None."""
+    path = os.path.join(ROOT, "profiles", f"traffic_{workload}.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d.get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+# ---------------------------------------------------------------- reference arm
+
+def run_reference(args):
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return
+    dim, n, precision, label = WORKLOADS[args.workload]
+    nthreads = os.cpu_count() or 1
+    steps = args.ref_steps
+    v, el = cpu_baseline_run(dim, n, steps=steps, warmup=min(args.warmup, 1), nthreads=nthreads)
+    emit({
+        "impl": "reference",
+        "metric": "MHD cell-updates/s (interior cells), plain MUSCL-Hancock+HLLD+CT step",
+        "value": v,
+        "unit": "cell-updates/s",
+        "n_gpus": world,
+        "steps": steps,
+        "warmup": min(args.warmup, 1),
+        "ms_per_step": el * 1e3 / steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic: Orszag-Tang initial condition"
+                + (" + seeded 1e-3 velocity perturbation" if dim == 3 else ""),
+        "config": {"workload": label, "grid": [n] * dim,
+                   "implementation": "CPU port of the reference step (oracle/mhd_oracle.c, "
+                                     "bitwise equal to the reference functors), OpenMP"},
+        "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": nthreads, "kind": "port",
+                         "sample": f"{steps} steps of the full {n}^{dim} grid"},
+        "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    })
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="ot3d_256_fp64", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--ref-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-variants", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,179 @@
+/*
+ * ppkmhd_gb300 -- C ABI of the GB300-native (sm_103a) MUSCL-Hancock + HLLD +
+ * constrained-transport MHD step.
+ *
+ * Drop-in boundary: this ABI replaces the device side of ppkMHD's
+ * SolverMHDMuscl<dim> (src/muscl/SolverMHDMuscl.h, .cpp).  The C++ host layer
+ * in ppkmhd_gb300/host (ConfigMap, HydroParams, SolverBase, SolverFactory,
+ * SolverMHDMusclGPU) keeps the reference's plugin interface and calls these
+ * functions.  All functions return an int status (MHD_OK = 0); on error the
+ * message is available from mhd_last_error().  No function aborts, traps or
+ * prints.  A context is used by one host thread at a time; it owns one CUDA
+ * stream and all device buffers.  Host arrays are owned by the caller and
+ * only copied.
+ *
+ * State arrays hold the 8 conservative variables of the reference
+ * (enums.h:17-34: rho, E, rho*u, rho*v, rho*w, Bx, By, Bz), ghost cells
+ * included (ghost width 3), with face-centred magnetic field components
+ * (U(i,j,k,IA) is Bx on the face at i-1/2).
+ */
+#ifndef PPKMHD_GB300_H
+#define PPKMHD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MHD_ABI_VERSION 1
+
+/* status codes */
+#define MHD_OK 0
+#define MHD_ERR_INVALID_ARG -1  /* bad pointer, size, enum value or unsupported option */
+#define MHD_ERR_CUDA -2         /* a CUDA runtime call failed (message has the CUDA error) */
+#define MHD_ERR_NO_DEVICE -3    /* no CUDA device / the CUDA kernels are missing */
+#define MHD_ERR_NUMERIC -4      /* device status word: non-finite or non-positive state */
+#define MHD_ERR_PARSE -5        /* .ini text rejected */
+#define MHD_ERR_TOO_LARGE -6    /* request larger than a fixed limit */
+
+/* enums.h:94-101 (RiemannSolverType); only the MHD solvers are accepted */
+#define MHD_RIEMANN_LLF 1
+#define MHD_RIEMANN_HLL 2
+#define MHD_RIEMANN_HLLD 4
+
+/* enums.h:105-112 (BoundaryConditionType) */
+#define MHD_BC_REFLECTING 1 /* BC_DIRICHLET */
+#define MHD_BC_OUTFLOW 2    /* BC_NEUMANN */
+#define MHD_BC_PERIODIC 3   /* BC_PERIODIC */
+
+/* arithmetic of the step */
+#define MHD_FP64 64
+#define MHD_FP32 32
+/* FP64 only: MHD_FP_EXACT compiles without FMA contraction and keeps every
+ * operation of the reference in its order, so results are bitwise equal to a
+ * serial run of the reference built without FMA; MHD_FP_FAST lets the
+ * compiler contract multiply-adds. */
+#define MHD_FP_FAST 0
+#define MHD_FP_EXACT 1
+
+/* host array layouts */
+#define MHD_LAYOUT_LEFT 0  /* [var][k][j][i], i fastest (Kokkos LayoutLeft, the CUDA build) */
+#define MHD_LAYOUT_RIGHT 1 /* [i][j][k][var], var fastest (Kokkos LayoutRight, the OpenMP build) */
+
+/* initial conditions */
+#define MHD_PROBLEM_ORSZAG_TANG 0
+
+/*
+ * Run/mesh/scheme parameters.  Mirrors the fields of HydroParams /
+ * HydroSettings (src/shared/HydroParams.h:28-234) that the MHD MUSCL step
+ * reads, plus SolverBase's tEnd/tCurrent (SolverBase.cpp:119-120).  Real
+ * parameters are doubles; mhd_params_from_ini() rounds them through float as
+ * ConfigMap::getFloat does (ConfigMap.cpp:38-46).
+ */
+typedef struct mhd_params
+{
+  int    dim;        /* 2 or 3 */
+  int    nx, ny, nz; /* interior cells (nz ignored in 2D) */
+  int    ghost;      /* ghost width, must be 3 */
+  double xmin, xmax, ymin, ymax, zmin, zmax;
+  double gamma0, cfl, slope_type, smallr, smallc;
+  int    riemann;    /* MHD_RIEMANN_* */
+  int    implementation_version; /* [OTHER] implementationVersion; 2 is implemented */
+  int    boundary[6];            /* xmin, xmax, ymin, ymax, zmin, zmax: MHD_BC_* */
+  double tEnd, tCurrent;
+  int    nStepmax;
+  int    problem;    /* MHD_PROBLEM_* */
+  double ot_kt;      /* [OrszagTang] kt */
+  int    precision;  /* MHD_FP64 or MHD_FP32 */
+  int    fp_mode;    /* MHD_FP_FAST or MHD_FP_EXACT */
+  int    device;     /* CUDA device ordinal the context binds (default 0) */
+} mhd_params;
+
+typedef struct mhd_ctx mhd_ctx;
+
+/* Fill defaults: HydroParams()/HydroSettings() constructors (HydroParams.h:41-58,
+ * :156-204), with the MHD solver's 3 ghost cells. */
+int mhd_params_default(mhd_params *p);
+
+/* Parse .ini text with the reference's rules: INIReader (lower-cased
+ * "section.name" keys, inline ';' comments, continuation lines),
+ * ConfigMap::getFloat (strtof, float-rounded), getInteger (strtol base 0), and
+ * HydroParams::setup (HydroParams.cpp:27-217).  Replaces
+ * broadcast_parameters() + HydroParams::setup() (main.cpp:133-137). */
+int mhd_params_from_ini(const char *ini_text, mhd_params *p, char *err, size_t errlen);
+
+/* Allocate device buffers for one problem and set up the stream.
+ * Replaces the allocations of SolverMHDMuscl<dim>::SolverMHDMuscl
+ * (SolverMHDMuscl.h:211-387).  The state is zero until mhd_init_problem or
+ * mhd_set_state. */
+int mhd_create(const mhd_params *p, mhd_ctx **ctx);
+int mhd_destroy(mhd_ctx *ctx);
+
+/* Initial condition + boundaries + U2 = U + primitives + dt, i.e. the tail of
+ * the solver constructor (SolverMHDMuscl.h:390-402). */
+int mhd_init_problem(mhd_ctx *ctx);
+
+/* Inject a full ghost-inclusive state (real_bytes 8 or 4, matching the
+ * context precision) and redo boundaries, primitives and dt; resets the
+ * iteration count to 0 and t to tCurrent. */
+int mhd_set_state(mhd_ctx *ctx, const void *U, int layout, int real_bytes);
+
+/* Copy out the current solution (the array the next step reads: U when the
+ * iteration count is even, U2 otherwise -- SolverMHDMuscl.h:791-805). */
+int mhd_get_state(mhd_ctx *ctx, void *U, int layout, int real_bytes);
+
+/* One SolverBase::next_iteration (SolverBase.cpp:205-220) = one
+ * godunov_unsplit (SolverMHDMuscl.h:791-805, .cpp:373-572): boundaries,
+ * primitives, CFL dt (clipped to tEnd), slopes, half step, edge fields, HLLD
+ * face fluxes, CT edge EMFs and the update; then iteration += 1, t += dt.
+ * Does nothing when finished() holds.  Asynchronous (dt stays on device). */
+int mhd_step(mhd_ctx *ctx);
+
+/* Up to nsteps iterations of main.cpp:154-159 from a CUDA graph, stopping
+ * (on device) when t >= tEnd - 1e-14 or iteration >= nStepmax.  Returns after
+ * the stream is synchronised; *done = iterations executed. */
+int mhd_run(mhd_ctx *ctx, int nsteps, int *done);
+
+/* godunov_unsplit_impl(data_in, data_out) on HOST arrays: copy U_in to the
+ * device, run one iteration, copy the result back.  The state inside the
+ * context is replaced by U_in first, so t/dt bookkeeping continues. */
+int mhd_step_host(mhd_ctx *ctx, const void *U_in, void *U_out, int layout, int real_bytes);
+
+/* t, the dt of the last computed CFL condition, and the iteration count
+ * (SolverBase m_t, m_dt, m_iteration).  Synchronises the stream. */
+int mhd_time(mhd_ctx *ctx, double *t, double *dt, int *iteration);
+
+/* FP64 diagnostics of the current state over interior cells: sums[8] of the
+ * conservative variables (cell-centred B for the field components), and the
+ * L1 / max norms of the discrete divergence of the face-centred field. */
+int mhd_diagnostics(mhd_ctx *ctx, double sums[8], double *divb_l1, double *divb_max);
+
+/* Device-resident stepping for timing: run nsteps iterations (no early stop
+ * check on the host) and return the elapsed device time measured with CUDA
+ * events on the context's stream. */
+int mhd_run_timed(mhd_ctx *ctx, int nsteps, float *ms);
+
+/* Time each kernel of one iteration separately (CUDA events around every
+ * launch, on the context's stream).  names/ms receive up to max entries;
+ * *count = number of kernels in an iteration. */
+int mhd_profile_step(mhd_ctx *ctx, const char **names, float *ms, int max, int *count);
+
+/* Cells updated per iteration (interior) and per the reference's own count
+ * (ghost cells included, SolverMHDMuscl.h:256 + solver_utils.h:55-56). */
+int mhd_cell_counts(mhd_ctx *ctx, int64_t *interior, int64_t *with_ghosts);
+
+/* Sizes of the ghost-inclusive arrays: isize, jsize, ksize (1 in 2D), nbvar. */
+int mhd_sizes(mhd_ctx *ctx, int sizes[4]);
+
+/* Number of kernel launches one iteration makes. */
+int mhd_launches_per_step(mhd_ctx *ctx, int *n);
+
+const char *mhd_last_error(mhd_ctx *ctx);
+const char *mhd_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PPKMHD_GB300_H */

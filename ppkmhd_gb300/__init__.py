@@ -1,0 +1,269 @@
+"""ppkmhd_gb300: GB300-native MUSCL-Hancock + HLLD + CT MHD step.
+
+Python view of the C ABI in ``include/ppkmhd_gb300.h`` (library
+``ppkmhd_gb300/lib/libppkmhd_gb300.so``, built by ``ppkmhd_gb300.build``).
+The compute path is the CUDA library only: if it is missing, importing the
+binding raises, and creating a solver without a GPU returns the library's
+MHD_ERR_NO_DEVICE as an exception.  There is no CPU fallback.
+
+Typical use, mirroring ppkMHD's driver (src/main.cpp)::
+
+    from ppkmhd_gb300 import MHDSolver
+    s = MHDSolver.from_ini(open("orszag_tang_2d.ini").read())
+    s.init_problem()
+    s.run(100)
+    U = s.get_state()           # numpy [var][(k)][j][i], ghosts included
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libppkmhd_gb300.so")
+
+MHD_OK = 0
+MHD_ERR_INVALID_ARG = -1
+MHD_ERR_CUDA = -2
+MHD_ERR_NO_DEVICE = -3
+MHD_ERR_NUMERIC = -4
+MHD_ERR_PARSE = -5
+MHD_ERR_TOO_LARGE = -6
+
+MHD_RIEMANN_LLF, MHD_RIEMANN_HLL, MHD_RIEMANN_HLLD = 1, 2, 4
+MHD_BC_REFLECTING, MHD_BC_OUTFLOW, MHD_BC_PERIODIC = 1, 2, 3
+MHD_FP64, MHD_FP32 = 64, 32
+MHD_FP_FAST, MHD_FP_EXACT = 0, 1
+MHD_LAYOUT_LEFT, MHD_LAYOUT_RIGHT = 0, 1
+MHD_PROBLEM_ORSZAG_TANG = 0
+
+
+class MHDParams(ctypes.Structure):
+    """Mirror of ``mhd_params`` (include/ppkmhd_gb300.h)."""
+
+    _fields_ = [
+        ("dim", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+        ("ghost", ctypes.c_int),
+        ("xmin", ctypes.c_double), ("xmax", ctypes.c_double), ("ymin", ctypes.c_double),
+        ("ymax", ctypes.c_double), ("zmin", ctypes.c_double), ("zmax", ctypes.c_double),
+        ("gamma0", ctypes.c_double), ("cfl", ctypes.c_double), ("slope_type", ctypes.c_double),
+        ("smallr", ctypes.c_double), ("smallc", ctypes.c_double),
+        ("riemann", ctypes.c_int), ("implementation_version", ctypes.c_int),
+        ("boundary", ctypes.c_int * 6),
+        ("tEnd", ctypes.c_double), ("tCurrent", ctypes.c_double), ("nStepmax", ctypes.c_int),
+        ("problem", ctypes.c_int), ("ot_kt", ctypes.c_double),
+        ("precision", ctypes.c_int), ("fp_mode", ctypes.c_int), ("device", ctypes.c_int),
+    ]
+
+    def as_dict(self):
+        d = {f: getattr(self, f) for f, _ in self._fields_}
+        d["boundary"] = list(self.boundary)
+        return d
+
+
+class MHDError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+# Every entry point of include/ppkmhd_gb300.h with its ctypes signature.
+_vp = ctypes.c_void_p
+_ip = ctypes.POINTER(ctypes.c_int)
+_dp = ctypes.POINTER(ctypes.c_double)
+_fp = ctypes.POINTER(ctypes.c_float)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+SIGNATURES = {
+    "mhd_params_default": (ctypes.c_int, [ctypes.POINTER(MHDParams)]),
+    "mhd_params_from_ini": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(MHDParams),
+                                           ctypes.c_char_p, ctypes.c_size_t]),
+    "mhd_create": (ctypes.c_int, [ctypes.POINTER(MHDParams), ctypes.POINTER(_vp)]),
+    "mhd_destroy": (ctypes.c_int, [_vp]),
+    "mhd_init_problem": (ctypes.c_int, [_vp]),
+    "mhd_set_state": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int]),
+    "mhd_get_state": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int]),
+    "mhd_step": (ctypes.c_int, [_vp]),
+    "mhd_run": (ctypes.c_int, [_vp, ctypes.c_int, _ip]),
+    "mhd_step_host": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int]),
+    "mhd_time": (ctypes.c_int, [_vp, _dp, _dp, _ip]),
+    "mhd_diagnostics": (ctypes.c_int, [_vp, _dp, _dp, _dp]),
+    "mhd_run_timed": (ctypes.c_int, [_vp, ctypes.c_int, _fp]),
+    "mhd_profile_step": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_char_p), _fp, ctypes.c_int,
+                                        _ip]),
+    "mhd_cell_counts": (ctypes.c_int, [_vp, _i64p, _i64p]),
+    "mhd_sizes": (ctypes.c_int, [_vp, _ip]),
+    "mhd_launches_per_step": (ctypes.c_int, [_vp, _ip]),
+    "mhd_last_error": (ctypes.c_char_p, [_vp]),
+    "mhd_version": (ctypes.c_char_p, []),
+}
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"{LIB_PATH} is missing: build it with `python -m ppkmhd_gb300.build` "
+                "(this package has no CPU fallback)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def params_from_ini(ini_text: str) -> MHDParams:
+    p = MHDParams()
+    err = ctypes.create_string_buffer(512)
+    rc = lib().mhd_params_from_ini(ini_text.encode(), ctypes.byref(p), err, len(err))
+    if rc != MHD_OK:
+        raise MHDError(rc, err.value.decode())
+    return p
+
+
+def default_params() -> MHDParams:
+    p = MHDParams()
+    lib().mhd_params_default(ctypes.byref(p))
+    return p
+
+
+class MHDSolver:
+    """One MHD problem on the GPU (an ``mhd_ctx``)."""
+
+    def __init__(self, params: MHDParams):
+        self.params = params
+        self.h = _vp()
+        rc = lib().mhd_create(ctypes.byref(params), ctypes.byref(self.h))
+        if rc != MHD_OK:
+            msg = lib().mhd_last_error(self.h).decode() if self.h else "mhd_create failed"
+            if self.h:
+                lib().mhd_destroy(self.h)
+                self.h = _vp()
+            raise MHDError(rc, msg)
+        self.real = np.float64 if params.precision == MHD_FP64 else np.float32
+        s = (ctypes.c_int * 4)()
+        lib().mhd_sizes(self.h, s)
+        self.isize, self.jsize, self.ksize, self.nbvar = list(s)
+
+    @classmethod
+    def from_ini(cls, ini_text: str, precision: int | None = None, fp_mode: int | None = None):
+        p = params_from_ini(ini_text)
+        if precision is not None:
+            p.precision = precision
+        if fp_mode is not None:
+            p.fp_mode = fp_mode
+        return cls(p)
+
+    # ------------------------------------------------------------------
+    def _check(self, rc: int):
+        if rc != MHD_OK:
+            raise MHDError(rc, lib().mhd_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            lib().mhd_destroy(self.h)
+            self.h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def shape_left(self):
+        if self.params.dim == 2:
+            return (8, self.jsize, self.isize)
+        return (8, self.ksize, self.jsize, self.isize)
+
+    @property
+    def shape_right(self):
+        if self.params.dim == 2:
+            return (self.isize, self.jsize, 8)
+        return (self.isize, self.jsize, self.ksize, 8)
+
+    def init_problem(self):
+        self._check(lib().mhd_init_problem(self.h))
+
+    def set_state(self, U: np.ndarray, layout: int = MHD_LAYOUT_LEFT):
+        U = np.ascontiguousarray(U, dtype=self.real)
+        want = self.shape_left if layout == MHD_LAYOUT_LEFT else self.shape_right
+        if U.shape != want:
+            raise ValueError(f"state shape {U.shape} != {want}")
+        self._check(lib().mhd_set_state(self.h, U.ctypes.data, layout, U.itemsize))
+
+    def get_state(self, layout: int = MHD_LAYOUT_LEFT, out: np.ndarray | None = None):
+        shape = self.shape_left if layout == MHD_LAYOUT_LEFT else self.shape_right
+        U = np.empty(shape, dtype=self.real) if out is None else out
+        self._check(lib().mhd_get_state(self.h, U.ctypes.data, layout, U.itemsize))
+        return U
+
+    def step(self):
+        self._check(lib().mhd_step(self.h))
+
+    def run(self, n: int) -> int:
+        done = ctypes.c_int(0)
+        self._check(lib().mhd_run(self.h, int(n), ctypes.byref(done)))
+        return done.value
+
+    def step_host(self, U_in: np.ndarray, U_out: np.ndarray, layout: int = MHD_LAYOUT_LEFT):
+        self._check(lib().mhd_step_host(self.h, U_in.ctypes.data, U_out.ctypes.data, layout,
+                                        U_in.itemsize))
+
+    def step_host_ptr(self, in_ptr: int, out_ptr: int, layout: int = MHD_LAYOUT_LEFT):
+        """Same as step_host on raw host pointers (e.g. pinned buffers)."""
+        itemsize = 8 if self.params.precision == MHD_FP64 else 4
+        self._check(lib().mhd_step_host(self.h, in_ptr, out_ptr, layout, itemsize))
+
+    def time(self):
+        t, dt, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        self._check(lib().mhd_time(self.h, ctypes.byref(t), ctypes.byref(dt), ctypes.byref(it)))
+        return t.value, dt.value, it.value
+
+    def diagnostics(self):
+        sums = (ctypes.c_double * 8)()
+        l1, mx = ctypes.c_double(), ctypes.c_double()
+        self._check(lib().mhd_diagnostics(self.h, sums, ctypes.byref(l1), ctypes.byref(mx)))
+        return np.array(list(sums)), l1.value, mx.value
+
+    def run_timed(self, n: int) -> float:
+        ms = ctypes.c_float()
+        self._check(lib().mhd_run_timed(self.h, int(n), ctypes.byref(ms)))
+        return ms.value
+
+    def profile_step(self):
+        names = (ctypes.c_char_p * 16)()
+        ms = (ctypes.c_float * 16)()
+        cnt = ctypes.c_int()
+        self._check(lib().mhd_profile_step(self.h, names, ms, 16, ctypes.byref(cnt)))
+        return [(names[q].decode(), ms[q]) for q in range(cnt.value)]
+
+    def cell_counts(self):
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        self._check(lib().mhd_cell_counts(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def launches_per_step(self) -> int:
+        n = ctypes.c_int()
+        self._check(lib().mhd_launches_per_step(self.h, ctypes.byref(n)))
+        return n.value
+
+
+def interior(U: np.ndarray, ghost: int = 3) -> np.ndarray:
+    g = ghost
+    if U.ndim == 3:
+        return U[:, g:-g, g:-g]
+    return U[:, g:-g, g:-g, g:-g]

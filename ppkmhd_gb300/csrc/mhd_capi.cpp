@@ -1,0 +1,433 @@
+// C ABI of ppkmhd_gb300 (include/ppkmhd_gb300.h): argument checking, variant
+// dispatch, .ini parsing, and the host-side Orszag-Tang initial condition.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "mhd_core.h"
+#include "ppkmhd_gb300.h"
+#include "../host/ConfigMap.h"
+#include "../host/HydroParams.h"
+
+struct mhd_ctx
+{
+  mhd::SolverCore * core = nullptr;
+  mhd_params        params{};
+  std::string       err;
+};
+
+namespace
+{
+
+int
+fail(mhd_ctx * ctx, int rc, const std::string & msg)
+{
+  if (ctx)
+    ctx->err = msg;
+  return rc;
+}
+
+int
+from_core(mhd_ctx * ctx, int rc)
+{
+  if (rc != MHD_OK)
+    ctx->err = ctx->core->err;
+  return rc;
+}
+
+// Empty string when the parameters can be run.
+std::string
+validate(const mhd_params & p)
+{
+  if (p.dim != 2 && p.dim != 3)
+    return "dim must be 2 or 3";
+  if (p.ghost != 3)
+    return "ghost width must be 3 for the MHD MUSCL scheme";
+  if (p.nx < p.ghost || p.ny < p.ghost || (p.dim == 3 && p.nz < p.ghost))
+    return "each interior extent must be at least the ghost width (3)";
+  const double cells = (double)(p.nx + 6) * (p.ny + 6) * (p.dim == 3 ? p.nz + 6 : 1);
+  if (cells * 8 > 4.0e9)
+    return "grid too large: ghost-inclusive cells x 8 variables must stay below 4e9";
+  if (p.riemann != MHD_RIEMANN_HLLD && p.riemann != MHD_RIEMANN_HLL && p.riemann != MHD_RIEMANN_LLF)
+    return "riemann solver must be hlld, hll or llf for MHD";
+  if (p.implementation_version != 2)
+    return "implementationVersion " + std::to_string(p.implementation_version) +
+           " is not available on this back-end; set [OTHER] implementationVersion=2";
+  for (int f = 0; f < (p.dim == 3 ? 6 : 4); ++f)
+    if (p.boundary[f] != MHD_BC_REFLECTING && p.boundary[f] != MHD_BC_OUTFLOW &&
+        p.boundary[f] != MHD_BC_PERIODIC)
+      return "boundary types must be 1 (reflecting), 2 (outflow) or 3 (periodic)";
+  if (!(p.gamma0 > 1.0) || !(p.cfl > 0.0) || !(p.smallr > 0.0) || !(p.smallc > 0.0))
+    return "gamma0 must be > 1 and cfl, smallr, smallc > 0";
+  if (!(p.xmax > p.xmin) || !(p.ymax > p.ymin) || (p.dim == 3 && !(p.zmax > p.zmin)))
+    return "domain bounds must satisfy max > min";
+  if (p.precision != MHD_FP64 && p.precision != MHD_FP32)
+    return "precision must be 64 or 32";
+  if (p.fp_mode != MHD_FP_FAST && p.fp_mode != MHD_FP_EXACT)
+    return "fp_mode must be MHD_FP_FAST or MHD_FP_EXACT";
+  if (p.precision == MHD_FP32 && p.fp_mode == MHD_FP_EXACT)
+    return "MHD_FP_EXACT is only available with MHD_FP64";
+  if (p.problem != MHD_PROBLEM_ORSZAG_TANG)
+    return "unknown problem id";
+  return "";
+}
+
+} // namespace
+
+namespace mhd
+{
+
+// Orszag-Tang vortex, FP64 on the host, LayoutLeft with ghosts
+// (InitOrszagTangFunctor2D, MHDInitFunctors2D.h:241-389;
+// InitOrszagTangFunctor3D, MHDInitFunctors3D.h:264-415): rho and p
+// uniform, v = (-sin 2 pi y, sin 2 pi x, 0), face-centred
+// B = B0 (-sin 2 pi y_c, sin 4 pi x_c, 0) (times cos(4 pi kt z') in 3D),
+// total energy from the cell-centred field.  Two passes like the
+// reference: everything but energy on all cells, then energy on
+// [0, size-1) in i and j.
+void
+init_orszag_tang_host(const mhd_params & p, double * U)
+{
+  const int     g = p.ghost;
+  const int     isize = p.nx + 2 * g, jsize = p.ny + 2 * g, ksize = p.dim == 3 ? p.nz + 2 * g : 1;
+  const int64_t sj = isize, sk = (int64_t)isize * jsize, sv = sk * ksize;
+  const double  dx = (p.xmax - p.xmin) / p.nx;
+  const double  dy = (p.ymax - p.ymin) / p.ny;
+  const double  dz = p.dim == 3 ? (p.zmax - p.zmin) / p.nz : 1.0;
+  const double  PI = 3.141592653589793238462643383279502884;
+  const double  TWOPI = 2 * PI;
+  const double  gamma0 = p.gamma0;
+  double        B0, p0, p0e;
+  if (p.dim == 2)
+  {
+    B0 = 1.0 / std::sqrt(2 * TWOPI);
+    p0 = gamma0 / (2 * TWOPI);
+    p0e = gamma0 / (2.0 * (4.0 * std::asin(1.0)));
+  }
+  else
+  {
+    B0 = 1.0 / std::sqrt(4 * PI);
+    p0 = gamma0 / (4 * PI);
+    p0e = p0;
+  }
+  const double d0 = gamma0 * p0;
+  const double v0 = 1.0;
+  enum
+  {
+    ID = 0,
+    IP = 1,
+    IU = 2,
+    IV = 3,
+    IW = 4,
+    IA = 5,
+    IB = 6,
+    IC = 7
+  };
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < ksize; ++k)
+  {
+    double zfac = 1.0;
+    if (p.dim == 3)
+    {
+      const double zPos = p.zmin + dz / 2 + (k - g) * dz;
+      zfac = std::cos(2 * TWOPI * p.ot_kt * (zPos - p.zmin) / (p.zmax - p.zmin));
+    }
+    for (int j = 0; j < jsize; ++j)
+      for (int i = 0; i < isize; ++i)
+      {
+        const double  xPos = p.xmin + dx / 2 + (i - g) * dx;
+        const double  yPos = p.ymin + dy / 2 + (j - g) * dy;
+        const int64_t c = i + j * sj + k * sk;
+        U[c + ID * sv] = d0;
+        U[c + IU * sv] = -d0 * v0 * std::sin(yPos * TWOPI);
+        U[c + IV * sv] = d0 * v0 * std::sin(xPos * TWOPI);
+        U[c + IW * sv] = 0.0;
+        if (p.dim == 2)
+        {
+          U[c + IA * sv] = -B0 * std::sin(yPos * TWOPI);
+          U[c + IB * sv] = B0 * std::sin(2.0 * xPos * TWOPI);
+        }
+        else
+        {
+          U[c + IA * sv] = -B0 * zfac * std::sin(yPos * TWOPI);
+          U[c + IB * sv] = B0 * zfac * std::sin(2.0 * xPos * TWOPI);
+        }
+        U[c + IC * sv] = 0.0;
+      }
+  }
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < ksize; ++k)
+    for (int j = 0; j < jsize - 1; ++j)
+      for (int i = 0; i < isize - 1; ++i)
+      {
+        const int64_t c = i + j * sj + k * sk;
+        const double  bxs = U[c + IA * sv] + U[c + 1 + IA * sv];
+        const double  bys = U[c + IB * sv] + U[c + sj + IB * sv];
+        U[c + IP * sv] = p0e / (gamma0 - 1.0) +
+                         0.5 * (U[c + IU * sv] * U[c + IU * sv] / U[c + ID * sv] +
+                                U[c + IV * sv] * U[c + IV * sv] / U[c + ID * sv] +
+                                0.25 * (bxs * bxs) + 0.25 * (bys * bys));
+      }
+}
+
+} // namespace mhd
+
+extern "C"
+{
+
+  const char *
+  mhd_version(void)
+  {
+    return "ppkmhd_gb300 1.0 (sm_103a)";
+  }
+
+  int
+  mhd_params_default(mhd_params * p)
+  {
+    if (!p)
+      return MHD_ERR_INVALID_ARG;
+    std::memset(p, 0, sizeof *p);
+    p->dim = 2;
+    p->nx = p->ny = p->nz = 1;
+    p->ghost = 3;
+    p->xmin = p->ymin = p->zmin = 0.0;
+    p->xmax = p->ymax = p->zmax = 1.0;
+    p->gamma0 = 1.4;
+    p->cfl = 1.0;
+    p->slope_type = 2.0;
+    p->smallr = 1e-8;
+    p->smallc = 1e-8;
+    p->riemann = MHD_RIEMANN_HLLD;
+    p->implementation_version = 2;
+    for (int f = 0; f < 6; ++f)
+      p->boundary[f] = MHD_BC_PERIODIC;
+    p->tEnd = 1.0;
+    p->tCurrent = 0.0;
+    p->nStepmax = 1000;
+    p->problem = MHD_PROBLEM_ORSZAG_TANG;
+    p->ot_kt = 0.0;
+    p->precision = MHD_FP64;
+    p->fp_mode = MHD_FP_FAST;
+    p->device = 0;
+    return MHD_OK;
+  }
+
+  int
+  mhd_params_from_ini(const char * ini_text, mhd_params * p, char * err, size_t errlen)
+  {
+    auto set_err = [&](const std::string & m) {
+      if (err && errlen)
+        std::snprintf(err, errlen, "%s", m.c_str());
+    };
+    if (!ini_text || !p)
+    {
+      set_err("null argument");
+      return MHD_ERR_INVALID_ARG;
+    }
+    ConfigMap                 map(ini_text, (int)std::strlen(ini_text));
+    ppkmhd_gb300::HydroParams hp;
+    hp.setup(map);
+    if (!hp.valid_solver)
+    {
+      set_err("[run] solver_name must be MHD_Muscl_2D or MHD_Muscl_3D");
+      return MHD_ERR_PARSE;
+    }
+    // back-end options (not in the reference): [gb300] precision = 64|32,
+    // [gb300] fp_mode = fast|exact
+    const int         precision = (int)map.getInteger("gb300", "precision", 64);
+    const std::string mode = map.getString("gb300", "fp_mode", "fast");
+    *p = hp.to_mhd_params(map, precision, mode == "exact" ? MHD_FP_EXACT : MHD_FP_FAST);
+    set_err("");
+    return MHD_OK;
+  }
+
+  int
+  mhd_create(const mhd_params * p, mhd_ctx ** out)
+  {
+    if (!p || !out)
+      return MHD_ERR_INVALID_ARG;
+    *out = nullptr;
+    const std::string bad = validate(*p);
+    mhd_ctx *         ctx = new (std::nothrow) mhd_ctx;
+    if (!ctx)
+      return MHD_ERR_CUDA;
+    ctx->params = *p;
+    if (!bad.empty())
+    {
+      ctx->err = bad;
+      *out = ctx; // so that mhd_last_error can report; the context has no core
+      return MHD_ERR_INVALID_ARG;
+    }
+    std::string err;
+    if (p->precision == MHD_FP32)
+      ctx->core = mhd::create_core_f32(*p, err);
+    else if (p->fp_mode == MHD_FP_EXACT)
+      ctx->core = mhd::create_core_f64x(*p, err);
+    else
+      ctx->core = mhd::create_core_f64(*p, err);
+    *out = ctx;
+    if (!ctx->core && err.find("out of range") != std::string::npos)
+    {
+      ctx->err = err;
+      return MHD_ERR_INVALID_ARG;
+    }
+    if (!ctx->core)
+    {
+      ctx->err = err;
+      return err.find("no CUDA device") != std::string::npos ? MHD_ERR_NO_DEVICE : MHD_ERR_CUDA;
+    }
+    return MHD_OK;
+  }
+
+  int
+  mhd_destroy(mhd_ctx * ctx)
+  {
+    if (!ctx)
+      return MHD_ERR_INVALID_ARG;
+    delete ctx->core;
+    delete ctx;
+    return MHD_OK;
+  }
+
+#define NEED_CORE(ctx)                                                   \
+  do                                                                     \
+  {                                                                      \
+    if (!(ctx))                                                          \
+      return MHD_ERR_INVALID_ARG;                                        \
+    if (!(ctx)->core)                                                    \
+      return fail((ctx), MHD_ERR_INVALID_ARG, "context was not created"); \
+    if (int rc_ = (ctx)->core->bind_device())                            \
+      return from_core((ctx), rc_);                                      \
+  } while (0)
+
+  int
+  mhd_init_problem(mhd_ctx * ctx)
+  {
+    NEED_CORE(ctx);
+    return from_core(ctx, ctx->core->init_problem());
+  }
+
+  static int
+  check_array(mhd_ctx * ctx, const void * U, int layout, int real_bytes)
+  {
+    if (!U)
+      return fail(ctx, MHD_ERR_INVALID_ARG, "null state array");
+    if (layout != MHD_LAYOUT_LEFT && layout != MHD_LAYOUT_RIGHT)
+      return fail(ctx, MHD_ERR_INVALID_ARG, "layout must be MHD_LAYOUT_LEFT or MHD_LAYOUT_RIGHT");
+    if (real_bytes != ctx->core->real_bytes())
+      return fail(ctx, MHD_ERR_INVALID_ARG,
+                  "real_bytes " + std::to_string(real_bytes) + " does not match the context precision");
+    return MHD_OK;
+  }
+
+  int
+  mhd_set_state(mhd_ctx * ctx, const void * U, int layout, int real_bytes)
+  {
+    NEED_CORE(ctx);
+    if (int rc = check_array(ctx, U, layout, real_bytes))
+      return rc;
+    return from_core(ctx, ctx->core->set_state(U, layout));
+  }
+
+  int
+  mhd_get_state(mhd_ctx * ctx, void * U, int layout, int real_bytes)
+  {
+    NEED_CORE(ctx);
+    if (int rc = check_array(ctx, U, layout, real_bytes))
+      return rc;
+    return from_core(ctx, ctx->core->get_state(U, layout));
+  }
+
+  int
+  mhd_step(mhd_ctx * ctx)
+  {
+    NEED_CORE(ctx);
+    return from_core(ctx, ctx->core->step());
+  }
+
+  int
+  mhd_run(mhd_ctx * ctx, int nsteps, int * done)
+  {
+    NEED_CORE(ctx);
+    if (nsteps < 0)
+      return fail(ctx, MHD_ERR_INVALID_ARG, "nsteps must be >= 0");
+    return from_core(ctx, ctx->core->run(nsteps, done));
+  }
+
+  int
+  mhd_step_host(mhd_ctx * ctx, const void * U_in, void * U_out, int layout, int real_bytes)
+  {
+    NEED_CORE(ctx);
+    if (int rc = check_array(ctx, U_in, layout, real_bytes))
+      return rc;
+    if (int rc = check_array(ctx, U_out, layout, real_bytes))
+      return rc;
+    return from_core(ctx, ctx->core->step_host(U_in, U_out, layout));
+  }
+
+  int
+  mhd_time(mhd_ctx * ctx, double * t, double * dt, int * iteration)
+  {
+    NEED_CORE(ctx);
+    return from_core(ctx, ctx->core->time(t, dt, iteration));
+  }
+
+  int
+  mhd_diagnostics(mhd_ctx * ctx, double sums[8], double * divb_l1, double * divb_max)
+  {
+    NEED_CORE(ctx);
+    if (!sums)
+      return fail(ctx, MHD_ERR_INVALID_ARG, "null sums");
+    return from_core(ctx, ctx->core->diagnostics(sums, divb_l1, divb_max));
+  }
+
+  int
+  mhd_run_timed(mhd_ctx * ctx, int nsteps, float * ms)
+  {
+    NEED_CORE(ctx);
+    if (!ms || nsteps < 0)
+      return fail(ctx, MHD_ERR_INVALID_ARG, "bad arguments");
+    return from_core(ctx, ctx->core->run_timed(nsteps, ms));
+  }
+
+  int
+  mhd_profile_step(mhd_ctx * ctx, const char ** names, float * ms, int max, int * count)
+  {
+    NEED_CORE(ctx);
+    if (!ms)
+      return fail(ctx, MHD_ERR_INVALID_ARG, "null ms");
+    return from_core(ctx, ctx->core->profile_step(names, ms, max, count));
+  }
+
+  int
+  mhd_cell_counts(mhd_ctx * ctx, int64_t * interior, int64_t * with_ghosts)
+  {
+    NEED_CORE(ctx);
+    return from_core(ctx, ctx->core->cell_counts(interior, with_ghosts));
+  }
+
+  int
+  mhd_sizes(mhd_ctx * ctx, int sizes[4])
+  {
+    NEED_CORE(ctx);
+    return from_core(ctx, ctx->core->sizes(sizes));
+  }
+
+  int
+  mhd_launches_per_step(mhd_ctx * ctx, int * n)
+  {
+    NEED_CORE(ctx);
+    if (n)
+      *n = ctx->core->launches_per_step();
+    return MHD_OK;
+  }
+
+  const char *
+  mhd_last_error(mhd_ctx * ctx)
+  {
+    return ctx ? ctx->err.c_str() : "null context";
+  }
+
+} // extern "C"

@@ -1,0 +1,46 @@
+// Host-side interface between the C ABI (mhd_capi.cpp) and the solver
+// cores, one per arithmetic variant (FP64 exact, FP64 fast, FP32), each
+// compiled from mhd_variant.cu into its own inline namespace.
+#pragma once
+
+#include <cstdint>
+#include <string>
+
+#include "ppkmhd_gb300.h"
+
+namespace mhd
+{
+
+class SolverCore
+{
+public:
+  virtual ~SolverCore() {}
+  virtual int init_problem() = 0;
+  virtual int set_state(const void * U, int layout) = 0;
+  virtual int get_state(void * U, int layout) = 0;
+  virtual int step() = 0;
+  virtual int run(int nsteps, int * done) = 0;
+  virtual int step_host(const void * Uin, void * Uout, int layout) = 0;
+  virtual int time(double * t, double * dt, int * it) = 0;
+  virtual int diagnostics(double sums[8], double * divb_l1, double * divb_max) = 0;
+  virtual int run_timed(int nsteps, float * ms) = 0;
+  virtual int profile_step(const char ** names, float * ms, int max, int * count) = 0;
+  virtual int cell_counts(int64_t * interior, int64_t * with_ghosts) = 0;
+  virtual int sizes(int s[4]) = 0;
+  virtual int launches_per_step() = 0;
+  virtual int real_bytes() const = 0;
+  //! make the context's device current for the calling thread
+  virtual int bind_device() = 0;
+  std::string err;
+};
+
+// Factories (return nullptr and fill err on failure).
+SolverCore * create_core_f64x(const mhd_params & p, std::string & err);
+SolverCore * create_core_f64(const mhd_params & p, std::string & err);
+SolverCore * create_core_f32(const mhd_params & p, std::string & err);
+
+// Orszag-Tang initial condition in FP64 on the host, LayoutLeft, ghosts
+// included (MHDInitFunctors2D.h:241-389, MHDInitFunctors3D.h:264-415).
+void init_orszag_tang_host(const mhd_params & p, double * U);
+
+} // namespace mhd

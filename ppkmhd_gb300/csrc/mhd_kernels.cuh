@@ -1,0 +1,784 @@
+// Kernels of one MUSCL-Hancock + HLLD + CT iteration (implementation
+// version 2 of ppkMHD), templated on the real type R and the dimension DIM.
+//
+// One iteration is 8 launches on one stream, all in gather form (every face
+// flux and edge EMF is computed once by one thread and every cell is updated
+// by the thread that owns it; no atomics, bitwise deterministic):
+//
+//   k_boundaries  ghost fill of U_in (periodic / reflecting / outflow)
+//   k_prim_dt     primitives Q over [0,size-1)^DIM + CFL max-reduction (FP64)
+//   k_finalize_dt dt = cfl / max, clipped to tEnd; dt/dx, dt/dy, dt/dz
+//   k_trace       limited slopes S_d, half-step primitives Q2, edge fields E
+//   k_flux        HLLD face fluxes F_d (face-normal B predicted with curl E)
+//   k_emf         reconstructed edge states -> 2D HLLD EMFs
+//   k_update      U_out = U_in - div F (hydro), U_out = U_in + curl EMF (face B)
+//   k_advance     iteration += 1, t += dt
+//
+// Device layout: SoA var-planes, i fastest, ghost cells included:
+//   U[i + isize*(j + jsize*(k + ksize*var))]   (Kokkos LayoutLeft)
+// The time-step state (t, dt, iteration, the reduction word) lives in device
+// memory so that whole runs replay from a CUDA graph without host syncs.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mhd_physics.cuh"
+
+#ifndef MHD_VARIANT_TAG
+#  define MHD_VARIANT_TAG v_default
+#endif
+
+namespace mhd
+{
+inline namespace MHD_VARIANT_TAG
+{
+
+// Device-resident time-step bookkeeping (SolverBase m_t, m_dt, m_iteration).
+struct DevState
+{
+  double             t, dt, tEnd;
+  double             dtdx, dtdy, dtdz;
+  unsigned long long invdt_bits; // max of the CFL rate, as the bits of a non-negative double
+  int                it, nStepmax;
+  int                status; // bit 0: non-finite or non-positive state seen
+  int                pad;
+};
+
+enum : int
+{
+  STATUS_NUMERIC = 1
+};
+
+template <class R>
+struct Grid
+{
+  int     dim, nx, ny, nz, g;
+  int     isize, jsize, ksize;
+  int64_t sj, sk, sv; // strides of j, k and var (i stride is 1)
+  int     bc[6];
+  int     riemann;
+  R       gamma0, smallr, smallp, smallc, slope_type;
+  double  cfl, dx, dy, dz;
+};
+
+template <class R>
+struct Buffers
+{
+  R *       Uin;
+  R *       Uout;
+  R *       Q;   // primitives, 8 planes
+  R *       Q2;  // half-step primitives, 8 planes
+  R *       S;   // limited slopes, DIM blocks of 8 planes
+  R *       E;   // edge electric field (1 plane in 2D, Ex/Ey/Ez in 3D)
+  R *       F;   // face fluxes, DIM blocks of NF planes
+  R *       Em;  // edge EMFs (1 plane in 2D, 3 in 3D)
+  DevState *st;
+};
+
+template <int DIM>
+struct FluxComps
+{
+  // hydro components updated by the face fluxes: 2D also updates Bz
+  // (MHDRunFunctors2D.h:1231-1273), 3D none of B (MHDRunFunctors3D.h:1255-1313)
+  static constexpr int NF = DIM == 2 ? 6 : 5;
+  __device__ static constexpr int var(int c) { return c < 5 ? c : IC; }
+};
+
+__device__ __forceinline__ bool
+step_finished(const DevState * st)
+{
+  // SolverBase::finished (SolverBase.cpp:195-201)
+  return st->t >= (st->tEnd - 1e-14) || st->it >= st->nStepmax;
+}
+
+// A box of cells [lo, lo+n) flattened with i fastest.
+struct Box
+{
+  int i0, j0, k0, ni, nj, nk;
+  __host__ __device__ int64_t
+  count() const
+  {
+    return (int64_t)ni * nj * nk;
+  }
+};
+
+__device__ __forceinline__ bool
+box_cell(const Box & b, int64_t idx, int & i, int & j, int & k)
+{
+  if (idx >= b.count())
+    return false;
+  const int64_t r = idx / b.ni;
+  i = b.i0 + (int)(idx - r * b.ni);
+  const int64_t kk = r / b.nj;
+  j = b.j0 + (int)(r - kk * b.nj);
+  k = b.k0 + (int)kk;
+  return true;
+}
+
+template <class R>
+__device__ __forceinline__ int64_t
+cell_at(const Grid<R> & G, int i, int j, int k)
+{
+  return (int64_t)i + (int64_t)j * G.sj + (int64_t)k * G.sk;
+}
+
+// ---------------------------------------------------------------- boundaries
+
+// Source index along one axis for ghost index c (BoundariesFunctors.h:535-1057).
+__device__ __forceinline__ int
+bc_source(int c, int n, int g, int type, bool hi, bool & flip)
+{
+  flip = false;
+  if (!hi)
+  {
+    if (type == 1)
+    {
+      flip = true;
+      return 2 * g - 1 - c;
+    }
+    if (type == 2)
+      return g;
+    return n + c;
+  }
+  if (type == 1)
+  {
+    flip = true;
+    return 2 * n + 2 * g - 1 - c;
+  }
+  if (type == 2)
+    return n + g - 1;
+  return c - n;
+}
+
+// Ghost fill.  The reference fills the X faces, then Y, then Z, each over
+// the full extent of the other axes; a ghost cell therefore ends up with the
+// interior value at the composition of the per-axis source maps, multiplied
+// by the per-axis reflection signs (normal velocity and normal field).
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+k_boundaries(const Grid<R> G, R * __restrict__ U, DevState * st, int force)
+{
+  if (!force && step_finished(st))
+    return;
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    st->invdt_bits = 0ull; // reset the CFL reduction of this iteration
+  const Box b{ 0, 0, 0, G.isize, G.jsize, DIM == 3 ? G.ksize : 1 };
+  int       i, j, k;
+  if (!box_cell(b, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
+    return;
+  const int g = G.g;
+  const bool gx = i < g || i >= G.nx + g;
+  const bool gy = j < g || j >= G.ny + g;
+  const bool gz = DIM == 3 && (k < g || k >= G.nz + g);
+  if (!gx && !gy && !gz)
+    return;
+  bool fx = false, fy = false, fz = false;
+  int  i0 = i, j0 = j, k0 = k;
+  if (gx)
+    i0 = bc_source(i, G.nx, g, G.bc[i < g ? 0 : 1], i >= g, fx);
+  if (gy)
+    j0 = bc_source(j, G.ny, g, G.bc[j < g ? 2 : 3], j >= g, fy);
+  if (gz)
+    k0 = bc_source(k, G.nz, g, G.bc[k < g ? 4 : 5], k >= g, fz);
+  const int64_t dst = cell_at(G, i, j, k), src = cell_at(G, i0, j0, k0);
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+  {
+    R x = U[src + v * G.sv];
+    if (fx && (v == IU || v == IA))
+      x = x * R(-1);
+    if (fy && (v == IV || v == IB))
+      x = x * R(-1);
+    if (fz && (v == IW || v == IC))
+      x = x * R(-1);
+    U[dst + v * G.sv] = x;
+  }
+}
+
+// ---------------------------------------------------------------- primitives + CFL
+
+__device__ __forceinline__ double
+warp_max(double v)
+{
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// ConvertToPrimitivesFunctor (MHDRunFunctors2D.h:85-159, 3D:88-163) with
+// constoprim_mhd (MHDBaseFunctor2D.h:194-242), fused with the CFL reduction
+// of ComputeDtFunctor (MHDRunFunctors2D.h:16-80, 3D:16-83): for interior
+// cells, max over sum_d (c_fast,d + |v_d|)/dx_d.  The max is reduced in FP64
+// (warp shuffles, then one atomicMax per block on the bit pattern, which
+// orders like the value for non-negative doubles) and is order-independent,
+// so dt is bitwise the reference's.
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+k_prim_dt(const Grid<R> G, const R * __restrict__ U, R * __restrict__ Q, DevState * st, int force)
+{
+  if (!force && step_finished(st))
+    return;
+  const Box b{ 0, 0, 0, G.isize - 1, G.jsize - 1, DIM == 3 ? G.ksize - 1 : 1 };
+  int       i, j, k;
+  double    rate = 0.0;
+  bool      bad = false;
+  if (box_cell(b, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
+  {
+    const int64_t c = cell_at(G, i, j, k);
+    const int64_t sv = G.sv;
+    const R       nbx = U[c + 1 + IA * sv];
+    const R       nby = U[c + G.sj + IB * sv];
+    const R       nbz = DIM == 3 ? U[c + G.sk + IC * sv] : R(0);
+    const R       d = fmax(U[c + ID * sv], G.smallr);
+    const R       vu = U[c + IU * sv] / d;
+    const R       vv = U[c + IV * sv] / d;
+    const R       vw = U[c + IW * sv] / d;
+    const R       a = R(0.5) * (U[c + IA * sv] + nbx);
+    const R       bb = R(0.5) * (U[c + IB * sv] + nby);
+    const R       cc = R(0.5) * (U[c + IC * sv] + nbz);
+    const R       eken = R(0.5) * (vu * vu + vv * vv + vw * vw);
+    const R       emag = R(0.5) * (a * a + bb * bb + cc * cc);
+    const R       eint = (U[c + IP * sv] - emag) / d - eken;
+    const R       p = fmax((G.gamma0 - R(1)) * d * eint, d * G.smallp);
+    Q[c + ID * sv] = d;
+    Q[c + IP * sv] = p;
+    Q[c + IU * sv] = vu;
+    Q[c + IV * sv] = vv;
+    Q[c + IW * sv] = vw;
+    Q[c + IA * sv] = a;
+    Q[c + IB * sv] = bb;
+    Q[c + IC * sv] = cc;
+    const int g = G.g;
+    const bool interior = i >= g && i < G.isize - g && j >= g && j < G.jsize - g &&
+                          (DIM == 2 || (k >= g && k < G.ksize - g));
+    if (interior)
+    {
+      // find_speed_info<NDIM> (mhd_utils.h:319-366)
+      const R b2 = a * a + bb * bb + cc * cc;
+      const R c2 = G.gamma0 * p / d;
+      const R d2 = R(0.5) * (b2 / d + c2);
+      const R sx = sqrt(d2 + sqrt(d2 * d2 - c2 * a * a / d)) + fabs(vu);
+      const R sy = sqrt(d2 + sqrt(d2 * d2 - c2 * bb * bb / d)) + fabs(vv);
+      R       val;
+      if constexpr (DIM == 3)
+      {
+        const R sz = sqrt(d2 + sqrt(d2 * d2 - c2 * cc * cc / d)) + fabs(vw);
+        val = sx / R(G.dx) + sy / R(G.dy) + sz / R(G.dz);
+      }
+      else
+        val = sx / R(G.dx) + sy / R(G.dy);
+      // fmax in the reference ignores NaN operands; a NaN rate is dropped
+      rate = (val >= R(0)) ? (double)val : 0.0;
+      const R Ein = U[c + IP * sv];
+      bad = !(U[c + ID * sv] > R(0)) || !isfinite(Ein) || !isfinite(val);
+    }
+  }
+  // block max in FP64
+  __shared__ double red[32];
+  rate = warp_max(rate);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0)
+    red[wid] = rate;
+  if (__syncthreads_or(bad) && threadIdx.x == 0)
+    atomicOr(&st->status, STATUS_NUMERIC);
+  if (wid == 0)
+  {
+    rate = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
+    rate = warp_max(rate);
+    if (lane == 0 && rate > 0.0)
+      atomicMax(&st->invdt_bits, (unsigned long long)__double_as_longlong(rate));
+  }
+}
+
+// compute_dt_local (SolverMHDMuscl.h:722-741) and the clip of
+// SolverBase::compute_dt (SolverBase.cpp:148-179); dtdx = m_dt / dx
+// (SolverMHDMuscl.cpp:390-391).
+template <class R>
+__global__ void
+k_finalize_dt(const Grid<R> G, DevState * st, int force)
+{
+  if (!force && step_finished(st))
+    return;
+  const double invDt = __longlong_as_double((long long)st->invdt_bits);
+  double       dt;
+  if constexpr (sizeof(R) == 8)
+    dt = G.cfl / invDt;
+  else
+    dt = G.cfl / invDt; // FP64 dt for the FP32 storage path
+  if (st->t + dt > st->tEnd)
+    dt = st->tEnd - st->t;
+  st->dt = dt;
+  st->dtdx = dt / G.dx;
+  st->dtdy = dt / G.dy;
+  st->dtdz = dt / G.dz;
+  if (!(invDt > 0.0) || !isfinite(dt))
+    st->status |= STATUS_NUMERIC;
+}
+
+template <class R>
+__global__ void
+k_advance(DevState * st)
+{
+  if (step_finished(st))
+    return;
+  st->it += 1;
+  st->t += st->dt;
+}
+
+// ---------------------------------------------------------------- trace
+
+// Slopes, half step and edge field over the box [g-1, size-g+1]^DIM:
+//  * ComputeSlopesFunctor (MHDRunFunctors2D.h:164-248, 3D:168-273): MC-type
+//    limited slopes per direction; the face-normal field slope is the
+//    unlimited face difference;
+//  * ComputeUpdatedPrimVarFunctor (MHDRunFunctors2D.h:920-1051,
+//    3D:865-1022): Q2 = Q + S/2 with the primitive MHD source terms;
+//  * ComputeElecFieldFunctor (MHDRunFunctors2D.h:253-314, 3D:278-362):
+//    E = v x B at the lower edges of the cell.
+// Slopes and Q2 are only consumed on [g-1, size-g]^DIM, the edge field on
+// [g-1, size-g+1]^DIM.
+template <class R, int DIM>
+__global__ void __launch_bounds__(128)
+k_trace(const Grid<R> G, Buffers<R> B)
+{
+  if (step_finished(B.st))
+    return;
+  const int g = G.g;
+  const Box b{ g - 1, g - 1, DIM == 3 ? g - 1 : 0, G.nx + 3, G.ny + 3, DIM == 3 ? G.nz + 3 : 1 };
+  int       i, j, k;
+  if (!box_cell(b, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
+    return;
+  const int64_t sv = G.sv, sj = G.sj, sk = G.sk;
+  const int64_t c = cell_at(G, i, j, k);
+  const R * __restrict__ Q = B.Q;
+  const R * __restrict__ U = B.Uin;
+  const double dtdx_d = B.st->dtdx, dtdy_d = B.st->dtdy, dtdz_d = B.st->dtdz;
+  const R      dtdx = R(dtdx_d), dtdy = R(dtdy_d), dtdz = R(dtdz_d);
+  (void)dtdz;
+
+  // edge electric field
+  if constexpr (DIM == 2)
+  {
+    const R u = R(0.25) * (Q[c - 1 - sj + IU * sv] + Q[c - 1 + IU * sv] + Q[c - sj + IU * sv] +
+                           Q[c + IU * sv]);
+    const R v = R(0.25) * (Q[c - 1 - sj + IV * sv] + Q[c - 1 + IV * sv] + Q[c - sj + IV * sv] +
+                           Q[c + IV * sv]);
+    const R A = R(0.5) * (U[c - sj + IA * sv] + U[c + IA * sv]);
+    const R Bf = R(0.5) * (U[c - 1 + IB * sv] + U[c + IB * sv]);
+    B.E[c] = u * Bf - v * A;
+  }
+  else
+  {
+    R u, v, w, A, Bf, C;
+    v = R(0.25) * (Q[c - sj - sk + IV * sv] + Q[c - sj + IV * sv] + Q[c - sk + IV * sv] +
+                   Q[c + IV * sv]);
+    w = R(0.25) * (Q[c - sj - sk + IW * sv] + Q[c - sj + IW * sv] + Q[c - sk + IW * sv] +
+                   Q[c + IW * sv]);
+    Bf = R(0.5) * (U[c - sk + IB * sv] + U[c + IB * sv]);
+    C = R(0.5) * (U[c - sj + IC * sv] + U[c + IC * sv]);
+    B.E[c] = v * C - w * Bf;
+    u = R(0.25) * (Q[c - 1 - sk + IU * sv] + Q[c - 1 + IU * sv] + Q[c - sk + IU * sv] +
+                   Q[c + IU * sv]);
+    w = R(0.25) * (Q[c - 1 - sk + IW * sv] + Q[c - 1 + IW * sv] + Q[c - sk + IW * sv] +
+                   Q[c + IW * sv]);
+    A = R(0.5) * (U[c - sk + IA * sv] + U[c + IA * sv]);
+    C = R(0.5) * (U[c - 1 + IC * sv] + U[c + IC * sv]);
+    B.E[c + sv] = w * A - u * C;
+    u = R(0.25) * (Q[c - 1 - sj + IU * sv] + Q[c - 1 + IU * sv] + Q[c - sj + IU * sv] +
+                   Q[c + IU * sv]);
+    v = R(0.25) * (Q[c - 1 - sj + IV * sv] + Q[c - 1 + IV * sv] + Q[c - sj + IV * sv] +
+                   Q[c + IV * sv]);
+    A = R(0.5) * (U[c - sj + IA * sv] + U[c + IA * sv]);
+    Bf = R(0.5) * (U[c - 1 + IB * sv] + U[c + IB * sv]);
+    B.E[c + 2 * sv] = u * Bf - v * A;
+  }
+
+  if (i > G.isize - g || j > G.jsize - g || (DIM == 3 && k > G.ksize - g))
+    return;
+
+  // limited slopes in each direction
+  R         q[NV], s[DIM][NV];
+  const int64_t off[3] = { 1, sj, sk };
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+    q[v] = Q[c + v * sv];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d)
+  {
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      s[d][v] = limited_slope(q[v], Q[c + off[d] + v * sv], Q[c - off[d] + v * sv], G.slope_type);
+    s[d][IA + d] = U[c + off[d] + (IA + d) * sv] - U[c + (IA + d) * sv];
+  }
+  R * S = B.S;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d)
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      S[c + (d * NV + v) * sv] = s[d][v];
+
+  // Hancock half step
+  const R r = q[ID], p = q[IP], u = q[IU], v = q[IV], w = q[IW], A = q[IA], Bc = q[IB], C = q[IC];
+  const R gamma = G.gamma0;
+  const R drx = s[0][ID], dpx = s[0][IP], dux = s[0][IU], dvx = s[0][IV], dwx = s[0][IW],
+          dBx = s[0][IB], dCx = s[0][IC];
+  const R dry = s[1][ID], dpy = s[1][IP], duy = s[1][IU], dvy = s[1][IV], dwy = s[1][IW],
+          dAy = s[1][IA], dCy = s[1][IC];
+  const R dAx = s[0][IA], dBy = s[1][IB];
+  R       sr0, su0, sv0, sw0, sp0, sA0, sB0, sC0;
+  if constexpr (DIM == 2)
+  {
+    sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy;
+    su0 = (-u * dux - dpx / r - Bc * dBx / r - C * dCx / r) * dtdx + (-v * duy + Bc * dAy / r) * dtdy;
+    sv0 = (-u * dvx + A * dBx / r) * dtdx + (-v * dvy - dpy / r - A * dAy / r - C * dCy / r) * dtdy;
+    sw0 = (-u * dwx + A * dCx / r) * dtdx + (-v * dwy + Bc * dCy / r) * dtdy;
+    sp0 = (-u * dpx - dux * gamma * p) * dtdx + (-v * dpy - dvy * gamma * p) * dtdy;
+    sA0 = (u * dBy + Bc * duy - v * dAy - A * dvy) * dtdy;
+    sB0 = (-u * dBx - Bc * dux + v * dAx + A * dvx) * dtdx;
+    sC0 = (w * dAx + A * dwx - u * dCx - C * dux) * dtdx +
+          (-v * dCy - C * dvy + w * dBy + Bc * dwy) * dtdy;
+  }
+  else
+  {
+    const R drz = s[DIM - 1][ID], dpz = s[DIM - 1][IP], duz = s[DIM - 1][IU],
+            dvz = s[DIM - 1][IV], dwz = s[DIM - 1][IW], dAz = s[DIM - 1][IA],
+            dBz = s[DIM - 1][IB], dCz = s[DIM - 1][IC];
+    sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy + (-w * drz - dwz * r) * dtdz;
+    su0 = (-u * dux - (dpx + Bc * dBx + C * dCx) / r) * dtdx + (-v * duy + Bc * dAy / r) * dtdy +
+          (-w * duz + C * dAz / r) * dtdz;
+    sv0 = (-u * dvx + A * dBx / r) * dtdx + (-v * dvy - (dpy + A * dAy + C * dCy) / r) * dtdy +
+          (-w * dvz + C * dBz / r) * dtdz;
+    sw0 = (-u * dwx + A * dCx / r) * dtdx + (-v * dwy + Bc * dCy / r) * dtdy +
+          (-w * dwz - (dpz + A * dAz + Bc * dBz) / r) * dtdz;
+    sp0 = (-u * dpx - dux * gamma * p) * dtdx + (-v * dpy - dvy * gamma * p) * dtdy +
+          (-w * dpz - dwz * gamma * p) * dtdz;
+    sA0 = (u * dBy + Bc * duy - v * dAy - A * dvy) * dtdy + (u * dCz + C * duz - w * dAz - A * dwz) * dtdz;
+    sB0 = (v * dAx + A * dvx - u * dBx - Bc * dux) * dtdx + (v * dCz + C * dvz - w * dBz - Bc * dwz) * dtdz;
+    sC0 = (w * dAx + A * dwx - u * dCx - C * dux) * dtdx + (w * dBy + Bc * dwy - v * dCy - C * dvy) * dtdy;
+  }
+  R * Q2 = B.Q2;
+  Q2[c + ID * sv] = r + R(0.5) * sr0;
+  Q2[c + IU * sv] = u + R(0.5) * su0;
+  Q2[c + IV * sv] = v + R(0.5) * sv0;
+  Q2[c + IW * sv] = w + R(0.5) * sw0;
+  Q2[c + IP * sv] = p + R(0.5) * sp0;
+  Q2[c + IA * sv] = A + R(0.5) * sA0;
+  Q2[c + IB * sv] = Bc + R(0.5) * sB0;
+  Q2[c + IC * sv] = C + R(0.5) * sC0;
+}
+
+// Half-step predictor of the face-centred field on face c normal to d
+// (ComputeSourceFaceMagFunctor2D, MHDRunFunctors2D.h:319-370;
+// ComputeSourceFaceMagFunctor3D, MHDRunFunctors3D.h:367-436), evaluated
+// on the fly from the stored edge field.
+template <class R, int DIM>
+__device__ __forceinline__ R
+face_source(const Grid<R> & G, const R * __restrict__ E, int64_t c, int d, R dtdx, R dtdy, R dtdz)
+{
+  const int64_t sj = G.sj, sk = G.sk, n1 = G.sv;
+  if constexpr (DIM == 2)
+  {
+    if (d == 0)
+      return (E[c + sj] - E[c]) * R(0.5) * dtdy;
+    return -(E[c + 1] - E[c]) * R(0.5) * dtdx;
+  }
+  else
+  {
+    const R *Ex = E, *Ey = E + n1, *Ez = E + 2 * n1;
+    if (d == 0)
+      return (Ez[c + sj] - Ez[c]) * R(0.5) * dtdy - (Ey[c + sk] - Ey[c]) * R(0.5) * dtdz;
+    if (d == 1)
+      return -(Ez[c + 1] - Ez[c]) * R(0.5) * dtdx + (Ex[c + sk] - Ex[c]) * R(0.5) * dtdz;
+    return (Ey[c + 1] - Ey[c]) * R(0.5) * dtdx - (Ex[c + sj] - Ex[c]) * R(0.5) * dtdy;
+  }
+}
+
+// ---------------------------------------------------------------- face fluxes
+
+// Reconstruction + Riemann solve of ComputeFluxAndUpdateAlongDirFunctor<dir>
+// (MHDRunFunctors2D.h:1110-1229, 3D:1097-1253) for faces [g, size-g]^DIM;
+// blockIdx.y selects the direction.  The reference adds the flux into cell i
+// and subtracts it from cell i-1 with atomics; here it is stored once and
+// gathered by k_update.
+template <class R, int DIM, int d>
+__device__ __forceinline__ void
+flux_face(const Grid<R> & G, const Buffers<R> & B, int i, int j, int k)
+{
+  const int64_t sv = G.sv;
+  const int64_t off = d == 0 ? 1 : (d == 1 ? G.sj : G.sk);
+  const int64_t c = cell_at(G, i, j, k), cn = c - off;
+  const R * __restrict__ Q2 = B.Q2;
+  const R * __restrict__ S = B.S + (int64_t)d * NV * sv;
+  const R dtdx = R(B.st->dtdx), dtdy = R(B.st->dtdy), dtdz = R(B.st->dtdz);
+  const R smallR = G.smallr, smallp = G.smallp;
+  constexpr int nrm = IA + d;
+
+  State<R> qR, qL, fl;
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+  {
+    if (v == nrm)
+      continue;
+    qR[v] = Q2[c + v * sv] - R(0.5) * S[c + v * sv];
+    qL[v] = Q2[cn + v * sv] + R(0.5) * S[cn + v * sv];
+  }
+  qR[ID] = fmax(smallR, qR[ID]);
+  qR[IP] = fmax(smallp * qR[ID], qR[IP]);
+  qL[ID] = fmax(smallR, qL[ID]);
+  qL[IP] = fmax(smallp * qL[ID], qL[IP]);
+  qR[nrm] = B.Uin[c + nrm * sv] + face_source<R, DIM>(G, B.E, c, d, dtdx, dtdy, dtdz);
+  qL[nrm] = qR[nrm];
+  // rotate into the face-normal frame: normal velocity -> IU, normal field -> IA
+  if constexpr (d > 0)
+  {
+    swap_vals(qL[IU], qL[IU + d]);
+    swap_vals(qL[IA], qL[IA + d]);
+    swap_vals(qR[IU], qR[IU + d]);
+    swap_vals(qR[IA], qR[IA + d]);
+  }
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+    fl[v] = R(0);
+  riemann(G.riemann, qL, qR, fl, G.gamma0);
+  if constexpr (d > 0)
+  {
+    swap_vals(fl[IU], fl[IU + d]);
+    swap_vals(fl[IA], fl[IA + d]);
+  }
+  constexpr int NF = FluxComps<DIM>::NF;
+  R * F = B.F + (int64_t)d * NF * sv;
+#pragma unroll
+  for (int q = 0; q < NF; ++q)
+    F[c + q * sv] = fl[FluxComps<DIM>::var(q)];
+}
+
+template <class R, int DIM>
+__global__ void __launch_bounds__(128)
+k_flux(const Grid<R> G, Buffers<R> B)
+{
+  if (step_finished(B.st))
+    return;
+  const int g = G.g;
+  const Box b{ g, g, DIM == 3 ? g : 0, G.nx + 1, G.ny + 1, DIM == 3 ? G.nz + 1 : 1 };
+  int       i, j, k;
+  if (!box_cell(b, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
+    return;
+  if (blockIdx.y == 0)
+    flux_face<R, DIM, 0>(G, B, i, j, k);
+  else if (blockIdx.y == 1)
+    flux_face<R, DIM, 1>(G, B, i, j, k);
+  else if constexpr (DIM == 3)
+    flux_face<R, DIM, 2>(G, B, i, j, k);
+}
+
+// ---------------------------------------------------------------- edge EMFs
+
+// compute_limited_slope<dir> of a face-centred field component
+// (MHDBaseFunctor2D.h:129-155, MHDBaseFunctor3D.h:128-158).  In 3D the
+// reference samples the minus neighbour along z at k + 1, so the z slope is
+// identically zero; that is kept.
+template <class R, int DIM>
+__device__ __forceinline__ R
+face_field_slope(const Grid<R> & G, const R * __restrict__ U, int64_t c, int comp, int dir)
+{
+  const int64_t cv = c + comp * G.sv;
+  if (dir == 0)
+    return limited_slope(U[cv], U[cv + 1], U[cv - 1], G.slope_type);
+  if (dir == 1)
+    return limited_slope(U[cv], U[cv + G.sj], U[cv - G.sj], G.slope_type);
+  return limited_slope(U[cv], U[cv + G.sk], U[cv + G.sk], G.slope_type);
+}
+
+// ReconstructEdgeComputeEmfAndUpdateFunctor (MHDRunFunctors2D.h:1291-1534,
+// 3D:1331-1778) for edges [g, size-g]^DIM; blockIdx.y is the edge direction
+// (0 = x, 1 = y, 2 = z; 2D has z edges only).  The corner states RT, RB,
+// LT, LB come from the cells (c - o0 - o1), (c - o0), (c - o1), c where
+// o0, o1 are the strides of the two transverse directions d0 < d1
+// (reconstruct_state_at_edge, MHDRunFunctors3D.h:1406-1529).
+template <class R, int DIM, int edir>
+__device__ __forceinline__ void
+emf_edge(const Grid<R> & G, const Buffers<R> & B, int i, int j, int k)
+{
+  constexpr int d0 = edir == 0 ? 1 : 0, d1 = edir == 2 ? 1 : 2;
+  const int64_t sv = G.sv;
+  const int64_t stride[3] = { 1, G.sj, G.sk };
+  const int64_t o0 = stride[d0], o1 = stride[d1];
+  const int64_t c = cell_at(G, i, j, k);
+  const R * __restrict__ Q2 = B.Q2;
+  const R * __restrict__ U = B.Uin;
+  const R * __restrict__ S0 = B.S + (int64_t)d0 * NV * sv;
+  const R * __restrict__ S1 = B.S + (int64_t)(DIM == 2 ? 1 : d1) * NV * sv;
+  const R dtdx = R(B.st->dtdx), dtdy = R(B.st->dtdy), dtdz = R(B.st->dtdz);
+  const R smallR = G.smallr, smallp = G.smallp;
+
+  State<R> qe[4]; // RT, RB, LT, LB
+#pragma unroll
+  for (int e = 0; e < 4; ++e)
+  {
+    const bool    r0 = (e == 0 || e == 1), r1 = (e == 0 || e == 2);
+    const R       sdq0 = r0 ? R(1) : R(-1), sdq1 = r1 ? R(1) : R(-1);
+    const R       sb0 = (e == 0 || e == 2) ? R(1) : R(-1);
+    const R       sb1 = (e == 0 || e == 1) ? R(1) : R(-1);
+    const int64_t cc = c - (r0 ? o0 : 0) - (r1 ? o1 : 0);
+    const int64_t c0 = cc + (r0 ? o0 : 0); // face carrying B_{d0}
+    const int64_t c1 = cc + (r1 ? o1 : 0); // face carrying B_{d1}
+    constexpr int dd1 = DIM == 2 ? 1 : d1;
+    const R B0 = U[c0 + (IA + d0) * sv] + face_source<R, DIM>(G, B.E, c0, d0, dtdx, dtdy, dtdz);
+    const R dB0d1 = face_field_slope<R, DIM>(G, U, c0, IA + d0, dd1);
+    const R B1 = U[c1 + (IA + dd1) * sv] + face_source<R, DIM>(G, B.E, c1, dd1, dtdx, dtdy, dtdz);
+    const R dB1d0 = face_field_slope<R, DIM>(G, U, c1, IA + dd1, d0);
+    State<R> & q = qe[e];
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      q[v] = Q2[cc + v * sv];
+    q[ID] += R(0.5) * (sdq0 * S0[cc + ID * sv] + sdq1 * S1[cc + ID * sv]);
+    q[IU] += R(0.5) * (sdq0 * S0[cc + IU * sv] + sdq1 * S1[cc + IU * sv]);
+    q[IV] += R(0.5) * (sdq0 * S0[cc + IV * sv] + sdq1 * S1[cc + IV * sv]);
+    q[IW] += R(0.5) * (sdq0 * S0[cc + IW * sv] + sdq1 * S1[cc + IW * sv]);
+    q[IP] += R(0.5) * (sdq0 * S0[cc + IP * sv] + sdq1 * S1[cc + IP * sv]);
+    if constexpr (DIM == 2)
+    {
+      // MHDRunFunctors2D.h:1424-1432
+      q[IA] = B0 + R(0.5) * (sb0 * dB0d1);
+      q[IB] = B1 + R(0.5) * (sb1 * dB1d0);
+      q[IC] += R(0.5) * (sdq0 * S0[cc + IC * sv] + sdq1 * S1[cc + IC * sv]);
+    }
+    else
+    {
+      // statement order of MHDRunFunctors3D.h:1490-1524, including the double
+      // transverse increment of IB on y and x edges
+      if constexpr (d0 == 0)
+        q[IA] = B0 + R(0.5) * (sb0 * dB0d1);
+      else
+        q[IA] += R(0.5) * (sdq0 * S0[cc + IA * sv] + sdq1 * S1[cc + IA * sv]);
+      if constexpr (d0 == 1)
+        q[IB] = B0 + R(0.5) * (sb0 * dB0d1);
+      else
+        q[IB] += R(0.5) * (sdq0 * S0[cc + IB * sv] + sdq1 * S1[cc + IB * sv]);
+      if constexpr (d1 == 1)
+        q[IB] = B1 + R(0.5) * (sb1 * dB1d0);
+      else
+        q[IB] += R(0.5) * (sdq0 * S0[cc + IB * sv] + sdq1 * S1[cc + IB * sv]);
+      if constexpr (d1 == 2)
+        q[IC] = B1 + R(0.5) * (sb1 * dB1d0);
+      else
+        q[IC] += R(0.5) * (sdq0 * S0[cc + IC * sv] + sdq1 * S1[cc + IC * sv]);
+    }
+    q[ID] = fmax(smallR, q[ID]);
+    q[IP] = fmax(smallp * q[ID], q[IP]);
+  }
+  if constexpr (DIM == 3 && edir == 1)
+  {
+    // y edges: RB and LT are exchanged before the solve (MHDRunFunctors3D.h:1688-1698)
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      swap_vals(qe[1][v], qe[2][v]);
+  }
+  B.Em[c + (DIM == 2 ? 0 : (int64_t)edir * sv)] = compute_emf(edir, qe, G.gamma0, G.smallc);
+}
+
+template <class R, int DIM>
+__global__ void __launch_bounds__(128)
+k_emf(const Grid<R> G, Buffers<R> B)
+{
+  if (step_finished(B.st))
+    return;
+  const int g = G.g;
+  const Box b{ g, g, DIM == 3 ? g : 0, G.nx + 1, G.ny + 1, DIM == 3 ? G.nz + 1 : 1 };
+  int       i, j, k;
+  if (!box_cell(b, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
+    return;
+  if constexpr (DIM == 2)
+    emf_edge<R, 2, 2>(G, B, i, j, k);
+  else if (blockIdx.y == 0)
+    emf_edge<R, 3, 0>(G, B, i, j, k);
+  else if (blockIdx.y == 1)
+    emf_edge<R, 3, 1>(G, B, i, j, k);
+  else
+    emf_edge<R, 3, 2>(G, B, i, j, k);
+}
+
+// ---------------------------------------------------------------- update
+
+// U_out from U_in for interior cells, replaying the reference's atomic
+// updates in the order a serial run applies them: per direction x, y(, z)
+// "+ F(face i) dt/dx, - F(face i+1) dt/dx" for the hydro variables
+// (MHDRunFunctors2D.h:1231-1273, 3D:1255-1313), then the CT update of the
+// face-centred field (MHDRunFunctors2D.h:1519-1523, 3D:1638-1766):
+//   2D  Bx: - Ez(j) dt/dy + Ez(j+1) dt/dy;   By: + Ez(i) dt/dx - Ez(i+1) dt/dx
+//   3D  Bx: + Ey(k) dt/dz - Ey(k+1) dt/dz - Ez(j) dt/dy + Ez(j+1) dt/dy
+//       By: - Ex(k) dt/dz + Ex(k+1) dt/dz + Ez(i) dt/dx - Ez(i+1) dt/dx
+//       Bz: + Ex(j) dt/dy - Ex(j+1) dt/dy - Ey(i) dt/dx + Ey(i+1) dt/dx
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+k_update(const Grid<R> G, Buffers<R> B)
+{
+  if (step_finished(B.st))
+    return;
+  const int g = G.g;
+  const Box b{ g, g, DIM == 3 ? g : 0, G.nx, G.ny, DIM == 3 ? G.nz : 1 };
+  int       i, j, k;
+  if (!box_cell(b, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
+    return;
+  const int64_t sv = G.sv, sj = G.sj, sk = G.sk;
+  const int64_t c = cell_at(G, i, j, k);
+  const R       dtd[3] = { R(B.st->dtdx), R(B.st->dtdy), R(B.st->dtdz) };
+  const int64_t off[3] = { 1, sj, sk };
+  constexpr int NF = FluxComps<DIM>::NF;
+#pragma unroll
+  for (int q = 0; q < NF; ++q)
+  {
+    const int v = FluxComps<DIM>::var(q);
+    R         x = B.Uin[c + v * sv];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+    {
+      const R * F = B.F + ((int64_t)d * NF + q) * sv;
+      x += F[c] * dtd[d];
+      x -= F[c + off[d]] * dtd[d];
+    }
+    B.Uout[c + v * sv] = x;
+  }
+  const R *Em = B.Em;
+  if constexpr (DIM == 2)
+  {
+    R x = B.Uin[c + IA * sv];
+    x -= Em[c] * dtd[1];
+    x += Em[c + sj] * dtd[1];
+    B.Uout[c + IA * sv] = x;
+    x = B.Uin[c + IB * sv];
+    x += Em[c] * dtd[0];
+    x -= Em[c + 1] * dtd[0];
+    B.Uout[c + IB * sv] = x;
+    if constexpr (NF == 6)
+    {
+    }
+  }
+  else
+  {
+    const R *eX = Em, *eY = Em + sv, *eZ = Em + 2 * sv;
+    R        x = B.Uin[c + IA * sv];
+    x += eY[c] * dtd[2];
+    x -= eY[c + sk] * dtd[2];
+    x -= eZ[c] * dtd[1];
+    x += eZ[c + sj] * dtd[1];
+    B.Uout[c + IA * sv] = x;
+    x = B.Uin[c + IB * sv];
+    x -= eX[c] * dtd[2];
+    x += eX[c + sk] * dtd[2];
+    x += eZ[c] * dtd[0];
+    x -= eZ[c + 1] * dtd[0];
+    B.Uout[c + IB * sv] = x;
+    x = B.Uin[c + IC * sv];
+    x += eX[c] * dtd[1];
+    x -= eX[c + sj] * dtd[1];
+    x -= eY[c] * dtd[0];
+    x += eY[c + 1] * dtd[0];
+    B.Uout[c + IC * sv] = x;
+  }
+}
+
+} // namespace MHD_VARIANT_TAG
+} // namespace mhd

@@ -1,0 +1,573 @@
+// Point-wise MHD physics of the MUSCL-Hancock + HLLD + CT step, as device
+// functions templated on the real type R (double or float).
+//
+// Each function keeps the operation order of the reference expression it
+// implements (cited per function), so that a build without FMA contraction
+// (nvcc --fmad=false, MHD_FP_EXACT) reproduces a serial CPU run of the
+// reference bit for bit.  The fast build lets nvcc contract multiply-adds.
+#pragma once
+
+#include <cstdint>
+
+#ifndef MHD_VARIANT_TAG
+#  define MHD_VARIANT_TAG v_default
+#endif
+
+namespace mhd
+{
+inline namespace MHD_VARIANT_TAG
+{
+
+enum : int
+{
+  ID = 0,
+  IP = 1,
+  IU = 2,
+  IV = 3,
+  IW = 4,
+  IA = 5,
+  IB = 6,
+  IC = 7,
+  NV = 8
+};
+
+enum : int
+{
+  RIEMANN_LLF = 1,
+  RIEMANN_HLL = 2,
+  RIEMANN_HLLD = 4
+};
+
+template <class R>
+struct State
+{
+  R v[NV];
+  __device__ __forceinline__ R &
+  operator[](int i)
+  {
+    return v[i];
+  }
+  __device__ __forceinline__ const R &
+  operator[](int i) const
+  {
+    return v[i];
+  }
+};
+
+template <class R>
+__device__ __forceinline__ void
+swap_vals(R & a, R & b)
+{
+  R t = a;
+  a = b;
+  b = t;
+}
+
+// Fast magnetosonic speed with the normal field in slot IA
+// (find_speed_fast<IX>, mhd_utils.h:89-117).
+template <class R>
+__device__ __forceinline__ R
+fast_speed_x(const State<R> & q, R gamma0)
+{
+  const R d = q[ID], p = q[IP], a = q[IA], b = q[IB], c = q[IC];
+  const R b2 = a * a + b * b + c * c;
+  const R c2 = gamma0 * p / d;
+  const R d2 = R(0.5) * (b2 / d + c2);
+  return sqrt(d2 + sqrt(d2 * d2 - c2 * a * a / d));
+}
+
+// Same with the normal field in slot IB (find_speed_fast<IY>).
+template <class R>
+__device__ __forceinline__ R
+fast_speed_y(const State<R> & q, R gamma0)
+{
+  const R d = q[ID], p = q[IP], a = q[IA], b = q[IB], c = q[IC];
+  const R b2 = a * a + b * b + c * c;
+  const R c2 = gamma0 * p / d;
+  const R d2 = R(0.5) * (b2 / d + c2);
+  return sqrt(d2 + sqrt(d2 * d2 - c2 * b * b / d));
+}
+
+// MC-type limited slope of one variable from its two neighbours
+// (slope_unsplit_hydro_2d_scalar, MHDBaseFunctor2D.h:370-383; the same
+// statement sequence as compute_limited_slope, MHDBaseFunctor2D.h:129-155).
+template <class R>
+__device__ __forceinline__ R
+limited_slope(R q, R qp, R qm, R slope_type)
+{
+  const R dlft = slope_type * (q - qm);
+  const R drgt = slope_type * (qp - q);
+  const R dcen = R(0.5) * (qp - qm);
+  const R dsgn = (dcen >= R(0)) ? R(1) : R(-1);
+  const R slop = fmin(fabs(dlft), fabs(drgt));
+  R       dlim = slop;
+  if ((dlft * drgt) <= R(0))
+    dlim = R(0);
+  return dsgn * fmin(dlim, fabs(dcen));
+}
+
+// Conservative variables and 1D flux of a primitive state
+// (find_mhd_flux, mhd_utils.h:173-231; isothermal branch inactive).
+template <class R>
+__device__ __forceinline__ void
+mhd_flux_and_cons(const State<R> & q, State<R> & u, State<R> & f, R gamma0)
+{
+  const R p = q[IP];
+  const R entho = R(1) / (gamma0 - R(1));
+  const R d = q[ID], vu = q[IU], vv = q[IV], vw = q[IW], a = q[IA], b = q[IB], c = q[IC];
+  const R ecin = R(0.5) * (vu * vu + vv * vv + vw * vw) * d;
+  const R emag = R(0.5) * (a * a + b * b + c * c);
+  const R etot = p * entho + ecin + emag;
+  const R ptot = p + emag;
+  u[ID] = d;
+  u[IP] = etot;
+  u[IU] = d * vu;
+  u[IV] = d * vv;
+  u[IW] = d * vw;
+  u[IA] = a;
+  u[IB] = b;
+  u[IC] = c;
+  f[ID] = d * vu;
+  f[IP] = (etot + ptot) * vu - a * (a * vu + b * vv + c * vw);
+  f[IU] = d * vu * vu - a * a + ptot;
+  f[IV] = d * vu * vv - a * b;
+  f[IW] = d * vu * vw - a * c;
+  f[IA] = R(0);
+  f[IB] = b * vu - a * vv;
+  f[IC] = c * vu - a * vw;
+}
+
+// HLL (riemann_hll, RiemannSolvers_MHD.h:27-67).
+template <class R>
+__device__ void
+riemann_hll(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
+{
+  const R bx_mean = R(0.5) * (ql[IA] + qr[IA]);
+  ql[IA] = bx_mean;
+  qr[IA] = bx_mean;
+  State<R> ul, fl, ur, fr;
+  mhd_flux_and_cons(ql, ul, fl, gamma0);
+  mhd_flux_and_cons(qr, ur, fr, gamma0);
+  const R cfl = fast_speed_x(ql, gamma0);
+  const R cfr = fast_speed_x(qr, gamma0);
+  const R vl = ql[IU], vr = qr[IU];
+  const R sl = fmin(fmin(vl, vr) - fmax(cfl, cfr), R(0));
+  const R sr = fmax(fmax(vl, vr) + fmax(cfl, cfr), R(0));
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+    flux[v] = (sr * fl[v] - sl * fr[v] + sr * sl * (ur[v] - ul[v])) / (sr - sl);
+}
+
+// Local Lax-Friedrichs (riemann_llf, RiemannSolvers_MHD.h:81-111) with the
+// fastest x information speed (find_speed_info, mhd_utils.h:374-401).
+template <class R>
+__device__ void
+riemann_llf(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
+{
+  const R bx_mean = R(0.5) * (ql[IA] + qr[IA]);
+  ql[IA] = bx_mean;
+  qr[IA] = bx_mean;
+  State<R> ul, fl, ur, fr;
+  mhd_flux_and_cons(ql, ul, fl, gamma0);
+  mhd_flux_and_cons(qr, ur, fr, gamma0);
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+    flux[v] = (fl[v] + fr[v]) / R(2);
+  const R cl = fast_speed_x(ql, gamma0) + fabs(ql[IU]);
+  const R cr = fast_speed_x(qr, gamma0) + fabs(qr[IU]);
+  const R vel = fmax(cl, cr);
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+    flux[v] -= vel * (ur[v] - ul[v]) / R(2);
+}
+
+// HLLD of Miyoshi & Kusano (2005) in the RAMSES/DUMSES form
+// (riemann_hlld, RiemannSolvers_MHD.h:133-367).  States are in the
+// face-normal frame (normal velocity IU, normal field IA).
+template <class R>
+__device__ void
+riemann_hlld(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
+{
+  const R entho = R(1) / (gamma0 - R(1));
+  const R a = R(0.5) * (ql[IA] + qr[IA]);
+  const R sgnm = (a >= R(0)) ? R(1) : R(-1);
+  ql[IA] = a;
+  qr[IA] = a;
+
+  const R rl = ql[ID], pl = ql[IP], ul = ql[IU], vl = ql[IV], wl = ql[IW], bl = ql[IB],
+          cl = ql[IC];
+  const R ecinl = R(0.5) * (ul * ul + vl * vl + wl * wl) * rl;
+  const R emagl = R(0.5) * (a * a + bl * bl + cl * cl);
+  const R etotl = pl * entho + ecinl + emagl;
+  const R ptotl = pl + emagl;
+  const R vdotbl = ul * a + vl * bl + wl * cl;
+
+  const R rr = qr[ID], pr = qr[IP], ur = qr[IU], vr = qr[IV], wr = qr[IW], br = qr[IB],
+          cr = qr[IC];
+  const R ecinr = R(0.5) * (ur * ur + vr * vr + wr * wr) * rr;
+  const R emagr = R(0.5) * (a * a + br * br + cr * cr);
+  const R etotr = pr * entho + ecinr + emagr;
+  const R ptotr = pr + emagr;
+  const R vdotbr = ur * a + vr * br + wr * cr;
+
+  const R cfastl = fast_speed_x(ql, gamma0);
+  const R cfastr = fast_speed_x(qr, gamma0);
+
+  const R sl = fmin(ul, ur) - fmax(cfastl, cfastr);
+  const R sr = fmax(ul, ur) + fmax(cfastl, cfastr);
+
+  const R rcl = rl * (ul - sl);
+  const R rcr = rr * (sr - ur);
+
+  const R ustar = (rcr * ur + rcl * ul + (ptotl - ptotr)) / (rcr + rcl);
+  const R ptotstar = (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) / (rcr + rcl);
+
+  // left star state
+  const R rstarl = rl * (sl - ul) / (sl - ustar);
+  R       estar = rl * (sl - ul) * (sl - ustar) - a * a;
+  const R el = rl * (sl - ul) * (sl - ul) - a * a;
+  R       vstarl, wstarl, bstarl, cstarl;
+  if (a * a > R(0) && fabs(estar / (a * a) - R(1)) <= R(1e-8))
+  {
+    vstarl = vl;
+    bstarl = bl;
+    wstarl = wl;
+    cstarl = cl;
+  }
+  else
+  {
+    vstarl = vl - a * bl * (ustar - ul) / estar;
+    bstarl = bl * el / estar;
+    wstarl = wl - a * cl * (ustar - ul) / estar;
+    cstarl = cl * el / estar;
+  }
+  const R vdotbstarl = ustar * a + vstarl * bstarl + wstarl * cstarl;
+  const R etotstarl =
+    ((sl - ul) * etotl - ptotl * ul + ptotstar * ustar + a * (vdotbl - vdotbstarl)) / (sl - ustar);
+  const R sqrrstarl = sqrt(rstarl);
+  const R calfvenl = fabs(a) / sqrrstarl;
+  const R sal = ustar - calfvenl;
+
+  // right star state
+  const R rstarr = rr * (sr - ur) / (sr - ustar);
+  estar = rr * (sr - ur) * (sr - ustar) - a * a;
+  const R er = rr * (sr - ur) * (sr - ur) - a * a;
+  R       vstarr, wstarr, bstarr, cstarr;
+  if (a * a > R(0) && fabs(estar / (a * a) - R(1)) <= R(1e-8))
+  {
+    vstarr = vr;
+    bstarr = br;
+    wstarr = wr;
+    cstarr = cr;
+  }
+  else
+  {
+    vstarr = vr - a * br * (ustar - ur) / estar;
+    bstarr = br * er / estar;
+    wstarr = wr - a * cr * (ustar - ur) / estar;
+    cstarr = cr * er / estar;
+  }
+  const R vdotbstarr = ustar * a + vstarr * bstarr + wstarr * cstarr;
+  const R etotstarr =
+    ((sr - ur) * etotr - ptotr * ur + ptotstar * ustar + a * (vdotbr - vdotbstarr)) / (sr - ustar);
+  const R sqrrstarr = sqrt(rstarr);
+  const R calfvenr = fabs(a) / sqrrstarr;
+  const R sar = ustar + calfvenr;
+
+  // sample the self-similar solution at x/t = 0, in the reference's order
+  R ro, uo, vo, wo, bo, co, ptoto, etoto, vdotbo;
+  if (sl > R(0))
+  {
+    ro = rl; uo = ul; vo = vl; wo = wl; bo = bl; co = cl;
+    ptoto = ptotl; etoto = etotl; vdotbo = vdotbl;
+  }
+  else if (sal > R(0))
+  {
+    ro = rstarl; uo = ustar; vo = vstarl; wo = wstarl; bo = bstarl; co = cstarl;
+    ptoto = ptotstar; etoto = etotstarl; vdotbo = vdotbstarl;
+  }
+  else if (!(ustar > R(0)) && !(sar > R(0)))
+  {
+    if (sr > R(0))
+    {
+      ro = rstarr; uo = ustar; vo = vstarr; wo = wstarr; bo = bstarr; co = cstarr;
+      ptoto = ptotstar; etoto = etotstarr; vdotbo = vdotbstarr;
+    }
+    else
+    {
+      ro = rr; uo = ur; vo = vr; wo = wr; bo = br; co = cr;
+      ptoto = ptotr; etoto = etotr; vdotbo = vdotbr;
+    }
+  }
+  else
+  {
+    // double-star states, only needed between the two Alfven waves
+    const R vstarstar = (sqrrstarl * vstarl + sqrrstarr * vstarr + sgnm * (bstarr - bstarl)) /
+                        (sqrrstarl + sqrrstarr);
+    const R wstarstar = (sqrrstarl * wstarl + sqrrstarr * wstarr + sgnm * (cstarr - cstarl)) /
+                        (sqrrstarl + sqrrstarr);
+    const R bstarstar =
+      (sqrrstarl * bstarr + sqrrstarr * bstarl + sgnm * sqrrstarl * sqrrstarr * (vstarr - vstarl)) /
+      (sqrrstarl + sqrrstarr);
+    const R cstarstar =
+      (sqrrstarl * cstarr + sqrrstarr * cstarl + sgnm * sqrrstarl * sqrrstarr * (wstarr - wstarl)) /
+      (sqrrstarl + sqrrstarr);
+    const R vdotbstarstar = ustar * a + vstarstar * bstarstar + wstarstar * cstarstar;
+    uo = ustar;
+    vo = vstarstar;
+    wo = wstarstar;
+    bo = bstarstar;
+    co = cstarstar;
+    ptoto = ptotstar;
+    vdotbo = vdotbstarstar;
+    if (ustar > R(0))
+    {
+      ro = rstarl;
+      etoto = etotstarl - sgnm * sqrrstarl * (vdotbstarl - vdotbstarstar);
+    }
+    else
+    {
+      ro = rstarr;
+      etoto = etotstarr + sgnm * sqrrstarr * (vdotbstarr - vdotbstarstar);
+    }
+  }
+
+  flux[ID] = ro * uo;
+  flux[IP] = (etoto + ptoto) * uo - a * vdotbo;
+  flux[IU] = ro * uo * uo - a * a + ptoto;
+  flux[IV] = ro * uo * vo - a * bo;
+  flux[IW] = ro * uo * wo - a * co;
+  flux[IA] = R(0);
+  flux[IB] = bo * uo - a * vo;
+  flux[IC] = co * uo - a * wo;
+}
+
+// riemann_mhd dispatch (RiemannSolvers_MHD.h:372-392)
+template <class R>
+__device__ __forceinline__ void
+riemann(int solver, State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
+{
+  if (solver == RIEMANN_HLLD)
+    riemann_hlld(ql, qr, flux, gamma0);
+  else if (solver == RIEMANN_HLL)
+    riemann_hll(ql, qr, flux, gamma0);
+  else
+    riemann_llf(ql, qr, flux, gamma0);
+}
+
+template <class R>
+__device__ __forceinline__ R
+max4(R a0, R a1, R a2, R a3)
+{
+  R r = a0;
+  r = (a1 > r) ? a1 : r;
+  r = (a2 > r) ? a2 : r;
+  r = (a3 > r) ? a3 : r;
+  return r;
+}
+template <class R>
+__device__ __forceinline__ R
+min4(R a0, R a1, R a2, R a3)
+{
+  R r = a0;
+  r = (a1 < r) ? a1 : r;
+  r = (a2 < r) ? a2 : r;
+  r = (a3 < r) ? a3 : r;
+  return r;
+}
+template <class R>
+__device__ __forceinline__ R
+max5(R a0, R a1, R a2, R a3, R a4)
+{
+  R r = a0;
+  r = (a1 > r) ? a1 : r;
+  r = (a2 > r) ? a2 : r;
+  r = (a3 > r) ? a3 : r;
+  r = (a4 > r) ? a4 : r;
+  return r;
+}
+
+// Two-dimensional HLLD magnetic Riemann solver giving the edge EMF
+// (mag_riemann2d_hlld, RiemannSolvers_MHD.h:398-630).  q[0..3] are the
+// LL, RL, LR, RR states; e[0..3] their corner emfs.  The region is selected
+// by the signs of SB, ST, SL, SR exactly as the reference's 0/1 masks do
+// (copysign based, :569-596); only the selected candidate is evaluated.
+template <class R>
+__device__ R
+mag_riemann2d_hlld(const State<R> (&q)[4], const R (&e)[4], R gamma0, R smallc)
+{
+  const State<R> &qLL = q[0], &qRL = q[1], &qLR = q[2], &qRR = q[3];
+  const R         ELL = e[0], ERL = e[1], ELR = e[2], ERR = e[3];
+
+  const R rLL = qLL[ID], pLL = qLL[IP], uLL = qLL[IU], vLL = qLL[IV], aLL = qLL[IA],
+          bLL = qLL[IB], cLL = qLL[IC];
+  const R rLR = qLR[ID], pLR = qLR[IP], uLR = qLR[IU], vLR = qLR[IV], aLR = qLR[IA],
+          bLR = qLR[IB], cLR = qLR[IC];
+  const R rRL = qRL[ID], pRL = qRL[IP], uRL = qRL[IU], vRL = qRL[IV], aRL = qRL[IA],
+          bRL = qRL[IB], cRL = qRL[IC];
+  const R rRR = qRR[ID], pRR = qRR[IP], uRR = qRR[IU], vRR = qRR[IV], aRR = qRR[IA],
+          bRR = qRR[IB], cRR = qRR[IC];
+
+  const R cFastLLx = fast_speed_x(qLL, gamma0);
+  const R cFastLRx = fast_speed_x(qLR, gamma0);
+  const R cFastRLx = fast_speed_x(qRL, gamma0);
+  const R cFastRRx = fast_speed_x(qRR, gamma0);
+  const R cFastLLy = fast_speed_y(qLL, gamma0);
+  const R cFastLRy = fast_speed_y(qLR, gamma0);
+  const R cFastRLy = fast_speed_y(qRL, gamma0);
+  const R cFastRRy = fast_speed_y(qRR, gamma0);
+
+  const R SL = min4(uLL, uLR, uRL, uRR) - max4(cFastLLx, cFastLRx, cFastRLx, cFastRRx);
+  const R SR = max4(uLL, uLR, uRL, uRR) + max4(cFastLLx, cFastLRx, cFastRLx, cFastRRx);
+  const R SB = min4(vLL, vLR, vRL, vRR) - max4(cFastLLy, cFastLRy, cFastRLy, cFastRRy);
+  const R ST = max4(vLL, vLR, vRL, vRR) + max4(cFastLLy, cFastLRy, cFastRLy, cFastRRy);
+
+  // region flags from the sign bits, as (int)(1 + copysign(1, S)) / 2 does
+  const bool SB_pos = !signbit(SB), ST_pos = !signbit(ST);
+  const bool SL_pos = !signbit(SL), SR_pos = !signbit(SR);
+
+  // Corner regions return an input emf directly.
+  if (SB_pos && SL_pos)
+    return ELL;
+  if (SB_pos && !SR_pos)
+    return ERL;
+  if (!SB_pos && !ST_pos && SL_pos)
+    return ELR;
+  if (!SB_pos && !ST_pos && !SR_pos)
+    return ERR;
+
+  const R PtotLL = pLL + R(0.5) * (aLL * aLL + bLL * bLL + cLL * cLL);
+  const R PtotLR = pLR + R(0.5) * (aLR * aLR + bLR * bLR + cLR * cLR);
+  const R PtotRL = pRL + R(0.5) * (aRL * aRL + bRL * bRL + cRL * cRL);
+  const R PtotRR = pRR + R(0.5) * (aRR * aRR + bRR * bRR + cRR * cRR);
+
+  const R rcLLx = rLL * (uLL - SL);
+  const R rcRLx = rRL * (SR - uRL);
+  const R rcLRx = rLR * (uLR - SL);
+  const R rcRRx = rRR * (SR - uRR);
+  const R rcLLy = rLL * (vLL - SB);
+  const R rcLRy = rLR * (ST - vLR);
+  const R rcRLy = rRL * (vRL - SB);
+  const R rcRRy = rRR * (ST - vRR);
+
+  const R ustar =
+    (rcLLx * uLL + rcLRx * uLR + rcRLx * uRL + rcRRx * uRR + (PtotLL - PtotRL + PtotLR - PtotRR)) /
+    (rcLLx + rcLRx + rcRLx + rcRRx);
+  const R vstar =
+    (rcLLy * vLL + rcLRy * vLR + rcRLy * vRL + rcRRy * vRR + (PtotLL - PtotLR + PtotRL - PtotRR)) /
+    (rcLLy + rcLRy + rcRLy + rcRRy);
+
+  const R rstarLLx = rLL * (SL - uLL) / (SL - ustar);
+  const R BstarLL = bLL * (SL - uLL) / (SL - ustar);
+  const R rstarLLy = rLL * (SB - vLL) / (SB - vstar);
+  const R AstarLL = aLL * (SB - vLL) / (SB - vstar);
+  const R rstarLL = rLL * (SL - uLL) / (SL - ustar) * (SB - vLL) / (SB - vstar);
+  const R EstarLLx = ustar * BstarLL - vLL * aLL;
+  const R EstarLLy = uLL * bLL - vstar * AstarLL;
+  const R EstarLL = ustar * BstarLL - vstar * AstarLL;
+
+  const R rstarLRx = rLR * (SL - uLR) / (SL - ustar);
+  const R BstarLR = bLR * (SL - uLR) / (SL - ustar);
+  const R rstarLRy = rLR * (ST - vLR) / (ST - vstar);
+  const R AstarLR = aLR * (ST - vLR) / (ST - vstar);
+  const R rstarLR = rLR * (SL - uLR) / (SL - ustar) * (ST - vLR) / (ST - vstar);
+  const R EstarLRx = ustar * BstarLR - vLR * aLR;
+  const R EstarLRy = uLR * bLR - vstar * AstarLR;
+  const R EstarLR = ustar * BstarLR - vstar * AstarLR;
+
+  const R rstarRLx = rRL * (SR - uRL) / (SR - ustar);
+  const R BstarRL = bRL * (SR - uRL) / (SR - ustar);
+  const R rstarRLy = rRL * (SB - vRL) / (SB - vstar);
+  const R AstarRL = aRL * (SB - vRL) / (SB - vstar);
+  const R rstarRL = rRL * (SR - uRL) / (SR - ustar) * (SB - vRL) / (SB - vstar);
+  const R EstarRLx = ustar * BstarRL - vRL * aRL;
+  const R EstarRLy = uRL * bRL - vstar * AstarRL;
+  const R EstarRL = ustar * BstarRL - vstar * AstarRL;
+
+  const R rstarRRx = rRR * (SR - uRR) / (SR - ustar);
+  const R BstarRR = bRR * (SR - uRR) / (SR - ustar);
+  const R rstarRRy = rRR * (ST - vRR) / (ST - vstar);
+  const R AstarRR = aRR * (ST - vRR) / (ST - vstar);
+  const R rstarRR = rRR * (SR - uRR) / (SR - ustar) * (ST - vRR) / (ST - vstar);
+  const R EstarRRx = ustar * BstarRR - vRR * aRR;
+  const R EstarRRy = uRR * bRR - vstar * AstarRR;
+  const R EstarRR = ustar * BstarRR - vstar * AstarRR;
+
+  const R calfvenL = max5(fabs(aLR) / sqrt(rstarLRx), fabs(AstarLR) / sqrt(rstarLR),
+                          fabs(aLL) / sqrt(rstarLLx), fabs(AstarLL) / sqrt(rstarLL), smallc);
+  const R calfvenR = max5(fabs(aRR) / sqrt(rstarRRx), fabs(AstarRR) / sqrt(rstarRR),
+                          fabs(aRL) / sqrt(rstarRLx), fabs(AstarRL) / sqrt(rstarRL), smallc);
+  const R calfvenB = max5(fabs(bLL) / sqrt(rstarLLy), fabs(BstarLL) / sqrt(rstarLL),
+                          fabs(bRL) / sqrt(rstarRLy), fabs(BstarRL) / sqrt(rstarRL), smallc);
+  const R calfvenT = max5(fabs(bLR) / sqrt(rstarLRy), fabs(BstarLR) / sqrt(rstarLR),
+                          fabs(bRR) / sqrt(rstarRRy), fabs(BstarRR) / sqrt(rstarRR), smallc);
+
+  const R SAL = fmin(ustar - calfvenL, R(0));
+  const R SAR = fmax(ustar + calfvenR, R(0));
+  const R SAB = fmin(vstar - calfvenB, R(0));
+  const R SAT = fmax(vstar + calfvenT, R(0));
+
+  if (SB_pos) // SL < 0 < SR
+    return (SAR * EstarLLx - SAL * EstarRLx + SAR * SAL * (bRL - bLL)) / (SAR - SAL);
+  if (!ST_pos) // SL < 0 < SR
+    return (SAR * EstarLRx - SAL * EstarRRx + SAR * SAL * (bRR - bLR)) / (SAR - SAL);
+  if (SL_pos)
+    return (SAT * EstarLLy - SAB * EstarLRy - SAT * SAB * (aLR - aLL)) / (SAT - SAB);
+  if (!SR_pos)
+    return (SAT * EstarRLy - SAB * EstarRRy - SAT * SAB * (aRR - aRL)) / (SAT - SAB);
+
+  const R AstarT = (SAR * AstarRR - SAL * AstarLR) / (SAR - SAL);
+  const R AstarB = (SAR * AstarRL - SAL * AstarLL) / (SAR - SAL);
+  const R BstarR = (SAT * BstarRR - SAB * BstarRL) / (SAT - SAB);
+  const R BstarL = (SAT * BstarLR - SAB * BstarLL) / (SAT - SAB);
+  return (SAL * SAB * EstarRR - SAL * SAT * EstarRL - SAR * SAB * EstarLR + SAR * SAT * EstarLL) /
+           (SAR - SAL) / (SAT - SAB) -
+         SAT * SAB / (SAT - SAB) * (AstarT - AstarB) + SAR * SAL / (SAR - SAL) * (BstarR - BstarL);
+}
+
+// compute_emf<EmfDir> (RiemannSolvers_MHD.h:651-874): rotate the four
+// reconstructed edge states (RT, RB, LT, LB) into the 2D frame of the edge,
+// average the parallel field components and call the 2D solver.
+// edir: 0 = EMFX, 1 = EMFY, 2 = EMFZ.
+template <class R>
+__device__ __forceinline__ R
+compute_emf(int edir, const State<R> (&qe)[4], R gamma0, R smallc)
+{
+  const State<R> &qRT = qe[0], &qRB = qe[1], &qLT = qe[2], &qLB = qe[3];
+  int             iu, iv, iw, ia, ib, ic;
+  if (edir == 2)
+  {
+    iu = IU; iv = IV; iw = IW; ia = IA; ib = IB; ic = IC;
+  }
+  else if (edir == 1)
+  {
+    iu = IW; iv = IU; iw = IV; ia = IC; ib = IA; ic = IB;
+  }
+  else
+  {
+    iu = IV; iv = IW; iw = IU; ia = IB; ib = IC; ic = IA;
+  }
+  State<R> q[4]; // LL, RL, LR, RR
+  q[0][ID] = qRT[ID]; q[1][ID] = qLT[ID]; q[2][ID] = qRB[ID]; q[3][ID] = qLB[ID];
+  q[0][IP] = qRT[IP]; q[1][IP] = qLT[IP]; q[2][IP] = qRB[IP]; q[3][IP] = qLB[IP];
+  q[0][IU] = qRT[iu]; q[1][IU] = qLT[iu]; q[2][IU] = qRB[iu]; q[3][IU] = qLB[iu];
+  q[0][IV] = qRT[iv]; q[1][IV] = qLT[iv]; q[2][IV] = qRB[iv]; q[3][IV] = qLB[iv];
+  q[0][IA] = R(0.5) * (qRT[ia] + qLT[ia]);
+  q[1][IA] = q[0][IA];
+  q[2][IA] = R(0.5) * (qRB[ia] + qLB[ia]);
+  q[3][IA] = q[2][IA];
+  q[0][IB] = R(0.5) * (qRT[ib] + qRB[ib]);
+  q[1][IB] = R(0.5) * (qLT[ib] + qLB[ib]);
+  q[2][IB] = q[0][IB];
+  q[3][IB] = q[1][IB];
+  q[0][IW] = qRT[iw]; q[1][IW] = qLT[iw]; q[2][IW] = qRB[iw]; q[3][IW] = qLB[iw];
+  q[0][IC] = qRT[ic]; q[1][IC] = qLT[ic]; q[2][IC] = qRB[ic]; q[3][IC] = qLB[ic];
+  R e[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+    e[c] = q[c][IU] * q[c][IB] - q[c][IV] * q[c][IA];
+  return mag_riemann2d_hlld(q, e, gamma0, smallc);
+}
+
+} // namespace MHD_VARIANT_TAG
+} // namespace mhd

@@ -1,0 +1,755 @@
+// Solver core for one arithmetic variant: device buffers, one CUDA stream,
+// the launch sequence of an iteration, CUDA-graph replay of whole runs,
+// host<->device state transfer in either Kokkos layout, FP64 diagnostics and
+// per-kernel timing.  Included by mhd_variant.cu, which fixes R and the
+// inline namespace MHD_VARIANT_TAG.
+#pragma once
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "mhd_core.h"
+#include "mhd_kernels.cuh"
+
+namespace mhd
+{
+inline namespace MHD_VARIANT_TAG
+{
+
+#define MHD_CK(call)                                                                  \
+  do                                                                                  \
+  {                                                                                   \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess)                                                            \
+    {                                                                                 \
+      err = std::string(#call) + ": " + cudaGetErrorString(e_);                       \
+      return MHD_ERR_CUDA;                                                            \
+    }                                                                                 \
+  } while (0)
+
+// LayoutRight <-> LayoutLeft.  dir = 0: right -> left, dir = 1: left -> right.
+template <class R>
+__global__ void
+k_transpose(const Grid<R> G, const R * __restrict__ src, R * __restrict__ dst, int dir)
+{
+  const int64_t n = G.sv * NV;
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx >= n)
+    return;
+  // idx enumerates the LayoutLeft index: i + isize*(j + jsize*(k + ksize*v))
+  const int64_t v = idx / G.sv;
+  const int64_t cell = idx - v * G.sv;
+  const int64_t k = cell / G.sk;
+  const int64_t rem = cell - k * G.sk;
+  const int64_t j = rem / G.sj;
+  const int64_t i = rem - j * G.sj;
+  const int64_t right = ((i * G.jsize + j) * G.ksize + k) * NV + v;
+  if (dir == 0)
+    dst[idx] = src[right];
+  else
+    dst[right] = src[idx];
+}
+
+// FP64 sums of the 8 stored variables and of |div B| over interior cells,
+// one partial record of 10 doubles per block (sums[8], sum |divB|, max |divB|).
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+k_diag(const Grid<R> G, const R * __restrict__ U, double * __restrict__ partial)
+{
+  const int g = G.g;
+  const Box b{ g, g, DIM == 3 ? g : 0, G.nx, G.ny, DIM == 3 ? G.nz : 1 };
+  double    acc[10];
+#pragma unroll
+  for (int q = 0; q < 10; ++q)
+    acc[q] = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < b.count(); idx += stride)
+  {
+    int i, j, k;
+    box_cell(b, idx, i, j, k);
+    const int64_t c = cell_at(G, i, j, k), sv = G.sv;
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      acc[v] += (double)U[c + v * sv];
+    double div = ((double)U[c + 1 + IA * sv] - (double)U[c + IA * sv]) / G.dx +
+                 ((double)U[c + G.sj + IB * sv] - (double)U[c + IB * sv]) / G.dy;
+    if (DIM == 3)
+      div += ((double)U[c + G.sk + IC * sv] - (double)U[c + IC * sv]) / G.dz;
+    acc[8] += fabs(div);
+    acc[9] = fmax(acc[9], fabs(div));
+  }
+  __shared__ double sh[10][256];
+#pragma unroll
+  for (int q = 0; q < 10; ++q)
+    sh[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1)
+  {
+    if ((int)threadIdx.x < s)
+    {
+#pragma unroll
+      for (int q = 0; q < 9; ++q)
+        sh[q][threadIdx.x] += sh[q][threadIdx.x + s];
+      sh[9][threadIdx.x] = fmax(sh[9][threadIdx.x], sh[9][threadIdx.x + s]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 10)
+    partial[blockIdx.x * 10 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void
+k_diag_final(const double * __restrict__ partial, int nblocks, double * __restrict__ out)
+{
+  const int q = threadIdx.x;
+  if (q >= 10)
+    return;
+  double a = 0.0;
+  for (int b = 0; b < nblocks; ++b)
+  {
+    const double x = partial[b * 10 + q];
+    a = (q == 9) ? fmax(a, x) : a + x;
+  }
+  out[q] = a;
+}
+
+template <class R>
+class SolverImpl final : public SolverCore
+{
+public:
+  static constexpr int kDiagBlocks = 1024;
+
+  mhd_params   P{};
+  Grid<R>      G{};
+  int          dim = 2;
+  int64_t      ncell = 0; // ghost-inclusive cells
+  R *          U = nullptr;
+  R *          U2 = nullptr;
+  R *          Q = nullptr;
+  R *          Q2 = nullptr;
+  R *          S = nullptr;
+  R *          E = nullptr;
+  R *          F = nullptr;
+  R *          Em = nullptr;
+  double *     diag = nullptr;
+  DevState *   st = nullptr;
+  DevState *   st_host = nullptr; // pinned
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph[2] = { nullptr, nullptr }; // one iteration starting from U / from U2
+  cudaGraphExec_t graph_pair[2] = { nullptr, nullptr }; // two iterations
+  int64_t launched = 0; // iterations enqueued since the last state reset (parity)
+
+  ~SolverImpl() override
+  {
+    for (int q = 0; q < 2; ++q)
+    {
+      if (graph[q])
+        cudaGraphExecDestroy(graph[q]);
+      if (graph_pair[q])
+        cudaGraphExecDestroy(graph_pair[q]);
+    }
+    R * bufs[] = { U, U2, Q, Q2, S, E, F, Em };
+    for (R * b : bufs)
+      if (b)
+        cudaFree(b);
+    if (diag)
+      cudaFree(diag);
+    if (st)
+      cudaFree(st);
+    if (st_host)
+      cudaFreeHost(st_host);
+    if (stream)
+      cudaStreamDestroy(stream);
+  }
+
+  int
+  real_bytes() const override
+  {
+    return (int)sizeof(R);
+  }
+
+  int
+  bind_device() override
+  {
+    MHD_CK(cudaSetDevice(P.device));
+    return MHD_OK;
+  }
+
+  int
+  setup(const mhd_params & p)
+  {
+    P = p;
+    dim = p.dim;
+    G.dim = p.dim;
+    G.nx = p.nx;
+    G.ny = p.ny;
+    G.nz = p.dim == 3 ? p.nz : 1;
+    G.g = p.ghost;
+    G.isize = p.nx + 2 * p.ghost;
+    G.jsize = p.ny + 2 * p.ghost;
+    G.ksize = p.dim == 3 ? p.nz + 2 * p.ghost : 1;
+    G.sj = G.isize;
+    G.sk = (int64_t)G.isize * G.jsize;
+    G.sv = G.sk * G.ksize;
+    for (int f = 0; f < 6; ++f)
+      G.bc[f] = p.boundary[f];
+    G.riemann = p.riemann;
+    G.gamma0 = R(p.gamma0);
+    G.smallr = R(p.smallr);
+    G.smallc = R(p.smallc);
+    // HydroParams::init (HydroParams.cpp:438): smallp = smallc^2 / gamma0, in real_t
+    G.smallp = R(R(p.smallc) * R(p.smallc) / R(p.gamma0));
+    G.slope_type = R(p.slope_type);
+    G.cfl = p.cfl;
+    // dx = (xmax - xmin) / nx in real_t (HydroParams.cpp:433-435)
+    G.dx = (double)R(R(p.xmax - p.xmin) / R(p.nx));
+    G.dy = (double)R(R(p.ymax - p.ymin) / R(p.ny));
+    G.dz = p.dim == 3 ? (double)R(R(p.zmax - p.zmin) / R(p.nz)) : 1.0;
+    ncell = G.sv;
+
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    {
+      err = "no CUDA device available";
+      return MHD_ERR_NO_DEVICE;
+    }
+    if (p.device < 0 || p.device >= ndev)
+    {
+      err = "device ordinal " + std::to_string(p.device) + " out of range";
+      return MHD_ERR_INVALID_ARG;
+    }
+    MHD_CK(cudaSetDevice(p.device));
+    MHD_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    const size_t n = (size_t)ncell;
+    const int    nplanes_e = dim == 3 ? 3 : 1;
+    const int    nf = dim == 3 ? 5 : 6;
+    MHD_CK(cudaMalloc(&U, n * NV * sizeof(R)));
+    MHD_CK(cudaMalloc(&U2, n * NV * sizeof(R)));
+    MHD_CK(cudaMalloc(&Q, n * NV * sizeof(R)));
+    MHD_CK(cudaMalloc(&Q2, n * NV * sizeof(R)));
+    MHD_CK(cudaMalloc(&S, n * NV * dim * sizeof(R)));
+    MHD_CK(cudaMalloc(&E, n * nplanes_e * sizeof(R)));
+    MHD_CK(cudaMalloc(&F, n * nf * dim * sizeof(R)));
+    MHD_CK(cudaMalloc(&Em, n * nplanes_e * sizeof(R)));
+    MHD_CK(cudaMalloc(&diag, (kDiagBlocks * 10 + 16) * sizeof(double)));
+    MHD_CK(cudaMalloc(&st, sizeof(DevState)));
+    MHD_CK(cudaMallocHost(&st_host, sizeof(DevState)));
+    // zero everything once: halo reads of never-written planes see zeros,
+    // as the reference's zero-initialised Kokkos views do
+    R * bufs[] = { U, U2, Q, Q2 };
+    for (R * b : bufs)
+      MHD_CK(cudaMemsetAsync(b, 0, n * NV * sizeof(R), stream));
+    MHD_CK(cudaMemsetAsync(S, 0, n * NV * dim * sizeof(R), stream));
+    MHD_CK(cudaMemsetAsync(E, 0, n * nplanes_e * sizeof(R), stream));
+    MHD_CK(cudaMemsetAsync(F, 0, n * nf * dim * sizeof(R), stream));
+    MHD_CK(cudaMemsetAsync(Em, 0, n * nplanes_e * sizeof(R), stream));
+    MHD_CK(reset_time_state());
+    MHD_CK(cudaStreamSynchronize(stream));
+    return MHD_OK;
+  }
+
+  cudaError_t
+  reset_time_state()
+  {
+    DevState h{};
+    h.t = P.tCurrent;
+    h.dt = 0.0;
+    h.tEnd = P.tEnd;
+    h.it = 0;
+    h.nStepmax = P.nStepmax;
+    h.status = 0;
+    *st_host = h;
+    launched = 0;
+    return cudaMemcpyAsync(st, st_host, sizeof(DevState), cudaMemcpyHostToDevice, stream);
+  }
+
+  Buffers<R>
+  buffers(int parity) const
+  {
+    Buffers<R> B;
+    B.Uin = parity ? U2 : U;
+    B.Uout = parity ? U : U2;
+    B.Q = Q;
+    B.Q2 = Q2;
+    B.S = S;
+    B.E = E;
+    B.F = F;
+    B.Em = Em;
+    B.st = st;
+    return B;
+  }
+
+  static unsigned
+  nblocks(int64_t n, int t)
+  {
+    return (unsigned)((n + t - 1) / t);
+  }
+
+  // ---- kernel launchers (dimension dispatch) ----
+  void
+  launch_boundaries(R * arr, int force)
+  {
+    const int64_t n = ncell;
+    if (dim == 2)
+      k_boundaries<R, 2><<<nblocks(n, 256), 256, 0, stream>>>(G, arr, st, force);
+    else
+      k_boundaries<R, 3><<<nblocks(n, 256), 256, 0, stream>>>(G, arr, st, force);
+  }
+  void
+  launch_prim_dt(const R * arr, int force)
+  {
+    const int64_t n = (int64_t)(G.isize - 1) * (G.jsize - 1) * (dim == 3 ? G.ksize - 1 : 1);
+    if (dim == 2)
+      k_prim_dt<R, 2><<<nblocks(n, 256), 256, 0, stream>>>(G, arr, Q, st, force);
+    else
+      k_prim_dt<R, 3><<<nblocks(n, 256), 256, 0, stream>>>(G, arr, Q, st, force);
+  }
+  void
+  launch_finalize(int force)
+  {
+    k_finalize_dt<R><<<1, 1, 0, stream>>>(G, st, force);
+  }
+  void
+  launch_trace(const Buffers<R> & B)
+  {
+    const int64_t n = (int64_t)(G.nx + 3) * (G.ny + 3) * (dim == 3 ? G.nz + 3 : 1);
+    if (dim == 2)
+      k_trace<R, 2><<<nblocks(n, 128), 128, 0, stream>>>(G, B);
+    else
+      k_trace<R, 3><<<nblocks(n, 128), 128, 0, stream>>>(G, B);
+  }
+  void
+  launch_flux(const Buffers<R> & B)
+  {
+    const int64_t n = (int64_t)(G.nx + 1) * (G.ny + 1) * (dim == 3 ? G.nz + 1 : 1);
+    if (dim == 2)
+      k_flux<R, 2><<<dim3(nblocks(n, 128), 2), 128, 0, stream>>>(G, B);
+    else
+      k_flux<R, 3><<<dim3(nblocks(n, 128), 3), 128, 0, stream>>>(G, B);
+  }
+  void
+  launch_emf(const Buffers<R> & B)
+  {
+    const int64_t n = (int64_t)(G.nx + 1) * (G.ny + 1) * (dim == 3 ? G.nz + 1 : 1);
+    if (dim == 2)
+      k_emf<R, 2><<<dim3(nblocks(n, 128), 1), 128, 0, stream>>>(G, B);
+    else
+      k_emf<R, 3><<<dim3(nblocks(n, 128), 3), 128, 0, stream>>>(G, B);
+  }
+  void
+  launch_update(const Buffers<R> & B)
+  {
+    const int64_t n = (int64_t)G.nx * G.ny * (dim == 3 ? G.nz : 1);
+    if (dim == 2)
+      k_update<R, 2><<<nblocks(n, 256), 256, 0, stream>>>(G, B);
+    else
+      k_update<R, 3><<<nblocks(n, 256), 256, 0, stream>>>(G, B);
+  }
+  void
+  launch_advance()
+  {
+    k_advance<R><<<1, 1, 0, stream>>>(st);
+  }
+
+  static constexpr int kLaunches = 8;
+
+  // One iteration (godunov_unsplit_impl + next_iteration bookkeeping).
+  void
+  enqueue_step(int parity)
+  {
+    const Buffers<R> B = buffers(parity);
+    launch_boundaries(B.Uin, 0);
+    launch_prim_dt(B.Uin, 0);
+    launch_finalize(0);
+    launch_trace(B);
+    launch_flux(B);
+    launch_emf(B);
+    launch_update(B);
+    launch_advance();
+  }
+
+  int
+  launches_per_step() override
+  {
+    return kLaunches;
+  }
+
+  int
+  check_launch()
+  {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+    {
+      err = std::string("kernel launch: ") + cudaGetErrorString(e);
+      return MHD_ERR_CUDA;
+    }
+    return MHD_OK;
+  }
+
+  int
+  build_graphs()
+  {
+    if (graph[0])
+      return MHD_OK;
+    for (int parity = 0; parity < 2; ++parity)
+    {
+      for (int pair = 0; pair < 2; ++pair)
+      {
+        cudaGraph_t g = nullptr;
+        MHD_CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_step(parity);
+        if (pair)
+          enqueue_step(1 - parity);
+        cudaError_t le = cudaGetLastError();
+        cudaError_t ce = cudaStreamEndCapture(stream, &g);
+        if (le != cudaSuccess || ce != cudaSuccess)
+        {
+          err = std::string("graph capture: ") +
+                cudaGetErrorString(le != cudaSuccess ? le : ce);
+          if (g)
+            cudaGraphDestroy(g);
+          return MHD_ERR_CUDA;
+        }
+        cudaGraphExec_t ex = nullptr;
+        cudaError_t     ie = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess)
+        {
+          err = std::string("graph instantiate: ") + cudaGetErrorString(ie);
+          return MHD_ERR_CUDA;
+        }
+        (pair ? graph_pair : graph)[parity] = ex;
+      }
+    }
+    return MHD_OK;
+  }
+
+  // boundaries + U2 = U + primitives + dt (SolverMHDMuscl.h:393-402)
+  int
+  apply_init()
+  {
+    launch_boundaries(U, 1);
+    MHD_CK(cudaMemcpyAsync(U2, U, (size_t)ncell * NV * sizeof(R), cudaMemcpyDeviceToDevice, stream));
+    launch_prim_dt(U, 1);
+    launch_finalize(1);
+    if (int rc = check_launch())
+      return rc;
+    MHD_CK(cudaStreamSynchronize(stream));
+    return MHD_OK;
+  }
+
+  int
+  upload(const void * host, R * dst, int layout)
+  {
+    const size_t bytes = (size_t)ncell * NV * sizeof(R);
+    if (layout == MHD_LAYOUT_LEFT)
+    {
+      MHD_CK(cudaMemcpyAsync(dst, host, bytes, cudaMemcpyHostToDevice, stream));
+    }
+    else
+    {
+      MHD_CK(cudaMemcpyAsync(Q, host, bytes, cudaMemcpyHostToDevice, stream));
+      k_transpose<R><<<nblocks(ncell * NV, 256), 256, 0, stream>>>(G, Q, dst, 0);
+      if (int rc = check_launch())
+        return rc;
+    }
+    return MHD_OK;
+  }
+
+  int
+  download(const R * src, void * host, int layout)
+  {
+    const size_t bytes = (size_t)ncell * NV * sizeof(R);
+    if (layout == MHD_LAYOUT_LEFT)
+    {
+      MHD_CK(cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, stream));
+    }
+    else
+    {
+      k_transpose<R><<<nblocks(ncell * NV, 256), 256, 0, stream>>>(G, src, Q, 1);
+      if (int rc = check_launch())
+        return rc;
+      MHD_CK(cudaMemcpyAsync(host, Q, bytes, cudaMemcpyDeviceToHost, stream));
+    }
+    return MHD_OK;
+  }
+
+  int
+  init_problem() override
+  {
+    std::vector<double> h((size_t)ncell * NV);
+    init_orszag_tang_host(P, h.data());
+    if constexpr (sizeof(R) == 8)
+    {
+      MHD_CK(cudaMemcpy(U, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    else
+    {
+      std::vector<float> f(h.size());
+      for (size_t q = 0; q < h.size(); ++q)
+        f[q] = (float)h[q];
+      MHD_CK(cudaMemcpy(U, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    MHD_CK(reset_time_state());
+    return apply_init();
+  }
+
+  int
+  set_state(const void * Uh, int layout) override
+  {
+    if (int rc = upload(Uh, U, layout))
+      return rc;
+    MHD_CK(reset_time_state());
+    return apply_init();
+  }
+
+  int
+  read_state()
+  {
+    MHD_CK(cudaMemcpyAsync(st_host, st, sizeof(DevState), cudaMemcpyDeviceToHost, stream));
+    MHD_CK(cudaStreamSynchronize(stream));
+    return MHD_OK;
+  }
+
+  R *
+  current()
+  {
+    return (st_host->it % 2 == 0) ? U : U2;
+  }
+
+  int
+  get_state(void * Uh, int layout) override
+  {
+    if (int rc = read_state())
+      return rc;
+    R * cur = current();
+    // ghost cells are refreshed from the current interior (idempotent: the
+    // next iteration starts with the same fill)
+    launch_boundaries(cur, 1);
+    if (int rc = check_launch())
+      return rc;
+    if (int rc = download(cur, Uh, layout))
+      return rc;
+    MHD_CK(cudaStreamSynchronize(stream));
+    return MHD_OK;
+  }
+
+  int
+  status_check()
+  {
+    if (st_host->status & STATUS_NUMERIC)
+    {
+      err = "non-finite or non-positive state detected (density, energy or CFL rate)";
+      return MHD_ERR_NUMERIC;
+    }
+    return MHD_OK;
+  }
+
+  int
+  step() override
+  {
+    enqueue_step((int)(launched & 1));
+    ++launched;
+    return check_launch();
+  }
+
+  int
+  run(int nsteps, int * done) override
+  {
+    if (int rc = build_graphs())
+      return rc;
+    if (int rc = read_state())
+      return rc;
+    const int it0 = st_host->it;
+    launched = it0;
+    int left = nsteps;
+    while (left >= 2)
+    {
+      MHD_CK(cudaGraphLaunch(graph_pair[launched & 1], stream));
+      launched += 2;
+      left -= 2;
+    }
+    if (left)
+    {
+      MHD_CK(cudaGraphLaunch(graph[launched & 1], stream));
+      launched += 1;
+    }
+    if (int rc = read_state())
+      return rc;
+    if (done)
+      *done = st_host->it - it0;
+    return status_check();
+  }
+
+  int
+  step_host(const void * Uin, void * Uout, int layout) override
+  {
+    if (int rc = read_state())
+      return rc;
+    launched = st_host->it;
+    R * cur = current();
+    if (int rc = upload(Uin, cur, layout))
+      return rc;
+    enqueue_step((int)(launched & 1));
+    ++launched;
+    if (int rc = check_launch())
+      return rc;
+    R * out = (launched & 1) ? U2 : U;
+    if (int rc = download(out, Uout, layout))
+      return rc;
+    if (int rc = read_state())
+      return rc;
+    return status_check();
+  }
+
+  int
+  time(double * t, double * dt, int * it) override
+  {
+    if (int rc = read_state())
+      return rc;
+    if (t)
+      *t = st_host->t;
+    if (dt)
+      *dt = st_host->dt;
+    if (it)
+      *it = st_host->it;
+    return MHD_OK;
+  }
+
+  int
+  diagnostics(double sums[8], double * divb_l1, double * divb_max) override
+  {
+    if (int rc = read_state())
+      return rc;
+    R * cur = current();
+    launch_boundaries(cur, 1);
+    if (dim == 2)
+      k_diag<R, 2><<<kDiagBlocks, 256, 0, stream>>>(G, cur, diag);
+    else
+      k_diag<R, 3><<<kDiagBlocks, 256, 0, stream>>>(G, cur, diag);
+    k_diag_final<<<1, 32, 0, stream>>>(diag, kDiagBlocks, diag + kDiagBlocks * 10);
+    if (int rc = check_launch())
+      return rc;
+    double out[10];
+    MHD_CK(cudaMemcpyAsync(out, diag + kDiagBlocks * 10, sizeof out, cudaMemcpyDeviceToHost, stream));
+    MHD_CK(cudaStreamSynchronize(stream));
+    for (int q = 0; q < 8; ++q)
+      sums[q] = out[q];
+    const double ncells = (double)G.nx * G.ny * (dim == 3 ? G.nz : 1);
+    if (divb_l1)
+      *divb_l1 = out[8] / ncells;
+    if (divb_max)
+      *divb_max = out[9];
+    return MHD_OK;
+  }
+
+  int
+  run_timed(int nsteps, float * ms) override
+  {
+    if (int rc = build_graphs())
+      return rc;
+    if (int rc = read_state())
+      return rc;
+    launched = st_host->it;
+    cudaEvent_t e0, e1;
+    MHD_CK(cudaEventCreate(&e0));
+    MHD_CK(cudaEventCreate(&e1));
+    MHD_CK(cudaEventRecord(e0, stream));
+    int left = nsteps;
+    while (left >= 2)
+    {
+      MHD_CK(cudaGraphLaunch(graph_pair[launched & 1], stream));
+      launched += 2;
+      left -= 2;
+    }
+    if (left)
+    {
+      MHD_CK(cudaGraphLaunch(graph[launched & 1], stream));
+      launched += 1;
+    }
+    MHD_CK(cudaEventRecord(e1, stream));
+    MHD_CK(cudaEventSynchronize(e1));
+    MHD_CK(cudaEventElapsedTime(ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (int rc = read_state())
+      return rc;
+    return status_check();
+  }
+
+  int
+  profile_step(const char ** names, float * ms, int max, int * count) override
+  {
+    static const char * kNames[kLaunches] = { "k_boundaries", "k_prim_dt", "k_finalize_dt",
+                                              "k_trace",      "k_flux",    "k_emf",
+                                              "k_update",     "k_advance" };
+    if (int rc = read_state())
+      return rc;
+    launched = st_host->it;
+    const Buffers<R> B = buffers((int)(launched & 1));
+    cudaEvent_t      ev[kLaunches + 1];
+    for (int q = 0; q <= kLaunches; ++q)
+      MHD_CK(cudaEventCreate(&ev[q]));
+    MHD_CK(cudaEventRecord(ev[0], stream));
+    launch_boundaries(B.Uin, 0);
+    MHD_CK(cudaEventRecord(ev[1], stream));
+    launch_prim_dt(B.Uin, 0);
+    MHD_CK(cudaEventRecord(ev[2], stream));
+    launch_finalize(0);
+    MHD_CK(cudaEventRecord(ev[3], stream));
+    launch_trace(B);
+    MHD_CK(cudaEventRecord(ev[4], stream));
+    launch_flux(B);
+    MHD_CK(cudaEventRecord(ev[5], stream));
+    launch_emf(B);
+    MHD_CK(cudaEventRecord(ev[6], stream));
+    launch_update(B);
+    MHD_CK(cudaEventRecord(ev[7], stream));
+    launch_advance();
+    MHD_CK(cudaEventRecord(ev[8], stream));
+    ++launched;
+    if (int rc = check_launch())
+      return rc;
+    MHD_CK(cudaEventSynchronize(ev[kLaunches]));
+    for (int q = 0; q < kLaunches && q < max; ++q)
+    {
+      if (names)
+        names[q] = kNames[q];
+      MHD_CK(cudaEventElapsedTime(&ms[q], ev[q], ev[q + 1]));
+    }
+    for (int q = 0; q <= kLaunches; ++q)
+      cudaEventDestroy(ev[q]);
+    if (count)
+      *count = kLaunches;
+    return MHD_OK;
+  }
+
+  int
+  cell_counts(int64_t * interior, int64_t * with_ghosts) override
+  {
+    if (interior)
+      *interior = (int64_t)G.nx * G.ny * (dim == 3 ? G.nz : 1);
+    if (with_ghosts)
+      *with_ghosts = (int64_t)G.isize * G.jsize * (dim == 3 ? G.ksize : 1);
+    return MHD_OK;
+  }
+
+  int
+  sizes(int s[4]) override
+  {
+    s[0] = G.isize;
+    s[1] = G.jsize;
+    s[2] = G.ksize;
+    s[3] = NV;
+    return MHD_OK;
+  }
+};
+
+#undef MHD_CK
+
+} // namespace MHD_VARIANT_TAG
+} // namespace mhd

@@ -1,0 +1,207 @@
+"""CUDA path (through the C ABI) against the reference and the CPU oracle.
+
+* MHD_FP_EXACT (FP64, no FMA contraction) must be BITWISE equal to the
+  reference's golden fixtures and to the oracle.
+* MHD_FP_FAST (FP64 with FMA contraction, the production build) must stay
+  within 1e-12 relative L1 per variable of the oracle after 100 steps of
+  2D Orszag-Tang 256^2 (the acceptance bound of the FP64 plain path).
+* FP32 storage/compute must stay within 1e-3 relative L1 of the FP64 oracle.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from mhd_cases import ot_ini, perturb
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+STEP_FILES = sorted(glob.glob(os.path.join(GOLDEN, "steps_*.npz")))
+
+TOL_FP64_FAST = 1e-12  # relative L1 per variable, FP64 with FMA contraction
+TOL_FP32 = 1e-3        # relative L1 per variable, FP32 storage and arithmetic
+
+
+def rel_l1(a, b):
+    ax = tuple(range(1, a.ndim))
+    return np.abs(a - b).sum(axis=ax) / np.maximum(np.abs(b).sum(axis=ax), 1e-300)
+
+
+def gpu_solver(mhdlib, ini, precision=64, exact=False):
+    return mhdlib.MHDSolver.from_ini(
+        ini, precision=precision, fp_mode=mhdlib.MHD_FP_EXACT if exact else mhdlib.MHD_FP_FAST)
+
+
+@pytest.mark.parametrize("path", STEP_FILES, ids=[os.path.basename(p)[6:-4] for p in STEP_FILES])
+def test_exact_matches_reference_golden_bitwise(mhdlib, path):
+    z = np.load(path)
+    s = gpu_solver(mhdlib, str(z["ini"]), exact=True)
+    if bool(z["perturbed"]):
+        s.set_state(z["U0"])
+    else:
+        s.init_problem()
+        assert np.array_equal(s.get_state(), z["U0"]), "initial condition differs"
+    t0, dt0, it0 = s.time()
+    assert (t0, dt0, it0) == (z["t"][0], z["dt"][0], 0)
+    assert s.run(1) == 1
+    assert np.array_equal(mhdlib.interior(s.get_state()), z["U1"])
+    s.run(int(z["nsteps"]) - 1)
+    assert np.array_equal(mhdlib.interior(s.get_state()), z["Un"])
+    t, dt, it = s.time()
+    assert (t, dt, it) == (z["t"][2], z["dt"][2], int(z["nsteps"]))
+
+
+@pytest.mark.parametrize("dim,kw,steps", [
+    (2, dict(nx=64, ny=48), 25),
+    (2, dict(nx=40, ny=33, riemann="hll", bc=(1, 1, 2, 2, 3, 3)), 15),
+    (3, dict(nx=24, ny=20, nz=16), 8),
+    (3, dict(nx=13, ny=17, nz=11, riemann="llf", bc=(2, 1, 3, 3, 1, 2)), 6),
+])
+def test_exact_matches_oracle_bitwise(mhdlib, oracle, dim, kw, steps):
+    ini = ot_ini(dim=dim, **kw)
+    o = oracle.OracleSolver(ini, nthreads=8)
+    U0 = perturb(o.get_state(), 3, amp=0.02)
+    o.set_state(U0)
+    s = gpu_solver(mhdlib, ini, exact=True)
+    s.set_state(U0)
+    o.run(steps)
+    s.run(steps)
+    assert np.array_equal(mhdlib.interior(s.get_state()), oracle.interior(o.get_state()))
+    assert s.time() == o.time()
+
+
+def test_fast_fp64_orszag_tang_2d_256_100_steps(mhdlib, oracle):
+    """The FP64 acceptance case: 2D OT 256^2, 100 steps, <= 1e-12 rel L1."""
+    ini = ot_ini(dim=2, nx=256, ny=256)
+    o = oracle.OracleSolver(ini, nthreads=16)
+    s = gpu_solver(mhdlib, ini)
+    s.init_problem()
+    o.run(100)
+    assert s.run(100) == 100
+    err = rel_l1(mhdlib.interior(s.get_state()), oracle.interior(o.get_state()))
+    assert err.max() <= TOL_FP64_FAST, err
+    t_g, _, it_g = s.time()
+    t_o, _, it_o = o.time()
+    assert it_g == it_o == 100
+    assert abs(t_g - t_o) <= 1e-12 * t_o
+    _, divb_l1, divb_max = s.diagnostics()
+    assert divb_max < 1e-10, divb_max
+
+
+def test_fast_fp64_orszag_tang_3d(mhdlib, oracle):
+    ini = ot_ini(dim=3, nx=32, ny=32, nz=32)
+    o = oracle.OracleSolver(ini, nthreads=16)
+    U0 = perturb(o.get_state(), 4, amp=0.01)
+    o.set_state(U0)
+    s = gpu_solver(mhdlib, ini)
+    s.set_state(U0)
+    o.run(20)
+    s.run(20)
+    err = rel_l1(mhdlib.interior(s.get_state()), oracle.interior(o.get_state()))
+    assert err.max() <= TOL_FP64_FAST, err
+
+
+@pytest.mark.parametrize("dim,n,steps", [(2, 128, 60), (3, 24, 15)])
+def test_fp32_against_fp64_oracle(mhdlib, oracle, dim, n, steps):
+    ini = ot_ini(dim=dim, nx=n, ny=n, nz=n)
+    o = oracle.OracleSolver(ini, nthreads=16)
+    s = gpu_solver(mhdlib, ini, precision=32)
+    s.init_problem()
+    o.run(steps)
+    s.run(steps)
+    err = rel_l1(mhdlib.interior(s.get_state()).astype(np.float64),
+                 oracle.interior(o.get_state()))
+    assert err.max() <= TOL_FP32, err
+
+
+def test_layout_right_roundtrip_and_equivalence(mhdlib, oracle):
+    ini = ot_ini(dim=3, nx=9, ny=7, nz=6)
+    o = oracle.OracleSolver(ini)
+    U0 = perturb(o.get_state(), 8)
+    a = gpu_solver(mhdlib, ini, exact=True)
+    b = gpu_solver(mhdlib, ini, exact=True)
+    a.set_state(U0, mhdlib.MHD_LAYOUT_LEFT)
+    b.set_state(np.ascontiguousarray(U0.T), mhdlib.MHD_LAYOUT_RIGHT)
+    a.run(3)
+    b.run(3)
+    UL = a.get_state(mhdlib.MHD_LAYOUT_LEFT)
+    UR = b.get_state(mhdlib.MHD_LAYOUT_RIGHT)
+    assert np.array_equal(UL, UR.T)
+
+
+def test_step_host_and_step_match_run(mhdlib):
+    ini = ot_ini(dim=2, nx=48, ny=40)
+    a = gpu_solver(mhdlib, ini, exact=True)
+    b = gpu_solver(mhdlib, ini, exact=True)
+    c = gpu_solver(mhdlib, ini, exact=True)
+    for s in (a, b, c):
+        s.init_problem()
+    a.run(6)
+    for _ in range(6):
+        b.step()
+    U = c.get_state()
+    out = np.empty_like(U)
+    for _ in range(6):
+        c.step_host(U, out)
+        U, out = out, U
+    Ua = mhdlib.interior(a.get_state())
+    assert np.array_equal(Ua, mhdlib.interior(b.get_state()))
+    assert np.array_equal(Ua, mhdlib.interior(U))
+    assert a.time() == b.time() == c.time()
+
+
+def test_stops_at_tend_like_the_reference(mhdlib, oracle):
+    """dt is clipped so the last step lands on tEnd; the loop then stops."""
+    ini = ot_ini(dim=2, nx=32, tend="0.05")
+    o = oracle.OracleSolver(ini)
+    s = gpu_solver(mhdlib, ini, exact=True)
+    s.init_problem()
+    n_o = o.run(1000)
+    n_g = s.run(1000)
+    assert n_g == n_o and 0 < n_g < 1000
+    assert s.time() == o.time()
+    assert s.run(10) == 0  # finished() holds
+
+
+def test_nstepmax_stops_the_loop(mhdlib):
+    s = gpu_solver(mhdlib, ot_ini(dim=2, nx=16, nstepmax=7))
+    s.init_problem()
+    assert s.run(20) == 7
+    assert s.time()[2] == 7
+
+
+def test_conservation_and_divergence(mhdlib):
+    """Periodic: mass, energy, momentum and field totals conserved; div B at round-off."""
+    s = gpu_solver(mhdlib, ot_ini(dim=3, nx=24, ny=24, nz=24))
+    s.init_problem()
+    m0, _, d0 = s.diagnostics()
+    s.run(20)
+    m1, l1, dmax = s.diagnostics()
+    assert abs(m1[0] - m0[0]) <= 1e-12 * abs(m0[0])
+    assert abs(m1[1] - m0[1]) <= 1e-12 * abs(m0[1])
+    scale = np.abs(mhdlib.interior(s.get_state())[5:8]).max() * 24
+    assert dmax <= 1e-12 * scale and d0 <= 1e-12 * scale
+
+
+def test_numeric_status_is_reported(mhdlib):
+    ini = ot_ini(dim=2, nx=16)
+    s = gpu_solver(mhdlib, ini)
+    s.init_problem()
+    U = s.get_state()
+    U[1, 8, 8] = np.nan  # corrupt the energy of one interior cell on the host
+    with pytest.raises(mhdlib.MHDError) as e:
+        s.set_state(U)
+        s.run(2)
+    assert e.value.code == mhdlib.MHD_ERR_NUMERIC
+
+
+def test_profile_and_counts(mhdlib):
+    s = gpu_solver(mhdlib, ot_ini(dim=3, nx=16))
+    s.init_problem()
+    prof = s.profile_step()
+    assert [n for n, _ in prof][:2] == ["k_boundaries", "k_prim_dt"]
+    assert all(ms >= 0 for _, ms in prof)
+    assert s.cell_counts() == (16 ** 3, 22 ** 3)
+    assert s.launches_per_step() == len(prof)
