@@ -37,6 +37,9 @@ WORKLOADS = {
     "ot3d_256_fp64": (3, 256, 64, "3D Orszag-Tang 256^3, FP64 plain MUSCL-Hancock+HLLD+CT"),
     "ot3d_256_fp32": (3, 256, 32, "3D Orszag-Tang 256^3, FP32 plain MUSCL-Hancock+HLLD+CT"),
     "ot2d_256_fp64": (2, 256, 64, "2D Orszag-Tang 256^2, FP64 plain MUSCL-Hancock+HLLD+CT"),
+    # reduced size for ncu captures (a few GB on the device, inputs still > L2)
+    "ot3d_128_fp64": (3, 128, 64, "3D Orszag-Tang 128^3, FP64 plain MUSCL-Hancock+HLLD+CT"),
+    "ot3d_128_fp32": (3, 128, 32, "3D Orszag-Tang 128^3, FP32 plain MUSCL-Hancock+HLLD+CT"),
 }
 
 
