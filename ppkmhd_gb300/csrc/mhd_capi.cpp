@@ -37,9 +37,14 @@ from_core(mhd_ctx * ctx, int rc)
   return rc;
 }
 
+} // namespace
+
+namespace mhd
+{
+
 // Empty string when the parameters can be run.
 std::string
-validate(const mhd_params & p)
+validate_params(const mhd_params & p)
 {
   if (p.dim != 2 && p.dim != 3)
     return "dim must be 2 or 3";
@@ -74,6 +79,11 @@ validate(const mhd_params & p)
   return "";
 }
 
+} // namespace mhd
+
+namespace
+{
+using mhd::validate_params;
 } // namespace
 
 namespace mhd
@@ -249,7 +259,7 @@ extern "C"
     if (!p || !out)
       return MHD_ERR_INVALID_ARG;
     *out = nullptr;
-    const std::string bad = validate(*p);
+    const std::string bad = validate_params(*p);
     mhd_ctx *         ctx = new (std::nothrow) mhd_ctx;
     if (!ctx)
       return MHD_ERR_CUDA;

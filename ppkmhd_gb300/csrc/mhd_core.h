@@ -39,6 +39,9 @@ SolverCore * create_core_f64x(const mhd_params & p, std::string & err);
 SolverCore * create_core_f64(const mhd_params & p, std::string & err);
 SolverCore * create_core_f32(const mhd_params & p, std::string & err);
 
+// Empty string when the parameters can be run, else the reason (mhd_capi.cpp).
+std::string validate_params(const mhd_params & p);
+
 // Orszag-Tang initial condition in FP64 on the host, LayoutLeft, ghosts
 // included (MHDInitFunctors2D.h:241-389, MHDInitFunctors3D.h:264-415).
 void init_orszag_tang_host(const mhd_params & p, double * U);
