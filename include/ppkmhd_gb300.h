@@ -173,6 +173,35 @@ int mhd_launches_per_step(mhd_ctx *ctx, int *n);
 const char *mhd_last_error(mhd_ctx *ctx);
 const char *mhd_version(void);
 
+/* Device scratch reserved by mhd_step_noalloc on every GPU that loads this
+ * library, for the process lifetime. */
+#define MHD_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+
+/*
+ * One iteration that allocates nothing.  This entry point has no counterpart
+ * in the reference; it is for callers that cannot call cudaMalloc (a host
+ * that owns all device memory through its own pool, a latency-bounded loop
+ * where an allocation may stall or fail, a job that must keep a fixed device
+ * footprint after start-up).
+ *
+ * U_in and U_out are the caller's DEVICE arrays (LayoutLeft, ghost cells
+ * included, real type per p->precision; U_in's ghost cells are refilled in
+ * place, as the reference's make_boundaries(data_in) does).  Every
+ * intermediate lives in a file-scope __device__ array of
+ * MHD_NOALLOC_SCRATCH_BYTES; grids that need more return MHD_ERR_TOO_LARGE
+ * (32 MiB holds about 300^2 interior cells in 2D or 35^3 in 3D in FP64, twice
+ * as many in FP32).  t is the current time (dt is clipped to p->tEnd; when
+ * t >= tEnd - 1e-14 nothing is computed and *dt = 0).  On return *dt holds
+ * the dt of the iteration; the call synchronises `stream` (a cudaStream_t,
+ * NULL for the legacy default stream).  Only MHD_FP_FAST is accepted.
+ * The first call on a device looks up the scratch array's device address
+ * (cudaGetSymbolAddress); make it before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race and must be serialised.
+ * Errors are reported by the status code only (no context exists).
+ */
+int mhd_step_noalloc(const mhd_params *p, const void *U_in, void *U_out, double t, double *dt,
+                     void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -97,6 +97,8 @@ SIGNATURES = {
     "mhd_launches_per_step": (ctypes.c_int, [_vp, _ip]),
     "mhd_last_error": (ctypes.c_char_p, [_vp]),
     "mhd_version": (ctypes.c_char_p, []),
+    "mhd_step_noalloc": (ctypes.c_int, [ctypes.POINTER(MHDParams), _vp, _vp, ctypes.c_double,
+                                        _dp, _vp]),
 }
 
 _lib = None

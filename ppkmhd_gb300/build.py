@@ -93,6 +93,10 @@ def build(jobs: int | None = None, force: bool = False, verbose: bool = False) -
         cmds.append([nvcc(), *GENCODE, *NVCC_COMMON, f"--fmad={fmad}", "-Xptxas", "-v",
                      f"-DMHD_VARIANT_TAG={tag}", f"-DMHD_REAL={real}", f"-DMHD_FACTORY={factory}",
                      "-c", os.path.join(CSRC, "mhd_variant.cu"), "-o", o])
+    o = os.path.join(OBJ, "mhd_noalloc.o")
+    objs.append(o)
+    cmds.append([nvcc(), *GENCODE, *NVCC_COMMON, "--fmad=true", "-Xptxas", "-v",
+                 "-c", os.path.join(CSRC, "mhd_noalloc.cu"), "-o", o])
     o = os.path.join(OBJ, "mhd_capi.o")
     objs.append(o)
     cmds.append(["g++", *CXX_COMMON, "-c", os.path.join(CSRC, "mhd_capi.cpp"), "-o", o])
