@@ -60,6 +60,7 @@ struct Grid
   int     riemann;
   R       gamma0, smallr, smallp, smallc, slope_type;
   double  cfl, dx, dy, dz;
+  double  idx, idy, idz; // 1/dx, 1/dy, 1/dz (used by the fast builds only)
 };
 
 template <class R>
@@ -232,15 +233,27 @@ k_prim_dt(const Grid<R> G, const R * __restrict__ U, R * __restrict__ Q, DevStat
     const R       nby = U[c + G.sj + IB * sv];
     const R       nbz = DIM == 3 ? U[c + G.sk + IC * sv] : R(0);
     const R       d = fmax(U[c + ID * sv], G.smallr);
-    const R       vu = U[c + IU * sv] / d;
-    const R       vv = U[c + IV * sv] / d;
-    const R       vw = U[c + IW * sv] / d;
+    R             vu, vv, vw;
+    const R       invd = kExactOrder ? R(0) : rcp(d);
+    if constexpr (kExactOrder)
+    {
+      vu = U[c + IU * sv] / d;
+      vv = U[c + IV * sv] / d;
+      vw = U[c + IW * sv] / d;
+    }
+    else
+    {
+      vu = U[c + IU * sv] * invd;
+      vv = U[c + IV * sv] * invd;
+      vw = U[c + IW * sv] * invd;
+    }
     const R       a = R(0.5) * (U[c + IA * sv] + nbx);
     const R       bb = R(0.5) * (U[c + IB * sv] + nby);
     const R       cc = R(0.5) * (U[c + IC * sv] + nbz);
     const R       eken = R(0.5) * (vu * vu + vv * vv + vw * vw);
     const R       emag = R(0.5) * (a * a + bb * bb + cc * cc);
-    const R       eint = (U[c + IP * sv] - emag) / d - eken;
+    const R       eint = kExactOrder ? (U[c + IP * sv] - emag) / d - eken
+                                     : (U[c + IP * sv] - emag) * invd - eken;
     const R       p = fmax((G.gamma0 - R(1)) * d * eint, d * G.smallp);
     Q[c + ID * sv] = d;
     Q[c + IP * sv] = p;
@@ -257,18 +270,36 @@ k_prim_dt(const Grid<R> G, const R * __restrict__ U, R * __restrict__ Q, DevStat
     {
       // find_speed_info<NDIM> (mhd_utils.h:319-366)
       const R b2 = a * a + bb * bb + cc * cc;
-      const R c2 = G.gamma0 * p / d;
-      const R d2 = R(0.5) * (b2 / d + c2);
-      const R sx = sqrt(d2 + sqrt(d2 * d2 - c2 * a * a / d)) + fabs(vu);
-      const R sy = sqrt(d2 + sqrt(d2 * d2 - c2 * bb * bb / d)) + fabs(vv);
       R       val;
-      if constexpr (DIM == 3)
+      if constexpr (kExactOrder)
       {
-        const R sz = sqrt(d2 + sqrt(d2 * d2 - c2 * cc * cc / d)) + fabs(vw);
-        val = sx / R(G.dx) + sy / R(G.dy) + sz / R(G.dz);
+        const R c2 = G.gamma0 * p / d;
+        const R d2 = R(0.5) * (b2 / d + c2);
+        const R sx = sqrt(d2 + sqrt(d2 * d2 - c2 * a * a / d)) + fabs(vu);
+        const R sy = sqrt(d2 + sqrt(d2 * d2 - c2 * bb * bb / d)) + fabs(vv);
+        if constexpr (DIM == 3)
+        {
+          const R sz = sqrt(d2 + sqrt(d2 * d2 - c2 * cc * cc / d)) + fabs(vw);
+          val = sx / R(G.dx) + sy / R(G.dy) + sz / R(G.dz);
+        }
+        else
+          val = sx / R(G.dx) + sy / R(G.dy);
       }
       else
-        val = sx / R(G.dx) + sy / R(G.dy);
+      {
+        const R c2 = G.gamma0 * p * invd;
+        const R d2 = R(0.5) * (b2 * invd + c2);
+        const R cd = c2 * invd;
+        const R sx = sqrt(d2 + sqrt(d2 * d2 - cd * a * a)) + fabs(vu);
+        const R sy = sqrt(d2 + sqrt(d2 * d2 - cd * bb * bb)) + fabs(vv);
+        if constexpr (DIM == 3)
+        {
+          const R sz = sqrt(d2 + sqrt(d2 * d2 - cd * cc * cc)) + fabs(vw);
+          val = sx * R(G.idx) + sy * R(G.idy) + sz * R(G.idz);
+        }
+        else
+          val = sx * R(G.idx) + sy * R(G.idy);
+      }
       // fmax in the reference ignores NaN operands; a NaN rate is dropped
       rate = (val >= R(0)) ? (double)val : 0.0;
       const R Ein = U[c + IP * sv];
@@ -428,7 +459,42 @@ k_trace(const Grid<R> G, Buffers<R> B)
           dAy = s[1][IA], dCy = s[1][IC];
   const R dAx = s[0][IA], dBy = s[1][IB];
   R       sr0, su0, sv0, sw0, sp0, sA0, sB0, sC0;
-  if constexpr (DIM == 2)
+  if constexpr (!kExactOrder)
+  {
+    // same source terms with one reciprocal of the density
+    const R ir = rcp(r);
+    if constexpr (DIM == 2)
+    {
+      sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy;
+      su0 = (-u * dux - (dpx + Bc * dBx + C * dCx) * ir) * dtdx + (-v * duy + Bc * dAy * ir) * dtdy;
+      sv0 = (-u * dvx + A * dBx * ir) * dtdx + (-v * dvy - (dpy + A * dAy + C * dCy) * ir) * dtdy;
+      sw0 = (-u * dwx + A * dCx * ir) * dtdx + (-v * dwy + Bc * dCy * ir) * dtdy;
+      sp0 = (-u * dpx - dux * gamma * p) * dtdx + (-v * dpy - dvy * gamma * p) * dtdy;
+      sA0 = (u * dBy + Bc * duy - v * dAy - A * dvy) * dtdy;
+      sB0 = (-u * dBx - Bc * dux + v * dAx + A * dvx) * dtdx;
+      sC0 = (w * dAx + A * dwx - u * dCx - C * dux) * dtdx +
+            (-v * dCy - C * dvy + w * dBy + Bc * dwy) * dtdy;
+    }
+    else
+    {
+      const R drz = s[DIM - 1][ID], dpz = s[DIM - 1][IP], duz = s[DIM - 1][IU],
+              dvz = s[DIM - 1][IV], dwz = s[DIM - 1][IW], dAz = s[DIM - 1][IA],
+              dBz = s[DIM - 1][IB], dCz = s[DIM - 1][IC];
+      sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy + (-w * drz - dwz * r) * dtdz;
+      su0 = (-u * dux - (dpx + Bc * dBx + C * dCx) * ir) * dtdx + (-v * duy + Bc * dAy * ir) * dtdy +
+            (-w * duz + C * dAz * ir) * dtdz;
+      sv0 = (-u * dvx + A * dBx * ir) * dtdx + (-v * dvy - (dpy + A * dAy + C * dCy) * ir) * dtdy +
+            (-w * dvz + C * dBz * ir) * dtdz;
+      sw0 = (-u * dwx + A * dCx * ir) * dtdx + (-v * dwy + Bc * dCy * ir) * dtdy +
+            (-w * dwz - (dpz + A * dAz + Bc * dBz) * ir) * dtdz;
+      sp0 = (-u * dpx - dux * gamma * p) * dtdx + (-v * dpy - dvy * gamma * p) * dtdy +
+            (-w * dpz - dwz * gamma * p) * dtdz;
+      sA0 = (u * dBy + Bc * duy - v * dAy - A * dvy) * dtdy + (u * dCz + C * duz - w * dAz - A * dwz) * dtdz;
+      sB0 = (v * dAx + A * dvx - u * dBx - Bc * dux) * dtdx + (v * dCz + C * dvz - w * dBz - Bc * dwz) * dtdz;
+      sC0 = (w * dAx + A * dwx - u * dCx - C * dux) * dtdx + (w * dBy + Bc * dwy - v * dCy - C * dvy) * dtdy;
+    }
+  }
+  else if constexpr (DIM == 2)
   {
     sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy;
     su0 = (-u * dux - dpx / r - Bc * dBx / r - C * dCx / r) * dtdx + (-v * duy + Bc * dAy / r) * dtdy;

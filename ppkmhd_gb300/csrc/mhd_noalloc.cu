@@ -127,6 +127,9 @@ step(const mhd_params & p, const void * U_in, void * U_out, double t, double * d
   G.dx = (double)R(R(p.xmax - p.xmin) / R(p.nx));
   G.dy = (double)R(R(p.ymax - p.ymin) / R(p.ny));
   G.dz = p.dim == 3 ? (double)R(R(p.zmax - p.zmin) / R(p.nz)) : 1.0;
+  G.idx = 1.0 / G.dx;
+  G.idy = 1.0 / G.dy;
+  G.idz = 1.0 / G.dz;
 
   const int     dim = p.dim;
   const size_t  n = (size_t)G.sv;

@@ -63,6 +63,52 @@ swap_vals(R & a, R & b)
   b = t;
 }
 
+// MHD_EXACT_BUILD = 1 (the FMA-free FP64 build) evaluates every expression in
+// the reference's operation order.  The other builds use algebraically equal
+// forms with fewer divides and square roots (shared reciprocals, rsqrt for
+// |B|/sqrt(rho)); they differ from the reference at round-off level only.
+#ifndef MHD_EXACT_BUILD
+#  define MHD_EXACT_BUILD 0
+#endif
+constexpr bool kExactOrder = MHD_EXACT_BUILD != 0;
+
+__device__ __forceinline__ double
+rcp(double x)
+{
+  return __drcp_rn(x);
+}
+__device__ __forceinline__ float
+rcp(float x)
+{
+  return __frcp_rn(x);
+}
+__device__ __forceinline__ double
+rsq(double x)
+{
+  return rsqrt(x);
+}
+__device__ __forceinline__ float
+rsq(float x)
+{
+  return rsqrtf(x);
+}
+
+// Both fast magnetosonic speeds (normal field in slot IA, then in slot IB)
+// of one state with one reciprocal of the density (mhd_utils.h:89-117).
+template <class R>
+__device__ __forceinline__ void
+fast_speeds_xy(const State<R> & q, R gamma0, R & cfx, R & cfy)
+{
+  const R invd = rcp(q[ID]);
+  const R a = q[IA], b = q[IB], c = q[IC];
+  const R b2 = a * a + b * b + c * c;
+  const R c2 = gamma0 * q[IP] * invd;
+  const R d2 = R(0.5) * (b2 * invd + c2);
+  const R cd = c2 * invd;
+  cfx = sqrt(d2 + sqrt(d2 * d2 - cd * a * a));
+  cfy = sqrt(d2 + sqrt(d2 * d2 - cd * b * b));
+}
+
 // Fast magnetosonic speed with the normal field in slot IA
 // (find_speed_fast<IX>, mhd_utils.h:89-117).
 template <class R>
@@ -342,13 +388,174 @@ riemann_hlld(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
   flux[IC] = co * uo - a * wo;
 }
 
+// HLLD, same states and sampling as riemann_hlld, with 8 reciprocals, 4
+// square roots and 2 rsqrt instead of ~28 divides and 6 square roots.
+template <class R>
+__device__ void
+riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
+{
+  const R entho = rcp(gamma0 - R(1));
+  const R a = R(0.5) * (ql[IA] + qr[IA]);
+  const R a2 = a * a;
+  const R sgnm = (a >= R(0)) ? R(1) : R(-1);
+
+  const R rl = ql[ID], pl = ql[IP], ul = ql[IU], vl = ql[IV], wl = ql[IW], bl = ql[IB],
+          cl = ql[IC];
+  const R b2l = a2 + bl * bl + cl * cl;
+  const R emagl = R(0.5) * b2l;
+  const R etotl = pl * entho + R(0.5) * (ul * ul + vl * vl + wl * wl) * rl + emagl;
+  const R ptotl = pl + emagl;
+  const R vdotbl = ul * a + vl * bl + wl * cl;
+
+  const R rr = qr[ID], pr = qr[IP], ur = qr[IU], vr = qr[IV], wr = qr[IW], br = qr[IB],
+          cr = qr[IC];
+  const R b2r = a2 + br * br + cr * cr;
+  const R emagr = R(0.5) * b2r;
+  const R etotr = pr * entho + R(0.5) * (ur * ur + vr * vr + wr * wr) * rr + emagr;
+  const R ptotr = pr + emagr;
+  const R vdotbr = ur * a + vr * br + wr * cr;
+
+  R cfastl, cfastr;
+  {
+    const R id = rcp(rl);
+    const R c2 = gamma0 * pl * id;
+    const R d2 = R(0.5) * (b2l * id + c2);
+    cfastl = sqrt(d2 + sqrt(d2 * d2 - c2 * a2 * id));
+  }
+  {
+    const R id = rcp(rr);
+    const R c2 = gamma0 * pr * id;
+    const R d2 = R(0.5) * (b2r * id + c2);
+    cfastr = sqrt(d2 + sqrt(d2 * d2 - c2 * a2 * id));
+  }
+  const R cmax = fmax(cfastl, cfastr);
+  const R sl = fmin(ul, ur) - cmax;
+  const R sr = fmax(ul, ur) + cmax;
+  const R rcl = rl * (ul - sl);
+  const R rcr = rr * (sr - ur);
+  const R irc = rcp(rcr + rcl);
+  const R ustar = (rcr * ur + rcl * ul + (ptotl - ptotr)) * irc;
+  const R ptotstar = (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) * irc;
+
+  // left star state
+  const R slu = sl - ul, sls = sl - ustar;
+  const R isls = rcp(sls);
+  const R rstarl = rl * slu * isls;
+  R       vstarl = vl, wstarl = wl, bstarl = bl, cstarl = cl;
+  {
+    const R estar = rl * slu * sls - a2;
+    if (!(a2 > R(0) && fabs(estar - a2) <= R(1e-8) * a2))
+    {
+      const R ie = rcp(estar);
+      const R el = rl * slu * slu - a2;
+      const R tv = a * (ustar - ul) * ie;
+      vstarl = vl - bl * tv;
+      wstarl = wl - cl * tv;
+      const R fe = el * ie;
+      bstarl = bl * fe;
+      cstarl = cl * fe;
+    }
+  }
+  const R vdotbstarl = ustar * a + vstarl * bstarl + wstarl * cstarl;
+  const R etotstarl = (slu * etotl - ptotl * ul + ptotstar * ustar + a * (vdotbl - vdotbstarl)) * isls;
+  const R rsl = rsq(rstarl);
+  const R sqrrstarl = rstarl * rsl;
+  const R sal = ustar - fabs(a) * rsl;
+
+  // right star state
+  const R sru = sr - ur, srs = sr - ustar;
+  const R isrs = rcp(srs);
+  const R rstarr = rr * sru * isrs;
+  R       vstarr = vr, wstarr = wr, bstarr = br, cstarr = cr;
+  {
+    const R estar = rr * sru * srs - a2;
+    if (!(a2 > R(0) && fabs(estar - a2) <= R(1e-8) * a2))
+    {
+      const R ie = rcp(estar);
+      const R er = rr * sru * sru - a2;
+      const R tv = a * (ustar - ur) * ie;
+      vstarr = vr - br * tv;
+      wstarr = wr - cr * tv;
+      const R fe = er * ie;
+      bstarr = br * fe;
+      cstarr = cr * fe;
+    }
+  }
+  const R vdotbstarr = ustar * a + vstarr * bstarr + wstarr * cstarr;
+  const R etotstarr = (sru * etotr - ptotr * ur + ptotstar * ustar + a * (vdotbr - vdotbstarr)) * isrs;
+  const R rsr = rsq(rstarr);
+  const R sqrrstarr = rstarr * rsr;
+  const R sar = ustar + fabs(a) * rsr;
+
+  R ro, uo, vo, wo, bo, co, ptoto, etoto, vdotbo;
+  if (sl > R(0))
+  {
+    ro = rl; uo = ul; vo = vl; wo = wl; bo = bl; co = cl;
+    ptoto = ptotl; etoto = etotl; vdotbo = vdotbl;
+  }
+  else if (sal > R(0))
+  {
+    ro = rstarl; uo = ustar; vo = vstarl; wo = wstarl; bo = bstarl; co = cstarl;
+    ptoto = ptotstar; etoto = etotstarl; vdotbo = vdotbstarl;
+  }
+  else if (!(ustar > R(0)) && !(sar > R(0)))
+  {
+    if (sr > R(0))
+    {
+      ro = rstarr; uo = ustar; vo = vstarr; wo = wstarr; bo = bstarr; co = cstarr;
+      ptoto = ptotstar; etoto = etotstarr; vdotbo = vdotbstarr;
+    }
+    else
+    {
+      ro = rr; uo = ur; vo = vr; wo = wr; bo = br; co = cr;
+      ptoto = ptotr; etoto = etotr; vdotbo = vdotbr;
+    }
+  }
+  else
+  {
+    const R is = rcp(sqrrstarl + sqrrstarr);
+    const R sq = sgnm * sqrrstarl * sqrrstarr;
+    vo = (sqrrstarl * vstarl + sqrrstarr * vstarr + sgnm * (bstarr - bstarl)) * is;
+    wo = (sqrrstarl * wstarl + sqrrstarr * wstarr + sgnm * (cstarr - cstarl)) * is;
+    bo = (sqrrstarl * bstarr + sqrrstarr * bstarl + sq * (vstarr - vstarl)) * is;
+    co = (sqrrstarl * cstarr + sqrrstarr * cstarl + sq * (wstarr - wstarl)) * is;
+    uo = ustar;
+    ptoto = ptotstar;
+    vdotbo = ustar * a + vo * bo + wo * co;
+    if (ustar > R(0))
+    {
+      ro = rstarl;
+      etoto = etotstarl - sgnm * sqrrstarl * (vdotbstarl - vdotbo);
+    }
+    else
+    {
+      ro = rstarr;
+      etoto = etotstarr + sgnm * sqrrstarr * (vdotbstarr - vdotbo);
+    }
+  }
+  const R rou = ro * uo;
+  flux[ID] = rou;
+  flux[IP] = (etoto + ptoto) * uo - a * vdotbo;
+  flux[IU] = rou * uo - a2 + ptoto;
+  flux[IV] = rou * vo - a * bo;
+  flux[IW] = rou * wo - a * co;
+  flux[IA] = R(0);
+  flux[IB] = bo * uo - a * vo;
+  flux[IC] = co * uo - a * wo;
+}
+
 // riemann_mhd dispatch (RiemannSolvers_MHD.h:372-392)
 template <class R>
 __device__ __forceinline__ void
 riemann(int solver, State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
 {
   if (solver == RIEMANN_HLLD)
-    riemann_hlld(ql, qr, flux, gamma0);
+  {
+    if constexpr (kExactOrder)
+      riemann_hlld(ql, qr, flux, gamma0);
+    else
+      riemann_hlld_fast(ql, qr, flux, gamma0);
+  }
   else if (solver == RIEMANN_HLL)
     riemann_hll(ql, qr, flux, gamma0);
   else
@@ -525,6 +732,111 @@ mag_riemann2d_hlld(const State<R> (&q)[4], const R (&e)[4], R gamma0, R smallc)
          SAT * SAB / (SAT - SAB) * (AstarT - AstarB) + SAR * SAL / (SAR - SAL) * (BstarR - BstarL);
 }
 
+// The same 2D HLLD solve with shared reciprocals: 12 reciprocals, 16 square
+// roots and 16 rsqrt instead of ~75 divides and 32 square roots.
+template <class R>
+__device__ R
+mag_riemann2d_hlld_fast(const State<R> (&q)[4], const R (&e)[4], R gamma0, R smallc)
+{
+  const State<R> &qLL = q[0], &qRL = q[1], &qLR = q[2], &qRR = q[3];
+  R               cFastLLx, cFastLLy, cFastLRx, cFastLRy, cFastRLx, cFastRLy, cFastRRx, cFastRRy;
+  fast_speeds_xy(qLL, gamma0, cFastLLx, cFastLLy);
+  fast_speeds_xy(qLR, gamma0, cFastLRx, cFastLRy);
+  fast_speeds_xy(qRL, gamma0, cFastRLx, cFastRLy);
+  fast_speeds_xy(qRR, gamma0, cFastRRx, cFastRRy);
+  const R uLL = qLL[IU], uLR = qLR[IU], uRL = qRL[IU], uRR = qRR[IU];
+  const R vLL = qLL[IV], vLR = qLR[IV], vRL = qRL[IV], vRR = qRR[IV];
+  const R cxm = max4(cFastLLx, cFastLRx, cFastRLx, cFastRRx);
+  const R cym = max4(cFastLLy, cFastLRy, cFastRLy, cFastRRy);
+  const R SL = min4(uLL, uLR, uRL, uRR) - cxm;
+  const R SR = max4(uLL, uLR, uRL, uRR) + cxm;
+  const R SB = min4(vLL, vLR, vRL, vRR) - cym;
+  const R ST = max4(vLL, vLR, vRL, vRR) + cym;
+  const bool SB_pos = !signbit(SB), ST_pos = !signbit(ST);
+  const bool SL_pos = !signbit(SL), SR_pos = !signbit(SR);
+  if (SB_pos && SL_pos)
+    return e[0];
+  if (SB_pos && !SR_pos)
+    return e[1];
+  if (!SB_pos && !ST_pos && SL_pos)
+    return e[2];
+  if (!SB_pos && !ST_pos && !SR_pos)
+    return e[3];
+
+  const R rLL = qLL[ID], rLR = qLR[ID], rRL = qRL[ID], rRR = qRR[ID];
+  const R aLL = qLL[IA], aLR = qLR[IA], aRL = qRL[IA], aRR = qRR[IA];
+  const R bLL = qLL[IB], bLR = qLR[IB], bRL = qRL[IB], bRR = qRR[IB];
+  const R PtotLL = qLL[IP] + R(0.5) * (aLL * aLL + bLL * bLL + qLL[IC] * qLL[IC]);
+  const R PtotLR = qLR[IP] + R(0.5) * (aLR * aLR + bLR * bLR + qLR[IC] * qLR[IC]);
+  const R PtotRL = qRL[IP] + R(0.5) * (aRL * aRL + bRL * bRL + qRL[IC] * qRL[IC]);
+  const R PtotRR = qRR[IP] + R(0.5) * (aRR * aRR + bRR * bRR + qRR[IC] * qRR[IC]);
+
+  const R rcLLx = rLL * (uLL - SL), rcRLx = rRL * (SR - uRL);
+  const R rcLRx = rLR * (uLR - SL), rcRRx = rRR * (SR - uRR);
+  const R rcLLy = rLL * (vLL - SB), rcLRy = rLR * (ST - vLR);
+  const R rcRLy = rRL * (vRL - SB), rcRRy = rRR * (ST - vRR);
+  const R ustar = (rcLLx * uLL + rcLRx * uLR + rcRLx * uRL + rcRRx * uRR +
+                   (PtotLL - PtotRL + PtotLR - PtotRR)) *
+                  rcp(rcLLx + rcLRx + rcRLx + rcRRx);
+  const R vstar = (rcLLy * vLL + rcLRy * vLR + rcRLy * vRL + rcRRy * vRR +
+                   (PtotLL - PtotLR + PtotRL - PtotRR)) *
+                  rcp(rcLLy + rcLRy + rcRLy + rcRRy);
+
+  const R iL = rcp(SL - ustar), iR = rcp(SR - ustar);
+  const R iB = rcp(SB - vstar), iT = rcp(ST - vstar);
+  // x and y compression factors of each corner state
+  const R fLLx = (SL - uLL) * iL, fLRx = (SL - uLR) * iL, fRLx = (SR - uRL) * iR, fRRx = (SR - uRR) * iR;
+  const R fLLy = (SB - vLL) * iB, fRLy = (SB - vRL) * iB, fLRy = (ST - vLR) * iT, fRRy = (ST - vRR) * iT;
+
+  const R rstarLLx = rLL * fLLx, BstarLL = bLL * fLLx, rstarLLy = rLL * fLLy, AstarLL = aLL * fLLy;
+  const R rstarLL = rstarLLx * fLLy;
+  const R rstarLRx = rLR * fLRx, BstarLR = bLR * fLRx, rstarLRy = rLR * fLRy, AstarLR = aLR * fLRy;
+  const R rstarLR = rstarLRx * fLRy;
+  const R rstarRLx = rRL * fRLx, BstarRL = bRL * fRLx, rstarRLy = rRL * fRLy, AstarRL = aRL * fRLy;
+  const R rstarRL = rstarRLx * fRLy;
+  const R rstarRRx = rRR * fRRx, BstarRR = bRR * fRRx, rstarRRy = rRR * fRRy, AstarRR = aRR * fRRy;
+  const R rstarRR = rstarRRx * fRRy;
+
+  const R calfvenL = max5(fabs(aLR) * rsq(rstarLRx), fabs(AstarLR) * rsq(rstarLR),
+                          fabs(aLL) * rsq(rstarLLx), fabs(AstarLL) * rsq(rstarLL), smallc);
+  const R calfvenR = max5(fabs(aRR) * rsq(rstarRRx), fabs(AstarRR) * rsq(rstarRR),
+                          fabs(aRL) * rsq(rstarRLx), fabs(AstarRL) * rsq(rstarRL), smallc);
+  const R calfvenB = max5(fabs(bLL) * rsq(rstarLLy), fabs(BstarLL) * rsq(rstarLL),
+                          fabs(bRL) * rsq(rstarRLy), fabs(BstarRL) * rsq(rstarRL), smallc);
+  const R calfvenT = max5(fabs(bLR) * rsq(rstarLRy), fabs(BstarLR) * rsq(rstarLR),
+                          fabs(bRR) * rsq(rstarRRy), fabs(BstarRR) * rsq(rstarRR), smallc);
+  const R SAL = fmin(ustar - calfvenL, R(0));
+  const R SAR = fmax(ustar + calfvenR, R(0));
+  const R SAB = fmin(vstar - calfvenB, R(0));
+  const R SAT = fmax(vstar + calfvenT, R(0));
+  const R iLR = rcp(SAR - SAL), iBT = rcp(SAT - SAB);
+
+  if (SB_pos)
+    return (SAR * (ustar * BstarLL - vLL * aLL) - SAL * (ustar * BstarRL - vRL * aRL) +
+            SAR * SAL * (bRL - bLL)) * iLR;
+  if (!ST_pos)
+    return (SAR * (ustar * BstarLR - vLR * aLR) - SAL * (ustar * BstarRR - vRR * aRR) +
+            SAR * SAL * (bRR - bLR)) * iLR;
+  if (SL_pos)
+    return (SAT * (uLL * bLL - vstar * AstarLL) - SAB * (uLR * bLR - vstar * AstarLR) -
+            SAT * SAB * (aLR - aLL)) * iBT;
+  if (!SR_pos)
+    return (SAT * (uRL * bRL - vstar * AstarRL) - SAB * (uRR * bRR - vstar * AstarRR) -
+            SAT * SAB * (aRR - aRL)) * iBT;
+
+  const R EstarLL = ustar * BstarLL - vstar * AstarLL;
+  const R EstarLR = ustar * BstarLR - vstar * AstarLR;
+  const R EstarRL = ustar * BstarRL - vstar * AstarRL;
+  const R EstarRR = ustar * BstarRR - vstar * AstarRR;
+  const R AstarT = (SAR * AstarRR - SAL * AstarLR) * iLR;
+  const R AstarB = (SAR * AstarRL - SAL * AstarLL) * iLR;
+  const R BstarR = (SAT * BstarRR - SAB * BstarRL) * iBT;
+  const R BstarL = (SAT * BstarLR - SAB * BstarLL) * iBT;
+  return (SAL * SAB * EstarRR - SAL * SAT * EstarRL - SAR * SAB * EstarLR + SAR * SAT * EstarLL) *
+           iLR * iBT -
+         SAT * SAB * iBT * (AstarT - AstarB) + SAR * SAL * iLR * (BstarR - BstarL);
+}
+
 // compute_emf<EmfDir> (RiemannSolvers_MHD.h:651-874): rotate the four
 // reconstructed edge states (RT, RB, LT, LB) into the 2D frame of the edge,
 // average the parallel field components and call the 2D solver.
@@ -566,7 +878,10 @@ compute_emf(int edir, const State<R> (&qe)[4], R gamma0, R smallc)
 #pragma unroll
   for (int c = 0; c < 4; ++c)
     e[c] = q[c][IU] * q[c][IB] - q[c][IV] * q[c][IA];
-  return mag_riemann2d_hlld(q, e, gamma0, smallc);
+  if constexpr (kExactOrder)
+    return mag_riemann2d_hlld(q, e, gamma0, smallc);
+  else
+    return mag_riemann2d_hlld_fast(q, e, gamma0, smallc);
 }
 
 } // namespace MHD_VARIANT_TAG
