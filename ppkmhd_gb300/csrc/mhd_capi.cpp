@@ -64,6 +64,10 @@ validate_params(const mhd_params & p)
     if (p.boundary[f] != MHD_BC_REFLECTING && p.boundary[f] != MHD_BC_OUTFLOW &&
         p.boundary[f] != MHD_BC_PERIODIC)
       return "boundary types must be 1 (reflecting), 2 (outflow) or 3 (periodic)";
+  // slope_unsplit_hydro_2d/3d compute slopes only for slope_type 1 or 2
+  // (MHDBaseFunctor2D.h:464-466, MHDBaseFunctor3D.h:525-526)
+  if (p.slope_type != 1.0 && p.slope_type != 2.0)
+    return "slope_type must be 1 (minmod) or 2 (monotonized central)";
   if (!(p.gamma0 > 1.0) || !(p.cfl > 0.0) || !(p.smallr > 0.0) || !(p.smallc > 0.0))
     return "gamma0 must be > 1 and cfl, smallr, smallc > 0";
   if (!(p.xmax > p.xmin) || !(p.ymax > p.ymin) || (p.dim == 3 && !(p.zmax > p.zmin)))

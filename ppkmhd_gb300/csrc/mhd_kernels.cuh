@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include "mhd_physics.cuh"
+#include "ppkmhd_gb300.h"
 
 #ifndef MHD_VARIANT_TAG
 #  define MHD_VARIANT_TAG v_default
@@ -43,25 +44,31 @@ struct DevState
   int                it, nStepmax;
   int                status; // bit 0: non-finite or non-positive state seen
   int                pad;
+  float              fdtdx, fdtdy, fdtdz; // dt/dx... rounded once for the FP32 kernels
+  float              fpad;
 };
+
+// dt/dx, dt/dy, dt/dz in the working precision
+__device__ __forceinline__ void
+dt_over_dx(const DevState * st, double & x, double & y, double & z)
+{
+  x = st->dtdx;
+  y = st->dtdy;
+  z = st->dtdz;
+}
+__device__ __forceinline__ void
+dt_over_dx(const DevState * st, float & x, float & y, float & z)
+{
+  x = st->fdtdx;
+  y = st->fdtdy;
+  z = st->fdtdz;
+}
 
 enum : int
 {
   STATUS_NUMERIC = 1
 };
 
-template <class R>
-struct Grid
-{
-  int     dim, nx, ny, nz, g;
-  int     isize, jsize, ksize;
-  int64_t sj, sk, sv; // strides of j, k and var (i stride is 1)
-  int     bc[6];
-  int     riemann;
-  R       gamma0, smallr, smallp, smallc, slope_type;
-  double  cfl, dx, dy, dz;
-  double  idx, idy, idz; // 1/dx, 1/dy, 1/dz (used by the fast builds only)
-};
 
 template <class R>
 struct Buffers
@@ -93,10 +100,46 @@ step_finished(const DevState * st)
   return st->t >= (st->tEnd - 1e-14) || st->it >= st->nStepmax;
 }
 
+// Unsigned 32-bit division by a run-time constant d >= 1 through a
+// multiply-high (Granlund & Montgomery, 1994): with s = ceil(log2 d) and
+// m = ceil(2^(32+s) / d) - 2^32, q = (umulhi(x, m) + x) >> s for every 32-bit x.
+// The constants are computed on the host.
+struct FastDiv
+{
+  unsigned d = 1, m = 0, s = 0;
+  FastDiv() = default;
+  explicit FastDiv(unsigned dv)
+    : d(dv)
+  {
+    s = 0;
+    while ((1ull << s) < dv)
+      ++s;
+    m = (unsigned)(((1ull << (32 + s)) + dv - 1) / dv - (1ull << 32));
+  }
+  __device__ __forceinline__ unsigned
+  div(unsigned x) const
+  {
+    const unsigned hi = __umulhi(x, m);
+    return (unsigned)(((unsigned long long)hi + x) >> s);
+  }
+};
+
 // A box of cells [lo, lo+n) flattened with i fastest.
 struct Box
 {
-  int i0, j0, k0, ni, nj, nk;
+  int     i0 = 0, j0 = 0, k0 = 0, ni = 1, nj = 1, nk = 1;
+  FastDiv di, dj;
+  Box() = default;
+  Box(int a, int b, int c, int n0, int n1, int n2)
+    : i0(a)
+    , j0(b)
+    , k0(c)
+    , ni(n0)
+    , nj(n1)
+    , nk(n2)
+    , di((unsigned)n0)
+    , dj((unsigned)n1)
+  {}
   __host__ __device__ int64_t
   count() const
   {
@@ -104,18 +147,45 @@ struct Box
   }
 };
 
+// The boxes the kernels iterate over (filled on the host by make_grid).
+enum BoxId : int
+{
+  BOX_ALL = 0,      // every cell (boundaries)
+  BOX_PRIM = 1,     // [0, size-1)^DIM (primitives)
+  BOX_TRACE = 2,    // [g-1, size-g+1]^DIM (slopes, half step, edge field)
+  BOX_FACE = 3,     // [g, size-g]^DIM (faces and edges)
+  BOX_INTERIOR = 4, // interior cells (update, diagnostics)
+  BOX_COUNT = 5
+};
+
 __device__ __forceinline__ bool
 box_cell(const Box & b, int64_t idx, int & i, int & j, int & k)
 {
   if (idx >= b.count())
     return false;
-  const int64_t r = idx / b.ni;
-  i = b.i0 + (int)(idx - r * b.ni);
-  const int64_t kk = r / b.nj;
-  j = b.j0 + (int)(r - kk * b.nj);
+  // counts stay below 2^31 (grids are limited to 4e9 values, i.e. 5e8 cells)
+  const unsigned x = (unsigned)idx;
+  const unsigned r = b.di.div(x);
+  i = b.i0 + (int)(x - r * (unsigned)b.ni);
+  const unsigned kk = b.dj.div(r);
+  j = b.j0 + (int)(r - kk * (unsigned)b.nj);
   k = b.k0 + (int)kk;
   return true;
 }
+
+template <class R>
+struct Grid
+{
+  int     dim, nx, ny, nz, g;
+  int     isize, jsize, ksize;
+  int64_t sj, sk, sv; // strides of j, k and var (i stride is 1)
+  int     bc[6];
+  int     riemann;
+  R       gamma0, smallr, smallp, smallc, slope_type;
+  double  cfl, dx, dy, dz;
+  double  idx, idy, idz; // 1/dx, 1/dy, 1/dz (used by the fast builds only)
+  Box     box[BOX_COUNT];
+};
 
 template <class R>
 __device__ __forceinline__ int64_t
@@ -164,7 +234,7 @@ k_boundaries(const Grid<R> G, R * __restrict__ U, DevState * st, int force)
     return;
   if (blockIdx.x == 0 && threadIdx.x == 0)
     st->invdt_bits = 0ull; // reset the CFL reduction of this iteration
-  const Box b{ 0, 0, 0, G.isize, G.jsize, DIM == 3 ? G.ksize : 1 };
+  const Box & b = G.box[BOX_ALL];
   int       i, j, k;
   if (!box_cell(b, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
     return;
@@ -199,8 +269,9 @@ k_boundaries(const Grid<R> G, R * __restrict__ U, DevState * st, int force)
 
 // ---------------------------------------------------------------- primitives + CFL
 
-__device__ __forceinline__ double
-warp_max(double v)
+template <class T>
+__device__ __forceinline__ T
+warp_max(T v)
 {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1)
@@ -221,9 +292,9 @@ k_prim_dt(const Grid<R> G, const R * __restrict__ U, R * __restrict__ Q, DevStat
 {
   if (!force && step_finished(st))
     return;
-  const Box b{ 0, 0, 0, G.isize - 1, G.jsize - 1, DIM == 3 ? G.ksize - 1 : 1 };
+  const Box & b = G.box[BOX_PRIM];
   int       i, j, k;
-  double    rate = 0.0;
+  R         rate = R(0);
   bool      bad = false;
   if (box_cell(b, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
   {
@@ -301,13 +372,14 @@ k_prim_dt(const Grid<R> G, const R * __restrict__ U, R * __restrict__ Q, DevStat
           val = sx * R(G.idx) + sy * R(G.idy);
       }
       // fmax in the reference ignores NaN operands; a NaN rate is dropped
-      rate = (val >= R(0)) ? (double)val : 0.0;
+      rate = (val >= R(0)) ? val : R(0);
       const R Ein = U[c + IP * sv];
       bad = !(U[c + ID * sv] > R(0)) || !isfinite(Ein) || !isfinite(val);
     }
   }
-  // block max in FP64
-  __shared__ double red[32];
+  // block max in the working precision (max is exact in any precision), then
+  // one FP64 atomicMax per block
+  __shared__ R red[32];
   rate = warp_max(rate);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (lane == 0)
@@ -316,10 +388,10 @@ k_prim_dt(const Grid<R> G, const R * __restrict__ U, R * __restrict__ Q, DevStat
     atomicOr(&st->status, STATUS_NUMERIC);
   if (wid == 0)
   {
-    rate = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
+    rate = lane < (int)(blockDim.x >> 5) ? red[lane] : R(0);
     rate = warp_max(rate);
-    if (lane == 0 && rate > 0.0)
-      atomicMax(&st->invdt_bits, (unsigned long long)__double_as_longlong(rate));
+    if (lane == 0 && rate > R(0))
+      atomicMax(&st->invdt_bits, (unsigned long long)__double_as_longlong((double)rate));
   }
 }
 
@@ -344,6 +416,9 @@ k_finalize_dt(const Grid<R> G, DevState * st, int force)
   st->dtdx = dt / G.dx;
   st->dtdy = dt / G.dy;
   st->dtdz = dt / G.dz;
+  st->fdtdx = (float)st->dtdx;
+  st->fdtdy = (float)st->dtdy;
+  st->fdtdz = (float)st->dtdz;
   if (!(invDt > 0.0) || !isfinite(dt))
     st->status |= STATUS_NUMERIC;
 }
@@ -377,7 +452,7 @@ k_trace(const Grid<R> G, Buffers<R> B)
   if (step_finished(B.st))
     return;
   const int g = G.g;
-  const Box b{ g - 1, g - 1, DIM == 3 ? g - 1 : 0, G.nx + 3, G.ny + 3, DIM == 3 ? G.nz + 3 : 1 };
+  const Box & b = G.box[BOX_TRACE];
   int       i, j, k;
   if (!box_cell(b, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
     return;
@@ -385,8 +460,8 @@ k_trace(const Grid<R> G, Buffers<R> B)
   const int64_t c = cell_at(G, i, j, k);
   const R * __restrict__ Q = B.Q;
   const R * __restrict__ U = B.Uin;
-  const double dtdx_d = B.st->dtdx, dtdy_d = B.st->dtdy, dtdz_d = B.st->dtdz;
-  const R      dtdx = R(dtdx_d), dtdy = R(dtdy_d), dtdz = R(dtdz_d);
+  R dtdx, dtdy, dtdz;
+  dt_over_dx(B.st, dtdx, dtdy, dtdz);
   (void)dtdz;
 
   // edge electric field
@@ -440,7 +515,7 @@ k_trace(const Grid<R> G, Buffers<R> B)
   {
 #pragma unroll
     for (int v = 0; v < NV; ++v)
-      s[d][v] = limited_slope(q[v], Q[c + off[d] + v * sv], Q[c - off[d] + v * sv], G.slope_type);
+      s[d][v] = slope_limited(q[v], Q[c + off[d] + v * sv], Q[c - off[d] + v * sv], G.slope_type);
     s[d][IA + d] = U[c + off[d] + (IA + d) * sv] - U[c + (IA + d) * sv];
   }
   R * S = B.S;
@@ -577,7 +652,8 @@ flux_face(const Grid<R> & G, const Buffers<R> & B, int i, int j, int k)
   const int64_t c = cell_at(G, i, j, k), cn = c - off;
   const R * __restrict__ Q2 = B.Q2;
   const R * __restrict__ S = B.S + (int64_t)d * NV * sv;
-  const R dtdx = R(B.st->dtdx), dtdy = R(B.st->dtdy), dtdz = R(B.st->dtdz);
+  R dtdx, dtdy, dtdz;
+  dt_over_dx(B.st, dtdx, dtdy, dtdz);
   const R smallR = G.smallr, smallp = G.smallp;
   constexpr int nrm = IA + d;
 
@@ -627,7 +703,7 @@ k_flux(const Grid<R> G, Buffers<R> B)
   if (step_finished(B.st))
     return;
   const int g = G.g;
-  const Box b{ g, g, DIM == 3 ? g : 0, G.nx + 1, G.ny + 1, DIM == 3 ? G.nz + 1 : 1 };
+  const Box & b = G.box[BOX_FACE];
   int       i, j, k;
   if (!box_cell(b, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
     return;
@@ -651,10 +727,10 @@ face_field_slope(const Grid<R> & G, const R * __restrict__ U, int64_t c, int com
 {
   const int64_t cv = c + comp * G.sv;
   if (dir == 0)
-    return limited_slope(U[cv], U[cv + 1], U[cv - 1], G.slope_type);
+    return slope_limited(U[cv], U[cv + 1], U[cv - 1], G.slope_type);
   if (dir == 1)
-    return limited_slope(U[cv], U[cv + G.sj], U[cv - G.sj], G.slope_type);
-  return limited_slope(U[cv], U[cv + G.sk], U[cv + G.sk], G.slope_type);
+    return slope_limited(U[cv], U[cv + G.sj], U[cv - G.sj], G.slope_type);
+  return slope_limited(U[cv], U[cv + G.sk], U[cv + G.sk], G.slope_type);
 }
 
 // ReconstructEdgeComputeEmfAndUpdateFunctor (MHDRunFunctors2D.h:1291-1534,
@@ -676,7 +752,8 @@ emf_edge(const Grid<R> & G, const Buffers<R> & B, int i, int j, int k)
   const R * __restrict__ U = B.Uin;
   const R * __restrict__ S0 = B.S + (int64_t)d0 * NV * sv;
   const R * __restrict__ S1 = B.S + (int64_t)(DIM == 2 ? 1 : d1) * NV * sv;
-  const R dtdx = R(B.st->dtdx), dtdy = R(B.st->dtdy), dtdz = R(B.st->dtdz);
+  R dtdx, dtdy, dtdz;
+  dt_over_dx(B.st, dtdx, dtdy, dtdz);
   const R smallR = G.smallr, smallp = G.smallp;
 
   State<R> qe[4]; // RT, RB, LT, LB
@@ -752,7 +829,7 @@ k_emf(const Grid<R> G, Buffers<R> B)
   if (step_finished(B.st))
     return;
   const int g = G.g;
-  const Box b{ g, g, DIM == 3 ? g : 0, G.nx + 1, G.ny + 1, DIM == 3 ? G.nz + 1 : 1 };
+  const Box & b = G.box[BOX_FACE];
   int       i, j, k;
   if (!box_cell(b, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
     return;
@@ -784,13 +861,14 @@ k_update(const Grid<R> G, Buffers<R> B)
   if (step_finished(B.st))
     return;
   const int g = G.g;
-  const Box b{ g, g, DIM == 3 ? g : 0, G.nx, G.ny, DIM == 3 ? G.nz : 1 };
+  const Box & b = G.box[BOX_INTERIOR];
   int       i, j, k;
   if (!box_cell(b, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
     return;
   const int64_t sv = G.sv, sj = G.sj, sk = G.sk;
   const int64_t c = cell_at(G, i, j, k);
-  const R       dtd[3] = { R(B.st->dtdx), R(B.st->dtdy), R(B.st->dtdz) };
+  R             dtd[3];
+  dt_over_dx(B.st, dtd[0], dtd[1], dtd[2]);
   const int64_t off[3] = { 1, sj, sk };
   constexpr int NF = FluxComps<DIM>::NF;
 #pragma unroll
@@ -844,6 +922,52 @@ k_update(const Grid<R> G, Buffers<R> B)
     x += eY[c + 1] * dtd[0];
     B.Uout[c + IC * sv] = x;
   }
+}
+
+// Grid description of one problem for the kernels (host side):
+// HydroParams::init (HydroParams.cpp:420-453) in the working precision R,
+// plus the iteration boxes and their divisors.
+template <class R>
+inline Grid<R>
+make_grid(const mhd_params & p)
+{
+  Grid<R> G{};
+  G.dim = p.dim;
+  G.nx = p.nx;
+  G.ny = p.ny;
+  G.nz = p.dim == 3 ? p.nz : 1;
+  G.g = p.ghost;
+  G.isize = p.nx + 2 * p.ghost;
+  G.jsize = p.ny + 2 * p.ghost;
+  G.ksize = p.dim == 3 ? p.nz + 2 * p.ghost : 1;
+  G.sj = G.isize;
+  G.sk = (int64_t)G.isize * G.jsize;
+  G.sv = G.sk * G.ksize;
+  for (int f = 0; f < 6; ++f)
+    G.bc[f] = p.boundary[f];
+  G.riemann = p.riemann;
+  G.gamma0 = R(p.gamma0);
+  G.smallr = R(p.smallr);
+  G.smallc = R(p.smallc);
+  // smallp = smallc^2 / gamma0 in real_t (HydroParams.cpp:438)
+  G.smallp = R(R(p.smallc) * R(p.smallc) / R(p.gamma0));
+  G.slope_type = R(p.slope_type);
+  G.cfl = p.cfl;
+  // dx = (xmax - xmin) / nx in real_t (HydroParams.cpp:433-435)
+  G.dx = (double)R(R(p.xmax - p.xmin) / R(p.nx));
+  G.dy = (double)R(R(p.ymax - p.ymin) / R(p.ny));
+  G.dz = p.dim == 3 ? (double)R(R(p.zmax - p.zmin) / R(p.nz)) : 1.0;
+  G.idx = 1.0 / G.dx;
+  G.idy = 1.0 / G.dy;
+  G.idz = 1.0 / G.dz;
+  const bool d3 = p.dim == 3;
+  const int  g = G.g;
+  G.box[BOX_ALL] = Box(0, 0, 0, G.isize, G.jsize, d3 ? G.ksize : 1);
+  G.box[BOX_PRIM] = Box(0, 0, 0, G.isize - 1, G.jsize - 1, d3 ? G.ksize - 1 : 1);
+  G.box[BOX_TRACE] = Box(g - 1, g - 1, d3 ? g - 1 : 0, G.nx + 3, G.ny + 3, d3 ? G.nz + 3 : 1);
+  G.box[BOX_FACE] = Box(g, g, d3 ? g : 0, G.nx + 1, G.ny + 1, d3 ? G.nz + 1 : 1);
+  G.box[BOX_INTERIOR] = Box(g, g, d3 ? g : 0, G.nx, G.ny, d3 ? G.nz : 1);
+  return G;
 }
 
 } // namespace MHD_VARIANT_TAG

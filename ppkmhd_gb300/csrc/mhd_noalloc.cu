@@ -103,33 +103,7 @@ int
 step(const mhd_params & p, const void * U_in, void * U_out, double t, double * dt,
      cudaStream_t s, std::string & err)
 {
-  Grid<R> G{};
-  G.dim = p.dim;
-  G.nx = p.nx;
-  G.ny = p.ny;
-  G.nz = p.dim == 3 ? p.nz : 1;
-  G.g = p.ghost;
-  G.isize = p.nx + 2 * p.ghost;
-  G.jsize = p.ny + 2 * p.ghost;
-  G.ksize = p.dim == 3 ? p.nz + 2 * p.ghost : 1;
-  G.sj = G.isize;
-  G.sk = (int64_t)G.isize * G.jsize;
-  G.sv = G.sk * G.ksize;
-  for (int f = 0; f < 6; ++f)
-    G.bc[f] = p.boundary[f];
-  G.riemann = p.riemann;
-  G.gamma0 = R(p.gamma0);
-  G.smallr = R(p.smallr);
-  G.smallc = R(p.smallc);
-  G.smallp = R(R(p.smallc) * R(p.smallc) / R(p.gamma0));
-  G.slope_type = R(p.slope_type);
-  G.cfl = p.cfl;
-  G.dx = (double)R(R(p.xmax - p.xmin) / R(p.nx));
-  G.dy = (double)R(R(p.ymax - p.ymin) / R(p.ny));
-  G.dz = p.dim == 3 ? (double)R(R(p.zmax - p.zmin) / R(p.nz)) : 1.0;
-  G.idx = 1.0 / G.dx;
-  G.idy = 1.0 / G.dy;
-  G.idz = 1.0 / G.dz;
+  const Grid<R> G = make_grid<R>(p);
 
   const int     dim = p.dim;
   const size_t  n = (size_t)G.sv;

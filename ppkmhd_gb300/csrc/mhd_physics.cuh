@@ -152,6 +152,63 @@ limited_slope(R q, R qp, R qm, R slope_type)
   return dsgn * fmin(dlim, fabs(dcen));
 }
 
+// The same limiter with the comparisons, minima and the sign transfer done
+// on IEEE bit patterns (integer pipe): magnitudes of doubles order like their
+// bit patterns, and the scalings by slope_type (1 or 2) and by 1/2 are exact,
+// so the result equals limited_slope except for the sign of a zero result and
+// when a product underflows.  5 floating-point operations instead of 11.
+__device__ __forceinline__ long long
+fbits(double x)
+{
+  return __double_as_longlong(x);
+}
+__device__ __forceinline__ int
+fbits(float x)
+{
+  return __float_as_int(x);
+}
+__device__ __forceinline__ double
+from_fbits(long long b, double)
+{
+  return __longlong_as_double(b);
+}
+__device__ __forceinline__ float
+from_fbits(int b, float)
+{
+  return __int_as_float(b);
+}
+
+template <class R>
+__device__ __forceinline__ R
+limited_slope_bits(R q, R qp, R qm, R slope_type)
+{
+  const R a = q - qm, b = qp - q, c = qp - qm;
+  const auto ia = fbits(a), ib = fbits(b);
+  using I = decltype(ia);
+  const I sign = I(1) << (sizeof(I) * 8 - 1);
+  const I aa = ia & ~sign, ab = ib & ~sign;
+  // dlft * drgt <= 0: opposite signs or a zero
+  if (((ia ^ ib) & sign) != 0 || aa == 0 || ab == 0)
+    return R(0);
+  R m = from_fbits(aa < ab ? aa : ab, R(0));
+  if (slope_type == R(2))
+    m = m + m;
+  const I hc = fbits(R(0.5) * c) & ~sign;
+  const I mb = fbits(m);
+  const I r = mb < hc ? mb : hc;
+  return from_fbits(r | (fbits(c) & sign), R(0));
+}
+
+template <class R>
+__device__ __forceinline__ R
+slope_limited(R q, R qp, R qm, R slope_type)
+{
+  if constexpr (kExactOrder)
+    return limited_slope(q, qp, qm, slope_type);
+  else
+    return limited_slope_bits(q, qp, qm, slope_type);
+}
+
 // Conservative variables and 1D flux of a primitive state
 // (find_mhd_flux, mhd_utils.h:173-231; isothermal branch inactive).
 template <class R>

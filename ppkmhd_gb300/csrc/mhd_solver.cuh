@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(256)
 k_diag(const Grid<R> G, const R * __restrict__ U, double * __restrict__ partial)
 {
   const int g = G.g;
-  const Box b{ g, g, DIM == 3 ? g : 0, G.nx, G.ny, DIM == 3 ? G.nz : 1 };
+  const Box & b = G.box[BOX_INTERIOR];
   double    acc[10];
 #pragma unroll
   for (int q = 0; q < 10; ++q)
@@ -184,34 +184,7 @@ public:
   {
     P = p;
     dim = p.dim;
-    G.dim = p.dim;
-    G.nx = p.nx;
-    G.ny = p.ny;
-    G.nz = p.dim == 3 ? p.nz : 1;
-    G.g = p.ghost;
-    G.isize = p.nx + 2 * p.ghost;
-    G.jsize = p.ny + 2 * p.ghost;
-    G.ksize = p.dim == 3 ? p.nz + 2 * p.ghost : 1;
-    G.sj = G.isize;
-    G.sk = (int64_t)G.isize * G.jsize;
-    G.sv = G.sk * G.ksize;
-    for (int f = 0; f < 6; ++f)
-      G.bc[f] = p.boundary[f];
-    G.riemann = p.riemann;
-    G.gamma0 = R(p.gamma0);
-    G.smallr = R(p.smallr);
-    G.smallc = R(p.smallc);
-    // HydroParams::init (HydroParams.cpp:438): smallp = smallc^2 / gamma0, in real_t
-    G.smallp = R(R(p.smallc) * R(p.smallc) / R(p.gamma0));
-    G.slope_type = R(p.slope_type);
-    G.cfl = p.cfl;
-    // dx = (xmax - xmin) / nx in real_t (HydroParams.cpp:433-435)
-    G.dx = (double)R(R(p.xmax - p.xmin) / R(p.nx));
-    G.dy = (double)R(R(p.ymax - p.ymin) / R(p.ny));
-    G.dz = p.dim == 3 ? (double)R(R(p.zmax - p.zmin) / R(p.nz)) : 1.0;
-    G.idx = 1.0 / G.dx;
-    G.idy = 1.0 / G.dy;
-    G.idz = 1.0 / G.dz;
+    G = make_grid<R>(p);
     ncell = G.sv;
 
     int ndev = 0;
