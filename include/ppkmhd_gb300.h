@@ -80,7 +80,7 @@ typedef struct mhd_params
   double xmin, xmax, ymin, ymax, zmin, zmax;
   double gamma0, cfl, slope_type, smallr, smallc;
   int    riemann;    /* MHD_RIEMANN_* */
-  int    implementation_version; /* [OTHER] implementationVersion; 2 is implemented */
+  int    implementation_version; /* [OTHER] implementationVersion: 0, 1 or 2 */
   int    boundary[6];            /* xmin, xmax, ymin, ymax, zmin, zmax: MHD_BC_* */
   double tEnd, tCurrent;
   int    nStepmax;
@@ -193,7 +193,8 @@ const char *mhd_version(void);
  * as many in FP32).  t is the current time (dt is clipped to p->tEnd; when
  * t >= tEnd - 1e-14 nothing is computed and *dt = 0).  On return *dt holds
  * the dt of the iteration; the call synchronises `stream` (a cudaStream_t,
- * NULL for the legacy default stream).  Only MHD_FP_FAST is accepted.
+ * NULL for the legacy default stream).  Only MHD_FP_FAST and implementation
+ * version 2 are accepted.
  * The first call on a device looks up the scratch array's device address
  * (cudaGetSymbolAddress); make it before any stream capture.  All calls share
  * the array: calls that overlap on the GPU race and must be serialised.

@@ -57,9 +57,8 @@ validate_params(const mhd_params & p)
     return "grid too large: ghost-inclusive cells x 8 variables must stay below 4e9";
   if (p.riemann != MHD_RIEMANN_HLLD && p.riemann != MHD_RIEMANN_HLL && p.riemann != MHD_RIEMANN_LLF)
     return "riemann solver must be hlld, hll or llf for MHD";
-  if (p.implementation_version != 2)
-    return "implementationVersion " + std::to_string(p.implementation_version) +
-           " is not available on this back-end; set [OTHER] implementationVersion=2";
+  if (p.implementation_version < 0 || p.implementation_version > 2)
+    return "implementationVersion must be 0, 1 or 2";
   for (int f = 0; f < (p.dim == 3 ? 6 : 4); ++f)
     if (p.boundary[f] != MHD_BC_REFLECTING && p.boundary[f] != MHD_BC_OUTFLOW &&
         p.boundary[f] != MHD_BC_PERIODIC)

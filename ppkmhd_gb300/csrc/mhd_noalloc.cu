@@ -203,7 +203,8 @@ extern "C"
   {
     if (!p || !U_in || !U_out || !dt || U_in == U_out)
       return MHD_ERR_INVALID_ARG;
-    if (!mhd::validate_params(*p).empty() || p->fp_mode != MHD_FP_FAST)
+    if (!mhd::validate_params(*p).empty() || p->fp_mode != MHD_FP_FAST ||
+        p->implementation_version != 2)
       return MHD_ERR_INVALID_ARG;
     std::string  err; // status codes carry the outcome; the text is not kept
     cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -14,6 +14,7 @@
 
 #include "mhd_core.h"
 #include "mhd_kernels.cuh"
+#include "mhd_kernels_v0.cuh"
 
 namespace mhd
 {
@@ -135,6 +136,9 @@ public:
   R *          E = nullptr;
   R *          F = nullptr;
   R *          Em = nullptr;
+  R *          T = nullptr;  // versions 0/1: stored trace states
+  R *          D = nullptr;  // versions 0/1 in 3D: transverse face-field slopes
+  int          version = 2;
   double *     diag = nullptr;
   DevState *   st = nullptr;
   DevState *   st_host = nullptr; // pinned
@@ -152,7 +156,7 @@ public:
       if (graph_pair[q])
         cudaGraphExecDestroy(graph_pair[q]);
     }
-    R * bufs[] = { U, U2, Q, Q2, S, E, F, Em };
+    R * bufs[] = { U, U2, Q, Q2, S, E, F, Em, T, D };
     for (R * b : bufs)
       if (b)
         cudaFree(b);
@@ -203,11 +207,21 @@ public:
     const size_t n = (size_t)ncell;
     const int    nplanes_e = dim == 3 ? 3 : 1;
     const int    nf = dim == 3 ? 5 : 6;
+    version = p.implementation_version;
     MHD_CK(cudaMalloc(&U, n * NV * sizeof(R)));
     MHD_CK(cudaMalloc(&U2, n * NV * sizeof(R)));
     MHD_CK(cudaMalloc(&Q, n * NV * sizeof(R)));
-    MHD_CK(cudaMalloc(&Q2, n * NV * sizeof(R)));
-    MHD_CK(cudaMalloc(&S, n * NV * dim * sizeof(R)));
+    if (version == 2)
+    {
+      MHD_CK(cudaMalloc(&Q2, n * NV * sizeof(R)));
+      MHD_CK(cudaMalloc(&S, n * NV * dim * sizeof(R)));
+    }
+    else
+    {
+      MHD_CK(cudaMalloc(&T, n * NV * (dim == 3 ? 18 : 8) * sizeof(R)));
+      if (dim == 3)
+        MHD_CK(cudaMalloc(&D, n * 6 * sizeof(R)));
+    }
     MHD_CK(cudaMalloc(&E, n * nplanes_e * sizeof(R)));
     MHD_CK(cudaMalloc(&F, n * nf * dim * sizeof(R)));
     MHD_CK(cudaMalloc(&Em, n * nplanes_e * sizeof(R)));
@@ -218,8 +232,14 @@ public:
     // as the reference's zero-initialised Kokkos views do
     R * bufs[] = { U, U2, Q, Q2 };
     for (R * b : bufs)
-      MHD_CK(cudaMemsetAsync(b, 0, n * NV * sizeof(R), stream));
-    MHD_CK(cudaMemsetAsync(S, 0, n * NV * dim * sizeof(R), stream));
+      if (b)
+        MHD_CK(cudaMemsetAsync(b, 0, n * NV * sizeof(R), stream));
+    if (S)
+      MHD_CK(cudaMemsetAsync(S, 0, n * NV * dim * sizeof(R), stream));
+    if (T)
+      MHD_CK(cudaMemsetAsync(T, 0, n * NV * (dim == 3 ? 18 : 8) * sizeof(R), stream));
+    if (D)
+      MHD_CK(cudaMemsetAsync(D, 0, n * 6 * sizeof(R), stream));
     MHD_CK(cudaMemsetAsync(E, 0, n * nplanes_e * sizeof(R), stream));
     MHD_CK(cudaMemsetAsync(F, 0, n * nf * dim * sizeof(R), stream));
     MHD_CK(cudaMemsetAsync(Em, 0, n * nplanes_e * sizeof(R), stream));
@@ -325,33 +345,133 @@ public:
     else
       k_update<R, 3><<<nblocks(n, 256), 256, 0, stream>>>(G, B);
   }
+  // ---- versions 0 and 1 ----
+  void
+  launch_v0_prep(const Buffers<R> & B)
+  {
+    const int64_t n = (int64_t)(G.isize - 1) * (G.jsize - 1) * (G.ksize - 1);
+    k_v0_prep3d<R><<<nblocks(n, 128), 128, 0, stream>>>(G, B.Uin, Q, E, D, st);
+  }
+  void
+  launch_v0_trace(const Buffers<R> & B)
+  {
+    const int64_t n = (int64_t)(G.isize - 1) * (G.jsize - 1) * (dim == 3 ? G.ksize - 1 : 1);
+    if (dim == 2)
+      k_v0_trace<R, 2><<<nblocks(n, 128), 128, 0, stream>>>(G, B.Uin, Q, E, D, T, st);
+    else
+      k_v0_trace<R, 3><<<nblocks(n, 128), 128, 0, stream>>>(G, B.Uin, Q, E, D, T, st);
+  }
+  void
+  launch_v0_flux()
+  {
+    const int64_t n = (int64_t)(G.nx + 1) * (G.ny + 1) * (dim == 3 ? G.nz + 1 : 1);
+    if (dim == 2)
+      k_v0_flux<R, 2><<<dim3(nblocks(n, 128), 2), 128, 0, stream>>>(G, T, F, st);
+    else
+      k_v0_flux<R, 3><<<dim3(nblocks(n, 128), 3), 128, 0, stream>>>(G, T, F, st);
+  }
+  void
+  launch_v0_emf()
+  {
+    const int64_t n = (int64_t)(G.nx + 1) * (G.ny + 1) * (dim == 3 ? G.nz + 1 : 1);
+    if (dim == 2)
+      k_v0_emf<R, 2><<<dim3(nblocks(n, 128), 1), 128, 0, stream>>>(G, T, Em, st);
+    else
+      k_v0_emf<R, 3><<<dim3(nblocks(n, 128), 3), 128, 0, stream>>>(G, T, Em, st);
+  }
+  void
+  launch_v0_update(const Buffers<R> & B)
+  {
+    const int64_t  n = (int64_t)G.nx * G.ny * (dim == 3 ? G.nz : 1);
+    const unsigned nb = nblocks(n, 256);
+    if (dim == 2 && version == 0)
+      k_v0_update<R, 2, 0><<<nb, 256, 0, stream>>>(G, B.Uin, B.Uout, F, Em, st);
+    else if (dim == 2)
+      k_v0_update<R, 2, 1><<<nb, 256, 0, stream>>>(G, B.Uin, B.Uout, F, Em, st);
+    else if (version == 0)
+      k_v0_update<R, 3, 0><<<nb, 256, 0, stream>>>(G, B.Uin, B.Uout, F, Em, st);
+    else
+      k_v0_update<R, 3, 1><<<nb, 256, 0, stream>>>(G, B.Uin, B.Uout, F, Em, st);
+  }
+
   void
   launch_advance()
   {
     k_advance<R><<<1, 1, 0, stream>>>(st);
   }
 
-  static constexpr int kLaunches = 8;
+  static constexpr int kMaxLaunches = 9;
+
+  // Names of the launches of one iteration, in order.
+  int
+  step_kernel_names(const char ** names) const
+  {
+    static const char * v2[] = { "k_boundaries", "k_prim_dt", "k_finalize_dt", "k_trace",
+                                  "k_flux",       "k_emf",     "k_update",      "k_advance" };
+    static const char * v0_2d[] = { "k_boundaries", "k_prim_dt", "k_finalize_dt", "k_v0_trace",
+                                    "k_v0_flux",    "k_v0_emf",  "k_v0_update",   "k_advance" };
+    static const char * v0_3d[] = { "k_boundaries", "k_prim_dt", "k_finalize_dt",
+                                    "k_v0_prep3d",  "k_v0_trace", "k_v0_flux",
+                                    "k_v0_emf",     "k_v0_update", "k_advance" };
+    const char ** src = version == 2 ? v2 : (dim == 3 ? v0_3d : v0_2d);
+    const int     n = version == 2 ? 8 : (dim == 3 ? 9 : 8);
+    for (int q = 0; q < n; ++q)
+      names[q] = src[q];
+    return n;
+  }
+
+  // Launch number q of one iteration.
+  void
+  launch_stage(int q, const Buffers<R> & B)
+  {
+    if (q == 0)
+      return launch_boundaries(B.Uin, 0);
+    if (q == 1)
+      return launch_prim_dt(B.Uin, 0);
+    if (q == 2)
+      return launch_finalize(0);
+    if (version == 2)
+    {
+      if (q == 3)
+        return launch_trace(B);
+      if (q == 4)
+        return launch_flux(B);
+      if (q == 5)
+        return launch_emf(B);
+      if (q == 6)
+        return launch_update(B);
+      return launch_advance();
+    }
+    const int r = dim == 3 ? q - 3 : q - 2; // 3D has the extra preparation launch
+    if (dim == 3 && q == 3)
+      return launch_v0_prep(B);
+    if (r == 1)
+      return launch_v0_trace(B);
+    if (r == 2)
+      return launch_v0_flux();
+    if (r == 3)
+      return launch_v0_emf();
+    if (r == 4)
+      return launch_v0_update(B);
+    return launch_advance();
+  }
 
   // One iteration (godunov_unsplit_impl + next_iteration bookkeeping).
   void
   enqueue_step(int parity)
   {
     const Buffers<R> B = buffers(parity);
-    launch_boundaries(B.Uin, 0);
-    launch_prim_dt(B.Uin, 0);
-    launch_finalize(0);
-    launch_trace(B);
-    launch_flux(B);
-    launch_emf(B);
-    launch_update(B);
-    launch_advance();
+    const char *     names[kMaxLaunches];
+    const int        n = step_kernel_names(names);
+    for (int q = 0; q < n; ++q)
+      launch_stage(q, B);
   }
 
   int
   launches_per_step() override
   {
-    return kLaunches;
+    const char * names[kMaxLaunches];
+    return step_kernel_names(names);
   }
 
   int
@@ -660,47 +780,35 @@ public:
   int
   profile_step(const char ** names, float * ms, int max, int * count) override
   {
-    static const char * kNames[kLaunches] = { "k_boundaries", "k_prim_dt", "k_finalize_dt",
-                                              "k_trace",      "k_flux",    "k_emf",
-                                              "k_update",     "k_advance" };
     if (int rc = read_state())
       return rc;
     launched = st_host->it;
     const Buffers<R> B = buffers((int)(launched & 1));
-    cudaEvent_t      ev[kLaunches + 1];
-    for (int q = 0; q <= kLaunches; ++q)
+    const char *     kn[kMaxLaunches];
+    const int        n = step_kernel_names(kn);
+    cudaEvent_t      ev[kMaxLaunches + 1];
+    for (int q = 0; q <= n; ++q)
       MHD_CK(cudaEventCreate(&ev[q]));
     MHD_CK(cudaEventRecord(ev[0], stream));
-    launch_boundaries(B.Uin, 0);
-    MHD_CK(cudaEventRecord(ev[1], stream));
-    launch_prim_dt(B.Uin, 0);
-    MHD_CK(cudaEventRecord(ev[2], stream));
-    launch_finalize(0);
-    MHD_CK(cudaEventRecord(ev[3], stream));
-    launch_trace(B);
-    MHD_CK(cudaEventRecord(ev[4], stream));
-    launch_flux(B);
-    MHD_CK(cudaEventRecord(ev[5], stream));
-    launch_emf(B);
-    MHD_CK(cudaEventRecord(ev[6], stream));
-    launch_update(B);
-    MHD_CK(cudaEventRecord(ev[7], stream));
-    launch_advance();
-    MHD_CK(cudaEventRecord(ev[8], stream));
+    for (int q = 0; q < n; ++q)
+    {
+      launch_stage(q, B);
+      MHD_CK(cudaEventRecord(ev[q + 1], stream));
+    }
     ++launched;
     if (int rc = check_launch())
       return rc;
-    MHD_CK(cudaEventSynchronize(ev[kLaunches]));
-    for (int q = 0; q < kLaunches && q < max; ++q)
+    MHD_CK(cudaEventSynchronize(ev[n]));
+    for (int q = 0; q < n && q < max; ++q)
     {
       if (names)
-        names[q] = kNames[q];
+        names[q] = kn[q];
       MHD_CK(cudaEventElapsedTime(&ms[q], ev[q], ev[q + 1]));
     }
-    for (int q = 0; q <= kLaunches; ++q)
+    for (int q = 0; q <= n; ++q)
       cudaEventDestroy(ev[q]);
     if (count)
-      *count = kLaunches;
+      *count = n;
     return MHD_OK;
   }
 

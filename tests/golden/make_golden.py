@@ -43,6 +43,14 @@ STEP_CASES = [
     ("ot3d_hll", dict(dim=3, nx=8, ny=9, nz=10, riemann="hll"), 3, 22),
     ("ot3d_llf", dict(dim=3, nx=8, ny=9, nz=10, riemann="llf"), 3, 23),
     ("ot3d_bc_mixed", dict(dim=3, nx=9, ny=8, nz=10, bc=(1, 2, 3, 3, 2, 1)), 4, 24),
+    # implementation versions 0 and 1 (trace + stored states; v0 is the
+    # default of the reference's 3D Orszag-Tang .ini)
+    ("v0_ot2d_hlld", dict(dim=2, nx=20, ny=18, version=0), 8, None),
+    ("v0_ot2d_pert", dict(dim=2, nx=16, ny=14, version=0, bc=(1, 2, 3, 3, 3, 3)), 6, 31),
+    ("v1_ot2d_pert", dict(dim=2, nx=16, ny=14, version=1), 6, 32),
+    ("v0_ot3d_hlld", dict(dim=3, nx=12, ny=12, nz=6, zmax="0.25", version=0), 4, None),
+    ("v0_ot3d_pert", dict(dim=3, nx=9, ny=10, nz=8, version=0, riemann="hll"), 3, 33),
+    ("v1_ot3d_pert", dict(dim=3, nx=9, ny=8, nz=10, version=1, bc=(3, 3, 1, 2, 3, 3)), 3, 34),
 ]
 
 

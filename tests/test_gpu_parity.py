@@ -58,6 +58,35 @@ def test_exact_matches_reference_golden_bitwise(mhdlib, path):
     assert (t, dt, it) == (z["t"][2], z["dt"][2], int(z["nsteps"]))
 
 
+V01_FILES = [p for p in STEP_FILES if os.path.basename(p).startswith(("steps_v0_", "steps_v1_"))]
+
+
+@pytest.mark.parametrize("path", V01_FILES, ids=[os.path.basename(p)[6:-4] for p in V01_FILES])
+def test_fast_versions_0_1_against_reference(mhdlib, path):
+    """Implementation versions 0 and 1 in the production FP64 build."""
+    z = np.load(path)
+    s = gpu_solver(mhdlib, str(z["ini"]))
+    if bool(z["perturbed"]):
+        s.set_state(z["U0"])
+    else:
+        s.init_problem()
+    s.run(int(z["nsteps"]))
+    err = rel_l1(mhdlib.interior(s.get_state()), z["Un"])
+    assert err.max() <= TOL_FP64_FAST, err
+
+
+@pytest.mark.parametrize("version", [0, 1])
+def test_versions_0_1_conserve_and_keep_div_b(mhdlib, version):
+    s = gpu_solver(mhdlib, ot_ini(dim=3, nx=32, ny=24, nz=16, version=version))
+    s.init_problem()
+    m0, _, _ = s.diagnostics()
+    assert s.run(15) == 15
+    m1, _, dmax = s.diagnostics()
+    assert abs(m1[0] - m0[0]) <= 1e-12 * abs(m0[0])
+    assert abs(m1[1] - m0[1]) <= 1e-12 * abs(m0[1])
+    assert dmax <= 1e-12 * np.abs(mhdlib.interior(s.get_state())[5:8]).max() * 32
+
+
 @pytest.mark.parametrize("dim,kw,steps", [
     (2, dict(nx=64, ny=48), 25),
     (2, dict(nx=40, ny=33, riemann="hll", bc=(1, 1, 2, 2, 3, 3)), 15),

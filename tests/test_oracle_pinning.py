@@ -15,8 +15,14 @@ GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 STEP_FILES = sorted(glob.glob(os.path.join(GOLDEN, "steps_*.npz")))
 
 
-@pytest.mark.parametrize("path", STEP_FILES, ids=[os.path.basename(p)[6:-4] for p in STEP_FILES])
+V2_STEP_FILES = [p for p in STEP_FILES if not os.path.basename(p).startswith(("steps_v0_", "steps_v1_"))]
+
+
+@pytest.mark.parametrize("path", V2_STEP_FILES,
+                         ids=[os.path.basename(p)[6:-4] for p in V2_STEP_FILES])
 def test_oracle_matches_reference_steps(oracle, path):
+    """The C restatement covers implementation version 2; the version 0/1
+    fixtures pin the GPU's FMA-free build directly (tests/test_gpu_parity.py)."""
     z = np.load(path)
     ini = str(z["ini"])
     s = oracle.OracleSolver(ini)
