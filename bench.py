@@ -37,6 +37,9 @@ WORKLOADS = {
     "ot3d_256_fp64": (3, 256, 64, "3D Orszag-Tang 256^3, FP64 plain MUSCL-Hancock+HLLD+CT"),
     "ot3d_256_fp32": (3, 256, 32, "3D Orszag-Tang 256^3, FP32 plain MUSCL-Hancock+HLLD+CT"),
     "ot2d_256_fp64": (2, 256, 64, "2D Orszag-Tang 256^2, FP64 plain MUSCL-Hancock+HLLD+CT"),
+    "ensemble512_fp32": (2, 0, 32, "512 independent 2D Orszag-Tang problems, N ~ logU[64,512] "
+                                    "(seed 2024), B0 ~ U[0.5,1.5]/sqrt(4 pi), 5% random-phase "
+                                    "Fourier velocity on |k|<=4, FP32, one ensemble context"),
     # reduced size for ncu captures (a few GB on the device, inputs still > L2)
     "ot3d_128_fp64": (3, 128, 64, "3D Orszag-Tang 128^3, FP64 plain MUSCL-Hancock+HLLD+CT"),
     "ot3d_128_fp32": (3, 128, 32, "3D Orszag-Tang 128^3, FP32 plain MUSCL-Hancock+HLLD+CT"),
@@ -313,6 +316,168 @@ def run_gb300(args):
         torch.distributed.destroy_process_group()
 
 
+def ensemble_sample(specs):
+    """Problems the CPU legs time: the smallest, the largest and 6 seeded
+    random ones."""
+    sizes = [sp["n"] for sp in specs]
+    rng = np.random.default_rng(99)
+    sub = {int(np.argmin(sizes)), int(np.argmax(sizes))}
+    sub |= set(int(x) for x in rng.choice(len(specs), 6, replace=False))
+    return sorted(sub)
+
+
+def cpu_ensemble_run(specs, steps: int, nthreads: int):
+    """The oracle port on the sample problems of the ensemble, one after the
+    other (the reference has no batching), `steps` timed iterations each."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+    from ppkmhd_gb300 import workloads
+
+    oracle_py.build_oracle()
+    cells = 0
+    el = 0.0
+    sample = ensemble_sample(specs)
+    for q in sample:
+        ini, U = workloads.ensemble_problem(specs[q])
+        o = oracle_py.OracleSolver(ini, nthreads=nthreads)
+        o.set_state(U)
+        o.run(1)
+        t0 = time.perf_counter()
+        o.run(steps)
+        el += time.perf_counter() - t0
+        cells += specs[q]["n"] ** 2 * steps
+        o.close()
+    desc = (f"{len(sample)} of the 512 problems (N = "
+            + ", ".join(str(specs[q]["n"]) for q in sample)
+            + f"), {steps} steps each after 1 warm-up step, oracle/mhd_oracle.c with {nthreads} "
+              f"OpenMP threads, FP64, one problem at a time ({el:.1f} s timed)")
+    return cells / el, el, desc
+
+
+def run_ensemble(args):
+    """The 512-problem FP32 ensemble: one context, autotuned launch shapes,
+    CUDA-graph replay; value = interior cell-updates/s over all problems."""
+    world, rank, local = dist_setup()
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import ppkmhd_gb300 as m
+    from ppkmhd_gb300 import workloads
+
+    specs = workloads.ensemble_specs(512, seed=2024)
+    params, states = [], []
+    for sp in specs:
+        ini, U = workloads.ensemble_problem(sp, precision=32)
+        p = m.params_from_ini(ini)
+        p.device = local
+        params.append(p)
+        states.append(U.astype(np.float32))
+    ens = m.MHDEnsemble(params)
+    for q, U in enumerate(states):
+        ens.set_state(q, U)
+    cells = ens.cell_count()
+    state_bytes = int(sum(U.nbytes for U in states))
+    tune = ens.autotune()
+
+    ens.run(max(args.warmup, 3))
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms = ens.run(args.steps)
+    torch.cuda.synchronize()
+    t_sec = ms / 1e3
+    if world > 1:
+        tt = torch.tensor([t_sec], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_sec = float(tt.item())
+    value = world * cells * args.steps / t_sec
+
+    prof = {}
+    for _ in range(3):
+        for name, kms in ens.profile_step():
+            prof.setdefault(name, []).append(kms)
+    prof = {k: float(np.median(v)) for k, v in prof.items()}
+    step_ms = sum(prof.values())
+    dom = max(prof, key=prof.get)
+
+    # end to end through the public API: upload every problem from pinned
+    # host memory, run the steps, read every problem back
+    e2e_steps = args.steps
+    pinned = []
+    for U in states:
+        h = torch.empty(U.shape, dtype=torch.float32, pin_memory=True)
+        h.numpy()[:] = U
+        pinned.append(h)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for q, h in enumerate(pinned):
+        m.lib().mhd_ensemble_set_state(ens.h, q, h.data_ptr(), m.MHD_LAYOUT_LEFT, 4)
+    ens.run(e2e_steps)
+    for q, h in enumerate(pinned):
+        m.lib().mhd_ensemble_get_state(ens.h, q, h.data_ptr(), m.MHD_LAYOUT_LEFT, 4)
+    e2e_sec = time.perf_counter() - t0
+    e2e_value = world * cells * e2e_steps / e2e_sec
+
+    hbm_peak, peak_kind = load_peaks()
+    alg = 16 * 4
+    achieved = alg * cells / (prof[dom] / 1e3) / 1e9
+    step_achieved = alg * cells / (step_ms / 1e3) / 1e9
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        v, el, desc = cpu_ensemble_run(specs, steps=args.cpu_steps, nthreads=nthreads)
+        cpu = {"value": v, "unit": "cell-updates/s", "cores": nthreads, "kind": "port",
+               "sample": desc}
+    if rank == 0:
+        sizes = [sp["n"] for sp in specs]
+        emit({
+            "metric": "MHD cell-updates/s (interior cells), 512-problem 2D ensemble",
+            "value": value,
+            "unit": "cell-updates/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": max(args.warmup, 3),
+            "ms_per_step": t_sec * 1e3 / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic: seeded Orszag-Tang ensemble (sizes, B0, Fourier velocity)",
+            "config": {"workload": WORKLOADS["ensemble512_fp32"][3], "problems": len(specs),
+                       "n_min": min(sizes), "n_max": max(sizes), "cells": cells,
+                       "state_bytes": state_bytes,
+                       "l2": "inputs larger than L2 (%.2f GB of state per array)" % (state_bytes / 1e9),
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "kernels_per_step": ens.launches_per_step(),
+                       "per_kernel_ms": prof,
+                       "autotune": [ln for ln in tune.splitlines() if ln.startswith("->")]},
+            "e2e": {"value": e2e_value, "unit": "cell-updates/s",
+                    "h2d_bytes_per_step": state_bytes / e2e_steps,
+                    "d2h_bytes_per_step": state_bytes / e2e_steps, "steps": e2e_steps,
+                    "call": "mhd_ensemble_set_state x512 + mhd_ensemble_run + "
+                            "mhd_ensemble_get_state x512 (pinned host buffers, inside the timed "
+                            "region)"},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved / hbm_peak,
+                         "traffic": load_profile_traffic("ensemble512_fp32", dom),
+                         "peak_source": f"hbm_gbs of {peak_kind}",
+                         "algorithmic_bytes_per_cell": alg,
+                         "step_achieved": step_achieved, "step_frac": step_achieved / hbm_peak},
+            "clocks": clk.summary(),
+            "gpu_launches": ens.launches_per_step() * args.steps,
+            "cpu_baseline": cpu,
+        })
+    ens.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
 def load_profile_traffic(workload: str, kernel: str):
     """DRAM bytes per launch of the dominant kernel from the committed ncu
     summary (profiles/*.json), or None."""
@@ -334,6 +499,24 @@ def run_reference(args):
     dim, n, precision, label = WORKLOADS[args.workload]
     nthreads = os.cpu_count() or 1
     steps = args.ref_steps
+    if args.workload.startswith("ensemble"):
+        from ppkmhd_gb300 import workloads
+
+        v, el, desc = cpu_ensemble_run(workloads.ensemble_specs(512, seed=2024), steps, nthreads)
+        emit({"impl": "reference",
+              "metric": "MHD cell-updates/s (interior cells), 512-problem 2D ensemble",
+              "value": v, "unit": "cell-updates/s", "n_gpus": world, "steps": steps,
+              "warmup": 1, "ms_per_step": el * 1e3 / steps, "higher_is_better": True,
+              "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+              "data": "synthetic: seeded Orszag-Tang ensemble (sizes, B0, Fourier velocity)",
+              "config": {"workload": label,
+                         "implementation": "CPU port of the reference step (oracle/mhd_oracle.c), "
+                                           "problems one at a time, OpenMP"},
+              "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": nthreads,
+                               "kind": "port", "sample": desc},
+              "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                      "d2h_bytes_per_step": 0}})
+        return
     v, el = cpu_baseline_run(dim, n, steps=steps, warmup=min(args.warmup, 1), nthreads=nthreads)
     emit({
         "impl": "reference",
@@ -374,6 +557,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload.startswith("ensemble"):
+        run_ensemble(args)
     else:
         run_gb300(args)
 

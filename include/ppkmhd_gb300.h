@@ -173,6 +173,57 @@ int mhd_launches_per_step(mhd_ctx *ctx, int *n);
 const char *mhd_last_error(mhd_ctx *ctx);
 const char *mhd_version(void);
 
+/*
+ * Ensembles: many independent problems of uneven size advanced together.
+ * The reference runs such problems one at a time, each through its own
+ * solver object (main.cpp:133-159 per .ini); here one context holds them
+ * all, and every kernel launch of an iteration covers every problem, each
+ * with its own CFL dt, time and stopping rule (SolverBase::finished), with
+ * whole runs replayed from CUDA graphs.  Each problem is exactly the
+ * single-problem iteration above (implementation version 2): results are
+ * bitwise those of separate mhd_ctx runs of the same parameters.
+ */
+typedef struct mhd_ensemble mhd_ensemble;
+
+/* p[0..n-1]: one parameter set per problem; all share dim, precision,
+ * fp_mode and device, and use implementation version 2.  States start at
+ * zero until mhd_ensemble_init_problem / mhd_ensemble_set_state.  On a
+ * parameter error *ens is still set, so mhd_ensemble_last_error can report. */
+int mhd_ensemble_create(const mhd_params *p, int n, mhd_ensemble **ens);
+int mhd_ensemble_destroy(mhd_ensemble *ens);
+
+/* Orszag-Tang initial condition of problem `prob`, then boundaries,
+ * primitives and dt (as mhd_init_problem). */
+int mhd_ensemble_init_problem(mhd_ensemble *ens, int prob);
+
+/* As mhd_set_state / mhd_get_state, for problem `prob`. */
+int mhd_ensemble_set_state(mhd_ensemble *ens, int prob, const void *U, int layout, int real_bytes);
+int mhd_ensemble_get_state(mhd_ensemble *ens, int prob, void *U, int layout, int real_bytes);
+
+/* nsteps iterations of every problem that is not finished (problems stop
+ * on device at their own tEnd / nStepmax); *ms = elapsed device time (CUDA
+ * events on the ensemble's stream; may be NULL).  All problems must be at
+ * iterations of the same parity (true after set_state/init of each). */
+int mhd_ensemble_run(mhd_ensemble *ens, int nsteps, float *ms);
+
+int mhd_ensemble_time(mhd_ensemble *ens, int prob, double *t, double *dt, int *iteration);
+int mhd_ensemble_diagnostics(mhd_ensemble *ens, int prob, double sums[8], double *divb_l1,
+                             double *divb_max);
+
+/* Pick the threads per block of every batched kernel by timing candidates
+ * on the current states (results unchanged); report = one line per
+ * candidate (may be NULL). */
+int mhd_ensemble_autotune(mhd_ensemble *ens, char *report, size_t report_len);
+
+/* As mhd_profile_step, for one iteration of the whole ensemble. */
+int mhd_ensemble_profile_step(mhd_ensemble *ens, const char **names, float *ms, int max,
+                              int *count);
+
+/* Interior cells over all problems (cell-updates per ensemble iteration). */
+int mhd_ensemble_cell_count(mhd_ensemble *ens, int64_t *interior);
+int mhd_ensemble_launches_per_step(mhd_ensemble *ens, int *n);
+const char *mhd_ensemble_last_error(mhd_ensemble *ens);
+
 /* Device scratch reserved by mhd_step_noalloc on every GPU that loads this
  * library, for the process lifetime. */
 #define MHD_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)

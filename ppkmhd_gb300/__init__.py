@@ -99,6 +99,21 @@ SIGNATURES = {
     "mhd_version": (ctypes.c_char_p, []),
     "mhd_step_noalloc": (ctypes.c_int, [ctypes.POINTER(MHDParams), _vp, _vp, ctypes.c_double,
                                         _dp, _vp]),
+    "mhd_ensemble_create": (ctypes.c_int, [ctypes.POINTER(MHDParams), ctypes.c_int,
+                                           ctypes.POINTER(_vp)]),
+    "mhd_ensemble_destroy": (ctypes.c_int, [_vp]),
+    "mhd_ensemble_init_problem": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "mhd_ensemble_set_state": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_int, ctypes.c_int]),
+    "mhd_ensemble_get_state": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_int, ctypes.c_int]),
+    "mhd_ensemble_run": (ctypes.c_int, [_vp, ctypes.c_int, _fp]),
+    "mhd_ensemble_time": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _ip]),
+    "mhd_ensemble_diagnostics": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp]),
+    "mhd_ensemble_autotune": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_size_t]),
+    "mhd_ensemble_profile_step": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_char_p), _fp,
+                                                 ctypes.c_int, _ip]),
+    "mhd_ensemble_cell_count": (ctypes.c_int, [_vp, _i64p]),
+    "mhd_ensemble_launches_per_step": (ctypes.c_int, [_vp, _ip]),
+    "mhd_ensemble_last_error": (ctypes.c_char_p, [_vp]),
 }
 
 _lib = None
@@ -269,3 +284,127 @@ def interior(U: np.ndarray, ghost: int = 3) -> np.ndarray:
     if U.ndim == 3:
         return U[:, g:-g, g:-g]
     return U[:, g:-g, g:-g, g:-g]
+
+
+class MHDEnsemble:
+    """Many independent problems advanced together (an ``mhd_ensemble``)."""
+
+    def __init__(self, params: list):
+        self.params = list(params)
+        n = len(self.params)
+        arr = (MHDParams * n)(*self.params)
+        self.h = _vp()
+        rc = lib().mhd_ensemble_create(arr, n, ctypes.byref(self.h))
+        if rc != MHD_OK:
+            msg = (lib().mhd_ensemble_last_error(self.h).decode() if self.h
+                   else "mhd_ensemble_create failed")
+            if self.h:
+                lib().mhd_ensemble_destroy(self.h)
+                self.h = _vp()
+            raise MHDError(rc, msg)
+        self.real = np.float64 if self.params[0].precision == MHD_FP64 else np.float32
+
+    @classmethod
+    def from_ini(cls, ini_texts, precision: int | None = None, fp_mode: int | None = None):
+        ps = []
+        for t in ini_texts:
+            p = params_from_ini(t)
+            if precision is not None:
+                p.precision = precision
+            if fp_mode is not None:
+                p.fp_mode = fp_mode
+            ps.append(p)
+        return cls(ps)
+
+    def _check(self, rc: int):
+        if rc != MHD_OK:
+            raise MHDError(rc, lib().mhd_ensemble_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            lib().mhd_ensemble_destroy(self.h)
+            self.h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __len__(self):
+        return len(self.params)
+
+    def shape_left(self, prob: int):
+        p = self.params[prob]
+        g = p.ghost
+        if p.dim == 2:
+            return (8, p.ny + 2 * g, p.nx + 2 * g)
+        return (8, p.nz + 2 * g, p.ny + 2 * g, p.nx + 2 * g)
+
+    def shape_right(self, prob: int):
+        return tuple(reversed(self.shape_left(prob)[1:])) + (8,)
+
+    def init_problem(self, prob: int):
+        self._check(lib().mhd_ensemble_init_problem(self.h, int(prob)))
+
+    def set_state(self, prob: int, U: np.ndarray, layout: int = MHD_LAYOUT_LEFT):
+        U = np.ascontiguousarray(U, dtype=self.real)
+        want = self.shape_left(prob) if layout == MHD_LAYOUT_LEFT else self.shape_right(prob)
+        if U.shape != want:
+            raise ValueError(f"state shape {U.shape} != {want}")
+        self._check(lib().mhd_ensemble_set_state(self.h, int(prob), U.ctypes.data, layout,
+                                                 U.itemsize))
+
+    def get_state(self, prob: int, layout: int = MHD_LAYOUT_LEFT):
+        shape = self.shape_left(prob) if layout == MHD_LAYOUT_LEFT else self.shape_right(prob)
+        U = np.empty(shape, dtype=self.real)
+        self._check(lib().mhd_ensemble_get_state(self.h, int(prob), U.ctypes.data, layout,
+                                                 U.itemsize))
+        return U
+
+    def run(self, n: int) -> float:
+        """n iterations of every unfinished problem; returns device milliseconds."""
+        ms = ctypes.c_float()
+        self._check(lib().mhd_ensemble_run(self.h, int(n), ctypes.byref(ms)))
+        return ms.value
+
+    def time(self, prob: int):
+        t, dt, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        self._check(lib().mhd_ensemble_time(self.h, int(prob), ctypes.byref(t), ctypes.byref(dt),
+                                            ctypes.byref(it)))
+        return t.value, dt.value, it.value
+
+    def diagnostics(self, prob: int):
+        sums = (ctypes.c_double * 8)()
+        l1, mx = ctypes.c_double(), ctypes.c_double()
+        self._check(lib().mhd_ensemble_diagnostics(self.h, int(prob), sums, ctypes.byref(l1),
+                                                   ctypes.byref(mx)))
+        return np.array(list(sums)), l1.value, mx.value
+
+    def autotune(self) -> str:
+        buf = ctypes.create_string_buffer(8192)
+        self._check(lib().mhd_ensemble_autotune(self.h, buf, len(buf)))
+        return buf.value.decode()
+
+    def profile_step(self):
+        names = (ctypes.c_char_p * 16)()
+        ms = (ctypes.c_float * 16)()
+        cnt = ctypes.c_int()
+        self._check(lib().mhd_ensemble_profile_step(self.h, names, ms, 16, ctypes.byref(cnt)))
+        return [(names[q].decode(), ms[q]) for q in range(cnt.value)]
+
+    def cell_count(self) -> int:
+        a = ctypes.c_int64()
+        self._check(lib().mhd_ensemble_cell_count(self.h, ctypes.byref(a)))
+        return a.value
+
+    def launches_per_step(self) -> int:
+        n = ctypes.c_int()
+        self._check(lib().mhd_ensemble_launches_per_step(self.h, ctypes.byref(n)))
+        return n.value

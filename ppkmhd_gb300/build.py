@@ -94,6 +94,13 @@ def build(jobs: int | None = None, force: bool = False, verbose: bool = False) -
                      f"-DMHD_VARIANT_TAG={tag}", f"-DMHD_REAL={real}", f"-DMHD_FACTORY={factory}",
                      f"-DMHD_EXACT_BUILD={1 if fmad == 'false' else 0}",
                      "-c", os.path.join(CSRC, "mhd_variant.cu"), "-o", o])
+        o = os.path.join(OBJ, f"mhd_ensemble_{tag}.o")
+        objs.append(o)
+        cmds.append([nvcc(), *GENCODE, *NVCC_COMMON, f"--fmad={fmad}", "-Xptxas", "-v",
+                     f"-DMHD_VARIANT_TAG={tag}", f"-DMHD_REAL={real}",
+                     f"-DMHD_ENSEMBLE_FACTORY={factory.replace('create_core', 'create_ensemble')}",
+                     f"-DMHD_EXACT_BUILD={1 if fmad == 'false' else 0}",
+                     "-c", os.path.join(CSRC, "mhd_ensemble.cu"), "-o", o])
     o = os.path.join(OBJ, "mhd_noalloc.o")
     objs.append(o)
     cmds.append([nvcc(), *GENCODE, *NVCC_COMMON, "--fmad=true", "-Xptxas", "-v",

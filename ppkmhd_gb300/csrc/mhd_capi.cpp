@@ -18,6 +18,13 @@ struct mhd_ctx
   std::string       err;
 };
 
+struct mhd_ensemble
+{
+  mhd::EnsembleCore * core = nullptr;
+  int                 n = 0;
+  std::string         err;
+};
+
 namespace
 {
 
@@ -34,6 +41,22 @@ from_core(mhd_ctx * ctx, int rc)
 {
   if (rc != MHD_OK)
     ctx->err = ctx->core->err;
+  return rc;
+}
+
+int
+fail(mhd_ensemble * e, int rc, const std::string & msg)
+{
+  if (e)
+    e->err = msg;
+  return rc;
+}
+
+int
+from_core(mhd_ensemble * e, int rc)
+{
+  if (rc != MHD_OK)
+    e->err = e->core->err;
   return rc;
 }
 
@@ -441,6 +464,180 @@ extern "C"
   mhd_last_error(mhd_ctx * ctx)
   {
     return ctx ? ctx->err.c_str() : "null context";
+  }
+
+  // ---------------------------------------------------------------- ensembles
+
+  int
+  mhd_ensemble_create(const mhd_params * p, int n, mhd_ensemble ** out)
+  {
+    if (!p || !out || n <= 0)
+      return MHD_ERR_INVALID_ARG;
+    *out = nullptr;
+    mhd_ensemble * e = new (std::nothrow) mhd_ensemble;
+    if (!e)
+      return MHD_ERR_CUDA;
+    e->n = n;
+    *out = e;
+    for (int q = 0; q < n; ++q)
+    {
+      const std::string bad = validate_params(p[q]);
+      if (!bad.empty())
+        return fail(e, MHD_ERR_INVALID_ARG, "problem " + std::to_string(q) + ": " + bad);
+      if (p[q].implementation_version != 2)
+        return fail(e, MHD_ERR_INVALID_ARG,
+                    "problem " + std::to_string(q) + ": ensembles use implementation version 2");
+      if (p[q].dim != p[0].dim || p[q].precision != p[0].precision ||
+          p[q].fp_mode != p[0].fp_mode || p[q].device != p[0].device)
+        return fail(e, MHD_ERR_INVALID_ARG,
+                    "problem " + std::to_string(q) +
+                      ": dim, precision, fp_mode and device must be the same for all problems");
+    }
+    std::string err;
+    if (p[0].precision == MHD_FP32)
+      e->core = mhd::create_ensemble_f32(p, n, err);
+    else if (p[0].fp_mode == MHD_FP_EXACT)
+      e->core = mhd::create_ensemble_f64x(p, n, err);
+    else
+      e->core = mhd::create_ensemble_f64(p, n, err);
+    if (!e->core)
+      return fail(e, err.find("no CUDA device") != std::string::npos ? MHD_ERR_NO_DEVICE : MHD_ERR_CUDA,
+                  err);
+    return MHD_OK;
+  }
+
+  int
+  mhd_ensemble_destroy(mhd_ensemble * e)
+  {
+    if (!e)
+      return MHD_ERR_INVALID_ARG;
+    delete e->core;
+    delete e;
+    return MHD_OK;
+  }
+
+#define NEED_ENSEMBLE(e)                                                   \
+  do                                                                       \
+  {                                                                        \
+    if (!(e))                                                              \
+      return MHD_ERR_INVALID_ARG;                                          \
+    if (!(e)->core)                                                        \
+      return fail((e), MHD_ERR_INVALID_ARG, "ensemble was not created");   \
+    if (int rc_ = (e)->core->bind_device())                                \
+      return from_core((e), rc_);                                          \
+  } while (0)
+
+  static int
+  check_problem_array(mhd_ensemble * e, int prob, const void * U, int layout, int real_bytes)
+  {
+    if (prob < 0 || prob >= e->n)
+      return fail(e, MHD_ERR_INVALID_ARG, "problem index out of range");
+    if (!U)
+      return fail(e, MHD_ERR_INVALID_ARG, "null state array");
+    if (layout != MHD_LAYOUT_LEFT && layout != MHD_LAYOUT_RIGHT)
+      return fail(e, MHD_ERR_INVALID_ARG, "layout must be MHD_LAYOUT_LEFT or MHD_LAYOUT_RIGHT");
+    if (real_bytes != e->core->real_bytes())
+      return fail(e, MHD_ERR_INVALID_ARG,
+                  "real_bytes " + std::to_string(real_bytes) + " does not match the ensemble precision");
+    return MHD_OK;
+  }
+
+  int
+  mhd_ensemble_init_problem(mhd_ensemble * e, int prob)
+  {
+    NEED_ENSEMBLE(e);
+    return from_core(e, e->core->init_problem(prob));
+  }
+
+  int
+  mhd_ensemble_set_state(mhd_ensemble * e, int prob, const void * U, int layout, int real_bytes)
+  {
+    NEED_ENSEMBLE(e);
+    if (int rc = check_problem_array(e, prob, U, layout, real_bytes))
+      return rc;
+    return from_core(e, e->core->set_state(prob, U, layout));
+  }
+
+  int
+  mhd_ensemble_get_state(mhd_ensemble * e, int prob, void * U, int layout, int real_bytes)
+  {
+    NEED_ENSEMBLE(e);
+    if (int rc = check_problem_array(e, prob, U, layout, real_bytes))
+      return rc;
+    return from_core(e, e->core->get_state(prob, U, layout));
+  }
+
+  int
+  mhd_ensemble_run(mhd_ensemble * e, int nsteps, float * ms)
+  {
+    NEED_ENSEMBLE(e);
+    if (nsteps < 0)
+      return fail(e, MHD_ERR_INVALID_ARG, "nsteps must be non-negative");
+    return from_core(e, e->core->run(nsteps, ms));
+  }
+
+  int
+  mhd_ensemble_time(mhd_ensemble * e, int prob, double * t, double * dt, int * iteration)
+  {
+    NEED_ENSEMBLE(e);
+    return from_core(e, e->core->time(prob, t, dt, iteration));
+  }
+
+  int
+  mhd_ensemble_diagnostics(mhd_ensemble * e, int prob, double sums[8], double * divb_l1,
+                           double * divb_max)
+  {
+    NEED_ENSEMBLE(e);
+    if (!sums)
+      return fail(e, MHD_ERR_INVALID_ARG, "null sums");
+    return from_core(e, e->core->diagnostics(prob, sums, divb_l1, divb_max));
+  }
+
+  int
+  mhd_ensemble_autotune(mhd_ensemble * e, char * report, size_t report_len)
+  {
+    NEED_ENSEMBLE(e);
+    std::string text;
+    const int   rc = e->core->autotune(text);
+    if (report && report_len)
+    {
+      std::strncpy(report, text.c_str(), report_len - 1);
+      report[report_len - 1] = 0;
+    }
+    return from_core(e, rc);
+  }
+
+  int
+  mhd_ensemble_profile_step(mhd_ensemble * e, const char ** names, float * ms, int max, int * count)
+  {
+    NEED_ENSEMBLE(e);
+    if (!ms)
+      return fail(e, MHD_ERR_INVALID_ARG, "null ms");
+    return from_core(e, e->core->profile_step(names, ms, max, count));
+  }
+
+  int
+  mhd_ensemble_cell_count(mhd_ensemble * e, int64_t * interior)
+  {
+    NEED_ENSEMBLE(e);
+    if (!interior)
+      return fail(e, MHD_ERR_INVALID_ARG, "null output");
+    return from_core(e, e->core->cells(interior));
+  }
+
+  int
+  mhd_ensemble_launches_per_step(mhd_ensemble * e, int * n)
+  {
+    NEED_ENSEMBLE(e);
+    if (n)
+      *n = e->core->launches_per_step();
+    return MHD_OK;
+  }
+
+  const char *
+  mhd_ensemble_last_error(mhd_ensemble * e)
+  {
+    return e ? e->err.c_str() : "null ensemble";
   }
 
 } // extern "C"

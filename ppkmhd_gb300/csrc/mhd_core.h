@@ -34,10 +34,34 @@ public:
   std::string err;
 };
 
+// An ensemble of independent problems of one dimension and precision,
+// advanced together (mhd_ensemble.cuh).
+class EnsembleCore
+{
+public:
+  virtual ~EnsembleCore() {}
+  virtual int init_problem(int p) = 0;
+  virtual int set_state(int p, const void * U, int layout) = 0;
+  virtual int get_state(int p, void * U, int layout) = 0;
+  virtual int run(int nsteps, float * ms) = 0;
+  virtual int time(int p, double * t, double * dt, int * it) = 0;
+  virtual int diagnostics(int p, double sums[8], double * divb_l1, double * divb_max) = 0;
+  virtual int autotune(std::string & report) = 0;
+  virtual int profile_step(const char ** names, float * ms, int max, int * count) = 0;
+  virtual int cells(int64_t * interior) = 0;
+  virtual int launches_per_step() const = 0;
+  virtual int real_bytes() const = 0;
+  virtual int bind_device() = 0;
+  std::string err;
+};
+
 // Factories (return nullptr and fill err on failure).
 SolverCore * create_core_f64x(const mhd_params & p, std::string & err);
 SolverCore * create_core_f64(const mhd_params & p, std::string & err);
 SolverCore * create_core_f32(const mhd_params & p, std::string & err);
+EnsembleCore * create_ensemble_f64x(const mhd_params * p, int n, std::string & err);
+EnsembleCore * create_ensemble_f64(const mhd_params * p, int n, std::string & err);
+EnsembleCore * create_ensemble_f32(const mhd_params * p, int n, std::string & err);
 
 // Empty string when the parameters can be run, else the reason (mhd_capi.cpp).
 std::string validate_params(const mhd_params & p);

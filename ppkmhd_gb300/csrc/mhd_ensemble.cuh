@@ -1,0 +1,818 @@
+// Ensemble of independent MHD problems of uneven size advanced together.
+//
+// Every launch of an iteration covers all problems at once: a block map
+// assigns each CUDA block to one problem and to a block of that problem's
+// box, so one set of 8 launches advances the whole ensemble by one
+// iteration, each problem with its own CFL dt, time and stopping rule
+// (SolverBase::finished per problem).  Whole runs replay from CUDA graphs
+// without host synchronisation.  The launch shape (threads per block) of
+// every kernel is picked by a small autotuner that times the candidates on
+// the ensemble itself.
+//
+// The reference has no ensemble mode: each problem is exactly the
+// single-problem iteration of mhd_kernels.cuh (implementation version 2),
+// and the tests check bitwise agreement with independent single runs.
+#pragma once
+
+#include <algorithm>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "mhd_core.h"
+#include "mhd_solver.cuh"
+
+namespace mhd
+{
+inline namespace MHD_VARIANT_TAG
+{
+
+// (problem, block index inside the problem's box) of every CUDA block
+struct BlockRef
+{
+  int p, b;
+};
+
+template <class R>
+__device__ __forceinline__ Buffers<R>
+buffers_of(const Buffers<R> * Bs, int p, int parity)
+{
+  Buffers<R> B = Bs[p];
+  if (parity)
+  {
+    R * t = B.Uin;
+    B.Uin = B.Uout;
+    B.Uout = t;
+  }
+  return B;
+}
+
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+kb_boundaries(const Grid<R> * Gs, const Buffers<R> * Bs, const BlockRef * map, int parity)
+{
+  const BlockRef   m = map[blockIdx.x];
+  const Buffers<R> B = buffers_of(Bs, m.p, parity);
+  boundaries_body<R, DIM>(Gs[m.p], B.Uin, B.st, 0, m.b * (int64_t)blockDim.x + threadIdx.x,
+                          m.b == 0 && threadIdx.x == 0);
+}
+
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+kb_prim_dt(const Grid<R> * Gs, const Buffers<R> * Bs, const BlockRef * map, int parity)
+{
+  const BlockRef   m = map[blockIdx.x];
+  const Buffers<R> B = buffers_of(Bs, m.p, parity);
+  prim_dt_body<R, DIM>(Gs[m.p], B.Uin, B.Q, B.st, 0, m.b * (int64_t)blockDim.x + threadIdx.x);
+}
+
+template <class R>
+__global__ void
+kb_finalize_dt(const Grid<R> * Gs, const Buffers<R> * Bs, int nprob)
+{
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < nprob)
+    finalize_dt_body<R>(Gs[p], Bs[p].st, 0);
+}
+
+template <class R>
+__global__ void
+kb_advance(const Buffers<R> * Bs, int nprob)
+{
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nprob)
+    return;
+  DevState * st = Bs[p].st;
+  if (step_finished(st))
+    return;
+  st->it += 1;
+  st->t += st->dt;
+}
+
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+kb_trace(const Grid<R> * Gs, const Buffers<R> * Bs, const BlockRef * map, int parity)
+{
+  const BlockRef m = map[blockIdx.x];
+  trace_body<R, DIM>(Gs[m.p], buffers_of(Bs, m.p, parity), m.b * (int64_t)blockDim.x + threadIdx.x);
+}
+
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+kb_flux(const Grid<R> * Gs, const Buffers<R> * Bs, const BlockRef * map, int parity)
+{
+  const BlockRef m = map[blockIdx.x];
+  flux_body<R, DIM>(Gs[m.p], buffers_of(Bs, m.p, parity), m.b * (int64_t)blockDim.x + threadIdx.x,
+                    blockIdx.y);
+}
+
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+kb_emf(const Grid<R> * Gs, const Buffers<R> * Bs, const BlockRef * map, int parity)
+{
+  const BlockRef m = map[blockIdx.x];
+  emf_body<R, DIM>(Gs[m.p], buffers_of(Bs, m.p, parity), m.b * (int64_t)blockDim.x + threadIdx.x,
+                   blockIdx.y);
+}
+
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+kb_update(const Grid<R> * Gs, const Buffers<R> * Bs, const BlockRef * map, int parity)
+{
+  const BlockRef m = map[blockIdx.x];
+  update_body<R, DIM>(Gs[m.p], buffers_of(Bs, m.p, parity), m.b * (int64_t)blockDim.x + threadIdx.x);
+}
+
+#define MHD_ECK(call)                                                                 \
+  do                                                                                  \
+  {                                                                                   \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess)                                                            \
+    {                                                                                 \
+      err = std::string(#call) + ": " + cudaGetErrorString(e_);                       \
+      return MHD_ERR_CUDA;                                                            \
+    }                                                                                 \
+  } while (0)
+
+template <class R>
+class EnsembleImpl final : public EnsembleCore
+{
+public:
+  // launch kinds with their own block map and launch shape
+  enum Kind
+  {
+    K_BC = 0,
+    K_PRIM,
+    K_TRACE,
+    K_FLUX,
+    K_EMF,
+    K_UPDATE,
+    K_COUNT
+  };
+  static constexpr const char * kKindName[K_COUNT] = { "boundaries", "prim_dt", "trace",
+                                                       "flux",       "emf",     "update" };
+
+  std::vector<mhd_params> P;
+  std::vector<Grid<R>>    G;     // host copies
+  std::vector<Buffers<R>> B;     // host copies (parity 0)
+  Grid<R> *               dG = nullptr;
+  Buffers<R> *            dB = nullptr;
+  R *                     arena = nullptr;
+  DevState *              st = nullptr;
+  DevState *              st_host = nullptr;
+  int                     dim = 2, n = 0;
+  int                     threads[K_COUNT] = { 256, 256, 128, 128, 128, 256 };
+  BlockRef *              map[K_COUNT] = {};
+  unsigned                nblk[K_COUNT] = {};
+  cudaStream_t            stream = nullptr;
+  cudaGraphExec_t         graph_pair[2] = { nullptr, nullptr };
+  int64_t                 launched = 0;
+
+  ~EnsembleImpl() override
+  {
+    drop_graphs();
+    for (auto & m : map)
+      if (m)
+        cudaFree(m);
+    if (dG)
+      cudaFree(dG);
+    if (dB)
+      cudaFree(dB);
+    if (arena)
+      cudaFree(arena);
+    if (st)
+      cudaFree(st);
+    if (st_host)
+      cudaFreeHost(st_host);
+    if (stream)
+      cudaStreamDestroy(stream);
+  }
+
+  void
+  drop_graphs()
+  {
+    for (auto & g : graph_pair)
+      if (g)
+      {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+  }
+
+  int
+  real_bytes() const override
+  {
+    return (int)sizeof(R);
+  }
+
+  int
+  bind_device() override
+  {
+    MHD_ECK(cudaSetDevice(P[0].device));
+    return MHD_OK;
+  }
+
+  static int64_t
+  box_count(const Grid<R> & g, Kind k)
+  {
+    switch (k)
+    {
+    case K_BC:
+      return g.box[BOX_ALL].count();
+    case K_PRIM:
+      return g.box[BOX_PRIM].count();
+    case K_TRACE:
+      return g.box[BOX_TRACE].count();
+    case K_FLUX:
+    case K_EMF:
+      return g.box[BOX_FACE].count();
+    default:
+      return g.box[BOX_INTERIOR].count();
+    }
+  }
+
+  int
+  build_map(Kind k)
+  {
+    std::vector<BlockRef> h;
+    for (int p = 0; p < n; ++p)
+    {
+      const int64_t cnt = box_count(G[p], k);
+      const int64_t nb = (cnt + threads[k] - 1) / threads[k];
+      for (int64_t b = 0; b < nb; ++b)
+        h.push_back(BlockRef{ p, (int)b });
+    }
+    if (map[k])
+      MHD_ECK(cudaFree(map[k]));
+    MHD_ECK(cudaMalloc(&map[k], h.size() * sizeof(BlockRef)));
+    MHD_ECK(cudaMemcpy(map[k], h.data(), h.size() * sizeof(BlockRef), cudaMemcpyHostToDevice));
+    nblk[k] = (unsigned)h.size();
+    return MHD_OK;
+  }
+
+  int
+  setup(const mhd_params * params, int nprob)
+  {
+    n = nprob;
+    dim = params[0].dim;
+    P.assign(params, params + nprob);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    {
+      err = "no CUDA device available";
+      return MHD_ERR_NO_DEVICE;
+    }
+    MHD_ECK(cudaSetDevice(params[0].device));
+    MHD_ECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    // one arena: per problem U, U2, Q, Q2, S (dim x 8), E, F (dim x nf), Em
+    const int          ne = dim == 3 ? 3 : 1, nf = dim == 3 ? 5 : 6;
+    const int          planes = 8 * 4 + 8 * dim + ne + nf * dim + ne;
+    std::vector<size_t> off(n);
+    size_t              total = 0;
+    G.resize(n);
+    for (int p = 0; p < n; ++p)
+    {
+      G[p] = make_grid<R>(P[p]);
+      off[p] = total;
+      const size_t cells = (size_t)G[p].sv;
+      total += ((cells * planes + 63) / 64) * 64; // 256-byte aligned problems (FP32)
+    }
+    MHD_ECK(cudaMalloc(&arena, total * sizeof(R)));
+    MHD_ECK(cudaMemsetAsync(arena, 0, total * sizeof(R), stream));
+    MHD_ECK(cudaMalloc(&st, n * sizeof(DevState)));
+    MHD_ECK(cudaMallocHost(&st_host, n * sizeof(DevState)));
+    B.resize(n);
+    for (int p = 0; p < n; ++p)
+    {
+      R *          a = arena + off[p];
+      const size_t c = (size_t)G[p].sv;
+      B[p].Uin = a;
+      a += 8 * c;
+      B[p].Uout = a;
+      a += 8 * c;
+      B[p].Q = a;
+      a += 8 * c;
+      B[p].Q2 = a;
+      a += 8 * c;
+      B[p].S = a;
+      a += 8 * dim * c;
+      B[p].E = a;
+      a += ne * c;
+      B[p].F = a;
+      a += nf * dim * c;
+      B[p].Em = a;
+      B[p].st = st + p;
+    }
+    MHD_ECK(cudaMalloc(&dG, n * sizeof(Grid<R>)));
+    MHD_ECK(cudaMalloc(&dB, n * sizeof(Buffers<R>)));
+    MHD_ECK(cudaMemcpy(dG, G.data(), n * sizeof(Grid<R>), cudaMemcpyHostToDevice));
+    MHD_ECK(cudaMemcpy(dB, B.data(), n * sizeof(Buffers<R>), cudaMemcpyHostToDevice));
+    for (int p = 0; p < n; ++p)
+      reset_record(p);
+    MHD_ECK(cudaMemcpyAsync(st, st_host, n * sizeof(DevState), cudaMemcpyHostToDevice, stream));
+    for (int k = 0; k < K_COUNT; ++k)
+      if (int rc = build_map((Kind)k))
+        return rc;
+    MHD_ECK(cudaStreamSynchronize(stream));
+    return MHD_OK;
+  }
+
+  void
+  reset_record(int p)
+  {
+    DevState h{};
+    h.t = P[p].tCurrent;
+    h.tEnd = P[p].tEnd;
+    h.nStepmax = P[p].nStepmax;
+    st_host[p] = h;
+  }
+
+  void
+  launch_kind(Kind k, int parity)
+  {
+    const unsigned nb = nblk[k];
+    const int      th = threads[k];
+    if (dim == 2)
+    {
+      switch (k)
+      {
+      case K_BC:
+        kb_boundaries<R, 2><<<nb, th, 0, stream>>>(dG, dB, map[k], parity);
+        break;
+      case K_PRIM:
+        kb_prim_dt<R, 2><<<nb, th, 0, stream>>>(dG, dB, map[k], parity);
+        break;
+      case K_TRACE:
+        kb_trace<R, 2><<<nb, th, 0, stream>>>(dG, dB, map[k], parity);
+        break;
+      case K_FLUX:
+        kb_flux<R, 2><<<dim3(nb, 2), th, 0, stream>>>(dG, dB, map[k], parity);
+        break;
+      case K_EMF:
+        kb_emf<R, 2><<<dim3(nb, 1), th, 0, stream>>>(dG, dB, map[k], parity);
+        break;
+      default:
+        kb_update<R, 2><<<nb, th, 0, stream>>>(dG, dB, map[k], parity);
+      }
+    }
+    else
+    {
+      switch (k)
+      {
+      case K_BC:
+        kb_boundaries<R, 3><<<nb, th, 0, stream>>>(dG, dB, map[k], parity);
+        break;
+      case K_PRIM:
+        kb_prim_dt<R, 3><<<nb, th, 0, stream>>>(dG, dB, map[k], parity);
+        break;
+      case K_TRACE:
+        kb_trace<R, 3><<<nb, th, 0, stream>>>(dG, dB, map[k], parity);
+        break;
+      case K_FLUX:
+        kb_flux<R, 3><<<dim3(nb, 3), th, 0, stream>>>(dG, dB, map[k], parity);
+        break;
+      case K_EMF:
+        kb_emf<R, 3><<<dim3(nb, 3), th, 0, stream>>>(dG, dB, map[k], parity);
+        break;
+      default:
+        kb_update<R, 3><<<nb, th, 0, stream>>>(dG, dB, map[k], parity);
+      }
+    }
+  }
+
+  void
+  enqueue_step(int parity)
+  {
+    launch_kind(K_BC, parity);
+    launch_kind(K_PRIM, parity);
+    kb_finalize_dt<R><<<(n + 127) / 128, 128, 0, stream>>>(dG, dB, n);
+    launch_kind(K_TRACE, parity);
+    launch_kind(K_FLUX, parity);
+    launch_kind(K_EMF, parity);
+    launch_kind(K_UPDATE, parity);
+    kb_advance<R><<<(n + 127) / 128, 128, 0, stream>>>(dB, n);
+  }
+
+  int
+  launches_per_step() const override
+  {
+    return 8;
+  }
+
+  int
+  check_launch()
+  {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+    {
+      err = std::string("kernel launch: ") + cudaGetErrorString(e);
+      return MHD_ERR_CUDA;
+    }
+    return MHD_OK;
+  }
+
+  int
+  build_graphs()
+  {
+    if (graph_pair[0])
+      return MHD_OK;
+    for (int parity = 0; parity < 2; ++parity)
+    {
+      cudaGraph_t g = nullptr;
+      MHD_ECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+      enqueue_step(parity);
+      enqueue_step(1 - parity);
+      cudaError_t le = cudaGetLastError();
+      cudaError_t ce = cudaStreamEndCapture(stream, &g);
+      if (le != cudaSuccess || ce != cudaSuccess)
+      {
+        err = std::string("graph capture: ") + cudaGetErrorString(le != cudaSuccess ? le : ce);
+        if (g)
+          cudaGraphDestroy(g);
+        return MHD_ERR_CUDA;
+      }
+      cudaError_t ie = cudaGraphInstantiate(&graph_pair[parity], g, 0);
+      cudaGraphDestroy(g);
+      if (ie != cudaSuccess)
+      {
+        err = std::string("graph instantiate: ") + cudaGetErrorString(ie);
+        return MHD_ERR_CUDA;
+      }
+    }
+    return MHD_OK;
+  }
+
+  // Per problem: boundaries + U2 = U + primitives + dt (SolverMHDMuscl.h:393-402)
+  int
+  apply_init(int p)
+  {
+    const Grid<R> & g = G[p];
+    const int64_t   nall = g.box[BOX_ALL].count(), nprim = g.box[BOX_PRIM].count();
+    if (dim == 2)
+    {
+      k_boundaries<R, 2><<<(unsigned)((nall + 255) / 256), 256, 0, stream>>>(g, B[p].Uin, B[p].st, 1);
+      k_prim_dt<R, 2><<<(unsigned)((nprim + 255) / 256), 256, 0, stream>>>(g, B[p].Uin, B[p].Q,
+                                                                             B[p].st, 1);
+    }
+    else
+    {
+      k_boundaries<R, 3><<<(unsigned)((nall + 255) / 256), 256, 0, stream>>>(g, B[p].Uin, B[p].st, 1);
+      k_prim_dt<R, 3><<<(unsigned)((nprim + 255) / 256), 256, 0, stream>>>(g, B[p].Uin, B[p].Q,
+                                                                             B[p].st, 1);
+    }
+    k_finalize_dt<R><<<1, 1, 0, stream>>>(g, B[p].st, 1);
+    MHD_ECK(cudaMemcpyAsync(B[p].Uout, B[p].Uin, (size_t)g.sv * NV * sizeof(R),
+                            cudaMemcpyDeviceToDevice, stream));
+    return check_launch();
+  }
+
+  int
+  check_problem(int p)
+  {
+    if (p < 0 || p >= n)
+    {
+      err = "problem index out of range";
+      return MHD_ERR_INVALID_ARG;
+    }
+    return MHD_OK;
+  }
+
+  static unsigned
+  blocks_for(int64_t cnt, int th)
+  {
+    return (unsigned)((cnt + th - 1) / th);
+  }
+
+  // Host array -> device state of problem p; LayoutRight goes through the
+  // problem's primitive array as staging (rewritten by the next iteration).
+  int
+  upload(int p, const void * host, int layout)
+  {
+    const size_t bytes = (size_t)G[p].sv * NV * sizeof(R);
+    if (layout == MHD_LAYOUT_LEFT)
+    {
+      MHD_ECK(cudaMemcpyAsync(B[p].Uin, host, bytes, cudaMemcpyHostToDevice, stream));
+      return MHD_OK;
+    }
+    MHD_ECK(cudaMemcpyAsync(B[p].Q, host, bytes, cudaMemcpyHostToDevice, stream));
+    k_transpose<R><<<blocks_for(G[p].sv * NV, 256), 256, 0, stream>>>(G[p], B[p].Q, B[p].Uin, 0);
+    return check_launch();
+  }
+
+  int
+  download(int p, const R * src, void * host, int layout)
+  {
+    const size_t bytes = (size_t)G[p].sv * NV * sizeof(R);
+    if (layout == MHD_LAYOUT_LEFT)
+    {
+      MHD_ECK(cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, stream));
+      return MHD_OK;
+    }
+    k_transpose<R><<<blocks_for(G[p].sv * NV, 256), 256, 0, stream>>>(G[p], src, B[p].Q, 1);
+    if (int rc = check_launch())
+      return rc;
+    MHD_ECK(cudaMemcpyAsync(host, B[p].Q, bytes, cudaMemcpyDeviceToHost, stream));
+    return MHD_OK;
+  }
+
+  int
+  set_state(int p, const void * U, int layout) override
+  {
+    if (int rc = check_problem(p))
+      return rc;
+    if (int rc = upload(p, U, layout))
+      return rc;
+    reset_record(p);
+    MHD_ECK(cudaMemcpyAsync(st + p, st_host + p, sizeof(DevState), cudaMemcpyHostToDevice, stream));
+    if (int rc = apply_init(p))
+      return rc;
+    MHD_ECK(cudaStreamSynchronize(stream));
+    return MHD_OK;
+  }
+
+  int
+  init_problem(int p) override
+  {
+    if (int rc = check_problem(p))
+      return rc;
+    std::vector<double> h((size_t)G[p].sv * NV);
+    init_orszag_tang_host(P[p], h.data());
+    if constexpr (sizeof(R) == 8)
+      return set_state(p, h.data(), MHD_LAYOUT_LEFT);
+    std::vector<float> f(h.size());
+    for (size_t q = 0; q < h.size(); ++q)
+      f[q] = (float)h[q];
+    return set_state(p, f.data(), MHD_LAYOUT_LEFT);
+  }
+
+  int
+  read_records()
+  {
+    MHD_ECK(cudaMemcpyAsync(st_host, st, n * sizeof(DevState), cudaMemcpyDeviceToHost, stream));
+    MHD_ECK(cudaStreamSynchronize(stream));
+    return MHD_OK;
+  }
+
+  // The array the next iteration of problem p reads (SolverMHDMuscl.h:791-805).
+  R *
+  current(int p) const
+  {
+    return (st_host[p].it % 2 == 0) ? B[p].Uin : B[p].Uout;
+  }
+
+  int
+  get_state(int p, void * U, int layout) override
+  {
+    if (int rc = check_problem(p))
+      return rc;
+    if (int rc = read_records())
+      return rc;
+    R *             cur = current(p);
+    const Grid<R> & g = G[p];
+    const int64_t   nall = g.box[BOX_ALL].count();
+    // ghost refresh from the interior: the next iteration starts with the same fill
+    if (dim == 2)
+      k_boundaries<R, 2><<<blocks_for(nall, 256), 256, 0, stream>>>(g, cur, B[p].st, 1);
+    else
+      k_boundaries<R, 3><<<blocks_for(nall, 256), 256, 0, stream>>>(g, cur, B[p].st, 1);
+    if (int rc = check_launch())
+      return rc;
+    if (int rc = download(p, cur, U, layout))
+      return rc;
+    MHD_ECK(cudaStreamSynchronize(stream));
+    return MHD_OK;
+  }
+
+  // FP64 conserved totals and div B of problem p on the GPU (the conventions
+  // of the single-problem diagnostics: plain sums over interior cells, mean
+  // and max |div B|); the problem's
+  // slope array is the scratch for the block partials (rewritten by the
+  // next iteration).
+  int
+  diagnostics(int p, double sums[8], double * divb_l1, double * divb_max) override
+  {
+    if (int rc = check_problem(p))
+      return rc;
+    if (int rc = read_records())
+      return rc;
+    const Grid<R> & g = G[p];
+    const unsigned  nb = std::min(1024u, blocks_for(g.box[BOX_INTERIOR].count(), 256));
+    double *        partial = reinterpret_cast<double *>(B[p].S);
+    double *        out = partial + (size_t)nb * 10;
+    const int64_t   nall = g.box[BOX_ALL].count();
+    if (dim == 2)
+    {
+      k_boundaries<R, 2><<<blocks_for(nall, 256), 256, 0, stream>>>(g, current(p), B[p].st, 1);
+      k_diag<R, 2><<<nb, 256, 0, stream>>>(g, current(p), partial);
+    }
+    else
+    {
+      k_boundaries<R, 3><<<blocks_for(nall, 256), 256, 0, stream>>>(g, current(p), B[p].st, 1);
+      k_diag<R, 3><<<nb, 256, 0, stream>>>(g, current(p), partial);
+    }
+    k_diag_final<<<1, 32, 0, stream>>>(partial, (int)nb, out);
+    if (int rc = check_launch())
+      return rc;
+    double h[10];
+    MHD_ECK(cudaMemcpyAsync(h, out, sizeof h, cudaMemcpyDeviceToHost, stream));
+    MHD_ECK(cudaStreamSynchronize(stream));
+    for (int v = 0; v < 8; ++v)
+      sums[v] = h[v];
+    if (divb_l1)
+      *divb_l1 = h[8] / (double)g.box[BOX_INTERIOR].count();
+    if (divb_max)
+      *divb_max = h[9];
+    return MHD_OK;
+  }
+
+  int
+  time(int p, double * t, double * dt, int * it) override
+  {
+    if (int rc = check_problem(p))
+      return rc;
+    if (int rc = read_records())
+      return rc;
+    if (t)
+      *t = st_host[p].t;
+    if (dt)
+      *dt = st_host[p].dt;
+    if (it)
+      *it = st_host[p].it;
+    return MHD_OK;
+  }
+
+  // All problems start from iteration 0 together; a problem that finishes
+  // early keeps its state while the others go on.
+  int
+  run(int nsteps, float * ms) override
+  {
+    if (int rc = build_graphs())
+      return rc;
+    if (int rc = read_records())
+      return rc;
+    int parity = 0;
+    for (int p = 0; p < n; ++p)
+      if (st_host[p].it % 2 != st_host[0].it % 2)
+      {
+        err = "problems are at iterations of different parity; set their states again";
+        return MHD_ERR_INVALID_ARG;
+      }
+    parity = st_host[0].it % 2;
+    cudaEvent_t e0, e1;
+    MHD_ECK(cudaEventCreate(&e0));
+    MHD_ECK(cudaEventCreate(&e1));
+    MHD_ECK(cudaEventRecord(e0, stream));
+    int left = nsteps;
+    while (left >= 2)
+    {
+      MHD_ECK(cudaGraphLaunch(graph_pair[parity], stream));
+      left -= 2;
+    }
+    if (left)
+    {
+      enqueue_step(parity);
+      if (int rc = check_launch())
+        return rc;
+    }
+    MHD_ECK(cudaEventRecord(e1, stream));
+    MHD_ECK(cudaEventSynchronize(e1));
+    float el = 0.f;
+    MHD_ECK(cudaEventElapsedTime(&el, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (ms)
+      *ms = el;
+    if (int rc = read_records())
+      return rc;
+    for (int p = 0; p < n; ++p)
+      if (st_host[p].status & STATUS_NUMERIC)
+      {
+        err = "problem " + std::to_string(p) + ": non-finite or non-positive state detected";
+        return MHD_ERR_NUMERIC;
+      }
+    return MHD_OK;
+  }
+
+  // Time each launch kind with every candidate block size on the current
+  // states (kernels other than the dt bookkeeping are idempotent for a
+  // fixed input), keep the fastest, rebuild the block maps and graphs.
+  int
+  autotune(std::string & report) override
+  {
+    if (int rc = read_records())
+      return rc;
+    const int parity = st_host[0].it % 2;
+    const int cand[3] = { 64, 128, 256 };
+    cudaEvent_t e0, e1;
+    MHD_ECK(cudaEventCreate(&e0));
+    MHD_ECK(cudaEventCreate(&e1));
+    char line[160];
+    // primitives and dt are needed by the kernels downstream of them
+    launch_kind(K_BC, parity);
+    launch_kind(K_PRIM, parity);
+    kb_finalize_dt<R><<<(n + 127) / 128, 128, 0, stream>>>(dG, dB, n);
+    for (int k = 0; k < K_COUNT; ++k)
+    {
+      float best = 1e30f;
+      int   best_t = threads[k];
+      for (int c : cand)
+      {
+        threads[k] = c;
+        if (int rc = build_map((Kind)k))
+          return rc;
+        launch_kind((Kind)k, parity); // warm
+        MHD_ECK(cudaEventRecord(e0, stream));
+        for (int r = 0; r < 3; ++r)
+          launch_kind((Kind)k, parity);
+        MHD_ECK(cudaEventRecord(e1, stream));
+        MHD_ECK(cudaEventSynchronize(e1));
+        float el = 0.f;
+        MHD_ECK(cudaEventElapsedTime(&el, e0, e1));
+        if (int rc = check_launch())
+          return rc;
+        std::snprintf(line, sizeof line, "%s threads=%d: %.3f ms\n", kKindName[k], c, el / 3);
+        report += line;
+        if (el < best)
+        {
+          best = el;
+          best_t = c;
+        }
+      }
+      threads[k] = best_t;
+      if (int rc = build_map((Kind)k))
+        return rc;
+      std::snprintf(line, sizeof line, "-> %s uses %d threads per block\n", kKindName[k], best_t);
+      report += line;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    drop_graphs();
+    // the tuning launches rewrote boundary cells and primitives of the
+    // current states only; restore the invariant of a fresh iteration
+    MHD_ECK(cudaStreamSynchronize(stream));
+    return MHD_OK;
+  }
+
+  // Time each launch of one iteration separately (CUDA events around each
+  // launch on the ensemble's stream); the iteration is a real one.
+  int
+  profile_step(const char ** names, float * ms, int max, int * count) override
+  {
+    if (int rc = read_records())
+      return rc;
+    const int   parity = st_host[0].it % 2;
+    cudaEvent_t ev[9];
+    for (auto & e : ev)
+      MHD_ECK(cudaEventCreate(&e));
+    static const char * kNames[8] = { "kb_boundaries", "kb_prim_dt", "kb_finalize_dt", "kb_trace",
+                                      "kb_flux",       "kb_emf",     "kb_update",      "kb_advance" };
+    MHD_ECK(cudaEventRecord(ev[0], stream));
+    launch_kind(K_BC, parity);
+    MHD_ECK(cudaEventRecord(ev[1], stream));
+    launch_kind(K_PRIM, parity);
+    MHD_ECK(cudaEventRecord(ev[2], stream));
+    kb_finalize_dt<R><<<(n + 127) / 128, 128, 0, stream>>>(dG, dB, n);
+    MHD_ECK(cudaEventRecord(ev[3], stream));
+    launch_kind(K_TRACE, parity);
+    MHD_ECK(cudaEventRecord(ev[4], stream));
+    launch_kind(K_FLUX, parity);
+    MHD_ECK(cudaEventRecord(ev[5], stream));
+    launch_kind(K_EMF, parity);
+    MHD_ECK(cudaEventRecord(ev[6], stream));
+    launch_kind(K_UPDATE, parity);
+    MHD_ECK(cudaEventRecord(ev[7], stream));
+    kb_advance<R><<<(n + 127) / 128, 128, 0, stream>>>(dB, n);
+    MHD_ECK(cudaEventRecord(ev[8], stream));
+    if (int rc = check_launch())
+      return rc;
+    MHD_ECK(cudaEventSynchronize(ev[8]));
+    for (int q = 0; q < 8 && q < max; ++q)
+    {
+      MHD_ECK(cudaEventElapsedTime(&ms[q], ev[q], ev[q + 1]));
+      if (names)
+        names[q] = kNames[q];
+    }
+    for (auto & e : ev)
+      cudaEventDestroy(e);
+    if (count)
+      *count = 8;
+    return MHD_OK;
+  }
+
+  int
+  cells(int64_t * interior) override
+  {
+    int64_t s = 0;
+    for (int p = 0; p < n; ++p)
+      s += G[p].box[BOX_INTERIOR].count();
+    *interior = s;
+    return MHD_OK;
+  }
+};
+
+#undef MHD_ECK
+
+} // namespace MHD_VARIANT_TAG
+} // namespace mhd

@@ -227,16 +227,17 @@ bc_source(int c, int n, int g, int type, bool hi, bool & flip)
 // interior value at the composition of the per-axis source maps, multiplied
 // by the per-axis reflection signs (normal velocity and normal field).
 template <class R, int DIM>
-__global__ void __launch_bounds__(256)
-k_boundaries(const Grid<R> G, R * __restrict__ U, DevState * st, int force)
+__device__ __forceinline__ void
+boundaries_body(const Grid<R> & G, R * __restrict__ U, DevState * st, int force, int64_t idx,
+                bool first)
 {
   if (!force && step_finished(st))
     return;
-  if (blockIdx.x == 0 && threadIdx.x == 0)
+  if (first)
     st->invdt_bits = 0ull; // reset the CFL reduction of this iteration
   const Box & b = G.box[BOX_ALL];
   int       i, j, k;
-  if (!box_cell(b, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
+  if (!box_cell(b, idx, i, j, k))
     return;
   const int g = G.g;
   const bool gx = i < g || i >= G.nx + g;
@@ -267,6 +268,14 @@ k_boundaries(const Grid<R> G, R * __restrict__ U, DevState * st, int force)
   }
 }
 
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+k_boundaries(const Grid<R> G, R * __restrict__ U, DevState * st, int force)
+{
+  boundaries_body<R, DIM>(G, U, st, force, blockIdx.x * (int64_t)blockDim.x + threadIdx.x,
+                          blockIdx.x == 0 && threadIdx.x == 0);
+}
+
 // ---------------------------------------------------------------- primitives + CFL
 
 template <class T>
@@ -287,8 +296,9 @@ warp_max(T v)
 // orders like the value for non-negative doubles) and is order-independent,
 // so dt is bitwise the reference's.
 template <class R, int DIM>
-__global__ void __launch_bounds__(256)
-k_prim_dt(const Grid<R> G, const R * __restrict__ U, R * __restrict__ Q, DevState * st, int force)
+__device__ __forceinline__ void
+prim_dt_body(const Grid<R> & G, const R * __restrict__ U, R * __restrict__ Q, DevState * st,
+             int force, int64_t idx)
 {
   if (!force && step_finished(st))
     return;
@@ -296,7 +306,7 @@ k_prim_dt(const Grid<R> G, const R * __restrict__ U, R * __restrict__ Q, DevStat
   int       i, j, k;
   R         rate = R(0);
   bool      bad = false;
-  if (box_cell(b, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
+  if (box_cell(b, idx, i, j, k))
   {
     const int64_t c = cell_at(G, i, j, k);
     const int64_t sv = G.sv;
@@ -395,12 +405,19 @@ k_prim_dt(const Grid<R> G, const R * __restrict__ U, R * __restrict__ Q, DevStat
   }
 }
 
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+k_prim_dt(const Grid<R> G, const R * __restrict__ U, R * __restrict__ Q, DevState * st, int force)
+{
+  prim_dt_body<R, DIM>(G, U, Q, st, force, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
 // compute_dt_local (SolverMHDMuscl.h:722-741) and the clip of
 // SolverBase::compute_dt (SolverBase.cpp:148-179); dtdx = m_dt / dx
 // (SolverMHDMuscl.cpp:390-391).
 template <class R>
-__global__ void
-k_finalize_dt(const Grid<R> G, DevState * st, int force)
+__device__ __forceinline__ void
+finalize_dt_body(const Grid<R> & G, DevState * st, int force)
 {
   if (!force && step_finished(st))
     return;
@@ -421,6 +438,13 @@ k_finalize_dt(const Grid<R> G, DevState * st, int force)
   st->fdtdz = (float)st->dtdz;
   if (!(invDt > 0.0) || !isfinite(dt))
     st->status |= STATUS_NUMERIC;
+}
+
+template <class R>
+__global__ void
+k_finalize_dt(const Grid<R> G, DevState * st, int force)
+{
+  finalize_dt_body<R>(G, st, force);
 }
 
 template <class R>
@@ -446,15 +470,15 @@ k_advance(DevState * st)
 // Slopes and Q2 are only consumed on [g-1, size-g]^DIM, the edge field on
 // [g-1, size-g+1]^DIM.
 template <class R, int DIM>
-__global__ void __launch_bounds__(128)
-k_trace(const Grid<R> G, Buffers<R> B)
+__device__ __forceinline__ void
+trace_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
 {
   if (step_finished(B.st))
     return;
   const int g = G.g;
   const Box & b = G.box[BOX_TRACE];
   int       i, j, k;
-  if (!box_cell(b, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
+  if (!box_cell(b, idx, i, j, k))
     return;
   const int64_t sv = G.sv, sj = G.sj, sk = G.sk;
   const int64_t c = cell_at(G, i, j, k);
@@ -610,6 +634,13 @@ k_trace(const Grid<R> G, Buffers<R> B)
   Q2[c + IC * sv] = C + R(0.5) * sC0;
 }
 
+template <class R, int DIM>
+__global__ void __launch_bounds__(128)
+k_trace(const Grid<R> G, Buffers<R> B)
+{
+  trace_body<R, DIM>(G, B, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
 // Half-step predictor of the face-centred field on face c normal to d
 // (ComputeSourceFaceMagFunctor2D, MHDRunFunctors2D.h:319-370;
 // ComputeSourceFaceMagFunctor3D, MHDRunFunctors3D.h:367-436), evaluated
@@ -697,22 +728,27 @@ flux_face(const Grid<R> & G, const Buffers<R> & B, int i, int j, int k)
 }
 
 template <class R, int DIM>
-__global__ void __launch_bounds__(128)
-k_flux(const Grid<R> G, Buffers<R> B)
+__device__ __forceinline__ void
+flux_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx, int dir)
 {
   if (step_finished(B.st))
     return;
-  const int g = G.g;
-  const Box & b = G.box[BOX_FACE];
-  int       i, j, k;
-  if (!box_cell(b, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
+  int i, j, k;
+  if (!box_cell(G.box[BOX_FACE], idx, i, j, k))
     return;
-  if (blockIdx.y == 0)
+  if (dir == 0)
     flux_face<R, DIM, 0>(G, B, i, j, k);
-  else if (blockIdx.y == 1)
+  else if (dir == 1)
     flux_face<R, DIM, 1>(G, B, i, j, k);
   else if constexpr (DIM == 3)
     flux_face<R, DIM, 2>(G, B, i, j, k);
+}
+
+template <class R, int DIM>
+__global__ void __launch_bounds__(128)
+k_flux(const Grid<R> G, Buffers<R> B)
+{
+  flux_body<R, DIM>(G, B, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, blockIdx.y);
 }
 
 // ---------------------------------------------------------------- edge EMFs
@@ -823,24 +859,29 @@ emf_edge(const Grid<R> & G, const Buffers<R> & B, int i, int j, int k)
 }
 
 template <class R, int DIM>
-__global__ void __launch_bounds__(128)
-k_emf(const Grid<R> G, Buffers<R> B)
+__device__ __forceinline__ void
+emf_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx, int dir)
 {
   if (step_finished(B.st))
     return;
-  const int g = G.g;
-  const Box & b = G.box[BOX_FACE];
-  int       i, j, k;
-  if (!box_cell(b, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
+  int i, j, k;
+  if (!box_cell(G.box[BOX_FACE], idx, i, j, k))
     return;
   if constexpr (DIM == 2)
     emf_edge<R, 2, 2>(G, B, i, j, k);
-  else if (blockIdx.y == 0)
+  else if (dir == 0)
     emf_edge<R, 3, 0>(G, B, i, j, k);
-  else if (blockIdx.y == 1)
+  else if (dir == 1)
     emf_edge<R, 3, 1>(G, B, i, j, k);
   else
     emf_edge<R, 3, 2>(G, B, i, j, k);
+}
+
+template <class R, int DIM>
+__global__ void __launch_bounds__(128)
+k_emf(const Grid<R> G, Buffers<R> B)
+{
+  emf_body<R, DIM>(G, B, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, blockIdx.y);
 }
 
 // ---------------------------------------------------------------- update
@@ -855,15 +896,14 @@ k_emf(const Grid<R> G, Buffers<R> B)
 //       By: - Ex(k) dt/dz + Ex(k+1) dt/dz + Ez(i) dt/dx - Ez(i+1) dt/dx
 //       Bz: + Ex(j) dt/dy - Ex(j+1) dt/dy - Ey(i) dt/dx + Ey(i+1) dt/dx
 template <class R, int DIM>
-__global__ void __launch_bounds__(256)
-k_update(const Grid<R> G, Buffers<R> B)
+__device__ __forceinline__ void
+update_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
 {
   if (step_finished(B.st))
     return;
-  const int g = G.g;
   const Box & b = G.box[BOX_INTERIOR];
   int       i, j, k;
-  if (!box_cell(b, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
+  if (!box_cell(b, idx, i, j, k))
     return;
   const int64_t sv = G.sv, sj = G.sj, sk = G.sk;
   const int64_t c = cell_at(G, i, j, k);
@@ -922,6 +962,13 @@ k_update(const Grid<R> G, Buffers<R> B)
     x += eY[c + 1] * dtd[0];
     B.Uout[c + IC * sv] = x;
   }
+}
+
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+k_update(const Grid<R> G, Buffers<R> B)
+{
+  update_body<R, DIM>(G, B, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
 }
 
 // Grid description of one problem for the kernels (host side):

@@ -103,7 +103,7 @@ k_diag(const Grid<R> G, const R * __restrict__ U, double * __restrict__ partial)
     partial[blockIdx.x * 10 + threadIdx.x] = sh[threadIdx.x][0];
 }
 
-__global__ void
+static __global__ void
 k_diag_final(const double * __restrict__ partial, int nblocks, double * __restrict__ out)
 {
   const int q = threadIdx.x;
