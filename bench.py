@@ -7,7 +7,12 @@ perturbation), FP64 plain path.  A "step" is one full iteration of the solver
 update).  Metric: interior cell-updates per second.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload ot3d_256_fp64|ot3d_256_fp32|ot2d_256_fp64]
+                  [--workload ot3d_256_fp64|ot3d_256_fp32|ot2d_256_fp64|
+                              ensemble512_fp32|kh2d_4096_fp32|ot3d_128_fp64|ot3d_128_fp32]
+
+Other workloads: the 512-problem 2D Orszag-Tang ensemble in FP32 (one
+ensemble context, autotuned launch shapes) and the 2D magnetised
+Kelvin-Helmholtz shear layer at 4096^2 in FP32.
 
 One JSON line is printed by rank 0.  Multi-GPU runs (torchrun) are independent
 replicas of the workload, one per GPU ("replicas only": the path has no
@@ -40,6 +45,9 @@ WORKLOADS = {
     "ensemble512_fp32": (2, 0, 32, "512 independent 2D Orszag-Tang problems, N ~ logU[64,512] "
                                     "(seed 2024), B0 ~ U[0.5,1.5]/sqrt(4 pi), 5% random-phase "
                                     "Fourier velocity on |k|<=4, FP32, one ensemble context"),
+    "kh2d_4096_fp32": (2, 4096, 32, "2D magnetised Kelvin-Helmholtz 4096^2 (periodic x, "
+                                    "reflecting y, gamma 1.4, Bx 0.1), FP32 plain "
+                                    "MUSCL-Hancock+HLLD+CT"),
     # reduced size for ncu captures (a few GB on the device, inputs still > L2)
     "ot3d_128_fp64": (3, 128, 64, "3D Orszag-Tang 128^3, FP64 plain MUSCL-Hancock+HLLD+CT"),
     "ot3d_128_fp32": (3, 128, 32, "3D Orszag-Tang 128^3, FP32 plain MUSCL-Hancock+HLLD+CT"),
@@ -71,6 +79,23 @@ def perturbed_ot_state(U: np.ndarray, seed: int = 1234, amp: float = 1e-3) -> np
     ekin_new = 0.5 * (U[2] ** 2 + U[3] ** 2 + U[4] ** 2) / rho
     U[1] += ekin_new - ekin_old
     return U
+
+
+def workload_setup(name: str, precision: int):
+    """(.ini text, state transform or None, data description) of a
+    single-problem workload; the transform maps the Orszag-Tang initial state
+    to the workload's (FP64, LayoutLeft)."""
+    dim, n, _, _ = WORKLOADS[name]
+    if name.startswith("kh2d"):
+        from ppkmhd_gb300 import workloads
+
+        return (workloads.kh_ini(n, precision=precision),
+                lambda U: workloads.kelvin_helmholtz(n),
+                "synthetic: seeded magnetised Kelvin-Helmholtz shear layer")
+    if dim == 3:
+        return (ot_ini(dim, n, precision), perturbed_ot_state,
+                "synthetic: Orszag-Tang initial condition + seeded 1e-3 velocity perturbation")
+    return ot_ini(dim, n, precision), None, "synthetic: Orszag-Tang initial condition"
 
 
 # ---------------------------------------------------------------- clocks
@@ -156,17 +181,18 @@ def emit(obj):
 
 # ---------------------------------------------------------------- CPU side
 
-def cpu_baseline_run(dim: int, n: int, steps: int, warmup: int, nthreads: int):
+def cpu_baseline_run(name: str, steps: int, warmup: int, nthreads: int):
     """The oracle port of the reference step (oracle/mhd_oracle.c) on the host
     cores: same workload, full grid, `steps` timed iterations."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py
 
     oracle_py.build_oracle()
-    ini = ot_ini(dim, n, 64)
+    dim, n, _, _ = WORKLOADS[name]
+    ini, transform, _ = workload_setup(name, 64)
     s = oracle_py.OracleSolver(ini, nthreads=nthreads)
-    if dim == 3:
-        s.set_state(perturbed_ot_state(s.get_state()))
+    if transform is not None:
+        s.set_state(transform(s.get_state()))
     if warmup:
         s.run(warmup)
     t0 = time.perf_counter()
@@ -191,14 +217,14 @@ def run_gb300(args):
     import ppkmhd_gb300 as m
 
     dim, n, precision, label = WORKLOADS[args.workload]
-    ini = ot_ini(dim, n, precision)
+    ini, transform, data_desc = workload_setup(args.workload, precision)
     p = m.params_from_ini(ini)
     p.device = local
     s = m.MHDSolver(p)
     s.init_problem()
     U0 = s.get_state()
-    if dim == 3:
-        s.set_state(perturbed_ot_state(U0).astype(s.real))
+    if transform is not None:
+        s.set_state(transform(U0.astype(np.float64)).astype(s.real))
         U0 = s.get_state()
     interior_cells, ghost_cells = s.cell_counts()
     state_bytes = U0.nbytes
@@ -268,7 +294,7 @@ def run_gb300(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
-        v, el = cpu_baseline_run(dim, n, steps=args.cpu_steps, warmup=1, nthreads=nthreads)
+        v, el = cpu_baseline_run(args.workload, steps=args.cpu_steps, warmup=1, nthreads=nthreads)
         cpu = {"value": v, "unit": "cell-updates/s", "cores": nthreads, "kind": "port",
                "sample": f"{args.cpu_steps} steps of the same {n}^{dim} grid after 1 warm-up "
                          f"step, oracle/mhd_oracle.c with {nthreads} OpenMP threads "
@@ -287,8 +313,7 @@ def run_gb300(args):
             "scaling": "weak",
             "vs_baseline": None,
             "dtype": "f64" if precision == 64 else "f32",
-            "data": "synthetic: Orszag-Tang initial condition"
-                    + (" + seeded 1e-3 velocity perturbation" if dim == 3 else ""),
+            "data": data_desc,
             "config": {"workload": label, "grid": [n] * dim, "cells": interior_cells,
                        "cells_with_ghosts": ghost_cells, "state_bytes": state_bytes,
                        "l2": "inputs larger than L2 (state %.2f GB per array)" % (state_bytes / 1e9),
@@ -517,7 +542,8 @@ def run_reference(args):
               "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
                       "d2h_bytes_per_step": 0}})
         return
-    v, el = cpu_baseline_run(dim, n, steps=steps, warmup=min(args.warmup, 1), nthreads=nthreads)
+    v, el = cpu_baseline_run(args.workload, steps=steps, warmup=min(args.warmup, 1),
+                             nthreads=nthreads)
     emit({
         "impl": "reference",
         "metric": "MHD cell-updates/s (interior cells), plain MUSCL-Hancock+HLLD+CT step",
@@ -531,8 +557,7 @@ def run_reference(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
-        "data": "synthetic: Orszag-Tang initial condition"
-                + (" + seeded 1e-3 velocity perturbation" if dim == 3 else ""),
+        "data": workload_setup(args.workload, 64)[2],
         "config": {"workload": label, "grid": [n] * dim,
                    "implementation": "CPU port of the reference step (oracle/mhd_oracle.c, "
                                      "bitwise equal to the reference functors), OpenMP"},
@@ -550,11 +575,18 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="ot3d_256_fp64", choices=sorted(WORKLOADS))
-    ap.add_argument("--cpu-steps", type=int, default=2)
-    ap.add_argument("--ref-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps", type=int, default=None,
+                    help="CPU leg iterations (default: about 10 s of host work)")
+    ap.add_argument("--ref-steps", type=int, default=None,
+                    help="reference-arm iterations (default: --steps, at most 20 full-grid "
+                         "iterations; 150 for the ensemble sample)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
     args = ap.parse_args()
+    if args.cpu_steps is None:
+        args.cpu_steps = 150 if args.workload.startswith("ensemble") else 6
+    if args.ref_steps is None:
+        args.ref_steps = 150 if args.workload.startswith("ensemble") else max(1, min(args.steps, 20))
     if args.impl == "reference":
         run_reference(args)
     elif args.workload.startswith("ensemble"):

@@ -1,0 +1,68 @@
+"""The magnetised Kelvin-Helmholtz shear layer (periodic x, reflecting y):
+the workload generator on the CPU; on the GPU the FP32 and FP64 paths
+against the FP64 oracle on a down-scaled grid, with the FP64 conserved
+totals and div B."""
+import numpy as np
+import pytest
+
+from ppkmhd_gb300 import workloads
+
+
+def rel_l1(a, b):
+    ax = tuple(range(1, a.ndim))
+    den = np.abs(b).sum(axis=ax)
+    den = np.where(den > 1e-12 * den[0], den, den[0])
+    return np.abs(a - b).sum(axis=ax) / den
+
+
+def test_kh_state():
+    U = workloads.kelvin_helmholtz(64)
+    g = 3
+    rho = U[0, g:-g, g:-g]
+    assert abs(rho.min() - 1.0) < 1e-6 and abs(rho.max() - 2.0) < 1e-6
+    vx = U[2, g:-g, g:-g] / rho
+    assert abs(vx.max() - 0.5) < 1e-6 and abs(vx.min() + 0.5) < 1e-6
+    vy = U[3, g:-g, g:-g] / rho
+    assert 0.005 < np.abs(vy).max() <= 0.01 + 1e-15
+    assert np.all(U[5] == 0.1) and np.all(U[6] == 0.0)
+    e_int = U[1] - 0.5 * (U[2] ** 2 + U[3] ** 2) / U[0] - 0.5 * 0.1 ** 2
+    assert np.allclose(e_int[g:-g, g:-g], 2.5 / (float(np.float32(1.4)) - 1.0), rtol=1e-12)
+    assert np.array_equal(U, workloads.kelvin_helmholtz(64))
+    ini = workloads.kh_ini(64)
+    assert "boundary_type_ymin=1" in ini and "boundary_type_xmin=3" in ini
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [(64, 1e-12), (32, 1e-3)])
+def test_kh_against_fp64_oracle(mhdlib, oracle, precision, tol):
+    n, steps = 256, 100
+    ini = workloads.kh_ini(n, precision=precision)
+    U = workloads.kelvin_helmholtz(n)
+    o = oracle.OracleSolver(workloads.kh_ini(n, precision=64), nthreads=16)
+    o.set_state(U)
+    o.run(steps)
+    s = mhdlib.MHDSolver.from_ini(ini)
+    s.set_state(U.astype(s.real))
+    d0, _, _ = s.diagnostics()
+    assert s.run(steps) == steps
+    err = rel_l1(mhdlib.interior(s.get_state()).astype(np.float64), oracle.interior(o.get_state()))
+    assert err.max() <= tol, err
+    d1, _, divb_max = s.diagnostics()
+    # mass, energy and x momentum are conserved with reflecting y walls
+    scale = np.abs(d0).max()
+    ctol = 1e-12 if precision == 64 else 1e-5
+    for v in (0, 1, 2):
+        assert abs(d1[v] - d0[v]) <= ctol * scale, (v, d1[v], d0[v])
+    # div B stays at round-off away from the walls.  In the first and last
+    # interior rows it does not: the reflecting fill sets the wall face's By
+    # from the mirrored interior face (BoundariesFunctors.h:535-748), as in
+    # the reference, whose state the GPU run matches above.
+    U = s.get_state().astype(np.float64)
+    g = 3
+    dx = 1.0 / n
+    div = ((U[5, g:-g, g + 1:-g + 1] - U[5, g:-g, g:-g]) + (U[6, g + 1:-g + 1, g:-g] - U[6, g:-g, g:-g])) / dx
+    inner = np.abs(div[1:-1]).max()
+    assert inner < (1e-10 if precision == 64 else 1e-3), inner
+    Uo = o.get_state()
+    div_o = ((Uo[5, g:-g, g + 1:-g + 1] - Uo[5, g:-g, g:-g]) + (Uo[6, g + 1:-g + 1, g:-g] - Uo[6, g:-g, g:-g])) / dx
+    assert abs(divb_max - np.abs(div_o).max()) <= (1e-9 if precision == 64 else 1e-2) * np.abs(div_o).max() + 1e-9
