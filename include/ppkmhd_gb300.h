@@ -224,6 +224,91 @@ int mhd_ensemble_cell_count(mhd_ensemble *ens, int64_t *interior);
 int mhd_ensemble_launches_per_step(mhd_ensemble *ens, int *n);
 const char *mhd_ensemble_last_error(mhd_ensemble *ens);
 
+/*
+ * Checkpoint / restart.  The reference restarts from its HDF5 output
+ * ([run] restart_enabled, restart_filename, restart_reset_totaltime;
+ * SolverMHDMuscl<dim>::init_restart, SolverMHDMuscl.h:613-643), which drops
+ * the magnetic field (the HDF5 writers pass 4 or 5 variables,
+ * IO_ReadWrite.cpp:102-106, :150-154).  Here a checkpoint is one binary file:
+ *   char magic[8] = "PPKMHDCK"; uint32 format = 1, dim, nx, ny, nz, ghost,
+ *   nbvar = 8, real_bytes; double t, dt; int64 iteration; int32 times_saved,
+ *   pad; double xmin, xmax, ymin, ymax, zmin, zmax, gamma0;
+ * followed by the ghost-inclusive state, LayoutLeft, in the context's
+ * precision (all fields little-endian).  Loading restores the state and t
+ * (0 with reset_time, as restart_reset_totaltime); the iteration count
+ * restarts at 0 as in the reference.  Continuing from a checkpoint is
+ * bitwise equal to the uninterrupted run.
+ */
+int mhd_checkpoint_save(mhd_ctx *ctx, const char *path, int times_saved);
+int mhd_checkpoint_load(mhd_ctx *ctx, const char *path, int reset_time, int *times_saved);
+
+/*
+ * HLLD flux surrogate.  The reference has no learned component; this is the
+ * GB300 build's FP32 option for the face-flux stage (riemann_hlld,
+ * RiemannSolvers_MHD.h:133-367, at the call site of
+ * ComputeFluxAndUpdateAlongDirFunctor, MHDRunFunctors{2D,3D}.h).
+ *
+ * A 15-64-64-7 perceptron (GELU, BF16 weights, FP32 accumulation) predicts
+ * the upwind dissipation D = (F(qL) + F(qR))/2 - F_HLLD of a face in the
+ * face's own dimensionless units; it is used on faces whose largest
+ * normalised half-jump J is at most tau, whose reconstructed density and
+ * pressure are above their floors and whose prediction is finite and
+ * bounded; every other face gets HLLD.  Training runs on the GPU with the
+ * library's own forward/backward kernels.
+ */
+#define MHD_MLP_PARAMS 5768      /* W1[16][64] b1[64] W2[64][64] b2[64] W3[64][8] b3[8] */
+#define MHD_SAMPLE_FLOATS 24     /* one harvested face record, see mhd_harvest_faces */
+#define MHD_MLP_TRAIN 0          /* BF16 weights/activations, hardware tanh (deployed numerics) */
+#define MHD_MLP_CHECK 1          /* plain FP32, tanhf: for gradient checks */
+
+typedef struct mhd_mlp mhd_mlp;
+
+/* Face samples of the context's next iteration (boundaries, primitives, dt
+ * and trace are computed; the state is not advanced): one record per
+ * stride-th face of each direction, records[q * MHD_SAMPLE_FLOATS + ...] =
+ * qL[7], qR[7] (rho, vn, vt1, vt2, p, Bt1, Bt2 in the face-normal frame), a
+ * (normal B), J (sensor value), D[7] (FP64 central flux minus FP64 HLLD of
+ * the same states: rho, E, mn, mt1, mt2, Bt1, Bt2), gamma0.  With
+ * records == NULL only *count is set. */
+int mhd_harvest_faces(mhd_ctx *ctx, int stride, float *records, int64_t capacity,
+                      int64_t *count);
+
+/* A network with Glorot-uniform weights from `seed`, for adiabatic index gamma0. */
+int mhd_mlp_create(uint64_t seed, double gamma0, mhd_mlp **mlp);
+int mhd_mlp_destroy(mhd_mlp *mlp);
+int mhd_mlp_set_params(mhd_mlp *mlp, const float *params, int n);
+int mhd_mlp_get_params(mhd_mlp *mlp, float *params, int n);
+int mhd_mlp_gamma(mhd_mlp *mlp, double *gamma0);
+
+/* Records -> features[n][16] and targets[n][8] (D / scale, FP64 on the GPU). */
+int mhd_mlp_encode(mhd_mlp *mlp, const float *records, int64_t n, float *features,
+                   float *targets);
+
+/* Gradient of the mean squared error (over n samples and the 7 used
+ * outputs) with respect to the MHD_MLP_PARAMS parameters; *loss = the error. */
+int mhd_mlp_gradient(mhd_mlp *mlp, const float *features, const float *targets, int64_t n,
+                     int mode, float *grad, double *loss);
+
+/* Adam on the harvested records (seeded shuffles, cosine learning-rate
+ * decay to lr/20); each sample's squared error is weighted by
+ * (sJ / 0.1)^weight_power (sJ = max(J, 1e-4); 0 = unweighted);
+ * loss_history[epochs] = mean batch loss (may be NULL). */
+int mhd_mlp_train(mhd_mlp *mlp, const float *records, int64_t n, int epochs, int batch,
+                  float lr, float weight_power, uint64_t seed, float *loss_history);
+
+/* The deployed tensor-core forward pass on features[n][16] -> out[n][8]. */
+int mhd_mlp_forward(mhd_mlp *mlp, const float *features, int64_t n, float *out);
+const char *mhd_mlp_last_error(mhd_mlp *mlp);
+
+/* Use the network in the flux stage of an FP32, version-2, HLLD context
+ * (mlp == NULL: back to HLLD everywhere).  The network's gamma0 must match
+ * the context's.  tau: sensor threshold on J (0 < tau <= 0.1). */
+int mhd_set_surrogate(mhd_ctx *ctx, const mhd_mlp *mlp, double tau);
+
+/* Faces given by the network and faces computed since the surrogate was
+ * set or the last reset (reset != 0 clears the counters). */
+int mhd_surrogate_stats(mhd_ctx *ctx, int64_t *faces_network, int64_t *faces_total, int reset);
+
 /* Device scratch reserved by mhd_step_noalloc on every GPU that loads this
  * library, for the process lifetime. */
 #define MHD_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)

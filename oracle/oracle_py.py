@@ -80,6 +80,15 @@ def lib():
         L.orc_riemann.argtypes = [ctypes.POINTER(OrcParams), _dp, _dp, _dp]
         L.orc_compute_emf.argtypes = [ctypes.POINTER(OrcParams), ctypes.c_int, _dp]
         L.orc_compute_emf.restype = ctypes.c_double
+        L.mlp_nparams.restype = ctypes.c_int
+        L.mlp_encode.argtypes = [_dp, _dp, ctypes.c_double, _dp, _dp]
+        L.mlp_encode.restype = ctypes.c_double
+        L.mlp_central_flux.argtypes = [_dp, _dp, ctypes.c_double, ctypes.c_double, _dp]
+        L.mlp_forward_batch.argtypes = [_dp, _dp, ctypes.c_long, _dp, ctypes.c_int]
+        L.mlp_loss_grad.argtypes = [_dp, _dp, _dp, ctypes.c_long, _dp]
+        L.mlp_loss_grad.restype = ctypes.c_double
+        L.mlp_bf16.argtypes = [ctypes.c_double]
+        L.mlp_bf16.restype = ctypes.c_double
         _lib = L
     return _lib
 
@@ -155,6 +164,46 @@ def riemann(p: OrcParams, qL, qR) -> np.ndarray:
 def compute_emf(p: OrcParams, emf_dir: int, q_edge) -> float:
     q = np.ascontiguousarray(q_edge, dtype=np.float64).reshape(4, 8)
     return float(lib().orc_compute_emf(ctypes.byref(p), int(emf_dir), _ptr(q)))
+
+
+# ---------------------------------------------------------------- flux surrogate
+
+MLP_NPARAM = 5768
+
+
+def mlp_encode(qL, qR, a: float):
+    """(features[16], scale[7], J) of one face (mlp_oracle.c)."""
+    l = np.ascontiguousarray(qL, dtype=np.float64)
+    r = np.ascontiguousarray(qR, dtype=np.float64)
+    f = np.zeros(16)
+    sc = np.zeros(7)
+    J = lib().mlp_encode(_ptr(l), _ptr(r), float(a), _ptr(f), _ptr(sc))
+    return f, sc, J
+
+
+def mlp_central_flux(qL, qR, a: float, gamma0: float):
+    l = np.ascontiguousarray(qL, dtype=np.float64)
+    r = np.ascontiguousarray(qR, dtype=np.float64)
+    F = np.zeros(7)
+    lib().mlp_central_flux(_ptr(l), _ptr(r), float(a), float(gamma0), _ptr(F))
+    return F
+
+
+def mlp_forward(params, X, rounding: bool = False):
+    P = np.ascontiguousarray(params, dtype=np.float64)
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    Y = np.zeros((X.shape[0], 8))
+    lib().mlp_forward_batch(_ptr(P), _ptr(X), X.shape[0], _ptr(Y), int(rounding))
+    return Y
+
+
+def mlp_loss_grad(params, X, T):
+    P = np.ascontiguousarray(params, dtype=np.float64)
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    T = np.ascontiguousarray(T, dtype=np.float64)
+    g = np.zeros(MLP_NPARAM)
+    loss = lib().mlp_loss_grad(_ptr(P), _ptr(X), _ptr(T), X.shape[0], _ptr(g))
+    return loss, g
 
 
 # ---------------------------------------------------------------- reference

@@ -38,6 +38,9 @@ MHD_FP64, MHD_FP32 = 64, 32
 MHD_FP_FAST, MHD_FP_EXACT = 0, 1
 MHD_LAYOUT_LEFT, MHD_LAYOUT_RIGHT = 0, 1
 MHD_PROBLEM_ORSZAG_TANG = 0
+MHD_MLP_PARAMS = 5768
+MHD_SAMPLE_FLOATS = 24
+MHD_MLP_TRAIN, MHD_MLP_CHECK = 0, 1
 
 
 class MHDParams(ctypes.Structure):
@@ -114,6 +117,22 @@ SIGNATURES = {
     "mhd_ensemble_cell_count": (ctypes.c_int, [_vp, _i64p]),
     "mhd_ensemble_launches_per_step": (ctypes.c_int, [_vp, _ip]),
     "mhd_ensemble_last_error": (ctypes.c_char_p, [_vp]),
+    "mhd_harvest_faces": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_int64, _i64p]),
+    "mhd_checkpoint_save": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int]),
+    "mhd_checkpoint_load": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int, _ip]),
+    "mhd_mlp_create": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(_vp)]),
+    "mhd_mlp_destroy": (ctypes.c_int, [_vp]),
+    "mhd_mlp_set_params": (ctypes.c_int, [_vp, _vp, ctypes.c_int]),
+    "mhd_mlp_get_params": (ctypes.c_int, [_vp, _vp, ctypes.c_int]),
+    "mhd_mlp_gamma": (ctypes.c_int, [_vp, _dp]),
+    "mhd_mlp_encode": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp]),
+    "mhd_mlp_gradient": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int64, ctypes.c_int, _vp, _dp]),
+    "mhd_mlp_train": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_float, ctypes.c_float, ctypes.c_uint64, _vp]),
+    "mhd_mlp_forward": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp]),
+    "mhd_mlp_last_error": (ctypes.c_char_p, [_vp]),
+    "mhd_set_surrogate": (ctypes.c_int, [_vp, _vp, ctypes.c_double]),
+    "mhd_surrogate_stats": (ctypes.c_int, [_vp, _i64p, _i64p, ctypes.c_int]),
 }
 
 _lib = None
@@ -277,6 +296,37 @@ class MHDSolver:
         n = ctypes.c_int()
         self._check(lib().mhd_launches_per_step(self.h, ctypes.byref(n)))
         return n.value
+
+    def checkpoint_save(self, path: str, times_saved: int = 0):
+        self._check(lib().mhd_checkpoint_save(self.h, os.fsencode(path), int(times_saved)))
+
+    def checkpoint_load(self, path: str, reset_time: bool = False) -> int:
+        """Restore state and time from a checkpoint; returns its output counter."""
+        ts = ctypes.c_int()
+        self._check(lib().mhd_checkpoint_load(self.h, os.fsencode(path), int(reset_time),
+                                              ctypes.byref(ts)))
+        return ts.value
+
+    def harvest(self, stride: int = 1) -> np.ndarray:
+        """Face records of the next iteration, shape (n, MHD_SAMPLE_FLOATS)."""
+        cnt = ctypes.c_int64()
+        self._check(lib().mhd_harvest_faces(self.h, int(stride), None, 0, ctypes.byref(cnt)))
+        out = np.empty((cnt.value, MHD_SAMPLE_FLOATS), dtype=np.float32)
+        self._check(lib().mhd_harvest_faces(self.h, int(stride), out.ctypes.data, cnt.value,
+                                            ctypes.byref(cnt)))
+        return out
+
+    def set_surrogate(self, mlp, tau: float = 0.01):
+        """Use the network `mlp` (an ppkmhd_gb300.surrogate.FluxMLP) in the flux
+        stage; None restores HLLD everywhere."""
+        self._check(lib().mhd_set_surrogate(self.h, mlp.h if mlp is not None else None,
+                                            float(tau)))
+
+    def surrogate_stats(self, reset: bool = False):
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        self._check(lib().mhd_surrogate_stats(self.h, ctypes.byref(a), ctypes.byref(b),
+                                              int(reset)))
+        return a.value, b.value
 
 
 def interior(U: np.ndarray, ghost: int = 3) -> np.ndarray:

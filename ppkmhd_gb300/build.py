@@ -101,6 +101,10 @@ def build(jobs: int | None = None, force: bool = False, verbose: bool = False) -
                      f"-DMHD_ENSEMBLE_FACTORY={factory.replace('create_core', 'create_ensemble')}",
                      f"-DMHD_EXACT_BUILD={1 if fmad == 'false' else 0}",
                      "-c", os.path.join(CSRC, "mhd_ensemble.cu"), "-o", o])
+    o = os.path.join(OBJ, "mhd_mlp.o")
+    objs.append(o)
+    cmds.append([nvcc(), *GENCODE, *NVCC_COMMON, "--fmad=true", "-Xptxas", "-v",
+                 "-c", os.path.join(CSRC, "mhd_mlp.cu"), "-o", o])
     o = os.path.join(OBJ, "mhd_noalloc.o")
     objs.append(o)
     cmds.append([nvcc(), *GENCODE, *NVCC_COMMON, "--fmad=true", "-Xptxas", "-v",

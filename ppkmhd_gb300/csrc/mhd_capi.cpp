@@ -5,6 +5,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "mhd_core.h"
 #include "ppkmhd_gb300.h"
@@ -17,6 +18,18 @@ struct mhd_ctx
   mhd_params        params{};
   std::string       err;
 };
+
+// On-disk header of mhd_checkpoint_save (documented in ppkmhd_gb300.h).
+struct CheckpointHeader
+{
+  char     magic[8];
+  uint32_t format, dim, nx, ny, nz, ghost, nbvar, real_bytes;
+  double   t, dt;
+  int64_t  iteration;
+  int32_t  times_saved, pad;
+  double   box[7]; // xmin, xmax, ymin, ymax, zmin, zmax, gamma0
+};
+static_assert(sizeof(CheckpointHeader) == 8 + 8 * 4 + 2 * 8 + 8 + 8 + 7 * 8, "checkpoint header");
 
 struct mhd_ensemble
 {
@@ -458,6 +471,124 @@ extern "C"
     if (n)
       *n = ctx->core->launches_per_step();
     return MHD_OK;
+  }
+
+  int
+  mhd_checkpoint_save(mhd_ctx * ctx, const char * path, int times_saved)
+  {
+    NEED_CORE(ctx);
+    if (!path)
+      return fail(ctx, MHD_ERR_INVALID_ARG, "null path");
+    int sz[4];
+    ctx->core->sizes(sz);
+    const size_t n = (size_t)sz[0] * sz[1] * sz[2] * sz[3];
+    const int    rb = ctx->core->real_bytes();
+    std::vector<unsigned char> U(n * rb);
+    if (int rc = ctx->core->get_state(U.data(), MHD_LAYOUT_LEFT))
+      return from_core(ctx, rc);
+    double t = 0, dt = 0;
+    int    it = 0;
+    if (int rc = ctx->core->time(&t, &dt, &it))
+      return from_core(ctx, rc);
+    const mhd_params & p = ctx->params;
+    CheckpointHeader   h{};
+    std::memcpy(h.magic, "PPKMHDCK", 8);
+    h.format = 1;
+    h.dim = (uint32_t)p.dim;
+    h.nx = (uint32_t)p.nx;
+    h.ny = (uint32_t)p.ny;
+    h.nz = (uint32_t)(p.dim == 3 ? p.nz : 1);
+    h.ghost = (uint32_t)p.ghost;
+    h.nbvar = 8;
+    h.real_bytes = (uint32_t)rb;
+    h.t = t;
+    h.dt = dt;
+    h.iteration = it;
+    h.times_saved = times_saved;
+    const double box[7] = { p.xmin, p.xmax, p.ymin, p.ymax, p.zmin, p.zmax, p.gamma0 };
+    std::memcpy(h.box, box, sizeof box);
+    FILE * f = std::fopen(path, "wb");
+    if (!f)
+      return fail(ctx, MHD_ERR_INVALID_ARG, std::string("cannot open ") + path + " for writing");
+    const bool ok = std::fwrite(&h, sizeof h, 1, f) == 1 && std::fwrite(U.data(), 1, U.size(), f) == U.size();
+    const bool closed = std::fclose(f) == 0;
+    if (!ok || !closed)
+      return fail(ctx, MHD_ERR_INVALID_ARG, std::string("short write to ") + path);
+    return MHD_OK;
+  }
+
+  int
+  mhd_checkpoint_load(mhd_ctx * ctx, const char * path, int reset_time, int * times_saved)
+  {
+    NEED_CORE(ctx);
+    if (!path)
+      return fail(ctx, MHD_ERR_INVALID_ARG, "null path");
+    FILE * f = std::fopen(path, "rb");
+    if (!f)
+      return fail(ctx, MHD_ERR_INVALID_ARG, std::string("cannot open ") + path);
+    CheckpointHeader h{};
+    const bool       got = std::fread(&h, sizeof h, 1, f) == 1;
+    const mhd_params & p = ctx->params;
+    std::string      bad;
+    if (!got || std::memcmp(h.magic, "PPKMHDCK", 8) != 0 || h.format != 1)
+      bad = "not a checkpoint file (format 1)";
+    else if ((int)h.dim != p.dim || (int)h.nx != p.nx || (int)h.ny != p.ny ||
+             (p.dim == 3 && (int)h.nz != p.nz) || (int)h.ghost != p.ghost || h.nbvar != 8)
+      bad = "checkpoint grid does not match the context";
+    else if ((int)h.real_bytes != ctx->core->real_bytes())
+      bad = "checkpoint precision does not match the context";
+    std::vector<unsigned char> U;
+    if (bad.empty())
+    {
+      int sz[4];
+      ctx->core->sizes(sz);
+      U.resize((size_t)sz[0] * sz[1] * sz[2] * sz[3] * h.real_bytes);
+      if (std::fread(U.data(), 1, U.size(), f) != U.size())
+        bad = "checkpoint file is truncated";
+    }
+    std::fclose(f);
+    if (!bad.empty())
+      return fail(ctx, MHD_ERR_INVALID_ARG, bad);
+    ctx->core->set_time_origin(reset_time ? 0.0 : h.t);
+    const int rc = ctx->core->set_state(U.data(), MHD_LAYOUT_LEFT);
+    ctx->core->set_time_origin(p.tCurrent);
+    if (rc)
+      return from_core(ctx, rc);
+    if (times_saved)
+      *times_saved = h.times_saved;
+    return MHD_OK;
+  }
+
+  int
+  mhd_harvest_faces(mhd_ctx * ctx, int stride, float * records, int64_t capacity, int64_t * count)
+  {
+    NEED_CORE(ctx);
+    if (stride < 1 || !count)
+      return fail(ctx, MHD_ERR_INVALID_ARG, "stride must be >= 1 and count non-null");
+    return from_core(ctx, ctx->core->harvest(stride, records, capacity, count));
+  }
+
+  int
+  mhd_set_surrogate(mhd_ctx * ctx, const mhd_mlp * mlp, double tau)
+  {
+    NEED_CORE(ctx);
+    if (!mlp)
+      return from_core(ctx, ctx->core->set_surrogate(nullptr, 0.0));
+    if (!(tau > 0.0) || tau > 0.1)
+      return fail(ctx, MHD_ERR_INVALID_ARG, "tau must be in (0, 0.1]");
+    if (std::fabs(mhd::mlp_gamma(mlp) - ctx->params.gamma0) > 1e-6 * ctx->params.gamma0)
+      return fail(ctx, MHD_ERR_INVALID_ARG,
+                  "the network was trained for another adiabatic index (gamma0)");
+    std::vector<uint32_t> pack(mhd::kMlpPackTotal);
+    mhd::mlp_pack(mhd::mlp_params(mlp), pack.data());
+    return from_core(ctx, ctx->core->set_surrogate(pack.data(), tau));
+  }
+
+  int
+  mhd_surrogate_stats(mhd_ctx * ctx, int64_t * faces_network, int64_t * faces_total, int reset)
+  {
+    NEED_CORE(ctx);
+    return from_core(ctx, ctx->core->surrogate_stats(faces_network, faces_total, reset));
   }
 
   const char *

@@ -31,6 +31,13 @@ public:
   virtual int real_bytes() const = 0;
   //! make the context's device current for the calling thread
   virtual int bind_device() = 0;
+  //! flux surrogate: packed weights + biases (mhd_mlp.cuh), nullptr = off
+  virtual int set_surrogate(const uint32_t * wpack, double tau) = 0;
+  virtual int surrogate_stats(int64_t * used, int64_t * total, int reset) = 0;
+  //! face samples of the next iteration (mhd_harvest_faces)
+  virtual int harvest(int stride, float * host, int64_t capacity, int64_t * count) = 0;
+  //! time that set_state / init_problem start from (tCurrent)
+  virtual void set_time_origin(double t) = 0;
   std::string err;
 };
 
@@ -62,6 +69,13 @@ SolverCore * create_core_f32(const mhd_params & p, std::string & err);
 EnsembleCore * create_ensemble_f64x(const mhd_params * p, int n, std::string & err);
 EnsembleCore * create_ensemble_f64(const mhd_params * p, int n, std::string & err);
 EnsembleCore * create_ensemble_f32(const mhd_params * p, int n, std::string & err);
+
+// Flux surrogate helpers (mhd_mlp.cu): packed weights + biases for the
+// flux stage (kMlpPackTotal words), the network's gamma0 and parameters.
+constexpr int kMlpPackTotal = 2816 + 136;
+void          mlp_pack(const float * params, uint32_t * out);
+double        mlp_gamma(const mhd_mlp * m);
+const float * mlp_params(const mhd_mlp * m);
 
 // Empty string when the parameters can be run, else the reason (mhd_capi.cpp).
 std::string validate_params(const mhd_params & p);

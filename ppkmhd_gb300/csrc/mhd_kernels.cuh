@@ -674,21 +674,22 @@ face_source(const Grid<R> & G, const R * __restrict__ E, int64_t c, int d, R dtd
 // blockIdx.y selects the direction.  The reference adds the flux into cell i
 // and subtracts it from cell i-1 with atomics; here it is stored once and
 // gathered by k_update.
+// Left/right states of the face at the lower side of cell (i,j,k) along d,
+// floored and rotated into the face-normal frame (normal velocity -> IU,
+// normal field -> IA): MHDRunFunctors2D.h:1110-1190, 3D:1097-1210.
 template <class R, int DIM, int d>
 __device__ __forceinline__ void
-flux_face(const Grid<R> & G, const Buffers<R> & B, int i, int j, int k)
+face_states(const Grid<R> & G, const Buffers<R> & B, int64_t c, State<R> & qL, State<R> & qR)
 {
   const int64_t sv = G.sv;
   const int64_t off = d == 0 ? 1 : (d == 1 ? G.sj : G.sk);
-  const int64_t c = cell_at(G, i, j, k), cn = c - off;
+  const int64_t cn = c - off;
   const R * __restrict__ Q2 = B.Q2;
   const R * __restrict__ S = B.S + (int64_t)d * NV * sv;
   R dtdx, dtdy, dtdz;
   dt_over_dx(B.st, dtdx, dtdy, dtdz);
   const R smallR = G.smallr, smallp = G.smallp;
   constexpr int nrm = IA + d;
-
-  State<R> qR, qL, fl;
 #pragma unroll
   for (int v = 0; v < NV; ++v)
   {
@@ -703,7 +704,6 @@ flux_face(const Grid<R> & G, const Buffers<R> & B, int i, int j, int k)
   qL[IP] = fmax(smallp * qL[ID], qL[IP]);
   qR[nrm] = B.Uin[c + nrm * sv] + face_source<R, DIM>(G, B.E, c, d, dtdx, dtdy, dtdz);
   qL[nrm] = qR[nrm];
-  // rotate into the face-normal frame: normal velocity -> IU, normal field -> IA
   if constexpr (d > 0)
   {
     swap_vals(qL[IU], qL[IU + d]);
@@ -711,20 +711,37 @@ flux_face(const Grid<R> & G, const Buffers<R> & B, int i, int j, int k)
     swap_vals(qR[IU], qR[IU + d]);
     swap_vals(qR[IA], qR[IA + d]);
   }
-#pragma unroll
-  for (int v = 0; v < NV; ++v)
-    fl[v] = R(0);
-  riemann(G.riemann, qL, qR, fl, G.gamma0);
+}
+
+// Rotate a normal-frame flux back and store the components the update reads.
+template <class R, int DIM, int d>
+__device__ __forceinline__ void
+store_face_flux(const Grid<R> & G, const Buffers<R> & B, int64_t c, State<R> & fl)
+{
   if constexpr (d > 0)
   {
     swap_vals(fl[IU], fl[IU + d]);
     swap_vals(fl[IA], fl[IA + d]);
   }
   constexpr int NF = FluxComps<DIM>::NF;
-  R * F = B.F + (int64_t)d * NF * sv;
+  R * F = B.F + (int64_t)d * NF * G.sv;
 #pragma unroll
   for (int q = 0; q < NF; ++q)
-    F[c + q * sv] = fl[FluxComps<DIM>::var(q)];
+    F[c + q * G.sv] = fl[FluxComps<DIM>::var(q)];
+}
+
+template <class R, int DIM, int d>
+__device__ __forceinline__ void
+flux_face(const Grid<R> & G, const Buffers<R> & B, int i, int j, int k)
+{
+  const int64_t c = cell_at(G, i, j, k);
+  State<R>      qR, qL, fl;
+  face_states<R, DIM, d>(G, B, c, qL, qR);
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+    fl[v] = R(0);
+  riemann(G.riemann, qL, qR, fl, G.gamma0);
+  store_face_flux<R, DIM, d>(G, B, c, fl);
 }
 
 template <class R, int DIM>

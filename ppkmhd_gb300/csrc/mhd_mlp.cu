@@ -1,0 +1,683 @@
+// Training and evaluation of the HLLD flux surrogate (mhd_mlp.cuh) on the
+// GPU: feature encoding of harvested face samples, forward + backward passes
+// with per-block partial gradients reduced in a fixed order, Adam, and the
+// tensor-core forward used by the flux stage.  Exposed through the
+// mhd_mlp_* entry points of include/ppkmhd_gb300.h.
+//
+// Training arithmetic: FP32 master weights; in MHD_MLP_TRAIN mode the
+// forward pass sees BF16 weights and inputs and the deployed BF16 GELU
+// (gelu_bf16: the same operations as the tensor-core path), and the
+// backward pass differentiates the FP32 GELU (rounding as the identity).  MHD_MLP_CHECK mode
+// is plain FP32 with tanhf (for gradient checks against the CPU oracle).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "mhd_core.h"
+#include "mhd_mlp.cuh"
+#include "ppkmhd_gb300.h"
+
+using namespace mhd::mlp;
+
+static_assert(mhd::kMlpPackTotal == kPackWords + kBiasFloats, "packed surrogate size");
+static_assert(kParams == MHD_MLP_PARAMS, "surrogate parameter count");
+static_assert(kRecord == MHD_SAMPLE_FLOATS, "face record size");
+
+struct mhd_mlp
+{
+  int          device = 0;
+  double       gamma0 = 5.0 / 3.0;
+  std::vector<float> params; // host copy of the master weights (kept in sync)
+  float *      d_params = nullptr;
+  float *      d_m = nullptr;
+  float *      d_v = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string  err;
+  int64_t      adam_step = 0;
+};
+
+namespace
+{
+
+constexpr int kTB = 64;                                  // samples per training block
+constexpr int kRowX = 0, kRowZ1 = 16, kRowH1 = 80, kRowZ2 = 144, kRowH2 = 208, kRowY = 272;
+constexpr int kRowLoss = 280;
+constexpr int kRowStride = 281;                           // odd: conflict-free columns
+constexpr int kSmemTrain = (kParams + kTB * kRowStride) * (int)sizeof(float);
+
+__device__ __forceinline__ float
+bf16_round(float x)
+{
+  return __bfloat162float(__float2bfloat16_rn(x));
+}
+
+__device__ __forceinline__ float
+gelu_exact(float x)
+{
+  return 0.5f * x * (1.0f + tanhf(kGeluC0 * (x + kGeluC1 * x * x * x)));
+}
+
+// d/dx of the tanh-form GELU, with the tanh of the same flavour as the forward pass
+__device__ __forceinline__ float
+gelu_grad(float x, int train)
+{
+  const float u = kGeluC0 * (x + kGeluC1 * x * x * x);
+  const float t = train ? tanh_hw(u) : tanhf(u);
+  return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * kGeluC0 * (1.0f + 3.0f * kGeluC1 * x * x);
+}
+
+// Records -> features (16) and targets D / scale (8), in FP64.
+__global__ void
+k_encode(const float * __restrict__ rec, int64_t n, float * __restrict__ feat,
+         float * __restrict__ tgt)
+{
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n)
+    return;
+  const float * r = rec + s * kRecord;
+  double        l7[7], r7[7], f[kIn], sc[7];
+  for (int q = 0; q < 7; ++q)
+  {
+    l7[q] = r[kRecQL + q];
+    r7[q] = r[kRecQR + q];
+  }
+  encode(l7, r7, (double)r[kRecA], f, sc);
+  for (int q = 0; q < kIn; ++q)
+    feat[s * kIn + q] = (float)f[q];
+  for (int q = 0; q < 7; ++q)
+    tgt[s * kOut + q] = (float)((double)r[kRecD + q] / sc[q]);
+  tgt[s * kOut + 7] = 0.f;
+}
+
+// Forward + backward of kTB samples per block; writes the block's summed
+// gradient (kParams) and summed squared error to partial[block].
+// idx (optional) maps sample slots to rows of feat/tgt.  norm = 1 / (N * 7).
+__global__ void __launch_bounds__(kTB)
+k_fwd_bwd(const float * __restrict__ W, const float * __restrict__ feat,
+          const float * __restrict__ tgt, const int * __restrict__ idx, int64_t first, int64_t n,
+          float norm, int train, float wpow, float * __restrict__ partial)
+{
+  extern __shared__ float sm[];
+  float *     w = sm;
+  float *     rows = sm + kParams;
+  const int   s = threadIdx.x;
+  for (int p = s; p < kParams; p += kTB)
+  {
+    const float x = W[p];
+    // biases stay FP32 in the deployed network; weights are BF16
+    const bool is_bias = (p >= kOffB1 && p < kOffW2) || (p >= kOffB2 && p < kOffW3) || p >= kOffB3;
+    w[p] = (train && !is_bias) ? bf16_round(x) : x;
+  }
+  float *       row = rows + s * kRowStride;
+  const int64_t slot = first + (int64_t)blockIdx.x * kTB + s;
+  const bool    active = slot < n;
+  const int64_t src = active ? (idx ? (int64_t)idx[slot] : slot) : 0;
+  for (int q = 0; q < kIn; ++q)
+  {
+    const float x = active ? feat[src * kIn + q] : 0.f;
+    row[kRowX + q] = train ? bf16_round(x) : x;
+  }
+  __syncthreads();
+  // layer 1
+  for (int k = 0; k < kHid; ++k)
+  {
+    float acc = w[kOffB1 + k];
+    for (int i = 0; i < kIn; ++i)
+      acc = fmaf(row[kRowX + i], w[kOffW1 + i * kHid + k], acc);
+    row[kRowZ1 + k] = acc;
+    row[kRowH1 + k] = train ? gelu_bf16(acc) : gelu_exact(acc);
+  }
+  // layer 2
+  for (int k = 0; k < kHid; ++k)
+  {
+    float acc = w[kOffB2 + k];
+    for (int j = 0; j < kHid; ++j)
+      acc = fmaf(row[kRowH1 + j], w[kOffW2 + j * kHid + k], acc);
+    row[kRowZ2 + k] = acc;
+    row[kRowH2 + k] = train ? gelu_bf16(acc) : gelu_exact(acc);
+  }
+  // layer 3 + loss gradient; sample weight (sJ / kTauRef)^wpow emphasises
+  // the faces with larger jumps, whose dissipation is larger in physical units
+  const float sw = wpow != 0.f ? powf(fmaxf(row[kRowX + 14], 1e-3f), wpow) : 1.f;
+  float       loss = 0.f;
+  for (int o = 0; o < kOut; ++o)
+  {
+    float acc = w[kOffB3 + o];
+    for (int j = 0; j < kHid; ++j)
+      acc = fmaf(row[kRowH2 + j], w[kOffW3 + j * kOut + o], acc);
+    const float e = (active && o < kOutUsed) ? acc - tgt[src * kOut + o] : 0.f;
+    loss = fmaf(sw * e, e, loss);
+    row[kRowY + o] = 2.f * sw * e * norm;
+  }
+  row[kRowLoss] = loss;
+  // back through layer 3 and 2: dz2 overwrites z2, dz1 overwrites z1
+  for (int j = 0; j < kHid; ++j)
+  {
+    float acc = 0.f;
+    for (int o = 0; o < kOut; ++o)
+      acc = fmaf(row[kRowY + o], w[kOffW3 + j * kOut + o], acc);
+    row[kRowZ2 + j] = acc * gelu_grad(row[kRowZ2 + j], train);
+  }
+  for (int j = 0; j < kHid; ++j)
+  {
+    float acc = 0.f;
+    for (int k = 0; k < kHid; ++k)
+      acc = fmaf(row[kRowZ2 + k], w[kOffW2 + j * kHid + k], acc);
+    row[kRowZ1 + j] = acc * gelu_grad(row[kRowZ1 + j], train);
+  }
+  __syncthreads();
+  // weight gradients summed over the block's samples (thread s owns column s)
+  float * out = partial + (size_t)blockIdx.x * (kParams + 1);
+  {
+    float acc[kIn], bacc = 0.f;
+    for (int i = 0; i < kIn; ++i)
+      acc[i] = 0.f;
+    for (int r = 0; r < kTB; ++r)
+    {
+      const float * rr = rows + r * kRowStride;
+      const float   dz = rr[kRowZ1 + s];
+      bacc += dz;
+      for (int i = 0; i < kIn; ++i)
+        acc[i] = fmaf(rr[kRowX + i], dz, acc[i]);
+    }
+    for (int i = 0; i < kIn; ++i)
+      out[kOffW1 + i * kHid + s] = acc[i];
+    out[kOffB1 + s] = bacc;
+  }
+  {
+    float acc[kHid], bacc = 0.f;
+    for (int j = 0; j < kHid; ++j)
+      acc[j] = 0.f;
+    for (int r = 0; r < kTB; ++r)
+    {
+      const float * rr = rows + r * kRowStride;
+      const float   dz = rr[kRowZ2 + s];
+      bacc += dz;
+      for (int j = 0; j < kHid; ++j)
+        acc[j] = fmaf(rr[kRowH1 + j], dz, acc[j]);
+    }
+    for (int j = 0; j < kHid; ++j)
+      out[kOffW2 + j * kHid + s] = acc[j];
+    out[kOffB2 + s] = bacc;
+  }
+  {
+    float acc[kOut];
+    for (int o = 0; o < kOut; ++o)
+      acc[o] = 0.f;
+    for (int r = 0; r < kTB; ++r)
+    {
+      const float * rr = rows + r * kRowStride;
+      const float   h = rr[kRowH2 + s];
+      for (int o = 0; o < kOut; ++o)
+        acc[o] = fmaf(h, rr[kRowY + o], acc[o]);
+    }
+    for (int o = 0; o < kOut; ++o)
+      out[kOffW3 + s * kOut + o] = acc[o];
+  }
+  if (s < kOut)
+  {
+    float b = 0.f;
+    for (int r = 0; r < kTB; ++r)
+      b += rows[r * kRowStride + kRowY + s];
+    out[kOffB3 + s] = b;
+  }
+  if (s == 0)
+  {
+    float l = 0.f;
+    for (int r = 0; r < kTB; ++r)
+      l += rows[r * kRowStride + kRowLoss];
+    out[kParams] = l;
+  }
+}
+
+// Sum of the block partials in block order (deterministic); optionally an
+// Adam step.  grad_out / loss_out receive the sums when non-null.
+__global__ void
+k_reduce_adam(const float * __restrict__ partial, int nblocks, float * __restrict__ W,
+              float * __restrict__ m, float * __restrict__ v, int adam, float lr, float bc1,
+              float bc2, float * __restrict__ grad_out, double * __restrict__ loss_out)
+{
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p > kParams)
+    return;
+  double g = 0.0;
+  for (int b = 0; b < nblocks; ++b)
+    g += partial[(size_t)b * (kParams + 1) + p];
+  if (p == kParams)
+  {
+    if (loss_out)
+      *loss_out = g;
+    return;
+  }
+  if (grad_out)
+    grad_out[p] = (float)g;
+  if (adam)
+  {
+    const float beta1 = 0.9f, beta2 = 0.999f, eps = 1e-8f;
+    const float gf = (float)g;
+    const float mm = beta1 * m[p] + (1.f - beta1) * gf;
+    const float vv = beta2 * v[p] + (1.f - beta2) * gf * gf;
+    m[p] = mm;
+    v[p] = vv;
+    W[p] -= lr * (mm / bc1) / (sqrtf(vv / bc2) + eps);
+  }
+}
+
+// Tensor-core forward (the deployed path) on features: one face per thread.
+__global__ void __launch_bounds__(128)
+k_forward_mma(const uint32_t * __restrict__ pack, const float * __restrict__ feat, int64_t n,
+              float * __restrict__ out)
+{
+  __shared__ __align__(16) uint32_t sw[kPackWords];
+  __shared__ float                  sb[kBiasFloats];
+  __shared__ uint32_t               sx[4][kStageXWords];
+  __shared__ float                  so[4][kStageOFloats];
+  for (int q = threadIdx.x; q < kPackWords; q += blockDim.x)
+    sw[q] = pack[q];
+  for (int q = threadIdx.x; q < kBiasFloats; q += blockDim.x)
+    sb[q] = reinterpret_cast<const float *>(pack + kPackWords)[q];
+  __syncthreads();
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  float         f[kIn], y[kOut];
+  for (int q = 0; q < kIn; ++q)
+    f[q] = s < n ? feat[s * kIn + q] : 0.f;
+  const int warp = threadIdx.x >> 5;
+  warp_forward(sw, sb, sx[warp], so[warp], f, y);
+  if (s < n)
+    for (int o = 0; o < kOut; ++o)
+      out[s * kOut + o] = y[o];
+}
+
+// ---------------------------------------------------------------- host
+
+uint16_t
+bf16_bits_rn(float x)
+{
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  if ((u & 0x7fffffffu) > 0x7f800000u) // NaN
+    return (uint16_t)((u >> 16) | 0x40u);
+  u += 0x7fffu + ((u >> 16) & 1u);
+  return (uint16_t)(u >> 16);
+}
+
+void
+pack_layer(const float * W, int K, int N, uint32_t * out)
+{
+  const int KT = K / 16, NT = N / 8;
+  for (int kt = 0; kt < KT; ++kt)
+    for (int nt = 0; nt < NT; ++nt)
+      for (int lane = 0; lane < 32; ++lane)
+      {
+        const int g = lane >> 2, t = lane & 3, n = nt * 8 + g;
+        auto      w = [&](int k) { return (uint32_t)bf16_bits_rn(W[k * N + n]); };
+        uint32_t *o = out + ((size_t)(kt * NT + nt) * 32 + lane) * 2;
+        o[0] = w(kt * 16 + 2 * t) | (w(kt * 16 + 2 * t + 1) << 16);
+        o[1] = w(kt * 16 + 8 + 2 * t) | (w(kt * 16 + 8 + 2 * t + 1) << 16);
+      }
+}
+
+uint64_t
+splitmix64(uint64_t & s)
+{
+  uint64_t z = (s += 0x9e3779b97f4a7c15ull);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+double
+uniform01(uint64_t & s)
+{
+  return (double)(splitmix64(s) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+int
+fail(mhd_mlp * m, int rc, const std::string & msg)
+{
+  if (m)
+    m->err = msg;
+  return rc;
+}
+
+#define MLP_CK(call)                                                                   \
+  do                                                                                   \
+  {                                                                                    \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess)                                                             \
+      return fail(m, MHD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+int
+upload_params(mhd_mlp * m)
+{
+  MLP_CK(cudaMemcpy(m->d_params, m->params.data(), kParams * sizeof(float), cudaMemcpyHostToDevice));
+  return MHD_OK;
+}
+
+int
+download_params(mhd_mlp * m)
+{
+  MLP_CK(cudaMemcpy(m->params.data(), m->d_params, kParams * sizeof(float), cudaMemcpyDeviceToHost));
+  return MHD_OK;
+}
+
+// RAII device buffer
+template <class T>
+struct DevBuf
+{
+  T * p = nullptr;
+  ~DevBuf()
+  {
+    if (p)
+      cudaFree(p);
+  }
+  cudaError_t
+  alloc(size_t n)
+  {
+    return cudaMalloc(&p, n * sizeof(T));
+  }
+};
+
+int
+encode_on_device(mhd_mlp * m, const float * records, int64_t n, DevBuf<float> & feat,
+                 DevBuf<float> & tgt)
+{
+  DevBuf<float> rec;
+  MLP_CK(rec.alloc((size_t)n * kRecord));
+  MLP_CK(feat.alloc((size_t)n * kIn));
+  MLP_CK(tgt.alloc((size_t)n * kOut));
+  MLP_CK(cudaMemcpyAsync(rec.p, records, (size_t)n * kRecord * sizeof(float), cudaMemcpyHostToDevice,
+                         m->stream));
+  k_encode<<<(unsigned)((n + 127) / 128), 128, 0, m->stream>>>(rec.p, n, feat.p, tgt.p);
+  MLP_CK(cudaGetLastError());
+  MLP_CK(cudaStreamSynchronize(m->stream));
+  return MHD_OK;
+}
+
+int
+set_train_smem()
+{
+  static bool done = false;
+  if (!done)
+  {
+    if (cudaFuncSetAttribute(k_fwd_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTrain) !=
+        cudaSuccess)
+      return MHD_ERR_CUDA;
+    done = true;
+  }
+  return MHD_OK;
+}
+
+} // namespace
+
+namespace mhd
+{
+// Packed weights + biases of a network for the flux stage (used by mhd_capi.cpp).
+void
+mlp_pack(const float * params, uint32_t * out)
+{
+  pack_layer(params + kOffW1, kIn, kHid, out + kPackW1);
+  pack_layer(params + kOffW2, kHid, kHid, out + kPackW2);
+  pack_layer(params + kOffW3, kHid, kOut, out + kPackW3);
+  float * b = reinterpret_cast<float *>(out + kPackWords);
+  std::memcpy(b, params + kOffB1, kHid * sizeof(float));
+  std::memcpy(b + kHid, params + kOffB2, kHid * sizeof(float));
+  std::memcpy(b + 2 * kHid, params + kOffB3, kOut * sizeof(float));
+}
+
+double
+mlp_gamma(const mhd_mlp * m)
+{
+  return m->gamma0;
+}
+
+const float *
+mlp_params(const mhd_mlp * m)
+{
+  return m->params.data();
+}
+} // namespace mhd
+
+extern "C"
+{
+
+  int
+  mhd_mlp_create(uint64_t seed, double gamma0, mhd_mlp ** out)
+  {
+    if (!out || !(gamma0 > 1.0))
+      return MHD_ERR_INVALID_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+      return MHD_ERR_NO_DEVICE;
+    mhd_mlp * m = new mhd_mlp;
+    *out = m;
+    m->gamma0 = gamma0;
+    MLP_CK(cudaGetDevice(&m->device));
+    MLP_CK(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+    MLP_CK(cudaMalloc(&m->d_params, kParams * sizeof(float)));
+    MLP_CK(cudaMalloc(&m->d_m, kParams * sizeof(float)));
+    MLP_CK(cudaMalloc(&m->d_v, kParams * sizeof(float)));
+    MLP_CK(cudaMemset(m->d_m, 0, kParams * sizeof(float)));
+    MLP_CK(cudaMemset(m->d_v, 0, kParams * sizeof(float)));
+    // Glorot-uniform weights, zero biases
+    m->params.assign(kParams, 0.f);
+    uint64_t  s = seed;
+    auto      init = [&](int off, int fan_in, int fan_out, int used_in, int used_out) {
+      const double lim = std::sqrt(6.0 / (used_in + used_out));
+      for (int i = 0; i < fan_in; ++i)
+        for (int o = 0; o < fan_out; ++o)
+        {
+          const double r = (2.0 * uniform01(s) - 1.0) * lim;
+          m->params[off + i * fan_out + o] = (i < used_in && o < used_out) ? (float)r : 0.f;
+        }
+    };
+    init(kOffW1, kIn, kHid, 15, kHid);
+    init(kOffW2, kHid, kHid, kHid, kHid);
+    init(kOffW3, kHid, kOut, kHid, kOutUsed);
+    return upload_params(m);
+  }
+
+  int
+  mhd_mlp_destroy(mhd_mlp * m)
+  {
+    if (!m)
+      return MHD_ERR_INVALID_ARG;
+    if (m->d_params)
+      cudaFree(m->d_params);
+    if (m->d_m)
+      cudaFree(m->d_m);
+    if (m->d_v)
+      cudaFree(m->d_v);
+    if (m->stream)
+      cudaStreamDestroy(m->stream);
+    delete m;
+    return MHD_OK;
+  }
+
+  const char *
+  mhd_mlp_last_error(mhd_mlp * m)
+  {
+    return m ? m->err.c_str() : "null network";
+  }
+
+  int
+  mhd_mlp_set_params(mhd_mlp * m, const float * params, int n)
+  {
+    if (!m || !params)
+      return MHD_ERR_INVALID_ARG;
+    if (n != kParams)
+      return fail(m, MHD_ERR_INVALID_ARG, "parameter count must be MHD_MLP_PARAMS");
+    MLP_CK(cudaSetDevice(m->device));
+    m->params.assign(params, params + kParams);
+    MLP_CK(cudaMemset(m->d_m, 0, kParams * sizeof(float)));
+    MLP_CK(cudaMemset(m->d_v, 0, kParams * sizeof(float)));
+    m->adam_step = 0;
+    return upload_params(m);
+  }
+
+  int
+  mhd_mlp_get_params(mhd_mlp * m, float * params, int n)
+  {
+    if (!m || !params)
+      return MHD_ERR_INVALID_ARG;
+    if (n != kParams)
+      return fail(m, MHD_ERR_INVALID_ARG, "parameter count must be MHD_MLP_PARAMS");
+    std::memcpy(params, m->params.data(), kParams * sizeof(float));
+    return MHD_OK;
+  }
+
+  int
+  mhd_mlp_gamma(mhd_mlp * m, double * gamma0)
+  {
+    if (!m || !gamma0)
+      return MHD_ERR_INVALID_ARG;
+    *gamma0 = m->gamma0;
+    return MHD_OK;
+  }
+
+  int
+  mhd_mlp_encode(mhd_mlp * m, const float * records, int64_t n, float * features,
+                 float * targets)
+  {
+    if (!m || !records || n <= 0 || !features || !targets)
+      return MHD_ERR_INVALID_ARG;
+    MLP_CK(cudaSetDevice(m->device));
+    DevBuf<float> feat, tgt;
+    if (int rc = encode_on_device(m, records, n, feat, tgt))
+      return rc;
+    MLP_CK(cudaMemcpy(features, feat.p, (size_t)n * kIn * sizeof(float), cudaMemcpyDeviceToHost));
+    MLP_CK(cudaMemcpy(targets, tgt.p, (size_t)n * kOut * sizeof(float), cudaMemcpyDeviceToHost));
+    return MHD_OK;
+  }
+
+  int
+  mhd_mlp_gradient(mhd_mlp * m, const float * features, const float * targets, int64_t n,
+                   int mode, float * grad, double * loss)
+  {
+    if (!m || !features || !targets || n <= 0 || !grad ||
+        (mode != MHD_MLP_CHECK && mode != MHD_MLP_TRAIN))
+      return MHD_ERR_INVALID_ARG;
+    MLP_CK(cudaSetDevice(m->device));
+    if (set_train_smem())
+      return fail(m, MHD_ERR_CUDA, "cannot reserve shared memory for the training kernel");
+    DevBuf<float> feat, tgt, partial, g;
+    DevBuf<double> l;
+    const int     nb = (int)((n + kTB - 1) / kTB);
+    MLP_CK(feat.alloc((size_t)n * kIn));
+    MLP_CK(tgt.alloc((size_t)n * kOut));
+    MLP_CK(partial.alloc((size_t)nb * (kParams + 1)));
+    MLP_CK(g.alloc(kParams));
+    MLP_CK(l.alloc(1));
+    MLP_CK(cudaMemcpy(feat.p, features, (size_t)n * kIn * sizeof(float), cudaMemcpyHostToDevice));
+    MLP_CK(cudaMemcpy(tgt.p, targets, (size_t)n * kOut * sizeof(float), cudaMemcpyHostToDevice));
+    const float norm = (float)(1.0 / ((double)n * kOutUsed));
+    k_fwd_bwd<<<nb, kTB, kSmemTrain, m->stream>>>(m->d_params, feat.p, tgt.p, nullptr, 0, n, norm,
+                                                  mode == MHD_MLP_TRAIN, 0.f, partial.p);
+    k_reduce_adam<<<(kParams + 1 + 255) / 256, 256, 0, m->stream>>>(
+      partial.p, nb, m->d_params, m->d_m, m->d_v, 0, 0.f, 1.f, 1.f, g.p, l.p);
+    MLP_CK(cudaGetLastError());
+    MLP_CK(cudaStreamSynchronize(m->stream));
+    MLP_CK(cudaMemcpy(grad, g.p, kParams * sizeof(float), cudaMemcpyDeviceToHost));
+    double lsum = 0.0;
+    MLP_CK(cudaMemcpy(&lsum, l.p, sizeof(double), cudaMemcpyDeviceToHost));
+    if (loss)
+      *loss = lsum * norm;
+    return MHD_OK;
+  }
+
+  int
+  mhd_mlp_train(mhd_mlp * m, const float * records, int64_t n, int epochs, int batch, float lr,
+                float weight_power, uint64_t seed, float * loss_history)
+  {
+    if (!m || !records || n < kTB || epochs <= 0 || batch < kTB || !(lr > 0.f))
+      return MHD_ERR_INVALID_ARG;
+    MLP_CK(cudaSetDevice(m->device));
+    if (set_train_smem())
+      return fail(m, MHD_ERR_CUDA, "cannot reserve shared memory for the training kernel");
+    batch = (batch / kTB) * kTB;
+    DevBuf<float> feat, tgt, partial;
+    DevBuf<int>   perm;
+    DevBuf<double> l;
+    if (int rc = encode_on_device(m, records, n, feat, tgt))
+      return rc;
+    const int nbb = batch / kTB;
+    MLP_CK(partial.alloc((size_t)nbb * (kParams + 1)));
+    MLP_CK(perm.alloc((size_t)n));
+    MLP_CK(l.alloc(1));
+    std::vector<int> h((size_t)n);
+    uint64_t         s = seed;
+    const int64_t    nbatch = n / batch > 0 ? n / batch : 1;
+    const int64_t    total = nbatch * epochs;
+    int64_t          it = 0;
+    for (int ep = 0; ep < epochs; ++ep)
+    {
+      for (int64_t q = 0; q < n; ++q)
+        h[q] = (int)q;
+      for (int64_t q = n - 1; q > 0; --q) // Fisher-Yates
+        std::swap(h[q], h[(int64_t)(uniform01(s) * (double)(q + 1)) % (q + 1)]);
+      MLP_CK(cudaMemcpyAsync(perm.p, h.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice,
+                             m->stream));
+      double ep_loss = 0.0;
+      for (int64_t b = 0; b < nbatch; ++b, ++it)
+      {
+        const int64_t first = b * batch;
+        const int64_t cnt = std::min<int64_t>(batch, n - first);
+        const int     nb = (int)((cnt + kTB - 1) / kTB);
+        const float   norm = (float)(1.0 / ((double)cnt * kOutUsed));
+        // cosine decay to lr / 20
+        const double  frac = (double)it / (double)std::max<int64_t>(total - 1, 1);
+        const float   lr_t = (float)(lr * (0.05 + 0.95 * 0.5 * (1.0 + std::cos(M_PI * frac))));
+        ++m->adam_step;
+        const float bc1 = (float)(1.0 - std::pow(0.9, (double)m->adam_step));
+        const float bc2 = (float)(1.0 - std::pow(0.999, (double)m->adam_step));
+        k_fwd_bwd<<<nb, kTB, kSmemTrain, m->stream>>>(m->d_params, feat.p, tgt.p, perm.p, first,
+                                                      first + cnt, norm, 1, weight_power,
+                                                      partial.p);
+        k_reduce_adam<<<(kParams + 1 + 255) / 256, 256, 0, m->stream>>>(
+          partial.p, nb, m->d_params, m->d_m, m->d_v, 1, lr_t, bc1, bc2, nullptr, l.p);
+        if (loss_history)
+        {
+          double lb = 0.0;
+          MLP_CK(cudaMemcpyAsync(&lb, l.p, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+          MLP_CK(cudaStreamSynchronize(m->stream));
+          ep_loss += lb * norm;
+        }
+      }
+      MLP_CK(cudaGetLastError());
+      if (loss_history)
+        loss_history[ep] = (float)(ep_loss / (double)nbatch);
+    }
+    MLP_CK(cudaStreamSynchronize(m->stream));
+    return download_params(m);
+  }
+
+  int
+  mhd_mlp_forward(mhd_mlp * m, const float * features, int64_t n, float * out)
+  {
+    if (!m || !features || n <= 0 || !out)
+      return MHD_ERR_INVALID_ARG;
+    MLP_CK(cudaSetDevice(m->device));
+    std::vector<uint32_t> pack(kPackWords + kBiasFloats);
+    mhd::mlp_pack(m->params.data(), pack.data());
+    DevBuf<uint32_t> dp;
+    DevBuf<float>    feat, o;
+    MLP_CK(dp.alloc(pack.size()));
+    MLP_CK(feat.alloc((size_t)n * kIn));
+    MLP_CK(o.alloc((size_t)n * kOut));
+    MLP_CK(cudaMemcpy(dp.p, pack.data(), pack.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    MLP_CK(cudaMemcpy(feat.p, features, (size_t)n * kIn * sizeof(float), cudaMemcpyHostToDevice));
+    k_forward_mma<<<(unsigned)((n + 127) / 128), 128, 0, m->stream>>>(dp.p, feat.p, n, o.p);
+    MLP_CK(cudaGetLastError());
+    MLP_CK(cudaStreamSynchronize(m->stream));
+    MLP_CK(cudaMemcpy(out, o.p, (size_t)n * kOut * sizeof(float), cudaMemcpyDeviceToHost));
+    return MHD_OK;
+  }
+
+} // extern "C"

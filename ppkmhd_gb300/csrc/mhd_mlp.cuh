@@ -1,0 +1,336 @@
+// The HLLD flux surrogate: a 15-64-64-7 multilayer perceptron with GELU
+// activations, BF16 weights and activations and FP32 accumulation.
+//
+// It replaces riemann_hlld (RiemannSolvers_MHD.h:133-367) on faces that a
+// jump sensor flags as smooth.  The network does not predict the flux
+// itself: the flux is split into the central part
+//     Fc = (F(qL) + F(qR)) / 2          (exact, from the physical MHD flux)
+// and the upwind dissipation D = Fc - F_HLLD, and the network predicts D in
+// units of the face's own scales times the jump size:
+//     F = Fc - scale * sJ * net(features).
+// Everything here is dimensionless per face, so one network serves every
+// density, pressure and field level.
+//
+// Per face, in the face-normal frame (a = normal B, q = [rho, vn, vt1, vt2,
+// p, Bt1, Bt2] left and right):
+//   rs = (rhoL + rhoR) / 2
+//   Ps = (pL + pR) / 2 + (|BL|^2 + |BR|^2) / 4       (total-pressure scale)
+//   vs = sqrt(Ps / rs), bs = sqrt(Ps)
+//   mean features  f0..f2 = mean(vn, vt1, vt2) / vs, f3 = mean(p) / Ps,
+//                  f4, f5 = mean(Bt1, Bt2) / bs, f6 = a / bs
+//   half jumps     h = (qR - qL) / 2 over (rs, vs, vs, vs, Ps, bs, bs)
+//   J = max |h|  (the smoothness sensor), sJ = max(J, kJFloor)
+//   f7..f13 = h / sJ, f14 = sJ / kTauRef, f15 = 0 (padding)
+//   scale = (rs vs, Ps vs, Ps, Ps, Ps, bs vs, bs vs) for the flux
+//           components (rho, E, mn, mt1, mt2, Bt1, Bt2)
+// GELU is the tanh form of Hendrycks and Gimpel (2016):
+//   gelu(x) = x/2 (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))).
+//
+// Parameter vector (FP32 master copy), row = input, column = output unit:
+//   W1[16][64] b1[64] W2[64][64] b2[64] W3[64][8] b3[8]   (5768 floats)
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+namespace mhd
+{
+namespace mlp
+{
+
+constexpr int kIn = 16;  // 15 features + 1 zero pad
+constexpr int kHid = 64;
+constexpr int kOut = 8;  // 7 flux components + 1 pad
+constexpr int kOutUsed = 7;
+
+constexpr int kOffW1 = 0;
+constexpr int kOffB1 = kOffW1 + kIn * kHid;
+constexpr int kOffW2 = kOffB1 + kHid;
+constexpr int kOffB2 = kOffW2 + kHid * kHid;
+constexpr int kOffW3 = kOffB2 + kHid;
+constexpr int kOffB3 = kOffW3 + kHid * kOut;
+constexpr int kParams = kOffB3 + kOut; // 5768
+
+// mma.m16n8k16 fragments of the three weight matrices, as bf16x2 words:
+// [k-tile][n-tile][lane][2]
+constexpr int kPackW1 = 0;
+constexpr int kPackW2 = kPackW1 + (kIn / 16) * (kHid / 8) * 64;
+constexpr int kPackW3 = kPackW2 + (kHid / 16) * (kHid / 8) * 64;
+constexpr int kPackWords = kPackW3 + (kHid / 16) * (kOut / 8) * 64; // 2816
+constexpr int kBiasFloats = kHid + kHid + kOut;                    // 136
+
+constexpr double kJFloor = 1e-4;
+constexpr double kTauRef = 0.1;
+
+// Harvested face sample: the public record of MHD_SAMPLE_FLOATS floats.
+constexpr int kRecord = 24;
+constexpr int kRecQL = 0, kRecQR = 7, kRecA = 14, kRecJ = 15, kRecD = 16, kRecGamma = 23;
+
+// Dimensionless encoding of one face (see the file comment).  q arrays in
+// the order rho, vn, vt1, vt2, p, Bt1, Bt2.  Returns J.
+template <class T>
+__host__ __device__ inline T
+encode(const T * qL, const T * qR, T a, T * f, T * scale)
+{
+  const T rs = T(0.5) * (qL[0] + qR[0]);
+  const T b2L = a * a + qL[5] * qL[5] + qL[6] * qL[6];
+  const T b2R = a * a + qR[5] * qR[5] + qR[6] * qR[6];
+  const T Ps = T(0.5) * (qL[4] + qR[4]) + T(0.25) * (b2L + b2R);
+  const T irs = T(1) / rs, iPs = T(1) / Ps;
+  const T vs = sqrt(Ps * irs), bs = sqrt(Ps);
+  const T ivs = T(1) / vs, ibs = T(1) / bs;
+  f[0] = T(0.5) * (qL[1] + qR[1]) * ivs;
+  f[1] = T(0.5) * (qL[2] + qR[2]) * ivs;
+  f[2] = T(0.5) * (qL[3] + qR[3]) * ivs;
+  f[3] = T(0.5) * (qL[4] + qR[4]) * iPs;
+  f[4] = T(0.5) * (qL[5] + qR[5]) * ibs;
+  f[5] = T(0.5) * (qL[6] + qR[6]) * ibs;
+  f[6] = a * ibs;
+  T h[7];
+  h[0] = T(0.5) * (qR[0] - qL[0]) * irs;
+  h[1] = T(0.5) * (qR[1] - qL[1]) * ivs;
+  h[2] = T(0.5) * (qR[2] - qL[2]) * ivs;
+  h[3] = T(0.5) * (qR[3] - qL[3]) * ivs;
+  h[4] = T(0.5) * (qR[4] - qL[4]) * iPs;
+  h[5] = T(0.5) * (qR[5] - qL[5]) * ibs;
+  h[6] = T(0.5) * (qR[6] - qL[6]) * ibs;
+  T J = T(0);
+  for (int q = 0; q < 7; ++q)
+    J = fmax(J, fabs(h[q]));
+  const T sJ = fmax(J, T(kJFloor));
+  const T isJ = T(1) / sJ;
+  for (int q = 0; q < 7; ++q)
+    f[7 + q] = h[q] * isJ;
+  f[14] = sJ * T(1.0 / kTauRef);
+  f[15] = T(0);
+  scale[0] = rs * vs * sJ;
+  scale[1] = Ps * vs * sJ;
+  scale[2] = Ps * sJ;
+  scale[3] = Ps * sJ;
+  scale[4] = Ps * sJ;
+  scale[5] = bs * vs * sJ;
+  scale[6] = bs * vs * sJ;
+  return J;
+}
+
+// Physical ideal-MHD flux in the face-normal frame, components (rho, E, mn,
+// mt1, mt2, Bt1, Bt2): the flux vector of riemann_hlld
+// (RiemannSolvers_MHD.h:358-366).
+template <class T>
+__host__ __device__ inline void
+physical_flux(const T * q, T a, T gamma0, T * F)
+{
+  const T r = q[0], u = q[1], v = q[2], w = q[3], p = q[4], b = q[5], c = q[6];
+  const T B2 = a * a + b * b + c * c;
+  const T Ptot = p + T(0.5) * B2;
+  const T E = p / (gamma0 - T(1)) + T(0.5) * r * (u * u + v * v + w * w) + T(0.5) * B2;
+  const T vB = u * a + v * b + w * c;
+  F[0] = r * u;
+  F[1] = (E + Ptot) * u - a * vB;
+  F[2] = r * u * u + Ptot - a * a;
+  F[3] = r * u * v - a * b;
+  F[4] = r * u * w - a * c;
+  F[5] = b * u - a * v;
+  F[6] = c * u - a * w;
+}
+
+template <class T>
+__host__ __device__ inline void
+central_flux(const T * qL, const T * qR, T a, T gamma0, T * Fc)
+{
+  T FL[7], FR[7];
+  physical_flux(qL, a, gamma0, FL);
+  physical_flux(qR, a, gamma0, FR);
+  for (int q = 0; q < 7; ++q)
+    Fc[q] = T(0.5) * (FL[q] + FR[q]);
+}
+
+// |D / scale| above this is treated as a failed prediction.
+constexpr float kDissBound = 16.0f;
+
+// ---------------------------------------------------------------- device
+
+#ifdef __CUDACC__
+
+constexpr float kGeluC0 = 0.7978845608028654f; // sqrt(2/pi)
+constexpr float kGeluC1 = 0.044715f;
+
+__device__ __forceinline__ float
+tanh_hw(float x)
+{
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// GELU with the hardware tanh approximation in FP32.
+__device__ __forceinline__ float
+gelu_hw(float x)
+{
+  const float u = x * (kGeluC0 + (kGeluC0 * kGeluC1) * x * x);
+  const float hx = 0.5f * x;
+  return fmaf(hx, tanh_hw(u), hx);
+}
+
+// The deployed activation: GELU evaluated in BF16 arithmetic on a BF16
+// input, two lanes per instruction (x^2, x (c0 + c0 c1 x^2), tanh, x/2 (1 +
+// tanh)).  gelu_bf16 is the same sequence on one value, for training.
+__device__ __forceinline__ uint32_t
+tanh_bf16x2(uint32_t x)
+{
+  uint32_t y;
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(y) : "r"(x));
+  return y;
+}
+
+__device__ __forceinline__ unsigned short
+tanh_bf16(unsigned short x)
+{
+  unsigned short y;
+  asm("tanh.approx.bf16 %0, %1;" : "=h"(y) : "h"(x));
+  return y;
+}
+
+__device__ __forceinline__ uint32_t
+gelu_bf16x2(uint32_t xw)
+{
+  const __nv_bfloat162 x = *reinterpret_cast<const __nv_bfloat162 *>(&xw);
+  const __nv_bfloat162 c0 = __float2bfloat162_rn(kGeluC0);
+  const __nv_bfloat162 c01 = __float2bfloat162_rn(kGeluC0 * kGeluC1);
+  const __nv_bfloat162 h = __float2bfloat162_rn(0.5f);
+  const __nv_bfloat162 u = __hmul2(x, __hfma2(__hmul2(x, x), c01, c0));
+  const uint32_t       uw = *reinterpret_cast<const uint32_t *>(&u);
+  const uint32_t       tw = tanh_bf16x2(uw);
+  const __nv_bfloat162 t = *reinterpret_cast<const __nv_bfloat162 *>(&tw);
+  const __nv_bfloat162 hx = __hmul2(x, h);
+  const __nv_bfloat162 g = __hfma2(hx, t, hx);
+  return *reinterpret_cast<const uint32_t *>(&g);
+}
+
+__device__ __forceinline__ float
+gelu_bf16(float z)
+{
+  const __nv_bfloat16 x = __float2bfloat16_rn(z);
+  const __nv_bfloat16 c0 = __float2bfloat16_rn(kGeluC0);
+  const __nv_bfloat16 c01 = __float2bfloat16_rn(kGeluC0 * kGeluC1);
+  const __nv_bfloat16 h = __float2bfloat16_rn(0.5f);
+  const __nv_bfloat16 u = __hmul(x, __hfma(__hmul(x, x), c01, c0));
+  const __nv_bfloat16 t = __ushort_as_bfloat16(tanh_bf16(__bfloat16_as_ushort(u)));
+  const __nv_bfloat16 hx = __hmul(x, h);
+  return __bfloat162float(__hfma(hx, t, hx));
+}
+
+__device__ __forceinline__ uint32_t
+pack_bf16x2(float lo, float hi)
+{
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t *>(&v);
+}
+
+__device__ __forceinline__ void
+mma_16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
+{
+  asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+               "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+               : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+               : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Shared staging of one warp: 32 feature rows of 16 bf16 (row stride 12
+// words: conflict-free fragment reads) and 32 output rows of 8 floats.
+constexpr int kStageXWords = 32 * 12;
+constexpr int kStageOFloats = 32 * 9;
+
+// C fragments (two adjacent 8-wide n-tiles) -> A fragment of the next layer,
+// with the activation applied.
+__device__ __forceinline__ void
+act_to_a(const float (&c0)[4], const float (&c1)[4], uint32_t (&a)[4])
+{
+  a[0] = gelu_bf16x2(pack_bf16x2(c0[0], c0[1]));
+  a[1] = gelu_bf16x2(pack_bf16x2(c0[2], c0[3]));
+  a[2] = gelu_bf16x2(pack_bf16x2(c1[0], c1[1]));
+  a[3] = gelu_bf16x2(pack_bf16x2(c1[2], c1[3]));
+}
+
+// Forward pass of the network for the 32 faces of a warp (one per lane);
+// every lane of the warp must call it.  wp: packed weights (shared), bias:
+// b1, b2, b3 (shared), sx / so: this warp's staging.
+__device__ __forceinline__ void
+warp_forward(const uint32_t * __restrict__ wp, const float * __restrict__ bias, uint32_t * sx,
+             float * so, const float (&f)[kIn], float (&out)[kOut])
+{
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int q = 0; q < 8; ++q)
+    sx[lane * 12 + q] = pack_bf16x2(f[2 * q], f[2 * q + 1]);
+  __syncwarp();
+  const uint2 * W1 = reinterpret_cast<const uint2 *>(wp + kPackW1);
+  const uint2 * W2 = reinterpret_cast<const uint2 *>(wp + kPackW2);
+  const uint2 * W3 = reinterpret_cast<const uint2 *>(wp + kPackW3);
+  const float * b1 = bias;
+  const float * b2 = bias + kHid;
+  const float * b3 = bias + 2 * kHid;
+#pragma unroll 1
+  for (int mt = 0; mt < 2; ++mt)
+  {
+    const int r0 = mt * 16 + g, r1 = r0 + 8;
+    uint32_t  a[4] = { sx[r0 * 12 + t], sx[r1 * 12 + t], sx[r0 * 12 + t + 4], sx[r1 * 12 + t + 4] };
+    float     c[8][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt)
+    {
+      const float x0 = b1[nt * 8 + 2 * t], x1 = b1[nt * 8 + 2 * t + 1];
+      c[nt][0] = x0;
+      c[nt][1] = x1;
+      c[nt][2] = x0;
+      c[nt][3] = x1;
+      const uint2 w = W1[nt * 32 + lane];
+      mma_16816(c[nt], a, w.x, w.y);
+    }
+    uint32_t h[4][4];
+#pragma unroll
+    for (int kt = 0; kt < 4; ++kt)
+      act_to_a(c[2 * kt], c[2 * kt + 1], h[kt]);
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt)
+    {
+      const float x0 = b2[nt * 8 + 2 * t], x1 = b2[nt * 8 + 2 * t + 1];
+      c[nt][0] = x0;
+      c[nt][1] = x1;
+      c[nt][2] = x0;
+      c[nt][3] = x1;
+#pragma unroll
+      for (int kt = 0; kt < 4; ++kt)
+      {
+        const uint2 w = W2[(kt * 8 + nt) * 32 + lane];
+        mma_16816(c[nt], h[kt], w.x, w.y);
+      }
+    }
+#pragma unroll
+    for (int kt = 0; kt < 4; ++kt)
+      act_to_a(c[2 * kt], c[2 * kt + 1], h[kt]);
+    float y[4] = { b3[2 * t], b3[2 * t + 1], b3[2 * t], b3[2 * t + 1] };
+#pragma unroll
+    for (int kt = 0; kt < 4; ++kt)
+    {
+      const uint2 w = W3[kt * 32 + lane];
+      mma_16816(y, h[kt], w.x, w.y);
+    }
+    so[r0 * 9 + 2 * t] = y[0];
+    so[r0 * 9 + 2 * t + 1] = y[1];
+    so[r1 * 9 + 2 * t] = y[2];
+    so[r1 * 9 + 2 * t + 1] = y[3];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int o = 0; o < kOut; ++o)
+    out[o] = so[lane * 9 + o];
+  __syncwarp();
+}
+
+#endif // __CUDACC__
+
+} // namespace mlp
+} // namespace mhd

@@ -5,6 +5,8 @@
 // inline namespace MHD_VARIANT_TAG.
 #pragma once
 
+#include <algorithm>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -14,6 +16,7 @@
 
 #include "mhd_core.h"
 #include "mhd_kernels.cuh"
+#include "mhd_surrogate.cuh"
 #include "mhd_kernels_v0.cuh"
 
 namespace mhd
@@ -146,6 +149,15 @@ public:
   cudaGraphExec_t graph[2] = { nullptr, nullptr }; // one iteration starting from U / from U2
   cudaGraphExec_t graph_pair[2] = { nullptr, nullptr }; // two iterations
   int64_t launched = 0; // iterations enqueued since the last state reset (parity)
+  // flux surrogate (FP32 builds only)
+  uint32_t *           sur_w = nullptr; // packed weights + biases (mhd_mlp.cuh)
+  unsigned long long * sur_count = nullptr;
+  uint32_t *           sur_list = nullptr; // faces left to HLLD
+  unsigned *           sur_nlist = nullptr;
+  float                sur_tau = 0.f;
+  bool                 sur_on = false;
+  int                  sm_count = 0;
+  int                  sur_blocks_per_sm = 1;
 
   ~SolverImpl() override
   {
@@ -160,6 +172,14 @@ public:
     for (R * b : bufs)
       if (b)
         cudaFree(b);
+    if (sur_w)
+      cudaFree(sur_w);
+    if (sur_count)
+      cudaFree(sur_count);
+    if (sur_list)
+      cudaFree(sur_list);
+    if (sur_nlist)
+      cudaFree(sur_nlist);
     if (diag)
       cudaFree(diag);
     if (st)
@@ -322,10 +342,44 @@ public:
   launch_flux(const Buffers<R> & B)
   {
     const int64_t n = (int64_t)(G.nx + 1) * (G.ny + 1) * (dim == 3 ? G.nz + 1 : 1);
+    if constexpr (sizeof(R) == 4)
+    {
+      if (sur_on)
+      {
+        SurrogateDev S{ sur_w,     reinterpret_cast<const float *>(sur_w + mlp::kPackWords),
+                        sur_tau,   sur_count,
+                        sur_list,  sur_nlist };
+        // grid-stride: one wave of resident blocks (per direction), each
+        // stages the weights once
+        const unsigned nb =
+          std::min(nblocks(n, kMlpThreads),
+                   (unsigned)std::max(1, sur_blocks_per_sm * sm_count / (dim == 2 ? 2 : 3)));
+        cudaMemsetAsync(sur_nlist, 0, sizeof(unsigned), stream);
+        if (dim == 2)
+          k_flux_mlp<2><<<dim3(nb, 2), kMlpThreads, 0, stream>>>(G, B, S);
+        else
+          k_flux_mlp<3><<<dim3(nb, 3), kMlpThreads, 0, stream>>>(G, B, S);
+        return;
+      }
+    }
     if (dim == 2)
       k_flux<R, 2><<<dim3(nblocks(n, 128), 2), 128, 0, stream>>>(G, B);
     else
       k_flux<R, 3><<<dim3(nblocks(n, 128), 3), 128, 0, stream>>>(G, B);
+  }
+  void
+  launch_flux_fallback(const Buffers<R> & B)
+  {
+    if constexpr (sizeof(R) == 4)
+    {
+      const unsigned nb = (unsigned)std::max(1, 4 * sm_count);
+      if (dim == 2)
+        k_flux_fallback<2><<<nb, 128, 0, stream>>>(G, B, sur_list, sur_nlist);
+      else
+        k_flux_fallback<3><<<nb, 128, 0, stream>>>(G, B, sur_list, sur_nlist);
+    }
+    else
+      (void)B;
   }
   void
   launch_emf(const Buffers<R> & B)
@@ -413,8 +467,11 @@ public:
     static const char * v0_3d[] = { "k_boundaries", "k_prim_dt", "k_finalize_dt",
                                     "k_v0_prep3d",  "k_v0_trace", "k_v0_flux",
                                     "k_v0_emf",     "k_v0_update", "k_advance" };
-    const char ** src = version == 2 ? v2 : (dim == 3 ? v0_3d : v0_2d);
-    const int     n = version == 2 ? 8 : (dim == 3 ? 9 : 8);
+    static const char * v2s[] = { "k_boundaries", "k_prim_dt",       "k_finalize_dt",
+                                  "k_trace",      "k_flux_mlp",      "k_flux_fallback",
+                                  "k_emf",        "k_update",        "k_advance" };
+    const char ** src = version == 2 ? (sur_on ? v2s : v2) : (dim == 3 ? v0_3d : v0_2d);
+    const int     n = version == 2 ? (sur_on ? 9 : 8) : (dim == 3 ? 9 : 8);
     for (int q = 0; q < n; ++q)
       names[q] = src[q];
     return n;
@@ -436,6 +493,12 @@ public:
         return launch_trace(B);
       if (q == 4)
         return launch_flux(B);
+      if (sur_on)
+      {
+        if (q == 5)
+          return launch_flux_fallback(B);
+        --q;
+      }
       if (q == 5)
         return launch_emf(B);
       if (q == 6)
@@ -810,6 +873,166 @@ public:
     if (count)
       *count = n;
     return MHD_OK;
+  }
+
+  void
+  drop_graphs()
+  {
+    for (int q = 0; q < 2; ++q)
+    {
+      if (graph[q])
+        cudaGraphExecDestroy(graph[q]);
+      if (graph_pair[q])
+        cudaGraphExecDestroy(graph_pair[q]);
+      graph[q] = graph_pair[q] = nullptr;
+    }
+  }
+
+  // Deploy (wpack != nullptr) or remove the flux surrogate; the packed words
+  // are followed by the biases (mlp::kBiasFloats floats).
+  int
+  set_surrogate(const uint32_t * wpack, double tau) override
+  {
+    if constexpr (sizeof(R) != 4)
+    {
+      (void)wpack;
+      (void)tau;
+      err = "the flux surrogate runs in FP32 contexts only";
+      return MHD_ERR_INVALID_ARG;
+    }
+    else
+    {
+      MHD_CK(cudaStreamSynchronize(stream));
+      drop_graphs();
+      if (!wpack)
+      {
+        sur_on = false;
+        return MHD_OK;
+      }
+      if (version != 2 || G.riemann != MHD_RIEMANN_HLLD)
+      {
+        err = "the flux surrogate needs implementation version 2 and the HLLD solver";
+        return MHD_ERR_INVALID_ARG;
+      }
+      const int64_t nlist = G.box[BOX_FACE].count() * dim;
+      if (nlist >= (int64_t)UINT32_MAX)
+      {
+        err = "grid too large for the surrogate's 32-bit face list";
+        return MHD_ERR_TOO_LARGE;
+      }
+      const size_t bytes = (mlp::kPackWords + mlp::kBiasFloats) * sizeof(uint32_t);
+      if (!sur_w)
+        MHD_CK(cudaMalloc(&sur_w, bytes));
+      if (!sur_count)
+        MHD_CK(cudaMalloc(&sur_count, 2 * sizeof(unsigned long long)));
+      if (!sur_list)
+        MHD_CK(cudaMalloc(&sur_list, nlist * sizeof(uint32_t)));
+      if (!sur_nlist)
+        MHD_CK(cudaMalloc(&sur_nlist, sizeof(unsigned)));
+      MHD_CK(cudaMemcpy(sur_w, wpack, bytes, cudaMemcpyHostToDevice));
+      MHD_CK(cudaMemset(sur_count, 0, 2 * sizeof(unsigned long long)));
+      MHD_CK(cudaMemset(sur_nlist, 0, sizeof(unsigned)));
+      if (!sm_count)
+        MHD_CK(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, P.device));
+      if (dim == 2)
+        MHD_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sur_blocks_per_sm, k_flux_mlp<2>,
+                                                             kMlpThreads, 0));
+      else
+        MHD_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sur_blocks_per_sm, k_flux_mlp<3>,
+                                                             kMlpThreads, 0));
+      sur_blocks_per_sm = std::max(1, sur_blocks_per_sm);
+      sur_tau = (float)tau;
+      sur_on = true;
+      return MHD_OK;
+    }
+  }
+
+  int
+  surrogate_stats(int64_t * used, int64_t * total, int reset) override
+  {
+    unsigned long long h[2] = { 0, 0 };
+    if (sur_count)
+    {
+      MHD_CK(cudaMemcpyAsync(h, sur_count, sizeof h, cudaMemcpyDeviceToHost, stream));
+      MHD_CK(cudaStreamSynchronize(stream));
+      if (reset)
+        MHD_CK(cudaMemset(sur_count, 0, sizeof h));
+    }
+    if (used)
+      *used = (int64_t)h[0];
+    if (total)
+      *total = (int64_t)h[1];
+    return MHD_OK;
+  }
+
+  // Face samples of the current state (the faces of the next iteration):
+  // boundaries, primitives, dt and the trace are computed, nothing is
+  // advanced.  One record per `stride`-th face of each direction.
+  int
+  harvest(int stride, float * host, int64_t capacity, int64_t * count) override
+  {
+    if (version != 2)
+    {
+      err = "face harvesting needs implementation version 2";
+      return MHD_ERR_INVALID_ARG;
+    }
+    if (int rc = read_state())
+      return rc;
+    if (step_finished_host())
+    {
+      err = "the run is finished: no next iteration to sample";
+      return MHD_ERR_INVALID_ARG;
+    }
+    const int64_t nface = G.box[BOX_FACE].count();
+    const int64_t nslot = (nface + stride - 1) / stride;
+    const int64_t nrec = nslot * dim;
+    if (count)
+      *count = nrec;
+    if (!host)
+      return MHD_OK; // size query
+    if (capacity < nrec)
+    {
+      err = "harvest buffer holds " + std::to_string(capacity) + " records, " +
+            std::to_string(nrec) + " needed";
+      return MHD_ERR_TOO_LARGE;
+    }
+    launched = st_host->it;
+    const Buffers<R> B = buffers((int)(launched & 1));
+    float *          d_out = nullptr;
+    MHD_CK(cudaMalloc(&d_out, nrec * mlp::kRecord * sizeof(float)));
+    launch_stage(0, B);
+    launch_stage(1, B);
+    launch_stage(2, B);
+    launch_stage(3, B);
+    if (dim == 2)
+      k_harvest<R, 2><<<dim3(nblocks(nslot, 128), 2), 128, 0, stream>>>(G, B, d_out, stride, nslot);
+    else
+      k_harvest<R, 3><<<dim3(nblocks(nslot, 128), 3), 128, 0, stream>>>(G, B, d_out, stride, nslot);
+    int rc = check_launch();
+    cudaError_t e = cudaMemcpyAsync(host, d_out, nrec * mlp::kRecord * sizeof(float),
+                                    cudaMemcpyDeviceToHost, stream);
+    cudaError_t e2 = cudaStreamSynchronize(stream);
+    cudaFree(d_out);
+    if (rc)
+      return rc;
+    if (e != cudaSuccess || e2 != cudaSuccess)
+    {
+      err = std::string("harvest copy: ") + cudaGetErrorString(e != cudaSuccess ? e : e2);
+      return MHD_ERR_CUDA;
+    }
+    return MHD_OK;
+  }
+
+  void
+  set_time_origin(double t) override
+  {
+    P.tCurrent = t;
+  }
+
+  bool
+  step_finished_host() const
+  {
+    return st_host->t >= st_host->tEnd - 1e-14 || st_host->it >= st_host->nStepmax;
   }
 
   int

@@ -1,0 +1,347 @@
+// Solver-side kernels of the HLLD flux surrogate (mhd_mlp.cuh):
+//  * k_harvest: face samples of the current iteration for training, each
+//    with the FP64 dissipation target D = Fc - F_HLLD;
+//  * k_flux_mlp + k_flux_fallback: the face-flux stage of the iteration
+//    (replacing k_flux): the network on faces the jump sensor flags as
+//    smooth, and HLLD, in a second kernel, on the faces it lists as not.
+// Both rebuild the face states exactly as k_flux does (face_states, the
+// reconstruction of ComputeFluxAndUpdateAlongDirFunctor, MHDRunFunctors2D.h:
+// 1110-1190, 3D:1097-1210).
+#pragma once
+
+#include "mhd_kernels.cuh"
+#include "mhd_mlp.cuh"
+
+namespace mhd
+{
+inline namespace MHD_VARIANT_TAG
+{
+
+// normal-frame State -> (rho, vn, vt1, vt2, p, Bt1, Bt2), a
+template <class R, class T>
+__device__ __forceinline__ void
+to_face7(const State<R> & q, T * o)
+{
+  o[0] = T(q[ID]);
+  o[1] = T(q[IU]);
+  o[2] = T(q[IV]);
+  o[3] = T(q[IW]);
+  o[4] = T(q[IP]);
+  o[5] = T(q[IB]);
+  o[6] = T(q[IC]);
+}
+
+template <class R, int DIM, int d>
+__device__ __forceinline__ void
+harvest_face(const Grid<R> & G, const Buffers<R> & B, int64_t c, float * rec)
+{
+  State<R> qL, qR;
+  face_states<R, DIM, d>(G, B, c, qL, qR);
+  double l7[7], r7[7];
+  to_face7(qL, l7);
+  to_face7(qR, r7);
+  const double a = double(qL[IA]);
+  double       f[mlp::kIn], sc[7], Fc[7];
+  const double J = mlp::encode(l7, r7, a, f, sc);
+  mlp::central_flux(l7, r7, a, double(G.gamma0), Fc);
+  // FP64 HLLD of the (working-precision) face states
+  State<double> dl, dr, fl;
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+  {
+    dl[v] = double(qL[v]);
+    dr[v] = double(qR[v]);
+    fl[v] = 0.0;
+  }
+  riemann_hlld(dl, dr, fl, double(G.gamma0));
+  const double Fh[7] = { fl[ID], fl[IP], fl[IU], fl[IV], fl[IW], fl[IB], fl[IC] };
+#pragma unroll
+  for (int q = 0; q < 7; ++q)
+  {
+    rec[mlp::kRecQL + q] = float(l7[q]);
+    rec[mlp::kRecQR + q] = float(r7[q]);
+    rec[mlp::kRecD + q] = float(Fc[q] - Fh[q]);
+  }
+  rec[mlp::kRecA] = float(a);
+  rec[mlp::kRecJ] = float(J);
+  rec[mlp::kRecGamma] = float(G.gamma0);
+}
+
+// One record per `stride`-th face of each direction:
+// out[(dir * nslot + s) * kRecord ...] for face index s * stride.
+template <class R, int DIM>
+__global__ void __launch_bounds__(128)
+k_harvest(const Grid<R> G, Buffers<R> B, float * __restrict__ out, int stride, int64_t nslot)
+{
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= nslot)
+    return;
+  int i, j, k;
+  if (!box_cell(G.box[BOX_FACE], s * stride, i, j, k))
+    return;
+  const int     dir = blockIdx.y;
+  const int64_t c = cell_at(G, i, j, k);
+  float *       rec = out + ((int64_t)dir * nslot + s) * mlp::kRecord;
+  if (dir == 0)
+    harvest_face<R, DIM, 0>(G, B, c, rec);
+  else if (dir == 1)
+    harvest_face<R, DIM, 1>(G, B, c, rec);
+  else if constexpr (DIM == 3)
+    harvest_face<R, DIM, 2>(G, B, c, rec);
+}
+
+// Device parameters of a deployed surrogate.
+struct SurrogateDev
+{
+  const uint32_t *     wpack; // mlp::kPackWords
+  const float *        bias;  // mlp::kBiasFloats
+  float                tau;   // sensor threshold on J
+  unsigned long long * count; // [0] faces given by the network, [1] faces computed
+  uint32_t *           list;  // faces left to HLLD: face index * DIM + direction
+  unsigned *           nlist; // number of entries (reset before each flux stage)
+};
+
+constexpr int kMlpThreads = 128;
+
+// Encoding of mlp::encode in FP32 with hardware reciprocals and rsqrt.
+__device__ __forceinline__ float
+encode_fast(const float * qL, const float * qR, float a, float * f, float * scale)
+{
+  const float rs = 0.5f * (qL[0] + qR[0]);
+  const float b2L = a * a + qL[5] * qL[5] + qL[6] * qL[6];
+  const float b2R = a * a + qR[5] * qR[5] + qR[6] * qR[6];
+  const float Ps = 0.5f * (qL[4] + qR[4]) + 0.25f * (b2L + b2R);
+  const float irs = __frcp_rn(rs), iPs = __frcp_rn(Ps);
+  const float ibs = rsqrtf(Ps), bs = Ps * ibs;
+  const float ivs = rs * rsqrtf(rs) * ibs, vs = Ps * ivs * irs; // sqrt(rs / Ps), sqrt(Ps / rs)
+  f[0] = 0.5f * (qL[1] + qR[1]) * ivs;
+  f[1] = 0.5f * (qL[2] + qR[2]) * ivs;
+  f[2] = 0.5f * (qL[3] + qR[3]) * ivs;
+  f[3] = 0.5f * (qL[4] + qR[4]) * iPs;
+  f[4] = 0.5f * (qL[5] + qR[5]) * ibs;
+  f[5] = 0.5f * (qL[6] + qR[6]) * ibs;
+  f[6] = a * ibs;
+  float h[7];
+  h[0] = 0.5f * (qR[0] - qL[0]) * irs;
+  h[1] = 0.5f * (qR[1] - qL[1]) * ivs;
+  h[2] = 0.5f * (qR[2] - qL[2]) * ivs;
+  h[3] = 0.5f * (qR[3] - qL[3]) * ivs;
+  h[4] = 0.5f * (qR[4] - qL[4]) * iPs;
+  h[5] = 0.5f * (qR[5] - qL[5]) * ibs;
+  h[6] = 0.5f * (qR[6] - qL[6]) * ibs;
+  float J = 0.f;
+#pragma unroll
+  for (int q = 0; q < 7; ++q)
+    J = fmaxf(J, fabsf(h[q]));
+  const float sJ = fmaxf(J, float(mlp::kJFloor));
+  const float isJ = __frcp_rn(sJ);
+#pragma unroll
+  for (int q = 0; q < 7; ++q)
+    f[7 + q] = h[q] * isJ;
+  f[14] = sJ * float(1.0 / mlp::kTauRef);
+  f[15] = 0.f;
+  const float rvs = rs * vs * sJ, pvs = Ps * vs * sJ, ps = Ps * sJ, bvs = bs * vs * sJ;
+  scale[0] = rvs;
+  scale[1] = pvs;
+  scale[2] = ps;
+  scale[3] = ps;
+  scale[4] = ps;
+  scale[5] = bvs;
+  scale[6] = bvs;
+  return J;
+}
+
+// Central flux (F(qL) + F(qR)) / 2 with 1 / (gamma - 1) given.
+__device__ __forceinline__ void
+central_flux_fast(const float * qL, const float * qR, float a, float igm1, float * Fc)
+{
+  float F[7] = { 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f };
+#pragma unroll
+  for (int side = 0; side < 2; ++side)
+  {
+    const float * q = side ? qR : qL;
+    const float   r = q[0], u = q[1], v = q[2], w = q[3], p = q[4], b = q[5], c = q[6];
+    const float   B2 = a * a + b * b + c * c;
+    const float   Pt = p + 0.5f * B2;
+    const float   E = p * igm1 + 0.5f * r * (u * u + v * v + w * w) + 0.5f * B2;
+    const float   vB = u * a + v * b + w * c;
+    F[0] += r * u;
+    F[1] += (E + Pt) * u - a * vB;
+    F[2] += r * u * u + Pt - a * a;
+    F[3] += r * u * v - a * b;
+    F[4] += r * u * w - a * c;
+    F[5] += b * u - a * v;
+    F[6] += c * u - a * w;
+  }
+#pragma unroll
+  for (int q = 0; q < 7; ++q)
+    Fc[q] = 0.5f * F[q];
+}
+
+// One face of the surrogate flux stage.  Returns true when the face must
+// be computed by HLLD (not smooth, at a floor, or a failed prediction).
+// Per-lane values kept in shared memory across the network evaluation
+// (the central flux and the output scales), which frees registers for the
+// tensor-core fragments.
+constexpr int kStash = 15; // Fc[7], scale[7], pad (odd stride)
+
+template <int DIM, int d>
+__device__ __forceinline__ bool
+flux_face_mlp(const Grid<float> & G, const Buffers<float> & B, const SurrogateDev & S, bool valid,
+              int64_t c, const uint32_t * sw, const float * sb, uint32_t * sx, float * so,
+              float * stash)
+{
+  float f[mlp::kIn];
+  bool  smooth = false;
+  const int lane = threadIdx.x & 31;
+  if (valid)
+  {
+    State<float> qL, qR;
+    face_states<float, DIM, d>(G, B, c, qL, qR);
+    float l7[7], r7[7], sc[7], Fc[7];
+    to_face7(qL, l7);
+    to_face7(qR, r7);
+    const float a = qL[IA];
+    const float J = encode_fast(l7, r7, a, f, sc);
+    // positivity: no reconstructed density or pressure at its floor
+    const float smallR = G.smallr, smallp = G.smallp;
+    smooth = J <= S.tau && l7[0] > smallR && r7[0] > smallR && l7[4] > smallp * l7[0] &&
+             r7[4] > smallp * r7[0];
+    central_flux_fast(l7, r7, a, __frcp_rn(G.gamma0 - 1.f), Fc);
+#pragma unroll
+    for (int q = 0; q < 7; ++q)
+    {
+      stash[lane * kStash + q] = Fc[q];
+      stash[lane * kStash + 7 + q] = sc[q];
+    }
+  }
+  if (!__any_sync(0xffffffffu, smooth))
+    return valid;
+  if (!smooth)
+  {
+#pragma unroll
+    for (int q = 0; q < mlp::kIn; ++q)
+      f[q] = 0.f;
+  }
+  float y[mlp::kOut];
+  mlp::warp_forward(sw, sb, sx, so, f, y);
+  if (!smooth)
+    return valid;
+  float Fc[7], sc[7];
+#pragma unroll
+  for (int q = 0; q < 7; ++q)
+  {
+    Fc[q] = stash[lane * kStash + q];
+    sc[q] = stash[lane * kStash + 7 + q];
+  }
+  bool ok = true;
+#pragma unroll
+  for (int q = 0; q < 7; ++q)
+    ok = ok && isfinite(y[q]) && fabsf(y[q]) <= mlp::kDissBound;
+  if (!ok)
+    return true;
+  State<float> fl;
+  fl[ID] = Fc[0] - sc[0] * y[0];
+  fl[IP] = Fc[1] - sc[1] * y[1];
+  fl[IU] = Fc[2] - sc[2] * y[2];
+  fl[IV] = Fc[3] - sc[3] * y[3];
+  fl[IW] = Fc[4] - sc[4] * y[4];
+  fl[IA] = 0.f;
+  fl[IB] = Fc[5] - sc[5] * y[5];
+  fl[IC] = Fc[6] - sc[6] * y[6];
+  store_face_flux<float, DIM, d>(G, B, c, fl);
+  return false;
+}
+
+// Face fluxes by the network; blockIdx.y = direction, grid-stride loop over
+// the faces so the weights are staged in shared memory once per block.
+// Faces the network does not answer are appended to S.list.
+template <int DIM>
+__global__ void __launch_bounds__(kMlpThreads, 4)
+k_flux_mlp(const Grid<float> G, Buffers<float> B, const SurrogateDev S)
+{
+  __shared__ __align__(16) uint32_t sw[mlp::kPackWords];
+  __shared__ float                  sb[mlp::kBiasFloats];
+  __shared__ uint32_t               sx[kMlpThreads / 32][mlp::kStageXWords];
+  __shared__ float                  so[kMlpThreads / 32][mlp::kStageOFloats];
+  __shared__ float                  stash[kMlpThreads / 32][32 * kStash];
+  for (int q = threadIdx.x; q < mlp::kPackWords; q += blockDim.x)
+    sw[q] = S.wpack[q];
+  for (int q = threadIdx.x; q < mlp::kBiasFloats; q += blockDim.x)
+    sb[q] = S.bias[q];
+  __syncthreads();
+  if (step_finished(B.st))
+    return;
+  const int     dir = blockIdx.y, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const Box &   bx = G.box[BOX_FACE];
+  const int64_t n = bx.count();
+  unsigned      used = 0, total = 0;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n;
+       base += (int64_t)gridDim.x * blockDim.x)
+  {
+    int           i = 0, j = 0, k = 0;
+    const int64_t idx = base + threadIdx.x;
+    const bool    valid = box_cell(bx, idx, i, j, k);
+    const int64_t c = valid ? cell_at(G, i, j, k) : 0;
+    bool          rest;
+    if (dir == 0)
+      rest = flux_face_mlp<DIM, 0>(G, B, S, valid, c, sw, sb, sx[warp], so[warp], stash[warp]);
+    else if (dir == 1)
+      rest = flux_face_mlp<DIM, 1>(G, B, S, valid, c, sw, sb, sx[warp], so[warp], stash[warp]);
+    else
+      rest = flux_face_mlp<DIM, DIM == 3 ? 2 : 1>(G, B, S, valid, c, sw, sb, sx[warp], so[warp],
+                                                  stash[warp]);
+    total += valid ? 1u : 0u;
+    used += (valid && !rest) ? 1u : 0u;
+    // warp-aggregated append of the faces left to HLLD
+    const unsigned m = __ballot_sync(0xffffffffu, rest);
+    if (m)
+    {
+      unsigned first = 0;
+      if (lane == __ffs(m) - 1)
+        first = atomicAdd(S.nlist, (unsigned)__popc(m));
+      first = __shfl_sync(0xffffffffu, first, __ffs(m) - 1);
+      if (rest)
+        S.list[first + __popc(m & ((1u << lane) - 1u))] = (uint32_t)(idx * DIM + dir);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+  {
+    used += __shfl_xor_sync(0xffffffffu, used, o);
+    total += __shfl_xor_sync(0xffffffffu, total, o);
+  }
+  if (lane == 0 && S.count)
+  {
+    atomicAdd(&S.count[0], (unsigned long long)used);
+    atomicAdd(&S.count[1], (unsigned long long)total);
+  }
+}
+
+// HLLD on the faces the network left (the list of k_flux_mlp).
+template <int DIM>
+__global__ void __launch_bounds__(128)
+k_flux_fallback(const Grid<float> G, Buffers<float> B, const uint32_t * __restrict__ list,
+                const unsigned * __restrict__ nlist)
+{
+  if (step_finished(B.st))
+    return;
+  const unsigned n = *nlist;
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+  {
+    const uint32_t e = list[q];
+    const int      dir = (int)(e % DIM);
+    int            i, j, k;
+    if (!box_cell(G.box[BOX_FACE], (int64_t)(e / DIM), i, j, k))
+      continue;
+    if (dir == 0)
+      flux_face<float, DIM, 0>(G, B, i, j, k);
+    else if (dir == 1)
+      flux_face<float, DIM, 1>(G, B, i, j, k);
+    else if constexpr (DIM == 3)
+      flux_face<float, DIM, 2>(G, B, i, j, k);
+  }
+}
+
+} // namespace MHD_VARIANT_TAG
+} // namespace mhd

@@ -16,7 +16,18 @@ SolverMHDMusclGPU<dim>::SolverMHDMusclGPU(HydroParams & p, ConfigMap & cfg)
   const std::string mode = cfg.getString("gb300", "fp_mode", "fast");
   mhd_params        mp = p.to_mhd_params(cfg, precision, mode == "exact" ? MHD_FP_EXACT : MHD_FP_FAST);
   int               rc = mhd_create(&mp, &ctx);
-  if (rc == MHD_OK)
+  // restart from a checkpoint (SolverMHDMuscl<dim>::init_restart,
+  // SolverMHDMuscl.h:613-643; keys of SolverBase.cpp:130-132)
+  const bool restart = cfg.getInteger("run", "restart_enabled", 0) != 0;
+  if (rc == MHD_OK && restart)
+  {
+    const std::string file = cfg.getString("run", "restart_filename", "");
+    const bool        reset = cfg.getBool("run", "restart_reset_totaltime", false);
+    rc = mhd_checkpoint_load(ctx, file.c_str(), reset ? 1 : 0, &m_times_saved);
+    if (rc == MHD_OK)
+      std::cout << "### This is a restarted run ! ###\n";
+  }
+  else if (rc == MHD_OK)
     rc = mhd_init_problem(ctx); // init + boundaries + U2 = U + primitives + dt
   if (rc != MHD_OK)
   {
@@ -130,6 +141,17 @@ SolverMHDMusclGPU<dim>::save_solution_impl()
   std::vector<double> U;
   if (copy_state(U))
     save_VTK(U.data(), params, configMap, m_variables_names, m_times_saved, dim);
+  // restartable checkpoint beside each output ([gb300] checkpoint = true)
+  if (configMap.getBool("gb300", "checkpoint", false))
+  {
+    char num[16];
+    std::snprintf(num, sizeof num, "%07d", m_times_saved);
+    const std::string file = configMap.getString("output", "outputDir", "./") + "/" +
+                             configMap.getString("output", "outputPrefix", "output") + "_" + num +
+                             ".ckpt";
+    if (mhd_checkpoint_save(ctx, file.c_str(), m_times_saved) != MHD_OK)
+      std::cerr << "checkpoint: " << mhd_last_error(ctx) << "\n";
+  }
   timers[TIMER_IO]->stop();
 }
 

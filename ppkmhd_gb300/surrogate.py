@@ -1,0 +1,274 @@
+"""The HLLD flux surrogate from Python.
+
+``FluxMLP`` wraps the ``mhd_mlp_*`` entry points (the network lives on the
+GPU; training uses the library's own forward/backward kernels).
+``harvest_training_set`` runs the FP32 solver on the training workloads and
+collects face records; ``train`` is the recipe that produced the committed
+weights ``ppkmhd_gb300/data/flux_mlp.npz``:
+
+    python -m ppkmhd_gb300.surrogate train --out ppkmhd_gb300/data/flux_mlp.npz
+
+Record layout (MHD_SAMPLE_FLOATS = 24 floats): qL[7], qR[7] (rho, vn, vt1,
+vt2, p, Bt1, Bt2, face-normal frame), a (normal B), J (sensor), D[7] (FP64
+central flux minus FP64 HLLD flux), gamma0.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import time
+
+import numpy as np
+
+from . import (MHD_FP32, MHD_MLP_CHECK, MHD_MLP_PARAMS, MHD_MLP_TRAIN, MHD_OK, MHD_SAMPLE_FLOATS,
+               MHDError, MHDSolver, lib, params_from_ini)
+from . import workloads
+
+DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
+DEFAULT_WEIGHTS = os.path.join(DATA, "flux_mlp.npz")
+GAMMA = workloads.f32("1.6666666666666667")
+REC_J = 15
+
+
+class FluxMLP:
+    """A 15-64-64-7 GELU network on the GPU (``mhd_mlp``)."""
+
+    def __init__(self, seed: int = 0, gamma0: float = GAMMA):
+        self.h = ctypes.c_void_p()
+        rc = lib().mhd_mlp_create(int(seed), float(gamma0), ctypes.byref(self.h))
+        if rc != MHD_OK:
+            msg = lib().mhd_mlp_last_error(self.h).decode() if self.h else "mhd_mlp_create failed"
+            raise MHDError(rc, msg)
+        self.gamma0 = gamma0
+
+    def _check(self, rc):
+        if rc != MHD_OK:
+            raise MHDError(rc, lib().mhd_mlp_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            lib().mhd_mlp_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def params(self) -> np.ndarray:
+        p = np.empty(MHD_MLP_PARAMS, dtype=np.float32)
+        self._check(lib().mhd_mlp_get_params(self.h, p.ctypes.data, MHD_MLP_PARAMS))
+        return p
+
+    @params.setter
+    def params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.shape == (MHD_MLP_PARAMS,)
+        self._check(lib().mhd_mlp_set_params(self.h, p.ctypes.data, MHD_MLP_PARAMS))
+
+    @classmethod
+    def load(cls, path: str = DEFAULT_WEIGHTS) -> "FluxMLP":
+        z = np.load(path)
+        m = cls(0, float(z["gamma0"]))
+        m.params = z["params"]
+        return m
+
+    def save(self, path: str, **meta):
+        os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+        np.savez(path, params=self.params, gamma0=np.float64(self.gamma0),
+                 meta=np.array(json.dumps(meta)))
+
+    def encode(self, records: np.ndarray):
+        rec = np.ascontiguousarray(records, dtype=np.float32)
+        n = rec.shape[0]
+        f = np.empty((n, 16), dtype=np.float32)
+        t = np.empty((n, 8), dtype=np.float32)
+        self._check(lib().mhd_mlp_encode(self.h, rec.ctypes.data, n, f.ctypes.data, t.ctypes.data))
+        return f, t
+
+    def gradient(self, features, targets, mode: int = MHD_MLP_CHECK):
+        f = np.ascontiguousarray(features, dtype=np.float32)
+        t = np.ascontiguousarray(targets, dtype=np.float32)
+        g = np.empty(MHD_MLP_PARAMS, dtype=np.float32)
+        loss = ctypes.c_double()
+        self._check(lib().mhd_mlp_gradient(self.h, f.ctypes.data, t.ctypes.data, f.shape[0],
+                                           int(mode), g.ctypes.data, ctypes.byref(loss)))
+        return g, loss.value
+
+    def train(self, records, epochs: int = 10, batch: int = 16384, lr: float = 2e-3,
+              seed: int = 1, weight_power: float = 0.0) -> np.ndarray:
+        rec = np.ascontiguousarray(records, dtype=np.float32)
+        hist = np.zeros(epochs, dtype=np.float32)
+        self._check(lib().mhd_mlp_train(self.h, rec.ctypes.data, rec.shape[0], int(epochs),
+                                        int(batch), float(lr), float(weight_power), int(seed),
+                                        hist.ctypes.data))
+        return hist
+
+    def forward(self, features) -> np.ndarray:
+        f = np.ascontiguousarray(features, dtype=np.float32)
+        out = np.empty((f.shape[0], 8), dtype=np.float32)
+        self._check(lib().mhd_mlp_forward(self.h, f.ctypes.data, f.shape[0], out.ctypes.data))
+        return out
+
+
+def smooth(records: np.ndarray, tau: float = 0.1) -> np.ndarray:
+    """Records whose sensor value J is at most tau and whose values are finite."""
+    ok = np.isfinite(records).all(axis=1) & (records[:, REC_J] <= tau)
+    return records[ok]
+
+
+def _solver(ini: str, U: np.ndarray | None = None) -> MHDSolver:
+    s = MHDSolver(params_from_ini(ini))
+    if U is None:
+        s.init_problem()
+    else:
+        s.set_state(U.astype(np.float32))
+    return s
+
+
+def _collect(s: MHDSolver, steps: int, every: int, stride: int, out: list):
+    done = 0
+    while done <= steps:
+        out.append(smooth(s.harvest(stride)))
+        if done == steps:
+            break
+        s.run(every)
+        done += every
+
+
+def harvest_training_set(scale: float = 1.0, seed: int = 5) -> np.ndarray:
+    """Face records from FP32 runs: 2D Orszag-Tang 256^2, four ensemble-style
+    2D problems, the 3D Orszag-Tang state with a 5 % velocity perturbation
+    (64^3) and the turbulence state (64^3, another seed than the deployed
+    one).  `scale` multiplies the number of harvests."""
+    g = "1.6666666666666667"
+    out: list = []
+    reps = max(1, int(round(6 * scale)))
+    # 2D Orszag-Tang
+    s = _solver(workloads.ot_ini(2, 256, gamma0=g, precision=32))
+    _collect(s, steps=60 * reps, every=60, stride=2, out=out)
+    s.close()
+    # ensemble-style problems
+    rng = np.random.default_rng(seed)
+    for q in range(4):
+        spec = dict(n=int(rng.integers(96, 256)), b0_scale=float(rng.uniform(0.5, 1.5)),
+                    seed=int(rng.integers(1, 2 ** 31 - 1)))
+        n = spec["n"]
+        _, U = workloads.ensemble_problem(spec)
+        s = _solver(workloads.ot_ini(2, n, gamma0=g, precision=32), U)
+        _collect(s, steps=50 * reps, every=50, stride=2, out=out)
+        s.close()
+    # 3D Orszag-Tang, perturbed
+    ini3 = workloads.ot_ini(3, 64, gamma0=g, precision=32)
+    s = MHDSolver(params_from_ini(ini3))
+    s.init_problem()
+    U = workloads.perturbed_ot_3d(s.get_state().astype(np.float64), seed=seed, amp=0.05,
+                                  gamma0=GAMMA)
+    s.set_state(U.astype(np.float32))
+    _collect(s, steps=30 * reps, every=30, stride=2, out=out)
+    s.close()
+    # turbulence
+    U = workloads.turbulence_3d(64, seed=seed + 100)
+    s = _solver(workloads.ot_ini(3, 64, gamma0=g, precision=32), U)
+    _collect(s, steps=30 * reps, every=30, stride=2, out=out)
+    s.close()
+    return np.concatenate(out, axis=0)
+
+
+def evaluate(m: FluxMLP, records: np.ndarray) -> dict:
+    """Errors of the deployed (tensor-core) forward on held-out records:
+    relative L1 of the dissipation D and of the full flux against HLLD."""
+    f, t = m.encode(records)
+    y = m.forward(f)[:, :7].astype(np.float64)
+    t = t[:, :7].astype(np.float64)
+    # physical units: D = scale * target; scale from the oracle-free formula
+    ql = records[:, 0:7].astype(np.float64)
+    qr = records[:, 7:14].astype(np.float64)
+    a = records[:, 14].astype(np.float64)
+    rs = 0.5 * (ql[:, 0] + qr[:, 0])
+    b2l = a ** 2 + ql[:, 5] ** 2 + ql[:, 6] ** 2
+    b2r = a ** 2 + qr[:, 5] ** 2 + qr[:, 6] ** 2
+    Ps = 0.5 * (ql[:, 4] + qr[:, 4]) + 0.25 * (b2l + b2r)
+    vs = np.sqrt(Ps / rs)
+    bs = np.sqrt(Ps)
+    sJ = np.maximum(records[:, REC_J].astype(np.float64), 1e-4)
+    sc = np.stack([rs * vs, Ps * vs, Ps, Ps, Ps, bs * vs, bs * vs], axis=1) * sJ[:, None]
+    D = records[:, 16:23].astype(np.float64)
+    Dp = sc * y
+    g0 = records[:, 23].astype(np.float64)
+
+    def flux(q):
+        r, u, v, w, p, b, c = (q[:, i] for i in range(7))
+        B2 = a ** 2 + b ** 2 + c ** 2
+        Pt = p + 0.5 * B2
+        E = p / (g0 - 1) + 0.5 * r * (u * u + v * v + w * w) + 0.5 * B2
+        vB = u * a + v * b + w * c
+        return np.stack([r * u, (E + Pt) * u - a * vB, r * u * u + Pt - a * a, r * u * v - a * b,
+                         r * u * w - a * c, b * u - a * v, c * u - a * w], axis=1)
+
+    Fc = 0.5 * (flux(ql) + flux(qr))
+    Fh = Fc - D
+    Fp = Fc - Dp
+    out = {
+        "samples": int(records.shape[0]),
+        "rms_error_normalised": float(np.sqrt(np.mean((y - t) ** 2))),
+        "rel_l1_dissipation": (np.abs(Dp - D).sum(0) / np.maximum(np.abs(D).sum(0), 1e-300)).tolist(),
+        "rel_l1_flux": (np.abs(Fp - Fh).sum(0) / np.maximum(np.abs(Fh).sum(0), 1e-300)).tolist(),
+    }
+    J = records[:, REC_J]
+    for tau in (0.01, 0.02, 0.05):
+        sel = J <= tau
+        if sel.sum() > 100:
+            out[f"rel_l1_flux_J<={tau}"] = (np.abs(Fp[sel] - Fh[sel]).sum(0)
+                                            / np.maximum(np.abs(Fh[sel]).sum(0), 1e-300)).tolist()
+            out[f"fraction_J<={tau}"] = float(sel.mean())
+    return out
+
+
+def train(out: str = DEFAULT_WEIGHTS, scale: float = 2.0, epochs: int = 250, batch: int = 16384,
+          lr: float = 3e-3, seed: int = 1, weight_power: float = 1.0, log=print) -> dict:
+    t0 = time.time()
+    rec = harvest_training_set(scale)
+    rng = np.random.default_rng(seed)
+    rng.shuffle(rec)
+    nval = min(200000, rec.shape[0] // 10)
+    val, trn = rec[:nval], rec[nval:]
+    log(f"harvested {rec.shape[0]} smooth face records in {time.time() - t0:.1f} s")
+    m = FluxMLP(seed=seed, gamma0=GAMMA)
+    t1 = time.time()
+    hist = m.train(trn, epochs=epochs, batch=batch, lr=lr, seed=seed, weight_power=weight_power)
+    t_train = time.time() - t1
+    log(f"trained {epochs} epochs in {t_train:.1f} s; loss {hist[0]:.3e} -> {hist[-1]:.3e}")
+    ev = evaluate(m, val)
+    log(json.dumps(ev))
+    meta = {"samples_train": int(trn.shape[0]), "samples_val": int(nval), "epochs": epochs,
+            "batch": batch, "lr": lr, "seed": seed, "weight_power": weight_power,
+            "scale": scale, "train_seconds": t_train,
+            "loss_history": [float(x) for x in hist], "validation": ev}
+    m.save(out, **meta)
+    return meta
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    t = sub.add_parser("train")
+    t.add_argument("--out", default=DEFAULT_WEIGHTS)
+    t.add_argument("--scale", type=float, default=2.0)
+    t.add_argument("--epochs", type=int, default=250)
+    t.add_argument("--batch", type=int, default=16384)
+    t.add_argument("--lr", type=float, default=3e-3)
+    t.add_argument("--seed", type=int, default=1)
+    t.add_argument("--weight-power", type=float, default=1.0)
+    a = ap.parse_args()
+    if a.cmd == "train":
+        meta = train(a.out, a.scale, a.epochs, a.batch, a.lr, a.seed, a.weight_power)
+        print(json.dumps({k: v for k, v in meta.items() if k != "loss_history"}))
+
+
+if __name__ == "__main__":
+    main()

@@ -18,6 +18,9 @@ LayoutLeft ``[var][k][j][i]`` with ghost cells).
   reference's own Kelvin-Helmholtz functor (MHDInitFunctors2D.h:420-560) fixes
   Bx = 0.5 and uses its own perturbation; this variant is injected through
   the state interface.
+* ``turbulence_3d``: random-phase solenoidal velocity and field on the
+  periodic cube (E(k) ~ k^-2 on 1 <= |k| <= 8, rms v = 1, rms B = 0.5,
+  rho = p = 1), B the discrete curl of an edge vector potential.
 
 All states include ghost cells; set_state refills them from the interior
 with the boundary conditions, so their content does not matter.
@@ -198,4 +201,77 @@ def kelvin_helmholtz(n: int, seed: int = 7, gamma0: float = f32("1.4")) -> np.nd
     U[IV] = rho * vy
     U[IA] = 0.1
     _energy_2d(U, 2.5 / (gamma0 - 1.0))
+    return U
+
+
+def turbulence_3d(n: int, seed: int = 11, kmin: float = 1.0, kmax: float = 8.0,
+                  vrms: float = 1.0, brms: float = 0.5, rho: float = 1.0, p: float = 1.0,
+                  gamma0: float = f32("1.6666666666666667"), dtype=np.float64) -> np.ndarray:
+    """Random-phase solenoidal velocity and field on the periodic unit cube,
+    spectrum E(k) ~ k^-2 on kmin <= |k| <= kmax (mode amplitudes ~ |k|^-2),
+    rms |v| = vrms and rms |B| (face values) = brms, uniform rho and p.
+
+    The velocity is projected onto divergence-free modes.  The face-centred
+    field is the discrete curl of an edge-centred vector potential, so its
+    discrete divergence vanishes to round-off."""
+    from numpy.fft import fftfreq, irfftn, rfftfreq
+
+    rng = np.random.default_rng(seed)
+    k1 = fftfreq(n) * n
+    kz = k1[:, None, None]
+    ky = k1[None, :, None]
+    kx = (rfftfreq(n) * n)[None, None, :]
+    kk = np.sqrt(kx ** 2 + ky ** 2 + kz ** 2)
+    band = (kk >= kmin) & (kk <= kmax)
+    kk_safe = np.where(kk > 0, kk, 1.0)
+    shape = kk.shape
+
+    def random_vector(power):
+        comps = [band * kk_safe ** power * np.exp(2j * np.pi * rng.random(shape))
+                 * rng.standard_normal(shape) for _ in range(3)]
+        return comps
+
+    # velocity (cell values), solenoidal projection
+    vx, vy, vz = random_vector(-2.0)
+    kdotv = (kx * vx + ky * vy + kz * vz) / kk_safe ** 2
+    vhat = [vx - kx * kdotv, vy - ky * kdotv, vz - kz * kdotv]
+    v = [irfftn(c, s=(n, n, n)) for c in vhat]
+    del vx, vy, vz, kdotv, vhat
+    norm = vrms / np.sqrt(np.mean(v[0] ** 2 + v[1] ** 2 + v[2] ** 2))
+    v = [c * norm for c in v]
+
+    # vector potential on edges (|A| ~ |k|^-3): Ax at (x+h/2, y, z), Ay at
+    # (x, y+h/2, z), Az at (x, y, z+h/2), grid points x = i / n
+    ax, ay, az = random_vector(-3.0)
+    half = np.pi / n  # 2 pi k * (h/2) with h = 1/n
+    A = [irfftn(ax * np.exp(1j * half * kx), s=(n, n, n)),
+         irfftn(ay * np.exp(1j * half * ky), s=(n, n, n)),
+         irfftn(az * np.exp(1j * half * kz), s=(n, n, n))]
+    del ax, ay, az
+    h = 1.0 / n
+
+    def d(f, axis):  # forward difference along axis (0 = z, 1 = y, 2 = x), periodic
+        return (np.roll(f, -1, axis=axis) - f) / h
+
+    Ax, Ay, Az = A
+    Bx = d(Az, 1) - d(Ay, 0)   # at (x_i, y_{j+1/2}, z_{k+1/2})
+    By = d(Ax, 0) - d(Az, 2)   # at (x_{i+1/2}, y_j, z_{k+1/2})
+    Bz = d(Ay, 2) - d(Ax, 1)   # at (x_{i+1/2}, y_{j+1/2}, z_k)
+    del A, Ax, Ay, Az
+    bnorm = brms / np.sqrt(np.mean(Bx ** 2 + By ** 2 + Bz ** 2))
+    Bx, By, Bz = Bx * bnorm, By * bnorm, Bz * bnorm
+
+    g = GHOST
+    U = np.zeros((8, n + 2 * g, n + 2 * g, n + 2 * g), dtype=dtype)
+    sl = (slice(g, -g),) * 3
+    U[(ID,) + sl] = rho
+    for comp, var in zip(v, (IU, IV, IW)):
+        U[(var,) + sl] = rho * comp
+    for comp, var in zip((Bx, By, Bz), (IA, IB, IC)):
+        U[(var,) + sl] = comp
+    bcx = 0.5 * (Bx + np.roll(Bx, -1, axis=2))
+    bcy = 0.5 * (By + np.roll(By, -1, axis=1))
+    bcz = 0.5 * (Bz + np.roll(Bz, -1, axis=0))
+    U[(IP,) + sl] = (p / (gamma0 - 1.0) + 0.5 * rho * (v[0] ** 2 + v[1] ** 2 + v[2] ** 2)
+                     + 0.5 * (bcx ** 2 + bcy ** 2 + bcz ** 2))
     return U

@@ -1,0 +1,66 @@
+"""Checkpoint / restart (mhd_checkpoint_save / mhd_checkpoint_load): a run
+continued from a checkpoint is bitwise the uninterrupted run; the header
+carries the grid, precision and time; mismatched or damaged files are
+rejected with MHD_ERR_INVALID_ARG."""
+import struct
+
+import numpy as np
+import pytest
+
+from mhd_cases import ot_ini
+
+
+HEADER = struct.Struct("<8s8I2dq2i7d")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim,precision", [(2, 64), (3, 32)])
+def test_restart_continues_bitwise(mhdlib, tmp_path, dim, precision):
+    ini = ot_ini(dim=dim, nx=32, ny=24, nz=16, precision=precision)
+    a = mhdlib.MHDSolver.from_ini(ini)
+    a.init_problem()
+    a.run(7)
+    path = str(tmp_path / "state.ckpt")
+    a.checkpoint_save(path, times_saved=3)
+    t7, dt7, _ = a.time()
+    a.run(9)
+    ref = a.get_state()
+    with open(path, "rb") as f:
+        h = HEADER.unpack(f.read(HEADER.size))
+    assert h[0] == b"PPKMHDCK" and h[1] == 1 and h[2] == dim
+    assert h[3:6] == (32, 24, 16 if dim == 3 else 1)
+    assert h[8] == precision // 8 and h[9] == t7 and h[11] == 7 and h[12] == 3
+    b = mhdlib.MHDSolver.from_ini(ini)
+    assert b.checkpoint_load(path) == 3
+    t, _, it = b.time()
+    assert t == t7 and it == 0   # iteration count restarts, as in the reference
+    b.run(9)
+    assert np.array_equal(b.get_state(), ref)
+    assert b.time()[0] == a.time()[0]
+    # restart_reset_totaltime
+    c = mhdlib.MHDSolver.from_ini(ini)
+    c.checkpoint_load(path, reset_time=True)
+    assert c.time()[0] == 0.0
+
+
+@pytest.mark.gpu
+def test_checkpoint_rejects_mismatch(mhdlib, tmp_path):
+    a = mhdlib.MHDSolver.from_ini(ot_ini(dim=2, nx=32))
+    a.init_problem()
+    path = str(tmp_path / "a.ckpt")
+    a.checkpoint_save(path)
+    other = mhdlib.MHDSolver.from_ini(ot_ini(dim=2, nx=40))
+    with pytest.raises(mhdlib.MHDError) as e:
+        other.checkpoint_load(path)
+    assert e.value.code == mhdlib.MHD_ERR_INVALID_ARG and "grid" in str(e.value)
+    f32 = mhdlib.MHDSolver.from_ini(ot_ini(dim=2, nx=32, precision=32))
+    with pytest.raises(mhdlib.MHDError) as e:
+        f32.checkpoint_load(path)
+    assert "precision" in str(e.value)
+    data = open(path, "rb").read()
+    open(path, "wb").write(data[: len(data) // 2])
+    with pytest.raises(mhdlib.MHDError) as e:
+        a.checkpoint_load(path)
+    assert "truncated" in str(e.value)
+    with pytest.raises(mhdlib.MHDError):
+        a.checkpoint_load(str(tmp_path / "missing.ckpt"))
