@@ -48,6 +48,9 @@ WORKLOADS = {
     "kh2d_4096_fp32": (2, 4096, 32, "2D magnetised Kelvin-Helmholtz 4096^2 (periodic x, "
                                     "reflecting y, gamma 1.4, Bx 0.1), FP32 plain "
                                     "MUSCL-Hancock+HLLD+CT"),
+    "turb3d_512_fp32_mlp": (3, 512, 32, "3D MHD turbulence 512^3 (random-phase solenoidal v and B, "
+                                        "E(k)~k^-2 on 1<=|k|<=8, rms v 1, rms B 0.5), FP32 with "
+                                        "the HLLD flux surrogate (tau 0.01)"),
     # reduced size for ncu captures (a few GB on the device, inputs still > L2)
     "ot3d_128_fp64": (3, 128, 64, "3D Orszag-Tang 128^3, FP64 plain MUSCL-Hancock+HLLD+CT"),
     "ot3d_128_fp32": (3, 128, 32, "3D Orszag-Tang 128^3, FP32 plain MUSCL-Hancock+HLLD+CT"),
@@ -86,6 +89,12 @@ def workload_setup(name: str, precision: int):
     single-problem workload; the transform maps the Orszag-Tang initial state
     to the workload's (FP64, LayoutLeft)."""
     dim, n, _, _ = WORKLOADS[name]
+    if name.startswith("turb"):
+        from ppkmhd_gb300 import workloads
+
+        return (workloads.ot_ini(3, n, gamma0="1.6666666666666667", precision=precision),
+                lambda U: workloads.turbulence_3d(n, seed=11),
+                "synthetic: seeded random-phase solenoidal MHD turbulence")
     if name.startswith("kh2d"):
         from ppkmhd_gb300 import workloads
 
@@ -503,6 +512,131 @@ def run_ensemble(args):
         torch.distributed.destroy_process_group()
 
 
+def run_turbulence(args):
+    """FP32 turbulence with the flux surrogate: throughput of the surrogate
+    run and of plain FP32, accuracy of both against the FP64 solution of the
+    same steps (GPU FP64 path, equal to the oracle within 1e-12)."""
+    world, rank, local = dist_setup()
+    import torch
+
+    torch.cuda.set_device(local)
+    import ppkmhd_gb300 as m
+    from ppkmhd_gb300 import surrogate, workloads
+
+    dim, n, precision, label = WORKLOADS[args.workload]
+    g = "1.6666666666666667"
+    ini32 = workloads.ot_ini(3, n, gamma0=g, precision=32)
+    ini64 = workloads.ot_ini(3, n, gamma0=g, precision=64)
+    U = workloads.turbulence_3d(n, seed=11)
+    mlp = surrogate.FluxMLP.load()
+    tau = 0.01
+
+    def ctx(ini, with_mlp):
+        p = m.params_from_ini(ini)
+        p.device = local
+        s = m.MHDSolver(p)
+        s.set_state(U.astype(s.real))
+        if with_mlp:
+            s.set_surrogate(mlp, tau=tau)
+        return s
+
+    # throughput (device-resident, graph replay)
+    s = ctx(ini32, True)
+    cells, _ = s.cell_counts()
+    s.run_timed(max(args.warmup, 3))
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms = s.run_timed(args.steps)
+    torch.cuda.synchronize()
+    value = cells * args.steps / (ms / 1e3)
+    prof = {}
+    for _ in range(3):
+        for name, kms in s.profile_step():
+            prof.setdefault(name, []).append(kms)
+    prof = {k: float(np.median(v)) for k, v in prof.items()}
+    dom = max(prof, key=prof.get)
+    used, total = s.surrogate_stats()
+    # e2e through the host-buffer call
+    U0 = s.get_state()
+    h_in = torch.empty(U0.size, dtype=torch.float32, pin_memory=True)
+    h_out = torch.empty_like(h_in, pin_memory=True)
+    h_in.numpy()[:] = U0.reshape(-1)
+    s.step_host_ptr(h_in.data_ptr(), h_out.data_ptr())
+    e2e_steps = 3
+    t0 = time.perf_counter()
+    for q in range(e2e_steps):
+        a, b = (h_in, h_out) if q % 2 == 0 else (h_out, h_in)
+        s.step_host_ptr(a.data_ptr(), b.data_ptr())
+    e2e_value = cells * e2e_steps / (time.perf_counter() - t0)
+    s.close()
+    p32 = ctx(ini32, False)
+    p32.run_timed(3)
+    ms_plain = p32.run_timed(args.steps)
+    p32.close()
+
+    # accuracy against FP64 after the same number of steps from the same state
+    acc_steps = args.acc_steps
+    out = {}
+    for tag, ini, with_mlp in (("fp64", ini64, False), ("fp32", ini32, False),
+                               ("fp32_mlp", ini32, True)):
+        c = ctx(ini, with_mlp)
+        c.run(acc_steps)
+        out[tag] = m.interior(c.get_state()).astype(np.float64)
+        c.close()
+    ref = out.pop("fp64")
+
+    def rel_l1(a):
+        ax = (1, 2, 3)
+        return float((np.abs(a - ref).sum(axis=ax) / np.abs(ref).sum(axis=ax)).max())
+
+    hbm_peak, peak_kind = load_peaks()
+    alg = 64
+    achieved = alg * cells / (prof[dom] / 1e3) / 1e9
+    step_ms = sum(prof.values())
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle_py
+
+        oracle_py.build_oracle()
+        nthreads = os.cpu_count() or 1
+        o = oracle_py.OracleSolver(ini64, nthreads=nthreads)
+        o.set_state(U)
+        t0 = time.perf_counter()
+        o.run(1)
+        el = time.perf_counter() - t0
+        o.close()
+        cpu = {"value": cells / el, "unit": "cell-updates/s", "cores": nthreads, "kind": "port",
+               "sample": f"1 step of the full {n}^3 grid, FP64, oracle/mhd_oracle.c with "
+                         f"{nthreads} OpenMP threads ({el:.1f} s)"}
+    if rank == 0:
+        emit({
+            "metric": "MHD cell-updates/s (interior cells), FP32 + HLLD flux surrogate",
+            "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16",
+            "data": "synthetic: seeded random-phase solenoidal MHD turbulence",
+            "config": {"workload": label, "grid": [n] * 3, "cells": cells, "tau": tau,
+                       "faces_by_network": used / max(total, 1),
+                       "l2": "inputs larger than L2", "per_kernel_ms": prof,
+                       "kernels_per_step": len(prof)},
+            "accuracy": {"steps": acc_steps, "rel_l1_vs_fp64_fp32_mlp": rel_l1(out["fp32_mlp"]),
+                         "rel_l1_vs_fp64_fp32_hlld": rel_l1(out["fp32"])},
+            "variants": {"fp32_hlld": {"value": cells * args.steps / (ms_plain / 1e3),
+                                       "ms_per_step": ms_plain / args.steps}},
+            "e2e": {"value": e2e_value, "unit": "cell-updates/s",
+                    "h2d_bytes_per_step": U0.nbytes, "d2h_bytes_per_step": U0.nbytes,
+                    "steps": e2e_steps, "call": "mhd_step_host (pinned host buffers)"},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                         "peak_source": f"hbm_gbs of {peak_kind}", "algorithmic_bytes_per_cell": alg,
+                         "step_achieved": alg * cells / (step_ms / 1e3) / 1e9},
+            "clocks": clk.summary(),
+            "gpu_launches": len(prof) * args.steps,
+            "cpu_baseline": cpu,
+        })
+
+
 def load_profile_traffic(workload: str, kernel: str):
     """DRAM bytes per launch of the dominant kernel from the committed ncu
     summary (profiles/*.json), or None."""
@@ -581,6 +715,8 @@ def main():
                     help="reference-arm iterations (default: --steps, at most 20 full-grid "
                          "iterations; 150 for the ensemble sample)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--acc-steps", type=int, default=40,
+                    help="steps of the accuracy comparison of the turbulence workload")
     ap.add_argument("--no-variants", action="store_true")
     args = ap.parse_args()
     if args.cpu_steps is None:
@@ -591,6 +727,8 @@ def main():
         run_reference(args)
     elif args.workload.startswith("ensemble"):
         run_ensemble(args)
+    elif args.workload.startswith("turb"):
+        run_turbulence(args)
     else:
         run_gb300(args)
 

@@ -62,8 +62,23 @@ extern "C" {
 #define MHD_LAYOUT_LEFT 0  /* [var][k][j][i], i fastest (Kokkos LayoutLeft, the CUDA build) */
 #define MHD_LAYOUT_RIGHT 1 /* [i][j][k][var], var fastest (Kokkos LayoutRight, the OpenMP build) */
 
-/* initial conditions */
-#define MHD_PROBLEM_ORSZAG_TANG 0
+/* initial conditions: [hydro] problem (SolverMHDMuscl.h:649-710) and the
+ * layout of mhd_params::problem_real / problem_int for each
+ * (src/shared/problems/*Params.h, values float-rounded as ConfigMap reads
+ * them) */
+#define MHD_PROBLEM_ORSZAG_TANG 0      /* ot_kt */
+#define MHD_PROBLEM_BLAST 1            /* real: radius, center_x, _y, _z, density_in, density_out,
+                                          pressure_in, pressure_out */
+#define MHD_PROBLEM_IMPLODE 2          /* real: outer rho, p, vx, vy, vz, Bx, By, Bz, then inner;
+                                          int: shape_region */
+#define MHD_PROBLEM_KELVIN_HELMHOLTZ 3 /* real: d_in, d_out, pressure, vflow_in, vflow_out,
+                                          amplitude, w0, delta; int: perturbation_sine,
+                                          perturbation_sine_robertson, mode */
+#define MHD_PROBLEM_ROTOR 4            /* real: r0, r1, u0, p0, b0 */
+#define MHD_PROBLEM_FIELD_LOOP 5       /* real: radius, density_in, amplitude, vflow */
+#define MHD_PROBLEM_WAVE 6             /* real: amplitude, V0, rev[7], d0, p0, sin_a2, cos_a2,
+                                          sin_a3, cos_a3, dby, dbz, bx0, by0, bz0, k_par
+                                          (WaveParams.h); int: type */
 
 /*
  * Run/mesh/scheme parameters.  Mirrors the fields of HydroParams /
@@ -89,6 +104,8 @@ typedef struct mhd_params
   int    precision;  /* MHD_FP64 or MHD_FP32 */
   int    fp_mode;    /* MHD_FP_FAST or MHD_FP_EXACT */
   int    device;     /* CUDA device ordinal the context binds (default 0) */
+  double problem_real[24]; /* per-problem parameters, see MHD_PROBLEM_* */
+  int    problem_int[4];
 } mhd_params;
 
 typedef struct mhd_ctx mhd_ctx;
@@ -114,6 +131,11 @@ int mhd_destroy(mhd_ctx *ctx);
 /* Initial condition + boundaries + U2 = U + primitives + dt, i.e. the tail of
  * the solver constructor (SolverMHDMuscl.h:390-402). */
 int mhd_init_problem(mhd_ctx *ctx);
+
+/* The initial condition of p->problem alone, computed on the host in FP64
+ * (no device needed): U receives the ghost-inclusive LayoutLeft state that
+ * the reference's init functor writes, before any boundary fill. */
+int mhd_initial_state(const mhd_params *p, double *U);
 
 /* Inject a full ghost-inclusive state (real_bytes 8 or 4, matching the
  * context precision) and redo boundaries, primitives and dt; resets the

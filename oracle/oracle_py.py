@@ -268,6 +268,21 @@ class RefSolver:
         return t.value, dt.value, it.value
 
 
+def ref_initial_state(ini_text: str, bits: int = 64) -> np.ndarray:
+    """The reference init functor's output for the .ini (no boundary fill),
+    LayoutLeft float64."""
+    r = RefSolver(ini_text, bits)
+    shape = r._right_shape()
+    r.close()
+    L = ctypes.CDLL(REF_SO[bits])
+    L.ref_initial_state.argtypes = [ctypes.c_char_p, ctypes.c_void_p]
+    L.ref_initial_state.restype = ctypes.c_long
+    U = np.empty(shape, dtype=np.float64 if bits == 64 else np.float32)
+    n = L.ref_initial_state(ini_text.encode(), U.ctypes.data_as(ctypes.c_void_p))
+    assert n == U.size
+    return np.ascontiguousarray(U.T, dtype=np.float64)
+
+
 def ref_probe_lib(bits: int = 64):
     L = ctypes.CDLL(REF_SO[bits])
     real = ctypes.c_double if bits == 64 else ctypes.c_float

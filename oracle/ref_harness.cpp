@@ -39,6 +39,50 @@ using namespace ppkMHD::muscl;
 namespace
 {
 
+// SolverMHDMuscl<dim>::init (SolverMHDMuscl.h:649-710): the reference's init
+// functor for [hydro] problem, Orszag-Tang for unknown names.
+template <class DA>
+void
+init_problem_2d(ConfigMap & cfg, HydroParams & params, DA U)
+{
+  const std::string problem = cfg.getString("hydro", "problem", "unknown");
+  if (problem == "blast")
+    InitBlastFunctor2D_MHD::apply(params, BlastParams(cfg), U);
+  else if (problem == "implode")
+    InitImplodeFunctor2D_MHD::apply(params, ImplodeParams(cfg), U);
+  else if (problem == "kelvin_helmholtz")
+    InitKelvinHelmholtzFunctor2D_MHD::apply(params, KHParams(cfg), U);
+  else if (problem == "rotor")
+    InitRotorFunctor2D_MHD::apply(params, RotorParams(cfg), U);
+  else if (problem == "field_loop" || problem == "field loop")
+    InitFieldLoopFunctor2D_MHD::apply(params, FieldLoopParams(cfg), U);
+  else if (problem == "wave")
+    InitWaveFunctor2D_MHD::apply(params, WaveParams(cfg), U);
+  else
+    InitOrszagTangFunctor2D::apply(params, OrszagTangParams(cfg), U);
+}
+
+template <class DA>
+void
+init_problem_3d(ConfigMap & cfg, HydroParams & params, DA U)
+{
+  const std::string problem = cfg.getString("hydro", "problem", "unknown");
+  if (problem == "blast")
+    InitBlastFunctor3D_MHD::apply(params, BlastParams(cfg), U);
+  else if (problem == "implode")
+    InitImplodeFunctor3D_MHD::apply(params, ImplodeParams(cfg), U);
+  else if (problem == "kelvin_helmholtz")
+    InitKelvinHelmholtzFunctor3D_MHD::apply(params, KHParams(cfg), U);
+  else if (problem == "rotor")
+    InitRotorFunctor3D_MHD::apply(params, RotorParams(cfg), U);
+  else if (problem == "field_loop" || problem == "field loop")
+    InitFieldLoopFunctor3D_MHD::apply(params, FieldLoopParams(cfg), U);
+  else if (problem == "wave")
+    InitWaveFunctor3D_MHD::apply(params, WaveParams(cfg), U);
+  else
+    InitOrszagTangFunctor3D::apply(params, OrszagTangParams(cfg), U);
+}
+
 struct RefBase
 {
   ConfigMap   cfg;
@@ -131,9 +175,9 @@ struct Ref2D : RefBase
       Fluxes_y = DA("Fluxes_y", isize, jsize, nbvar);
       Emf1 = DataArrayScalar("Emf", isize, jsize);
     }
-    // SolverMHDMuscl.h:390-402 (Orszag-Tang initial condition)
-    OrszagTangParams otParams(cfg);
-    InitOrszagTangFunctor2D::apply(params, otParams, U);
+    // SolverMHDMuscl.h:390-402 (initial condition by [hydro] problem,
+    // dispatched as SolverMHDMuscl<dim>::init, SolverMHDMuscl.h:649-710)
+    init_problem_2d(cfg, params, U);
     finish_init();
   }
   void
@@ -303,8 +347,7 @@ struct Ref3D : RefBase
       Fluxes_z = DA("Fluxes_z", isize, jsize, ksize, nbvar);
       Emf = DataArrayVector3("Emf", isize, jsize, ksize);
     }
-    OrszagTangParams otParams(cfg);
-    InitOrszagTangFunctor3D::apply(params, otParams, U);
+    init_problem_3d(cfg, params, U);
     finish_init();
   }
   void
@@ -469,6 +512,37 @@ extern "C"
   ref_destroy(void * h)
   {
     delete static_cast<RefBase *>(h);
+  }
+
+  // The init functor's output alone (no boundary fill), LayoutRight, for the
+  // sizes of ref_create on the same text.  Returns the element count, 0 on
+  // an unknown solver.
+  long
+  ref_initial_state(const char * ini_text, real_t * out)
+  {
+    std::string s(ini_text);
+    char *      buf = &s[0];
+    ConfigMap   cfg(buf, (int)s.size());
+    HydroParams params;
+    params.setup(cfg);
+    const std::string solver = cfg.getString("run", "solver_name", "unknown");
+    if (solver == "MHD_Muscl_2D")
+    {
+      DataArray2d U("U", params.isize, params.jsize, params.nbvar);
+      init_problem_2d(cfg, params, U);
+      if (out)
+        std::memcpy(out, U.data(), U.size() * sizeof(real_t));
+      return (long)U.size();
+    }
+    if (solver == "MHD_Muscl_3D")
+    {
+      DataArray3d U("U", params.isize, params.jsize, params.ksize, params.nbvar);
+      init_problem_3d(cfg, params, U);
+      if (out)
+        std::memcpy(out, U.data(), U.size() * sizeof(real_t));
+      return (long)U.size();
+    }
+    return 0;
   }
 
   // sizes: isize, jsize, ksize, nbvar, dim, ghostWidth

@@ -38,6 +38,8 @@ MHD_FP64, MHD_FP32 = 64, 32
 MHD_FP_FAST, MHD_FP_EXACT = 0, 1
 MHD_LAYOUT_LEFT, MHD_LAYOUT_RIGHT = 0, 1
 MHD_PROBLEM_ORSZAG_TANG = 0
+(MHD_PROBLEM_BLAST, MHD_PROBLEM_IMPLODE, MHD_PROBLEM_KELVIN_HELMHOLTZ, MHD_PROBLEM_ROTOR,
+ MHD_PROBLEM_FIELD_LOOP, MHD_PROBLEM_WAVE) = range(1, 7)
 MHD_MLP_PARAMS = 5768
 MHD_SAMPLE_FLOATS = 24
 MHD_MLP_TRAIN, MHD_MLP_CHECK = 0, 1
@@ -58,11 +60,13 @@ class MHDParams(ctypes.Structure):
         ("tEnd", ctypes.c_double), ("tCurrent", ctypes.c_double), ("nStepmax", ctypes.c_int),
         ("problem", ctypes.c_int), ("ot_kt", ctypes.c_double),
         ("precision", ctypes.c_int), ("fp_mode", ctypes.c_int), ("device", ctypes.c_int),
+        ("problem_real", ctypes.c_double * 24), ("problem_int", ctypes.c_int * 4),
     ]
 
     def as_dict(self):
         d = {f: getattr(self, f) for f, _ in self._fields_}
-        d["boundary"] = list(self.boundary)
+        for f in ("boundary", "problem_real", "problem_int"):
+            d[f] = list(getattr(self, f))
         return d
 
 
@@ -85,6 +89,7 @@ SIGNATURES = {
     "mhd_create": (ctypes.c_int, [ctypes.POINTER(MHDParams), ctypes.POINTER(_vp)]),
     "mhd_destroy": (ctypes.c_int, [_vp]),
     "mhd_init_problem": (ctypes.c_int, [_vp]),
+    "mhd_initial_state": (ctypes.c_int, [ctypes.POINTER(MHDParams), _vp]),
     "mhd_set_state": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int]),
     "mhd_get_state": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int]),
     "mhd_step": (ctypes.c_int, [_vp]),
@@ -162,6 +167,19 @@ def params_from_ini(ini_text: str) -> MHDParams:
     if rc != MHD_OK:
         raise MHDError(rc, err.value.decode())
     return p
+
+
+def initial_state(params: MHDParams) -> np.ndarray:
+    """The initial condition of params.problem (host FP64, LayoutLeft, ghosts
+    included, before any boundary fill)."""
+    g = params.ghost
+    shape = (8, params.ny + 2 * g, params.nx + 2 * g) if params.dim == 2 else \
+        (8, params.nz + 2 * g, params.ny + 2 * g, params.nx + 2 * g)
+    U = np.empty(shape, dtype=np.float64)
+    rc = lib().mhd_initial_state(ctypes.byref(params), U.ctypes.data)
+    if rc != MHD_OK:
+        raise MHDError(rc, "invalid parameters")
+    return U
 
 
 def default_params() -> MHDParams:

@@ -109,9 +109,10 @@ def build(jobs: int | None = None, force: bool = False, verbose: bool = False) -
     objs.append(o)
     cmds.append([nvcc(), *GENCODE, *NVCC_COMMON, "--fmad=true", "-Xptxas", "-v",
                  "-c", os.path.join(CSRC, "mhd_noalloc.cu"), "-o", o])
-    o = os.path.join(OBJ, "mhd_capi.o")
-    objs.append(o)
-    cmds.append(["g++", *CXX_COMMON, "-c", os.path.join(CSRC, "mhd_capi.cpp"), "-o", o])
+    for src in ("mhd_capi.cpp", "mhd_init.cpp"):
+        o = os.path.join(OBJ, src.replace(".cpp", ".o"))
+        objs.append(o)
+        cmds.append(["g++", *CXX_COMMON, "-c", os.path.join(CSRC, src), "-o", o])
     for src in HOST_SOURCES:
         o = os.path.join(OBJ, src.replace(".cpp", ".o"))
         objs.append(o)

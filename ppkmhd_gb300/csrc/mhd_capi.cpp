@@ -113,8 +113,15 @@ validate_params(const mhd_params & p)
     return "fp_mode must be MHD_FP_FAST or MHD_FP_EXACT";
   if (p.precision == MHD_FP32 && p.fp_mode == MHD_FP_EXACT)
     return "MHD_FP_EXACT is only available with MHD_FP64";
-  if (p.problem != MHD_PROBLEM_ORSZAG_TANG)
+  if (p.problem < MHD_PROBLEM_ORSZAG_TANG || p.problem > MHD_PROBLEM_WAVE)
     return "unknown problem id";
+  if (p.problem == MHD_PROBLEM_KELVIN_HELMHOLTZ && p.problem_int[3])
+    return "kelvin_helmholtz: perturbation_rand draws from Kokkos' own generator; use the sine "
+           "perturbations";
+  if (p.problem == MHD_PROBLEM_KELVIN_HELMHOLTZ && !p.problem_int[0] && !p.problem_int[1])
+    return "kelvin_helmholtz: no perturbation selected (the reference leaves the state empty)";
+  if (p.problem == MHD_PROBLEM_WAVE && (p.problem_int[0] < 0 || p.problem_int[0] > 3))
+    return "wave: type must be 0 (fast), 1 (Alfven), 2 (slow) or 3 (contact)";
   return "";
 }
 
@@ -128,98 +135,6 @@ using mhd::validate_params;
 namespace mhd
 {
 
-// Orszag-Tang vortex, FP64 on the host, LayoutLeft with ghosts
-// (InitOrszagTangFunctor2D, MHDInitFunctors2D.h:241-389;
-// InitOrszagTangFunctor3D, MHDInitFunctors3D.h:264-415): rho and p
-// uniform, v = (-sin 2 pi y, sin 2 pi x, 0), face-centred
-// B = B0 (-sin 2 pi y_c, sin 4 pi x_c, 0) (times cos(4 pi kt z') in 3D),
-// total energy from the cell-centred field.  Two passes like the
-// reference: everything but energy on all cells, then energy on
-// [0, size-1) in i and j.
-void
-init_orszag_tang_host(const mhd_params & p, double * U)
-{
-  const int     g = p.ghost;
-  const int     isize = p.nx + 2 * g, jsize = p.ny + 2 * g, ksize = p.dim == 3 ? p.nz + 2 * g : 1;
-  const int64_t sj = isize, sk = (int64_t)isize * jsize, sv = sk * ksize;
-  const double  dx = (p.xmax - p.xmin) / p.nx;
-  const double  dy = (p.ymax - p.ymin) / p.ny;
-  const double  dz = p.dim == 3 ? (p.zmax - p.zmin) / p.nz : 1.0;
-  const double  PI = 3.141592653589793238462643383279502884;
-  const double  TWOPI = 2 * PI;
-  const double  gamma0 = p.gamma0;
-  double        B0, p0, p0e;
-  if (p.dim == 2)
-  {
-    B0 = 1.0 / std::sqrt(2 * TWOPI);
-    p0 = gamma0 / (2 * TWOPI);
-    p0e = gamma0 / (2.0 * (4.0 * std::asin(1.0)));
-  }
-  else
-  {
-    B0 = 1.0 / std::sqrt(4 * PI);
-    p0 = gamma0 / (4 * PI);
-    p0e = p0;
-  }
-  const double d0 = gamma0 * p0;
-  const double v0 = 1.0;
-  enum
-  {
-    ID = 0,
-    IP = 1,
-    IU = 2,
-    IV = 3,
-    IW = 4,
-    IA = 5,
-    IB = 6,
-    IC = 7
-  };
-#pragma omp parallel for schedule(static)
-  for (int k = 0; k < ksize; ++k)
-  {
-    double zfac = 1.0;
-    if (p.dim == 3)
-    {
-      const double zPos = p.zmin + dz / 2 + (k - g) * dz;
-      zfac = std::cos(2 * TWOPI * p.ot_kt * (zPos - p.zmin) / (p.zmax - p.zmin));
-    }
-    for (int j = 0; j < jsize; ++j)
-      for (int i = 0; i < isize; ++i)
-      {
-        const double  xPos = p.xmin + dx / 2 + (i - g) * dx;
-        const double  yPos = p.ymin + dy / 2 + (j - g) * dy;
-        const int64_t c = i + j * sj + k * sk;
-        U[c + ID * sv] = d0;
-        U[c + IU * sv] = -d0 * v0 * std::sin(yPos * TWOPI);
-        U[c + IV * sv] = d0 * v0 * std::sin(xPos * TWOPI);
-        U[c + IW * sv] = 0.0;
-        if (p.dim == 2)
-        {
-          U[c + IA * sv] = -B0 * std::sin(yPos * TWOPI);
-          U[c + IB * sv] = B0 * std::sin(2.0 * xPos * TWOPI);
-        }
-        else
-        {
-          U[c + IA * sv] = -B0 * zfac * std::sin(yPos * TWOPI);
-          U[c + IB * sv] = B0 * zfac * std::sin(2.0 * xPos * TWOPI);
-        }
-        U[c + IC * sv] = 0.0;
-      }
-  }
-#pragma omp parallel for schedule(static)
-  for (int k = 0; k < ksize; ++k)
-    for (int j = 0; j < jsize - 1; ++j)
-      for (int i = 0; i < isize - 1; ++i)
-      {
-        const int64_t c = i + j * sj + k * sk;
-        const double  bxs = U[c + IA * sv] + U[c + 1 + IA * sv];
-        const double  bys = U[c + IB * sv] + U[c + sj + IB * sv];
-        U[c + IP * sv] = p0e / (gamma0 - 1.0) +
-                         0.5 * (U[c + IU * sv] * U[c + IU * sv] / U[c + ID * sv] +
-                                U[c + IV * sv] * U[c + IV * sv] / U[c + ID * sv] +
-                                0.25 * (bxs * bxs) + 0.25 * (bys * bys));
-      }
-}
 
 } // namespace mhd
 
@@ -350,6 +265,18 @@ extern "C"
     if (int rc_ = (ctx)->core->bind_device())                            \
       return from_core((ctx), rc_);                                      \
   } while (0)
+
+  int
+  mhd_initial_state(const mhd_params * p, double * U)
+  {
+    if (!p || !U || !validate_params(*p).empty())
+      return MHD_ERR_INVALID_ARG;
+    const size_t n = (size_t)(p->nx + 2 * p->ghost) * (p->ny + 2 * p->ghost) *
+                     (p->dim == 3 ? p->nz + 2 * p->ghost : 1) * 8;
+    std::memset(U, 0, n * sizeof(double));
+    mhd::init_problem_host(*p, U);
+    return MHD_OK;
+  }
 
   int
   mhd_init_problem(mhd_ctx * ctx)

@@ -80,8 +80,11 @@ const float * mlp_params(const mhd_mlp * m);
 // Empty string when the parameters can be run, else the reason (mhd_capi.cpp).
 std::string validate_params(const mhd_params & p);
 
-// Orszag-Tang initial condition in FP64 on the host, LayoutLeft, ghosts
-// included (MHDInitFunctors2D.h:241-389, MHDInitFunctors3D.h:264-415).
+// Initial condition of p.problem in FP64 on the host, LayoutLeft, ghosts
+// included, into a zeroed array (mhd_init.cpp).
+void init_problem_host(const mhd_params & p, double * U);
+// Orszag-Tang initial condition (MHDInitFunctors2D.h:241-389,
+// MHDInitFunctors3D.h:264-415).
 void init_orszag_tang_host(const mhd_params & p, double * U);
 
 } // namespace mhd

@@ -538,7 +538,7 @@ public:
     if (int rc = check_problem(p))
       return rc;
     std::vector<double> h((size_t)G[p].sv * NV);
-    init_orszag_tang_host(P[p], h.data());
+    init_problem_host(P[p], h.data());
     if constexpr (sizeof(R) == 8)
       return set_state(p, h.data(), MHD_LAYOUT_LEFT);
     std::vector<float> f(h.size());

@@ -641,7 +641,7 @@ public:
   init_problem() override
   {
     std::vector<double> h((size_t)ncell * NV);
-    init_orszag_tang_host(P, h.data());
+    init_problem_host(P, h.data());
     if constexpr (sizeof(R) == 8)
     {
       MHD_CK(cudaMemcpy(U, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));

@@ -1,5 +1,7 @@
 #include "HydroParams.h"
 
+#include <cmath>
+
 #include <cstdio>
 #include <iostream>
 
@@ -174,6 +176,122 @@ HydroParams::to_mhd_params(const ConfigMap & map, int precision, int fp_mode) co
   const std::string problem = map.getString("hydro", "problem", "unknown");
   p.problem = MHD_PROBLEM_ORSZAG_TANG; // unknown problems default to Orszag-Tang (SolverMHDMuscl.h:700-708)
   p.ot_kt = map.getFloat("OrszagTang", "kt", 0.0f);
+  double * r = p.problem_real;
+  int *    n = p.problem_int;
+  if (problem == "blast")
+  {
+    // BlastParams (src/shared/problems/BlastParams.h)
+    p.problem = MHD_PROBLEM_BLAST;
+    const double x0 = map.getFloat("mesh", "xmin", 0.0f), y0 = map.getFloat("mesh", "ymin", 0.0f);
+    const double z0 = map.getFloat("mesh", "zmin", 0.0f), x1 = map.getFloat("mesh", "xmax", 1.0f);
+    const double y1 = map.getFloat("mesh", "ymax", 1.0f), z1 = map.getFloat("mesh", "zmax", 1.0f);
+    r[0] = map.getFloat("blast", "radius", (float)((x0 + x1) / 2.0 / 10));
+    r[1] = map.getFloat("blast", "center_x", (float)((x0 + x1) / 2));
+    r[2] = map.getFloat("blast", "center_y", (float)((y0 + y1) / 2));
+    r[3] = map.getFloat("blast", "center_z", (float)((z0 + z1) / 2));
+    r[4] = map.getFloat("blast", "density_in", 1.0f);
+    r[5] = map.getFloat("blast", "density_out", 1.2f);
+    r[6] = map.getFloat("blast", "pressure_in", 10.0f);
+    r[7] = map.getFloat("blast", "pressure_out", 0.1f);
+  }
+  else if (problem == "implode")
+  {
+    // ImplodeParams (src/shared/problems/ImplodeParams.h)
+    p.problem = MHD_PROBLEM_IMPLODE;
+    const char * side[2] = { "outer", "inner" };
+    const float  dflt[2][8] = { { 1.0f, 1.0f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f },
+                                { 0.125f, 0.14f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f } };
+    const char * key[8] = { "density_", "pressure_", "vx_", "vy_", "vz_", "Bx_", "By_", "Bz_" };
+    for (int s = 0; s < 2; ++s)
+      for (int q = 0; q < 8; ++q)
+        r[8 * s + q] = map.getFloat("implode", std::string(key[q]) + side[s], dflt[s][q]);
+    n[0] = (int)map.getInteger("implode", "shape_region", 0);
+  }
+  else if (problem == "kelvin_helmholtz")
+  {
+    // KHParams (src/shared/problems/KHParams.h)
+    p.problem = MHD_PROBLEM_KELVIN_HELMHOLTZ;
+    r[0] = map.getFloat("KH", "d_in", 1.0f);
+    r[1] = map.getFloat("KH", "d_out", 1.0f);
+    r[2] = map.getFloat("KH", "pressure", 10.0f);
+    r[3] = map.getFloat("KH", "vflow_in", -0.5f);
+    r[4] = map.getFloat("KH", "vflow_out", 0.5f);
+    r[5] = map.getFloat("KH", "amplitude", 0.1f);
+    r[6] = map.getFloat("KH", "w0", 0.1f);
+    r[7] = map.getFloat("KH", "delta", 0.03f);
+    n[0] = map.getBool("KH", "perturbation_sine", false) ? 1 : 0;
+    n[1] = map.getBool("KH", "perturbation_sine_robertson", true) ? 1 : 0;
+    n[2] = (int)map.getInteger("KH", "mode", 2);
+    n[3] = map.getBool("KH", "perturbation_rand", false) ? 1 : 0;
+  }
+  else if (problem == "rotor")
+  {
+    // RotorParams (src/shared/problems/RotorParams.h)
+    p.problem = MHD_PROBLEM_ROTOR;
+    r[0] = map.getFloat("rotor", "r0", 0.1f);
+    r[1] = map.getFloat("rotor", "r1", 0.115f);
+    r[2] = map.getFloat("rotor", "u0", 2.0f);
+    r[3] = map.getFloat("rotor", "p0", 1.0f);
+    r[4] = map.getFloat("rotor", "b0", (float)(5.0 / std::sqrt(4 * M_PI)));
+  }
+  else if (problem == "field_loop" || problem == "field loop")
+  {
+    // FieldLoopParams (src/shared/problems/FieldLoopParams.h)
+    p.problem = MHD_PROBLEM_FIELD_LOOP;
+    r[0] = map.getFloat("FieldLoop", "radius", 1.0f);
+    r[1] = map.getFloat("FieldLoop", "density_in", 1.0f);
+    r[2] = map.getFloat("FieldLoop", "amplitude", 1.0f);
+    r[3] = map.getFloat("FieldLoop", "vflow", 1.0f);
+  }
+  else if (problem == "wave")
+  {
+    // WaveParams (src/shared/problems/WaveParams.h): right eigenvectors of
+    // the fast, Alfven, slow and contact waves and the rotated wave vector
+    p.problem = MHD_PROBLEM_WAVE;
+    const double xmn = map.getFloat("mesh", "xmin", 0.0f), ymn = map.getFloat("mesh", "ymin", 0.0f);
+    const double zmn = map.getFloat("mesh", "zmin", 0.0f), xmx = map.getFloat("mesh", "xmax", 3.0f);
+    const double ymx = map.getFloat("mesh", "ymax", 1.5f), zmx = map.getFloat("mesh", "zmax", 1.5f);
+    const double Lx = xmx - xmn, Ly = ymx - ymn, Lz = zmx - zmn;
+    const double g = map.getFloat("hydro", "gamma0", 1.66667f);
+    const double amp = map.getFloat("wave", "amplitude", 1.0e-6f);
+    const int    type = (int)map.getInteger("wave", "type", 0);
+    static const double ev[4][7] = {
+      { 4.472136e-01, -8.944272e-01, 4.216370e-01, 1.490712e-01, 2.012461e+00, 8.432740e-01,
+        2.981424e-01 },
+      { 0.0, 0.0, -3.333333e-01, 9.428090e-01, 0.0, -3.333333e-01, 9.428090e-01 },
+      { 8.944272e-01, -4.472136e-01, -8.432740e-01, -2.981424e-01, 6.708204e-01, -4.216370e-01,
+        -1.490712e-01 },
+      { 1.0, 1.0, 0.0, 0.0, 0.5, 0.0, 0.0 } };
+    n[0] = type;
+    if (type >= 0 && type <= 3)
+    {
+      r[0] = amp;
+      r[1] = type == 3 ? 1.0 : 0.0;
+      for (int q = 0; q < 7; ++q)
+        r[2 + q] = ev[type][q];
+      r[9] = 1.0;
+      r[10] = 1.0 / g;
+      const double TwoPi = 4.0 * std::asin(1.0);
+      const double ang_3 = std::atan(Lx / Ly);
+      r[13] = std::sin(ang_3);
+      r[14] = std::cos(ang_3);
+      const double ang_2 = std::atan(0.5 * (Lx * r[14] + Ly * r[13]) / Lz);
+      r[11] = std::sin(ang_2);
+      r[12] = std::cos(ang_2);
+      const double x1 = Lx * r[12] * r[14], x2 = Ly * r[12] * r[13], x3 = Lz * r[11];
+      double       lambda = x1;
+      if (ang_3 != 0.0)
+        lambda = std::fmin(lambda, x2);
+      if (ang_2 != 0.)
+        lambda = std::fmin(lambda, x3);
+      r[20] = TwoPi / lambda;
+      r[15] = amp * r[2 + 5];
+      r[16] = amp * r[2 + 6];
+      r[17] = 1.0;
+      r[18] = std::sqrt(2.0);
+      r[19] = 0.5;
+    }
+  }
   p.precision = precision;
   p.fp_mode = fp_mode;
   return p;

@@ -11,8 +11,13 @@ seeded cases, and stores inputs and outputs as .npz:
   emf.npz        compute_emf<EMFX/Y/Z> for random edge states
   params.npz     HydroParams fields parsed from .ini texts
 
+  problem_*.npz  other initial conditions of SolverMHDMuscl<dim>::init
+                 (blast, implode, Kelvin-Helmholtz, rotor, field loop,
+                 linear wave): init-functor output, state after the
+                 boundary fill, interior state after n steps
+
 usage (from the repository root, where the reference tree is present):
-    oracle/build_ref.sh && python tests/golden/make_golden.py
+    oracle/build_ref.sh && python tests/golden/make_golden.py [steps|problems|riemann|emf|params ...]
 """
 from __future__ import annotations
 
@@ -73,6 +78,78 @@ def make_steps():
                             U1=U1, Un=Un, nsteps=nsteps, t=np.array([t0, t1, tn]),
                             dt=np.array([dt0, dt1, dtn]), perturbed=seed is not None)
         print(f"steps_{name}: {nsteps} steps, t={tn:.6f}")
+
+
+# Other problems of SolverMHDMuscl<dim>::init through the reference's own
+# init functors (settings of the reference's .ini files, smaller grids).
+def problem_ini(dim, n, problem, section="", bc=3, gamma0="1.666", cfl="0.8", version=2,
+                mesh="", nsteps=1000) -> str:
+    nx, ny = n[0], n[1]
+    lines = ["[run]", f"solver_name=MHD_Muscl_{dim}D", "tEnd=10.0", f"nStepmax={nsteps}",
+             "nOutput=0", "", "[mesh]", f"nx={nx}", f"ny={ny}"]
+    if dim == 3:
+        lines.append(f"nz={n[2]}")
+    for f in ("xmin", "xmax", "ymin", "ymax", "zmin", "zmax")[: 2 * dim]:
+        lines.append(f"boundary_type_{f}={bc}")
+    lines += [mesh, "", "[hydro]", f"gamma0={gamma0}", f"cfl={cfl}", "niter_riemann=10",
+              "iorder=2", "slope_type=2", f"problem={problem}", "riemann=hlld", "smallr=1e-8",
+              "smallc=1e-8", "", section, "", "[OTHER]", f"implementationVersion={version}"]
+    return "\n".join(lines) + "\n"
+
+
+PROBLEM_CASES = [
+    # name, ini, steps
+    ("rotor2d", problem_ini(2, (32, 32), "rotor", "[rotor]\nr0=0.1\nr1=0.115\nu0=1.0\np0=1.5",
+                            bc=2, gamma0="1.4", cfl="0.4"), 8),
+    ("rotor2d_v0", problem_ini(2, (24, 24), "rotor", "[rotor]\nr0=0.1\nr1=0.115\nu0=1.0\np0=1.5",
+                               bc=2, gamma0="1.4", cfl="0.4", version=0), 6),
+    ("blast2d", problem_ini(2, (24, 36), "blast", "[blast]\ndensity_in=1.0\ndensity_out=1.2",
+                            mesh="xmin=0.0\nxmax=1.0\nymin=0.0\nymax=1.5"), 8),
+    ("implode2d", problem_ini(2, (24, 24), "implode", "", bc=1, gamma0="1.4"), 8),
+    ("field_loop2d", problem_ini(2, (32, 16), "field_loop",
+                                 "[FieldLoop]\nradius=0.3\namplitude=0.001\nvflow=3",
+                                 gamma0="1.4", cfl="0.4",
+                                 mesh="xmin=-1.0\nxmax=1.0\nymin=-0.5\nymax=0.5"), 8),
+    ("kh2d", problem_ini(2, (24, 24), "kelvin_helmholtz",
+                         "[kh]\namplitude=0.01\nperturbation_sine_robertson=1\nmode=2\n"
+                         "w0=0.1\ndelta=0.02\nd_in=2.0\nd_out=1.0\npressure=2.5"), 6),
+    ("kh2d_sine", problem_ini(2, (20, 20), "kelvin_helmholtz",
+                              "[kh]\nperturbation_sine=1\nperturbation_sine_robertson=0\n"
+                              "mode=1\nw0=0.05\nd_in=2.0\nd_out=1.0\npressure=2.5"), 6),
+    ("blast3d", problem_ini(3, (12, 12, 12), "blast", ""), 4),
+    ("rotor3d", problem_ini(3, (12, 12, 6), "rotor", "", bc=2, gamma0="1.4", cfl="0.4"), 4),
+    ("implode3d", problem_ini(3, (10, 10, 10), "implode", "[implode]\nshape_region=1", bc=1,
+                              gamma0="1.4"), 3),
+    ("field_loop3d", problem_ini(3, (16, 8, 8), "field_loop",
+                                 "[FieldLoop]\nradius=0.3\namplitude=0.001\nvflow=3",
+                                 cfl="0.4", mesh="xmin=-1.0\nxmax=1.0\nymin=-0.5\nymax=0.5\n"
+                                 "zmin=-0.5\nzmax=0.5"), 4),
+    ("kh3d", problem_ini(3, (10, 10, 10), "kelvin_helmholtz",
+                         "[kh]\nperturbation_sine_robertson=1\nmode=2\nw0=0.1\ndelta=0.05\n"
+                         "d_in=2.0\nd_out=1.0\npressure=2.5"), 3),
+    ("wave3d_fast", problem_ini(3, (16, 8, 8), "wave", "[wave]\ntype=0\namplitude=1e-6",
+                                gamma0="1.6666666667", cfl="0.4",
+                                mesh="xmax=3.0\nymax=1.5\nzmax=1.5"), 4),
+    ("wave3d_alfven", problem_ini(3, (16, 8, 8), "wave", "[wave]\ntype=1\namplitude=1e-6",
+                                  gamma0="1.6666666667", cfl="0.4",
+                                  mesh="xmax=3.0\nymax=1.5\nzmax=1.5"), 4),
+    ("unknown_is_ot", problem_ini(2, (16, 16), "FieldLoop", ""), 3),
+]
+
+
+def make_problems():
+    for name, ini, nsteps in PROBLEM_CASES:
+        Uinit = op.ref_initial_state(ini)
+        r = op.RefSolver(ini)
+        U0 = r.get_state()
+        t0, dt0, _ = r.time()
+        r.run(nsteps)
+        Un = op.interior(r.get_state())
+        tn, dtn, itn = r.time()
+        np.savez_compressed(os.path.join(HERE, f"problem_{name}.npz"), ini=np.array(ini),
+                            Uinit=Uinit, U0=U0, Un=Un, nsteps=nsteps, t=np.array([t0, tn]),
+                            dt=np.array([dt0, dtn]))
+        print(f"problem_{name}: {nsteps} steps, t={tn:.6f}")
 
 
 def riemann_states(rng, n):
@@ -176,9 +253,9 @@ def make_params():
 if __name__ == "__main__":
     if not op.ref_available(64):
         sys.exit("oracle/_ref/libppkmhd_ref64.so missing: run oracle/build_ref.sh first")
-    make_steps()
-    make_riemann()
-    make_emf()
-    make_params()
+    parts = sys.argv[1:] or ["steps", "problems", "riemann", "emf", "params"]
+    for part in parts:
+        {"steps": make_steps, "problems": make_problems, "riemann": make_riemann,
+         "emf": make_emf, "params": make_params}[part]()
     with open(os.path.join(HERE, "MANIFEST.json"), "w") as f:
         json.dump(sorted(n for n in os.listdir(HERE) if n.endswith(".npz")), f, indent=1)
