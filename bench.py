@@ -289,16 +289,44 @@ def run_gb300(args):
     # FP32 companion figure for the same workload (device-resident)
     variants = {}
     if args.workload == "ot3d_256_fp64" and not args.no_variants:
-        p32 = m.params_from_ini(ot_ini(dim, n, 32))
-        p32.device = local
-        s32 = m.MHDSolver(p32)
-        s32.set_state(U0.astype(np.float32))
-        s32.run_timed(3)
-        ms32 = s32.run_timed(args.steps)
-        variants["fp32"] = {"value": interior_cells * args.steps / (ms32 / 1e3),
-                            "ms_per_step": ms32 / args.steps, "dtype": "f32",
-                            "note": "FP32 storage and arithmetic, FP64 dt/sums/div B"}
-        s32.close()
+        # FP32 and FP32 + flux surrogate on the same initial state: throughput,
+        # and relative L1 (max over variables) against the FP64 solution after
+        # the same number of steps
+        from ppkmhd_gb300 import surrogate
+
+        acc_steps = 20
+        p64 = m.params_from_ini(ini)
+        p64.device = local
+        s64 = m.MHDSolver(p64)
+        s64.set_state(U0)
+        s64.run(acc_steps)
+        ref = m.interior(s64.get_state())
+        s64.close()
+        den = np.abs(ref).sum(axis=(1, 2, 3))
+        den = np.where(den > 1e-12 * den[0], den, den[0])
+        for tag, use_mlp in (("fp32", False), ("fp32_surrogate", True)):
+            p32 = m.params_from_ini(ot_ini(dim, n, 32))
+            p32.device = local
+            s32 = m.MHDSolver(p32)
+            s32.set_state(U0.astype(np.float32))
+            if use_mlp:
+                s32.set_surrogate(surrogate.FluxMLP.load(), tau=0.01)
+            s32.run(acc_steps)
+            err = np.abs(m.interior(s32.get_state()).astype(np.float64) - ref).sum(axis=(1, 2, 3))
+            s32.set_state(U0.astype(np.float32))
+            s32.run_timed(3)
+            ms32 = s32.run_timed(args.steps)
+            v = {"value": interior_cells * args.steps / (ms32 / 1e3),
+                 "ms_per_step": ms32 / args.steps, "dtype": "f32",
+                 "rel_l1_vs_fp64": float((err / den).max()), "accuracy_steps": acc_steps,
+                 "note": "FP32 storage and arithmetic, FP64 dt/sums/div B"}
+            if use_mlp:
+                used, total = s32.surrogate_stats()
+                v["faces_by_network"] = used / max(total, 1)
+                v["note"] += "; HLLD flux surrogate (BF16 tensor-core MLP, tau 0.01)"
+                v["dtype"] = "f32+bf16"
+            variants[tag] = v
+            s32.close()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -339,6 +367,10 @@ def run_gb300(args):
                          "algorithmic_bytes_per_cell": alg_bytes_per_cell,
                          "step_achieved": step_achieved,
                          "step_frac": step_achieved / hbm_peak},
+            "alu_roofline": (lambda a: None if a is None or precision != 64 else {
+                "bound": "fp64 pipe (2 DFMA/SM/cycle, 1.26 TFLOP/s at 2070 MHz)",
+                "kernel": dom, "pipe_active_frac": a.get("pipe_active", {}).get(dom),
+                "source": a.get("source")})(load_alu_profile(args.workload.replace("256", "128"))),
             "clocks": clk.summary(),
             "gpu_launches": s.launches_per_step() * args.steps,
             "cpu_baseline": cpu,
@@ -635,6 +667,17 @@ def run_turbulence(args):
             "gpu_launches": len(prof) * args.steps,
             "cpu_baseline": cpu,
         })
+
+
+def load_alu_profile(workload: str):
+    """FP64-pipe utilisation of the kernels from the committed ncu summary
+    (profiles/fp64_pipe_<workload>.json), or None."""
+    path = os.path.join(ROOT, "profiles", f"fp64_pipe_{workload}.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
 
 
 def load_profile_traffic(workload: str, kernel: str):

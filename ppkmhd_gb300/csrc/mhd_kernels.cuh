@@ -382,9 +382,11 @@ prim_dt_body(const Grid<R> & G, const R * __restrict__ U, R * __restrict__ Q, De
           val = sx * R(G.idx) + sy * R(G.idy);
       }
       // fmax in the reference ignores NaN operands; a NaN rate is dropped
+      // (it arises legitimately when round-off makes the inner root of the
+      // fast speed slightly negative, e.g. for a field along one axis)
       rate = (val >= R(0)) ? val : R(0);
       const R Ein = U[c + IP * sv];
-      bad = !(U[c + ID * sv] > R(0)) || !isfinite(Ein) || !isfinite(val);
+      bad = !(U[c + ID * sv] > R(0)) || !isfinite(Ein);
     }
   }
   // block max in the working precision (max is exact in any precision), then

@@ -8,6 +8,9 @@ weights ``ppkmhd_gb300/data/flux_mlp.npz``:
 
     python -m ppkmhd_gb300.surrogate train --out ppkmhd_gb300/data/flux_mlp.npz
 
+``python -m ppkmhd_gb300.surrogate run --n 96 --steps 3`` runs the
+turbulence state with the network (the case the flux-stage profile uses).
+
 Record layout (MHD_SAMPLE_FLOATS = 24 floats): qL[7], qR[7] (rho, vn, vt1,
 vt2, p, Bt1, Bt2, face-normal frame), a (normal B), J (sensor), D[7] (FP64
 central flux minus FP64 HLLD flux), gamma0.
@@ -253,9 +256,26 @@ def train(out: str = DEFAULT_WEIGHTS, scale: float = 2.0, epochs: int = 250, bat
     return meta
 
 
+def run_turbulence(n: int = 96, steps: int = 3, tau: float = 0.01, weights: str = DEFAULT_WEIGHTS):
+    """The FP32 turbulence state with the network in the flux stage: returns
+    (faces by the network, faces computed)."""
+    ini = workloads.ot_ini(3, n, gamma0="1.6666666666666667", precision=32)
+    s = MHDSolver(params_from_ini(ini))
+    s.set_state(workloads.turbulence_3d(n, seed=11).astype(np.float32))
+    s.set_surrogate(FluxMLP.load(weights), tau=tau)
+    s.run(steps)
+    out = s.surrogate_stats()
+    s.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     sub = ap.add_subparsers(dest="cmd", required=True)
+    r = sub.add_parser("run", help="turbulence state with the network in the flux stage")
+    r.add_argument("--n", type=int, default=96)
+    r.add_argument("--steps", type=int, default=3)
+    r.add_argument("--tau", type=float, default=0.01)
     t = sub.add_parser("train")
     t.add_argument("--out", default=DEFAULT_WEIGHTS)
     t.add_argument("--scale", type=float, default=2.0)
@@ -265,6 +285,9 @@ def main():
     t.add_argument("--seed", type=int, default=1)
     t.add_argument("--weight-power", type=float, default=1.0)
     a = ap.parse_args()
+    if a.cmd == "run":
+        used, total = run_turbulence(a.n, a.steps, a.tau)
+        print(json.dumps({"faces_network": used, "faces_total": total}))
     if a.cmd == "train":
         meta = train(a.out, a.scale, a.epochs, a.batch, a.lr, a.seed, a.weight_power)
         print(json.dumps({k: v for k, v in meta.items() if k != "loss_history"}))
