@@ -371,11 +371,11 @@ prim_dt_body(const Grid<R> & G, const R * __restrict__ U, R * __restrict__ Q, De
         const R c2 = G.gamma0 * p * invd;
         const R d2 = R(0.5) * (b2 * invd + c2);
         const R cd = c2 * invd;
-        const R sx = sqrt(d2 + sqrt(d2 * d2 - cd * a * a)) + fabs(vu);
-        const R sy = sqrt(d2 + sqrt(d2 * d2 - cd * bb * bb)) + fabs(vv);
+        const R sx = fsqrt(d2 + fsqrt(d2 * d2 - cd * a * a)) + fabs(vu);
+        const R sy = fsqrt(d2 + fsqrt(d2 * d2 - cd * bb * bb)) + fabs(vv);
         if constexpr (DIM == 3)
         {
-          const R sz = sqrt(d2 + sqrt(d2 * d2 - cd * cc * cc)) + fabs(vw);
+          const R sz = fsqrt(d2 + fsqrt(d2 * d2 - cd * cc * cc)) + fabs(vw);
           val = sx * R(G.idx) + sy * R(G.idy) + sz * R(G.idz);
         }
         else

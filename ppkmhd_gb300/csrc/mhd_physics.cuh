@@ -72,6 +72,11 @@ swap_vals(R & a, R & b)
 #endif
 constexpr bool kExactOrder = MHD_EXACT_BUILD != 0;
 
+// Reciprocal, reciprocal square root and square root of the fast builds.
+// FP64 keeps the CUDA library's correctly rounded reciprocal, its rsqrt and
+// the IEEE square root (a Newton-Raphson refinement of the hardware
+// approximations measured 13 % slower on the FP64-bound kernels).  FP32
+// uses the hardware approximations alone (about 1 ulp).
 __device__ __forceinline__ double
 rcp(double x)
 {
@@ -80,7 +85,9 @@ rcp(double x)
 __device__ __forceinline__ float
 rcp(float x)
 {
-  return __frcp_rn(x);
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
 }
 __device__ __forceinline__ double
 rsq(double x)
@@ -90,7 +97,23 @@ rsq(double x)
 __device__ __forceinline__ float
 rsq(float x)
 {
-  return rsqrtf(x);
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+// FP32: sqrt(x) = x / sqrt(x) for positive finite arguments (zero, negative,
+// infinite and NaN arguments take the IEEE square root); FP64: IEEE.
+__device__ __forceinline__ float
+fsqrt(float x)
+{
+  if (x > 0.f && x < INFINITY)
+    return x * rsq(x);
+  return sqrtf(x);
+}
+__device__ __forceinline__ double
+fsqrt(double x)
+{
+  return sqrt(x);
 }
 
 // Both fast magnetosonic speeds (normal field in slot IA, then in slot IB)
@@ -105,8 +128,8 @@ fast_speeds_xy(const State<R> & q, R gamma0, R & cfx, R & cfy)
   const R c2 = gamma0 * q[IP] * invd;
   const R d2 = R(0.5) * (b2 * invd + c2);
   const R cd = c2 * invd;
-  cfx = sqrt(d2 + sqrt(d2 * d2 - cd * a * a));
-  cfy = sqrt(d2 + sqrt(d2 * d2 - cd * b * b));
+  cfx = fsqrt(d2 + fsqrt(d2 * d2 - cd * a * a));
+  cfy = fsqrt(d2 + fsqrt(d2 * d2 - cd * b * b));
 }
 
 // Fast magnetosonic speed with the normal field in slot IA
@@ -477,13 +500,13 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
     const R id = rcp(rl);
     const R c2 = gamma0 * pl * id;
     const R d2 = R(0.5) * (b2l * id + c2);
-    cfastl = sqrt(d2 + sqrt(d2 * d2 - c2 * a2 * id));
+    cfastl = fsqrt(d2 + fsqrt(d2 * d2 - c2 * a2 * id));
   }
   {
     const R id = rcp(rr);
     const R c2 = gamma0 * pr * id;
     const R d2 = R(0.5) * (b2r * id + c2);
-    cfastr = sqrt(d2 + sqrt(d2 * d2 - c2 * a2 * id));
+    cfastr = fsqrt(d2 + fsqrt(d2 * d2 - c2 * a2 * id));
   }
   const R cmax = fmax(cfastl, cfastr);
   const R sl = fmin(ul, ur) - cmax;

@@ -111,7 +111,7 @@ encode_fast(const float * qL, const float * qR, float a, float * f, float * scal
   const float b2L = a * a + qL[5] * qL[5] + qL[6] * qL[6];
   const float b2R = a * a + qR[5] * qR[5] + qR[6] * qR[6];
   const float Ps = 0.5f * (qL[4] + qR[4]) + 0.25f * (b2L + b2R);
-  const float irs = __frcp_rn(rs), iPs = __frcp_rn(Ps);
+  const float irs = rcp(rs), iPs = rcp(Ps);
   const float ibs = rsqrtf(Ps), bs = Ps * ibs;
   const float ivs = rs * rsqrtf(rs) * ibs, vs = Ps * ivs * irs; // sqrt(rs / Ps), sqrt(Ps / rs)
   f[0] = 0.5f * (qL[1] + qR[1]) * ivs;
@@ -134,7 +134,7 @@ encode_fast(const float * qL, const float * qR, float a, float * f, float * scal
   for (int q = 0; q < 7; ++q)
     J = fmaxf(J, fabsf(h[q]));
   const float sJ = fmaxf(J, float(mlp::kJFloor));
-  const float isJ = __frcp_rn(sJ);
+  const float isJ = rcp(sJ);
 #pragma unroll
   for (int q = 0; q < 7; ++q)
     f[7 + q] = h[q] * isJ;
@@ -207,7 +207,7 @@ flux_face_mlp(const Grid<float> & G, const Buffers<float> & B, const SurrogateDe
     const float smallR = G.smallr, smallp = G.smallp;
     smooth = J <= S.tau && l7[0] > smallR && r7[0] > smallR && l7[4] > smallp * l7[0] &&
              r7[4] > smallp * r7[0];
-    central_flux_fast(l7, r7, a, __frcp_rn(G.gamma0 - 1.f), Fc);
+    central_flux_fast(l7, r7, a, rcp(G.gamma0 - 1.f), Fc);
 #pragma unroll
     for (int q = 0; q < 7; ++q)
     {

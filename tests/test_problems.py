@@ -104,3 +104,21 @@ def test_linear_wave_convergence(mhdlib, wave_type, tend):
     orders = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
     print(f"\nwave type {wave_type}: L1 errors {errs}, orders {orders}")
     assert np.all(orders > 1.0), (errs, orders)
+
+
+@pytest.mark.gpu
+def test_non_finite_reference_state_is_reported(mhdlib, oracle):
+    """The reference's 3D rotor at 12x12x6 turns NaN from its third step
+    (the oracle, bitwise the reference, shows it); the library stops with
+    MHD_ERR_NUMERIC instead of carrying NaN on."""
+    z = load("rotor3d")
+    ini = str(z["ini"])
+    o = oracle.OracleSolver(ini)
+    o.set_state(z["U0"])
+    o.run(4)
+    assert np.isnan(o.get_state()).any()
+    s = mhdlib.MHDSolver.from_ini(ini, fp_mode=mhdlib.MHD_FP_EXACT)
+    s.init_problem()
+    with pytest.raises(mhdlib.MHDError) as e:
+        s.run(4)
+    assert e.value.code == mhdlib.MHD_ERR_NUMERIC
