@@ -318,7 +318,9 @@ def run_gb300(args):
             ms32 = s32.run_timed(args.steps)
             v = {"value": interior_cells * args.steps / (ms32 / 1e3),
                  "ms_per_step": ms32 / args.steps, "dtype": "f32",
-                 "rel_l1_vs_fp64": float((err / den).max()), "accuracy_steps": acc_steps,
+                 "rel_l1_vs_fp64": float((err / den).max()),
+                 "rel_l1_vs_fp64_per_variable": [float(x) for x in err / den],
+                 "accuracy_steps": acc_steps,
                  "note": "FP32 storage and arithmetic, FP64 dt/sums/div B"}
             if use_mlp:
                 used, total = s32.surrogate_stats()

@@ -270,15 +270,18 @@ int mhd_checkpoint_load(mhd_ctx *ctx, const char *path, int reset_time, int *tim
  * RiemannSolvers_MHD.h:133-367, at the call site of
  * ComputeFluxAndUpdateAlongDirFunctor, MHDRunFunctors{2D,3D}.h).
  *
- * A 15-64-64-7 perceptron (GELU, BF16 weights, FP32 accumulation) predicts
+ * A 27-64-64-19 perceptron (GELU, BF16 weights, FP32 accumulation) predicts
  * the upwind dissipation D = (F(qL) + F(qR))/2 - F_HLLD of a face in the
- * face's own dimensionless units; it is used on faces whose largest
+ * face's own dimensionless units, odd in each transverse direction by
+ * construction (reflection-invariant inputs; the odd components are the
+ * network's coefficients times odd bases); it is used on faces whose largest
  * normalised half-jump J is at most tau, whose reconstructed density and
  * pressure are above their floors and whose prediction is finite and
  * bounded; every other face gets HLLD.  Training runs on the GPU with the
  * library's own forward/backward kernels.
  */
-#define MHD_MLP_PARAMS 5768      /* W1[16][64] b1[64] W2[64][64] b2[64] W3[64][8] b3[8] */
+#define MHD_MLP_PARAMS 7832      /* W1[32][64] b1[64] W2[64][64] b2[64] W3[64][24] b3[24] */
+#define MHD_MLP_FEATURES 40      /* per face: 32 network inputs, then the 8 odd bases */
 #define MHD_SAMPLE_FLOATS 24     /* one harvested face record, see mhd_harvest_faces */
 #define MHD_MLP_TRAIN 0          /* BF16 weights/activations, hardware tanh (deployed numerics) */
 #define MHD_MLP_CHECK 1          /* plain FP32, tanhf: for gradient checks */
@@ -302,7 +305,8 @@ int mhd_mlp_set_params(mhd_mlp *mlp, const float *params, int n);
 int mhd_mlp_get_params(mhd_mlp *mlp, float *params, int n);
 int mhd_mlp_gamma(mhd_mlp *mlp, double *gamma0);
 
-/* Records -> features[n][16] and targets[n][8] (D / scale, FP64 on the GPU). */
+/* Records -> features[n][MHD_MLP_FEATURES] and targets[n][8] (D / scale:
+ * rho, E, mn, mt1, mt2, Bt1, Bt2, pad; FP64 on the GPU). */
 int mhd_mlp_encode(mhd_mlp *mlp, const float *records, int64_t n, float *features,
                    float *targets);
 
@@ -318,7 +322,8 @@ int mhd_mlp_gradient(mhd_mlp *mlp, const float *features, const float *targets, 
 int mhd_mlp_train(mhd_mlp *mlp, const float *records, int64_t n, int epochs, int batch,
                   float lr, float weight_power, uint64_t seed, float *loss_history);
 
-/* The deployed tensor-core forward pass on features[n][16] -> out[n][8]. */
+/* The deployed tensor-core forward pass on features[n][MHD_MLP_FEATURES]
+ * -> out[n][8] (the 7 dimensionless dissipation components and a pad). */
 int mhd_mlp_forward(mhd_mlp *mlp, const float *features, int64_t n, float *out);
 const char *mhd_mlp_last_error(mhd_mlp *mlp);
 

@@ -3,24 +3,27 @@
  *
  * Restates, in double precision, what ppkmhd_gb300/csrc/mhd_mlp.cuh and
  * mhd_mlp.cu compute on the GPU: the dimensionless face encoding, the
- * central flux, the 15-64-64-7 GELU perceptron (tanh form of Hendrycks and
- * Gimpel, 2016) with optional emulation of the deployed BF16 rounding of
- * weights, inputs and hidden activations, and the mean-squared-error loss
- * with its gradient by back-propagation.  The physical flux follows the flux
+ * central flux, the 27-64-64-19 GELU perceptron (tanh form of Hendrycks and
+ * Gimpel, 2016) whose odd transverse flux components are its coefficients
+ * times the odd bases, with optional emulation of the deployed BF16
+ * rounding of weights, inputs and hidden activations, and the
+ * mean-squared-error loss with its gradient by back-propagation.  The physical flux follows the flux
  * vector of riemann_hlld (RiemannSolvers_MHD.h:358-366).  The gradient is
  * checked against central finite differences in the tests, so this file is
  * pinned independently of the GPU code.
  *
- * Parameter vector: W1[16][64] b1[64] W2[64][64] b2[64] W3[64][8] b3[8].
+ * Parameter vector: W1[32][64] b1[64] W2[64][64] b2[64] W3[64][24] b3[24].
+ * Features of a face: 32 network inputs, then the 8 odd bases u1[4], u2[4].
  */
 #include <math.h>
 #include <stdint.h>
 #include <string.h>
 
-#define NIN 16
+#define NIN 32
 #define NH 64
-#define NOUT 8
+#define NOUT 24
 #define NUSED 7
+#define NFEAT 40
 #define OFF_W1 0
 #define OFF_B1 (OFF_W1 + NIN * NH)
 #define OFF_W2 (OFF_B1 + NH)
@@ -61,7 +64,8 @@ mlp_bf16(double x)
   return bf16(x);
 }
 
-/* q = rho, vn, vt1, vt2, p, Bt1, Bt2; returns J */
+/* q = rho, vn, vt1, vt2, p, Bt1, Bt2; f[NFEAT] = inputs, then odd bases;
+ * returns J */
 double
 mlp_encode(const double * qL, const double * qR, double a, double * f, double * scale)
 {
@@ -71,14 +75,7 @@ mlp_encode(const double * qL, const double * qR, double a, double * f, double * 
   const double Ps = 0.5 * (qL[4] + qR[4]) + 0.25 * (b2L + b2R);
   const double vs = sqrt(Ps / rs), bs = sqrt(Ps);
   const double div[7] = { rs, vs, vs, vs, Ps, bs, bs };
-  f[0] = 0.5 * (qL[1] + qR[1]) / vs;
-  f[1] = 0.5 * (qL[2] + qR[2]) / vs;
-  f[2] = 0.5 * (qL[3] + qR[3]) / vs;
-  f[3] = 0.5 * (qL[4] + qR[4]) / Ps;
-  f[4] = 0.5 * (qL[5] + qR[5]) / bs;
-  f[5] = 0.5 * (qL[6] + qR[6]) / bs;
-  f[6] = a / bs;
-  double h[7], J = 0.0;
+  double       h[7], J = 0.0;
   for (int q = 0; q < 7; ++q)
   {
     h[q] = 0.5 * (qR[q] - qL[q]) / div[q];
@@ -86,15 +83,51 @@ mlp_encode(const double * qL, const double * qR, double a, double * f, double * 
       J = fabs(h[q]);
   }
   const double sJ = J > J_FLOOR ? J : J_FLOOR;
-  for (int q = 0; q < 7; ++q)
-    f[7 + q] = h[q] / sJ;
-  f[14] = sJ / TAU_REF;
-  f[15] = 0.0;
+  f[0] = 0.5 * (qL[1] + qR[1]) / vs;
+  f[1] = 0.5 * (qL[4] + qR[4]) / Ps;
+  f[2] = a / bs;
+  f[3] = h[0] / sJ;
+  f[4] = h[1] / sJ;
+  f[5] = h[4] / sJ;
+  f[6] = sJ / TAU_REF;
+  double * u1 = f + NIN;
+  double * u2 = f + NIN + 4;
+  u1[0] = 0.5 * (qL[2] + qR[2]) / vs;
+  u1[1] = 0.5 * (qL[5] + qR[5]) / bs;
+  u1[2] = h[2] / sJ;
+  u1[3] = h[5] / sJ;
+  u2[0] = 0.5 * (qL[3] + qR[3]) / vs;
+  u2[1] = 0.5 * (qL[6] + qR[6]) / bs;
+  u2[2] = h[3] / sJ;
+  u2[3] = h[6] / sJ;
+  int o = 7;
+  for (int i = 0; i < 4; ++i)
+    for (int j = i; j < 4; ++j)
+      f[o++] = u1[i] * u1[j];
+  for (int i = 0; i < 4; ++i)
+    for (int j = i; j < 4; ++j)
+      f[o++] = u2[i] * u2[j];
+  for (; o < NIN; ++o)
+    f[o] = 0.0;
   scale[0] = rs * vs * sJ;
   scale[1] = Ps * vs * sJ;
   scale[2] = scale[3] = scale[4] = Ps * sJ;
   scale[5] = scale[6] = bs * vs * sJ;
   return J;
+}
+
+/* raw outputs y[NOUT] and bases u[8] -> dissipation D[7] */
+static void
+combine(const double * y, const double * u, double * D)
+{
+  const double *u1 = u, *u2 = u + 4;
+  D[0] = y[0];
+  D[1] = y[1];
+  D[2] = y[2];
+  D[3] = y[3] * u1[0] + y[4] * u1[1] + y[5] * u1[2] + y[6] * u1[3];
+  D[5] = y[7] * u1[0] + y[8] * u1[1] + y[9] * u1[2] + y[10] * u1[3];
+  D[4] = y[11] * u2[0] + y[12] * u2[1] + y[13] * u2[2] + y[14] * u2[3];
+  D[6] = y[15] * u2[0] + y[16] * u2[1] + y[17] * u2[2] + y[18] * u2[3];
 }
 
 static void
@@ -153,9 +186,9 @@ gelu_grad(double x)
  * to BF16 (biases stay exact) and the activation is the BF16 evaluation of
  * GELU, as deployed. */
 void
-mlp_forward(const double * P, const double * x_in, double * y, int rounding)
+mlp_forward(const double * P, const double * x_in, double * D, int rounding)
 {
-  double x[NIN], h1[NH], h2[NH];
+  double x[NIN], h1[NH], h2[NH], y[NOUT];
 #define W(off, idx) (rounding ? bf16(P[(off) + (idx)]) : P[(off) + (idx)])
   for (int i = 0; i < NIN; ++i)
     x[i] = rounding ? bf16(x_in[i]) : x_in[i];
@@ -181,6 +214,8 @@ mlp_forward(const double * P, const double * x_in, double * y, int rounding)
     y[o] = z;
   }
 #undef W
+  combine(y, x_in + NIN, D);
+  D[7] = 0.0;
 }
 
 void
@@ -188,7 +223,7 @@ mlp_forward_batch(const double * P, const double * X, long n, double * Y, int ro
 {
 #pragma omp parallel for schedule(static)
   for (long s = 0; s < n; ++s)
-    mlp_forward(P, X + s * NIN, Y + s * NOUT, rounding);
+    mlp_forward(P, X + s * NFEAT, Y + s * 8, rounding);
 }
 
 /* Mean squared error over n samples and the 7 used outputs (no rounding),
@@ -201,9 +236,12 @@ mlp_loss_grad(const double * P, const double * X, const double * T, long n, doub
   double       loss = 0.0;
   for (long s = 0; s < n; ++s)
   {
-    const double * x = X + s * NIN;
-    const double * t = T + s * NOUT;
-    double         z1[NH], h1[NH], z2[NH], h2[NH], dy[NOUT], dz2[NH], dz1[NH];
+    const double * x = X + s * NFEAT;
+    const double * t = T + s * 8;
+    const double * u1 = x + NIN;
+    const double * u2 = x + NIN + 4;
+    double         z1[NH], h1[NH], z2[NH], h2[NH], y[NOUT], D[NUSED], dD[NUSED], dy[NOUT];
+    double         dz2[NH], dz1[NH];
     for (int k = 0; k < NH; ++k)
     {
       double z = P[OFF_B1 + k];
@@ -225,9 +263,26 @@ mlp_loss_grad(const double * P, const double * X, const double * T, long n, doub
       double z = P[OFF_B3 + o];
       for (int j = 0; j < NH; ++j)
         z += h2[j] * P[OFF_W3 + j * NOUT + o];
-      const double e = o < NUSED ? z - t[o] : 0.0;
+      y[o] = z;
+    }
+    combine(y, x + NIN, D);
+    for (int c = 0; c < NUSED; ++c)
+    {
+      const double e = D[c] - t[c];
       loss += e * e;
-      dy[o] = 2.0 * e * norm;
+      dD[c] = 2.0 * e * norm;
+    }
+    for (int o = 0; o < NOUT; ++o)
+      dy[o] = 0.0;
+    dy[0] = dD[0];
+    dy[1] = dD[1];
+    dy[2] = dD[2];
+    for (int k = 0; k < 4; ++k)
+    {
+      dy[3 + k] = dD[3] * u1[k];
+      dy[7 + k] = dD[5] * u1[k];
+      dy[11 + k] = dD[4] * u2[k];
+      dy[15 + k] = dD[6] * u2[k];
     }
     for (int j = 0; j < NH; ++j)
     {

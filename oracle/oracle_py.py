@@ -168,14 +168,15 @@ def compute_emf(p: OrcParams, emf_dir: int, q_edge) -> float:
 
 # ---------------------------------------------------------------- flux surrogate
 
-MLP_NPARAM = 5768
+MLP_NPARAM = 7832
+MLP_NFEAT = 40
 
 
 def mlp_encode(qL, qR, a: float):
-    """(features[16], scale[7], J) of one face (mlp_oracle.c)."""
+    """(features[40], scale[7], J) of one face (mlp_oracle.c)."""
     l = np.ascontiguousarray(qL, dtype=np.float64)
     r = np.ascontiguousarray(qR, dtype=np.float64)
-    f = np.zeros(16)
+    f = np.zeros(MLP_NFEAT)
     sc = np.zeros(7)
     J = lib().mlp_encode(_ptr(l), _ptr(r), float(a), _ptr(f), _ptr(sc))
     return f, sc, J

@@ -40,7 +40,8 @@ MHD_LAYOUT_LEFT, MHD_LAYOUT_RIGHT = 0, 1
 MHD_PROBLEM_ORSZAG_TANG = 0
 (MHD_PROBLEM_BLAST, MHD_PROBLEM_IMPLODE, MHD_PROBLEM_KELVIN_HELMHOLTZ, MHD_PROBLEM_ROTOR,
  MHD_PROBLEM_FIELD_LOOP, MHD_PROBLEM_WAVE) = range(1, 7)
-MHD_MLP_PARAMS = 5768
+MHD_MLP_PARAMS = 7832
+MHD_MLP_FEATURES = 40
 MHD_SAMPLE_FLOATS = 24
 MHD_MLP_TRAIN, MHD_MLP_CHECK = 0, 1
 

@@ -72,7 +72,7 @@ EnsembleCore * create_ensemble_f32(const mhd_params * p, int n, std::string & er
 
 // Flux surrogate helpers (mhd_mlp.cu): packed weights + biases for the
 // flux stage (kMlpPackTotal words), the network's gamma0 and parameters.
-constexpr int kMlpPackTotal = 2816 + 136;
+constexpr int kMlpPackTotal = 3840 + 152;
 void          mlp_pack(const float * params, uint32_t * out);
 double        mlp_gamma(const mhd_mlp * m);
 const float * mlp_params(const mhd_mlp * m);

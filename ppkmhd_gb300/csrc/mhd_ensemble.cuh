@@ -35,27 +35,51 @@ struct BlockRef
   int p, b;
 };
 
+// The grid and buffers of the block's problem, copied into shared memory
+// by the block (the bodies then read them like kernel parameters), with the
+// state arrays swapped for odd parities.
 template <class R>
-__device__ __forceinline__ Buffers<R>
-buffers_of(const Buffers<R> * Bs, int p, int parity)
+struct ProblemView
 {
-  Buffers<R> B = Bs[p];
-  if (parity)
+  Grid<R>    G;
+  Buffers<R> B;
+};
+
+template <class R>
+__device__ __forceinline__ void
+load_problem(ProblemView<R> & v, const Grid<R> * Gs, const Buffers<R> * Bs, int p, int parity)
+{
+  static_assert(sizeof(Grid<R>) % 4 == 0 && sizeof(Buffers<R>) % 4 == 0, "word copies");
+  const int nG = (int)(sizeof(Grid<R>) / 4), nB = (int)(sizeof(Buffers<R>) / 4);
+  const unsigned * gsrc = reinterpret_cast<const unsigned *>(Gs + p);
+  const unsigned * bsrc = reinterpret_cast<const unsigned *>(Bs + p);
+  unsigned *       gdst = reinterpret_cast<unsigned *>(&v.G);
+  unsigned *       bdst = reinterpret_cast<unsigned *>(&v.B);
+  for (int q = threadIdx.x; q < nG + nB; q += blockDim.x)
   {
-    R * t = B.Uin;
-    B.Uin = B.Uout;
-    B.Uout = t;
+    if (q < nG)
+      gdst[q] = gsrc[q];
+    else
+      bdst[q - nG] = bsrc[q - nG];
   }
-  return B;
+  __syncthreads();
+  if (parity && threadIdx.x == 0)
+  {
+    R * t = v.B.Uin;
+    v.B.Uin = v.B.Uout;
+    v.B.Uout = t;
+  }
+  __syncthreads();
 }
 
 template <class R, int DIM>
 __global__ void __launch_bounds__(256)
 kb_boundaries(const Grid<R> * Gs, const Buffers<R> * Bs, const BlockRef * map, int parity)
 {
-  const BlockRef   m = map[blockIdx.x];
-  const Buffers<R> B = buffers_of(Bs, m.p, parity);
-  boundaries_body<R, DIM>(Gs[m.p], B.Uin, B.st, 0, m.b * (int64_t)blockDim.x + threadIdx.x,
+  __shared__ ProblemView<R> v;
+  const BlockRef            m = map[blockIdx.x];
+  load_problem(v, Gs, Bs, m.p, parity);
+  boundaries_body<R, DIM>(v.G, v.B.Uin, v.B.st, 0, m.b * (int64_t)blockDim.x + threadIdx.x,
                           m.b == 0 && threadIdx.x == 0);
 }
 
@@ -63,9 +87,10 @@ template <class R, int DIM>
 __global__ void __launch_bounds__(256)
 kb_prim_dt(const Grid<R> * Gs, const Buffers<R> * Bs, const BlockRef * map, int parity)
 {
-  const BlockRef   m = map[blockIdx.x];
-  const Buffers<R> B = buffers_of(Bs, m.p, parity);
-  prim_dt_body<R, DIM>(Gs[m.p], B.Uin, B.Q, B.st, 0, m.b * (int64_t)blockDim.x + threadIdx.x);
+  __shared__ ProblemView<R> v;
+  const BlockRef            m = map[blockIdx.x];
+  load_problem(v, Gs, Bs, m.p, parity);
+  prim_dt_body<R, DIM>(v.G, v.B.Uin, v.B.Q, v.B.st, 0, m.b * (int64_t)blockDim.x + threadIdx.x);
 }
 
 template <class R>
@@ -95,34 +120,40 @@ template <class R, int DIM>
 __global__ void __launch_bounds__(256)
 kb_trace(const Grid<R> * Gs, const Buffers<R> * Bs, const BlockRef * map, int parity)
 {
-  const BlockRef m = map[blockIdx.x];
-  trace_body<R, DIM>(Gs[m.p], buffers_of(Bs, m.p, parity), m.b * (int64_t)blockDim.x + threadIdx.x);
+  __shared__ ProblemView<R> v;
+  const BlockRef            m = map[blockIdx.x];
+  load_problem(v, Gs, Bs, m.p, parity);
+  trace_body<R, DIM>(v.G, v.B, m.b * (int64_t)blockDim.x + threadIdx.x);
 }
 
 template <class R, int DIM>
 __global__ void __launch_bounds__(256)
 kb_flux(const Grid<R> * Gs, const Buffers<R> * Bs, const BlockRef * map, int parity)
 {
-  const BlockRef m = map[blockIdx.x];
-  flux_body<R, DIM>(Gs[m.p], buffers_of(Bs, m.p, parity), m.b * (int64_t)blockDim.x + threadIdx.x,
-                    blockIdx.y);
+  __shared__ ProblemView<R> v;
+  const BlockRef            m = map[blockIdx.x];
+  load_problem(v, Gs, Bs, m.p, parity);
+  flux_body<R, DIM>(v.G, v.B, m.b * (int64_t)blockDim.x + threadIdx.x, blockIdx.y);
 }
 
 template <class R, int DIM>
 __global__ void __launch_bounds__(256)
 kb_emf(const Grid<R> * Gs, const Buffers<R> * Bs, const BlockRef * map, int parity)
 {
-  const BlockRef m = map[blockIdx.x];
-  emf_body<R, DIM>(Gs[m.p], buffers_of(Bs, m.p, parity), m.b * (int64_t)blockDim.x + threadIdx.x,
-                   blockIdx.y);
+  __shared__ ProblemView<R> v;
+  const BlockRef            m = map[blockIdx.x];
+  load_problem(v, Gs, Bs, m.p, parity);
+  emf_body<R, DIM>(v.G, v.B, m.b * (int64_t)blockDim.x + threadIdx.x, blockIdx.y);
 }
 
 template <class R, int DIM>
 __global__ void __launch_bounds__(256)
 kb_update(const Grid<R> * Gs, const Buffers<R> * Bs, const BlockRef * map, int parity)
 {
-  const BlockRef m = map[blockIdx.x];
-  update_body<R, DIM>(Gs[m.p], buffers_of(Bs, m.p, parity), m.b * (int64_t)blockDim.x + threadIdx.x);
+  __shared__ ProblemView<R> v;
+  const BlockRef            m = map[blockIdx.x];
+  load_problem(v, Gs, Bs, m.p, parity);
+  update_body<R, DIM>(v.G, v.B, m.b * (int64_t)blockDim.x + threadIdx.x);
 }
 
 #define MHD_ECK(call)                                                                 \

@@ -27,6 +27,7 @@ using namespace mhd::mlp;
 static_assert(mhd::kMlpPackTotal == kPackWords + kBiasFloats, "packed surrogate size");
 static_assert(kParams == MHD_MLP_PARAMS, "surrogate parameter count");
 static_assert(kRecord == MHD_SAMPLE_FLOATS, "face record size");
+static_assert(kFeat == MHD_MLP_FEATURES, "face feature count");
 
 struct mhd_mlp
 {
@@ -44,10 +45,17 @@ struct mhd_mlp
 namespace
 {
 
-constexpr int kTB = 64;                                  // samples per training block
-constexpr int kRowX = 0, kRowZ1 = 16, kRowH1 = 80, kRowZ2 = 144, kRowH2 = 208, kRowY = 272;
-constexpr int kRowLoss = 280;
-constexpr int kRowStride = 281;                           // odd: conflict-free columns
+constexpr int kTB = 64; // samples per training block
+constexpr int kTgt = 8; // target / prediction stride: 7 flux components + pad
+constexpr int kRowX = 0;                      // inputs [kIn]
+constexpr int kRowZ1 = kRowX + kIn;           // layer-1 pre-activations, then their gradient
+constexpr int kRowH1 = kRowZ1 + kHid;         // layer-1 activations
+constexpr int kRowZ2 = kRowH1 + kHid;         // layer-2 pre-activations, then their gradient
+constexpr int kRowH2 = kRowZ2 + kHid;         // layer-2 activations
+constexpr int kRowU = kRowH2 + kHid;          // odd bases [kBasis]
+constexpr int kRowY = kRowU + kBasis;         // gradient of the raw outputs [kOut]
+constexpr int kRowLoss = kRowY + kOut;
+constexpr int kRowStride = kRowLoss + 1;      // 321, odd: conflict-free columns
 constexpr int kSmemTrain = (kParams + kTB * kRowStride) * (int)sizeof(float);
 
 __device__ __forceinline__ float
@@ -71,7 +79,8 @@ gelu_grad(float x, int train)
   return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * kGeluC0 * (1.0f + 3.0f * kGeluC1 * x * x);
 }
 
-// Records -> features (16) and targets D / scale (8), in FP64.
+// Records -> features (kFeat: inputs and odd bases) and targets D / scale
+// (8: 7 components + pad), in FP64.
 __global__ void
 k_encode(const float * __restrict__ rec, int64_t n, float * __restrict__ feat,
          float * __restrict__ tgt)
@@ -80,18 +89,18 @@ k_encode(const float * __restrict__ rec, int64_t n, float * __restrict__ feat,
   if (s >= n)
     return;
   const float * r = rec + s * kRecord;
-  double        l7[7], r7[7], f[kIn], sc[7];
+  double        l7[7], r7[7], f[kFeat], sc[7];
   for (int q = 0; q < 7; ++q)
   {
     l7[q] = r[kRecQL + q];
     r7[q] = r[kRecQR + q];
   }
   encode(l7, r7, (double)r[kRecA], f, sc);
-  for (int q = 0; q < kIn; ++q)
-    feat[s * kIn + q] = (float)f[q];
+  for (int q = 0; q < kFeat; ++q)
+    feat[s * kFeat + q] = (float)f[q];
   for (int q = 0; q < 7; ++q)
-    tgt[s * kOut + q] = (float)((double)r[kRecD + q] / sc[q]);
-  tgt[s * kOut + 7] = 0.f;
+    tgt[s * kTgt + q] = (float)((double)r[kRecD + q] / sc[q]);
+  tgt[s * kTgt + 7] = 0.f;
 }
 
 // Forward + backward of kTB samples per block; writes the block's summed
@@ -119,9 +128,11 @@ k_fwd_bwd(const float * __restrict__ W, const float * __restrict__ feat,
   const int64_t src = active ? (idx ? (int64_t)idx[slot] : slot) : 0;
   for (int q = 0; q < kIn; ++q)
   {
-    const float x = active ? feat[src * kIn + q] : 0.f;
+    const float x = active ? feat[src * kFeat + q] : 0.f;
     row[kRowX + q] = train ? bf16_round(x) : x;
   }
+  for (int q = 0; q < kBasis; ++q)
+    row[kRowU + q] = active ? feat[src * kFeat + kIn + q] : 0.f;
   __syncthreads();
   // layer 1
   for (int k = 0; k < kHid; ++k)
@@ -141,18 +152,41 @@ k_fwd_bwd(const float * __restrict__ W, const float * __restrict__ feat,
     row[kRowZ2 + k] = acc;
     row[kRowH2 + k] = train ? gelu_bf16(acc) : gelu_exact(acc);
   }
-  // layer 3 + loss gradient; sample weight (sJ / kTauRef)^wpow emphasises
-  // the faces with larger jumps, whose dissipation is larger in physical units
-  const float sw = wpow != 0.f ? powf(fmaxf(row[kRowX + 14], 1e-3f), wpow) : 1.f;
-  float       loss = 0.f;
+  // layer 3, basis combination and loss gradient; sample weight
+  // (sJ / kTauRef)^wpow emphasises the faces with larger jumps, whose
+  // dissipation is larger in physical units
+  const float sw = wpow != 0.f ? powf(fmaxf(row[kRowX + 6], 1e-3f), wpow) : 1.f;
+  float       y[kOut], Dn[kOutUsed];
   for (int o = 0; o < kOut; ++o)
   {
     float acc = w[kOffB3 + o];
     for (int j = 0; j < kHid; ++j)
       acc = fmaf(row[kRowH2 + j], w[kOffW3 + j * kOut + o], acc);
-    const float e = (active && o < kOutUsed) ? acc - tgt[src * kOut + o] : 0.f;
+    y[o] = acc;
+  }
+  combine(y, row + kRowU, Dn);
+  float loss = 0.f, dD[kOutUsed];
+  for (int c = 0; c < kOutUsed; ++c)
+  {
+    const float e = active ? Dn[c] - tgt[src * kTgt + c] : 0.f;
     loss = fmaf(sw * e, e, loss);
-    row[kRowY + o] = 2.f * sw * e * norm;
+    dD[c] = 2.f * sw * e * norm;
+  }
+  // d(loss)/d(raw outputs): the transpose of combine
+  const float * u1 = row + kRowU;
+  const float * u2 = row + kRowU + 4;
+  float *       dy = row + kRowY;
+  for (int o = 0; o < kOut; ++o)
+    dy[o] = 0.f;
+  dy[0] = dD[0];
+  dy[1] = dD[1];
+  dy[2] = dD[2];
+  for (int k = 0; k < 4; ++k)
+  {
+    dy[3 + k] = dD[3] * u1[k];
+    dy[7 + k] = dD[5] * u1[k];
+    dy[11 + k] = dD[4] * u2[k];
+    dy[15 + k] = dD[6] * u2[k];
   }
   row[kRowLoss] = loss;
   // back through layer 3 and 2: dz2 overwrites z2, dz1 overwrites z1
@@ -283,14 +317,20 @@ k_forward_mma(const uint32_t * __restrict__ pack, const float * __restrict__ fea
     sb[q] = reinterpret_cast<const float *>(pack + kPackWords)[q];
   __syncthreads();
   const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  float         f[kIn], y[kOut];
+  float         f[kIn], u[kBasis], y[kOut], Dn[kOutUsed];
   for (int q = 0; q < kIn; ++q)
-    f[q] = s < n ? feat[s * kIn + q] : 0.f;
+    f[q] = s < n ? feat[s * kFeat + q] : 0.f;
+  for (int q = 0; q < kBasis; ++q)
+    u[q] = s < n ? feat[s * kFeat + kIn + q] : 0.f;
   const int warp = threadIdx.x >> 5;
   warp_forward(sw, sb, sx[warp], so[warp], f, y);
   if (s < n)
-    for (int o = 0; o < kOut; ++o)
-      out[s * kOut + o] = y[o];
+  {
+    combine(y, u, Dn);
+    for (int c = 0; c < kOutUsed; ++c)
+      out[s * kTgt + c] = Dn[c];
+    out[s * kTgt + 7] = 0.f;
+  }
 }
 
 // ---------------------------------------------------------------- host
@@ -390,8 +430,8 @@ encode_on_device(mhd_mlp * m, const float * records, int64_t n, DevBuf<float> & 
 {
   DevBuf<float> rec;
   MLP_CK(rec.alloc((size_t)n * kRecord));
-  MLP_CK(feat.alloc((size_t)n * kIn));
-  MLP_CK(tgt.alloc((size_t)n * kOut));
+  MLP_CK(feat.alloc((size_t)n * kFeat));
+  MLP_CK(tgt.alloc((size_t)n * kTgt));
   MLP_CK(cudaMemcpyAsync(rec.p, records, (size_t)n * kRecord * sizeof(float), cudaMemcpyHostToDevice,
                          m->stream));
   k_encode<<<(unsigned)((n + 127) / 128), 128, 0, m->stream>>>(rec.p, n, feat.p, tgt.p);
@@ -478,9 +518,9 @@ extern "C"
           m->params[off + i * fan_out + o] = (i < used_in && o < used_out) ? (float)r : 0.f;
         }
     };
-    init(kOffW1, kIn, kHid, 15, kHid);
+    init(kOffW1, kIn, kHid, kInUsed, kHid);
     init(kOffW2, kHid, kHid, kHid, kHid);
-    init(kOffW3, kHid, kOut, kHid, kOutUsed);
+    init(kOffW3, kHid, kOut, kHid, kRawUsed);
     return upload_params(m);
   }
 
@@ -552,8 +592,8 @@ extern "C"
     DevBuf<float> feat, tgt;
     if (int rc = encode_on_device(m, records, n, feat, tgt))
       return rc;
-    MLP_CK(cudaMemcpy(features, feat.p, (size_t)n * kIn * sizeof(float), cudaMemcpyDeviceToHost));
-    MLP_CK(cudaMemcpy(targets, tgt.p, (size_t)n * kOut * sizeof(float), cudaMemcpyDeviceToHost));
+    MLP_CK(cudaMemcpy(features, feat.p, (size_t)n * kFeat * sizeof(float), cudaMemcpyDeviceToHost));
+    MLP_CK(cudaMemcpy(targets, tgt.p, (size_t)n * kTgt * sizeof(float), cudaMemcpyDeviceToHost));
     return MHD_OK;
   }
 
@@ -570,13 +610,13 @@ extern "C"
     DevBuf<float> feat, tgt, partial, g;
     DevBuf<double> l;
     const int     nb = (int)((n + kTB - 1) / kTB);
-    MLP_CK(feat.alloc((size_t)n * kIn));
-    MLP_CK(tgt.alloc((size_t)n * kOut));
+    MLP_CK(feat.alloc((size_t)n * kFeat));
+    MLP_CK(tgt.alloc((size_t)n * kTgt));
     MLP_CK(partial.alloc((size_t)nb * (kParams + 1)));
     MLP_CK(g.alloc(kParams));
     MLP_CK(l.alloc(1));
-    MLP_CK(cudaMemcpy(feat.p, features, (size_t)n * kIn * sizeof(float), cudaMemcpyHostToDevice));
-    MLP_CK(cudaMemcpy(tgt.p, targets, (size_t)n * kOut * sizeof(float), cudaMemcpyHostToDevice));
+    MLP_CK(cudaMemcpy(feat.p, features, (size_t)n * kFeat * sizeof(float), cudaMemcpyHostToDevice));
+    MLP_CK(cudaMemcpy(tgt.p, targets, (size_t)n * kTgt * sizeof(float), cudaMemcpyHostToDevice));
     const float norm = (float)(1.0 / ((double)n * kOutUsed));
     k_fwd_bwd<<<nb, kTB, kSmemTrain, m->stream>>>(m->d_params, feat.p, tgt.p, nullptr, 0, n, norm,
                                                   mode == MHD_MLP_TRAIN, 0.f, partial.p);
@@ -669,14 +709,14 @@ extern "C"
     DevBuf<uint32_t> dp;
     DevBuf<float>    feat, o;
     MLP_CK(dp.alloc(pack.size()));
-    MLP_CK(feat.alloc((size_t)n * kIn));
-    MLP_CK(o.alloc((size_t)n * kOut));
+    MLP_CK(feat.alloc((size_t)n * kFeat));
+    MLP_CK(o.alloc((size_t)n * kTgt));
     MLP_CK(cudaMemcpy(dp.p, pack.data(), pack.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
-    MLP_CK(cudaMemcpy(feat.p, features, (size_t)n * kIn * sizeof(float), cudaMemcpyHostToDevice));
+    MLP_CK(cudaMemcpy(feat.p, features, (size_t)n * kFeat * sizeof(float), cudaMemcpyHostToDevice));
     k_forward_mma<<<(unsigned)((n + 127) / 128), 128, 0, m->stream>>>(dp.p, feat.p, n, o.p);
     MLP_CK(cudaGetLastError());
     MLP_CK(cudaStreamSynchronize(m->stream));
-    MLP_CK(cudaMemcpy(out, o.p, (size_t)n * kOut * sizeof(float), cudaMemcpyDeviceToHost));
+    MLP_CK(cudaMemcpy(out, o.p, (size_t)n * kTgt * sizeof(float), cudaMemcpyDeviceToHost));
     return MHD_OK;
   }
 

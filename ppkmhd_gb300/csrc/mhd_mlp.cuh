@@ -1,4 +1,4 @@
-// The HLLD flux surrogate: a 15-64-64-7 multilayer perceptron with GELU
+// The HLLD flux surrogate: a 27-64-64-19 multilayer perceptron with GELU
 // activations, BF16 weights and activations and FP32 accumulation.
 //
 // It replaces riemann_hlld (RiemannSolvers_MHD.h:133-367) on faces that a
@@ -7,8 +7,8 @@
 //     Fc = (F(qL) + F(qR)) / 2          (exact, from the physical MHD flux)
 // and the upwind dissipation D = Fc - F_HLLD, and the network predicts D in
 // units of the face's own scales times the jump size:
-//     F = Fc - scale * sJ * net(features).
-// Everything here is dimensionless per face, so one network serves every
+//     F = Fc - scale * sJ * Dn.
+// Everything is dimensionless per face, so one network serves every
 // density, pressure and field level.
 //
 // Per face, in the face-normal frame (a = normal B, q = [rho, vn, vt1, vt2,
@@ -16,18 +16,26 @@
 //   rs = (rhoL + rhoR) / 2
 //   Ps = (pL + pR) / 2 + (|BL|^2 + |BR|^2) / 4       (total-pressure scale)
 //   vs = sqrt(Ps / rs), bs = sqrt(Ps)
-//   mean features  f0..f2 = mean(vn, vt1, vt2) / vs, f3 = mean(p) / Ps,
-//                  f4, f5 = mean(Bt1, Bt2) / bs, f6 = a / bs
-//   half jumps     h = (qR - qL) / 2 over (rs, vs, vs, vs, Ps, bs, bs)
-//   J = max |h|  (the smoothness sensor), sJ = max(J, kJFloor)
-//   f7..f13 = h / sJ, f14 = sJ / kTauRef, f15 = 0 (padding)
+//   means   m = (vn, vt1, vt2) / vs, p / Ps, (Bt1, Bt2) / bs, and a / bs
+//   jumps   h = (qR - qL) / 2 over (rs, vs, vs, vs, Ps, bs, bs)
+//   J = max |h| (the smoothness sensor), sJ = max(J, kJFloor), hn = h / sJ
 //   scale = (rs vs, Ps vs, Ps, Ps, Ps, bs vs, bs vs) for the flux
 //           components (rho, E, mn, mt1, mt2, Bt1, Bt2)
+// The flux is odd in each transverse direction: reflecting t1 (vt1, Bt1 ->
+// -vt1, -Bt1 on both sides) flips the mt1 and Bt1 components and leaves the
+// others.  The network keeps that exactly: its inputs are invariant under
+// both reflections -- the even scalars (mean vn, p, a; jumps of rho, vn, p;
+// sJ / kTauRef) and the 10 pairwise products of each transverse set
+// u1 = (mean vt1, mean Bt1, hn_vt1, hn_Bt1), u2 likewise -- and its 19
+// outputs are the three even components (rho, E, mn) and, for each odd
+// component, 4 coefficients c of its basis: Dn_mt1 = sum_k c_k u1_k, etc.
+// An odd component therefore vanishes with its transverse set, whatever
+// the weights.
 // GELU is the tanh form of Hendrycks and Gimpel (2016):
 //   gelu(x) = x/2 (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))).
 //
 // Parameter vector (FP32 master copy), row = input, column = output unit:
-//   W1[16][64] b1[64] W2[64][64] b2[64] W3[64][8] b3[8]   (5768 floats)
+//   W1[32][64] b1[64] W2[64][64] b2[64] W3[64][24] b3[24]   (7832 floats)
 #pragma once
 
 #include <cstdint>
@@ -40,10 +48,14 @@ namespace mhd
 namespace mlp
 {
 
-constexpr int kIn = 16;  // 15 features + 1 zero pad
+constexpr int kIn = 32;     // 27 invariant inputs + 5 zero pads
+constexpr int kInUsed = 27;
 constexpr int kHid = 64;
-constexpr int kOut = 8;  // 7 flux components + 1 pad
-constexpr int kOutUsed = 7;
+constexpr int kOut = 24;    // 19 raw outputs + 5 pads
+constexpr int kRawUsed = 19;
+constexpr int kOutUsed = 7; // flux components after the basis combination
+constexpr int kBasis = 8;   // u1[4], u2[4]
+constexpr int kFeat = kIn + kBasis; // features of one face: inputs then basis
 
 constexpr int kOffW1 = 0;
 constexpr int kOffB1 = kOffW1 + kIn * kHid;
@@ -51,15 +63,15 @@ constexpr int kOffW2 = kOffB1 + kHid;
 constexpr int kOffB2 = kOffW2 + kHid * kHid;
 constexpr int kOffW3 = kOffB2 + kHid;
 constexpr int kOffB3 = kOffW3 + kHid * kOut;
-constexpr int kParams = kOffB3 + kOut; // 5768
+constexpr int kParams = kOffB3 + kOut; // 7832
 
 // mma.m16n8k16 fragments of the three weight matrices, as bf16x2 words:
 // [k-tile][n-tile][lane][2]
 constexpr int kPackW1 = 0;
 constexpr int kPackW2 = kPackW1 + (kIn / 16) * (kHid / 8) * 64;
 constexpr int kPackW3 = kPackW2 + (kHid / 16) * (kHid / 8) * 64;
-constexpr int kPackWords = kPackW3 + (kHid / 16) * (kOut / 8) * 64; // 2816
-constexpr int kBiasFloats = kHid + kHid + kOut;                    // 136
+constexpr int kPackWords = kPackW3 + (kHid / 16) * (kOut / 8) * 64; // 3840
+constexpr int kBiasFloats = kHid + kHid + kOut;                    // 152
 
 constexpr double kJFloor = 1e-4;
 constexpr double kTauRef = 0.1;
@@ -68,11 +80,12 @@ constexpr double kTauRef = 0.1;
 constexpr int kRecord = 24;
 constexpr int kRecQL = 0, kRecQR = 7, kRecA = 14, kRecJ = 15, kRecD = 16, kRecGamma = 23;
 
-// Dimensionless encoding of one face (see the file comment).  q arrays in
-// the order rho, vn, vt1, vt2, p, Bt1, Bt2.  Returns J.
+// Dimensionless encoding of one face (see the file comment): feat[0..31]
+// the network inputs, feat[32..39] the odd bases u1, u2; scale[7] the flux
+// units.  q arrays in the order rho, vn, vt1, vt2, p, Bt1, Bt2.  Returns J.
 template <class T>
 __host__ __device__ inline T
-encode(const T * qL, const T * qR, T a, T * f, T * scale)
+encode(const T * qL, const T * qR, T a, T * feat, T * scale)
 {
   const T rs = T(0.5) * (qL[0] + qR[0]);
   const T b2L = a * a + qL[5] * qL[5] + qL[6] * qL[6];
@@ -81,13 +94,6 @@ encode(const T * qL, const T * qR, T a, T * f, T * scale)
   const T irs = T(1) / rs, iPs = T(1) / Ps;
   const T vs = sqrt(Ps * irs), bs = sqrt(Ps);
   const T ivs = T(1) / vs, ibs = T(1) / bs;
-  f[0] = T(0.5) * (qL[1] + qR[1]) * ivs;
-  f[1] = T(0.5) * (qL[2] + qR[2]) * ivs;
-  f[2] = T(0.5) * (qL[3] + qR[3]) * ivs;
-  f[3] = T(0.5) * (qL[4] + qR[4]) * iPs;
-  f[4] = T(0.5) * (qL[5] + qR[5]) * ibs;
-  f[5] = T(0.5) * (qL[6] + qR[6]) * ibs;
-  f[6] = a * ibs;
   T h[7];
   h[0] = T(0.5) * (qR[0] - qL[0]) * irs;
   h[1] = T(0.5) * (qR[1] - qL[1]) * ivs;
@@ -101,10 +107,35 @@ encode(const T * qL, const T * qR, T a, T * f, T * scale)
     J = fmax(J, fabs(h[q]));
   const T sJ = fmax(J, T(kJFloor));
   const T isJ = T(1) / sJ;
-  for (int q = 0; q < 7; ++q)
-    f[7 + q] = h[q] * isJ;
-  f[14] = sJ * T(1.0 / kTauRef);
-  f[15] = T(0);
+  // even scalars
+  feat[0] = T(0.5) * (qL[1] + qR[1]) * ivs;
+  feat[1] = T(0.5) * (qL[4] + qR[4]) * iPs;
+  feat[2] = a * ibs;
+  feat[3] = h[0] * isJ;
+  feat[4] = h[1] * isJ;
+  feat[5] = h[4] * isJ;
+  feat[6] = sJ * T(1.0 / kTauRef);
+  // odd bases
+  T * u1 = feat + kIn;
+  T * u2 = feat + kIn + 4;
+  u1[0] = T(0.5) * (qL[2] + qR[2]) * ivs;
+  u1[1] = T(0.5) * (qL[5] + qR[5]) * ibs;
+  u1[2] = h[2] * isJ;
+  u1[3] = h[5] * isJ;
+  u2[0] = T(0.5) * (qL[3] + qR[3]) * ivs;
+  u2[1] = T(0.5) * (qL[6] + qR[6]) * ibs;
+  u2[2] = h[3] * isJ;
+  u2[3] = h[6] * isJ;
+  // their pairwise products (invariant under the reflections)
+  int o = 7;
+  for (int i = 0; i < 4; ++i)
+    for (int j = i; j < 4; ++j)
+      feat[o++] = u1[i] * u1[j];
+  for (int i = 0; i < 4; ++i)
+    for (int j = i; j < 4; ++j)
+      feat[o++] = u2[i] * u2[j];
+  for (; o < kIn; ++o)
+    feat[o] = T(0);
   scale[0] = rs * vs * sJ;
   scale[1] = Ps * vs * sJ;
   scale[2] = Ps * sJ;
@@ -113,6 +144,22 @@ encode(const T * qL, const T * qR, T a, T * f, T * scale)
   scale[5] = bs * vs * sJ;
   scale[6] = bs * vs * sJ;
   return J;
+}
+
+// Raw network outputs -> dimensionless dissipation of the 7 flux components
+// (rho, E, mn, mt1, mt2, Bt1, Bt2).
+template <class T>
+__host__ __device__ inline void
+combine(const T * y, const T * u, T * Dn)
+{
+  const T *u1 = u, *u2 = u + 4;
+  Dn[0] = y[0];
+  Dn[1] = y[1];
+  Dn[2] = y[2];
+  Dn[3] = y[3] * u1[0] + y[4] * u1[1] + y[5] * u1[2] + y[6] * u1[3];
+  Dn[5] = y[7] * u1[0] + y[8] * u1[1] + y[9] * u1[2] + y[10] * u1[3];
+  Dn[4] = y[11] * u2[0] + y[12] * u2[1] + y[13] * u2[2] + y[14] * u2[3];
+  Dn[6] = y[15] * u2[0] + y[16] * u2[1] + y[17] * u2[2] + y[18] * u2[3];
 }
 
 // Physical ideal-MHD flux in the face-normal frame, components (rho, E, mn,
@@ -238,10 +285,12 @@ mma_16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
                : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// Shared staging of one warp: 32 feature rows of 16 bf16 (row stride 12
-// words: conflict-free fragment reads) and 32 output rows of 8 floats.
-constexpr int kStageXWords = 32 * 12;
-constexpr int kStageOFloats = 32 * 9;
+// Shared staging of one warp: 32 input rows of 32 bf16 (row stride 20
+// words: conflict-free fragment reads) and 32 output rows of 24 floats.
+constexpr int kStageRow = 20;
+constexpr int kStageXWords = 32 * kStageRow;
+constexpr int kStageORow = kOut + 1;
+constexpr int kStageOFloats = 32 * kStageORow;
 
 // C fragments (two adjacent 8-wide n-tiles) -> A fragment of the next layer,
 // with the activation applied.
@@ -256,15 +305,16 @@ act_to_a(const float (&c0)[4], const float (&c1)[4], uint32_t (&a)[4])
 
 // Forward pass of the network for the 32 faces of a warp (one per lane);
 // every lane of the warp must call it.  wp: packed weights (shared), bias:
-// b1, b2, b3 (shared), sx / so: this warp's staging.
+// b1, b2, b3 (shared), sx / so: this warp's staging; x: this lane's inputs,
+// out: its raw outputs.
 __device__ __forceinline__ void
 warp_forward(const uint32_t * __restrict__ wp, const float * __restrict__ bias, uint32_t * sx,
-             float * so, const float (&f)[kIn], float (&out)[kOut])
+             float * so, const float (&x)[kIn], float (&out)[kOut])
 {
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
 #pragma unroll
-  for (int q = 0; q < 8; ++q)
-    sx[lane * 12 + q] = pack_bf16x2(f[2 * q], f[2 * q + 1]);
+  for (int q = 0; q < kIn / 2; ++q)
+    sx[lane * kStageRow + q] = pack_bf16x2(x[2 * q], x[2 * q + 1]);
   __syncwarp();
   const uint2 * W1 = reinterpret_cast<const uint2 *>(wp + kPackW1);
   const uint2 * W2 = reinterpret_cast<const uint2 *>(wp + kPackW2);
@@ -276,7 +326,6 @@ warp_forward(const uint32_t * __restrict__ wp, const float * __restrict__ bias, 
   for (int mt = 0; mt < 2; ++mt)
   {
     const int r0 = mt * 16 + g, r1 = r0 + 8;
-    uint32_t  a[4] = { sx[r0 * 12 + t], sx[r1 * 12 + t], sx[r0 * 12 + t + 4], sx[r1 * 12 + t + 4] };
     float     c[8][4];
 #pragma unroll
     for (int nt = 0; nt < 8; ++nt)
@@ -286,8 +335,19 @@ warp_forward(const uint32_t * __restrict__ wp, const float * __restrict__ bias, 
       c[nt][1] = x1;
       c[nt][2] = x0;
       c[nt][3] = x1;
-      const uint2 w = W1[nt * 32 + lane];
-      mma_16816(c[nt], a, w.x, w.y);
+    }
+#pragma unroll
+    for (int kt = 0; kt < kIn / 16; ++kt)
+    {
+      const int      w0 = kt * 8;
+      const uint32_t a[4] = { sx[r0 * kStageRow + w0 + t], sx[r1 * kStageRow + w0 + t],
+                              sx[r0 * kStageRow + w0 + t + 4], sx[r1 * kStageRow + w0 + t + 4] };
+#pragma unroll
+      for (int nt = 0; nt < 8; ++nt)
+      {
+        const uint2 w = W1[(kt * 8 + nt) * 32 + lane];
+        mma_16816(c[nt], a, w.x, w.y);
+      }
     }
     uint32_t h[4][4];
 #pragma unroll
@@ -311,22 +371,27 @@ warp_forward(const uint32_t * __restrict__ wp, const float * __restrict__ bias, 
 #pragma unroll
     for (int kt = 0; kt < 4; ++kt)
       act_to_a(c[2 * kt], c[2 * kt + 1], h[kt]);
-    float y[4] = { b3[2 * t], b3[2 * t + 1], b3[2 * t], b3[2 * t + 1] };
 #pragma unroll
-    for (int kt = 0; kt < 4; ++kt)
+    for (int nt = 0; nt < kOut / 8; ++nt)
     {
-      const uint2 w = W3[kt * 32 + lane];
-      mma_16816(y, h[kt], w.x, w.y);
+      float y[4] = { b3[nt * 8 + 2 * t], b3[nt * 8 + 2 * t + 1], b3[nt * 8 + 2 * t],
+                     b3[nt * 8 + 2 * t + 1] };
+#pragma unroll
+      for (int kt = 0; kt < 4; ++kt)
+      {
+        const uint2 w = W3[(kt * (kOut / 8) + nt) * 32 + lane];
+        mma_16816(y, h[kt], w.x, w.y);
+      }
+      so[r0 * kStageORow + nt * 8 + 2 * t] = y[0];
+      so[r0 * kStageORow + nt * 8 + 2 * t + 1] = y[1];
+      so[r1 * kStageORow + nt * 8 + 2 * t] = y[2];
+      so[r1 * kStageORow + nt * 8 + 2 * t + 1] = y[3];
     }
-    so[r0 * 9 + 2 * t] = y[0];
-    so[r0 * 9 + 2 * t + 1] = y[1];
-    so[r1 * 9 + 2 * t] = y[2];
-    so[r1 * 9 + 2 * t + 1] = y[3];
   }
   __syncwarp();
 #pragma unroll
   for (int o = 0; o < kOut; ++o)
-    out[o] = so[lane * 9 + o];
+    out[o] = so[lane * kStageORow + o];
   __syncwarp();
 }
 

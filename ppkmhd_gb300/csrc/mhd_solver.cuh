@@ -356,9 +356,9 @@ public:
                    (unsigned)std::max(1, sur_blocks_per_sm * sm_count / (dim == 2 ? 2 : 3)));
         cudaMemsetAsync(sur_nlist, 0, sizeof(unsigned), stream);
         if (dim == 2)
-          k_flux_mlp<2><<<dim3(nb, 2), kMlpThreads, 0, stream>>>(G, B, S);
+          k_flux_mlp<2><<<dim3(nb, 2), kMlpThreads, kMlpSmemBytes, stream>>>(G, B, S);
         else
-          k_flux_mlp<3><<<dim3(nb, 3), kMlpThreads, 0, stream>>>(G, B, S);
+          k_flux_mlp<3><<<dim3(nb, 3), kMlpThreads, kMlpSmemBytes, stream>>>(G, B, S);
         return;
       }
     }
@@ -935,11 +935,19 @@ public:
       if (!sm_count)
         MHD_CK(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, P.device));
       if (dim == 2)
+      {
+        MHD_CK(cudaFuncSetAttribute(k_flux_mlp<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kMlpSmemBytes));
         MHD_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sur_blocks_per_sm, k_flux_mlp<2>,
-                                                             kMlpThreads, 0));
+                                                             kMlpThreads, kMlpSmemBytes));
+      }
       else
+      {
+        MHD_CK(cudaFuncSetAttribute(k_flux_mlp<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kMlpSmemBytes));
         MHD_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sur_blocks_per_sm, k_flux_mlp<3>,
-                                                             kMlpThreads, 0));
+                                                             kMlpThreads, kMlpSmemBytes));
+      }
       sur_blocks_per_sm = std::max(1, sur_blocks_per_sm);
       sur_tau = (float)tau;
       sur_on = true;

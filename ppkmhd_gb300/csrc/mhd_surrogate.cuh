@@ -102,26 +102,24 @@ struct SurrogateDev
 };
 
 constexpr int kMlpThreads = 128;
+constexpr int kStash = 23; // per lane: Fc[7], scale[7], u[8], pad (odd stride)
+constexpr int kMlpSmemShared = ((mlp::kPackWords + mlp::kBiasFloats) * 4 + 15) / 16 * 16;
+constexpr int kMlpSmemPerWarp = (mlp::kStageXWords + mlp::kStageOFloats + 32 * kStash) * 4;
+constexpr int kMlpSmemBytes = kMlpSmemShared + (kMlpThreads / 32) * kMlpSmemPerWarp;
 
-// Encoding of mlp::encode in FP32 with hardware reciprocals and rsqrt.
+// Encoding of mlp::encode in FP32 with hardware reciprocals and rsqrt:
+// feat[0..31] network inputs, feat[32..39] odd bases, scale[7].
 __device__ __forceinline__ float
-encode_fast(const float * qL, const float * qR, float a, float * f, float * scale)
+encode_fast(const float * qL, const float * qR, float a, float * feat, float * scale)
 {
   const float rs = 0.5f * (qL[0] + qR[0]);
   const float b2L = a * a + qL[5] * qL[5] + qL[6] * qL[6];
   const float b2R = a * a + qR[5] * qR[5] + qR[6] * qR[6];
   const float Ps = 0.5f * (qL[4] + qR[4]) + 0.25f * (b2L + b2R);
   const float irs = rcp(rs), iPs = rcp(Ps);
-  const float ibs = rsqrtf(Ps), bs = Ps * ibs;
-  const float ivs = rs * rsqrtf(rs) * ibs, vs = Ps * ivs * irs; // sqrt(rs / Ps), sqrt(Ps / rs)
-  f[0] = 0.5f * (qL[1] + qR[1]) * ivs;
-  f[1] = 0.5f * (qL[2] + qR[2]) * ivs;
-  f[2] = 0.5f * (qL[3] + qR[3]) * ivs;
-  f[3] = 0.5f * (qL[4] + qR[4]) * iPs;
-  f[4] = 0.5f * (qL[5] + qR[5]) * ibs;
-  f[5] = 0.5f * (qL[6] + qR[6]) * ibs;
-  f[6] = a * ibs;
-  float h[7];
+  const float ibs = rsq(Ps), bs = Ps * ibs;
+  const float ivs = rs * rsq(rs) * ibs, vs = Ps * ivs * irs; // sqrt(rs / Ps), sqrt(Ps / rs)
+  float       h[7];
   h[0] = 0.5f * (qR[0] - qL[0]) * irs;
   h[1] = 0.5f * (qR[1] - qL[1]) * ivs;
   h[2] = 0.5f * (qR[2] - qL[2]) * ivs;
@@ -135,11 +133,37 @@ encode_fast(const float * qL, const float * qR, float a, float * f, float * scal
     J = fmaxf(J, fabsf(h[q]));
   const float sJ = fmaxf(J, float(mlp::kJFloor));
   const float isJ = rcp(sJ);
+  feat[0] = 0.5f * (qL[1] + qR[1]) * ivs;
+  feat[1] = 0.5f * (qL[4] + qR[4]) * iPs;
+  feat[2] = a * ibs;
+  feat[3] = h[0] * isJ;
+  feat[4] = h[1] * isJ;
+  feat[5] = h[4] * isJ;
+  feat[6] = sJ * float(1.0 / mlp::kTauRef);
+  float * u1 = feat + mlp::kIn;
+  float * u2 = feat + mlp::kIn + 4;
+  u1[0] = 0.5f * (qL[2] + qR[2]) * ivs;
+  u1[1] = 0.5f * (qL[5] + qR[5]) * ibs;
+  u1[2] = h[2] * isJ;
+  u1[3] = h[5] * isJ;
+  u2[0] = 0.5f * (qL[3] + qR[3]) * ivs;
+  u2[1] = 0.5f * (qL[6] + qR[6]) * ibs;
+  u2[2] = h[3] * isJ;
+  u2[3] = h[6] * isJ;
+  int o = 7;
 #pragma unroll
-  for (int q = 0; q < 7; ++q)
-    f[7 + q] = h[q] * isJ;
-  f[14] = sJ * float(1.0 / mlp::kTauRef);
-  f[15] = 0.f;
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = i; j < 4; ++j)
+      feat[o++] = u1[i] * u1[j];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = i; j < 4; ++j)
+      feat[o++] = u2[i] * u2[j];
+#pragma unroll
+  for (int q = mlp::kInUsed; q < mlp::kIn; ++q)
+    feat[q] = 0.f;
   const float rvs = rs * vs * sJ, pvs = Ps * vs * sJ, ps = Ps * sJ, bvs = bs * vs * sJ;
   scale[0] = rvs;
   scale[1] = pvs;
@@ -180,10 +204,9 @@ central_flux_fast(const float * qL, const float * qR, float a, float igm1, float
 
 // One face of the surrogate flux stage.  Returns true when the face must
 // be computed by HLLD (not smooth, at a floor, or a failed prediction).
-// Per-lane values kept in shared memory across the network evaluation
-// (the central flux and the output scales), which frees registers for the
-// tensor-core fragments.
-constexpr int kStash = 15; // Fc[7], scale[7], pad (odd stride)
+// Per-lane values (central flux, output scales, odd bases) are kept in
+// shared memory across the network evaluation, which frees registers for
+// the tensor-core fragments.
 
 template <int DIM, int d>
 __device__ __forceinline__ bool
@@ -191,9 +214,10 @@ flux_face_mlp(const Grid<float> & G, const Buffers<float> & B, const SurrogateDe
               int64_t c, const uint32_t * sw, const float * sb, uint32_t * sx, float * so,
               float * stash)
 {
-  float f[mlp::kIn];
-  bool  smooth = false;
+  float     f[mlp::kFeat];
+  bool      smooth = false;
   const int lane = threadIdx.x & 31;
+  float *   my = stash + lane * kStash;
   if (valid)
   {
     State<float> qL, qR;
@@ -211,44 +235,43 @@ flux_face_mlp(const Grid<float> & G, const Buffers<float> & B, const SurrogateDe
 #pragma unroll
     for (int q = 0; q < 7; ++q)
     {
-      stash[lane * kStash + q] = Fc[q];
-      stash[lane * kStash + 7 + q] = sc[q];
+      my[q] = Fc[q];
+      my[7 + q] = sc[q];
     }
+#pragma unroll
+    for (int q = 0; q < mlp::kBasis; ++q)
+      my[14 + q] = f[mlp::kIn + q];
   }
   if (!__any_sync(0xffffffffu, smooth))
     return valid;
-  if (!smooth)
-  {
+  float x[mlp::kIn];
 #pragma unroll
-    for (int q = 0; q < mlp::kIn; ++q)
-      f[q] = 0.f;
-  }
+  for (int q = 0; q < mlp::kIn; ++q)
+    x[q] = smooth ? f[q] : 0.f;
   float y[mlp::kOut];
-  mlp::warp_forward(sw, sb, sx, so, f, y);
+  mlp::warp_forward(sw, sb, sx, so, x, y);
   if (!smooth)
     return valid;
-  float Fc[7], sc[7];
+  float u[mlp::kBasis], Dn[mlp::kOutUsed];
 #pragma unroll
-  for (int q = 0; q < 7; ++q)
-  {
-    Fc[q] = stash[lane * kStash + q];
-    sc[q] = stash[lane * kStash + 7 + q];
-  }
+  for (int q = 0; q < mlp::kBasis; ++q)
+    u[q] = my[14 + q];
+  mlp::combine(y, u, Dn);
   bool ok = true;
 #pragma unroll
   for (int q = 0; q < 7; ++q)
-    ok = ok && isfinite(y[q]) && fabsf(y[q]) <= mlp::kDissBound;
+    ok = ok && isfinite(Dn[q]) && fabsf(Dn[q]) <= mlp::kDissBound;
   if (!ok)
     return true;
   State<float> fl;
-  fl[ID] = Fc[0] - sc[0] * y[0];
-  fl[IP] = Fc[1] - sc[1] * y[1];
-  fl[IU] = Fc[2] - sc[2] * y[2];
-  fl[IV] = Fc[3] - sc[3] * y[3];
-  fl[IW] = Fc[4] - sc[4] * y[4];
+  fl[ID] = my[0] - my[7] * Dn[0];
+  fl[IP] = my[1] - my[8] * Dn[1];
+  fl[IU] = my[2] - my[9] * Dn[2];
+  fl[IV] = my[3] - my[10] * Dn[3];
+  fl[IW] = my[4] - my[11] * Dn[4];
   fl[IA] = 0.f;
-  fl[IB] = Fc[5] - sc[5] * y[5];
-  fl[IC] = Fc[6] - sc[6] * y[6];
+  fl[IB] = my[5] - my[12] * Dn[5];
+  fl[IC] = my[6] - my[13] * Dn[6];
   store_face_flux<float, DIM, d>(G, B, c, fl);
   return false;
 }
@@ -257,14 +280,19 @@ flux_face_mlp(const Grid<float> & G, const Buffers<float> & B, const SurrogateDe
 // the faces so the weights are staged in shared memory once per block.
 // Faces the network does not answer are appended to S.list.
 template <int DIM>
-__global__ void __launch_bounds__(kMlpThreads, 4)
+__global__ void __launch_bounds__(kMlpThreads, 3)
 k_flux_mlp(const Grid<float> G, Buffers<float> B, const SurrogateDev S)
 {
-  __shared__ __align__(16) uint32_t sw[mlp::kPackWords];
-  __shared__ float                  sb[mlp::kBiasFloats];
-  __shared__ uint32_t               sx[kMlpThreads / 32][mlp::kStageXWords];
-  __shared__ float                  so[kMlpThreads / 32][mlp::kStageOFloats];
-  __shared__ float                  stash[kMlpThreads / 32][32 * kStash];
+  // dynamic shared memory (kMlpSmemBytes): weights, biases, then per warp
+  // the input staging, the output staging and the stash
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint32_t * sw = reinterpret_cast<uint32_t *>(smem);
+  float *    sb = reinterpret_cast<float *>(sw + mlp::kPackWords);
+  const int  warp = threadIdx.x >> 5;
+  unsigned char * wbase = smem + kMlpSmemShared + (size_t)warp * kMlpSmemPerWarp;
+  uint32_t * sx = reinterpret_cast<uint32_t *>(wbase);
+  float *    so = reinterpret_cast<float *>(sx + mlp::kStageXWords);
+  float *    stash = so + mlp::kStageOFloats;
   for (int q = threadIdx.x; q < mlp::kPackWords; q += blockDim.x)
     sw[q] = S.wpack[q];
   for (int q = threadIdx.x; q < mlp::kBiasFloats; q += blockDim.x)
@@ -272,7 +300,7 @@ k_flux_mlp(const Grid<float> G, Buffers<float> B, const SurrogateDev S)
   __syncthreads();
   if (step_finished(B.st))
     return;
-  const int     dir = blockIdx.y, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int     dir = blockIdx.y, lane = threadIdx.x & 31;
   const Box &   bx = G.box[BOX_FACE];
   const int64_t n = bx.count();
   unsigned      used = 0, total = 0;
@@ -285,12 +313,11 @@ k_flux_mlp(const Grid<float> G, Buffers<float> B, const SurrogateDev S)
     const int64_t c = valid ? cell_at(G, i, j, k) : 0;
     bool          rest;
     if (dir == 0)
-      rest = flux_face_mlp<DIM, 0>(G, B, S, valid, c, sw, sb, sx[warp], so[warp], stash[warp]);
+      rest = flux_face_mlp<DIM, 0>(G, B, S, valid, c, sw, sb, sx, so, stash);
     else if (dir == 1)
-      rest = flux_face_mlp<DIM, 1>(G, B, S, valid, c, sw, sb, sx[warp], so[warp], stash[warp]);
+      rest = flux_face_mlp<DIM, 1>(G, B, S, valid, c, sw, sb, sx, so, stash);
     else
-      rest = flux_face_mlp<DIM, DIM == 3 ? 2 : 1>(G, B, S, valid, c, sw, sb, sx[warp], so[warp],
-                                                  stash[warp]);
+      rest = flux_face_mlp<DIM, DIM == 3 ? 2 : 1>(G, B, S, valid, c, sw, sb, sx, so, stash);
     total += valid ? 1u : 0u;
     used += (valid && !rest) ? 1u : 0u;
     // warp-aggregated append of the faces left to HLLD

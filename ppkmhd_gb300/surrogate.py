@@ -25,8 +25,8 @@ import time
 
 import numpy as np
 
-from . import (MHD_FP32, MHD_MLP_CHECK, MHD_MLP_PARAMS, MHD_MLP_TRAIN, MHD_OK, MHD_SAMPLE_FLOATS,
-               MHDError, MHDSolver, lib, params_from_ini)
+from . import (MHD_MLP_CHECK, MHD_MLP_FEATURES, MHD_MLP_PARAMS, MHD_OK, MHDError, MHDSolver, lib,
+               params_from_ini)
 from . import workloads
 
 DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
@@ -36,7 +36,8 @@ REC_J = 15
 
 
 class FluxMLP:
-    """A 15-64-64-7 GELU network on the GPU (``mhd_mlp``)."""
+    """A 27-64-64-19 GELU network on the GPU (``mhd_mlp``), odd in each
+    transverse direction by construction."""
 
     def __init__(self, seed: int = 0, gamma0: float = GAMMA):
         self.h = ctypes.c_void_p()
@@ -88,7 +89,7 @@ class FluxMLP:
     def encode(self, records: np.ndarray):
         rec = np.ascontiguousarray(records, dtype=np.float32)
         n = rec.shape[0]
-        f = np.empty((n, 16), dtype=np.float32)
+        f = np.empty((n, MHD_MLP_FEATURES), dtype=np.float32)
         t = np.empty((n, 8), dtype=np.float32)
         self._check(lib().mhd_mlp_encode(self.h, rec.ctypes.data, n, f.ctypes.data, t.ctypes.data))
         return f, t

@@ -32,8 +32,8 @@ def _random_faces(rng, n):
 def test_oracle_gradient_matches_finite_differences(oracle):
     rng = np.random.default_rng(0)
     P = rng.normal(0, 0.2, oracle.MLP_NPARAM)
-    X = rng.normal(0, 1, (24, 16))
-    X[:, 15] = 0
+    X = rng.normal(0, 1, (24, oracle.MLP_NFEAT))
+    X[:, 27:32] = 0
     T = rng.normal(0, 1, (24, 8))
     T[:, 7] = 0
     _, g = oracle.mlp_loss_grad(P, X, T)
@@ -61,6 +61,27 @@ def test_oracle_encoding_is_dimensionless(oracle):
         assert np.allclose(sc2[[0, 2, 3, 4]], k * sc[[0, 2, 3, 4]], rtol=1e-12)
 
 
+def test_oracle_network_is_odd_in_each_transverse_direction(oracle):
+    """Reflecting t1 (vt1, Bt1 -> -vt1, -Bt1) flips the mt1 and Bt1
+    dissipation and leaves the others, for any weights; a face without
+    transverse components gets exactly zero transverse dissipation."""
+    rng = np.random.default_rng(8)
+    P = rng.normal(0, 0.3, oracle.MLP_NPARAM)
+    ql, qr, a = _random_faces(rng, 16)
+    for s in range(16):
+        f, _, _ = oracle.mlp_encode(ql[s], qr[s], a[s])
+        m = np.array([1, 1, -1, 1, 1, -1, 1.0])
+        g, _, _ = oracle.mlp_encode(ql[s] * m, qr[s] * m, a[s])
+        y = oracle.mlp_forward(P, f[None])[0]
+        z = oracle.mlp_forward(P, g[None])[0]
+        assert np.allclose(z[[0, 1, 2, 4, 6]], y[[0, 1, 2, 4, 6]], rtol=1e-13, atol=1e-15)
+        assert np.allclose(z[[3, 5]], -y[[3, 5]], rtol=1e-13, atol=1e-15)
+        m2 = np.array([1, 1, 1, 0, 1, 1, 0.0])  # no t2 components at all
+        h, _, _ = oracle.mlp_encode(ql[s] * m2, qr[s] * m2, a[s])
+        w = oracle.mlp_forward(P, h[None])[0]
+        assert w[4] == 0.0 and w[6] == 0.0
+
+
 def test_oracle_central_flux_is_hlld_for_equal_states(oracle):
     """Equal states: HLLD returns the physical flux, so D = 0
     (RiemannSolvers_MHD.h:133-367 samples the left state)."""
@@ -79,7 +100,7 @@ def test_committed_weights_file():
     from ppkmhd_gb300 import surrogate
 
     z = np.load(surrogate.DEFAULT_WEIGHTS)
-    assert z["params"].shape == (5768,) and z["params"].dtype == np.float32
+    assert z["params"].shape == (7832,) and z["params"].dtype == np.float32
     assert np.isfinite(z["params"]).all()
     assert abs(float(z["gamma0"]) - GAMMA) < 1e-12
 
@@ -144,11 +165,11 @@ def test_tensor_core_forward_matches_oracle(mhdlib, oracle):
     rng = np.random.default_rng(4)
     m = FluxMLP(seed=5)
     P = m.params.copy()
-    P[P != 0] += rng.normal(0, 0.05, (P != 0).sum()).astype(np.float32)  # non-trivial biases too
-    P[1024:1088] = rng.normal(0, 0.3, 64)
+    P[P != 0] += rng.normal(0, 0.05, (P != 0).sum()).astype(np.float32)
+    P[32 * 64:33 * 64] = rng.normal(0, 0.3, 64)  # non-trivial b1
     m.params = P
-    X = rng.normal(0, 1, (1000, 16)).astype(np.float32)
-    X[:, 15] = 0
+    X = rng.normal(0, 1, (1000, 40)).astype(np.float32)
+    X[:, 27:32] = 0
     y = m.forward(X).astype(np.float64)
     yo = oracle.mlp_forward(m.params.astype(np.float64), X.astype(np.float64), rounding=True)
     yx = oracle.mlp_forward(m.params.astype(np.float64), X.astype(np.float64), rounding=False)
