@@ -190,9 +190,12 @@ def emit(obj):
 
 # ---------------------------------------------------------------- CPU side
 
-def cpu_baseline_run(name: str, steps: int, warmup: int, nthreads: int):
+def cpu_baseline_run(name: str, steps: int | None, warmup: int, nthreads: int,
+                     target_s: float = 8.0):
     """The oracle port of the reference step (oracle/mhd_oracle.c) on the host
-    cores: same workload, full grid, `steps` timed iterations."""
+    cores: same workload, full grid.  steps=None sizes the timed sample to
+    about target_s seconds from the duration of the warm-up step.  Returns
+    (cell-updates/s, seconds timed, steps timed)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py
 
@@ -202,14 +205,17 @@ def cpu_baseline_run(name: str, steps: int, warmup: int, nthreads: int):
     s = oracle_py.OracleSolver(ini, nthreads=nthreads)
     if transform is not None:
         s.set_state(transform(s.get_state()))
-    if warmup:
-        s.run(warmup)
+    t0 = time.perf_counter()
+    s.run(max(warmup, 1))
+    t_one = (time.perf_counter() - t0) / max(warmup, 1)
+    if steps is None:
+        steps = int(min(5000, max(2, target_s / max(t_one, 1e-6))))
     t0 = time.perf_counter()
     s.run(steps)
     el = time.perf_counter() - t0
     s.close()
     cells = n ** dim
-    return cells * steps / el, el
+    return cells * steps / el, el, steps
 
 
 # ---------------------------------------------------------------- GPU side
@@ -333,9 +339,10 @@ def run_gb300(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
-        v, el = cpu_baseline_run(args.workload, steps=args.cpu_steps, warmup=1, nthreads=nthreads)
+        v, el, ns = cpu_baseline_run(args.workload, steps=args.cpu_steps, warmup=1,
+                                     nthreads=nthreads)
         cpu = {"value": v, "unit": "cell-updates/s", "cores": nthreads, "kind": "port",
-               "sample": f"{args.cpu_steps} steps of the same {n}^{dim} grid after 1 warm-up "
+               "sample": f"{ns} steps of the same {n}^{dim} grid after 1 warm-up "
                          f"step, oracle/mhd_oracle.c with {nthreads} OpenMP threads "
                          f"({el:.1f} s timed)"}
 
@@ -721,8 +728,8 @@ def run_reference(args):
               "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
                       "d2h_bytes_per_step": 0}})
         return
-    v, el = cpu_baseline_run(args.workload, steps=steps, warmup=min(args.warmup, 1),
-                             nthreads=nthreads)
+    v, el, steps = cpu_baseline_run(args.workload, steps=steps, warmup=1, nthreads=nthreads,
+                                    target_s=20.0)
     emit({
         "impl": "reference",
         "metric": "MHD cell-updates/s (interior cells), plain MUSCL-Hancock+HLLD+CT step",
@@ -730,7 +737,7 @@ def run_reference(args):
         "unit": "cell-updates/s",
         "n_gpus": world,
         "steps": steps,
-        "warmup": min(args.warmup, 1),
+        "warmup": 1,
         "ms_per_step": el * 1e3 / steps,
         "higher_is_better": True,
         "scaling": "weak",
@@ -741,7 +748,8 @@ def run_reference(args):
                    "implementation": "CPU port of the reference step (oracle/mhd_oracle.c, "
                                      "bitwise equal to the reference functors), OpenMP"},
         "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": nthreads, "kind": "port",
-                         "sample": f"{steps} steps of the full {n}^{dim} grid"},
+                         "sample": f"{steps} steps of the full {n}^{dim} grid after 1 warm-up "
+                                   f"step ({el:.1f} s timed)"},
         "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     })
@@ -755,19 +763,19 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="ot3d_256_fp64", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-steps", type=int, default=None,
-                    help="CPU leg iterations (default: about 10 s of host work)")
+                    help="CPU leg iterations (default: about 8 s of host work)")
     ap.add_argument("--ref-steps", type=int, default=None,
-                    help="reference-arm iterations (default: --steps, at most 20 full-grid "
-                         "iterations; 150 for the ensemble sample)")
+                    help="reference-arm iterations (default: about 20 s of host work; 150 "
+                         "iterations of the 8-problem sample for the ensemble)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--acc-steps", type=int, default=40,
                     help="steps of the accuracy comparison of the turbulence workload")
     ap.add_argument("--no-variants", action="store_true")
     args = ap.parse_args()
-    if args.cpu_steps is None:
-        args.cpu_steps = 150 if args.workload.startswith("ensemble") else 6
-    if args.ref_steps is None:
-        args.ref_steps = 150 if args.workload.startswith("ensemble") else max(1, min(args.steps, 20))
+    if args.cpu_steps is None and args.workload.startswith("ensemble"):
+        args.cpu_steps = 150
+    if args.ref_steps is None and args.workload.startswith("ensemble"):
+        args.ref_steps = 150
     if args.impl == "reference":
         run_reference(args)
     elif args.workload.startswith("ensemble"):
