@@ -700,10 +700,10 @@ face_states(const Grid<R> & G, const Buffers<R> & B, int64_t c, State<R> & qL, S
     qR[v] = Q2[c + v * sv] - R(0.5) * S[c + v * sv];
     qL[v] = Q2[cn + v * sv] + R(0.5) * S[cn + v * sv];
   }
-  qR[ID] = fmax(smallR, qR[ID]);
-  qR[IP] = fmax(smallp * qR[ID], qR[IP]);
-  qL[ID] = fmax(smallR, qL[ID]);
-  qL[IP] = fmax(smallp * qL[ID], qL[IP]);
+  qR[ID] = sel_max(smallR, qR[ID]);
+  qR[IP] = sel_max(smallp * qR[ID], qR[IP]);
+  qL[ID] = sel_max(smallR, qL[ID]);
+  qL[IP] = sel_max(smallp * qL[ID], qL[IP]);
   qR[nrm] = B.Uin[c + nrm * sv] + face_source<R, DIM>(G, B.E, c, d, dtdx, dtdy, dtdz);
   qL[nrm] = qR[nrm];
   if constexpr (d > 0)
@@ -864,8 +864,8 @@ emf_edge(const Grid<R> & G, const Buffers<R> & B, int i, int j, int k)
       else
         q[IC] += R(0.5) * (sdq0 * S0[cc + IC * sv] + sdq1 * S1[cc + IC * sv]);
     }
-    q[ID] = fmax(smallR, q[ID]);
-    q[IP] = fmax(smallp * q[ID], q[IP]);
+    q[ID] = sel_max(smallR, q[ID]);
+    q[IP] = sel_max(smallp * q[ID], q[IP]);
   }
   if constexpr (DIM == 3 && edir == 1)
   {

@@ -116,11 +116,63 @@ fsqrt(double x)
   return sqrt(x);
 }
 
-// Both fast magnetosonic speeds (normal field in slot IA, then in slot IB)
-// of one state with one reciprocal of the density (mhd_utils.h:89-117).
+// Selection by comparison.  GB300 runs FP64 comparisons on the narrow FP64
+// pipe; the fast FP64 build compares the bit patterns as integers instead
+// (key(x) = bits ^ ((bits >> 63) & 0x7fff...) orders like the values for
+// non-NaN doubles, with -0 below +0), which runs on the integer pipes.  The
+// exact build keeps the reference's FP comparisons (mhd_utils.h:36-77).
+__device__ __forceinline__ long long
+order_key(double x)
+{
+  const long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+template <class R>
+__device__ __forceinline__ R
+sel_max(R r, R a)
+{
+  if constexpr (sizeof(R) == 8 && !kExactOrder)
+    return order_key(a) > order_key(r) ? a : r;
+  else
+    return (a > r) ? a : r;
+}
+template <class R>
+__device__ __forceinline__ R
+sel_min(R r, R a)
+{
+  if constexpr (sizeof(R) == 8 && !kExactOrder)
+    return order_key(a) < order_key(r) ? a : r;
+  else
+    return (a < r) ? a : r;
+}
+template <class R>
+__device__ __forceinline__ R
+max4(R a0, R a1, R a2, R a3)
+{
+  return sel_max(sel_max(sel_max(a0, a1), a2), a3);
+}
+template <class R>
+__device__ __forceinline__ R
+min4(R a0, R a1, R a2, R a3)
+{
+  return sel_min(sel_min(sel_min(a0, a1), a2), a3);
+}
+template <class R>
+__device__ __forceinline__ R
+max5(R a0, R a1, R a2, R a3, R a4)
+{
+  return sel_max(sel_max(sel_max(sel_max(a0, a1), a2), a3), a4);
+}
+
+
+// Squares of both fast magnetosonic speeds (normal field in slot IA, then in
+// slot IB) of one state with one reciprocal of the density
+// (mhd_utils.h:89-117).  The callers take the square root of the largest
+// only: the square root is correctly rounded and monotone, so
+// max_i sqrt(x_i) = sqrt(max_i x_i) exactly.
 template <class R>
 __device__ __forceinline__ void
-fast_speeds_xy(const State<R> & q, R gamma0, R & cfx, R & cfy)
+fast_speeds2_xy(const State<R> & q, R gamma0, R & cfx2, R & cfy2)
 {
   const R invd = rcp(q[ID]);
   const R a = q[IA], b = q[IB], c = q[IC];
@@ -128,8 +180,8 @@ fast_speeds_xy(const State<R> & q, R gamma0, R & cfx, R & cfy)
   const R c2 = gamma0 * q[IP] * invd;
   const R d2 = R(0.5) * (b2 * invd + c2);
   const R cd = c2 * invd;
-  cfx = fsqrt(d2 + fsqrt(d2 * d2 - cd * a * a));
-  cfy = fsqrt(d2 + fsqrt(d2 * d2 - cd * b * b));
+  cfx2 = d2 + fsqrt(d2 * d2 - cd * a * a);
+  cfy2 = d2 + fsqrt(d2 * d2 - cd * b * b);
 }
 
 // Fast magnetosonic speed with the normal field in slot IA
@@ -500,17 +552,17 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
     const R id = rcp(rl);
     const R c2 = gamma0 * pl * id;
     const R d2 = R(0.5) * (b2l * id + c2);
-    cfastl = fsqrt(d2 + fsqrt(d2 * d2 - c2 * a2 * id));
+    cfastl = d2 + fsqrt(d2 * d2 - c2 * a2 * id); // squared speed
   }
   {
     const R id = rcp(rr);
     const R c2 = gamma0 * pr * id;
     const R d2 = R(0.5) * (b2r * id + c2);
-    cfastr = fsqrt(d2 + fsqrt(d2 * d2 - c2 * a2 * id));
+    cfastr = d2 + fsqrt(d2 * d2 - c2 * a2 * id);
   }
-  const R cmax = fmax(cfastl, cfastr);
-  const R sl = fmin(ul, ur) - cmax;
-  const R sr = fmax(ul, ur) + cmax;
+  const R cmax = fsqrt(sel_max(cfastl, cfastr)); // = max of the square roots
+  const R sl = sel_min(ul, ur) - cmax;
+  const R sr = sel_max(ul, ur) + cmax;
   const R rcl = rl * (ul - sl);
   const R rcr = rr * (sr - ur);
   const R irc = rcp(rcr + rcl);
@@ -640,38 +692,6 @@ riemann(int solver, State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
     riemann_hll(ql, qr, flux, gamma0);
   else
     riemann_llf(ql, qr, flux, gamma0);
-}
-
-template <class R>
-__device__ __forceinline__ R
-max4(R a0, R a1, R a2, R a3)
-{
-  R r = a0;
-  r = (a1 > r) ? a1 : r;
-  r = (a2 > r) ? a2 : r;
-  r = (a3 > r) ? a3 : r;
-  return r;
-}
-template <class R>
-__device__ __forceinline__ R
-min4(R a0, R a1, R a2, R a3)
-{
-  R r = a0;
-  r = (a1 < r) ? a1 : r;
-  r = (a2 < r) ? a2 : r;
-  r = (a3 < r) ? a3 : r;
-  return r;
-}
-template <class R>
-__device__ __forceinline__ R
-max5(R a0, R a1, R a2, R a3, R a4)
-{
-  R r = a0;
-  r = (a1 > r) ? a1 : r;
-  r = (a2 > r) ? a2 : r;
-  r = (a3 > r) ? a3 : r;
-  r = (a4 > r) ? a4 : r;
-  return r;
 }
 
 // Two-dimensional HLLD magnetic Riemann solver giving the edge EMF
@@ -820,14 +840,14 @@ mag_riemann2d_hlld_fast(const State<R> (&q)[4], const R (&e)[4], R gamma0, R sma
 {
   const State<R> &qLL = q[0], &qRL = q[1], &qLR = q[2], &qRR = q[3];
   R               cFastLLx, cFastLLy, cFastLRx, cFastLRy, cFastRLx, cFastRLy, cFastRRx, cFastRRy;
-  fast_speeds_xy(qLL, gamma0, cFastLLx, cFastLLy);
-  fast_speeds_xy(qLR, gamma0, cFastLRx, cFastLRy);
-  fast_speeds_xy(qRL, gamma0, cFastRLx, cFastRLy);
-  fast_speeds_xy(qRR, gamma0, cFastRRx, cFastRRy);
+  fast_speeds2_xy(qLL, gamma0, cFastLLx, cFastLLy);
+  fast_speeds2_xy(qLR, gamma0, cFastLRx, cFastLRy);
+  fast_speeds2_xy(qRL, gamma0, cFastRLx, cFastRLy);
+  fast_speeds2_xy(qRR, gamma0, cFastRRx, cFastRRy);
   const R uLL = qLL[IU], uLR = qLR[IU], uRL = qRL[IU], uRR = qRR[IU];
   const R vLL = qLL[IV], vLR = qLR[IV], vRL = qRL[IV], vRR = qRR[IV];
-  const R cxm = max4(cFastLLx, cFastLRx, cFastRLx, cFastRRx);
-  const R cym = max4(cFastLLy, cFastLRy, cFastRLy, cFastRRy);
+  const R cxm = fsqrt(max4(cFastLLx, cFastLRx, cFastRLx, cFastRRx));
+  const R cym = fsqrt(max4(cFastLLy, cFastLRy, cFastRLy, cFastRRy));
   const R SL = min4(uLL, uLR, uRL, uRR) - cxm;
   const R SR = max4(uLL, uLR, uRL, uRR) + cxm;
   const R SB = min4(vLL, vLR, vRL, vRR) - cym;
@@ -885,10 +905,10 @@ mag_riemann2d_hlld_fast(const State<R> (&q)[4], const R (&e)[4], R gamma0, R sma
                           fabs(bRL) * rsq(rstarRLy), fabs(BstarRL) * rsq(rstarRL), smallc);
   const R calfvenT = max5(fabs(bLR) * rsq(rstarLRy), fabs(BstarLR) * rsq(rstarLR),
                           fabs(bRR) * rsq(rstarRRy), fabs(BstarRR) * rsq(rstarRR), smallc);
-  const R SAL = fmin(ustar - calfvenL, R(0));
-  const R SAR = fmax(ustar + calfvenR, R(0));
-  const R SAB = fmin(vstar - calfvenB, R(0));
-  const R SAT = fmax(vstar + calfvenT, R(0));
+  const R SAL = sel_min(ustar - calfvenL, R(0));
+  const R SAR = sel_max(ustar + calfvenR, R(0));
+  const R SAB = sel_min(vstar - calfvenB, R(0));
+  const R SAT = sel_max(vstar + calfvenT, R(0));
   const R iLR = rcp(SAR - SAL), iBT = rcp(SAT - SAB);
 
   if (SB_pos)
