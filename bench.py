@@ -184,6 +184,23 @@ def dist_setup():
     return world, rank, local
 
 
+def max_over_ranks(t_sec: float, world: int, device: str) -> float:
+    """The slowest rank's time (every rank times the same replica work)."""
+    if world <= 1:
+        return t_sec
+    import torch
+
+    tt = torch.tensor([t_sec], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def replica_value(units_per_rank: float, t_sec: float, world: int) -> float:
+    """Whole-job throughput of N independent replicas: all ranks' units over
+    the slowest rank's time."""
+    return world * units_per_rank / t_sec
+
+
 def emit(obj):
     print(json.dumps(obj), flush=True)
 
@@ -256,11 +273,8 @@ def run_gb300(args):
         ms = s.run_timed(args.steps)
     torch.cuda.synchronize()
     t_sec = ms / 1e3
-    if world > 1:
-        tt = torch.tensor([t_sec], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_sec = float(tt.item())
-    value = world * interior_cells * args.steps / t_sec
+    t_sec = max_over_ranks(t_sec, world, "cuda")
+    value = replica_value(interior_cells * args.steps, t_sec, world)
 
     # ---- per-kernel timing of one iteration (events around every launch)
     prof = {}
@@ -466,11 +480,8 @@ def run_ensemble(args):
         ms = ens.run(args.steps)
     torch.cuda.synchronize()
     t_sec = ms / 1e3
-    if world > 1:
-        tt = torch.tensor([t_sec], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_sec = float(tt.item())
-    value = world * cells * args.steps / t_sec
+    t_sec = max_over_ranks(t_sec, world, "cuda")
+    value = replica_value(cells * args.steps, t_sec, world)
 
     prof = {}
     for _ in range(3):
