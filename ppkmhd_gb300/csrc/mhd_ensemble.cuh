@@ -297,9 +297,9 @@ public:
     }
     MHD_ECK(cudaSetDevice(params[0].device));
     MHD_ECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-    // one arena: per problem U, U2, Q, Q2, S (dim x 8), E, F (dim x nf), Em
-    const int          ne = dim == 3 ? 3 : 1, nf = dim == 3 ? 5 : 6;
-    const int          planes = 8 * 4 + 8 * dim + ne + nf * dim + ne;
+    // one arena: per problem U, U2, Q, Q2, S (dim x 8), E, F (dim x nf), Em, H
+    const int          ne = dim == 3 ? 3 : 1, nf = dim == 3 ? 5 : 6, nh = face_data_planes(dim);
+    const int          planes = 8 * 4 + 8 * dim + ne + nf * dim + ne + nh;
     std::vector<size_t> off(n);
     size_t              total = 0;
     G.resize(n);
@@ -334,6 +334,8 @@ public:
       B[p].F = a;
       a += nf * dim * c;
       B[p].Em = a;
+      a += ne * c;
+      B[p].H = a;
       B[p].st = st + p;
     }
     MHD_ECK(cudaMalloc(&dG, n * sizeof(Grid<R>)));
@@ -471,7 +473,10 @@ public:
         err = std::string("graph instantiate: ") + cudaGetErrorString(ie);
         return MHD_ERR_CUDA;
       }
+      // upload now so that the first replay does not pay for it
+      MHD_ECK(cudaGraphUpload(graph_pair[parity], stream));
     }
+    MHD_ECK(cudaStreamSynchronize(stream));
     return MHD_OK;
   }
 

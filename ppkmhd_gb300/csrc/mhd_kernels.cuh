@@ -81,8 +81,43 @@ struct Buffers
   R *       E;   // edge electric field (1 plane in 2D, Ex/Ey/Ez in 3D)
   R *       F;   // face fluxes, DIM blocks of NF planes
   R *       Em;  // edge EMFs (1 plane in 2D, 3 in 3D)
+  R *       H;   // face data, FaceData<DIM>::NPLANES planes (below)
   DevState *st;
 };
+
+// Face-centred quantities the edge reconstruction reads many times, stored
+// once: planes [0, DIM) hold the half-step face-normal field
+// B_d + (curl E)_d dt/2 of face (c, d), written by the flux stage on the
+// face box (the edge stage evaluates the layer below it with the same
+// expression, face_field); planes [DIM, NPLANES) the limited slopes of the
+// face-centred field along the transverse directions the edges use, written
+// by the trace stage.  Every stored value is the expression the edge stage
+// would otherwise evaluate, so the edge EMFs are unchanged bit for bit.
+template <int DIM>
+struct FaceData
+{
+  static constexpr int NSLOPE = DIM == 2 ? 2 : 4;
+  static constexpr int NPLANES = DIM + NSLOPE;
+  // plane holding the slope of face field f (0 = Bx, 1 = By, 2 = Bz) along
+  // direction t; -1 for the slopes along z, which are identically zero
+  // (compute_limited_slope<IZ> samples its minus neighbour at k + 1,
+  // MHDBaseFunctor3D.h:128-158)
+  __host__ __device__ static constexpr int
+  slope_plane(int f, int t)
+  {
+    return (f == 0 && t == 1)   ? DIM
+           : (f == 1 && t == 0) ? DIM + 1
+           : (f == 2 && t == 0) ? DIM + 2
+           : (f == 2 && t == 1) ? DIM + 3
+                                : -1;
+  }
+};
+
+inline int
+face_data_planes(int dim)
+{
+  return dim == 3 ? FaceData<3>::NPLANES : FaceData<2>::NPLANES;
+}
 
 template <int DIM>
 struct FluxComps
@@ -182,6 +217,7 @@ struct Grid
   int     bc[6];
   int     riemann;
   R       gamma0, smallr, smallp, smallc, slope_type;
+  R       entho; // 1 / (gamma0 - 1)
   double  cfl, dx, dy, dz;
   double  idx, idy, idz; // 1/dx, 1/dy, 1/dz (used by the fast builds only)
   Box     box[BOX_COUNT];
@@ -461,6 +497,23 @@ k_advance(DevState * st)
 
 // ---------------------------------------------------------------- trace
 
+// compute_limited_slope<dir> of a face-centred field component
+// (MHDBaseFunctor2D.h:129-155, MHDBaseFunctor3D.h:128-158).  In 3D the
+// reference samples the minus neighbour along z at k + 1, so the z slope is
+// identically zero; that is kept.
+template <class R, int DIM>
+__device__ __forceinline__ R
+face_field_slope(const Grid<R> & G, const R * __restrict__ U, int64_t c, int comp, int dir)
+{
+  const int64_t cv = c + comp * G.sv;
+  if (dir == 0)
+    return slope_limited(U[cv], U[cv + 1], U[cv - 1], G.slope_type);
+  if (dir == 1)
+    return slope_limited(U[cv], U[cv + G.sj], U[cv - G.sj], G.slope_type);
+  return slope_limited(U[cv], U[cv + G.sk], U[cv + G.sk], G.slope_type);
+}
+
+
 // Slopes, half step and edge field over the box [g-1, size-g+1]^DIM:
 //  * ComputeSlopesFunctor (MHDRunFunctors2D.h:164-248, 3D:168-273): MC-type
 //    limited slopes per direction; the face-normal field slope is the
@@ -550,6 +603,15 @@ trace_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
 #pragma unroll
     for (int v = 0; v < NV; ++v)
       S[c + (d * NV + v) * sv] = s[d][v];
+  // transverse slopes of the face-centred field for the edge stage
+  R * H = B.H;
+  H[c + FaceData<DIM>::slope_plane(0, 1) * sv] = face_field_slope<R, DIM>(G, U, c, IA, 1);
+  H[c + FaceData<DIM>::slope_plane(1, 0) * sv] = face_field_slope<R, DIM>(G, U, c, IB, 0);
+  if constexpr (DIM == 3)
+  {
+    H[c + FaceData<DIM>::slope_plane(2, 0) * sv] = face_field_slope<R, DIM>(G, U, c, IC, 0);
+    H[c + FaceData<DIM>::slope_plane(2, 1) * sv] = face_field_slope<R, DIM>(G, U, c, IC, 1);
+  }
 
   // Hancock half step
   const R r = q[ID], p = q[IP], u = q[IU], v = q[IV], w = q[IW], A = q[IA], Bc = q[IB], C = q[IC];
@@ -669,6 +731,45 @@ face_source(const Grid<R> & G, const R * __restrict__ E, int64_t c, int d, R dtd
   }
 }
 
+// Half-step normal field of face (c, d): B_d + face_source.  The fast builds
+// evaluate it with explicitly rounded operations (no contraction, the exact
+// factor 1/2 folded into dt/dx), so that every kernel that evaluates it
+// obtains the same bits whatever the surrounding code; the exact build keeps
+// the reference's statement.
+template <class R, int DIM>
+__device__ __forceinline__ R
+face_field(const Grid<R> & G, const R * __restrict__ U, const R * __restrict__ E, int64_t c, int d,
+           R dtdx, R dtdy, R dtdz)
+{
+  const R b = U[c + (IA + d) * G.sv];
+  if constexpr (kExactOrder)
+    return b + face_source<R, DIM>(G, E, c, d, dtdx, dtdy, dtdz);
+  else
+  {
+    const int64_t sj = G.sj, sk = G.sk, n1 = G.sv;
+    const R       hx = R(0.5) * dtdx, hy = R(0.5) * dtdy, hz = R(0.5) * dtdz;
+    R             s;
+    if constexpr (DIM == 2)
+    {
+      if (d == 0)
+        s = rn_mul(rn_sub(E[c + sj], E[c]), hy);
+      else
+        s = rn_mul(rn_sub(E[c], E[c + 1]), hx);
+    }
+    else
+    {
+      const R *Ex = E, *Ey = E + n1, *Ez = E + 2 * n1;
+      if (d == 0)
+        s = rn_sub(rn_mul(rn_sub(Ez[c + sj], Ez[c]), hy), rn_mul(rn_sub(Ey[c + sk], Ey[c]), hz));
+      else if (d == 1)
+        s = rn_sub(rn_mul(rn_sub(Ex[c + sk], Ex[c]), hz), rn_mul(rn_sub(Ez[c + 1], Ez[c]), hx));
+      else
+        s = rn_sub(rn_mul(rn_sub(Ey[c + 1], Ey[c]), hx), rn_mul(rn_sub(Ex[c + sj], Ex[c]), hy));
+    }
+    return rn_add(b, s);
+  }
+}
+
 // ---------------------------------------------------------------- face fluxes
 
 // Reconstruction + Riemann solve of ComputeFluxAndUpdateAlongDirFunctor<dir>
@@ -704,7 +805,7 @@ face_states(const Grid<R> & G, const Buffers<R> & B, int64_t c, State<R> & qL, S
   qR[IP] = sel_max(smallp * qR[ID], qR[IP]);
   qL[ID] = sel_max(smallR, qL[ID]);
   qL[IP] = sel_max(smallp * qL[ID], qL[IP]);
-  qR[nrm] = B.Uin[c + nrm * sv] + face_source<R, DIM>(G, B.E, c, d, dtdx, dtdy, dtdz);
+  qR[nrm] = face_field<R, DIM>(G, B.Uin, B.E, c, d, dtdx, dtdy, dtdz);
   qL[nrm] = qR[nrm];
   if constexpr (d > 0)
   {
@@ -739,10 +840,11 @@ flux_face(const Grid<R> & G, const Buffers<R> & B, int i, int j, int k)
   const int64_t c = cell_at(G, i, j, k);
   State<R>      qR, qL, fl;
   face_states<R, DIM, d>(G, B, c, qL, qR);
+  B.H[c + d * G.sv] = qR[IA]; // half-step normal field of the face
 #pragma unroll
   for (int v = 0; v < NV; ++v)
     fl[v] = R(0);
-  riemann(G.riemann, qL, qR, fl, G.gamma0);
+  riemann(G.riemann, qL, qR, fl, G.gamma0, G.entho);
   store_face_flux<R, DIM, d>(G, B, c, fl);
 }
 
@@ -771,22 +873,6 @@ k_flux(const Grid<R> G, Buffers<R> B)
 }
 
 // ---------------------------------------------------------------- edge EMFs
-
-// compute_limited_slope<dir> of a face-centred field component
-// (MHDBaseFunctor2D.h:129-155, MHDBaseFunctor3D.h:128-158).  In 3D the
-// reference samples the minus neighbour along z at k + 1, so the z slope is
-// identically zero; that is kept.
-template <class R, int DIM>
-__device__ __forceinline__ R
-face_field_slope(const Grid<R> & G, const R * __restrict__ U, int64_t c, int comp, int dir)
-{
-  const int64_t cv = c + comp * G.sv;
-  if (dir == 0)
-    return slope_limited(U[cv], U[cv + 1], U[cv - 1], G.slope_type);
-  if (dir == 1)
-    return slope_limited(U[cv], U[cv + G.sj], U[cv - G.sj], G.slope_type);
-  return slope_limited(U[cv], U[cv + G.sk], U[cv + G.sk], G.slope_type);
-}
 
 // ReconstructEdgeComputeEmfAndUpdateFunctor (MHDRunFunctors2D.h:1291-1534,
 // 3D:1331-1778) for edges [g, size-g]^DIM; blockIdx.y is the edge direction
@@ -823,10 +909,20 @@ emf_edge(const Grid<R> & G, const Buffers<R> & B, int i, int j, int k)
     const int64_t c0 = cc + (r0 ? o0 : 0); // face carrying B_{d0}
     const int64_t c1 = cc + (r1 ? o1 : 0); // face carrying B_{d1}
     constexpr int dd1 = DIM == 2 ? 1 : d1;
-    const R B0 = U[c0 + (IA + d0) * sv] + face_source<R, DIM>(G, B.E, c0, d0, dtdx, dtdy, dtdz);
-    const R dB0d1 = face_field_slope<R, DIM>(G, U, c0, IA + d0, dd1);
-    const R B1 = U[c1 + (IA + dd1) * sv] + face_source<R, DIM>(G, B.E, c1, dd1, dtdx, dtdy, dtdz);
-    const R dB1d0 = face_field_slope<R, DIM>(G, U, c1, IA + dd1, d0);
+    // half-step face fields: stored by the flux stage on the face box; the
+    // layer below it (index g-1 along the other transverse direction) is
+    // evaluated here with the same expression
+    const int id0 = d0 == 0 ? i : j;
+    const int id1 = dd1 == 1 ? j : k;
+    const R   B0 = (r1 && id1 == G.g) ? face_field<R, DIM>(G, U, B.E, c0, d0, dtdx, dtdy, dtdz)
+                                      : B.H[c0 + d0 * sv];
+    const R   B1 = (r0 && id0 == G.g) ? face_field<R, DIM>(G, U, B.E, c1, dd1, dtdx, dtdy, dtdz)
+                                      : B.H[c1 + dd1 * sv];
+    // transverse face-field slopes from the trace stage (zero along z)
+    constexpr int p0 = FaceData<DIM>::slope_plane(d0, dd1);
+    constexpr int p1 = FaceData<DIM>::slope_plane(dd1, d0);
+    const R       dB0d1 = p0 < 0 ? R(0) : B.H[c0 + p0 * sv];
+    const R       dB1d0 = p1 < 0 ? R(0) : B.H[c1 + p1 * sv];
     State<R> & q = qe[e];
 #pragma unroll
     for (int v = 0; v < NV; ++v)
@@ -1013,6 +1109,7 @@ make_grid(const mhd_params & p)
     G.bc[f] = p.boundary[f];
   G.riemann = p.riemann;
   G.gamma0 = R(p.gamma0);
+  G.entho = R(1) / (G.gamma0 - R(1));
   G.smallr = R(p.smallr);
   G.smallc = R(p.smallc);
   // smallp = smallc^2 / gamma0 in real_t (HydroParams.cpp:438)

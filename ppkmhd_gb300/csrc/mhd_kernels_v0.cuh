@@ -420,7 +420,7 @@ v0_flux_face(const Grid<R> & G, const R * __restrict__ T, R * __restrict__ F, in
 #pragma unroll
   for (int v = 0; v < NV; ++v)
     fl[v] = R(0);
-  riemann(G.riemann, qL, qR, fl, G.gamma0);
+  riemann(G.riemann, qL, qR, fl, G.gamma0, G.entho);
   if constexpr (d > 0)
   {
     swap_vals(fl[IU], fl[IU + d]);

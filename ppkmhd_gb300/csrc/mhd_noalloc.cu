@@ -112,7 +112,7 @@ step(const mhd_params & p, const void * U_in, void * U_out, double t, double * d
   const size_t  b8 = align256(n * NV * sizeof(R));
   const size_t  need = 2 * b8 + align256(n * NV * dim * sizeof(R)) +
                       2 * align256(n * ne * sizeof(R)) + align256(n * nf * dim * sizeof(R)) +
-                      align256(sizeof(DevState));
+                      align256(n * face_data_planes(dim) * sizeof(R)) + align256(sizeof(DevState));
   if (need > (size_t)MHD_NOALLOC_SCRATCH_BYTES)
   {
     err = "grid needs " + std::to_string(need) + " bytes of scratch; the no-allocation path has " +
@@ -138,6 +138,8 @@ step(const mhd_params & p, const void * U_in, void * U_out, double t, double * d
   q += align256(n * nf * dim * sizeof(R));
   B.Em = reinterpret_cast<R *>(q);
   q += align256(n * ne * sizeof(R));
+  B.H = reinterpret_cast<R *>(q);
+  q += align256(n * face_data_planes(dim) * sizeof(R));
   B.st = reinterpret_cast<DevState *>(q);
 
   auto nb = [](int64_t cnt, int th) { return (unsigned)((cnt + th - 1) / th); };

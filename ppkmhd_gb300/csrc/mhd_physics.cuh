@@ -72,14 +72,32 @@ swap_vals(R & a, R & b)
 #endif
 constexpr bool kExactOrder = MHD_EXACT_BUILD != 0;
 
-// Reciprocal, reciprocal square root and square root of the fast builds.
-// FP64 keeps the CUDA library's correctly rounded reciprocal, its rsqrt and
-// the IEEE square root (a Newton-Raphson refinement of the hardware
-// approximations measured 13 % slower on the FP64-bound kernels).  FP32
-// uses the hardware approximations alone (about 1 ulp).
+// Reciprocal, reciprocal square root and square root of the fast builds
+// (GB300 issues 2 FP64 FMAs per SM per cycle, so FP64 operation counts set
+// the speed of the FP64 kernels).
+//  * FP64 reciprocal: the hardware approximation rcp.approx.ftz.f64 (relative
+//    error below 2^-18 on 1e6 log-uniform samples) refined by one third-order
+//    Newton step y (1 + e + e^2), e = 1 - x y, whose relative error is e^3:
+//    at most 0.51 ulp (99.97 % of the samples correctly rounded) in 3 FMAs,
+//    against 5 FP64 operations for the correctly rounded library reciprocal.
+//    Arguments whose reciprocal is not a normal number (zero, subnormal,
+//    |x| >= 2^1021, infinite, NaN) take the library reciprocal.
+//  * FP64 rsqrt: the library's (within 0.51 ulp; 5 FP64 operations).
+//  * FP64 square root: x * rsqrt(x) for positive finite x (within ~1 ulp,
+//    6 FP64 operations against 8 for the IEEE square root); other arguments
+//    take the IEEE square root.
+//  * FP32: the hardware approximations alone (about 1 ulp).
 __device__ __forceinline__ double
 rcp(double x)
 {
+  const unsigned ex = ((unsigned)__double2hiint(x) >> 20) & 0x7ffu;
+  if (ex - 1u < 0x7fcu) // 1 <= biased exponent <= 0x7fc
+  {
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    const double e = fma(-x, y, 1.0);
+    return fma(y, fma(e, e, e), y);
+  }
   return __drcp_rn(x);
 }
 __device__ __forceinline__ float
@@ -101,8 +119,6 @@ rsq(float x)
   asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
-// FP32: sqrt(x) = x / sqrt(x) for positive finite arguments (zero, negative,
-// infinite and NaN arguments take the IEEE square root); FP64: IEEE.
 __device__ __forceinline__ float
 fsqrt(float x)
 {
@@ -113,7 +129,44 @@ fsqrt(float x)
 __device__ __forceinline__ double
 fsqrt(double x)
 {
+  const long long b = __double_as_longlong(x);
+  if (b > 0 && b < 0x7ff0000000000000LL)
+    return x * rsq(x);
   return sqrt(x);
+}
+
+// Round-to-nearest add, subtract and multiply that the compiler never
+// contracts into fused multiply-adds: values computed with them are the same
+// bits in every kernel that evaluates them.
+__device__ __forceinline__ double
+rn_add(double a, double b)
+{
+  return __dadd_rn(a, b);
+}
+__device__ __forceinline__ float
+rn_add(float a, float b)
+{
+  return __fadd_rn(a, b);
+}
+__device__ __forceinline__ double
+rn_sub(double a, double b)
+{
+  return __dsub_rn(a, b);
+}
+__device__ __forceinline__ float
+rn_sub(float a, float b)
+{
+  return __fsub_rn(a, b);
+}
+__device__ __forceinline__ double
+rn_mul(double a, double b)
+{
+  return __dmul_rn(a, b);
+}
+__device__ __forceinline__ float
+rn_mul(float a, float b)
+{
+  return __fmul_rn(a, b);
 }
 
 // Selection by comparison.  GB300 runs FP64 comparisons on the narrow FP64
@@ -168,8 +221,8 @@ max5(R a0, R a1, R a2, R a3, R a4)
 // Squares of both fast magnetosonic speeds (normal field in slot IA, then in
 // slot IB) of one state with one reciprocal of the density
 // (mhd_utils.h:89-117).  The callers take the square root of the largest
-// only: the square root is correctly rounded and monotone, so
-// max_i sqrt(x_i) = sqrt(max_i x_i) exactly.
+// only: the square root is monotone, so max_i sqrt(x_i) = sqrt(max_i x_i)
+// (exactly for a correctly rounded root, within the ~1 ulp of fsqrt).
 template <class R>
 __device__ __forceinline__ void
 fast_speeds2_xy(const State<R> & q, R gamma0, R & cfx2, R & cfy2)
@@ -524,9 +577,8 @@ riemann_hlld(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
 // square roots and 2 rsqrt instead of ~28 divides and 6 square roots.
 template <class R>
 __device__ void
-riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
+riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R entho)
 {
-  const R entho = rcp(gamma0 - R(1));
   const R a = R(0.5) * (ql[IA] + qr[IA]);
   const R a2 = a * a;
   const R sgnm = (a >= R(0)) ? R(1) : R(-1);
@@ -676,17 +728,18 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
   flux[IC] = co * uo - a * wo;
 }
 
-// riemann_mhd dispatch (RiemannSolvers_MHD.h:372-392)
+// riemann_mhd dispatch (RiemannSolvers_MHD.h:372-392); entho = 1/(gamma0-1),
+// precomputed once per run for the fast HLLD
 template <class R>
 __device__ __forceinline__ void
-riemann(int solver, State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
+riemann(int solver, State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R entho)
 {
   if (solver == RIEMANN_HLLD)
   {
     if constexpr (kExactOrder)
       riemann_hlld(ql, qr, flux, gamma0);
     else
-      riemann_hlld_fast(ql, qr, flux, gamma0);
+      riemann_hlld_fast(ql, qr, flux, gamma0, entho);
   }
   else if (solver == RIEMANN_HLL)
     riemann_hll(ql, qr, flux, gamma0);

@@ -139,6 +139,7 @@ public:
   R *          E = nullptr;
   R *          F = nullptr;
   R *          Em = nullptr;
+  R *          H = nullptr;  // version 2: face data (FaceData<DIM>)
   R *          T = nullptr;  // versions 0/1: stored trace states
   R *          D = nullptr;  // versions 0/1 in 3D: transverse face-field slopes
   int          version = 2;
@@ -168,7 +169,7 @@ public:
       if (graph_pair[q])
         cudaGraphExecDestroy(graph_pair[q]);
     }
-    R * bufs[] = { U, U2, Q, Q2, S, E, F, Em, T, D };
+    R * bufs[] = { U, U2, Q, Q2, S, E, F, Em, H, T, D };
     for (R * b : bufs)
       if (b)
         cudaFree(b);
@@ -235,6 +236,7 @@ public:
     {
       MHD_CK(cudaMalloc(&Q2, n * NV * sizeof(R)));
       MHD_CK(cudaMalloc(&S, n * NV * dim * sizeof(R)));
+      MHD_CK(cudaMalloc(&H, n * face_data_planes(dim) * sizeof(R)));
     }
     else
     {
@@ -256,6 +258,8 @@ public:
         MHD_CK(cudaMemsetAsync(b, 0, n * NV * sizeof(R), stream));
     if (S)
       MHD_CK(cudaMemsetAsync(S, 0, n * NV * dim * sizeof(R), stream));
+    if (H)
+      MHD_CK(cudaMemsetAsync(H, 0, n * face_data_planes(dim) * sizeof(R), stream));
     if (T)
       MHD_CK(cudaMemsetAsync(T, 0, n * NV * (dim == 3 ? 18 : 8) * sizeof(R), stream));
     if (D)
@@ -295,6 +299,7 @@ public:
     B.E = E;
     B.F = F;
     B.Em = Em;
+    B.H = H;
     B.st = st;
     return B;
   }
@@ -582,8 +587,11 @@ public:
           return MHD_ERR_CUDA;
         }
         (pair ? graph_pair : graph)[parity] = ex;
+        // upload now so that the first replay does not pay for it
+        MHD_CK(cudaGraphUpload(ex, stream));
       }
     }
+    MHD_CK(cudaStreamSynchronize(stream));
     return MHD_OK;
   }
 

@@ -222,6 +222,7 @@ flux_face_mlp(const Grid<float> & G, const Buffers<float> & B, const SurrogateDe
   {
     State<float> qL, qR;
     face_states<float, DIM, d>(G, B, c, qL, qR);
+    B.H[c + d * G.sv] = qR[IA]; // half-step normal field of the face
     float l7[7], r7[7], sc[7], Fc[7];
     to_face7(qL, l7);
     to_face7(qR, r7);

@@ -131,14 +131,18 @@ def test_ensemble_equals_independent_runs(mhdlib, precision, exact):
         s.set_state(U.astype(s.real))
         s.run(9)
         a, b = ens.get_state(q), s.get_state()
-        if exact or precision == 32:
-            # identical kernel bodies and arithmetic: bitwise
+        if exact:
+            # identical kernel bodies and arithmetic without contraction: bitwise
             assert np.array_equal(a, b), (q, np.abs(a - b).max())
             assert ens.time(q) == s.time()
-        else:
+        elif precision == 64:
             # FMA contraction may differ between the two instantiations
             assert rel_l1(a, b).max() <= 1e-13
             assert np.allclose(ens.time(q), s.time(), rtol=1e-14, atol=0)
+        else:
+            # FP32 with contraction: a few ulp after 9 iterations
+            assert rel_l1(a.astype(np.float64), b.astype(np.float64)).max() <= 2e-6, q
+            assert np.allclose(ens.time(q), s.time(), rtol=1e-6, atol=0)
 
 
 @pytest.mark.gpu
