@@ -216,6 +216,39 @@ max5(R a0, R a1, R a2, R a3, R a4)
 {
   return sel_max(sel_max(sel_max(sel_max(a0, a1), a2), a3), a4);
 }
+// Sign tests and |d| <= t (t >= 0) of the fast FP64 build on bit patterns
+// (integer pipe).  They agree with the FP comparisons for every non-NaN
+// argument, -0 included.
+template <class R>
+__device__ __forceinline__ bool
+gt0(R x)
+{
+  if constexpr (sizeof(R) == 8 && !kExactOrder)
+    return __double_as_longlong(x) > 0;
+  else
+    return x > R(0);
+}
+template <class R>
+__device__ __forceinline__ bool
+ge0(R x)
+{
+  if constexpr (sizeof(R) == 8 && !kExactOrder)
+  {
+    const long long b = __double_as_longlong(x);
+    return b >= 0 || (b & 0x7fffffffffffffffLL) == 0;
+  }
+  else
+    return x >= R(0);
+}
+template <class R>
+__device__ __forceinline__ bool
+abs_le(R d, R t)
+{
+  if constexpr (sizeof(R) == 8 && !kExactOrder)
+    return (__double_as_longlong(d) & 0x7fffffffffffffffLL) <= __double_as_longlong(t);
+  else
+    return fabs(d) <= t;
+}
 
 
 // Squares of both fast magnetosonic speeds (normal field in slot IA, then in
@@ -284,7 +317,8 @@ limited_slope(R q, R qp, R qm, R slope_type)
 // on IEEE bit patterns (integer pipe): magnitudes of doubles order like their
 // bit patterns, and the scalings by slope_type (1 or 2) and by 1/2 are exact,
 // so the result equals limited_slope except for the sign of a zero result and
-// when a product underflows.  5 floating-point operations instead of 11.
+// when a product underflows.  5 floating-point operations instead of 11
+// (3 in FP64).
 __device__ __forceinline__ long long
 fbits(double x)
 {
@@ -318,13 +352,30 @@ limited_slope_bits(R q, R qp, R qm, R slope_type)
   // dlft * drgt <= 0: opposite signs or a zero
   if (((ia ^ ib) & sign) != 0 || aa == 0 || ab == 0)
     return R(0);
-  R m = from_fbits(aa < ab ? aa : ab, R(0));
-  if (slope_type == R(2))
-    m = m + m;
-  const I hc = fbits(R(0.5) * c) & ~sign;
-  const I mb = fbits(m);
-  const I r = mb < hc ? mb : hc;
-  return from_fbits(r | (fbits(c) & sign), R(0));
+  if constexpr (sizeof(R) == 8)
+  {
+    // FP64: the doubling and the halving on the exponent field too, so the
+    // limiter costs 3 FP64 operations.  Exact for normal numbers; 2m
+    // saturates at infinity and |c|/2 below 2^-1022 is taken as zero.
+    constexpr long long one = 1LL << 52, inf = 0x7ff0000000000000LL;
+    long long mb = aa < ab ? aa : ab;
+    if (fbits(slope_type) == fbits(R(2)))
+      mb = mb < one ? (mb << 1) : (mb + one < inf ? mb + one : inf);
+    const long long cb = fbits(c) & ~sign;
+    const long long hc = cb >= 2 * one ? cb - one : 0;
+    const long long r = mb < hc ? mb : hc;
+    return from_fbits(r | (fbits(c) & sign), R(0));
+  }
+  else
+  {
+    R m = from_fbits(aa < ab ? aa : ab, R(0));
+    if (slope_type == R(2))
+      m = m + m;
+    const I hc = fbits(R(0.5) * c) & ~sign;
+    const I mb = fbits(m);
+    const I r = mb < hc ? mb : hc;
+    return from_fbits(r | (fbits(c) & sign), R(0));
+  }
 }
 
 template <class R>
@@ -581,7 +632,7 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R ent
 {
   const R a = R(0.5) * (ql[IA] + qr[IA]);
   const R a2 = a * a;
-  const R sgnm = (a >= R(0)) ? R(1) : R(-1);
+  const R sgnm = ge0(a) ? R(1) : R(-1);
 
   const R rl = ql[ID], pl = ql[IP], ul = ql[IU], vl = ql[IV], wl = ql[IW], bl = ql[IB],
           cl = ql[IC];
@@ -628,7 +679,7 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R ent
   R       vstarl = vl, wstarl = wl, bstarl = bl, cstarl = cl;
   {
     const R estar = rl * slu * sls - a2;
-    if (!(a2 > R(0) && fabs(estar - a2) <= R(1e-8) * a2))
+    if (!(gt0(a2) && abs_le(estar - a2, R(1e-8) * a2)))
     {
       const R ie = rcp(estar);
       const R el = rl * slu * slu - a2;
@@ -653,7 +704,7 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R ent
   R       vstarr = vr, wstarr = wr, bstarr = br, cstarr = cr;
   {
     const R estar = rr * sru * srs - a2;
-    if (!(a2 > R(0) && fabs(estar - a2) <= R(1e-8) * a2))
+    if (!(gt0(a2) && abs_le(estar - a2, R(1e-8) * a2)))
     {
       const R ie = rcp(estar);
       const R er = rr * sru * sru - a2;
@@ -672,19 +723,19 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R ent
   const R sar = ustar + fabs(a) * rsr;
 
   R ro, uo, vo, wo, bo, co, ptoto, etoto, vdotbo;
-  if (sl > R(0))
+  if (gt0(sl))
   {
     ro = rl; uo = ul; vo = vl; wo = wl; bo = bl; co = cl;
     ptoto = ptotl; etoto = etotl; vdotbo = vdotbl;
   }
-  else if (sal > R(0))
+  else if (gt0(sal))
   {
     ro = rstarl; uo = ustar; vo = vstarl; wo = wstarl; bo = bstarl; co = cstarl;
     ptoto = ptotstar; etoto = etotstarl; vdotbo = vdotbstarl;
   }
-  else if (!(ustar > R(0)) && !(sar > R(0)))
+  else if (!gt0(ustar) && !gt0(sar))
   {
-    if (sr > R(0))
+    if (gt0(sr))
     {
       ro = rstarr; uo = ustar; vo = vstarr; wo = wstarr; bo = bstarr; co = cstarr;
       ptoto = ptotstar; etoto = etotstarr; vdotbo = vdotbstarr;
@@ -706,7 +757,7 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R ent
     uo = ustar;
     ptoto = ptotstar;
     vdotbo = ustar * a + vo * bo + wo * co;
-    if (ustar > R(0))
+    if (gt0(ustar))
     {
       ro = rstarl;
       etoto = etotstarl - sgnm * sqrrstarl * (vdotbstarl - vdotbo);
@@ -885,8 +936,27 @@ mag_riemann2d_hlld(const State<R> (&q)[4], const R (&e)[4], R gamma0, R smallc)
          SAT * SAB / (SAT - SAB) * (AstarT - AstarB) + SAR * SAL / (SAR - SAL) * (BstarR - BstarL);
 }
 
-// The same 2D HLLD solve with shared reciprocals: 12 reciprocals, 16 square
-// roots and 16 rsqrt instead of ~75 divides and 32 square roots.
+// max_i |n_i| / sqrt(r_i) over four candidates with r_i > 0, with one rsqrt
+// instead of four: a knock-out between pairs compares n_i^2 r_j with
+// n_j^2 r_i (two FP64 multiplies and an integer-keyed compare), and only the
+// winner is evaluated.  The result is the largest candidate, or within one
+// rounding of it when two candidates tie to the last bits.
+template <class R>
+__device__ __forceinline__ R
+alfven_max4(R n0, R r0, R n1, R r1, R n2, R r2, R n3, R r3)
+{
+  const R    w0 = n0 * n0, w1 = n1 * n1, w2 = n2 * n2, w3 = n3 * n3;
+  const bool s1 = order_key(w1 * r0) > order_key(w0 * r1);
+  const R    na = s1 ? n1 : n0, ra = s1 ? r1 : r0, wa = s1 ? w1 : w0;
+  const bool s3 = order_key(w3 * r2) > order_key(w2 * r3);
+  const R    nb = s3 ? n3 : n2, rb = s3 ? r3 : r2, wb = s3 ? w3 : w2;
+  const bool sb = order_key(wb * ra) > order_key(wa * rb);
+  return fabs(sb ? nb : na) * rsq(sb ? rb : ra);
+}
+
+// The same 2D HLLD solve with shared reciprocals: 12 reciprocals, 10 square
+// roots and 12 rsqrt (4 in FP64, through alfven_max4) instead of ~75
+// divides and 32 square roots.
 template <class R>
 __device__ R
 mag_riemann2d_hlld_fast(const State<R> (&q)[4], const R (&e)[4], R gamma0, R smallc)
@@ -950,14 +1020,25 @@ mag_riemann2d_hlld_fast(const State<R> (&q)[4], const R (&e)[4], R gamma0, R sma
   const R rstarRRx = rRR * fRRx, BstarRR = bRR * fRRx, rstarRRy = rRR * fRRy, AstarRR = aRR * fRRy;
   const R rstarRR = rstarRRx * fRRy;
 
-  const R calfvenL = max5(fabs(aLR) * rsq(rstarLRx), fabs(AstarLR) * rsq(rstarLR),
-                          fabs(aLL) * rsq(rstarLLx), fabs(AstarLL) * rsq(rstarLL), smallc);
-  const R calfvenR = max5(fabs(aRR) * rsq(rstarRRx), fabs(AstarRR) * rsq(rstarRR),
-                          fabs(aRL) * rsq(rstarRLx), fabs(AstarRL) * rsq(rstarRL), smallc);
-  const R calfvenB = max5(fabs(bLL) * rsq(rstarLLy), fabs(BstarLL) * rsq(rstarLL),
-                          fabs(bRL) * rsq(rstarRLy), fabs(BstarRL) * rsq(rstarRL), smallc);
-  const R calfvenT = max5(fabs(bLR) * rsq(rstarLRy), fabs(BstarLR) * rsq(rstarLR),
-                          fabs(bRR) * rsq(rstarRRy), fabs(BstarRR) * rsq(rstarRR), smallc);
+  R calfvenL, calfvenR, calfvenB, calfvenT;
+  if constexpr (sizeof(R) == 8)
+  {
+    calfvenL = sel_max(alfven_max4(aLR, rstarLRx, AstarLR, rstarLR, aLL, rstarLLx, AstarLL, rstarLL), smallc);
+    calfvenR = sel_max(alfven_max4(aRR, rstarRRx, AstarRR, rstarRR, aRL, rstarRLx, AstarRL, rstarRL), smallc);
+    calfvenB = sel_max(alfven_max4(bLL, rstarLLy, BstarLL, rstarLL, bRL, rstarRLy, BstarRL, rstarRL), smallc);
+    calfvenT = sel_max(alfven_max4(bLR, rstarLRy, BstarLR, rstarLR, bRR, rstarRRy, BstarRR, rstarRR), smallc);
+  }
+  else
+  {
+    calfvenL = max5(fabs(aLR) * rsq(rstarLRx), fabs(AstarLR) * rsq(rstarLR),
+                    fabs(aLL) * rsq(rstarLLx), fabs(AstarLL) * rsq(rstarLL), smallc);
+    calfvenR = max5(fabs(aRR) * rsq(rstarRRx), fabs(AstarRR) * rsq(rstarRR),
+                    fabs(aRL) * rsq(rstarRLx), fabs(AstarRL) * rsq(rstarRL), smallc);
+    calfvenB = max5(fabs(bLL) * rsq(rstarLLy), fabs(BstarLL) * rsq(rstarLL),
+                    fabs(bRL) * rsq(rstarRLy), fabs(BstarRL) * rsq(rstarRL), smallc);
+    calfvenT = max5(fabs(bLR) * rsq(rstarLRy), fabs(BstarLR) * rsq(rstarLR),
+                    fabs(bRR) * rsq(rstarRRy), fabs(BstarRR) * rsq(rstarRR), smallc);
+  }
   const R SAL = sel_min(ustar - calfvenL, R(0));
   const R SAR = sel_max(ustar + calfvenR, R(0));
   const R SAB = sel_min(vstar - calfvenB, R(0));
