@@ -352,7 +352,7 @@ int mhd_surrogate_stats(mhd_ctx *ctx, int64_t *faces_network, int64_t *faces_tot
  * place, as the reference's make_boundaries(data_in) does).  Every
  * intermediate lives in a file-scope __device__ array of
  * MHD_NOALLOC_SCRATCH_BYTES; grids that need more return MHD_ERR_TOO_LARGE
- * (32 MiB holds about 300^2 interior cells in 2D or 35^3 in 3D in FP64, twice
+ * (32 MiB holds about 280^2 interior cells in 2D or 33^3 in 3D in FP64, twice
  * as many in FP32).  t is the current time (dt is clipped to p->tEnd; when
  * t >= tEnd - 1e-14 nothing is computed and *dt = 0).  On return *dt holds
  * the dt of the iteration; the call synchronises `stream` (a cudaStream_t,

@@ -959,7 +959,7 @@ alfven_max4(R n0, R r0, R n1, R r1, R n2, R r2, R n3, R r3)
 // divides and 32 square roots.
 template <class R>
 __device__ R
-mag_riemann2d_hlld_fast(const State<R> (&q)[4], const R (&e)[4], R gamma0, R smallc)
+mag_riemann2d_hlld_fast(const State<R> (&q)[4], R gamma0, R smallc)
 {
   const State<R> &qLL = q[0], &qRL = q[1], &qLR = q[2], &qRR = q[3];
   R               cFastLLx, cFastLLy, cFastLRx, cFastLRy, cFastRLx, cFastRLy, cFastRRx, cFastRRy;
@@ -977,14 +977,15 @@ mag_riemann2d_hlld_fast(const State<R> (&q)[4], const R (&e)[4], R gamma0, R sma
   const R ST = max4(vLL, vLR, vRL, vRR) + cym;
   const bool SB_pos = !signbit(SB), ST_pos = !signbit(ST);
   const bool SL_pos = !signbit(SL), SR_pos = !signbit(SR);
+  // corner regions: the corner state's own emf u b - v a
   if (SB_pos && SL_pos)
-    return e[0];
+    return uLL * qLL[IB] - vLL * qLL[IA];
   if (SB_pos && !SR_pos)
-    return e[1];
+    return uRL * qRL[IB] - vRL * qRL[IA];
   if (!SB_pos && !ST_pos && SL_pos)
-    return e[2];
+    return uLR * qLR[IB] - vLR * qLR[IA];
   if (!SB_pos && !ST_pos && !SR_pos)
-    return e[3];
+    return uRR * qRR[IB] - vRR * qRR[IA];
 
   const R rLL = qLL[ID], rLR = qLR[ID], rRL = qRL[ID], rRR = qRR[ID];
   const R aLL = qLL[IA], aLR = qLR[IA], aRL = qRL[IA], aRR = qRR[IA];
@@ -1108,14 +1109,16 @@ compute_emf(int edir, const State<R> (&qe)[4], R gamma0, R smallc)
   q[3][IB] = q[1][IB];
   q[0][IW] = qRT[iw]; q[1][IW] = qLT[iw]; q[2][IW] = qRB[iw]; q[3][IW] = qLB[iw];
   q[0][IC] = qRT[ic]; q[1][IC] = qLT[ic]; q[2][IC] = qRB[ic]; q[3][IC] = qLB[ic];
-  R e[4];
-#pragma unroll
-  for (int c = 0; c < 4; ++c)
-    e[c] = q[c][IU] * q[c][IB] - q[c][IV] * q[c][IA];
   if constexpr (kExactOrder)
+  {
+    R e[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+      e[c] = q[c][IU] * q[c][IB] - q[c][IV] * q[c][IA];
     return mag_riemann2d_hlld(q, e, gamma0, smallc);
+  }
   else
-    return mag_riemann2d_hlld_fast(q, e, gamma0, smallc);
+    return mag_riemann2d_hlld_fast(q, gamma0, smallc);
 }
 
 } // namespace MHD_VARIANT_TAG

@@ -1,0 +1,36 @@
+"""Accuracy of the fast builds' FP64 reciprocal and square root.
+
+The fast FP64 build replaces the library's correctly rounded reciprocal by
+one third-order Newton step on the hardware approximation and the IEEE
+square root by x * rsqrt(x) (ppkmhd_gb300/csrc/mhd_physics.cuh).  This test
+compiles tests/fast_math_probe.cu against that header and checks their error
+bounds on 2^20 log-uniform arguments over [1e-30, 1e30] against correctly
+rounded host references.
+"""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.mark.gpu
+def test_fast_fp64_reciprocal_and_sqrt_error_bounds(tmp_path):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    exe = str(tmp_path / "fast_math_probe")
+    subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-o", exe,
+                    os.path.join(HERE, "fast_math_probe.cu")], check=True)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True, timeout=300).stdout
+    res = {}
+    for line in out.splitlines():
+        f = line.split()
+        res[f[0]] = (float(f[2]), float(f[4]))
+    # library references: correctly rounded (rsqrt within its documented bound)
+    assert res["drcp_rn"][0] <= 0.5 and res["sqrt"][0] <= 0.5
+    assert res["rsq"][0] <= 0.52
+    # fast reciprocal: relative error e0^3 of the seed on top of one rounding
+    assert res["rcp"][0] <= 0.52 and res["rcp"][1] >= 0.999
+    # x * rsqrt(x): two roundings
+    assert res["fsqrt"][0] <= 1.05 and res["fsqrt"][1] >= 0.5
