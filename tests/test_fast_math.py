@@ -32,5 +32,6 @@ def test_fast_fp64_reciprocal_and_sqrt_error_bounds(tmp_path):
     assert res["rsq"][0] <= 0.52
     # fast reciprocal: relative error e0^3 of the seed on top of one rounding
     assert res["rcp"][0] <= 0.52 and res["rcp"][1] >= 0.999
-    # x * rsqrt(x): two roundings
-    assert res["fsqrt"][0] <= 1.05 and res["fsqrt"][1] >= 0.5
+    # x * rsqrt(x): two roundings (the relative error of rsqrt doubles in ulps
+    # of the product when the two mantissas sit at opposite ends of a binade)
+    assert res["fsqrt"][0] <= 1.6 and res["fsqrt"][1] >= 0.5
