@@ -322,8 +322,10 @@ int mhd_mlp_gradient(mhd_mlp *mlp, const float *features, const float *targets, 
 int mhd_mlp_train(mhd_mlp *mlp, const float *records, int64_t n, int epochs, int batch,
                   float lr, float weight_power, uint64_t seed, float *loss_history);
 
-/* The deployed tensor-core forward pass on features[n][MHD_MLP_FEATURES]
- * -> out[n][8] (the 7 dimensionless dissipation components and a pad). */
+/* Batch forward pass on features[n][MHD_MLP_FEATURES] -> out[n][8] (the 7
+ * dimensionless dissipation components and a pad), on the 5th-generation
+ * tensor cores (tcgen05, FP32 accumulators in TMEM) with the deployed
+ * numerics: BF16 weights and activations, FP32 accumulation, BF16 GELU. */
 int mhd_mlp_forward(mhd_mlp *mlp, const float *features, int64_t n, float *out);
 const char *mhd_mlp_last_error(mhd_mlp *mlp);
 

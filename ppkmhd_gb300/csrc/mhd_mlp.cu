@@ -1,7 +1,8 @@
 // Training and evaluation of the HLLD flux surrogate (mhd_mlp.cuh) on the
 // GPU: feature encoding of harvested face samples, forward + backward passes
 // with per-block partial gradients reduced in a fixed order, Adam, and the
-// tensor-core forward used by the flux stage.  Exposed through the
+// tensor-core forward passes (the warp-level one of the flux stage is in
+// mhd_mlp.cuh; the tcgen05 batch forward below).  Exposed through the
 // mhd_mlp_* entry points of include/ppkmhd_gb300.h.
 //
 // Training arithmetic: FP32 master weights; in MHD_MLP_TRAIN mode the
@@ -302,34 +303,51 @@ k_reduce_adam(const float * __restrict__ partial, int nblocks, float * __restric
   }
 }
 
-// Tensor-core forward (the deployed path) on features: one face per thread.
-__global__ void __launch_bounds__(128)
-k_forward_mma(const uint32_t * __restrict__ pack, const float * __restrict__ feat, int64_t n,
-              float * __restrict__ out)
+// Batch forward on the 5th-generation tensor cores (mlp::block_forward,
+// tcgen05 with accumulators in TMEM) on features: one face per thread, one
+// 128-row tile per block.  status[0] is set when a completion wait reached
+// its limit.  (The flux stage keeps the warp-level mma.sync forward: with
+// one tile in flight per block, the three dependent MMA -> commit -> TMEM
+// round trips per tile made the fused flux stage 2.3x slower.)
+__global__ void __launch_bounds__(kTcRows)
+k_forward_tc(const uint32_t * __restrict__ pack, const float * __restrict__ feat, int64_t n,
+             float * __restrict__ out, int * __restrict__ status)
 {
-  __shared__ __align__(16) uint32_t sw[kPackWords];
-  __shared__ float                  sb[kBiasFloats];
-  __shared__ uint32_t               sx[4][kStageXWords];
-  __shared__ float                  so[4][kStageOFloats];
-  for (int q = threadIdx.x; q < kPackWords; q += blockDim.x)
-    sw[q] = pack[q];
-  for (int q = threadIdx.x; q < kBiasFloats; q += blockDim.x)
-    sb[q] = reinterpret_cast<const float *>(pack + kPackWords)[q];
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint32_t * slot = reinterpret_cast<uint32_t *>(smem + kTcBar + 8);
+  stage_network_tc(pack, smem);
+  if (threadIdx.x == 0)
+    mhd::umma::mbar_init(mhd::umma::smem_addr(smem + kTcBar), 1);
+  if (threadIdx.x < 32)
+    mhd::umma::tmem_alloc(mhd::umma::smem_addr(slot), kTcCols);
+  mhd::umma::fence_before_sync();
   __syncthreads();
-  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  float         f[kIn], u[kBasis], y[kOut], Dn[kOutUsed];
+  mhd::umma::fence_after_sync();
+  const uint32_t tmem = *slot;
+  const int64_t  s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  float          f[kIn], u[kBasis], y[kOut], Dn[kOutUsed];
   for (int q = 0; q < kIn; ++q)
     f[q] = s < n ? feat[s * kFeat + q] : 0.f;
   for (int q = 0; q < kBasis; ++q)
     u[q] = s < n ? feat[s * kFeat + kIn + q] : 0.f;
-  const int warp = threadIdx.x >> 5;
-  warp_forward(sw, sb, sx[warp], so[warp], f, y);
-  if (s < n)
+  uint32_t   parity = 0;
+  const bool ok = block_forward(smem, tmem, parity, f, y);
+  if (ok && s < n)
   {
     combine(y, u, Dn);
     for (int c = 0; c < kOutUsed; ++c)
       out[s * kTgt + c] = Dn[c];
     out[s * kTgt + 7] = 0.f;
+  }
+  if (!ok && threadIdx.x == 0)
+    atomicOr(status, 1);
+  // every thread's TMEM accesses are complete before warp 0 frees it
+  mhd::umma::fence_before_sync();
+  __syncthreads();
+  if (threadIdx.x < 32)
+  {
+    mhd::umma::fence_after_sync();
+    mhd::umma::tmem_dealloc(tmem, kTcCols);
   }
 }
 
@@ -360,6 +378,34 @@ pack_layer(const float * W, int K, int N, uint32_t * out)
         o[0] = w(kt * 16 + 2 * t) | (w(kt * 16 + 2 * t + 1) << 16);
         o[1] = w(kt * 16 + 8 + 2 * t) | (w(kt * 16 + 8 + 2 * t + 1) << 16);
       }
+}
+
+// W[K][N] (row = input, column = output unit) -> W^T[Npad][K] in BF16 (round
+// to nearest even) in the tensor cores' canonical K-major layout; rows
+// n >= N are zero.
+void
+pack_layer_tc(const float * W, int K, int N, int Npad, unsigned char * out)
+{
+  for (int n = 0; n < Npad; ++n)
+    for (int k = 0; k < K; ++k)
+    {
+      const uint16_t v = n < N ? bf16_bits_rn(W[k * N + n]) : (uint16_t)0;
+      std::memcpy(out + mhd::umma::canon_offset(n, k, K), &v, sizeof(v));
+    }
+}
+
+// The tcgen05 network image (kTcPackWords words).
+void
+pack_tc(const float * params, uint32_t * out)
+{
+  unsigned char * w = reinterpret_cast<unsigned char *>(out);
+  pack_layer_tc(params + kOffW1, kIn, kHid, kHid, w + kTcW1);
+  pack_layer_tc(params + kOffW2, kHid, kHid, kHid, w + kTcW2);
+  pack_layer_tc(params + kOffW3, kHid, kOut, kN3, w + kTcW3);
+  float * b = reinterpret_cast<float *>(out + kTcWBytes / 4);
+  std::memcpy(b, params + kOffB1, kHid * sizeof(float));
+  std::memcpy(b + kHid, params + kOffB2, kHid * sizeof(float));
+  std::memcpy(b + 2 * kHid, params + kOffB3, kOut * sizeof(float));
 }
 
 uint64_t
@@ -704,18 +750,26 @@ extern "C"
     if (!m || !features || n <= 0 || !out)
       return MHD_ERR_INVALID_ARG;
     MLP_CK(cudaSetDevice(m->device));
-    std::vector<uint32_t> pack(kPackWords + kBiasFloats);
-    mhd::mlp_pack(m->params.data(), pack.data());
+    std::vector<uint32_t> pack(kTcPackWords);
+    pack_tc(m->params.data(), pack.data());
     DevBuf<uint32_t> dp;
     DevBuf<float>    feat, o;
+    DevBuf<int>      status;
     MLP_CK(dp.alloc(pack.size()));
     MLP_CK(feat.alloc((size_t)n * kFeat));
     MLP_CK(o.alloc((size_t)n * kTgt));
+    MLP_CK(status.alloc(1));
     MLP_CK(cudaMemcpy(dp.p, pack.data(), pack.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     MLP_CK(cudaMemcpy(feat.p, features, (size_t)n * kFeat * sizeof(float), cudaMemcpyHostToDevice));
-    k_forward_mma<<<(unsigned)((n + 127) / 128), 128, 0, m->stream>>>(dp.p, feat.p, n, o.p);
+    MLP_CK(cudaMemset(status.p, 0, sizeof(int)));
+    k_forward_tc<<<(unsigned)((n + kTcRows - 1) / kTcRows), kTcRows, kTcSmemBytes, m->stream>>>(
+      dp.p, feat.p, n, o.p, status.p);
     MLP_CK(cudaGetLastError());
     MLP_CK(cudaStreamSynchronize(m->stream));
+    int st = 0;
+    MLP_CK(cudaMemcpy(&st, status.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st)
+      return fail(m, MHD_ERR_CUDA, "a tensor-core completion wait reached its limit");
     MLP_CK(cudaMemcpy(out, o.p, (size_t)n * kTgt * sizeof(float), cudaMemcpyDeviceToHost));
     return MHD_OK;
   }

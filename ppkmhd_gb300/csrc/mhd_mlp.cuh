@@ -43,6 +43,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include "mhd_umma.cuh"
+
 namespace mhd
 {
 namespace mlp
@@ -72,6 +74,18 @@ constexpr int kPackW2 = kPackW1 + (kIn / 16) * (kHid / 8) * 64;
 constexpr int kPackW3 = kPackW2 + (kHid / 16) * (kHid / 8) * 64;
 constexpr int kPackWords = kPackW3 + (kHid / 16) * (kOut / 8) * 64; // 3840
 constexpr int kBiasFloats = kHid + kHid + kOut;                    // 152
+
+// Image of the network for the tensor-core (tcgen05) batch forward: the
+// transposed weight matrices W^T[N][K] of the three layers in BF16, in the
+// tensor cores' K-major canonical layout (mhd_umma.cuh), then the biases in
+// FP32.  Layer 3's 24 output rows are padded with zero rows to kN3 = 32 (for
+// M = 128 the MMA's N is a multiple of 16).
+constexpr int kN3 = 32;
+constexpr int kTcW1 = 0;                         // byte offsets
+constexpr int kTcW2 = kTcW1 + kHid * kIn * 2;    // 4096
+constexpr int kTcW3 = kTcW2 + kHid * kHid * 2;   // 12288
+constexpr int kTcWBytes = kTcW3 + kN3 * kHid * 2; // 16384
+constexpr int kTcPackWords = kTcWBytes / 4 + kBiasFloats;
 
 constexpr double kJFloor = 1e-4;
 constexpr double kTauRef = 0.1;
@@ -393,6 +407,135 @@ warp_forward(const uint32_t * __restrict__ wp, const float * __restrict__ bias, 
   for (int o = 0; o < kOut; ++o)
     out[o] = so[lane * kStageORow + o];
   __syncwarp();
+}
+
+// ---------------------------------------------------------------- tcgen05 batch forward
+
+// Shared memory of one 128-thread block running the network on the 5th-
+// generation tensor cores: the tcgen05 network image (kTcWBytes of weights,
+// then the biases), the activation tile (128 rows x 64 bf16, canonical
+// layout; the 32-wide input tile uses its first half), the mbarrier and the
+// TMEM address slot.
+constexpr int      kTcRows = 128;
+constexpr int      kTcAct = kTcWBytes + ((kBiasFloats * 4 + 127) / 128) * 128;
+constexpr int      kTcBar = kTcAct + kTcRows * kHid * 2;
+constexpr int      kTcSmemBytes = kTcBar + 16;
+constexpr uint32_t kTcCols = 64; // TMEM columns per block (FP32 accumulators)
+constexpr int      kTcWaitPolls = 1 << 20;
+
+__device__ __forceinline__ void
+stage_network_tc(const uint32_t * __restrict__ pack, unsigned char * smem)
+{
+  const uint4 * src = reinterpret_cast<const uint4 *>(pack);
+  uint4 *       dst = reinterpret_cast<uint4 *>(smem);
+  for (int q = threadIdx.x; q < kTcWBytes / 16; q += blockDim.x)
+    dst[q] = src[q];
+  float *       b = reinterpret_cast<float *>(smem + kTcWBytes);
+  const float * bs = reinterpret_cast<const float *>(pack + kTcWBytes / 4);
+  for (int q = threadIdx.x; q < kBiasFloats; q += blockDim.x)
+    b[q] = bs[q];
+}
+
+// Hidden-layer epilogue of row r: z = accumulator + bias, gelu in BF16, the
+// result written as row r of the next layer's A tile (K = 64).
+__device__ __forceinline__ void
+hidden_epilogue(uint32_t trow, const float * bias, unsigned char * act, int r)
+{
+#pragma unroll
+  for (int half = 0; half < 2; ++half)
+  {
+    uint32_t v[32];
+    umma::ld32(trow + 32 * half, v);
+    uint32_t w[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q)
+      w[q] = gelu_bf16x2(pack_bf16x2(__uint_as_float(v[2 * q]) + bias[32 * half + 2 * q],
+                                     __uint_as_float(v[2 * q + 1]) + bias[32 * half + 2 * q + 1]));
+#pragma unroll
+    for (int kc = 0; kc < 4; ++kc)
+      *reinterpret_cast<uint4 *>(act + umma::canon_offset(r, 32 * half + 8 * kc, kHid)) =
+        make_uint4(w[4 * kc], w[4 * kc + 1], w[4 * kc + 2], w[4 * kc + 3]);
+  }
+}
+
+// Forward pass of 128 rows on the tensor cores, one row per thread of the
+// block (row = threadIdx.x = TMEM lane); every thread of the block must call
+// it.  x: this row's inputs; y: its raw outputs (biases included).  tmem: the
+// block's kTcCols TMEM columns; parity: the mbarrier phase to wait for next
+// (advanced by three on success).  Thread 0 issues each layer's MMAs
+// (M = 128, K = 16 per instruction) and commits them to the mbarrier; every
+// thread then moves its row from TMEM through bias and activation into the
+// next A tile.  Numerics are those of warp_forward: BF16 operands, FP32
+// accumulation, bias added in FP32, BF16 GELU.  Returns false, for every
+// thread, when a wait reached its limit: the outputs are then invalid, the
+// pending phase has been waited for once more (bounded) and the caller must
+// stop using the tile and free TMEM.
+__device__ __forceinline__ bool
+block_forward(unsigned char * smem, uint32_t tmem, uint32_t & parity, const float (&x)[kIn],
+              float (&y)[kOut])
+{
+  const int       r = threadIdx.x;
+  unsigned char * act = smem + kTcAct;
+  const float *   bias = reinterpret_cast<const float *>(smem + kTcWBytes);
+  const uint32_t  mbar = umma::smem_addr(smem + kTcBar);
+  const uint32_t  trow = tmem + ((uint32_t)(r & ~31) << 16); // the warp's lane quarter
+  const uint32_t  a0 = umma::smem_addr(act), w0 = umma::smem_addr(smem);
+#pragma unroll
+  for (int kc = 0; kc < kIn / 8; ++kc)
+    *reinterpret_cast<uint4 *>(act + umma::canon_offset(r, 8 * kc, kIn)) =
+      make_uint4(pack_bf16x2(x[8 * kc], x[8 * kc + 1]), pack_bf16x2(x[8 * kc + 2], x[8 * kc + 3]),
+                 pack_bf16x2(x[8 * kc + 4], x[8 * kc + 5]), pack_bf16x2(x[8 * kc + 6], x[8 * kc + 7]));
+  bool ok = true;
+#pragma unroll 1
+  for (int layer = 0; layer < 3; ++layer)
+  {
+    // generic stores of the A tile -> tensor-core reads; every thread's
+    // TMEM loads of the previous layer -> this layer's accumulator writes
+    umma::fence_proxy_async();
+    umma::fence_before_sync();
+    const bool failed = __syncthreads_or(!ok);
+    umma::fence_after_sync();
+    if (failed)
+    {
+      // drain: a thread whose wait gave up waits once more for that phase
+      if (!ok)
+        umma::mbar_wait(mbar, parity, kTcWaitPolls);
+      return false;
+    }
+    if (r == 0)
+    {
+      const int      K = layer == 0 ? kIn : kHid;
+      const int      N = layer == 2 ? kN3 : kHid;
+      const uint32_t wl = w0 + (layer == 0 ? kTcW1 : layer == 1 ? kTcW2 : kTcW3);
+      const uint32_t idesc = umma::idesc_bf16_f32(kTcRows, N);
+      for (int ks = 0; ks < K / 16; ++ks)
+        umma::mma_bf16(tmem, umma::desc_kmajor(a0 + ks * 2 * umma::kLBO, K * 16),
+                       umma::desc_kmajor(wl + ks * 2 * umma::kLBO, K * 16), idesc, ks > 0);
+      umma::commit(mbar);
+    }
+    ok = umma::mbar_wait(mbar, parity, kTcWaitPolls);
+    umma::fence_after_sync();
+    if (ok)
+    {
+      parity ^= 1u;
+      if (layer < 2)
+        hidden_epilogue(trow, bias + layer * kHid, act, r);
+      else
+      {
+        uint32_t v[32];
+        umma::ld32(trow, v);
+#pragma unroll
+        for (int o = 0; o < kOut; ++o)
+          y[o] = __uint_as_float(v[o]) + bias[2 * kHid + o];
+      }
+    }
+  }
+  umma::fence_before_sync();
+  const bool failed = __syncthreads_or(!ok);
+  umma::fence_after_sync();
+  if (failed && !ok)
+    umma::mbar_wait(mbar, parity, kTcWaitPolls);
+  return !failed;
 }
 
 #endif // __CUDACC__

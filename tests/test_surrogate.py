@@ -170,7 +170,7 @@ def test_tensor_core_forward_matches_oracle(mhdlib, oracle):
     m.params = P
     X = rng.normal(0, 1, (1000, 40)).astype(np.float32)
     X[:, 27:32] = 0
-    y = m.forward(X).astype(np.float64)
+    y = m.forward(X).astype(np.float64)  # the tcgen05 batch forward (TMEM accumulators)
     yo = oracle.mlp_forward(m.params.astype(np.float64), X.astype(np.float64), rounding=True)
     yx = oracle.mlp_forward(m.params.astype(np.float64), X.astype(np.float64), rounding=False)
     err = np.sqrt(np.mean((y - yo) ** 2)) / np.sqrt(np.mean(yo ** 2))
