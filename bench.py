@@ -680,7 +680,8 @@ def run_turbulence(args):
                     "h2d_bytes_per_step": U0.nbytes, "d2h_bytes_per_step": U0.nbytes,
                     "steps": e2e_steps, "call": "mhd_step_host (pinned host buffers)"},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
-                         "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                         "unit": "GB/s", "frac": achieved / hbm_peak,
+                         "traffic": load_profile_traffic(args.workload, dom),
                          "peak_source": f"hbm_gbs of {peak_kind}", "algorithmic_bytes_per_cell": alg,
                          "step_achieved": alg * cells / (step_ms / 1e3) / 1e9},
             "clocks": clk.summary(),
