@@ -503,14 +503,15 @@ k_advance(DevState * st)
 // identically zero; that is kept.
 template <class R, int DIM>
 __device__ __forceinline__ R
-face_field_slope(const Grid<R> & G, const R * __restrict__ U, int64_t c, int comp, int dir)
+face_field_slope(const Grid<R> & G, const R * __restrict__ U, uint32_t c, int comp, int dir)
 {
-  const int64_t cv = c + comp * G.sv;
+  const uint32_t cv = c + (uint32_t)comp * (uint32_t)G.sv;
+  const uint32_t sj = (uint32_t)G.sj, sk = (uint32_t)G.sk;
   if (dir == 0)
     return slope_limited(U[cv], U[cv + 1], U[cv - 1], G.slope_type);
   if (dir == 1)
-    return slope_limited(U[cv], U[cv + G.sj], U[cv - G.sj], G.slope_type);
-  return slope_limited(U[cv], U[cv + G.sk], U[cv + G.sk], G.slope_type);
+    return slope_limited(U[cv], U[cv + sj], U[cv - sj], G.slope_type);
+  return slope_limited(U[cv], U[cv + sk], U[cv + sk], G.slope_type);
 }
 
 
@@ -535,8 +536,10 @@ trace_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
   int       i, j, k;
   if (!box_cell(b, idx, i, j, k))
     return;
-  const int64_t sv = G.sv, sj = G.sj, sk = G.sk;
-  const int64_t c = cell_at(G, i, j, k);
+  // 32-bit element offsets inside arrays of at most 8 planes (grids hold
+  // fewer than 4e9 values, checked at context creation)
+  const uint32_t sv = (uint32_t)G.sv, sj = (uint32_t)G.sj, sk = (uint32_t)G.sk;
+  const uint32_t c = (uint32_t)cell_at(G, i, j, k);
   const R * __restrict__ Q = B.Q;
   const R * __restrict__ U = B.Uin;
   R dtdx, dtdy, dtdz;
@@ -585,7 +588,7 @@ trace_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
 
   // limited slopes in each direction
   R         q[NV], s[DIM][NV];
-  const int64_t off[3] = { 1, sj, sk };
+  const uint32_t off[3] = { 1u, sj, sk };
 #pragma unroll
   for (int v = 0; v < NV; ++v)
     q[v] = Q[c + v * sv];
@@ -597,12 +600,14 @@ trace_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
       s[d][v] = slope_limited(q[v], Q[c + off[d] + v * sv], Q[c - off[d] + v * sv], G.slope_type);
     s[d][IA + d] = U[c + off[d] + (IA + d) * sv] - U[c + (IA + d) * sv];
   }
-  R * S = B.S;
 #pragma unroll
   for (int d = 0; d < DIM; ++d)
+  {
+    R * Sd = B.S + (int64_t)d * NV * sv; // the 8 slope planes of direction d
 #pragma unroll
     for (int v = 0; v < NV; ++v)
-      S[c + (d * NV + v) * sv] = s[d][v];
+      Sd[c + v * sv] = s[d][v];
+  }
   // transverse slopes of the face-centred field for the edge stage
   R * H = B.H;
   H[c + FaceData<DIM>::slope_plane(0, 1) * sv] = face_field_slope<R, DIM>(G, U, c, IA, 1);
@@ -784,9 +789,10 @@ template <class R, int DIM, int d>
 __device__ __forceinline__ void
 face_states(const Grid<R> & G, const Buffers<R> & B, int64_t c, State<R> & qL, State<R> & qR)
 {
-  const int64_t sv = G.sv;
-  const int64_t off = d == 0 ? 1 : (d == 1 ? G.sj : G.sk);
-  const int64_t cn = c - off;
+  // 32-bit element offsets inside arrays of at most 8 planes
+  const uint32_t sv = (uint32_t)G.sv;
+  const uint32_t cu = (uint32_t)c;
+  const uint32_t cn = cu - (uint32_t)(d == 0 ? 1 : (d == 1 ? G.sj : G.sk));
   const R * __restrict__ Q2 = B.Q2;
   const R * __restrict__ S = B.S + (int64_t)d * NV * sv;
   R dtdx, dtdy, dtdz;
@@ -798,7 +804,7 @@ face_states(const Grid<R> & G, const Buffers<R> & B, int64_t c, State<R> & qL, S
   {
     if (v == nrm)
       continue;
-    qR[v] = Q2[c + v * sv] - R(0.5) * S[c + v * sv];
+    qR[v] = Q2[cu + v * sv] - R(0.5) * S[cu + v * sv];
     qL[v] = Q2[cn + v * sv] + R(0.5) * S[cn + v * sv];
   }
   qR[ID] = sel_max(smallR, qR[ID]);
@@ -885,10 +891,12 @@ __device__ __forceinline__ void
 emf_edge(const Grid<R> & G, const Buffers<R> & B, int i, int j, int k)
 {
   constexpr int d0 = edir == 0 ? 1 : 0, d1 = edir == 2 ? 1 : 2;
-  const int64_t sv = G.sv;
-  const int64_t stride[3] = { 1, G.sj, G.sk };
-  const int64_t o0 = stride[d0], o1 = stride[d1];
-  const int64_t c = cell_at(G, i, j, k);
+  // 32-bit element offsets inside arrays of at most 8 planes (grids hold
+  // fewer than 4e9 values, checked at context creation)
+  const uint32_t sv = (uint32_t)G.sv;
+  const uint32_t stride[3] = { 1u, (uint32_t)G.sj, (uint32_t)G.sk };
+  const uint32_t o0 = stride[d0], o1 = stride[d1];
+  const uint32_t c = (uint32_t)cell_at(G, i, j, k);
   const R * __restrict__ Q2 = B.Q2;
   const R * __restrict__ U = B.Uin;
   const R * __restrict__ S0 = B.S + (int64_t)d0 * NV * sv;
@@ -905,9 +913,9 @@ emf_edge(const Grid<R> & G, const Buffers<R> & B, int i, int j, int k)
     const R       sdq0 = r0 ? R(1) : R(-1), sdq1 = r1 ? R(1) : R(-1);
     const R       sb0 = (e == 0 || e == 2) ? R(1) : R(-1);
     const R       sb1 = (e == 0 || e == 1) ? R(1) : R(-1);
-    const int64_t cc = c - (r0 ? o0 : 0) - (r1 ? o1 : 0);
-    const int64_t c0 = cc + (r0 ? o0 : 0); // face carrying B_{d0}
-    const int64_t c1 = cc + (r1 ? o1 : 0); // face carrying B_{d1}
+    const uint32_t cc = c - (r0 ? o0 : 0u) - (r1 ? o1 : 0u);
+    const uint32_t c0 = cc + (r0 ? o0 : 0u); // face carrying B_{d0}
+    const uint32_t c1 = cc + (r1 ? o1 : 0u); // face carrying B_{d1}
     constexpr int dd1 = DIM == 2 ? 1 : d1;
     // half-step face fields: stored by the flux stage on the face box; the
     // layer below it (index g-1 along the other transverse direction) is
@@ -970,7 +978,7 @@ emf_edge(const Grid<R> & G, const Buffers<R> & B, int i, int j, int k)
     for (int v = 0; v < NV; ++v)
       swap_vals(qe[1][v], qe[2][v]);
   }
-  B.Em[c + (DIM == 2 ? 0 : (int64_t)edir * sv)] = compute_emf(edir, qe, G.gamma0, G.smallc);
+  B.Em[c + (DIM == 2 ? 0u : (uint32_t)edir * sv)] = compute_emf(edir, qe, G.gamma0, G.smallc);
 }
 
 template <class R, int DIM>
