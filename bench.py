@@ -285,21 +285,6 @@ def run_gb300(args):
     step_ms = sum(prof.values())
     dom = max(prof, key=prof.get)
 
-    # ---- end to end through the host-buffer ABI call (H2D + step + D2H per step)
-    e2e_steps = max(2, min(args.steps, 10))
-    h_in = torch.empty(U0.size, dtype=torch.float64 if precision == 64 else torch.float32,
-                       pin_memory=True)
-    h_out = torch.empty_like(h_in, pin_memory=True)
-    h_in.numpy()[:] = U0.reshape(-1)
-    s.step_host_ptr(h_in.data_ptr(), h_out.data_ptr())  # warm
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for q in range(e2e_steps):
-        a, b = (h_in, h_out) if q % 2 == 0 else (h_out, h_in)
-        s.step_host_ptr(a.data_ptr(), b.data_ptr())
-    e2e_sec = time.perf_counter() - t0
-    e2e_value = world * interior_cells * e2e_steps / e2e_sec
-
     hbm_peak, peak_kind = load_peaks()
     alg_bytes_per_cell = 16 * real_bytes
     achieved = alg_bytes_per_cell * interior_cells / (prof[dom] / 1e3) / 1e9
@@ -359,6 +344,27 @@ def run_gb300(args):
                "sample": f"{ns} steps of the same {n}^{dim} grid after 1 warm-up "
                          f"step, oracle/mhd_oracle.c with {nthreads} OpenMP threads "
                          f"({el:.1f} s timed)"}
+
+    # ---- end to end through the host-buffer ABI call (H2D + step + D2H per
+    # step), measured last: right after a process that freed much device
+    # memory exits, the driver's background clearing of that memory competes
+    # with host<->device copies for the first seconds of the next process
+    e2e_steps = max(2, min(args.steps, 10))
+    h_in = torch.empty(U0.size, dtype=torch.float64 if precision == 64 else torch.float32,
+                       pin_memory=True)
+    h_out = torch.empty_like(h_in, pin_memory=True)
+    h_in.numpy()[:] = U0.reshape(-1)
+    for _ in range(2):  # warm
+        s.step_host_ptr(h_in.data_ptr(), h_out.data_ptr())
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for q in range(e2e_steps):
+        a, b = (h_in, h_out) if q % 2 == 0 else (h_out, h_in)
+        s.step_host_ptr(a.data_ptr(), b.data_ptr())
+    e2e_sec = max_over_ranks(time.perf_counter() - t0, world, "cuda")
+    e2e_value = world * interior_cells * e2e_steps / e2e_sec
 
     if rank == 0:
         out = {
