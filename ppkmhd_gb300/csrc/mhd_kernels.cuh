@@ -8,8 +8,10 @@
 //   k_boundaries  ghost fill of U_in (periodic / reflecting / outflow)
 //   k_prim_dt     primitives Q over [0,size-1)^DIM + CFL max-reduction (FP64)
 //   k_finalize_dt dt = cfl / max, clipped to tEnd; dt/dx, dt/dy, dt/dz
-//   k_trace       limited slopes S_d, half-step primitives Q2, edge fields E
-//   k_flux        HLLD face fluxes F_d (face-normal B predicted with curl E)
+//   k_trace       limited slopes S_d, half-step primitives Q2, edge fields E,
+//                 transverse face-field slopes (H)
+//   k_flux        HLLD face fluxes F_d (face-normal B predicted with curl E,
+//                 stored in H for the edge stage)
 //   k_emf         reconstructed edge states -> 2D HLLD EMFs
 //   k_update      U_out = U_in - div F (hydro), U_out = U_in + curl EMF (face B)
 //   k_advance     iteration += 1, t += dt
