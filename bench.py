@@ -347,7 +347,7 @@ def run_gb300(args):
 
     # ---- end to end through the host-buffer ABI call (H2D + step + D2H per
     # step), measured last: right after a process that freed much device
-    # memory exits, the driver's background clearing of that memory competes
+    # memory exits, the GPU's background clearing of that memory competes
     # with host<->device copies for the first seconds of the next process
     e2e_steps = max(2, min(args.steps, 10))
     h_in = torch.empty(U0.size, dtype=torch.float64 if precision == 64 else torch.float32,
