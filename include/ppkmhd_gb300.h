@@ -327,6 +327,14 @@ int mhd_mlp_train(mhd_mlp *mlp, const float *records, int64_t n, int epochs, int
  * tensor cores (tcgen05, FP32 accumulators in TMEM) with the deployed
  * numerics: BF16 weights and activations, FP32 accumulation, BF16 GELU. */
 int mhd_mlp_forward(mhd_mlp *mlp, const float *features, int64_t n, float *out);
+
+/* Bound (number of polls, >= 0; default MHD_MLP_WAIT_POLLS) of each wait of
+ * mhd_mlp_forward for a tensor-core completion.  A wait that reaches it makes
+ * the call return MHD_ERR_CUDA after the pending work has drained (with the
+ * default bound); the network and the device stay usable.  0 makes every
+ * wait give up at once: the way to exercise that error path. */
+#define MHD_MLP_WAIT_POLLS (1 << 20)
+int mhd_mlp_set_wait_limit(mhd_mlp *mlp, int polls);
 const char *mhd_mlp_last_error(mhd_mlp *mlp);
 
 /* Use the network in the flux stage of an FP32, version-2, HLLD context

@@ -29,12 +29,14 @@ static_assert(mhd::kMlpPackTotal == kPackWords + kBiasFloats, "packed surrogate 
 static_assert(kParams == MHD_MLP_PARAMS, "surrogate parameter count");
 static_assert(kRecord == MHD_SAMPLE_FLOATS, "face record size");
 static_assert(kFeat == MHD_MLP_FEATURES, "face feature count");
+static_assert(kTcWaitPolls == MHD_MLP_WAIT_POLLS, "default tensor-core wait bound");
 
 struct mhd_mlp
 {
   int          device = 0;
   double       gamma0 = 5.0 / 3.0;
   std::vector<float> params; // host copy of the master weights (kept in sync)
+  int          wait_polls = kTcWaitPolls; // bound of the tensor-core completion waits
   float *      d_params = nullptr;
   float *      d_m = nullptr;
   float *      d_v = nullptr;
@@ -311,7 +313,7 @@ k_reduce_adam(const float * __restrict__ partial, int nblocks, float * __restric
 // round trips per tile made the fused flux stage 2.3x slower.)
 __global__ void __launch_bounds__(kTcRows)
 k_forward_tc(const uint32_t * __restrict__ pack, const float * __restrict__ feat, int64_t n,
-             float * __restrict__ out, int * __restrict__ status)
+             float * __restrict__ out, int * __restrict__ status, int polls)
 {
   extern __shared__ __align__(128) unsigned char smem[];
   uint32_t * slot = reinterpret_cast<uint32_t *>(smem + kTcBar + 8);
@@ -331,7 +333,7 @@ k_forward_tc(const uint32_t * __restrict__ pack, const float * __restrict__ feat
   for (int q = 0; q < kBasis; ++q)
     u[q] = s < n ? feat[s * kFeat + kIn + q] : 0.f;
   uint32_t   parity = 0;
-  const bool ok = block_forward(smem, tmem, parity, f, y);
+  const bool ok = block_forward(smem, tmem, parity, f, y, polls);
   if (ok && s < n)
   {
     combine(y, u, Dn);
@@ -587,6 +589,15 @@ extern "C"
     return MHD_OK;
   }
 
+  int
+  mhd_mlp_set_wait_limit(mhd_mlp * m, int polls)
+  {
+    if (!m || polls < 0)
+      return MHD_ERR_INVALID_ARG;
+    m->wait_polls = polls;
+    return MHD_OK;
+  }
+
   const char *
   mhd_mlp_last_error(mhd_mlp * m)
   {
@@ -763,7 +774,7 @@ extern "C"
     MLP_CK(cudaMemcpy(feat.p, features, (size_t)n * kFeat * sizeof(float), cudaMemcpyHostToDevice));
     MLP_CK(cudaMemset(status.p, 0, sizeof(int)));
     k_forward_tc<<<(unsigned)((n + kTcRows - 1) / kTcRows), kTcRows, kTcSmemBytes, m->stream>>>(
-      dp.p, feat.p, n, o.p, status.p);
+      dp.p, feat.p, n, o.p, status.p, m->wait_polls);
     MLP_CK(cudaGetLastError());
     MLP_CK(cudaStreamSynchronize(m->stream));
     int st = 0;

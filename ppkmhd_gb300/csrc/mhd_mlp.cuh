@@ -469,10 +469,11 @@ hidden_epilogue(uint32_t trow, const float * bias, unsigned char * act, int r)
 // accumulation, bias added in FP32, BF16 GELU.  Returns false, for every
 // thread, when a wait reached its limit: the outputs are then invalid, the
 // pending phase has been waited for once more (bounded) and the caller must
-// stop using the tile and free TMEM.
+// stop using the tile and free TMEM.  polls bounds each layer's wait (the
+// drain always allows kTcWaitPolls).
 __device__ __forceinline__ bool
 block_forward(unsigned char * smem, uint32_t tmem, uint32_t & parity, const float (&x)[kIn],
-              float (&y)[kOut])
+              float (&y)[kOut], int polls = kTcWaitPolls)
 {
   const int       r = threadIdx.x;
   unsigned char * act = smem + kTcAct;
@@ -513,7 +514,7 @@ block_forward(unsigned char * smem, uint32_t tmem, uint32_t & parity, const floa
                        umma::desc_kmajor(wl + ks * 2 * umma::kLBO, K * 16), idesc, ks > 0);
       umma::commit(mbar);
     }
-    ok = umma::mbar_wait(mbar, parity, kTcWaitPolls);
+    ok = umma::mbar_wait(mbar, parity, polls);
     umma::fence_after_sync();
     if (ok)
     {

@@ -25,8 +25,8 @@ import time
 
 import numpy as np
 
-from . import (MHD_MLP_CHECK, MHD_MLP_FEATURES, MHD_MLP_PARAMS, MHD_OK, MHDError, MHDSolver, lib,
-               params_from_ini)
+from . import (MHD_MLP_CHECK, MHD_MLP_FEATURES, MHD_MLP_PARAMS, MHD_MLP_WAIT_POLLS, MHD_OK,
+               MHDError, MHDSolver, lib, params_from_ini)
 from . import workloads
 
 DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
@@ -117,6 +117,11 @@ class FluxMLP:
         out = np.empty((f.shape[0], 8), dtype=np.float32)
         self._check(lib().mhd_mlp_forward(self.h, f.ctypes.data, f.shape[0], out.ctypes.data))
         return out
+
+    def set_wait_limit(self, polls: int = MHD_MLP_WAIT_POLLS):
+        """Bound of the tensor-core completion waits of forward() (0: give up
+        at once, which makes forward() report the failure)."""
+        self._check(lib().mhd_mlp_set_wait_limit(self.h, int(polls)))
 
 
 def smooth(records: np.ndarray, tau: float = 0.1) -> np.ndarray:

@@ -236,3 +236,22 @@ def test_surrogate_flux_stage_against_fp64_oracle(mhdlib, oracle):
     assert abs(m1[0] - m0[0]) <= 1e-5 * abs(m0[0])  # conservative: one flux per face
     assert dmax < 1e-3
     assert "k_flux_mlp" in [k for k, _ in s.profile_step()]
+
+
+@pytest.mark.gpu
+def test_tensor_core_wait_limit_reports_and_recovers(mhdlib):
+    """A tensor-core completion wait that gives up is reported as an error
+    (after the pending work drained), and the next call works again."""
+    from ppkmhd_gb300.surrogate import FluxMLP
+
+    m = FluxMLP(seed=3)
+    X = np.random.default_rng(1).normal(0, 1, (300, 40)).astype(np.float32)
+    X[:, 27:32] = 0
+    y0 = m.forward(X)
+    m.set_wait_limit(0)
+    with pytest.raises(mhdlib.MHDError) as e:
+        m.forward(X)
+    assert e.value.code == mhdlib.MHD_ERR_CUDA
+    assert "wait" in str(e.value)
+    m.set_wait_limit()
+    assert np.array_equal(m.forward(X), y0)
