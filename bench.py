@@ -293,6 +293,7 @@ def run_gb300(args):
 
     # FP32 companion figure for the same workload (device-resident)
     variants = {}
+    accuracy = None
     if args.workload == "ot3d_256_fp64" and not args.no_variants:
         # FP32 and FP32 + flux surrogate on the same initial state: throughput,
         # and relative L1 (max over variables) against the FP64 solution after
@@ -300,15 +301,37 @@ def run_gb300(args):
         from ppkmhd_gb300 import surrogate
 
         acc_steps = 20
+        # the FMA-free FP64 build in the reference's operation order (bitwise
+        # equal to the reference): the accuracy reference, and timed as well
+        px = m.params_from_ini(ini)
+        px.device = local
+        px.fp_mode = m.MHD_FP_EXACT
+        sx = m.MHDSolver(px)
+        sx.set_state(U0)
+        sx.run(acc_steps)
+        ref = m.interior(sx.get_state())
+        sx.set_state(U0)
+        sx.run_timed(3)
+        msx = sx.run_timed(args.steps)
+        sx.close()
+        den = np.abs(ref).sum(axis=(1, 2, 3))
+        den = np.where(den > 1e-12 * den[0], den, den[0])
         p64 = m.params_from_ini(ini)
         p64.device = local
         s64 = m.MHDSolver(p64)
         s64.set_state(U0)
         s64.run(acc_steps)
-        ref = m.interior(s64.get_state())
+        err64 = np.abs(m.interior(s64.get_state()) - ref).sum(axis=(1, 2, 3)) / den
         s64.close()
-        den = np.abs(ref).sum(axis=(1, 2, 3))
-        den = np.where(den > 1e-12 * den[0], den, den[0])
+        accuracy = {"steps": acc_steps, "reference": "FP64 exact build (bitwise the reference)",
+                    "rel_l1_per_variable": [float(x) for x in err64],
+                    "note": "FMA contraction; z momentum and z field are the 1e-3 seed and "
+                            "differ at the level two valid FP64 builds differ (the CPU oracle "
+                            "with and without contraction: 5e-12 after 100 steps at 48^3)"}
+        variants["fp64_exact"] = {"value": interior_cells * args.steps / (msx / 1e3),
+                                  "ms_per_step": msx / args.steps, "dtype": "f64",
+                                  "note": "FMA-free build in the reference's operation order: "
+                                          "bitwise equal to the reference"}
         for tag, use_mlp in (("fp32", False), ("fp32_surrogate", True)):
             p32 = m.params_from_ini(ot_ini(dim, n, 32))
             p32.device = local
@@ -405,6 +428,8 @@ def run_gb300(args):
             "cpu_baseline": cpu,
             "variants": variants,
         }
+        if accuracy is not None:
+            out["accuracy"] = accuracy
         emit(out)
     s.close()
     if world > 1:

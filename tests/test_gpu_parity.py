@@ -137,6 +137,47 @@ def test_fast_fp64_orszag_tang_3d(mhdlib, oracle):
     assert err.max() <= TOL_FP64_FAST, err
 
 
+def test_fp64_perturbed_orszag_tang_3d_100_steps(mhdlib, oracle):
+    """The FP64 acceptance case in 3D: the benchmark's initial condition (3D
+    Orszag-Tang with the seeded 1e-3 velocity perturbation) at 48^3, 100
+    steps against the oracle.
+
+    The exact build is bitwise equal.  The fast build (FMA contraction) is
+    within 1e-12 relative L1 on the six variables of order one; the z
+    momentum and z field are only the 1e-3 seed and what it induces, and on
+    them any two valid FP64 builds differ at the 5e-12 level: the oracle
+    itself compiled with the C compiler's default FMA contraction
+    (-ffp-contract=fast) differs from its contraction-free build by 5.2e-12
+    (mz) and 6.1e-12 (Bz) after these 100 steps on the GB300 host, as the
+    fast GPU build does.  Those two are held to 1e-11."""
+    from ppkmhd_gb300 import workloads
+
+    ini = ot_ini(dim=3, nx=48, ny=48, nz=48)
+    o = oracle.OracleSolver(ini, nthreads=16)
+    U0 = workloads.perturbed_ot_3d(o.get_state().astype(np.float64))
+    o.set_state(U0)
+    o.run(100)
+    ref = oracle.interior(o.get_state())
+    x = gpu_solver(mhdlib, ini, exact=True)
+    x.set_state(U0)
+    assert x.run(100) == 100
+    assert np.array_equal(mhdlib.interior(x.get_state()), ref)
+    s = gpu_solver(mhdlib, ini)
+    s.set_state(U0)
+    assert s.run(100) == 100
+    err = rel_l1(mhdlib.interior(s.get_state()), ref)
+    seeded = [4, 7]  # IW, IC
+    order_one = [v for v in range(8) if v not in seeded]
+    assert err[order_one].max() <= TOL_FP64_FAST, err
+    assert err[seeded].max() <= 1e-11, err
+    t_g, _, it_g = s.time()
+    t_o, _, it_o = o.time()
+    assert it_g == it_o == 100
+    assert abs(t_g - t_o) <= 1e-12 * t_o
+    _, divb_l1, divb_max = s.diagnostics()
+    assert divb_max < 1e-10, divb_max
+
+
 @pytest.mark.parametrize("dim,n,steps", [(2, 128, 60), (3, 24, 15)])
 def test_fp32_against_fp64_oracle(mhdlib, oracle, dim, n, steps):
     ini = ot_ini(dim=dim, nx=n, ny=n, nz=n)
