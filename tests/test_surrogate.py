@@ -2,7 +2,6 @@
 differences; on the GPU the encoding, harvested dissipation targets,
 gradients and the tensor-core forward pass against the oracle, training,
 and the deployed network in the flux stage against the FP64 solution."""
-import os
 
 import numpy as np
 import pytest
