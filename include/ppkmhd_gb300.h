@@ -153,6 +153,16 @@ int mhd_get_state(mhd_ctx *ctx, void *U, int layout, int real_bytes);
  * Does nothing when finished() holds.  Asynchronous (dt stays on device). */
 int mhd_step(mhd_ctx *ctx);
 
+/* SolverBase::compute_dt (SolverBase.cpp:148-179): the CFL time step of the
+ * current state, clipped to tEnd — the dt the next mhd_step will take.  The
+ * state, t and the iteration count are unchanged.  Synchronises the stream. */
+int mhd_compute_dt(mhd_ctx *ctx, double *dt);
+
+/* godunov_unsplit(dt) with the caller's dt (dt > 0, not clipped), then
+ * t += dt and iteration += 1; mhd_step is mhd_compute_dt followed by this
+ * with the CFL dt.  Does nothing when finished() holds.  Asynchronous. */
+int mhd_step_dt(mhd_ctx *ctx, double dt);
+
 /* Up to nsteps iterations of main.cpp:154-159 from a CUDA graph, stopping
  * (on device) when t >= tEnd - 1e-14 or iteration >= nStepmax.  Returns after
  * the stream is synchronised; *done = iterations executed. */

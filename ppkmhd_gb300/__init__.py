@@ -95,6 +95,8 @@ SIGNATURES = {
     "mhd_set_state": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int]),
     "mhd_get_state": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int]),
     "mhd_step": (ctypes.c_int, [_vp]),
+    "mhd_compute_dt": (ctypes.c_int, [_vp, _dp]),
+    "mhd_step_dt": (ctypes.c_int, [_vp, ctypes.c_double]),
     "mhd_run": (ctypes.c_int, [_vp, ctypes.c_int, _ip]),
     "mhd_step_host": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int]),
     "mhd_time": (ctypes.c_int, [_vp, _dp, _dp, _ip]),
@@ -270,6 +272,16 @@ class MHDSolver:
 
     def step(self):
         self._check(lib().mhd_step(self.h))
+
+    def compute_dt(self) -> float:
+        """The CFL dt (clipped to tEnd) the next step would take."""
+        dt = ctypes.c_double()
+        self._check(lib().mhd_compute_dt(self.h, ctypes.byref(dt)))
+        return dt.value
+
+    def step_dt(self, dt: float):
+        """One iteration with the given dt instead of the CFL dt."""
+        self._check(lib().mhd_step_dt(self.h, float(dt)))
 
     def run(self, n: int) -> int:
         done = ctypes.c_int(0)

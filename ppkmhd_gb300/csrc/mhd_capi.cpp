@@ -324,6 +324,22 @@ extern "C"
   }
 
   int
+  mhd_compute_dt(mhd_ctx * ctx, double * dt)
+  {
+    NEED_CORE(ctx);
+    if (!dt)
+      return fail(ctx, MHD_ERR_INVALID_ARG, "dt must not be NULL");
+    return from_core(ctx, ctx->core->compute_dt(dt));
+  }
+
+  int
+  mhd_step_dt(mhd_ctx * ctx, double dt)
+  {
+    NEED_CORE(ctx);
+    return from_core(ctx, ctx->core->step_dt(dt));
+  }
+
+  int
   mhd_run(mhd_ctx * ctx, int nsteps, int * done)
   {
     NEED_CORE(ctx);

@@ -19,6 +19,8 @@ public:
   virtual int set_state(const void * U, int layout) = 0;
   virtual int get_state(void * U, int layout) = 0;
   virtual int step() = 0;
+  virtual int compute_dt(double * dt) = 0;
+  virtual int step_dt(double dt) = 0;
   virtual int run(int nsteps, int * done) = 0;
   virtual int step_host(const void * Uin, void * Uout, int layout) = 0;
   virtual int time(double * t, double * dt, int * it) = 0;

@@ -487,6 +487,23 @@ k_finalize_dt(const Grid<R> G, DevState * st, int force)
   finalize_dt_body<R>(G, st, force);
 }
 
+// godunov_unsplit(dt) with the caller's dt (SolverMHDMuscl.cpp:390-391:
+// dtdx = dt / dx): the dt of this iteration instead of the CFL one.
+template <class R>
+__global__ void
+k_set_dt(const Grid<R> G, DevState * st, double dt)
+{
+  if (step_finished(st))
+    return;
+  st->dt = dt;
+  st->dtdx = dt / G.dx;
+  st->dtdy = dt / G.dy;
+  st->dtdz = dt / G.dz;
+  st->fdtdx = (float)st->dtdx;
+  st->fdtdy = (float)st->dtdy;
+  st->fdtdz = (float)st->dtdz;
+}
+
 template <class R>
 __global__ void
 k_advance(DevState * st)

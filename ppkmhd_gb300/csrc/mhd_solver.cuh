@@ -6,6 +6,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -720,6 +721,49 @@ public:
   step() override
   {
     enqueue_step((int)(launched & 1));
+    ++launched;
+    return check_launch();
+  }
+
+  // SolverBase::compute_dt (SolverBase.cpp:148-179): the CFL dt, clipped to
+  // tEnd, that the next iteration would take; the state is not advanced.
+  int
+  compute_dt(double * dt) override
+  {
+    if (int rc = read_state())
+      return rc;
+    launched = st_host->it;
+    R * cur = current();
+    launch_boundaries(cur, 1);
+    launch_prim_dt(cur, 1);
+    launch_finalize(1);
+    if (int rc = check_launch())
+      return rc;
+    if (int rc = read_state())
+      return rc;
+    if (dt)
+      *dt = st_host->dt;
+    return status_check();
+  }
+
+  // One iteration with the caller's dt instead of the CFL dt
+  // (godunov_unsplit(dt), then next_iteration's t += dt, iteration += 1).
+  int
+  step_dt(double dt) override
+  {
+    if (!(dt > 0.0) || !std::isfinite(dt))
+    {
+      err = "dt must be positive and finite";
+      return MHD_ERR_INVALID_ARG;
+    }
+    const Buffers<R> B = buffers((int)(launched & 1));
+    const char *     names[kMaxLaunches];
+    const int        n = step_kernel_names(names);
+    launch_stage(0, B);
+    launch_stage(1, B);
+    k_set_dt<R><<<1, 1, 0, stream>>>(G, st, dt);
+    for (int q = 3; q < n; ++q)
+      launch_stage(q, B);
     ++launched;
     return check_launch();
   }

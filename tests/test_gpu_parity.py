@@ -280,3 +280,29 @@ def test_profile_and_counts(mhdlib):
     assert all(ms >= 0 for _, ms in prof)
     assert s.cell_counts() == (16 ** 3, 22 ** 3)
     assert s.launches_per_step() == len(prof)
+
+
+def test_compute_dt_and_step_dt(mhdlib):
+    """mhd_compute_dt is the dt the next iteration takes; mhd_step_dt with it
+    is mhd_step bit for bit; a caller's dt advances t by exactly that dt."""
+    ini = ot_ini(dim=3, nx=20, ny=16, nz=12)
+    a = gpu_solver(mhdlib, ini, exact=True)
+    b = gpu_solver(mhdlib, ini, exact=True)
+    a.init_problem()
+    b.init_problem()
+    for _ in range(3):
+        dt = b.compute_dt()
+        a.step()
+        b.step_dt(dt)
+        ta, dta, ita = a.time()
+        tb, dtb, itb = b.time()
+        assert dta == dt and dtb == dt and ta == tb and ita == itb
+        assert np.array_equal(a.get_state(), b.get_state())
+    t0, _, it0 = b.time()
+    b.step_dt(0.5 * dt)
+    t1, dt1, it1 = b.time()
+    assert t1 == t0 + 0.5 * dt and it1 == it0 + 1 and dt1 == 0.5 * dt
+    with pytest.raises(mhdlib.MHDError):
+        b.step_dt(-1.0)
+    a.close()
+    b.close()
