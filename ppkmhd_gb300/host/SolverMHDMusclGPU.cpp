@@ -71,7 +71,12 @@ template <int dim>
 double
 SolverMHDMusclGPU<dim>::compute_dt_local()
 {
-  // dt is computed on the device at the start of every iteration
+  // the CFL dt of the current state from the device reduction (already
+  // clipped to tEnd, which SolverBase::compute_dt does again); every
+  // iteration recomputes it on the device
+  double dt = 0.0;
+  if (mhd_compute_dt(ctx, &dt) == MHD_OK)
+    return dt;
   sync_time();
   return m_dt;
 }
