@@ -924,71 +924,128 @@ emf_edge(const Grid<R> & G, const Buffers<R> & B, int i, int j, int k)
   dt_over_dx(B.st, dtdx, dtdy, dtdz);
   const R smallR = G.smallr, smallp = G.smallp;
 
-  State<R> qe[4]; // RT, RB, LT, LB
+  // Corner cells and face data of the four corners (RT, RB, LT, LB)
+  constexpr int dd1 = DIM == 2 ? 1 : d1;
+  constexpr int p0 = FaceData<DIM>::slope_plane(d0, dd1);
+  constexpr int p1 = FaceData<DIM>::slope_plane(dd1, d0);
+  const int     id0 = d0 == 0 ? i : j;
+  const int     id1 = dd1 == 1 ? j : k;
+  uint32_t      cc[4];
+  R             fb0[4], fb1[4]; // B_{d0} + slope term, B_{d1} + slope term
 #pragma unroll
   for (int e = 0; e < 4; ++e)
   {
-    const bool    r0 = (e == 0 || e == 1), r1 = (e == 0 || e == 2);
-    const R       sdq0 = r0 ? R(1) : R(-1), sdq1 = r1 ? R(1) : R(-1);
-    const R       sb0 = (e == 0 || e == 2) ? R(1) : R(-1);
-    const R       sb1 = (e == 0 || e == 1) ? R(1) : R(-1);
-    const uint32_t cc = c - (r0 ? o0 : 0u) - (r1 ? o1 : 0u);
-    const uint32_t c0 = cc + (r0 ? o0 : 0u); // face carrying B_{d0}
-    const uint32_t c1 = cc + (r1 ? o1 : 0u); // face carrying B_{d1}
-    constexpr int dd1 = DIM == 2 ? 1 : d1;
+    const bool     r0 = (e == 0 || e == 1), r1 = (e == 0 || e == 2);
+    const R        sb0 = (e == 0 || e == 2) ? R(1) : R(-1);
+    const R        sb1 = (e == 0 || e == 1) ? R(1) : R(-1);
+    cc[e] = c - (r0 ? o0 : 0u) - (r1 ? o1 : 0u);
+    const uint32_t c0 = cc[e] + (r0 ? o0 : 0u); // face carrying B_{d0}
+    const uint32_t c1 = cc[e] + (r1 ? o1 : 0u); // face carrying B_{d1}
     // half-step face fields: stored by the flux stage on the face box; the
     // layer below it (index g-1 along the other transverse direction) is
     // evaluated here with the same expression
-    const int id0 = d0 == 0 ? i : j;
-    const int id1 = dd1 == 1 ? j : k;
-    const R   B0 = (r1 && id1 == G.g) ? face_field<R, DIM>(G, U, B.E, c0, d0, dtdx, dtdy, dtdz)
-                                      : B.H[c0 + d0 * sv];
-    const R   B1 = (r0 && id0 == G.g) ? face_field<R, DIM>(G, U, B.E, c1, dd1, dtdx, dtdy, dtdz)
-                                      : B.H[c1 + dd1 * sv];
+    const R B0 = (r1 && id1 == G.g) ? face_field<R, DIM>(G, U, B.E, c0, d0, dtdx, dtdy, dtdz)
+                                    : B.H[c0 + d0 * sv];
+    const R B1 = (r0 && id0 == G.g) ? face_field<R, DIM>(G, U, B.E, c1, dd1, dtdx, dtdy, dtdz)
+                                    : B.H[c1 + dd1 * sv];
     // transverse face-field slopes from the trace stage (zero along z)
-    constexpr int p0 = FaceData<DIM>::slope_plane(d0, dd1);
-    constexpr int p1 = FaceData<DIM>::slope_plane(dd1, d0);
-    const R       dB0d1 = p0 < 0 ? R(0) : B.H[c0 + p0 * sv];
-    const R       dB1d0 = p1 < 0 ? R(0) : B.H[c1 + p1 * sv];
-    State<R> & q = qe[e];
+    const R dB0d1 = p0 < 0 ? R(0) : B.H[c0 + p0 * sv];
+    const R dB1d0 = p1 < 0 ? R(0) : B.H[c1 + p1 * sv];
+    fb0[e] = B0 + R(0.5) * (sb0 * dB0d1);
+    fb1[e] = B1 + R(0.5) * (sb1 * dB1d0);
+  }
+  // Corner states, one variable at a time for the four corners (one plane
+  // base per variable): q = Q2 + (+-S0 +- S1)/2, the face-normal fields from
+  // the face data, in the statement order of reconstruct_state_at_edge
+  State<R> qe[4];
+  auto hydro = [&](int v, bool twice = false) {
+    const R * __restrict__ q2 = Q2 + v * sv;
+    const R * __restrict__ s0 = S0 + v * sv;
+    const R * __restrict__ s1 = S1 + v * sv;
 #pragma unroll
-    for (int v = 0; v < NV; ++v)
-      q[v] = Q2[cc + v * sv];
-    q[ID] += R(0.5) * (sdq0 * S0[cc + ID * sv] + sdq1 * S1[cc + ID * sv]);
-    q[IU] += R(0.5) * (sdq0 * S0[cc + IU * sv] + sdq1 * S1[cc + IU * sv]);
-    q[IV] += R(0.5) * (sdq0 * S0[cc + IV * sv] + sdq1 * S1[cc + IV * sv]);
-    q[IW] += R(0.5) * (sdq0 * S0[cc + IW * sv] + sdq1 * S1[cc + IW * sv]);
-    q[IP] += R(0.5) * (sdq0 * S0[cc + IP * sv] + sdq1 * S1[cc + IP * sv]);
-    if constexpr (DIM == 2)
+    for (int e = 0; e < 4; ++e)
     {
-      // MHDRunFunctors2D.h:1424-1432
-      q[IA] = B0 + R(0.5) * (sb0 * dB0d1);
-      q[IB] = B1 + R(0.5) * (sb1 * dB1d0);
-      q[IC] += R(0.5) * (sdq0 * S0[cc + IC * sv] + sdq1 * S1[cc + IC * sv]);
+      const bool r0 = (e == 0 || e == 1), r1 = (e == 0 || e == 2);
+      const R    sdq0 = r0 ? R(1) : R(-1), sdq1 = r1 ? R(1) : R(-1);
+      const R    inc = R(0.5) * (sdq0 * s0[cc[e]] + sdq1 * s1[cc[e]]);
+      qe[e][v] = q2[cc[e]] + inc;
+      if (twice)
+        qe[e][v] += inc;
+    }
+  };
+  hydro(ID);
+  hydro(IU);
+  hydro(IV);
+  hydro(IW);
+  hydro(IP);
+  if constexpr (DIM == 2)
+  {
+    // MHDRunFunctors2D.h:1424-1432
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+    {
+      qe[e][IA] = fb0[e];
+      qe[e][IB] = fb1[e];
+    }
+    hydro(IC);
+  }
+  else
+  {
+    // statement order of MHDRunFunctors3D.h:1490-1524, including the double
+    // transverse increment of IB on y and x edges
+    if constexpr (d0 == 0)
+    {
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        qe[e][IA] = fb0[e];
+    }
+    else
+      hydro(IA);
+    if constexpr (d0 == 1)
+    {
+      if constexpr (d1 == 1)
+      {
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          qe[e][IB] = fb1[e];
+      }
+      else
+      {
+        // q[IB] = B0 term, then += the IB slope increment
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+        {
+          const bool r0 = (e == 0 || e == 1), r1 = (e == 0 || e == 2);
+          const R    sdq0 = r0 ? R(1) : R(-1), sdq1 = r1 ? R(1) : R(-1);
+          qe[e][IB] = fb0[e] + R(0.5) * (sdq0 * S0[cc[e] + IB * sv] + sdq1 * S1[cc[e] + IB * sv]);
+        }
+      }
     }
     else
     {
-      // statement order of MHDRunFunctors3D.h:1490-1524, including the double
-      // transverse increment of IB on y and x edges
-      if constexpr (d0 == 0)
-        q[IA] = B0 + R(0.5) * (sb0 * dB0d1);
-      else
-        q[IA] += R(0.5) * (sdq0 * S0[cc + IA * sv] + sdq1 * S1[cc + IA * sv]);
-      if constexpr (d0 == 1)
-        q[IB] = B0 + R(0.5) * (sb0 * dB0d1);
-      else
-        q[IB] += R(0.5) * (sdq0 * S0[cc + IB * sv] + sdq1 * S1[cc + IB * sv]);
       if constexpr (d1 == 1)
-        q[IB] = B1 + R(0.5) * (sb1 * dB1d0);
+      {
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          qe[e][IB] = fb1[e];
+      }
       else
-        q[IB] += R(0.5) * (sdq0 * S0[cc + IB * sv] + sdq1 * S1[cc + IB * sv]);
-      if constexpr (d1 == 2)
-        q[IC] = B1 + R(0.5) * (sb1 * dB1d0);
-      else
-        q[IC] += R(0.5) * (sdq0 * S0[cc + IC * sv] + sdq1 * S1[cc + IC * sv]);
+        hydro(IB, true); // Q2 + inc, then += inc again
     }
-    q[ID] = sel_max(smallR, q[ID]);
-    q[IP] = sel_max(smallp * q[ID], q[IP]);
+    if constexpr (d1 == 2)
+    {
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        qe[e][IC] = fb1[e];
+    }
+    else
+      hydro(IC);
+  }
+#pragma unroll
+  for (int e = 0; e < 4; ++e)
+  {
+    qe[e][ID] = sel_max(smallR, qe[e][ID]);
+    qe[e][IP] = sel_max(smallp * qe[e][ID], qe[e][IP]);
   }
   if constexpr (DIM == 3 && edir == 1)
   {
