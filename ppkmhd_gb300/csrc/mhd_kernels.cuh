@@ -625,7 +625,15 @@ trace_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
     R * Sd = B.S + (int64_t)d * NV * sv; // the 8 slope planes of direction d
 #pragma unroll
     for (int v = 0; v < NV; ++v)
+    {
+      // the normal-field slope of directions x (and z in 3D, y in 2D) is
+      // read by no later stage: the face states take the face field, the
+      // edge states the face fields (only the y slope of By is read, by the
+      // 3D x edges' double increment)
+      if (v == IA + d && (d == 0 || d == DIM - 1))
+        continue;
       Sd[c + v * sv] = s[d][v];
+    }
   }
   // transverse slopes of the face-centred field for the edge stage
   R * H = B.H;
