@@ -412,7 +412,9 @@ def run_gb300(args):
             "e2e": {"value": e2e_value, "unit": "cell-updates/s",
                     "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes,
                     "steps": e2e_steps,
-                    "call": "mhd_step_host (pinned host buffers, copies inside the timed region)"},
+                    "call": "mhd_step_host (pinned host buffers, copies inside the timed region; "
+                            "uploads and downloads overlap the step slab by slab, one slab "
+                            "per 64 MiB of state, at most 8)"},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                          "peak_source": f"hbm_gbs of {peak_kind}",

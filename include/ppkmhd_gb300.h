@@ -170,8 +170,16 @@ int mhd_run(mhd_ctx *ctx, int nsteps, int *done);
 
 /* godunov_unsplit_impl(data_in, data_out) on HOST arrays: copy U_in to the
  * device, run one iteration, copy the result back.  The state inside the
- * context is replaced by U_in first, so t/dt bookkeeping continues. */
+ * context is replaced by U_in first, so t/dt bookkeeping continues.  With
+ * MHD_LAYOUT_LEFT and implementation version 2, the edge and update stages
+ * run in slabs along the slowest axis and each finished slab of U_out is
+ * copied back while the next one computes (same result, bitwise). */
 int mhd_step_host(mhd_ctx *ctx, const void *U_in, void *U_out, int layout, int real_bytes);
+
+/* Slab count of mhd_step_host: 0 (default) = one slab per 64 MiB of state,
+ * at most 8; 1 = no overlap; at most 16; never more than the grid's planes.
+ * No counterpart in the reference (its state never leaves the device). */
+int mhd_set_host_slabs(mhd_ctx *ctx, int nslabs);
 
 /* t, the dt of the last computed CFL condition, and the iteration count
  * (SolverBase m_t, m_dt, m_iteration).  Synchronises the stream. */

@@ -99,6 +99,7 @@ SIGNATURES = {
     "mhd_step_dt": (ctypes.c_int, [_vp, ctypes.c_double]),
     "mhd_run": (ctypes.c_int, [_vp, ctypes.c_int, _ip]),
     "mhd_step_host": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int]),
+    "mhd_set_host_slabs": (ctypes.c_int, [_vp, ctypes.c_int]),
     "mhd_time": (ctypes.c_int, [_vp, _dp, _dp, _ip]),
     "mhd_diagnostics": (ctypes.c_int, [_vp, _dp, _dp, _dp]),
     "mhd_run_timed": (ctypes.c_int, [_vp, ctypes.c_int, _fp]),
@@ -296,6 +297,10 @@ class MHDSolver:
         """Same as step_host on raw host pointers (e.g. pinned buffers)."""
         itemsize = 8 if self.params.precision == MHD_FP64 else 4
         self._check(lib().mhd_step_host(self.h, in_ptr, out_ptr, layout, itemsize))
+
+    def set_host_slabs(self, n: int):
+        """Slab count of step_host (0 = automatic, 1 = no copy/compute overlap)."""
+        self._check(lib().mhd_set_host_slabs(self.h, int(n)))
 
     def time(self):
         t, dt, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()

@@ -360,6 +360,13 @@ extern "C"
   }
 
   int
+  mhd_set_host_slabs(mhd_ctx * ctx, int nslabs)
+  {
+    NEED_CORE(ctx);
+    return from_core(ctx, ctx->core->set_host_slabs(nslabs));
+  }
+
+  int
   mhd_time(mhd_ctx * ctx, double * t, double * dt, int * iteration)
   {
     NEED_CORE(ctx);

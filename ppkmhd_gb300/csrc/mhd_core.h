@@ -23,6 +23,7 @@ public:
   virtual int step_dt(double dt) = 0;
   virtual int run(int nsteps, int * done) = 0;
   virtual int step_host(const void * Uin, void * Uout, int layout) = 0;
+  virtual int set_host_slabs(int n) = 0;
   virtual int time(double * t, double * dt, int * it) = 0;
   virtual int diagnostics(double sums[8], double * divb_l1, double * divb_max) = 0;
   virtual int run_timed(int nsteps, float * ms) = 0;

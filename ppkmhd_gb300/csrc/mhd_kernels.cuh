@@ -314,6 +314,19 @@ k_boundaries(const Grid<R> G, R * __restrict__ U, DevState * st, int force)
                           blockIdx.x == 0 && threadIdx.x == 0);
 }
 
+// Ghost fill of the cells base <= index < end of BOX_ALL (a range of planes
+// of the slowest axis); reset: this launch is the iteration's first and
+// clears the CFL reduction.
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+k_boundaries_range(const Grid<R> G, R * __restrict__ U, DevState * st, int64_t base, int64_t end,
+                   int reset)
+{
+  const int64_t idx = base + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx < end)
+    boundaries_body<R, DIM>(G, U, st, 0, idx, reset && blockIdx.x == 0 && threadIdx.x == 0);
+}
+
 // ---------------------------------------------------------------- primitives + CFL
 
 template <class T>
@@ -336,7 +349,7 @@ warp_max(T v)
 template <class R, int DIM>
 __device__ __forceinline__ void
 prim_dt_body(const Grid<R> & G, const R * __restrict__ U, R * __restrict__ Q, DevState * st,
-             int force, int64_t idx)
+             int force, int64_t idx, int64_t end = INT64_MAX)
 {
   if (!force && step_finished(st))
     return;
@@ -344,7 +357,7 @@ prim_dt_body(const Grid<R> & G, const R * __restrict__ U, R * __restrict__ Q, De
   int       i, j, k;
   R         rate = R(0);
   bool      bad = false;
-  if (box_cell(b, idx, i, j, k))
+  if (idx < end && box_cell(b, idx, i, j, k))
   {
     const int64_t c = cell_at(G, i, j, k);
     const int64_t sv = G.sv;
@@ -450,6 +463,16 @@ __global__ void __launch_bounds__(256)
 k_prim_dt(const Grid<R> G, const R * __restrict__ U, R * __restrict__ Q, DevState * st, int force)
 {
   prim_dt_body<R, DIM>(G, U, Q, st, force, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
+// cells base <= index < end of BOX_PRIM (threads past end still join the
+// block reduction)
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+k_prim_dt_range(const Grid<R> G, const R * __restrict__ U, R * __restrict__ Q, DevState * st,
+                int64_t base, int64_t end)
+{
+  prim_dt_body<R, DIM>(G, U, Q, st, 0, base + blockIdx.x * (int64_t)blockDim.x + threadIdx.x, end);
 }
 
 // compute_dt_local (SolverMHDMuscl.h:722-741) and the clip of
@@ -1084,11 +1107,15 @@ emf_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx, int dir)
     emf_edge<R, 3, 2>(G, B, i, j, k);
 }
 
+// Edges base <= index < end of BOX_FACE (a whole launch: 0 and the box's
+// count; slab launches of the host-buffer step cover a range of planes)
 template <class R, int DIM>
 __global__ void __launch_bounds__(128)
-k_emf(const Grid<R> G, Buffers<R> B)
+k_emf(const Grid<R> G, Buffers<R> B, int64_t base, int64_t end)
 {
-  emf_body<R, DIM>(G, B, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, blockIdx.y);
+  const int64_t idx = base + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx < end)
+    emf_body<R, DIM>(G, B, idx, blockIdx.y);
 }
 
 // ---------------------------------------------------------------- update
@@ -1171,11 +1198,14 @@ update_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
   }
 }
 
+// interior cells base <= index < end of BOX_INTERIOR
 template <class R, int DIM>
 __global__ void __launch_bounds__(256)
-k_update(const Grid<R> G, Buffers<R> B)
+k_update(const Grid<R> G, Buffers<R> B, int64_t base, int64_t end)
 {
-  update_body<R, DIM>(G, B, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+  const int64_t idx = base + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx < end)
+    update_body<R, DIM>(G, B, idx);
 }
 
 // Grid description of one problem for the kernels (host side):

@@ -156,8 +156,8 @@ step(const mhd_params & p, const void * U_in, void * U_out, double t, double * d
     k_finalize_dt<R><<<1, 1, 0, s>>>(G, B.st, 0);
     k_trace<R, 2><<<nb(ntrace, 128), 128, 0, s>>>(G, B);
     k_flux<R, 2><<<dim3(nb(nface, 128), 2), 128, 0, s>>>(G, B);
-    k_emf<R, 2><<<dim3(nb(nface, 128), 1), 128, 0, s>>>(G, B);
-    k_update<R, 2><<<nb(ncell, 256), 256, 0, s>>>(G, B);
+    k_emf<R, 2><<<dim3(nb(nface, 128), 1), 128, 0, s>>>(G, B, 0, nface);
+    k_update<R, 2><<<nb(ncell, 256), 256, 0, s>>>(G, B, 0, ncell);
   }
   else
   {
@@ -166,8 +166,8 @@ step(const mhd_params & p, const void * U_in, void * U_out, double t, double * d
     k_finalize_dt<R><<<1, 1, 0, s>>>(G, B.st, 0);
     k_trace<R, 3><<<nb(ntrace, 128), 128, 0, s>>>(G, B);
     k_flux<R, 3><<<dim3(nb(nface, 128), 3), 128, 0, s>>>(G, B);
-    k_emf<R, 3><<<dim3(nb(nface, 128), 3), 128, 0, s>>>(G, B);
-    k_update<R, 3><<<nb(ncell, 256), 256, 0, s>>>(G, B);
+    k_emf<R, 3><<<dim3(nb(nface, 128), 3), 128, 0, s>>>(G, B, 0, nface);
+    k_update<R, 3><<<nb(ncell, 256), 256, 0, s>>>(G, B, 0, ncell);
   }
   k_advance<R><<<1, 1, 0, s>>>(B.st);
   cudaError_t e = cudaGetLastError();

@@ -151,6 +151,14 @@ public:
   cudaGraphExec_t graph[2] = { nullptr, nullptr }; // one iteration starting from U / from U2
   cudaGraphExec_t graph_pair[2] = { nullptr, nullptr }; // two iterations
   int64_t launched = 0; // iterations enqueued since the last state reset (parity)
+  // host-buffer step: slabs of the edge/update stages whose download overlaps
+  // the rest of the edge stage (0 = chosen from the array size)
+  static constexpr int kMaxHostSlabs = 16;
+  int          host_slabs_req = 0;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t  slab_ev[kMaxHostSlabs] = {};
+  cudaEvent_t  up_ev[kMaxHostSlabs] = {};
+  cudaEvent_t  copy_ev = nullptr;
   // flux surrogate (FP32 builds only)
   uint32_t *           sur_w = nullptr; // packed weights + biases (mhd_mlp.cuh)
   unsigned long long * sur_count = nullptr;
@@ -170,6 +178,16 @@ public:
       if (graph_pair[q])
         cudaGraphExecDestroy(graph_pair[q]);
     }
+    for (cudaEvent_t e : slab_ev)
+      if (e)
+        cudaEventDestroy(e);
+    for (cudaEvent_t e : up_ev)
+      if (e)
+        cudaEventDestroy(e);
+    if (copy_ev)
+      cudaEventDestroy(copy_ev);
+    if (copy_stream)
+      cudaStreamDestroy(copy_stream);
     R * bufs[] = { U, U2, Q, Q2, S, E, F, Em, H, T, D };
     for (R * b : bufs)
       if (b)
@@ -387,23 +405,48 @@ public:
     else
       (void)B;
   }
+  // Planes along the slowest axis (z in 3D, y in 2D): the edge box has
+  // n + 1 of them, the interior box n.
+  int
+  slow_cells() const
+  {
+    return dim == 3 ? G.nz : G.ny;
+  }
+  // edges p0 <= plane < p1 of BOX_FACE
+  void
+  launch_emf_planes(const Buffers<R> & B, int p0, int p1)
+  {
+    const int64_t plane = (int64_t)(G.nx + 1) * (dim == 3 ? G.ny + 1 : 1);
+    const int64_t n = (int64_t)(p1 - p0) * plane;
+    if (n <= 0)
+      return;
+    if (dim == 2)
+      k_emf<R, 2><<<dim3(nblocks(n, 128), 1), 128, 0, stream>>>(G, B, p0 * plane, p1 * plane);
+    else
+      k_emf<R, 3><<<dim3(nblocks(n, 128), 3), 128, 0, stream>>>(G, B, p0 * plane, p1 * plane);
+  }
+  // interior cells p0 <= plane < p1
+  void
+  launch_update_planes(const Buffers<R> & B, int p0, int p1)
+  {
+    const int64_t plane = (int64_t)G.nx * (dim == 3 ? G.ny : 1);
+    const int64_t n = (int64_t)(p1 - p0) * plane;
+    if (n <= 0)
+      return;
+    if (dim == 2)
+      k_update<R, 2><<<nblocks(n, 256), 256, 0, stream>>>(G, B, p0 * plane, p1 * plane);
+    else
+      k_update<R, 3><<<nblocks(n, 256), 256, 0, stream>>>(G, B, p0 * plane, p1 * plane);
+  }
   void
   launch_emf(const Buffers<R> & B)
   {
-    const int64_t n = (int64_t)(G.nx + 1) * (G.ny + 1) * (dim == 3 ? G.nz + 1 : 1);
-    if (dim == 2)
-      k_emf<R, 2><<<dim3(nblocks(n, 128), 1), 128, 0, stream>>>(G, B);
-    else
-      k_emf<R, 3><<<dim3(nblocks(n, 128), 3), 128, 0, stream>>>(G, B);
+    launch_emf_planes(B, 0, slow_cells() + 1);
   }
   void
   launch_update(const Buffers<R> & B)
   {
-    const int64_t n = (int64_t)G.nx * G.ny * (dim == 3 ? G.nz : 1);
-    if (dim == 2)
-      k_update<R, 2><<<nblocks(n, 256), 256, 0, stream>>>(G, B);
-    else
-      k_update<R, 3><<<nblocks(n, 256), 256, 0, stream>>>(G, B);
+    launch_update_planes(B, 0, slow_cells());
   }
   // ---- versions 0 and 1 ----
   void
@@ -796,22 +839,178 @@ public:
     return status_check();
   }
 
+  // Slabs of the host-buffer step: one per 64 MiB of state, at most 8 (or
+  // the count set by set_host_slabs), never more than the planes.
+  int
+  host_slabs() const
+  {
+    const size_t bytes = (size_t)ncell * NV * sizeof(R);
+    int          n = host_slabs_req > 0 ? host_slabs_req
+                                        : (int)std::min<size_t>(8, bytes / ((size_t)64 << 20));
+    return std::max(1, std::min(n, slow_cells()));
+  }
+
+  int
+  set_host_slabs(int n) override
+  {
+    if (n < 0 || n > kMaxHostSlabs)
+    {
+      err = "host slabs must be in 0.." + std::to_string(kMaxHostSlabs);
+      return MHD_ERR_INVALID_ARG;
+    }
+    host_slabs_req = n;
+    return MHD_OK;
+  }
+
+  // One iteration on host arrays with the copies overlapped, in nslab slabs
+  // along the slowest axis (z in 3D, y in 2D).
+  //  in:  slab s of U_in goes up on a second stream; the main stream fills
+  //       the ghost cells of the slab's interior planes along the fast axes
+  //       (their sources lie in the same plane) and computes primitives and
+  //       CFL rates of every plane whose next plane has arrived (the cell
+  //       reads the face field of its +1 neighbour).  After the last slab:
+  //       the ghost planes of the slow axis, then their primitives.
+  //  out: edge EMFs and the update run slab by slab; update slab [u0, u1)
+  //       reads the edges of planes u0 .. u1, so the edge launch before it
+  //       covers every plane up to u1; each finished slab of U_out goes down
+  //       on the second stream while the next slab computes.
+  // Ghost planes travel with the first and last slab.  Every cell is
+  // computed once by the kernel bodies of enqueue_step, so the result is
+  // bitwise the same; only the order of the CFL atomics differs, and their
+  // maximum is order-independent.
+  int
+  enqueue_step_host(int parity, const void * in_host, void * out_host, int nslab)
+  {
+    if (!copy_stream)
+    {
+      MHD_CK(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+      MHD_CK(cudaEventCreateWithFlags(&copy_ev, cudaEventDisableTiming));
+      for (cudaEvent_t & e : slab_ev)
+        MHD_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      for (cudaEvent_t & e : up_ev)
+        MHD_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    const Buffers<R> B = buffers(parity);
+    const int        ns = slow_cells(), g = G.g;
+    const int        nplanes = dim == 3 ? G.ksize : G.jsize;
+    const int64_t    plane = dim == 3 ? G.sk : G.sj;      // array cells per plane
+    const int64_t    pplane = dim == 3 ? (int64_t)(G.isize - 1) * (G.jsize - 1)
+                                       : (int64_t)(G.isize - 1); // BOX_PRIM cells per plane
+    auto             u_lo = [&](int s) { return (int)((int64_t)s * ns / nslab); };
+    auto             a_lo = [&](int s) { return s == 0 ? 0 : g + u_lo(s); };
+    auto             a_hi = [&](int s) { return s == nslab - 1 ? nplanes : g + u_lo(s + 1); };
+    auto             copy = [&](void * dst, const void * src, int s, cudaMemcpyKind kind) -> int {
+      for (int v = 0; v < NV; ++v)
+      {
+        const int64_t off = v * G.sv + (int64_t)a_lo(s) * plane;
+        const size_t  bytes = (size_t)(a_hi(s) - a_lo(s)) * plane * sizeof(R);
+        MHD_CK(cudaMemcpyAsync(static_cast<R *>(dst) + off, static_cast<const R *>(src) + off,
+                               bytes, kind, copy_stream));
+      }
+      return MHD_OK;
+    };
+    auto bound = [&](int p0, int p1, int reset) {
+      const int64_t n = (int64_t)(p1 - p0) * plane;
+      if (n <= 0)
+        return;
+      if (dim == 2)
+        k_boundaries_range<R, 2>
+          <<<nblocks(n, 256), 256, 0, stream>>>(G, B.Uin, st, p0 * plane, p1 * plane, reset);
+      else
+        k_boundaries_range<R, 3>
+          <<<nblocks(n, 256), 256, 0, stream>>>(G, B.Uin, st, p0 * plane, p1 * plane, reset);
+    };
+    auto prim = [&](int p0, int p1) {
+      const int64_t n = (int64_t)(p1 - p0) * pplane;
+      if (n <= 0)
+        return;
+      if (dim == 2)
+        k_prim_dt_range<R, 2>
+          <<<nblocks(n, 256), 256, 0, stream>>>(G, B.Uin, Q, st, p0 * pplane, p1 * pplane);
+      else
+        k_prim_dt_range<R, 3>
+          <<<nblocks(n, 256), 256, 0, stream>>>(G, B.Uin, Q, st, p0 * pplane, p1 * pplane);
+    };
+    // uploads (ordered after everything already on the main stream)
+    MHD_CK(cudaEventRecord(copy_ev, stream));
+    MHD_CK(cudaStreamWaitEvent(copy_stream, copy_ev, 0));
+    for (int s = 0; s < nslab; ++s)
+    {
+      if (int rc = copy(B.Uin, in_host, s, cudaMemcpyHostToDevice))
+        return rc;
+      MHD_CK(cudaEventRecord(up_ev[s], copy_stream));
+    }
+    // ghost fill, primitives, CFL
+    int pdone = g; // BOX_PRIM planes g .. pdone-1 are done
+    for (int s = 0; s < nslab; ++s)
+    {
+      MHD_CK(cudaStreamWaitEvent(stream, up_ev[s], 0));
+      bound(g + u_lo(s), g + u_lo(s + 1), s == 0);
+      const int p1 = g + u_lo(s + 1) - 1;
+      prim(pdone, p1);
+      pdone = std::max(pdone, p1);
+    }
+    bound(0, g, 0);
+    bound(g + ns, nplanes, 0);
+    prim(0, g);
+    prim(pdone, nplanes - 1);
+    // dt, trace, face fluxes
+    const char * names[kMaxLaunches];
+    const int    n = step_kernel_names(names);
+    const int    q_emf = sur_on ? 6 : 5;
+    for (int q = 2; q < q_emf; ++q)
+      launch_stage(q, B);
+    // edges and update in slabs
+    int e_done = 0;
+    for (int s = 0; s < nslab; ++s)
+    {
+      launch_emf_planes(B, e_done, u_lo(s + 1) + 1);
+      e_done = u_lo(s + 1) + 1;
+      launch_update_planes(B, u_lo(s), u_lo(s + 1));
+      MHD_CK(cudaEventRecord(slab_ev[s], stream));
+    }
+    for (int q = q_emf + 2; q < n; ++q)
+      launch_stage(q, B);
+    if (int rc = check_launch())
+      return rc;
+    // downloads
+    for (int s = 0; s < nslab; ++s)
+    {
+      MHD_CK(cudaStreamWaitEvent(copy_stream, slab_ev[s], 0));
+      if (int rc = copy(out_host, B.Uout, s, cudaMemcpyDeviceToHost))
+        return rc;
+    }
+    MHD_CK(cudaEventRecord(copy_ev, copy_stream));
+    MHD_CK(cudaStreamWaitEvent(stream, copy_ev, 0));
+    return MHD_OK;
+  }
+
   int
   step_host(const void * Uin, void * Uout, int layout) override
   {
     if (int rc = read_state())
       return rc;
     launched = st_host->it;
-    R * cur = current();
-    if (int rc = upload(Uin, cur, layout))
-      return rc;
-    enqueue_step((int)(launched & 1));
-    ++launched;
-    if (int rc = check_launch())
-      return rc;
-    R * out = (launched & 1) ? U2 : U;
-    if (int rc = download(out, Uout, layout))
-      return rc;
+    const int  nslab = host_slabs();
+    const bool overlap = layout == MHD_LAYOUT_LEFT && version == 2 && nslab > 1;
+    R *        out = (launched & 1) ? U : U2; // the buffer this iteration writes
+    if (overlap)
+    {
+      if (int rc = enqueue_step_host((int)(launched & 1), Uin, Uout, nslab))
+        return rc;
+      ++launched;
+    }
+    else
+    {
+      if (int rc = upload(Uin, current(), layout))
+        return rc;
+      enqueue_step((int)(launched & 1));
+      ++launched;
+      if (int rc = check_launch())
+        return rc;
+      if (int rc = download(out, Uout, layout))
+        return rc;
+    }
     if (int rc = read_state())
       return rc;
     return status_check();

@@ -227,6 +227,53 @@ def test_step_host_and_step_match_run(mhdlib):
     assert a.time() == b.time() == c.time()
 
 
+@pytest.mark.parametrize("dim,nslab,bc", [(2, 2, (3,) * 6), (2, 5, (1, 2, 3, 3, 1, 1)),
+                                          (3, 3, (3,) * 6), (3, 16, (3,) * 6),
+                                          (3, 4, (1, 2, 3, 3, 2, 1))])
+def test_step_host_slabs_match_run(mhdlib, dim, nslab, bc):
+    """The host-buffer step in slabs (uploads overlapping the ghost fill and
+    primitives, downloads overlapping the edge stage) gives the state of
+    run(), bitwise: uneven slabs, more slabs requested than planes, and
+    reflecting / outflow / periodic faces."""
+    ini = (ot_ini(dim=2, nx=37, ny=29, bc=bc) if dim == 2
+           else ot_ini(dim=3, nx=13, ny=11, nz=9, bc=bc))
+    a = gpu_solver(mhdlib, ini, exact=True)
+    c = gpu_solver(mhdlib, ini, exact=True)
+    for s in (a, c):
+        s.init_problem()
+    c.set_host_slabs(nslab)
+    a.run(5)
+    U = c.get_state()
+    out = np.zeros_like(U)
+    for _ in range(5):
+        c.step_host(U, out)
+        U, out = out, U
+    assert np.array_equal(mhdlib.interior(a.get_state()), mhdlib.interior(U))
+    assert a.time() == c.time()
+
+
+def test_step_host_slabs_pinned_fp32(mhdlib):
+    """Pinned host buffers (copies truly asynchronous) in FP32, 3D."""
+    torch = pytest.importorskip("torch")
+    ini = ot_ini(dim=3, nx=24, ny=20, nz=18)
+    a = gpu_solver(mhdlib, ini, precision=32)
+    c = gpu_solver(mhdlib, ini, precision=32)
+    for s in (a, c):
+        s.init_problem()
+    c.set_host_slabs(4)
+    a.run(4)
+    U0 = c.get_state()
+    h_in = torch.from_numpy(U0.reshape(-1).copy()).pin_memory()
+    h_out = torch.zeros_like(h_in).pin_memory()
+    for q in range(4):
+        x, y = (h_in, h_out) if q % 2 == 0 else (h_out, h_in)
+        c.step_host_ptr(x.data_ptr(), y.data_ptr())
+    got = h_in.numpy().reshape(U0.shape)
+    assert np.array_equal(mhdlib.interior(a.get_state()), mhdlib.interior(got))
+    with pytest.raises(mhdlib.MHDError):
+        c.set_host_slabs(17)
+
+
 def test_stops_at_tend_like_the_reference(mhdlib, oracle):
     """dt is clipped so the last step lands on tEnd; the loop then stops."""
     ini = ot_ini(dim=2, nx=32, tend="0.05")

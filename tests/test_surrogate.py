@@ -238,6 +238,29 @@ def test_surrogate_flux_stage_against_fp64_oracle(mhdlib, oracle):
 
 
 @pytest.mark.gpu
+def test_surrogate_step_host_slabs_match_run(mhdlib):
+    """The host-buffer step in slabs with the network in the flux stage (one
+    more launch before the edge stage) gives the state of run(), bitwise."""
+    from ppkmhd_gb300.surrogate import FluxMLP
+
+    ini, U = _turbulence_case(24)
+    mlp = FluxMLP.load()
+    a = mhdlib.MHDSolver.from_ini(ini)
+    c = mhdlib.MHDSolver.from_ini(ini)
+    for s in (a, c):
+        s.set_state(U.astype(np.float32))
+        s.set_surrogate(mlp, tau=0.01)
+    c.set_host_slabs(3)
+    a.run(3)
+    V = c.get_state()
+    out = np.zeros_like(V)
+    for _ in range(3):
+        c.step_host(V, out)
+        V, out = out, V
+    assert np.array_equal(mhdlib.interior(a.get_state()), mhdlib.interior(V))
+
+
+@pytest.mark.gpu
 def test_tensor_core_wait_limit_reports_and_recovers(mhdlib):
     """A tensor-core completion wait that gives up is reported as an error
     (after the pending work drained), and the next call works again."""
