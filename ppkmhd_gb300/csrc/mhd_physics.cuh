@@ -691,8 +691,6 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R ent
       cstarl = cl * fe;
     }
   }
-  const R vdotbstarl = ustar * a + vstarl * bstarl + wstarl * cstarl;
-  const R etotstarl = (slu * etotl - ptotl * ul + ptotstar * ustar + a * (vdotbl - vdotbstarl)) * isls;
   const R rsl = rsq(rstarl);
   const R sqrrstarl = rstarl * rsl;
   const R sal = ustar - fabs(a) * rsl;
@@ -716,11 +714,21 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R ent
       cstarr = cr * fe;
     }
   }
-  const R vdotbstarr = ustar * a + vstarr * bstarr + wstarr * cstarr;
-  const R etotstarr = (sru * etotr - ptotr * ur + ptotstar * ustar + a * (vdotbr - vdotbstarr)) * isrs;
   const R rsr = rsq(rstarr);
   const R sqrrstarr = rstarr * rsr;
   const R sar = ustar + fabs(a) * rsr;
+
+  // Every star region takes its total energy (and v.B) from one side only:
+  // the left star region (sal > 0) from the left, the right ones
+  // (ustar <= 0, sar <= 0) from the right, the double-star region from the
+  // left iff ustar > 0.  So one side's energy is computed, with the
+  // reference's expressions; `left` is those region tests (with a number
+  // for sal, sal > 0 implies ustar > 0).
+  const bool left = gt0(sal) || gt0(ustar);
+  const R    vdotbstar = left ? ustar * a + vstarl * bstarl + wstarl * cstarl
+                              : ustar * a + vstarr * bstarr + wstarr * cstarr;
+  const R    etotstar = left ? (slu * etotl - ptotl * ul + ptotstar * ustar + a * (vdotbl - vdotbstar)) * isls
+                             : (sru * etotr - ptotr * ur + ptotstar * ustar + a * (vdotbr - vdotbstar)) * isrs;
 
   R ro, uo, vo, wo, bo, co, ptoto, etoto, vdotbo;
   if (gt0(sl))
@@ -731,14 +739,14 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R ent
   else if (gt0(sal))
   {
     ro = rstarl; uo = ustar; vo = vstarl; wo = wstarl; bo = bstarl; co = cstarl;
-    ptoto = ptotstar; etoto = etotstarl; vdotbo = vdotbstarl;
+    ptoto = ptotstar; etoto = etotstar; vdotbo = vdotbstar;
   }
   else if (!gt0(ustar) && !gt0(sar))
   {
     if (gt0(sr))
     {
       ro = rstarr; uo = ustar; vo = vstarr; wo = wstarr; bo = bstarr; co = cstarr;
-      ptoto = ptotstar; etoto = etotstarr; vdotbo = vdotbstarr;
+      ptoto = ptotstar; etoto = etotstar; vdotbo = vdotbstar;
     }
     else
     {
@@ -757,15 +765,15 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R ent
     uo = ustar;
     ptoto = ptotstar;
     vdotbo = ustar * a + vo * bo + wo * co;
-    if (gt0(ustar))
+    if (left)
     {
       ro = rstarl;
-      etoto = etotstarl - sgnm * sqrrstarl * (vdotbstarl - vdotbo);
+      etoto = etotstar - sgnm * sqrrstarl * (vdotbstar - vdotbo);
     }
     else
     {
       ro = rstarr;
-      etoto = etotstarr + sgnm * sqrrstarr * (vdotbstarr - vdotbo);
+      etoto = etotstar + sgnm * sqrrstarr * (vdotbstar - vdotbo);
     }
   }
   const R rou = ro * uo;
@@ -936,26 +944,29 @@ mag_riemann2d_hlld(const State<R> (&q)[4], const R (&e)[4], R gamma0, R smallc)
          SAT * SAB / (SAT - SAB) * (AstarT - AstarB) + SAR * SAL / (SAR - SAL) * (BstarR - BstarL);
 }
 
-// max_i |n_i| / sqrt(r_i) over four candidates with r_i > 0, with one rsqrt
-// instead of four: a knock-out between pairs compares n_i^2 r_j with
-// n_j^2 r_i (two FP64 multiplies and an integer-keyed compare), and only the
-// winner is evaluated.  The result is the largest candidate, or within one
-// rounding of it when two candidates tie to the last bits.
+// The Alfven-speed maximum of one side of the 2D HLLD: the largest |n|/sqrt(r)
+// over two corners, each with its state (n, r) and its compressed state
+// (n f, r f) (for example aLR over rstarLRx and AstarLR = aLR fLRy over
+// rstarLR = rstarLRx fLRy).  The compressed candidate squared is the plain
+// one times f, so it wins its corner iff f > 1 (an integer-keyed compare);
+// the two corner winners meet in one cross-multiplied comparison and only
+// the overall winner takes an rsqrt.  nf, rf are the compressed values as
+// the caller computed them, so the result is one of the four candidates,
+// the largest or within one rounding of it where two tie to the last bits.
 template <class R>
 __device__ __forceinline__ R
-alfven_max4(R n0, R r0, R n1, R r1, R n2, R r2, R n3, R r3)
+alfven_max2x2(R n0, R r0, R nf0, R rf0, R f0, R n1, R r1, R nf1, R rf1, R f1)
 {
-  const R    w0 = n0 * n0, w1 = n1 * n1, w2 = n2 * n2, w3 = n3 * n3;
-  const bool s1 = order_key(w1 * r0) > order_key(w0 * r1);
-  const R    na = s1 ? n1 : n0, ra = s1 ? r1 : r0, wa = s1 ? w1 : w0;
-  const bool s3 = order_key(w3 * r2) > order_key(w2 * r3);
-  const R    nb = s3 ? n3 : n2, rb = s3 ? r3 : r2, wb = s3 ? w3 : w2;
-  const bool sb = order_key(wb * ra) > order_key(wa * rb);
+  const long long one = order_key(R(1));
+  const bool      c0 = order_key(f0) > one, c1 = order_key(f1) > one;
+  const R         na = c0 ? nf0 : n0, ra = c0 ? rf0 : r0;
+  const R         nb = c1 ? nf1 : n1, rb = c1 ? rf1 : r1;
+  const bool      sb = order_key(nb * nb * ra) > order_key(na * na * rb);
   return fabs(sb ? nb : na) * rsq(sb ? rb : ra);
 }
 
 // The same 2D HLLD solve with shared reciprocals: 12 reciprocals, 10 square
-// roots and 12 rsqrt (4 in FP64, through alfven_max4) instead of ~75
+// roots and 12 rsqrt (4 in FP64, through alfven_max2x2) instead of ~75
 // divides and 32 square roots.
 template <class R>
 __device__ R
@@ -1024,10 +1035,14 @@ mag_riemann2d_hlld_fast(const State<R> (&q)[4], R gamma0, R smallc)
   R calfvenL, calfvenR, calfvenB, calfvenT;
   if constexpr (sizeof(R) == 8)
   {
-    calfvenL = sel_max(alfven_max4(aLR, rstarLRx, AstarLR, rstarLR, aLL, rstarLLx, AstarLL, rstarLL), smallc);
-    calfvenR = sel_max(alfven_max4(aRR, rstarRRx, AstarRR, rstarRR, aRL, rstarRLx, AstarRL, rstarRL), smallc);
-    calfvenB = sel_max(alfven_max4(bLL, rstarLLy, BstarLL, rstarLL, bRL, rstarRLy, BstarRL, rstarRL), smallc);
-    calfvenT = sel_max(alfven_max4(bLR, rstarLRy, BstarLR, rstarLR, bRR, rstarRRy, BstarRR, rstarRR), smallc);
+    calfvenL = sel_max(alfven_max2x2(aLR, rstarLRx, AstarLR, rstarLR, fLRy,
+                                     aLL, rstarLLx, AstarLL, rstarLL, fLLy), smallc);
+    calfvenR = sel_max(alfven_max2x2(aRR, rstarRRx, AstarRR, rstarRR, fRRy,
+                                     aRL, rstarRLx, AstarRL, rstarRL, fRLy), smallc);
+    calfvenB = sel_max(alfven_max2x2(bLL, rstarLLy, BstarLL, rstarLL, fLLx,
+                                     bRL, rstarRLy, BstarRL, rstarRL, fRLx), smallc);
+    calfvenT = sel_max(alfven_max2x2(bLR, rstarLRy, BstarLR, rstarLR, fLRx,
+                                     bRR, rstarRRy, BstarRR, rstarRR, fRRx), smallc);
   }
   else
   {
