@@ -126,12 +126,23 @@ fsqrt(float x)
     return x * rsq(x);
   return sqrtf(x);
 }
+// Square root of a positive normal double from the rsqrt.approx.ftz.f64 seed
+// y ~ x^-1/2: s = x y and e = 1 - s y (= 1 - x y^2 up to one rounding), then
+// one third-order Householder correction s (1 + e/2 + 3e^2/8), the Taylor
+// series of (1 - e)^-1/2 to second order: 5 FP64 operations (x * rsqrt(x)
+// takes 6).  Zero, subnormal, negative, infinite and NaN arguments go to sqrt.
 __device__ __forceinline__ double
 fsqrt(double x)
 {
-  const long long b = __double_as_longlong(x);
-  if (b > 0 && b < 0x7ff0000000000000LL)
-    return x * rsq(x);
+  const unsigned se = (unsigned)__double2hiint(x) >> 20; // sign and biased exponent
+  if (se - 1u < 0x7feu)                                  // positive, exponent 1 .. 0x7fe
+  {
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    const double s = x * y;
+    const double e = fma(-s, y, 1.0);
+    return fma(s * e, fma(e, 0.375, 0.5), s);
+  }
   return sqrt(x);
 }
 

@@ -1,8 +1,9 @@
 // Accuracy check of the fast builds' FP64 reciprocal and square root
 // (mhd_physics.cuh: rcp = one third-order Newton step on rcp.approx.ftz.f64,
-// fsqrt = x * rsqrt(x)) against correctly rounded host references, next to
-// the CUDA library's __drcp_rn, sqrt and rsqrt.  One thread per element, every
-// access in bounds.  Prints one line per function:
+// fsqrt = one third-order Householder correction of x * rsqrt.approx.ftz.f64)
+// against correctly rounded host references, next to the CUDA library's
+// __drcp_rn, sqrt and rsqrt and the two hardware seeds.  One thread per
+// element, every access in bounds.  Prints one line per function:
 //   <name> max_ulp <m> correctly_rounded <fraction>
 // and exits non-zero on a CUDA error.
 //
@@ -25,7 +26,9 @@ enum Op : int
   OP_FSQRT = 2,    // mhd::fsqrt(double)
   OP_SQRT = 3,     // sqrt
   OP_RSQ = 4,      // mhd::rsq(double) (= rsqrt)
-  OP_COUNT = 5
+  OP_RCP_SEED = 5, // rcp.approx.ftz.f64
+  OP_RSQ_SEED = 6, // rsqrt.approx.ftz.f64
+  OP_COUNT = 7
 };
 
 template <int OP>
@@ -45,8 +48,12 @@ k_apply(const double * __restrict__ x, double * __restrict__ y, int n)
     r = mhd::fsqrt(v);
   else if constexpr (OP == OP_SQRT)
     r = sqrt(v);
-  else
+  else if constexpr (OP == OP_RSQ)
     r = mhd::rsq(v);
+  else if constexpr (OP == OP_RCP_SEED)
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(v));
+  else
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(v));
   y[i] = r;
 }
 
@@ -79,7 +86,7 @@ main()
     return 1;
   }
   cudaMemcpy(dx, hx.data(), n * sizeof(double), cudaMemcpyHostToDevice);
-  const char * names[OP_COUNT] = { "rcp", "drcp_rn", "fsqrt", "sqrt", "rsq" };
+  const char * names[OP_COUNT] = { "rcp", "drcp_rn", "fsqrt", "sqrt", "rsq", "rcp_seed", "rsq_seed" };
   for (int op = 0; op < OP_COUNT; ++op)
   {
     const dim3 grid((n + 255) / 256), block(256);
@@ -89,7 +96,9 @@ main()
     case OP_DRCP_RN: k_apply<OP_DRCP_RN><<<grid, block>>>(dx, dy, n); break;
     case OP_FSQRT: k_apply<OP_FSQRT><<<grid, block>>>(dx, dy, n); break;
     case OP_SQRT: k_apply<OP_SQRT><<<grid, block>>>(dx, dy, n); break;
-    default: k_apply<OP_RSQ><<<grid, block>>>(dx, dy, n); break;
+    case OP_RSQ: k_apply<OP_RSQ><<<grid, block>>>(dx, dy, n); break;
+    case OP_RCP_SEED: k_apply<OP_RCP_SEED><<<grid, block>>>(dx, dy, n); break;
+    default: k_apply<OP_RSQ_SEED><<<grid, block>>>(dx, dy, n); break;
     }
     const cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess)
@@ -103,9 +112,9 @@ main()
     for (int i = 0; i < n; ++i)
     {
       const long double xv = hx[i];
-      const long double ref = (op == OP_RCP || op == OP_DRCP_RN) ? 1.0L / xv
-                              : (op == OP_RSQ)                   ? 1.0L / sqrtl(xv)
-                                                                 : sqrtl(xv);
+      const long double ref = (op == OP_RCP || op == OP_DRCP_RN || op == OP_RCP_SEED) ? 1.0L / xv
+                              : (op == OP_RSQ || op == OP_RSQ_SEED) ? 1.0L / sqrtl(xv)
+                                                                    : sqrtl(xv);
       const double u = ulp_error(hy[i], ref);
       maxu = u > maxu ? u : maxu;
       exact += hy[i] == (double)ref;
