@@ -711,7 +711,10 @@ def run_turbulence(args):
                                        "ms_per_step": ms_plain / args.steps}},
             "e2e": {"value": e2e_value, "unit": "cell-updates/s",
                     "h2d_bytes_per_step": U0.nbytes, "d2h_bytes_per_step": U0.nbytes,
-                    "steps": e2e_steps, "call": "mhd_step_host (pinned host buffers)"},
+                    "steps": e2e_steps,
+                    "call": "mhd_step_host (pinned host buffers, copies inside the timed region; "
+                            "uploads and downloads overlap the step slab by slab, one slab "
+                            "per 64 MiB of state, at most 8)"},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak,
                          "traffic": load_profile_traffic(args.workload, dom),
