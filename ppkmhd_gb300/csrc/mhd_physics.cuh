@@ -83,8 +83,10 @@ constexpr bool kExactOrder = MHD_EXACT_BUILD != 0;
 //    Arguments whose reciprocal is not a normal number (zero, subnormal,
 //    |x| >= 2^1021, infinite, NaN) take the library reciprocal.
 //  * FP64 rsqrt: the library's (within 0.51 ulp; 5 FP64 operations).
-//  * FP64 square root: x * rsqrt(x) for positive finite x (within 1.5 ulp,
-//    6 FP64 operations against 8 for the IEEE square root); other arguments
+//  * FP64 square root: x times the hardware approximation
+//    rsqrt.approx.ftz.f64 (relative error below 2^-20), refined by one
+//    third-order correction, for positive normal x: within 0.76 ulp in 5
+//    FP64 operations against 8 for the IEEE square root; other arguments
 //    take the IEEE square root.
 //  * FP32: the hardware approximations alone (about 1 ulp).
 __device__ __forceinline__ double
@@ -266,7 +268,7 @@ abs_le(R d, R t)
 // slot IB) of one state with one reciprocal of the density
 // (mhd_utils.h:89-117).  The callers take the square root of the largest
 // only: the square root is monotone, so max_i sqrt(x_i) = sqrt(max_i x_i)
-// (exactly for a correctly rounded root, within the 1.5 ulp of fsqrt).
+// (exactly for a correctly rounded root, within the 0.76 ulp of fsqrt).
 template <class R>
 __device__ __forceinline__ void
 fast_speeds2_xy(const State<R> & q, R gamma0, R & cfx2, R & cfy2)
