@@ -589,7 +589,25 @@ trace_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
   (void)dtdz;
 
   // edge electric field
-  if constexpr (DIM == 2)
+  if constexpr (!kExactOrder)
+  {
+    // E = u B - v A with u, v the means of 4 cells and A, B of 2 faces, as
+    // 0.125 (sum u sum B - sum v sum A): scaling by a power of two commutes
+    // with rounding, so this is the same value with 3 fewer FP64 operations
+    auto s4 = [&](uint32_t d1, uint32_t d2, int v) {
+      return Q[c - d1 - d2 + v * sv] + Q[c - d1 + v * sv] + Q[c - d2 + v * sv] + Q[c + v * sv];
+    };
+    auto s2 = [&](uint32_t d, int v) { return U[c - d + v * sv] + U[c + v * sv]; };
+    if constexpr (DIM == 2)
+      B.E[c] = R(0.125) * (s4(1u, sj, IU) * s2(1u, IB) - s4(1u, sj, IV) * s2(sj, IA));
+    else
+    {
+      B.E[c] = R(0.125) * (s4(sj, sk, IV) * s2(sj, IC) - s4(sj, sk, IW) * s2(sk, IB));
+      B.E[c + sv] = R(0.125) * (s4(1u, sk, IW) * s2(sk, IA) - s4(1u, sk, IU) * s2(1u, IC));
+      B.E[c + 2 * sv] = R(0.125) * (s4(1u, sj, IU) * s2(1u, IB) - s4(1u, sj, IV) * s2(sj, IA));
+    }
+  }
+  else if constexpr (DIM == 2)
   {
     const R u = R(0.25) * (Q[c - 1 - sj + IU * sv] + Q[c - 1 + IU * sv] + Q[c - sj + IU * sv] +
                            Q[c + IU * sv]);
