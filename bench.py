@@ -184,6 +184,28 @@ def dist_setup():
     return world, rank, local
 
 
+def link_bandwidth(h_src, h_dst) -> dict:
+    """GB/s of one plain host->device and one device->host copy of a pinned
+    host tensor (the host<->device link the host-buffer step uses), timed
+    after one untimed copy each way (the first touch of fresh pages is slow)."""
+    import torch
+
+    d = torch.empty_like(h_src, device="cuda")
+    nb = h_src.numel() * h_src.element_size()
+    d.copy_(h_src, non_blocking=True)
+    h_dst.copy_(d, non_blocking=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d.copy_(h_src, non_blocking=True)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    h_dst.copy_(d, non_blocking=True)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    del d
+    return {"h2d": round(nb / (t1 - t0) / 1e9, 1), "d2h": round(nb / (t2 - t1) / 1e9, 1)}
+
+
 def max_over_ranks(t_sec: float, world: int, device: str) -> float:
     """The slowest rank's time (every rank times the same replica work)."""
     if world <= 1:
@@ -377,6 +399,7 @@ def run_gb300(args):
                        pin_memory=True)
     h_out = torch.empty_like(h_in, pin_memory=True)
     h_in.numpy()[:] = U0.reshape(-1)
+    link = link_bandwidth(h_in, h_out)
     for _ in range(2):  # warm
         s.step_host_ptr(h_in.data_ptr(), h_out.data_ptr())
     torch.cuda.synchronize()
@@ -414,7 +437,8 @@ def run_gb300(args):
                     "steps": e2e_steps,
                     "call": "mhd_step_host (pinned host buffers, copies inside the timed region; "
                             "uploads and downloads overlap the step slab by slab, one slab "
-                            "per 64 MiB of state, at most 8)"},
+                            "per 64 MiB of state, at most 8)",
+                    "link_gbs": link},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                          "peak_source": f"hbm_gbs of {peak_kind}",
@@ -532,13 +556,14 @@ def run_ensemble(args):
         h = torch.empty(U.shape, dtype=torch.float32, pin_memory=True)
         h.numpy()[:] = U
         pinned.append(h)
+    ptrs = [h.data_ptr() for h in pinned]
+    ens.set_states_ptr(ptrs)  # untimed: first touch of the pinned pages
+    ens.get_states_ptr(ptrs)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for q, h in enumerate(pinned):
-        m.lib().mhd_ensemble_set_state(ens.h, q, h.data_ptr(), m.MHD_LAYOUT_LEFT, 4)
+    ens.set_states_ptr(ptrs)
     ens.run(e2e_steps)
-    for q, h in enumerate(pinned):
-        m.lib().mhd_ensemble_get_state(ens.h, q, h.data_ptr(), m.MHD_LAYOUT_LEFT, 4)
+    ens.get_states_ptr(ptrs)
     e2e_sec = time.perf_counter() - t0
     e2e_value = world * cells * e2e_steps / e2e_sec
 
@@ -579,8 +604,8 @@ def run_ensemble(args):
             "e2e": {"value": e2e_value, "unit": "cell-updates/s",
                     "h2d_bytes_per_step": state_bytes / e2e_steps,
                     "d2h_bytes_per_step": state_bytes / e2e_steps, "steps": e2e_steps,
-                    "call": "mhd_ensemble_set_state x512 + mhd_ensemble_run + "
-                            "mhd_ensemble_get_state x512 (pinned host buffers, inside the timed "
+                    "call": "mhd_ensemble_set_states + mhd_ensemble_run + "
+                            "mhd_ensemble_get_states (512 pinned host buffers, inside the timed "
                             "region)"},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak,
@@ -646,6 +671,7 @@ def run_turbulence(args):
     h_in = torch.empty(U0.size, dtype=torch.float32, pin_memory=True)
     h_out = torch.empty_like(h_in, pin_memory=True)
     h_in.numpy()[:] = U0.reshape(-1)
+    link = link_bandwidth(h_in, h_out)
     s.step_host_ptr(h_in.data_ptr(), h_out.data_ptr())
     e2e_steps = 3
     t0 = time.perf_counter()
@@ -714,7 +740,8 @@ def run_turbulence(args):
                     "steps": e2e_steps,
                     "call": "mhd_step_host (pinned host buffers, copies inside the timed region; "
                             "uploads and downloads overlap the step slab by slab, one slab "
-                            "per 64 MiB of state, at most 8)"},
+                            "per 64 MiB of state, at most 8)",
+                    "link_gbs": link},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak,
                          "traffic": load_profile_traffic(args.workload, dom),

@@ -242,6 +242,13 @@ int mhd_ensemble_init_problem(mhd_ensemble *ens, int prob);
 int mhd_ensemble_set_state(mhd_ensemble *ens, int prob, const void *U, int layout, int real_bytes);
 int mhd_ensemble_get_state(mhd_ensemble *ens, int prob, void *U, int layout, int real_bytes);
 
+/* Every problem at once: U[p] is problem p's array (n pointers, one layout
+ * and precision for all).  The copies and per-problem set-up are queued
+ * together and the stream is synchronised once per call, where the
+ * per-problem calls synchronise once per problem. */
+int mhd_ensemble_set_states(mhd_ensemble *ens, const void *const *U, int layout, int real_bytes);
+int mhd_ensemble_get_states(mhd_ensemble *ens, void *const *U, int layout, int real_bytes);
+
 /* nsteps iterations of every problem that is not finished (problems stop
  * on device at their own tEnd / nStepmax); *ms = elapsed device time (CUDA
  * events on the ensemble's stream; may be NULL).  All problems must be at

@@ -117,6 +117,8 @@ SIGNATURES = {
     "mhd_ensemble_destroy": (ctypes.c_int, [_vp]),
     "mhd_ensemble_init_problem": (ctypes.c_int, [_vp, ctypes.c_int]),
     "mhd_ensemble_set_state": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_int, ctypes.c_int]),
+    "mhd_ensemble_set_states": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int]),
+    "mhd_ensemble_get_states": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int]),
     "mhd_ensemble_get_state": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_int, ctypes.c_int]),
     "mhd_ensemble_run": (ctypes.c_int, [_vp, ctypes.c_int, _fp]),
     "mhd_ensemble_time": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _ip]),
@@ -455,6 +457,40 @@ class MHDEnsemble:
         self._check(lib().mhd_ensemble_get_state(self.h, int(prob), U.ctypes.data, layout,
                                                  U.itemsize))
         return U
+
+    def set_states(self, states, layout: int = MHD_LAYOUT_LEFT):
+        """Every problem's state in one call (one synchronisation)."""
+        arrs = []
+        for q, U in enumerate(states):
+            U = np.ascontiguousarray(U, dtype=self.real)
+            want = self.shape_left(q) if layout == MHD_LAYOUT_LEFT else self.shape_right(q)
+            if U.shape != want:
+                raise ValueError(f"state {q} shape {U.shape} != {want}")
+            arrs.append(U)
+        if len(arrs) != len(self.params):
+            raise ValueError(f"{len(arrs)} states for {len(self.params)} problems")
+        self.set_states_ptr([U.ctypes.data for U in arrs], layout)
+
+    def set_states_ptr(self, ptrs, layout: int = MHD_LAYOUT_LEFT):
+        """set_states on raw host pointers (e.g. pinned buffers), one per problem."""
+        if len(ptrs) != len(self.params):
+            raise ValueError(f"{len(ptrs)} pointers for {len(self.params)} problems")
+        arr = (ctypes.c_void_p * len(ptrs))(*ptrs)
+        self._check(lib().mhd_ensemble_set_states(self.h, arr, layout, np.dtype(self.real).itemsize))
+
+    def get_states(self, layout: int = MHD_LAYOUT_LEFT):
+        """Every problem's state in one call (one synchronisation)."""
+        out = [np.empty(self.shape_left(q) if layout == MHD_LAYOUT_LEFT else self.shape_right(q),
+                        dtype=self.real) for q in range(len(self.params))]
+        self.get_states_ptr([U.ctypes.data for U in out], layout)
+        return out
+
+    def get_states_ptr(self, ptrs, layout: int = MHD_LAYOUT_LEFT):
+        """get_states into raw host pointers, one per problem."""
+        if len(ptrs) != len(self.params):
+            raise ValueError(f"{len(ptrs)} pointers for {len(self.params)} problems")
+        arr = (ctypes.c_void_p * len(ptrs))(*ptrs)
+        self._check(lib().mhd_ensemble_get_states(self.h, arr, layout, np.dtype(self.real).itemsize))
 
     def run(self, n: int) -> float:
         """n iterations of every unfinished problem; returns device milliseconds."""

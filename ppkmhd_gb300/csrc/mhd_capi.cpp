@@ -648,6 +648,35 @@ extern "C"
     return from_core(e, e->core->get_state(prob, U, layout));
   }
 
+  static int
+  check_problem_arrays(mhd_ensemble * e, const void * const * U, int layout, int real_bytes)
+  {
+    if (!U)
+      return fail(e, MHD_ERR_INVALID_ARG, "null array of state pointers");
+    for (int p = 0; p < e->n; ++p)
+      if (int rc = check_problem_array(e, p, U[p], layout, real_bytes))
+        return rc;
+    return MHD_OK;
+  }
+
+  int
+  mhd_ensemble_set_states(mhd_ensemble * e, const void * const * U, int layout, int real_bytes)
+  {
+    NEED_ENSEMBLE(e);
+    if (int rc = check_problem_arrays(e, U, layout, real_bytes))
+      return rc;
+    return from_core(e, e->core->set_states(U, layout));
+  }
+
+  int
+  mhd_ensemble_get_states(mhd_ensemble * e, void * const * U, int layout, int real_bytes)
+  {
+    NEED_ENSEMBLE(e);
+    if (int rc = check_problem_arrays(e, U, layout, real_bytes))
+      return rc;
+    return from_core(e, e->core->get_states(U, layout));
+  }
+
   int
   mhd_ensemble_run(mhd_ensemble * e, int nsteps, float * ms)
   {

@@ -53,6 +53,8 @@ public:
   virtual int init_problem(int p) = 0;
   virtual int set_state(int p, const void * U, int layout) = 0;
   virtual int get_state(int p, void * U, int layout) = 0;
+  virtual int set_states(const void * const * U, int layout) = 0;
+  virtual int get_states(void * const * U, int layout) = 0;
   virtual int run(int nsteps, float * ms) = 0;
   virtual int time(int p, double * t, double * dt, int * it) = 0;
   virtual int diagnostics(int p, double sums[8], double * divb_l1, double * divb_max) = 0;

@@ -568,6 +568,27 @@ public:
     return MHD_OK;
   }
 
+  // Every problem's state in one call: uploads, record resets and the
+  // per-problem initialisation are queued together and the stream is
+  // synchronised once (set_state synchronises per problem).
+  int
+  set_states(const void * const * U, int layout) override
+  {
+    for (int p = 0; p < n; ++p)
+    {
+      if (int rc = upload(p, U[p], layout))
+        return rc;
+      reset_record(p);
+    }
+    MHD_ECK(cudaMemcpyAsync(st, st_host, (size_t)n * sizeof(DevState), cudaMemcpyHostToDevice,
+                            stream));
+    for (int p = 0; p < n; ++p)
+      if (int rc = apply_init(p))
+        return rc;
+    MHD_ECK(cudaStreamSynchronize(stream));
+    return MHD_OK;
+  }
+
   int
   init_problem(int p) override
   {
@@ -617,6 +638,30 @@ public:
       return rc;
     if (int rc = download(p, cur, U, layout))
       return rc;
+    MHD_ECK(cudaStreamSynchronize(stream));
+    return MHD_OK;
+  }
+
+  // Every problem's state in one call (one record read, one synchronisation).
+  int
+  get_states(void * const * U, int layout) override
+  {
+    if (int rc = read_records())
+      return rc;
+    for (int p = 0; p < n; ++p)
+    {
+      R *             cur = current(p);
+      const Grid<R> & g = G[p];
+      const int64_t   nall = g.box[BOX_ALL].count();
+      if (dim == 2)
+        k_boundaries<R, 2><<<blocks_for(nall, 256), 256, 0, stream>>>(g, cur, B[p].st, 1);
+      else
+        k_boundaries<R, 3><<<blocks_for(nall, 256), 256, 0, stream>>>(g, cur, B[p].st, 1);
+      if (int rc = check_launch())
+        return rc;
+      if (int rc = download(p, cur, U[p], layout))
+        return rc;
+    }
     MHD_ECK(cudaStreamSynchronize(stream));
     return MHD_OK;
   }

@@ -180,6 +180,34 @@ def test_ensemble_layout_right_and_stop_rules(mhdlib):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("layout", ["left", "right"])
+def test_ensemble_batched_state_calls_match_per_problem_calls(mhdlib, layout):
+    """set_states / get_states (one synchronisation per call) give what the
+    per-problem calls give, bitwise, in both layouts; a mismatched count or
+    precision is rejected."""
+    lay = mhdlib.MHD_LAYOUT_LEFT if layout == "left" else mhdlib.MHD_LAYOUT_RIGHT
+    probs = [workloads.ensemble_problem(s, precision=64, fp_mode="exact") for s in _small_specs()]
+    a = mhdlib.MHDEnsemble.from_ini([ini for ini, _ in probs])
+    b = mhdlib.MHDEnsemble.from_ini([ini for ini, _ in probs])
+    states = [U if lay == mhdlib.MHD_LAYOUT_LEFT else np.ascontiguousarray(U.transpose(2, 1, 0))
+              for _, U in probs]
+    for q, U in enumerate(states):
+        a.set_state(q, U, layout=lay)
+    b.set_states(states, layout=lay)
+    assert [a.time(q) for q in range(len(probs))] == [b.time(q) for q in range(len(probs))]
+    a.run(4)
+    b.run(4)
+    got = b.get_states(layout=lay)
+    for q in range(len(probs)):
+        assert np.array_equal(a.get_state(q, layout=lay), got[q]), q
+        assert a.time(q) == b.time(q)
+    with pytest.raises(ValueError):
+        b.set_states(states[:-1], layout=lay)
+    bad = (ctypes.c_void_p * len(states))(*[U.ctypes.data for U in states])
+    assert mhdlib.lib().mhd_ensemble_set_states(b.h, bad, lay, 4) == mhdlib.MHD_ERR_INVALID_ARG
+
+
+@pytest.mark.gpu
 def test_ensemble_autotune_keeps_results(mhdlib):
     probs = [workloads.ensemble_problem(s, precision=64, fp_mode="exact") for s in _small_specs()]
     a = mhdlib.MHDEnsemble.from_ini([ini for ini, _ in probs])
