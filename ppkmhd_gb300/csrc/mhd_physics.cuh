@@ -643,7 +643,11 @@ template <class R>
 __device__ void
 riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R entho)
 {
-  const R a = R(0.5) * (ql[IA] + qr[IA]);
+  // the version-2 face stage gives both states the face-centred normal field,
+  // and then the mean is that value exactly
+  R a = ql[IA];
+  if (fbits(ql[IA]) != fbits(qr[IA]))
+    a = R(0.5) * (ql[IA] + qr[IA]);
   const R a2 = a * a;
   const R sgnm = ge0(a) ? R(1) : R(-1);
 

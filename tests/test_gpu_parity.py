@@ -252,6 +252,25 @@ def test_step_host_slabs_match_run(mhdlib, dim, nslab, bc):
     assert a.time() == c.time()
 
 
+@pytest.mark.parametrize("version", [0, 1])
+def test_step_host_versions_0_1_ignore_slabs(mhdlib, version):
+    """Implementation versions 0 and 1 take the plain host-buffer path
+    whatever slab count is set, and still match run() bitwise."""
+    ini = ot_ini(dim=3, nx=12, ny=10, nz=9, version=version)
+    a = gpu_solver(mhdlib, ini, exact=True)
+    c = gpu_solver(mhdlib, ini, exact=True)
+    for s in (a, c):
+        s.init_problem()
+    c.set_host_slabs(4)
+    a.run(3)
+    U = c.get_state()
+    out = np.zeros_like(U)
+    for _ in range(3):
+        c.step_host(U, out)
+        U, out = out, U
+    assert np.array_equal(mhdlib.interior(a.get_state()), mhdlib.interior(U))
+
+
 def test_step_host_slabs_pinned_fp32(mhdlib):
     """Pinned host buffers (copies truly asynchronous) in FP32, 3D."""
     torch = pytest.importorskip("torch")
