@@ -85,6 +85,21 @@ def test_create_rejects_bad_parameters(mhdlib, field, value):
     assert e.value.code == mhdlib.MHD_ERR_INVALID_ARG
 
 
+def test_grid_size_limit(mhdlib):
+    """Kernels index inside an array with 32-bit offsets: ghost-inclusive
+    cells x 8 variables must stay below 4e9 (806^3 x 8 = 4.19e9 is refused
+    before any device work; 3 cells per direction is the smallest grid)."""
+    p = mhdlib.default_params()
+    p.dim, p.nx, p.ny, p.nz = 3, 800, 800, 800
+    with pytest.raises(mhdlib.MHDError) as e:
+        mhdlib.MHDSolver(p)
+    assert e.value.code == mhdlib.MHD_ERR_INVALID_ARG and "too large" in str(e.value)
+    p.nx = p.ny = p.nz = 2
+    with pytest.raises(mhdlib.MHDError) as e:
+        mhdlib.MHDSolver(p)
+    assert e.value.code == mhdlib.MHD_ERR_INVALID_ARG
+
+
 def test_fp32_exact_is_rejected(mhdlib):
     p = mhdlib.default_params()
     p.nx = p.ny = 16
