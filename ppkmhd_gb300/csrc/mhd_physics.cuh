@@ -735,17 +735,32 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R ent
   const R sqrrstarr = rstarr * rsr;
   const R sar = ustar + fabs(a) * rsr;
 
-  // Every star region takes its total energy (and v.B) from one side only:
-  // the left star region (sal > 0) from the left, the right ones
+  // Star-state total energy and v.B.  Every star region takes them from one
+  // side only: the left star region (sal > 0) from the left, the right ones
   // (ustar <= 0, sar <= 0) from the right, the double-star region from the
-  // left iff ustar > 0.  So one side's energy is computed, with the
-  // reference's expressions; `left` is those region tests (with a number
-  // for sal, sal > 0 implies ustar > 0).
-  const bool left = gt0(sal) || gt0(ustar);
-  const R    vdotbstar = left ? ustar * a + vstarl * bstarl + wstarl * cstarl
-                              : ustar * a + vstarr * bstarr + wstarr * cstarr;
-  const R    etotstar = left ? (slu * etotl - ptotl * ul + ptotstar * ustar + a * (vdotbl - vdotbstar)) * isls
-                             : (sru * etotr - ptotr * ur + ptotstar * ustar + a * (vdotbr - vdotbstar)) * isrs;
+  // left iff ustar > 0.  In FP64 (FP64-pipe bound) only that side is
+  // computed, with the reference's expressions, and both names below carry
+  // it; `left` repeats the region tests (with a number for sal, sal > 0
+  // implies ustar > 0).  In FP32 (issue bound) both sides cost fewer
+  // instructions than selecting the operands.
+  R vdotbstarl, etotstarl, vdotbstarr, etotstarr;
+  if constexpr (sizeof(R) == 8)
+  {
+    const bool left = gt0(sal) || gt0(ustar);
+    vdotbstarl = left ? ustar * a + vstarl * bstarl + wstarl * cstarl
+                      : ustar * a + vstarr * bstarr + wstarr * cstarr;
+    etotstarl = left ? (slu * etotl - ptotl * ul + ptotstar * ustar + a * (vdotbl - vdotbstarl)) * isls
+                     : (sru * etotr - ptotr * ur + ptotstar * ustar + a * (vdotbr - vdotbstarl)) * isrs;
+    vdotbstarr = vdotbstarl;
+    etotstarr = etotstarl;
+  }
+  else
+  {
+    vdotbstarl = ustar * a + vstarl * bstarl + wstarl * cstarl;
+    etotstarl = (slu * etotl - ptotl * ul + ptotstar * ustar + a * (vdotbl - vdotbstarl)) * isls;
+    vdotbstarr = ustar * a + vstarr * bstarr + wstarr * cstarr;
+    etotstarr = (sru * etotr - ptotr * ur + ptotstar * ustar + a * (vdotbr - vdotbstarr)) * isrs;
+  }
 
   R ro, uo, vo, wo, bo, co, ptoto, etoto, vdotbo;
   if (gt0(sl))
@@ -756,14 +771,14 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R ent
   else if (gt0(sal))
   {
     ro = rstarl; uo = ustar; vo = vstarl; wo = wstarl; bo = bstarl; co = cstarl;
-    ptoto = ptotstar; etoto = etotstar; vdotbo = vdotbstar;
+    ptoto = ptotstar; etoto = etotstarl; vdotbo = vdotbstarl;
   }
   else if (!gt0(ustar) && !gt0(sar))
   {
     if (gt0(sr))
     {
       ro = rstarr; uo = ustar; vo = vstarr; wo = wstarr; bo = bstarr; co = cstarr;
-      ptoto = ptotstar; etoto = etotstar; vdotbo = vdotbstar;
+      ptoto = ptotstar; etoto = etotstarr; vdotbo = vdotbstarr;
     }
     else
     {
@@ -782,15 +797,15 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R ent
     uo = ustar;
     ptoto = ptotstar;
     vdotbo = ustar * a + vo * bo + wo * co;
-    if (left)
+    if (gt0(ustar))
     {
       ro = rstarl;
-      etoto = etotstar - sgnm * sqrrstarl * (vdotbstar - vdotbo);
+      etoto = etotstarl - sgnm * sqrrstarl * (vdotbstarl - vdotbo);
     }
     else
     {
       ro = rstarr;
-      etoto = etotstar + sgnm * sqrrstarr * (vdotbstar - vdotbo);
+      etoto = etotstarr + sgnm * sqrrstarr * (vdotbstarr - vdotbo);
     }
   }
   const R rou = ro * uo;
