@@ -553,7 +553,10 @@ face_field_slope(const Grid<R> & G, const R * __restrict__ U, uint32_t c, int co
     return slope_limited(U[cv], U[cv + 1], U[cv - 1], G.slope_type);
   if (dir == 1)
     return slope_limited(U[cv], U[cv + sj], U[cv - sj], G.slope_type);
-  return slope_limited(U[cv], U[cv + sk], U[cv - sk], G.slope_type);
+  // the reference takes the minus sample at k + 1 as well
+  // (compute_limited_slope, MHDBaseFunctor3D.h:142), so the z slope is zero;
+  // the edge stage uses that zero directly and never calls this for z
+  return slope_limited(U[cv], U[cv + sk], U[cv + sk], G.slope_type);
 }
 
 
