@@ -405,10 +405,13 @@ def run_gb300(args):
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
+    per_step = []
     t0 = time.perf_counter()
     for q in range(e2e_steps):
         a, b = (h_in, h_out) if q % 2 == 0 else (h_out, h_in)
+        tq = time.perf_counter()
         s.step_host_ptr(a.data_ptr(), b.data_ptr())
+        per_step.append((time.perf_counter() - tq) * 1e3)
     e2e_sec = max_over_ranks(time.perf_counter() - t0, world, "cuda")
     e2e_value = world * interior_cells * e2e_steps / e2e_sec
 
@@ -438,7 +441,8 @@ def run_gb300(args):
                     "call": "mhd_step_host (pinned host buffers, copies inside the timed region; "
                             "uploads and downloads overlap the step slab by slab, one slab "
                             "per 64 MiB of state, at most 8)",
-                    "link_gbs": link},
+                    "link_gbs": link,
+                    "ms_each_step": [round(x, 2) for x in per_step]},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                          "peak_source": f"hbm_gbs of {peak_kind}",

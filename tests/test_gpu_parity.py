@@ -272,7 +272,8 @@ def test_step_host_versions_0_1_ignore_slabs(mhdlib, version):
 
 
 def test_step_host_slabs_pinned_fp32(mhdlib):
-    """Pinned host buffers (copies truly asynchronous) in FP32, 3D."""
+    """Pinned host buffers (copies truly asynchronous) in FP32, 3D, with the
+    slab count changed between steps: bitwise the state of run()."""
     torch = pytest.importorskip("torch")
     ini = ot_ini(dim=3, nx=24, ny=20, nz=18)
     a = gpu_solver(mhdlib, ini, precision=32)
@@ -280,15 +281,18 @@ def test_step_host_slabs_pinned_fp32(mhdlib):
     for s in (a, c):
         s.init_problem()
     c.set_host_slabs(4)
-    a.run(4)
+    a.run(6)
     U0 = c.get_state()
     h_in = torch.from_numpy(U0.reshape(-1).copy()).pin_memory()
     h_out = torch.zeros_like(h_in).pin_memory()
-    for q in range(4):
+    for q in range(6):
+        if q == 4:
+            c.set_host_slabs(3)
         x, y = (h_in, h_out) if q % 2 == 0 else (h_out, h_in)
         c.step_host_ptr(x.data_ptr(), y.data_ptr())
     got = h_in.numpy().reshape(U0.shape)
     assert np.array_equal(mhdlib.interior(a.get_state()), mhdlib.interior(got))
+    assert a.time() == c.time()
     with pytest.raises(mhdlib.MHDError):
         c.set_host_slabs(17)
 
