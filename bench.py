@@ -680,12 +680,16 @@ def run_turbulence(args):
     h_out = torch.empty_like(h_in, pin_memory=True)
     h_in.numpy()[:] = U0.reshape(-1)
     link = link_bandwidth(h_in, h_out)
-    s.step_host_ptr(h_in.data_ptr(), h_out.data_ptr())
+    for _ in range(2):  # warm
+        s.step_host_ptr(h_in.data_ptr(), h_out.data_ptr())
     e2e_steps = 3
+    per_step = []
     t0 = time.perf_counter()
     for q in range(e2e_steps):
         a, b = (h_in, h_out) if q % 2 == 0 else (h_out, h_in)
+        tq = time.perf_counter()
         s.step_host_ptr(a.data_ptr(), b.data_ptr())
+        per_step.append((time.perf_counter() - tq) * 1e3)
     e2e_value = cells * e2e_steps / (time.perf_counter() - t0)
     s.close()
     p32 = ctx(ini32, False)
@@ -749,7 +753,8 @@ def run_turbulence(args):
                     "call": "mhd_step_host (pinned host buffers, copies inside the timed region; "
                             "uploads and downloads overlap the step slab by slab, one slab "
                             "per 64 MiB of state, at most 8)",
-                    "link_gbs": link},
+                    "link_gbs": link,
+                    "ms_each_step": [round(x, 2) for x in per_step]},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak,
                          "traffic": load_profile_traffic(args.workload, dom),
