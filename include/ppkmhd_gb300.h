@@ -172,8 +172,9 @@ int mhd_run(mhd_ctx *ctx, int nsteps, int *done);
  * device, run one iteration, copy the result back.  The state inside the
  * context is replaced by U_in first, so t/dt bookkeeping continues.  With
  * MHD_LAYOUT_LEFT and implementation version 2 the copies overlap the step
- * in slabs along the slowest axis: each uploaded slab gets its ghost fill
- * and primitives while the next one arrives, and each finished slab of U_out
+ * in slabs along the slowest axis: each uploaded slab gets its ghost fill,
+ * primitives, slopes and edge field while the next one arrives, and each
+ * finished slab of U_out
  * is copied back while the next one's edges compute (same result, bitwise).
  * Pinned host buffers make the copies asynchronous. */
 int mhd_step_host(mhd_ctx *ctx, const void *U_in, void *U_out, int layout, int real_bytes);

@@ -570,7 +570,13 @@ face_field_slope(const Grid<R> & G, const R * __restrict__ U, uint32_t c, int co
 //    E = v x B at the lower edges of the cell.
 // Slopes and Q2 are only consumed on [g-1, size-g]^DIM, the edge field on
 // [g-1, size-g+1]^DIM.
-template <class R, int DIM>
+//
+// PART 0 does all of it.  The host-buffer step splits it where the time step
+// is first needed: PART 1 (edge field, slopes, face-field slopes: no dt) runs
+// while the state is still arriving, PART 2 (half step) after the CFL
+// reduction, reading the slopes back from S (the two normal-field slopes S
+// does not keep are the same face differences, taken again).
+template <class R, int DIM, int PART = 0>
 __device__ __forceinline__ void
 trace_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
 {
@@ -592,7 +598,10 @@ trace_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
   (void)dtdz;
 
   // edge electric field
-  if constexpr (!kExactOrder)
+  if constexpr (PART == 2)
+  {
+  }
+  else if constexpr (!kExactOrder)
   {
     // E = u B - v A with u, v the means of 4 cells and A, B of 2 faces, as
     // 0.125 (sum u sum B - sum v sum A): scaling by a power of two commutes
@@ -655,38 +664,54 @@ trace_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
 #pragma unroll
   for (int v = 0; v < NV; ++v)
     q[v] = Q[c + v * sv];
-#pragma unroll
-  for (int d = 0; d < DIM; ++d)
+  if constexpr (PART == 2)
   {
 #pragma unroll
-    for (int v = 0; v < NV; ++v)
-      s[d][v] = slope_limited(q[v], Q[c + off[d] + v * sv], Q[c - off[d] + v * sv], G.slope_type);
-    s[d][IA + d] = U[c + off[d] + (IA + d) * sv] - U[c + (IA + d) * sv];
-  }
-#pragma unroll
-  for (int d = 0; d < DIM; ++d)
-  {
-    R * Sd = B.S + (int64_t)d * NV * sv; // the 8 slope planes of direction d
-#pragma unroll
-    for (int v = 0; v < NV; ++v)
+    for (int d = 0; d < DIM; ++d)
     {
-      // the normal-field slope of directions x (and z in 3D, y in 2D) is
-      // read by no later stage: the face states take the face field, the
-      // edge states the face fields (only the y slope of By is read, by the
-      // 3D x edges' double increment)
-      if (v == IA + d && (d == 0 || d == DIM - 1))
-        continue;
-      Sd[c + v * sv] = s[d][v];
+      const R * Sd = B.S + (int64_t)d * NV * sv;
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+        s[d][v] = v == IA + d ? U[c + off[d] + (IA + d) * sv] - U[c + (IA + d) * sv] : Sd[c + v * sv];
     }
   }
-  // transverse slopes of the face-centred field for the edge stage
-  R * H = B.H;
-  H[c + FaceData<DIM>::slope_plane(0, 1) * sv] = face_field_slope<R, DIM>(G, U, c, IA, 1);
-  H[c + FaceData<DIM>::slope_plane(1, 0) * sv] = face_field_slope<R, DIM>(G, U, c, IB, 0);
-  if constexpr (DIM == 3)
+  else
   {
-    H[c + FaceData<DIM>::slope_plane(2, 0) * sv] = face_field_slope<R, DIM>(G, U, c, IC, 0);
-    H[c + FaceData<DIM>::slope_plane(2, 1) * sv] = face_field_slope<R, DIM>(G, U, c, IC, 1);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+    {
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+        s[d][v] = slope_limited(q[v], Q[c + off[d] + v * sv], Q[c - off[d] + v * sv], G.slope_type);
+      s[d][IA + d] = U[c + off[d] + (IA + d) * sv] - U[c + (IA + d) * sv];
+    }
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+    {
+      R * Sd = B.S + (int64_t)d * NV * sv; // the 8 slope planes of direction d
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+      {
+        // the normal-field slope of directions x (and z in 3D, y in 2D) is
+        // read by no later stage: the face states take the face field, the
+        // edge states the face fields (only the y slope of By is read, by the
+        // 3D x edges' double increment)
+        if (v == IA + d && (d == 0 || d == DIM - 1))
+          continue;
+        Sd[c + v * sv] = s[d][v];
+      }
+    }
+    // transverse slopes of the face-centred field for the edge stage
+    R * H = B.H;
+    H[c + FaceData<DIM>::slope_plane(0, 1) * sv] = face_field_slope<R, DIM>(G, U, c, IA, 1);
+    H[c + FaceData<DIM>::slope_plane(1, 0) * sv] = face_field_slope<R, DIM>(G, U, c, IB, 0);
+    if constexpr (DIM == 3)
+    {
+      H[c + FaceData<DIM>::slope_plane(2, 0) * sv] = face_field_slope<R, DIM>(G, U, c, IC, 0);
+      H[c + FaceData<DIM>::slope_plane(2, 1) * sv] = face_field_slope<R, DIM>(G, U, c, IC, 1);
+    }
+    if constexpr (PART == 1)
+      return;
   }
 
   // Hancock half step
@@ -779,6 +804,17 @@ __global__ void __launch_bounds__(128)
 k_trace(const Grid<R> G, Buffers<R> B)
 {
   trace_body<R, DIM>(G, B, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
+// Cells base <= index < end of BOX_TRACE, one part of trace_body (1: edge
+// field and slopes, 2: half step).
+template <class R, int DIM, int PART>
+__global__ void __launch_bounds__(128)
+k_trace_range(const Grid<R> G, Buffers<R> B, int64_t base, int64_t end)
+{
+  const int64_t idx = base + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx < end)
+    trace_body<R, DIM, PART>(G, B, idx);
 }
 
 // Half-step predictor of the face-centred field on face c normal to d

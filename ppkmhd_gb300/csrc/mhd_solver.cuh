@@ -940,8 +940,27 @@ public:
         return rc;
       MHD_CK(cudaEventRecord(up_ev[s], copy_stream));
     }
-    // ghost fill, primitives, CFL
-    int pdone = g; // BOX_PRIM planes g .. pdone-1 are done
+    // the trace stage in two parts over BOX_TRACE, whose plane kb is array
+    // plane g - 1 + kb: part 1 (no dt) of array planes p0 .. p1-1, part 2
+    const int64_t tplane = dim == 3 ? (int64_t)(G.nx + 3) * (G.ny + 3) : (int64_t)(G.nx + 3);
+    auto          trace = [&](int part, int p0, int p1) {
+      const int64_t t0 = (int64_t)(p0 - (g - 1)) * tplane, t1 = (int64_t)(p1 - (g - 1)) * tplane;
+      if (t1 <= t0)
+        return;
+      const unsigned nb = nblocks(t1 - t0, 128);
+      if (dim == 2 && part == 1)
+        k_trace_range<R, 2, 1><<<nb, 128, 0, stream>>>(G, B, t0, t1);
+      else if (dim == 2)
+        k_trace_range<R, 2, 2><<<nb, 128, 0, stream>>>(G, B, t0, t1);
+      else if (part == 1)
+        k_trace_range<R, 3, 1><<<nb, 128, 0, stream>>>(G, B, t0, t1);
+      else
+        k_trace_range<R, 3, 2><<<nb, 128, 0, stream>>>(G, B, t0, t1);
+    };
+    // ghost fill, primitives, CFL; part 1 of the trace stage on the planes
+    // whose primitives on both sides are done (it reads planes k-1 .. k+1)
+    int pdone = g;     // BOX_PRIM planes g .. pdone-1 are done
+    int tdone = g + 1; // trace part 1 of array planes g+1 .. tdone-1 is done
     for (int s = 0; s < nslab; ++s)
     {
       MHD_CK(cudaStreamWaitEvent(stream, up_ev[s], 0));
@@ -949,16 +968,22 @@ public:
       const int p1 = g + u_lo(s + 1) - 1;
       prim(pdone, p1);
       pdone = std::max(pdone, p1);
+      trace(1, tdone, pdone - 1);
+      tdone = std::max(tdone, pdone - 1);
     }
     bound(0, g, 0);
     bound(g + ns, nplanes, 0);
     prim(0, g);
     prim(pdone, nplanes - 1);
-    // dt, trace, face fluxes
+    trace(1, g - 1, g + 1);
+    trace(1, tdone, g + ns + 2);
+    // dt, trace part 2, face fluxes
     const char * names[kMaxLaunches];
     const int    n = step_kernel_names(names);
     const int    q_emf = sur_on ? 6 : 5;
-    for (int q = 2; q < q_emf; ++q)
+    launch_stage(2, B);
+    trace(2, g - 1, g + ns + 2);
+    for (int q = 4; q < q_emf; ++q)
       launch_stage(q, B);
     // edges and update in slabs
     int e_done = 0;
