@@ -174,14 +174,13 @@ int mhd_run(mhd_ctx *ctx, int nsteps, int *done);
  * MHD_LAYOUT_LEFT and implementation version 2 the copies overlap the step
  * in slabs along the slowest axis: each uploaded slab gets its ghost fill,
  * primitives, slopes and edge field while the next one arrives, and each
- * finished slab of U_out
- * is copied back while the next one's edges compute (same result, bitwise).
- * Pinned host buffers make the copies asynchronous. */
+ * finished slab of U_out is copied back while the next one's edges compute
+ * (same result, bitwise).  Pinned host buffers make the copies asynchronous. */
 int mhd_step_host(mhd_ctx *ctx, const void *U_in, void *U_out, int layout, int real_bytes);
 
 /* Slab count of mhd_step_host: 0 (default) = one slab per 64 MiB of state,
  * at most 8; 1 = no overlap; at most 16; never more than the grid's planes.
- * No counterpart in the reference (its state never leaves the device). */
+ * No counterpart in the reference, which copies no state per step. */
 int mhd_set_host_slabs(mhd_ctx *ctx, int nslabs);
 
 /* t, the dt of the last computed CFL condition, and the iteration count
