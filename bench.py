@@ -440,7 +440,7 @@ def run_gb300(args):
                     "steps": e2e_steps,
                     "call": "mhd_step_host (pinned host buffers, copies inside the timed region; "
                             "uploads and downloads overlap the step slab by slab, one slab "
-                            "per 64 MiB of state, at most 8)",
+                            "per 64 MiB of state, at most 16)",
                     "link_gbs": link,
                     "ms_each_step": [round(x, 2) for x in per_step]},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
@@ -752,7 +752,7 @@ def run_turbulence(args):
                     "steps": e2e_steps,
                     "call": "mhd_step_host (pinned host buffers, copies inside the timed region; "
                             "uploads and downloads overlap the step slab by slab, one slab "
-                            "per 64 MiB of state, at most 8)",
+                            "per 64 MiB of state, at most 16)",
                     "link_gbs": link,
                     "ms_each_step": [round(x, 2) for x in per_step]},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,

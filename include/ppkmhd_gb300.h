@@ -179,7 +179,7 @@ int mhd_run(mhd_ctx *ctx, int nsteps, int *done);
 int mhd_step_host(mhd_ctx *ctx, const void *U_in, void *U_out, int layout, int real_bytes);
 
 /* Slab count of mhd_step_host: 0 (default) = one slab per 64 MiB of state,
- * at most 8; 1 = no overlap; at most 16; never more than the grid's planes.
+ * at most 16; 1 = no overlap; never more than the grid's planes or 16.
  * No counterpart in the reference, which copies no state per step. */
 int mhd_set_host_slabs(mhd_ctx *ctx, int nslabs);
 

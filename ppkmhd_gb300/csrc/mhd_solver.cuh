@@ -839,14 +839,14 @@ public:
     return status_check();
   }
 
-  // Slabs of the host-buffer step: one per 64 MiB of state, at most 8 (or
+  // Slabs of the host-buffer step: one per 64 MiB of state, at most 16 (or
   // the count set by set_host_slabs), never more than the planes.
   int
   host_slabs() const
   {
     const size_t bytes = (size_t)ncell * NV * sizeof(R);
     int          n = host_slabs_req > 0 ? host_slabs_req
-                                        : (int)std::min<size_t>(8, bytes / ((size_t)64 << 20));
+                                        : (int)std::min<size_t>(16, bytes / ((size_t)64 << 20));
     return std::max(1, std::min(n, slow_cells()));
   }
 
