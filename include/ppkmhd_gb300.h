@@ -37,6 +37,7 @@ extern "C" {
 #define MHD_ERR_NUMERIC -4      /* device status word: non-finite or non-positive state */
 #define MHD_ERR_PARSE -5        /* .ini text rejected */
 #define MHD_ERR_TOO_LARGE -6    /* request larger than a fixed limit */
+#define MHD_FINISHED 1          /* mhd_step_noalloc: t >= tEnd, nothing was computed */
 
 /* enums.h:94-101 (RiemannSolverType); only the MHD solvers are accepted */
 #define MHD_RIEMANN_LLF 1
@@ -384,23 +385,30 @@ int mhd_surrogate_stats(mhd_ctx *ctx, int64_t *faces_network, int64_t *faces_tot
  * where an allocation may stall or fail, a job that must keep a fixed device
  * footprint after start-up).
  *
- * U_in and U_out are the caller's DEVICE arrays (LayoutLeft, ghost cells
- * included, real type per p->precision; U_in's ghost cells are refilled in
- * place, as the reference's make_boundaries(data_in) does).  Every
+ * U_in and U_out are the caller's DEVICE arrays on GPU p->device
+ * (LayoutLeft, ghost cells included, real type per p->precision).  U_in is
+ * written too: its ghost cells are refilled in place, as the reference's
+ * make_boundaries(data_in) does; its interior is only read.  Every
  * intermediate lives in a file-scope __device__ array of
- * MHD_NOALLOC_SCRATCH_BYTES; grids that need more return MHD_ERR_TOO_LARGE
- * (32 MiB holds about 280^2 interior cells in 2D or 33^3 in 3D in FP64, twice
- * as many in FP32).  t is the current time (dt is clipped to p->tEnd; when
- * t >= tEnd - 1e-14 nothing is computed and *dt = 0).  On return *dt holds
- * the dt of the iteration; the call synchronises `stream` (a cudaStream_t,
- * NULL for the legacy default stream).  Only MHD_FP_FAST and implementation
- * version 2 are accepted.
+ * MHD_NOALLOC_SCRATCH_BYTES, cleared by each call (cudaMemsetAsync, no
+ * allocation); grids that need more return MHD_ERR_TOO_LARGE (32 MiB holds
+ * about 280^2 interior cells in 2D or 33^3 in 3D in FP64, twice as many in
+ * FP32).  t is the current time and dt is clipped to p->tEnd.  When
+ * t >= tEnd - 1e-14 the call returns MHD_FINISHED with *dt = 0 and U_out
+ * untouched (no GPU work).  Otherwise, on MHD_OK, *dt holds the dt of the
+ * iteration and U_out the new state; the call synchronises `stream` (a
+ * cudaStream_t of p->device, NULL for the legacy default stream).  The
+ * kernels run on p->device; the calling thread's current device is restored
+ * before the call returns.  Only MHD_FP_FAST and implementation version 2
+ * are accepted.
  * The first call on a device looks up the scratch array's device address
- * (cudaGetSymbolAddress); make it before any stream capture.  All calls share
- * the array: calls that overlap on the GPU race and must be serialised.
- * Errors are reported by the status code only (no context exists).
+ * (cudaGetSymbolAddress) and keeps it for the process; make that call before
+ * any stream capture.  Calls after a cudaDeviceReset of that device are not
+ * supported (the address goes stale).  All calls share the array: calls that
+ * overlap on the GPU race and must be serialised.  Errors are reported by
+ * the status code only (no context exists).
  */
-int mhd_step_noalloc(const mhd_params *p, const void *U_in, void *U_out, double t, double *dt,
+int mhd_step_noalloc(const mhd_params *p, void *U_in, void *U_out, double t, double *dt,
                      void *stream);
 
 #ifdef __cplusplus

@@ -4,10 +4,16 @@
 # Test infrastructure only: used to pin the C restatement and to regenerate
 # tests/golden/.  Does not run the reference's own CMake build.
 #
-# usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   REFERENCE_ROOT defaults to $PPKMHD_REFERENCE_ROOT, else /root/reference.
+#   Where that tree is absent (the GPU host) the script does nothing.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${PPKMHD_REFERENCE_ROOT:-/root/reference}}"
+if [ ! -d "$REF/src/muscl" ]; then
+  echo "reference tree not found at $REF: oracle/_ref not built"
+  exit 0
+fi
 OUT="$HERE/_ref"
 mkdir -p "$OUT"
 SRCS=(

@@ -31,6 +31,7 @@ MHD_ERR_NO_DEVICE = -3
 MHD_ERR_NUMERIC = -4
 MHD_ERR_PARSE = -5
 MHD_ERR_TOO_LARGE = -6
+MHD_FINISHED = 1  # mhd_step_noalloc: t >= tEnd, nothing computed
 
 MHD_RIEMANN_LLF, MHD_RIEMANN_HLL, MHD_RIEMANN_HLLD = 1, 2, 4
 MHD_BC_REFLECTING, MHD_BC_OUTFLOW, MHD_BC_PERIODIC = 1, 2, 3

@@ -11,15 +11,20 @@
 // record) in one file-scope __device__ array of MHD_NOALLOC_SCRATCH_BYTES,
 // reserved by every GPU that loads this library until the process exits.
 //
-// The array is shared by all calls and keeps the last call's contents; the
-// time-step record is cleared at the start of each call, and every other
-// scratch value is written before it is read.  Calls that overlap on the GPU
+// The array is shared by all calls and keeps the last call's contents, so
+// each call clears the part it uses (cudaMemsetAsync on the caller's stream,
+// which allocates nothing) before its kernels run: the halo planes that no
+// stage writes (the last plane of the primitives, read by the slopes of the
+// last trace plane) then read zeros, as in the context path, whatever grid
+// or precision the previous call ran.  Calls that overlap on the GPU
 // (concurrent streams, or several host threads) race on the array: serialise
 // them.
 //
 // The first call on a device looks up the array's device address with
 // cudaGetSymbolAddress (host code cannot use the array's name as an address)
-// and caches it; make that first call before any stream capture.
+// and caches it per device; make that first call before any stream capture.
+// A cudaDeviceReset unloads the module and the cached address goes stale:
+// calls made after a reset of the device are not supported.
 #include <climits>
 #include <cstring>
 #include <mutex>
@@ -100,8 +105,8 @@ align256(size_t b)
 
 template <class R>
 int
-step(const mhd_params & p, const void * U_in, void * U_out, double t, double * dt,
-     cudaStream_t s, std::string & err)
+step(const mhd_params & p, void * U_in, void * U_out, double t, double * dt, cudaStream_t s,
+     std::string & err)
 {
   const Grid<R> G = make_grid<R>(p);
 
@@ -124,7 +129,7 @@ step(const mhd_params & p, const void * U_in, void * U_out, double t, double * d
     return rc;
   unsigned char * q = static_cast<unsigned char *>(base);
   Buffers<R>      B{};
-  B.Uin = const_cast<R *>(static_cast<const R *>(U_in));
+  B.Uin = static_cast<R *>(U_in);
   B.Uout = static_cast<R *>(U_out);
   B.Q = reinterpret_cast<R *>(q);
   q += b8;
@@ -143,6 +148,12 @@ step(const mhd_params & p, const void * U_in, void * U_out, double t, double * d
   B.st = reinterpret_cast<DevState *>(q);
 
   auto nb = [](int64_t cnt, int th) { return (unsigned)((cnt + th - 1) / th); };
+  cudaError_t e = cudaMemsetAsync(base, 0, need, s);
+  if (e != cudaSuccess)
+  {
+    err = std::string("clearing the scratch array: ") + cudaGetErrorString(e);
+    return MHD_ERR_CUDA;
+  }
   k_noalloc_reset<<<1, 1, 0, s>>>(B.st, t, p.tEnd);
   const int64_t nall = (int64_t)n;
   const int64_t nprim = (int64_t)(G.isize - 1) * (G.jsize - 1) * (dim == 3 ? G.ksize - 1 : 1);
@@ -170,7 +181,7 @@ step(const mhd_params & p, const void * U_in, void * U_out, double t, double * d
     k_update<R, 3><<<nb(ncell, 256), 256, 0, s>>>(G, B, 0, ncell);
   }
   k_advance<R><<<1, 1, 0, s>>>(B.st);
-  cudaError_t e = cudaGetLastError();
+  e = cudaGetLastError();
   if (e != cudaSuccess)
   {
     err = std::string("kernel launch: ") + cudaGetErrorString(e);
@@ -200,7 +211,7 @@ extern "C"
 {
 
   int
-  mhd_step_noalloc(const mhd_params * p, const void * U_in, void * U_out, double t, double * dt,
+  mhd_step_noalloc(const mhd_params * p, void * U_in, void * U_out, double t, double * dt,
                    void * stream)
   {
     if (!p || !U_in || !U_out || !dt || U_in == U_out)
@@ -208,11 +219,25 @@ extern "C"
     if (!mhd::validate_params(*p).empty() || p->fp_mode != MHD_FP_FAST ||
         p->implementation_version != 2)
       return MHD_ERR_INVALID_ARG;
+    // the reference's finished() test (SolverBase.cpp:195-201): nothing to do
+    if (t >= p->tEnd - 1e-14)
+    {
+      *dt = 0.0;
+      return MHD_FINISHED;
+    }
+    // run on p->device and give the caller's current device back afterwards
+    int prev = 0;
+    if (cudaGetDevice(&prev) != cudaSuccess)
+      return MHD_ERR_NO_DEVICE;
+    if (prev != p->device && cudaSetDevice(p->device) != cudaSuccess)
+      return MHD_ERR_NO_DEVICE;
     std::string  err; // status codes carry the outcome; the text is not kept
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (p->precision == MHD_FP32)
-      return step<float>(*p, U_in, U_out, t, dt, s, err);
-    return step<double>(*p, U_in, U_out, t, dt, s, err);
+    const int    rc = p->precision == MHD_FP32 ? step<float>(*p, U_in, U_out, t, dt, s, err)
+                                               : step<double>(*p, U_in, U_out, t, dt, s, err);
+    if (prev != p->device)
+      cudaSetDevice(prev);
+    return rc;
   }
 
 } // extern "C"

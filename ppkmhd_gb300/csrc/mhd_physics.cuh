@@ -93,7 +93,7 @@ __device__ __forceinline__ double
 rcp(double x)
 {
   const unsigned ex = ((unsigned)__double2hiint(x) >> 20) & 0x7ffu;
-  if (ex - 1u < 0x7fcu) // 1 <= biased exponent <= 0x7fc
+  if (ex - 1u < 0x7fbu) // 1 <= biased exponent <= 0x7fb: 2^-1022 <= |x| < 2^1021
   {
     double y;
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));

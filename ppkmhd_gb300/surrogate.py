@@ -8,6 +8,9 @@ weights ``ppkmhd_gb300/data/flux_mlp.npz``:
 
     python -m ppkmhd_gb300.surrogate train --out ppkmhd_gb300/data/flux_mlp.npz
 
+``python -m ppkmhd_gb300.surrogate train --workload kh`` makes the
+Kelvin-Helmholtz network (gamma0 = 1.4) ``ppkmhd_gb300/data/flux_mlp_kh.npz``.
+
 ``python -m ppkmhd_gb300.surrogate run --n 96 --steps 3`` runs the
 turbulence state with the network (the case the flux-stage profile uses).
 
@@ -188,6 +191,27 @@ def harvest_training_set(scale: float = 1.0, seed: int = 5) -> np.ndarray:
     return np.concatenate(out, axis=0)
 
 
+KH_GAMMA = workloads.f32("1.4")
+KH_WEIGHTS = os.path.join(DATA, "flux_mlp_kh.npz")
+
+
+def harvest_kh_training_set(scale: float = 1.0, seed: int = 5) -> np.ndarray:
+    """Face records from FP32 runs of the magnetised Kelvin-Helmholtz shear
+    layer (gamma0 = 1.4, periodic x, reflecting y) at 512^2 and 1024^2 with
+    other perturbation seeds than the deployed 4096^2 run, harvested every
+    100 steps over 1000 steps (`scale` multiplies the number of runs)."""
+    out: list = []
+    rng = np.random.default_rng(seed)
+    reps = max(1, int(round(2 * scale)))
+    for n in (512, 1024):
+        for _ in range(reps):
+            U = workloads.kelvin_helmholtz(n, seed=int(rng.integers(100, 2 ** 31 - 1)))
+            s = _solver(workloads.kh_ini(n, precision=32), U)
+            _collect(s, steps=1000, every=100, stride=2 if n == 512 else 4, out=out)
+            s.close()
+    return np.concatenate(out, axis=0)
+
+
 def evaluate(m: FluxMLP, records: np.ndarray) -> dict:
     """Errors of the deployed (tensor-core) forward on held-out records:
     relative L1 of the dissipation D and of the full flux against HLLD."""
@@ -239,15 +263,19 @@ def evaluate(m: FluxMLP, records: np.ndarray) -> dict:
 
 
 def train(out: str = DEFAULT_WEIGHTS, scale: float = 2.0, epochs: int = 250, batch: int = 16384,
-          lr: float = 3e-3, seed: int = 1, weight_power: float = 1.0, log=print) -> dict:
+          lr: float = 3e-3, seed: int = 1, weight_power: float = 1.0, log=print,
+          workload: str = "ot") -> dict:
+    """Harvest, train and save.  workload "ot": the Orszag-Tang and turbulence
+    set at gamma0 = 5/3 (the committed flux_mlp.npz); "kh": the Kelvin-Helmholtz
+    set at gamma0 = 1.4 (flux_mlp_kh.npz)."""
     t0 = time.time()
-    rec = harvest_training_set(scale)
+    rec = harvest_kh_training_set(scale) if workload == "kh" else harvest_training_set(scale)
     rng = np.random.default_rng(seed)
     rng.shuffle(rec)
     nval = min(200000, rec.shape[0] // 10)
     val, trn = rec[:nval], rec[nval:]
     log(f"harvested {rec.shape[0]} smooth face records in {time.time() - t0:.1f} s")
-    m = FluxMLP(seed=seed, gamma0=GAMMA)
+    m = FluxMLP(seed=seed, gamma0=KH_GAMMA if workload == "kh" else GAMMA)
     t1 = time.time()
     hist = m.train(trn, epochs=epochs, batch=batch, lr=lr, seed=seed, weight_power=weight_power)
     t_train = time.time() - t1
@@ -256,7 +284,7 @@ def train(out: str = DEFAULT_WEIGHTS, scale: float = 2.0, epochs: int = 250, bat
     log(json.dumps(ev))
     meta = {"samples_train": int(trn.shape[0]), "samples_val": int(nval), "epochs": epochs,
             "batch": batch, "lr": lr, "seed": seed, "weight_power": weight_power,
-            "scale": scale, "train_seconds": t_train,
+            "scale": scale, "train_seconds": t_train, "workload": workload,
             "loss_history": [float(x) for x in hist], "validation": ev}
     m.save(out, **meta)
     return meta
@@ -290,12 +318,15 @@ def main():
     t.add_argument("--lr", type=float, default=3e-3)
     t.add_argument("--seed", type=int, default=1)
     t.add_argument("--weight-power", type=float, default=1.0)
+    t.add_argument("--workload", choices=("ot", "kh"), default="ot")
     a = ap.parse_args()
     if a.cmd == "run":
         used, total = run_turbulence(a.n, a.steps, a.tau)
         print(json.dumps({"faces_network": used, "faces_total": total}))
     if a.cmd == "train":
-        meta = train(a.out, a.scale, a.epochs, a.batch, a.lr, a.seed, a.weight_power)
+        out = a.out if not (a.workload == "kh" and a.out == DEFAULT_WEIGHTS) else KH_WEIGHTS
+        meta = train(out, a.scale, a.epochs, a.batch, a.lr, a.seed, a.weight_power,
+                     workload=a.workload)
         print(json.dumps({k: v for k, v in meta.items() if k != "loss_history"}))
 
 

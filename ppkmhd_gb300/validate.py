@@ -10,7 +10,9 @@ are defined with and reports what must hold at the end:
 * C2  512-problem 2D ensemble FP32, 500 steps
 * C3  3D turbulence 512^3 FP32 with the flux surrogate, 300 steps (relative
       L1 against plain FP32 HLLD per variable)
-* C4  2D Kelvin-Helmholtz 4096^2 FP32, 2000 steps
+* C4  2D Kelvin-Helmholtz 4096^2 FP32, 2000 steps, plain and with the flux
+      surrogate, relative L1 of both against FP64 (4096^2, and 512^2 against
+      the bitwise-reference FP64 build)
 
 For every run: the largest |div B| (FP64 sums of the face-centred field),
 and the relative drift of the conserved totals that the boundary conditions
@@ -148,11 +150,33 @@ def c3(device: int) -> dict:
             "plain_fp32": r_plain, "rel_l1_vs_plain_fp32": err}
 
 
-def c4(device: int) -> dict:
-    n, steps = 4096, 2000
-    s = _solver(workloads.kh_ini(n, precision=32), workloads.kelvin_helmholtz(n), device)
-    out = {"config": "C4 2D Kelvin-Helmholtz 4096^2 FP32"} | _run(s, steps)
+def _kh(n: int, steps: int, device: int, precision: int, mlp=None, fp_mode=None):
+    U = workloads.kelvin_helmholtz(n)
+    s = _solver(workloads.kh_ini(n, precision=precision, fp_mode=fp_mode), U, device, mlp=mlp)
+    out = _run(s, steps)
+    if mlp is not None:
+        used, total = s.surrogate_stats()
+        out["faces_by_network"] = used / max(total, 1)
+    state = interior(s.get_state())
     s.close()
+    return out, state
+
+
+def c4(device: int) -> dict:
+    """Kelvin-Helmholtz 4096^2, 2000 steps: FP32, FP32 with the flux surrogate
+    (the gamma0 = 1.4 network), and FP64 as the accuracy reference; the same
+    three at 512^2 with the bitwise-reference FP64 build."""
+    steps = 2000
+    mlp = surrogate.FluxMLP.load(surrogate.KH_WEIGHTS)
+    out = {"config": "C4 2D Kelvin-Helmholtz 4096^2 FP32 (+ flux surrogate)"}
+    for n, mode in ((4096, "fast"), (512, "exact")):
+        r64, ref = _kh(n, steps, device, 64, fp_mode=mode)
+        r32, s32 = _kh(n, steps, device, 32)
+        rmlp, smlp = _kh(n, steps, device, 32, mlp=mlp)
+        tag = "" if n == 4096 else "_512"
+        out[f"fp32{tag}"] = r32 | {"rel_l1_vs_fp64": _rel_l1(s32, ref)}
+        out[f"fp32_surrogate{tag}"] = rmlp | {"rel_l1_vs_fp64": _rel_l1(smlp, ref)}
+        out[f"fp64{tag}"] = r64 | {"fp_mode": mode}
     return out
 
 

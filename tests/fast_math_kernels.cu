@@ -1,0 +1,192 @@
+// Test kernels of tests/test_fast_math.py: the fast builds' FP64 reciprocal
+// and square root (mhd_physics.cuh: rcp = one third-order Newton step on
+// rcp.approx.ftz.f64, fsqrt = one third-order Householder correction of
+// x * rsqrt.approx.ftz.f64) against correctly rounded host references, next
+// to the CUDA library's __drcp_rn, sqrt and rsqrt; and, on the arguments that
+// take the fallback branches (zeros, subnormals, |x| >= 2^1021, infinities,
+// NaN, negative numbers), bit for bit against the library function they fall
+// back to.  One thread per element, every access in bounds.  Prints
+//   <name> max_ulp <m> correctly_rounded <fraction>      (normal arguments)
+//   special_<name> mismatches <count> of <n>             (fallback arguments)
+// and exits non-zero on a CUDA error.
+//
+// Build and run (GB300):
+//   nvcc -gencode arch=compute_103a,code=sm_103a -O3 -o fast_math_kernels tests/fast_math_kernels.cu
+//   ./fast_math_kernels
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../ppkmhd_gb300/csrc/mhd_physics.cuh"
+
+enum Op : int
+{
+  OP_RCP = 0,      // mhd::rcp(double)
+  OP_DRCP_RN = 1,  // __drcp_rn
+  OP_FSQRT = 2,    // mhd::fsqrt(double)
+  OP_SQRT = 3,     // sqrt
+  OP_RSQ = 4,      // mhd::rsq(double) (= rsqrt)
+  OP_COUNT = 5
+};
+
+template <int OP>
+__global__ void
+k_apply(const double * __restrict__ x, double * __restrict__ y, int n)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  const double v = x[i];
+  double       r;
+  if constexpr (OP == OP_RCP)
+    r = mhd::rcp(v);
+  else if constexpr (OP == OP_DRCP_RN)
+    r = __drcp_rn(v);
+  else if constexpr (OP == OP_FSQRT)
+    r = mhd::fsqrt(v);
+  else if constexpr (OP == OP_SQRT)
+    r = sqrt(v);
+  else
+    r = mhd::rsq(v);
+  y[i] = r;
+}
+
+static double
+ulp_error(double got, long double ref)
+{
+  const double r = (double)ref;
+  const double u = std::nextafter(std::fabs(r), INFINITY) - std::fabs(r);
+  return (double)(std::fabs((long double)got - ref) / (long double)u);
+}
+
+template <int OP>
+static int
+launch(const double * dx, double * dy, int n)
+{
+  k_apply<OP><<<(n + 255) / 256, 256>>>(dx, dy, n);
+  return cudaDeviceSynchronize() == cudaSuccess ? 0 : 1;
+}
+
+static int
+apply(int op, const double * dx, double * dy, int n)
+{
+  switch (op)
+  {
+  case OP_RCP: return launch<OP_RCP>(dx, dy, n);
+  case OP_DRCP_RN: return launch<OP_DRCP_RN>(dx, dy, n);
+  case OP_FSQRT: return launch<OP_FSQRT>(dx, dy, n);
+  case OP_SQRT: return launch<OP_SQRT>(dx, dy, n);
+  default: return launch<OP_RSQ>(dx, dy, n);
+  }
+}
+
+static bool
+same_bits(double a, double b)
+{
+  if (std::isnan(a) && std::isnan(b))
+    return true;
+  uint64_t x, y;
+  std::memcpy(&x, &a, 8);
+  std::memcpy(&y, &b, 8);
+  return x == y;
+}
+
+int
+main()
+{
+  const int           n = 1 << 20;
+  std::vector<double> hx(n), hy(n), hz(n);
+  // log-uniform over [1e-30, 1e30] from a fixed LCG, plus exact powers of two
+  uint64_t s = 0x2545F4914F6CDD1DULL;
+  for (int i = 0; i < n; ++i)
+  {
+    s = s * 6364136223846793005ULL + 1442695040888963407ULL;
+    const double u = (double)(s >> 11) / 9007199254740992.0;
+    hx[i] = (i % 97 == 0) ? std::ldexp(1.0, (i / 97) % 200 - 100) : std::pow(10.0, -30.0 + 60.0 * u);
+  }
+  // arguments of the fallback branches and the edges of the fast ranges
+  std::vector<double> sp = { 0.0, -0.0, INFINITY, -INFINITY, NAN, -NAN,
+                             std::ldexp(1.0, -1074), std::ldexp(1.0, -1073), std::ldexp(3.0, -1050),
+                             -std::ldexp(1.0, -1074), std::nextafter(std::ldexp(1.0, -1022), 0.0),
+                             std::ldexp(1.0, -1022), std::nextafter(std::ldexp(1.0, -1022), 1.0),
+                             std::ldexp(1.0, 1021), std::nextafter(std::ldexp(1.0, 1021), 0.0),
+                             std::ldexp(1.5, 1021), std::ldexp(1.0, 1022), std::ldexp(1.0, 1023),
+                             std::nextafter(std::ldexp(1.0, 1022), 0.0), -std::ldexp(1.9, 1021),
+                             1.7976931348623157e308, -1.0, -2.5e-300, -1e300, 1.0, 2.0, 0.5 };
+  for (int e = -1074; e <= 1023; e += 7)
+  {
+    sp.push_back(std::ldexp(1.0, e));
+    sp.push_back(-std::ldexp(1.3, e < 1023 ? e : 1022));
+    sp.push_back(std::ldexp(1.7, e < 1023 ? e : 1022));
+  }
+  const int ns = (int)sp.size();
+  double *  dx = nullptr, *dy = nullptr;
+  if (cudaMalloc(&dx, n * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&dy, n * sizeof(double)) != cudaSuccess)
+  {
+    std::printf("cudaMalloc failed\n");
+    return 1;
+  }
+  const char * names[OP_COUNT] = { "rcp", "drcp_rn", "fsqrt", "sqrt", "rsq" };
+  cudaMemcpy(dx, hx.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+  for (int op = 0; op < OP_COUNT; ++op)
+  {
+    if (apply(op, dx, dy, n))
+    {
+      std::printf("%s: CUDA error\n", names[op]);
+      return 1;
+    }
+    cudaMemcpy(hy.data(), dy, n * sizeof(double), cudaMemcpyDeviceToHost);
+    double maxu = 0.0;
+    long   exact = 0;
+    for (int i = 0; i < n; ++i)
+    {
+      const long double xv = hx[i];
+      const long double ref = (op == OP_RCP || op == OP_DRCP_RN) ? 1.0L / xv
+                              : (op == OP_RSQ)                  ? 1.0L / sqrtl(xv)
+                                                                : sqrtl(xv);
+      const double u = ulp_error(hy[i], ref);
+      maxu = u > maxu ? u : maxu;
+      exact += hy[i] == (double)ref;
+    }
+    std::printf("%s max_ulp %.6f correctly_rounded %.6f\n", names[op], maxu, (double)exact / n);
+  }
+  // fallback arguments: the fast function against the library one it falls
+  // back to (rcp -> __drcp_rn, fsqrt -> sqrt), bit for bit
+  cudaMemcpy(dx, sp.data(), ns * sizeof(double), cudaMemcpyHostToDevice);
+  const int pairs[2][2] = { { OP_RCP, OP_DRCP_RN }, { OP_FSQRT, OP_SQRT } };
+  for (const auto & pr : pairs)
+  {
+    if (apply(pr[0], dx, dy, ns))
+      return 1;
+    cudaMemcpy(hy.data(), dy, ns * sizeof(double), cudaMemcpyDeviceToHost);
+    if (apply(pr[1], dx, dy, ns))
+      return 1;
+    cudaMemcpy(hz.data(), dy, ns * sizeof(double), cudaMemcpyDeviceToHost);
+    int bad = 0;
+    for (int i = 0; i < ns; ++i)
+    {
+      // inside the fast ranges the fast function may differ by its rounding
+      const double v = sp[i];
+      const bool   fast_range = (pr[0] == OP_RCP)
+                                  ? (std::isfinite(v) && std::fabs(v) >= std::ldexp(1.0, -1022) &&
+                                   std::fabs(v) < std::ldexp(1.0, 1021))
+                                  : (std::isfinite(v) && v >= std::ldexp(1.0, -1022));
+      if (fast_range)
+      {
+        const long double ref = pr[0] == OP_RCP ? 1.0L / (long double)v : sqrtl((long double)v);
+        bad += ulp_error(hy[i], ref) > 0.8;
+      }
+      else
+        bad += !same_bits(hy[i], hz[i]);
+    }
+    std::printf("special_%s mismatches %d of %d\n", names[pr[0]], bad, ns);
+  }
+  cudaFree(dx);
+  cudaFree(dy);
+  return 0;
+}
