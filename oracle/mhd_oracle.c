@@ -32,6 +32,15 @@
 #define NV 8
 enum { ID = 0, IP = 1, IU = 2, IV = 3, IW = 4, IA = 5, IB = 6, IC = 7 };
 
+/* Stage markers of the FP64 operation counter (oracle/flop_count.cpp
+ * compiles this file with a counting scalar type and defines ORC_STAGE);
+ * no-ops in the oracle itself. */
+#ifndef ORC_STAGE
+#  define ORC_STAGE(s) ((void)0)
+#endif
+enum { STG_OTHER = 0, STG_PRIM, STG_DT, STG_SLOPES, STG_HALF, STG_EFIELD, STG_FACEB, STG_FLUX,
+       STG_EMF, STG_UPDATE, STG_COUNT };
+
 /* ====================================================================== */
 /* INI parsing: inih ini.cpp:100-190 + INIReader.cpp:40-117 + ConfigMap.cpp:38-82 */
 /* ====================================================================== */
@@ -1431,14 +1440,19 @@ step3d(orc_solver *s, double *Uin, double *Uout)
   const int         nt = s->nthreads;
   const int64_t     stride[3] = { 1, sj, sk };
 
+  ORC_STAGE(STG_OTHER);
   orc_make_boundaries(p, Uin);
   memcpy(Uout, Uin, (size_t)orc_nelem(p) * sizeof(double));
+  ORC_STAGE(STG_PRIM);
   convert_to_primitives(s, Uin);
+  ORC_STAGE(STG_DT);
   compute_dt(s);
+  ORC_STAGE(STG_OTHER);
   const double dtdx = s->dt / p->dx;
   const double dtdy = s->dt / p->dy;
   const double dtdz = s->dt / p->dz;
 
+  ORC_STAGE(STG_SLOPES);
   /* ComputeSlopesFunctor3D_MHD (MHDRunFunctors3D.h:168-273), [1, size-1) */
 #pragma omp parallel for collapse(2) schedule(static) num_threads(nt)
   for (int k = 1; k < ksize - 1; ++k)
@@ -1458,6 +1472,7 @@ step3d(orc_solver *s, double *Uin, double *Uout)
         Sz[c + IC * sv] = Uin[c + sk + IC * sv] - Uin[c + IC * sv];
       }
 
+  ORC_STAGE(STG_HALF);
   /* ComputeUpdatedPrimVarFunctor3D_MHD (MHDRunFunctors3D.h:865-1022), [g-2, size-g+1) */
 #pragma omp parallel for collapse(2) schedule(static) num_threads(nt)
   for (int k = g - 2; k < ksize - g + 1; ++k)
@@ -1508,6 +1523,7 @@ step3d(orc_solver *s, double *Uin, double *Uout)
         Q2[c + IC * sv] = C + 0.5 * sC0;
       }
 
+  ORC_STAGE(STG_EFIELD);
   /* ComputeElecFieldFunctor3D (MHDRunFunctors3D.h:278-362), [1, size-1) */
 #pragma omp parallel for collapse(2) schedule(static) num_threads(nt)
   for (int k = 1; k < ksize - 1; ++k)
@@ -1539,6 +1555,7 @@ step3d(orc_solver *s, double *Uin, double *Uout)
         E[c + 2 * n1] = u * B - v * A;
       }
 
+  ORC_STAGE(STG_FACEB);
   /* ComputeSourceFaceMagFunctor3D (MHDRunFunctors3D.h:367-436), [1, size-1) */
 #pragma omp parallel for collapse(2) schedule(static) num_threads(nt)
   for (int k = 1; k < ksize - 1; ++k)
@@ -1552,6 +1569,7 @@ step3d(orc_solver *s, double *Uin, double *Uout)
         sF[c + 2 * n1] = (Ey[c + 1] - Ey[c]) * 0.5 * dtdx - (Ex[c + sj] - Ex[c]) * 0.5 * dtdy;
       }
 
+  ORC_STAGE(STG_FLUX);
   /* ComputeFluxAndUpdateAlongDirFunctor3D_MHD<dir> flux part
    * (MHDRunFunctors3D.h:1100-1253), faces [g, size-g] */
   for (int dir = 0; dir < 3; ++dir)
@@ -1613,6 +1631,7 @@ step3d(orc_solver *s, double *Uin, double *Uout)
         }
   }
 
+  ORC_STAGE(STG_EMF);
   /* ReconstructEdgeComputeEmfAndUpdateFunctor3D<dir> (MHDRunFunctors3D.h:1331-1778),
    * edges [g, size-g]; edge direction edir, transverse directions d0 < d1. */
   for (int edir = 0; edir < 3; ++edir)
@@ -1686,6 +1705,7 @@ step3d(orc_solver *s, double *Uin, double *Uout)
         }
   }
 
+  ORC_STAGE(STG_UPDATE);
   /* update: hydro variables by X, then Y, then Z fluxes (atomic updates of
    * MHDRunFunctors3D.h:1255-1313 in serial order) */
 #pragma omp parallel for collapse(2) schedule(static) num_threads(nt)
@@ -1743,6 +1763,7 @@ step3d(orc_solver *s, double *Uin, double *Uout)
           Uout[c + IC * sv] = x;
         }
       }
+  ORC_STAGE(STG_OTHER);
 }
 
 /* SolverBase.cpp:195-220 (finished, next_iteration) and
