@@ -2,11 +2,15 @@
 
 Default workload: 3D Orszag-Tang 256^3 (periodic, HLLD, CFL 0.8, gamma0 5/3
 float-rounded as the reference's ConfigMap does, seeded 1e-3 uniform velocity
-perturbation), FP64 plain path.  A "step" is one full iteration of the solver
-(boundaries, primitives, CFL dt, slopes, half step, HLLD fluxes, CT EMFs,
-update).  Metric: interior cell-updates per second.
+perturbation), FP64 plain path in the FMA-free build (`--fp-mode exact`, the
+default: the reference's operation order, bitwise equal to the reference; the
+FMA-contracted build is `--fp-mode fast` and the line's `variants.fp64_fast`).
+A "step" is one full iteration of the solver (boundaries, primitives, CFL dt,
+slopes, half step, HLLD fluxes, CT EMFs, update).  Metric: interior
+cell-updates per second.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--fp-mode exact|fast]
                   [--workload ot3d_256_fp64|ot3d_256_fp32|ot2d_256_fp64|
                               ensemble512_fp32|kh2d_4096_fp32|ot3d_128_fp64|ot3d_128_fp32]
 
@@ -230,11 +234,13 @@ def emit(obj):
 # ---------------------------------------------------------------- CPU side
 
 def cpu_baseline_run(name: str, steps: int | None, warmup: int, nthreads: int,
-                     target_s: float = 8.0):
+                     target_s: float = 8.0, want_state: bool = False):
     """The oracle port of the reference step (oracle/mhd_oracle.c) on the host
     cores: same workload, full grid.  steps=None sizes the timed sample to
-    about target_s seconds from the duration of the warm-up step.  Returns
-    (cell-updates/s, seconds timed, steps timed)."""
+    about target_s seconds from the duration of the warm-up steps (and caps a
+    given count there).  Returns
+    (cell-updates/s, seconds timed, steps timed), plus the interior state
+    after the warm-up and timed steps when want_state."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py
 
@@ -247,13 +253,16 @@ def cpu_baseline_run(name: str, steps: int | None, warmup: int, nthreads: int,
     t0 = time.perf_counter()
     s.run(max(warmup, 1))
     t_one = (time.perf_counter() - t0) / max(warmup, 1)
-    if steps is None:
-        steps = int(min(5000, max(2, target_s / max(t_one, 1e-6))))
+    cap = int(min(5000, max(2, target_s / max(t_one, 1e-6))))
+    steps = cap if steps is None else min(steps, cap)
     t0 = time.perf_counter()
     s.run(steps)
     el = time.perf_counter() - t0
+    state = oracle_py.interior(s.get_state()) if want_state else None
     s.close()
     cells = n ** dim
+    if want_state:
+        return cells * steps / el, el, steps, state
     return cells * steps / el, el, steps
 
 
@@ -274,6 +283,9 @@ def run_gb300(args):
     ini, transform, data_desc = workload_setup(args.workload, precision)
     p = m.params_from_ini(ini)
     p.device = local
+    # FP64 headline: the FMA-free build, bitwise equal to the reference
+    exact = precision == 64 and args.fp_mode == "exact"
+    p.fp_mode = m.MHD_FP_EXACT if exact else m.MHD_FP_FAST
     s = m.MHDSolver(p)
     s.init_problem()
     U0 = s.get_state()
@@ -313,18 +325,15 @@ def run_gb300(args):
     step_achieved = alg_bytes_per_cell * interior_cells / (step_ms / 1e3) / 1e9
     traffic = load_profile_traffic(args.workload, dom)
 
-    # FP32 companion figure for the same workload (device-resident)
+    # Companion figures for the same workload (device-resident): the other
+    # FP64 build, FP32 and FP32 + flux surrogate, each with its relative L1
+    # per variable against the exact FP64 state after the same steps
     variants = {}
     accuracy = None
     if args.workload == "ot3d_256_fp64" and not args.no_variants:
-        # FP32 and FP32 + flux surrogate on the same initial state: throughput,
-        # and relative L1 (max over variables) against the FP64 solution after
-        # the same number of steps
         from ppkmhd_gb300 import surrogate
 
         acc_steps = 20
-        # the FMA-free FP64 build in the reference's operation order (bitwise
-        # equal to the reference): the accuracy reference, and timed as well
         px = m.params_from_ini(ini)
         px.device = local
         px.fp_mode = m.MHD_FP_EXACT
@@ -332,28 +341,32 @@ def run_gb300(args):
         sx.set_state(U0)
         sx.run(acc_steps)
         ref = m.interior(sx.get_state())
-        sx.set_state(U0)
-        sx.run_timed(3)
-        msx = sx.run_timed(args.steps)
         sx.close()
         den = np.abs(ref).sum(axis=(1, 2, 3))
         den = np.where(den > 1e-12 * den[0], den, den[0])
-        p64 = m.params_from_ini(ini)
-        p64.device = local
-        s64 = m.MHDSolver(p64)
-        s64.set_state(U0)
-        s64.run(acc_steps)
-        err64 = np.abs(m.interior(s64.get_state()) - ref).sum(axis=(1, 2, 3)) / den
-        s64.close()
-        accuracy = {"steps": acc_steps, "reference": "FP64 exact build (bitwise the reference)",
-                    "rel_l1_per_variable": [float(x) for x in err64],
-                    "note": "FMA contraction; z momentum and z field are the 1e-3 seed and "
-                            "differ at the level two valid FP64 builds differ (the CPU oracle "
-                            "with and without contraction: 5e-12 after 100 steps at 48^3)"}
-        variants["fp64_exact"] = {"value": interior_cells * args.steps / (msx / 1e3),
-                                  "ms_per_step": msx / args.steps, "dtype": "f64",
-                                  "note": "FMA-free build in the reference's operation order: "
-                                          "bitwise equal to the reference"}
+        other = "fp64_fast" if exact else "fp64_exact"
+        po = m.params_from_ini(ini)
+        po.device = local
+        po.fp_mode = m.MHD_FP_FAST if exact else m.MHD_FP_EXACT
+        so = m.MHDSolver(po)
+        so.set_state(U0)
+        so.run(acc_steps)
+        err_o = np.abs(m.interior(so.get_state()) - ref).sum(axis=(1, 2, 3)) / den
+        so.set_state(U0)
+        so.run_timed(3)
+        mso = so.run_timed(args.steps)
+        so.close()
+        variants[other] = {"value": interior_cells * args.steps / (mso / 1e3),
+                           "ms_per_step": mso / args.steps, "dtype": "f64",
+                           "rel_l1_vs_exact_per_variable": [float(x) for x in err_o],
+                           "accuracy_steps": acc_steps,
+                           "note": ("FMA-contracted build with shared reciprocals: within 1e-12 "
+                                    "of the reference on the order-one variables; the seeded z "
+                                    "momentum and z field differ at the FP64 round-off floor of "
+                                    "the reference's own update, which a 1-ulp change of dt alone "
+                                    "reproduces (tests/test_oracle_pinning.py)")
+                           if exact else "FMA-free build in the reference's operation order: "
+                                         "bitwise equal to the reference"}
         for tag, use_mlp in (("fp32", False), ("fp32_surrogate", True)):
             p32 = m.params_from_ini(ot_ini(dim, n, 32))
             p32.device = local
@@ -371,7 +384,7 @@ def run_gb300(args):
                  "rel_l1_vs_fp64": float((err / den).max()),
                  "rel_l1_vs_fp64_per_variable": [float(x) for x in err / den],
                  "accuracy_steps": acc_steps,
-                 "note": "FP32 storage and arithmetic, FP64 dt/sums/div B"}
+                 "note": "FP32 arithmetic, compensated FP32 state (float pair), FP64 dt/sums/div B"}
             if use_mlp:
                 used, total = s32.surrogate_stats()
                 v["faces_by_network"] = used / max(total, 1)
@@ -383,12 +396,30 @@ def run_gb300(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
-        v, el, ns = cpu_baseline_run(args.workload, steps=args.cpu_steps, warmup=1,
-                                     nthreads=nthreads)
+        v, el, ns, cpu_state = cpu_baseline_run(args.workload, steps=args.cpu_steps, warmup=1,
+                                                nthreads=nthreads, want_state=True)
         cpu = {"value": v, "unit": "cell-updates/s", "cores": nthreads, "kind": "port",
                "sample": f"{ns} steps of the same {n}^{dim} grid after 1 warm-up "
                          f"step, oracle/mhd_oracle.c with {nthreads} OpenMP threads "
                          f"({el:.1f} s timed)"}
+        if precision == 64:
+            # the headline build against the CPU run of the same steps
+            pc = m.params_from_ini(ini)
+            pc.device = local
+            pc.fp_mode = p.fp_mode
+            sc = m.MHDSolver(pc)
+            sc.set_state(U0)
+            sc.run(ns + 1)
+            mine = m.interior(sc.get_state())
+            sc.close()
+            dn = np.abs(cpu_state).sum(axis=tuple(range(1, dim + 1)))
+            dn = np.where(dn > 1e-12 * dn[0], dn, dn[0])
+            accuracy = {"steps": ns + 1, "reference": "oracle/mhd_oracle.c (bitwise the "
+                        "reference compiled without FMA contraction), same initial state",
+                        "bitwise_equal": bool(np.array_equal(mine, cpu_state)),
+                        "rel_l1_per_variable": [float(x) for x in
+                                                np.abs(mine - cpu_state).sum(
+                                                    axis=tuple(range(1, dim + 1))) / dn]}
 
     # ---- end to end through the host-buffer ABI call (H2D + step + D2H per
     # step), measured last: right after a process that freed much device
@@ -428,6 +459,8 @@ def run_gb300(args):
             "scaling": "weak",
             "vs_baseline": None,
             "dtype": "f64" if precision == 64 else "f32",
+            "fp_mode": ("exact (FMA-free, the reference's operation order)" if exact
+                        else "fast (FMA contraction)") if precision == 64 else "fp32",
             "data": data_desc,
             "config": {"workload": label, "grid": [n] * dim, "cells": interior_cells,
                        "cells_with_ghosts": ghost_cells, "state_bytes": state_bytes,
@@ -449,10 +482,8 @@ def run_gb300(args):
                          "algorithmic_bytes_per_cell": alg_bytes_per_cell,
                          "step_achieved": step_achieved,
                          "step_frac": step_achieved / hbm_peak},
-            "alu_roofline": (lambda a: None if a is None or precision != 64 else {
-                "bound": "fp64 pipe (2 DFMA/SM/cycle, 1.26 TFLOP/s at 2070 MHz)",
-                "kernel": dom, "pipe_active_frac": a.get("pipe_active", {}).get(dom),
-                "source": a.get("source")})(load_alu_profile(args.workload.replace("256", "128"))),
+            "alu_roofline": fp64_roofline(args.workload, value, dom, exact)
+            if precision == 64 and dim == 3 else None,
             "clocks": clk.summary(),
             "gpu_launches": s.launches_per_step() * args.steps,
             "cpu_baseline": cpu,
@@ -766,6 +797,37 @@ def run_turbulence(args):
         })
 
 
+def fp64_roofline(workload: str, value: float, kernel: str, exact: bool):
+    """FP64-arithmetic roofline of a 3D FP64 line: the reference algorithm's
+    FP64 operations per cell-update (additions, multiplications, divisions
+    and square roots, each one flop; counted by the oracle compiled with a
+    counting scalar, profiles/fp64_ops_ot3d_256.json) times the cell-update
+    rate, against 1.26 TFLOP/s (2 DFMA per SM per cycle, 152 SMs, 2.07 GHz;
+    an FMA-free build issues at most half of that as separate operations).
+    Beside it the FP64-pipe utilisation ncu measured on the kernels."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "fp64_ops_ot3d_256.json")) as f:
+            ops = json.load(f)
+    except (OSError, ValueError):
+        return None
+    per = ops["per_cell_update"]["minimal"]
+    peak = float(ops["fp64_peak_tflops"])
+    achieved = per["flop"] * value / 1e12
+    out = {"bound": "fp64 pipe (2 DFMA/SM/cycle, 1.26 TFLOP/s at 2070 MHz)",
+           "flop_per_cell_update": round(per["flop"], 1),
+           "div_per_cell_update": round(per["div"], 1),
+           "sqrt_per_cell_update": round(per["sqrt"], 1),
+           "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+           "source": "oracle/flop_count.py (the reference's operations, minimal halo)"}
+    if exact:
+        out["fma_free_ceiling_frac"] = 0.5
+    a = load_alu_profile(workload.replace("256", "128"))
+    if a is not None and not exact:
+        out["pipe_active_frac"] = a.get("pipe_active", {}).get(kernel)
+        out["pipe_source"] = a.get("source")
+    return out
+
+
 def load_alu_profile(workload: str):
     """FP64-pipe utilisation of the kernels from the committed ncu summary
     (profiles/fp64_pipe_<workload>.json), or None."""
@@ -816,8 +878,12 @@ def run_reference(args):
               "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
                       "d2h_bytes_per_step": 0}})
         return
-    v, el, steps = cpu_baseline_run(args.workload, steps=steps, warmup=1, nthreads=nthreads,
-                                    target_s=20.0)
+    if steps is None:
+        # the GPU arm's K steps after W warm-up steps, unless that exceeds a
+        # few minutes of host work (then ~150 s worth, stated in "steps")
+        steps = args.steps
+    v, el, steps = cpu_baseline_run(args.workload, steps=steps, warmup=args.warmup,
+                                    nthreads=nthreads, target_s=150.0)
     emit({
         "impl": "reference",
         "metric": "MHD cell-updates/s (interior cells), plain MUSCL-Hancock+HLLD+CT step",
@@ -825,7 +891,7 @@ def run_reference(args):
         "unit": "cell-updates/s",
         "n_gpus": world,
         "steps": steps,
-        "warmup": 1,
+        "warmup": args.warmup,
         "ms_per_step": el * 1e3 / steps,
         "higher_is_better": True,
         "scaling": "weak",
@@ -836,8 +902,8 @@ def run_reference(args):
                    "implementation": "CPU port of the reference step (oracle/mhd_oracle.c, "
                                      "bitwise equal to the reference functors), OpenMP"},
         "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": nthreads, "kind": "port",
-                         "sample": f"{steps} steps of the full {n}^{dim} grid after 1 warm-up "
-                                   f"step ({el:.1f} s timed)"},
+                         "sample": f"{steps} steps of the full {n}^{dim} grid after "
+                                   f"{args.warmup} warm-up steps ({el:.1f} s timed)"},
         "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     })
@@ -859,6 +925,8 @@ def main():
     ap.add_argument("--acc-steps", type=int, default=40,
                     help="steps of the accuracy comparison of the turbulence workload")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--fp-mode", default="exact", choices=["exact", "fast"],
+                    help="FP64 build of the headline line (exact: bitwise the reference)")
     args = ap.parse_args()
     if args.cpu_steps is None and args.workload.startswith("ensemble"):
         args.cpu_steps = 150

@@ -125,7 +125,17 @@ int mhd_params_from_ini(const char *ini_text, mhd_params *p, char *err, size_t e
 /* Allocate device buffers for one problem and set up the stream.
  * Replaces the allocations of SolverMHDMuscl<dim>::SolverMHDMuscl
  * (SolverMHDMuscl.h:211-387).  The state is zero until mhd_init_problem or
- * mhd_set_state. */
+ * mhd_set_state.
+ * MHD_FP32 with implementation version 2 keeps the device state compensated:
+ * next to the float state the context holds its low parts (8 more float
+ * planes, to about 48 significant bits together), each iteration adds its
+ * FP32 increment to the pair without rounding loss, and the momentum fluxes
+ * are computed and stored relative to one constant total pressure per
+ * iteration.  The arithmetic stays FP32; what no longer accumulates is the
+ * rounding of the state itself.  mhd_get_state returns the float state (the
+ * pair rounded once); a state set from the host (mhd_set_state,
+ * mhd_step_host) starts with zero low parts; checkpoints carry them
+ * (format 2). */
 int mhd_create(const mhd_params *p, mhd_ctx **ctx);
 int mhd_destroy(mhd_ctx *ctx);
 
@@ -280,11 +290,13 @@ const char *mhd_ensemble_last_error(mhd_ensemble *ens);
  * SolverMHDMuscl<dim>::init_restart, SolverMHDMuscl.h:613-643), which drops
  * the magnetic field (the HDF5 writers pass 4 or 5 variables,
  * IO_ReadWrite.cpp:102-106, :150-154).  Here a checkpoint is one binary file:
- *   char magic[8] = "PPKMHDCK"; uint32 format = 1, dim, nx, ny, nz, ghost,
- *   nbvar = 8, real_bytes; double t, dt; int64 iteration; int32 times_saved,
- *   pad; double xmin, xmax, ymin, ymax, zmin, zmax, gamma0;
+ *   char magic[8] = "PPKMHDCK"; uint32 format = 1 or 2, dim, nx, ny, nz,
+ *   ghost, nbvar = 8, real_bytes; double t, dt; int64 iteration; int32
+ *   times_saved, pad; double xmin, xmax, ymin, ymax, zmin, zmax, gamma0;
  * followed by the ghost-inclusive state, LayoutLeft, in the context's
- * precision (all fields little-endian).  Loading restores the state and t
+ * precision (all fields little-endian); format 2 (FP32, implementation
+ * version 2) then holds the same number of floats again: the low parts of
+ * the compensated FP32 state (see mhd_create).  Loading restores the state and t
  * (0 with reset_time, as restart_reset_totaltime); the iteration count
  * restarts at 0 as in the reference.  Continuing from a checkpoint is
  * bitwise equal to the uninterrupted run.

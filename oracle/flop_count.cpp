@@ -176,6 +176,11 @@ fmin(CD a, CD b)
   return CD(std::fmin(a.v, b.v));
 }
 static inline CD
+nextafter(CD a, double b)
+{
+  return CD(std::nextafter(a.v, b));
+}
+static inline CD
 sin(CD a)
 {
   return CD(std::sin(a.v));

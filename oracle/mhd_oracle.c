@@ -993,6 +993,7 @@ struct orc_solver
   double    *U, *U2, *Q, *Q2, *Sx, *Sy, *Sz, *E, *sF, *Fx, *Fy, *Fz, *Em;
   double     t, dt;
   int        it;
+  int        dt_ulps; /* test hook: dt moved by this many ulps (orc_set_dt_ulps) */
 };
 
 static double *
@@ -1118,8 +1119,19 @@ compute_dt(orc_solver *s)
         invDt = fmax(invDt, val);
       }
   s->dt = p->cfl / invDt;
+  for (int u = 0; u < s->dt_ulps; ++u)
+    s->dt = nextafter(s->dt, INFINITY);
   if (s->t + s->dt > p->tEnd)
     s->dt = p->tEnd - s->t;
+}
+
+/* Test hook: every later dt of the solver is moved up by `ulps` units in the
+ * last place (0 restores the reference's dt).  Used to measure how far one
+ * rounding difference carries (tests/test_oracle_pinning.py). */
+void
+orc_set_dt_ulps(orc_solver *s, int ulps)
+{
+  s->dt_ulps = ulps;
 }
 
 void

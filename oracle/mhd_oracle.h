@@ -68,6 +68,8 @@ void orc_get_state(const orc_solver *s, double *U);
 /* Run up to n iterations of the main loop; returns the number executed. */
 int  orc_run(orc_solver *s, int n);
 void orc_time(const orc_solver *s, double *t, double *dt, int *iteration);
+/* Test hook: move every later dt up by `ulps` ulps (0: the reference's dt). */
+void orc_set_dt_ulps(orc_solver *s, int ulps);
 int64_t orc_nelem(const orc_params *p);
 
 /* Function-level probes (normal-frame 8-component states). */

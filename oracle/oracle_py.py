@@ -73,6 +73,7 @@ def lib():
         L.orc_run.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.orc_run.restype = ctypes.c_int
         L.orc_time.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.POINTER(ctypes.c_int)]
+        L.orc_set_dt_ulps.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.orc_nelem.argtypes = [ctypes.POINTER(OrcParams)]
         L.orc_nelem.restype = ctypes.c_int64
         L.orc_init_orszag_tang.argtypes = [ctypes.POINTER(OrcParams), _dp]
@@ -140,6 +141,10 @@ class OracleSolver:
 
     def run(self, n: int) -> int:
         return lib().orc_run(self.h, int(n))
+
+    def set_dt_ulps(self, ulps: int):
+        """Test hook: move every later dt up by `ulps` ulps."""
+        lib().orc_set_dt_ulps(self.h, int(ulps))
 
     def time(self):
         t, dt, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()

@@ -436,6 +436,11 @@ extern "C"
     std::vector<unsigned char> U(n * rb);
     if (int rc = ctx->core->get_state(U.data(), MHD_LAYOUT_LEFT))
       return from_core(ctx, rc);
+    // format 2: format 1 followed by the FP32 low parts of the state
+    std::vector<unsigned char> lo((size_t)ctx->core->low_part_bytes());
+    if (!lo.empty())
+      if (int rc = ctx->core->get_low_parts(lo.data()))
+        return from_core(ctx, rc);
     double t = 0, dt = 0;
     int    it = 0;
     if (int rc = ctx->core->time(&t, &dt, &it))
@@ -443,7 +448,7 @@ extern "C"
     const mhd_params & p = ctx->params;
     CheckpointHeader   h{};
     std::memcpy(h.magic, "PPKMHDCK", 8);
-    h.format = 1;
+    h.format = lo.empty() ? 1 : 2;
     h.dim = (uint32_t)p.dim;
     h.nx = (uint32_t)p.nx;
     h.ny = (uint32_t)p.ny;
@@ -460,7 +465,9 @@ extern "C"
     FILE * f = std::fopen(path, "wb");
     if (!f)
       return fail(ctx, MHD_ERR_INVALID_ARG, std::string("cannot open ") + path + " for writing");
-    const bool ok = std::fwrite(&h, sizeof h, 1, f) == 1 && std::fwrite(U.data(), 1, U.size(), f) == U.size();
+    const bool ok = std::fwrite(&h, sizeof h, 1, f) == 1 &&
+                    std::fwrite(U.data(), 1, U.size(), f) == U.size() &&
+                    std::fwrite(lo.data(), 1, lo.size(), f) == lo.size();
     const bool closed = std::fclose(f) == 0;
     if (!ok || !closed)
       return fail(ctx, MHD_ERR_INVALID_ARG, std::string("short write to ") + path);
@@ -480,14 +487,14 @@ extern "C"
     const bool       got = std::fread(&h, sizeof h, 1, f) == 1;
     const mhd_params & p = ctx->params;
     std::string      bad;
-    if (!got || std::memcmp(h.magic, "PPKMHDCK", 8) != 0 || h.format != 1)
-      bad = "not a checkpoint file (format 1)";
+    if (!got || std::memcmp(h.magic, "PPKMHDCK", 8) != 0 || (h.format != 1 && h.format != 2))
+      bad = "not a checkpoint file (format 1 or 2)";
     else if ((int)h.dim != p.dim || (int)h.nx != p.nx || (int)h.ny != p.ny ||
              (p.dim == 3 && (int)h.nz != p.nz) || (int)h.ghost != p.ghost || h.nbvar != 8)
       bad = "checkpoint grid does not match the context";
     else if ((int)h.real_bytes != ctx->core->real_bytes())
       bad = "checkpoint precision does not match the context";
-    std::vector<unsigned char> U;
+    std::vector<unsigned char> U, lo;
     if (bad.empty())
     {
       int sz[4];
@@ -495,13 +502,23 @@ extern "C"
       U.resize((size_t)sz[0] * sz[1] * sz[2] * sz[3] * h.real_bytes);
       if (std::fread(U.data(), 1, U.size(), f) != U.size())
         bad = "checkpoint file is truncated";
+      if (bad.empty() && h.format == 2)
+      {
+        lo.resize((size_t)ctx->core->low_part_bytes());
+        if (lo.empty())
+          bad = "checkpoint has low parts the context does not keep";
+        else if (std::fread(lo.data(), 1, lo.size(), f) != lo.size())
+          bad = "checkpoint file is truncated";
+      }
     }
     std::fclose(f);
     if (!bad.empty())
       return fail(ctx, MHD_ERR_INVALID_ARG, bad);
     ctx->core->set_time_origin(reset_time ? 0.0 : h.t);
-    const int rc = ctx->core->set_state(U.data(), MHD_LAYOUT_LEFT);
+    int rc = ctx->core->set_state(U.data(), MHD_LAYOUT_LEFT);
     ctx->core->set_time_origin(p.tCurrent);
+    if (rc == MHD_OK && !lo.empty())
+      rc = ctx->core->set_low_parts(lo.data());
     if (rc)
       return from_core(ctx, rc);
     if (times_saved)

@@ -41,6 +41,11 @@ public:
   virtual int harvest(int stride, float * host, int64_t capacity, int64_t * count) = 0;
   //! time that set_state / init_problem start from (tCurrent)
   virtual void set_time_origin(double t) = 0;
+  //! FP32 version-2 contexts keep the low parts of the state (Buffers::Ulo):
+  //! their size in bytes (0: none), and host copies for checkpoints
+  virtual int64_t low_part_bytes() = 0;
+  virtual int     get_low_parts(void * host) = 0;
+  virtual int     set_low_parts(const void * host) = 0;
   std::string err;
 };
 

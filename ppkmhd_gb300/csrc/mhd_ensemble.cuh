@@ -298,8 +298,10 @@ public:
     MHD_ECK(cudaSetDevice(params[0].device));
     MHD_ECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     // one arena: per problem U, U2, Q, Q2, S (dim x 8), E, F (dim x nf), Em, H
+    // and, in FP32, the low parts of the state (Buffers::Ulo, 8 planes)
     const int          ne = dim == 3 ? 3 : 1, nf = dim == 3 ? 5 : 6, nh = face_data_planes(dim);
-    const int          planes = 8 * 4 + 8 * dim + ne + nf * dim + ne + nh;
+    const int          nlo = sizeof(R) == 4 ? 8 : 0;
+    const int          planes = 8 * 4 + 8 * dim + ne + nf * dim + ne + nh + nlo;
     std::vector<size_t> off(n);
     size_t              total = 0;
     G.resize(n);
@@ -336,6 +338,8 @@ public:
       B[p].Em = a;
       a += ne * c;
       B[p].H = a;
+      a += nh * c;
+      B[p].Ulo = nlo ? a : nullptr;
       B[p].st = st + p;
     }
     MHD_ECK(cudaMalloc(&dG, n * sizeof(Grid<R>)));
@@ -485,6 +489,9 @@ public:
   apply_init(int p)
   {
     const Grid<R> & g = G[p];
+    // a state from the host has zero low parts
+    if (B[p].Ulo)
+      MHD_ECK(cudaMemsetAsync(B[p].Ulo, 0, (size_t)g.sv * NV * sizeof(R), stream));
     const int64_t   nall = g.box[BOX_ALL].count(), nprim = g.box[BOX_PRIM].count();
     if (dim == 2)
     {

@@ -47,8 +47,28 @@ struct DevState
   int                status; // bit 0: non-finite or non-positive state seen
   int                pad;
   float              fdtdx, fdtdy, fdtdz; // dt/dx... rounded once for the FP32 kernels
-  float              fpad;
+  // FP32 kernels: the momentum fluxes of this iteration are stored minus the
+  // constant fp0 = (max + min) / 2 of the interior cells' total pressure
+  // p + B^2/2 (bit patterns of positive floats order like the values)
+  float              fp0;
+  unsigned           ptmax_bits, ptmin_bits;
 };
+
+// The total-pressure shift of the momentum fluxes: the flux divergence only
+// sees differences of fluxes of one direction, so subtracting one constant
+// from all of them leaves the update unchanged, while the FP32 rounding of
+// the Riemann solver's total pressure and of the stored flux applies to
+// |p_tot - fp0| instead of p_tot.  FP64 kernels take no shift.
+__device__ __forceinline__ double
+flux_shift(const DevState *, double)
+{
+  return 0.0;
+}
+__device__ __forceinline__ float
+flux_shift(const DevState * st, float)
+{
+  return st->fp0;
+}
 
 // dt/dx, dt/dy, dt/dz in the working precision
 __device__ __forceinline__ void
@@ -84,6 +104,9 @@ struct Buffers
   R *       F;   // face fluxes, DIM blocks of NF planes
   R *       Em;  // edge EMFs (1 plane in 2D, 3 in 3D)
   R *       H;   // face data, FaceData<DIM>::NPLANES planes (below)
+  // FP32 contexts: the low parts of the state (8 planes; U = U_in + Ulo to
+  // about 48 bits), updated in place by k_update; nullptr: plain FP32 state
+  R *       Ulo;
   DevState *st;
 };
 
@@ -272,7 +295,11 @@ boundaries_body(const Grid<R> & G, R * __restrict__ U, DevState * st, int force,
   if (!force && step_finished(st))
     return;
   if (first)
+  {
     st->invdt_bits = 0ull; // reset the CFL reduction of this iteration
+    st->ptmax_bits = 0u;
+    st->ptmin_bits = 0x7f800000u; // +inf
+  }
   const Box & b = G.box[BOX_ALL];
   int       i, j, k;
   if (!box_cell(b, idx, i, j, k))
@@ -356,6 +383,7 @@ prim_dt_body(const Grid<R> & G, const R * __restrict__ U, R * __restrict__ Q, De
   const Box & b = G.box[BOX_PRIM];
   int       i, j, k;
   R         rate = R(0);
+  R         ptot = R(-1); // FP32: interior total pressure, -1 elsewhere
   bool      bad = false;
   if (idx < end && box_cell(b, idx, i, j, k))
   {
@@ -436,6 +464,8 @@ prim_dt_body(const Grid<R> & G, const R * __restrict__ U, R * __restrict__ Q, De
       // (it arises legitimately when round-off makes the inner root of the
       // fast speed slightly negative, e.g. for a field along one axis)
       rate = (val >= R(0)) ? val : R(0);
+      if constexpr (sizeof(R) == 4)
+        ptot = p + emag;
       const R Ein = U[c + IP * sv];
       bad = !(U[c + ID * sv] > R(0)) || !isfinite(Ein);
     }
@@ -455,6 +485,32 @@ prim_dt_body(const Grid<R> & G, const R * __restrict__ U, R * __restrict__ Q, De
     rate = warp_max(rate);
     if (lane == 0 && rate > R(0))
       atomicMax(&st->invdt_bits, (unsigned long long)__double_as_longlong((double)rate));
+  }
+  if constexpr (sizeof(R) == 4)
+  {
+    // range of the positive, finite total pressures (max and min are
+    // order-independent, so the shift is deterministic): warp, then block
+    // reductions on the bit patterns, one atomic of each kind per block
+    __shared__ unsigned rhi[32], rlo[32];
+    const bool ok = ptot > 0.f && ptot < INFINITY;
+    unsigned   hi = __reduce_max_sync(0xffffffffu, ok ? __float_as_uint(ptot) : 0u);
+    unsigned   lo = __reduce_min_sync(0xffffffffu, ok ? __float_as_uint(ptot) : 0x7f800000u);
+    if (lane == 0)
+    {
+      rhi[wid] = hi;
+      rlo[wid] = lo;
+    }
+    __syncthreads();
+    if (wid == 0)
+    {
+      const bool in = lane < (int)(blockDim.x >> 5);
+      hi = __reduce_max_sync(0xffffffffu, in ? rhi[lane] : 0u);
+      lo = __reduce_min_sync(0xffffffffu, in ? rlo[lane] : 0x7f800000u);
+      if (lane == 0 && hi != 0u)
+        atomicMax(&st->ptmax_bits, hi);
+      if (lane == 0 && lo != 0x7f800000u)
+        atomicMin(&st->ptmin_bits, lo);
+    }
   }
 }
 
@@ -499,6 +555,10 @@ finalize_dt_body(const Grid<R> & G, DevState * st, int force)
   st->fdtdx = (float)st->dtdx;
   st->fdtdy = (float)st->dtdy;
   st->fdtdz = (float)st->dtdz;
+  if constexpr (sizeof(R) == 4)
+    st->fp0 = st->ptmax_bits >= st->ptmin_bits && st->ptmin_bits < 0x7f800000u
+                ? 0.5f * (__uint_as_float(st->ptmax_bits) + __uint_as_float(st->ptmin_bits))
+                : 0.f;
   if (!(invDt > 0.0) || !isfinite(dt))
     st->status |= STATUS_NUMERIC;
 }
@@ -957,7 +1017,7 @@ flux_face(const Grid<R> & G, const Buffers<R> & B, int i, int j, int k)
 #pragma unroll
   for (int v = 0; v < NV; ++v)
     fl[v] = R(0);
-  riemann(G.riemann, qL, qR, fl, G.gamma0, G.entho);
+  riemann(G.riemann, qL, qR, fl, G.gamma0, G.entho, flux_shift(B.st, R(0)));
   store_face_flux<R, DIM, d>(G, B, c, fl);
 }
 
@@ -1186,6 +1246,77 @@ k_emf(const Grid<R> G, Buffers<R> B, int64_t base, int64_t end)
 //   3D  Bx: + Ey(k) dt/dz - Ey(k+1) dt/dz - Ez(j) dt/dy + Ez(j+1) dt/dy
 //       By: - Ex(k) dt/dz + Ex(k+1) dt/dz + Ez(i) dt/dx - Ez(i+1) dt/dx
 //       Bz: + Ex(j) dt/dy - Ex(j+1) dt/dy - Ey(i) dt/dx + Ey(i+1) dt/dx
+//
+// FP32 takes another operation order, with the same values in exact
+// arithmetic: the flux (EMF) differences of each direction are summed into
+// one increment d before it meets the state, so the rounding of the update
+// is relative to d rather than to the O(1) fluxes; and the state is kept as
+// a float pair (U_in, Ulo) whose sum carries about 48 bits: the increment
+// is added with an error-free two-sum and the pair renormalised, so the
+// state's own rounding no longer accumulates over the iterations.  Without
+// an Ulo array (the no-allocation path) U_out = U_in + d.
+__device__ __forceinline__ void
+add_compensated(float * hi_out, float * lo, int64_t c, float h, float d)
+{
+  if (!lo)
+  {
+    hi_out[c] = __fadd_rn(h, d);
+    return;
+  }
+  // two-sum h + d = s + e exactly (Knuth), then the low parts
+  const float s = __fadd_rn(h, d);
+  const float bb = __fsub_rn(s, h);
+  const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(d, bb));
+  const float t = __fadd_rn(e, lo[c]);
+  // fast two-sum renormalisation (|s| >= |t|)
+  const float hn = __fadd_rn(s, t);
+  hi_out[c] = hn;
+  lo[c] = __fsub_rn(t, __fsub_rn(hn, s));
+}
+
+template <int DIM>
+__device__ __forceinline__ void
+update_fp32(const Grid<float> & G, const Buffers<float> & B, int64_t c)
+{
+  const int64_t sv = G.sv, sj = G.sj, sk = G.sk;
+  float         dtd[3];
+  dt_over_dx(B.st, dtd[0], dtd[1], dtd[2]);
+  const int64_t off[3] = { 1, sj, sk };
+  constexpr int NF = FluxComps<DIM>::NF;
+#pragma unroll
+  for (int q = 0; q < NF; ++q)
+  {
+    const int v = FluxComps<DIM>::var(q);
+    float     d = 0.f;
+#pragma unroll
+    for (int dd = 0; dd < DIM; ++dd)
+    {
+      const float * F = B.F + ((int64_t)dd * NF + q) * sv;
+      d = d + (F[c] - F[c + off[dd]]) * dtd[dd];
+    }
+    add_compensated(B.Uout + v * sv, B.Ulo ? B.Ulo + v * sv : nullptr, c, B.Uin[c + v * sv], d);
+  }
+  const float * Em = B.Em;
+  float *       lo = B.Ulo;
+  if constexpr (DIM == 2)
+  {
+    const float da = (Em[c + sj] - Em[c]) * dtd[1];
+    const float db = (Em[c] - Em[c + 1]) * dtd[0];
+    add_compensated(B.Uout + IA * sv, lo ? lo + IA * sv : nullptr, c, B.Uin[c + IA * sv], da);
+    add_compensated(B.Uout + IB * sv, lo ? lo + IB * sv : nullptr, c, B.Uin[c + IB * sv], db);
+  }
+  else
+  {
+    const float *eX = Em, *eY = Em + sv, *eZ = Em + 2 * sv;
+    const float  da = (eY[c] - eY[c + sk]) * dtd[2] + (eZ[c + sj] - eZ[c]) * dtd[1];
+    const float  db = (eX[c + sk] - eX[c]) * dtd[2] + (eZ[c] - eZ[c + 1]) * dtd[0];
+    const float  dc = (eX[c] - eX[c + sj]) * dtd[1] + (eY[c + 1] - eY[c]) * dtd[0];
+    add_compensated(B.Uout + IA * sv, lo ? lo + IA * sv : nullptr, c, B.Uin[c + IA * sv], da);
+    add_compensated(B.Uout + IB * sv, lo ? lo + IB * sv : nullptr, c, B.Uin[c + IB * sv], db);
+    add_compensated(B.Uout + IC * sv, lo ? lo + IC * sv : nullptr, c, B.Uin[c + IC * sv], dc);
+  }
+}
+
 template <class R, int DIM>
 __device__ __forceinline__ void
 update_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
@@ -1198,6 +1329,11 @@ update_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
     return;
   const int64_t sv = G.sv, sj = G.sj, sk = G.sk;
   const int64_t c = cell_at(G, i, j, k);
+  if constexpr (sizeof(R) == 4)
+  {
+    update_fp32<DIM>(G, B, c);
+    return;
+  }
   R             dtd[3];
   dt_over_dx(B.st, dtd[0], dtd[1], dtd[2]);
   const int64_t off[3] = { 1, sj, sk };

@@ -296,6 +296,33 @@ fast_speed_x(const State<R> & q, R gamma0)
   return sqrt(d2 + sqrt(d2 * d2 - c2 * a * a / d));
 }
 
+// Squared fast speeds in the same operation order (everything under the
+// outer square root of fast_speed_x / fast_speed_y).  The IEEE square root
+// is correctly rounded and non-decreasing, so the maximum of the square roots
+// of several such values is the square root of their maximum, bit for bit
+// (a NaN, from a slightly negative inner argument, is skipped or kept by the
+// same comparisons before and after the root).
+template <class R>
+__device__ __forceinline__ R
+fast_speed2_x(const State<R> & q, R gamma0)
+{
+  const R d = q[ID], p = q[IP], a = q[IA], b = q[IB], c = q[IC];
+  const R b2 = a * a + b * b + c * c;
+  const R c2 = gamma0 * p / d;
+  const R d2 = R(0.5) * (b2 / d + c2);
+  return d2 + sqrt(d2 * d2 - c2 * a * a / d);
+}
+template <class R>
+__device__ __forceinline__ R
+fast_speed2_y(const State<R> & q, R gamma0)
+{
+  const R d = q[ID], p = q[IP], a = q[IA], b = q[IB], c = q[IC];
+  const R b2 = a * a + b * b + c * c;
+  const R c2 = gamma0 * p / d;
+  const R d2 = R(0.5) * (b2 / d + c2);
+  return d2 + sqrt(d2 * d2 - c2 * b * b / d);
+}
+
 // Same with the normal field in slot IB (find_speed_fast<IY>).
 template <class R>
 __device__ __forceinline__ R
@@ -443,11 +470,11 @@ riemann_hll(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
   State<R> ul, fl, ur, fr;
   mhd_flux_and_cons(ql, ul, fl, gamma0);
   mhd_flux_and_cons(qr, ur, fr, gamma0);
-  const R cfl = fast_speed_x(ql, gamma0);
-  const R cfr = fast_speed_x(qr, gamma0);
+  // fmax(cfl, cfr) as the root of the larger square (fast_speed2_x)
+  const R cfm = sqrt(fmax(fast_speed2_x(ql, gamma0), fast_speed2_x(qr, gamma0)));
   const R vl = ql[IU], vr = qr[IU];
-  const R sl = fmin(fmin(vl, vr) - fmax(cfl, cfr), R(0));
-  const R sr = fmax(fmax(vl, vr) + fmax(cfl, cfr), R(0));
+  const R sl = fmin(fmin(vl, vr) - cfm, R(0));
+  const R sr = fmax(fmax(vl, vr) + cfm, R(0));
 #pragma unroll
   for (int v = 0; v < NV; ++v)
     flux[v] = (sr * fl[v] - sl * fr[v] + sr * sl * (ur[v] - ul[v])) / (sr - sl);
@@ -505,11 +532,11 @@ riemann_hlld(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
   const R ptotr = pr + emagr;
   const R vdotbr = ur * a + vr * br + wr * cr;
 
-  const R cfastl = fast_speed_x(ql, gamma0);
-  const R cfastr = fast_speed_x(qr, gamma0);
+  // fmax(cfastl, cfastr) as the root of the larger square (fast_speed2_x)
+  const R cfm = sqrt(fmax(fast_speed2_x(ql, gamma0), fast_speed2_x(qr, gamma0)));
 
-  const R sl = fmin(ul, ur) - fmax(cfastl, cfastr);
-  const R sr = fmax(ul, ur) + fmax(cfastl, cfastr);
+  const R sl = fmin(ul, ur) - cfm;
+  const R sr = fmax(ul, ur) + cfm;
 
   const R rcl = rl * (ul - sl);
   const R rcr = rr * (sr - ur);
@@ -641,8 +668,12 @@ riemann_hlld(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
 // square roots and 2 rsqrt instead of ~28 divides and 6 square roots.
 template <class R>
 __device__ void
-riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R entho)
+riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R entho, R p0 = R(0))
 {
+  // FP32: total pressures are carried minus the constant p0 (the momentum
+  // flux comes out shifted by -p0; the energy flux and the wave speeds use
+  // the unshifted values), see flux_shift
+  constexpr bool shifted = sizeof(R) == 4;
   // the version-2 face stage gives both states the face-centred normal field,
   // and then the mean is that value exactly
   R a = ql[IA];
@@ -656,7 +687,7 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R ent
   const R b2l = a2 + bl * bl + cl * cl;
   const R emagl = R(0.5) * b2l;
   const R etotl = pl * entho + R(0.5) * (ul * ul + vl * vl + wl * wl) * rl + emagl;
-  const R ptotl = pl + emagl;
+  const R ptotl = shifted ? (pl - p0) + emagl : pl + emagl;
   const R vdotbl = ul * a + vl * bl + wl * cl;
 
   const R rr = qr[ID], pr = qr[IP], ur = qr[IU], vr = qr[IV], wr = qr[IW], br = qr[IB],
@@ -664,7 +695,7 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R ent
   const R b2r = a2 + br * br + cr * cr;
   const R emagr = R(0.5) * b2r;
   const R etotr = pr * entho + R(0.5) * (ur * ur + vr * vr + wr * wr) * rr + emagr;
-  const R ptotr = pr + emagr;
+  const R ptotr = shifted ? (pr - p0) + emagr : pr + emagr;
   const R vdotbr = ur * a + vr * br + wr * cr;
 
   R cfastl, cfastr;
@@ -756,10 +787,13 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R ent
   }
   else
   {
+    // with the shift: -ptot ul + ptot* u* = -(ptot - p0) ul + (ptot* - p0) u* + p0 (u* - ul)
     vdotbstarl = ustar * a + vstarl * bstarl + wstarl * cstarl;
-    etotstarl = (slu * etotl - ptotl * ul + ptotstar * ustar + a * (vdotbl - vdotbstarl)) * isls;
+    etotstarl = (slu * etotl - ptotl * ul + ptotstar * ustar + p0 * (ustar - ul) +
+                 a * (vdotbl - vdotbstarl)) * isls;
     vdotbstarr = ustar * a + vstarr * bstarr + wstarr * cstarr;
-    etotstarr = (sru * etotr - ptotr * ur + ptotstar * ustar + a * (vdotbr - vdotbstarr)) * isrs;
+    etotstarr = (sru * etotr - ptotr * ur + ptotstar * ustar + p0 * (ustar - ur) +
+                 a * (vdotbr - vdotbstarr)) * isrs;
   }
 
   R ro, uo, vo, wo, bo, co, ptoto, etoto, vdotbo;
@@ -810,7 +844,7 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R ent
   }
   const R rou = ro * uo;
   flux[ID] = rou;
-  flux[IP] = (etoto + ptoto) * uo - a * vdotbo;
+  flux[IP] = (etoto + (shifted ? ptoto + p0 : ptoto)) * uo - a * vdotbo;
   flux[IU] = rou * uo - a2 + ptoto;
   flux[IV] = rou * vo - a * bo;
   flux[IW] = rou * wo - a * co;
@@ -820,22 +854,27 @@ riemann_hlld_fast(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R ent
 }
 
 // riemann_mhd dispatch (RiemannSolvers_MHD.h:372-392); entho = 1/(gamma0-1),
-// precomputed once per run for the fast HLLD
+// precomputed once per run for the fast HLLD.  p0: the FP32 momentum-flux
+// shift (flux_shift); the HLL and LLF fluxes get it subtracted afterwards.
 template <class R>
 __device__ __forceinline__ void
-riemann(int solver, State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R entho)
+riemann(int solver, State<R> & ql, State<R> & qr, State<R> & flux, R gamma0, R entho,
+        R p0 = R(0))
 {
   if (solver == RIEMANN_HLLD)
   {
     if constexpr (kExactOrder)
       riemann_hlld(ql, qr, flux, gamma0);
     else
-      riemann_hlld_fast(ql, qr, flux, gamma0, entho);
+      riemann_hlld_fast(ql, qr, flux, gamma0, entho, p0);
+    return;
   }
-  else if (solver == RIEMANN_HLL)
+  if (solver == RIEMANN_HLL)
     riemann_hll(ql, qr, flux, gamma0);
   else
     riemann_llf(ql, qr, flux, gamma0);
+  if constexpr (sizeof(R) == 4)
+    flux[IU] = flux[IU] - p0;
 }
 
 // Two-dimensional HLLD magnetic Riemann solver giving the edge EMF
@@ -859,19 +898,17 @@ mag_riemann2d_hlld(const State<R> (&q)[4], const R (&e)[4], R gamma0, R smallc)
   const R rRR = qRR[ID], pRR = qRR[IP], uRR = qRR[IU], vRR = qRR[IV], aRR = qRR[IA],
           bRR = qRR[IB], cRR = qRR[IC];
 
-  const R cFastLLx = fast_speed_x(qLL, gamma0);
-  const R cFastLRx = fast_speed_x(qLR, gamma0);
-  const R cFastRLx = fast_speed_x(qRL, gamma0);
-  const R cFastRRx = fast_speed_x(qRR, gamma0);
-  const R cFastLLy = fast_speed_y(qLL, gamma0);
-  const R cFastLRy = fast_speed_y(qLR, gamma0);
-  const R cFastRLy = fast_speed_y(qRL, gamma0);
-  const R cFastRRy = fast_speed_y(qRR, gamma0);
+  // FMAX4 of the eight fast speeds as the roots of the largest squares
+  // (fast_speed2_x / _y): two square roots instead of eight
+  const R cxm = sqrt(max4(fast_speed2_x(qLL, gamma0), fast_speed2_x(qLR, gamma0),
+                          fast_speed2_x(qRL, gamma0), fast_speed2_x(qRR, gamma0)));
+  const R cym = sqrt(max4(fast_speed2_y(qLL, gamma0), fast_speed2_y(qLR, gamma0),
+                          fast_speed2_y(qRL, gamma0), fast_speed2_y(qRR, gamma0)));
 
-  const R SL = min4(uLL, uLR, uRL, uRR) - max4(cFastLLx, cFastLRx, cFastRLx, cFastRRx);
-  const R SR = max4(uLL, uLR, uRL, uRR) + max4(cFastLLx, cFastLRx, cFastRLx, cFastRRx);
-  const R SB = min4(vLL, vLR, vRL, vRR) - max4(cFastLLy, cFastLRy, cFastRLy, cFastRRy);
-  const R ST = max4(vLL, vLR, vRL, vRR) + max4(cFastLLy, cFastLRy, cFastRLy, cFastRRy);
+  const R SL = min4(uLL, uLR, uRL, uRR) - cxm;
+  const R SR = max4(uLL, uLR, uRL, uRR) + cxm;
+  const R SB = min4(vLL, vLR, vRL, vRR) - cym;
+  const R ST = max4(vLL, vLR, vRL, vRR) + cym;
 
   // region flags from the sign bits, as (int)(1 + copysign(1, S)) / 2 does
   const bool SB_pos = !signbit(SB), ST_pos = !signbit(ST);

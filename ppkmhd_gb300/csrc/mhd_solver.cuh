@@ -141,6 +141,7 @@ public:
   R *          F = nullptr;
   R *          Em = nullptr;
   R *          H = nullptr;  // version 2: face data (FaceData<DIM>)
+  R *          Ulo = nullptr; // FP32 version 2: low parts of the state (Buffers::Ulo)
   R *          T = nullptr;  // versions 0/1: stored trace states
   R *          D = nullptr;  // versions 0/1 in 3D: transverse face-field slopes
   int          version = 2;
@@ -188,7 +189,7 @@ public:
       cudaEventDestroy(copy_ev);
     if (copy_stream)
       cudaStreamDestroy(copy_stream);
-    R * bufs[] = { U, U2, Q, Q2, S, E, F, Em, H, T, D };
+    R * bufs[] = { U, U2, Q, Q2, S, E, F, Em, H, T, D, Ulo };
     for (R * b : bufs)
       if (b)
         cudaFree(b);
@@ -267,11 +268,13 @@ public:
     MHD_CK(cudaMalloc(&F, n * nf * dim * sizeof(R)));
     MHD_CK(cudaMalloc(&Em, n * nplanes_e * sizeof(R)));
     MHD_CK(cudaMalloc(&diag, (kDiagBlocks * 10 + 16) * sizeof(double)));
+    if (sizeof(R) == 4 && version == 2)
+      MHD_CK(cudaMalloc(&Ulo, n * NV * sizeof(R)));
     MHD_CK(cudaMalloc(&st, sizeof(DevState)));
     MHD_CK(cudaMallocHost(&st_host, sizeof(DevState)));
     // zero everything once: halo reads of never-written planes see zeros,
     // as the reference's zero-initialised Kokkos views do
-    R * bufs[] = { U, U2, Q, Q2 };
+    R * bufs[] = { U, U2, Q, Q2, Ulo };
     for (R * b : bufs)
       if (b)
         MHD_CK(cudaMemsetAsync(b, 0, n * NV * sizeof(R), stream));
@@ -319,6 +322,7 @@ public:
     B.F = F;
     B.Em = Em;
     B.H = H;
+    B.Ulo = Ulo;
     B.st = st;
     return B;
   }
@@ -639,10 +643,47 @@ public:
     return MHD_OK;
   }
 
+  int64_t
+  low_part_bytes() override
+  {
+    return Ulo ? ncell * NV * (int64_t)sizeof(R) : 0;
+  }
+
+  int
+  get_low_parts(void * host) override
+  {
+    if (!Ulo)
+      return MHD_OK;
+    MHD_CK(cudaMemcpyAsync(host, Ulo, (size_t)low_part_bytes(), cudaMemcpyDeviceToHost, stream));
+    MHD_CK(cudaStreamSynchronize(stream));
+    return MHD_OK;
+  }
+
+  int
+  set_low_parts(const void * host) override
+  {
+    if (!Ulo)
+      return MHD_OK;
+    MHD_CK(cudaMemcpyAsync(Ulo, host, (size_t)low_part_bytes(), cudaMemcpyHostToDevice, stream));
+    MHD_CK(cudaStreamSynchronize(stream));
+    return MHD_OK;
+  }
+
+  // the low parts of a state that comes from the host are zero
+  int
+  clear_low_parts()
+  {
+    if (Ulo)
+      MHD_CK(cudaMemsetAsync(Ulo, 0, (size_t)ncell * NV * sizeof(R), stream));
+    return MHD_OK;
+  }
+
   // boundaries + U2 = U + primitives + dt (SolverMHDMuscl.h:393-402)
   int
   apply_init()
   {
+    if (int rc = clear_low_parts())
+      return rc;
     launch_boundaries(U, 1);
     MHD_CK(cudaMemcpyAsync(U2, U, (size_t)ncell * NV * sizeof(R), cudaMemcpyDeviceToDevice, stream));
     launch_prim_dt(U, 1);
@@ -1019,6 +1060,9 @@ public:
     const int  nslab = host_slabs();
     const bool overlap = layout == MHD_LAYOUT_LEFT && version == 2 && nslab > 1;
     R *        out = (launched & 1) ? U : U2; // the buffer this iteration writes
+    // the host state is one float per value: the step starts without low parts
+    if (int rc = clear_low_parts())
+      return rc;
     if (overlap)
     {
       if (int rc = enqueue_step_host((int)(launched & 1), Uin, Uout, nslab))

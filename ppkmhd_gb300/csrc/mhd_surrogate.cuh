@@ -175,9 +175,11 @@ encode_fast(const float * qL, const float * qR, float a, float * feat, float * s
   return J;
 }
 
-// Central flux (F(qL) + F(qR)) / 2 with 1 / (gamma - 1) given.
+// Central flux (F(qL) + F(qR)) / 2 with 1 / (gamma - 1) given; the momentum
+// component minus the total-pressure shift p0 (flux_shift), as the HLLD
+// fallback faces store it.
 __device__ __forceinline__ void
-central_flux_fast(const float * qL, const float * qR, float a, float igm1, float * Fc)
+central_flux_fast(const float * qL, const float * qR, float a, float igm1, float * Fc, float p0)
 {
   float F[7] = { 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f };
 #pragma unroll
@@ -187,11 +189,12 @@ central_flux_fast(const float * qL, const float * qR, float a, float igm1, float
     const float   r = q[0], u = q[1], v = q[2], w = q[3], p = q[4], b = q[5], c = q[6];
     const float   B2 = a * a + b * b + c * c;
     const float   Pt = p + 0.5f * B2;
+    const float   Ps = (p - p0) + 0.5f * B2;
     const float   E = p * igm1 + 0.5f * r * (u * u + v * v + w * w) + 0.5f * B2;
     const float   vB = u * a + v * b + w * c;
     F[0] += r * u;
     F[1] += (E + Pt) * u - a * vB;
-    F[2] += r * u * u + Pt - a * a;
+    F[2] += r * u * u + Ps - a * a;
     F[3] += r * u * v - a * b;
     F[4] += r * u * w - a * c;
     F[5] += b * u - a * v;
@@ -232,7 +235,7 @@ flux_face_mlp(const Grid<float> & G, const Buffers<float> & B, const SurrogateDe
     const float smallR = G.smallr, smallp = G.smallp;
     smooth = J <= S.tau && l7[0] > smallR && r7[0] > smallR && l7[4] > smallp * l7[0] &&
              r7[4] > smallp * r7[0];
-    central_flux_fast(l7, r7, a, rcp(G.gamma0 - 1.f), Fc);
+    central_flux_fast(l7, r7, a, rcp(G.gamma0 - 1.f), Fc, flux_shift(B.st, 0.f));
 #pragma unroll
     for (int q = 0; q < 7; ++q)
     {

@@ -27,7 +27,8 @@ def test_restart_continues_bitwise(mhdlib, tmp_path, dim, precision):
     ref = a.get_state()
     with open(path, "rb") as f:
         h = HEADER.unpack(f.read(HEADER.size))
-    assert h[0] == b"PPKMHDCK" and h[1] == 1 and h[2] == dim
+    # format 2 carries the low parts of the compensated FP32 state
+    assert h[0] == b"PPKMHDCK" and h[1] == (2 if precision == 32 else 1) and h[2] == dim
     assert h[3:6] == (32, 24, 16 if dim == 3 else 1)
     assert h[8] == precision // 8 and h[9] == t7 and h[11] == 7 and h[12] == 3
     b = mhdlib.MHDSolver.from_ini(ini)

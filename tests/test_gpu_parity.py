@@ -191,6 +191,31 @@ def test_fp32_against_fp64_oracle(mhdlib, oracle, dim, n, steps):
     assert err.max() <= TOL_FP32, err
 
 
+def test_fp32_perturbed_orszag_tang_3d_200_steps(mhdlib, oracle):
+    """The FP32 acceptance case: the benchmark's initial condition (3D
+    Orszag-Tang + seeded 1e-3 velocity perturbation) at 64^3, 200 steps,
+    against the FP64 oracle, within 1e-3 relative L1 on every variable --
+    the z momentum and z field (the seed and what it induces, 1e-4 in size)
+    included.  Those two are where a plain float state fails: the state's
+    own rounding (about 3e-8 of the O(1) variables per step) accumulates into
+    them, to 3.4e-3 / 4.3e-3 on this case in IEEE FP32 arithmetic.  The
+    compensated state (float pair, momentum fluxes relative to one total
+    pressure) holds them within the bound while the arithmetic stays FP32."""
+    from ppkmhd_gb300 import workloads
+
+    ini = ot_ini(dim=3, nx=64, ny=64, nz=64)
+    o = oracle.OracleSolver(ini, nthreads=16)
+    U0 = workloads.perturbed_ot_3d(o.get_state().astype(np.float64))
+    o.set_state(U0)
+    o.run(200)
+    s = gpu_solver(mhdlib, ini, precision=32)
+    s.set_state(U0.astype(np.float32))
+    assert s.run(200) == 200
+    err = rel_l1(mhdlib.interior(s.get_state()).astype(np.float64),
+                 oracle.interior(o.get_state()))
+    assert err.max() <= TOL_FP32, err
+
+
 def test_layout_right_roundtrip_and_equivalence(mhdlib, oracle):
     ini = ot_ini(dim=3, nx=9, ny=7, nz=6)
     o = oracle.OracleSolver(ini)
@@ -273,7 +298,9 @@ def test_step_host_versions_0_1_ignore_slabs(mhdlib, version):
 
 def test_step_host_slabs_pinned_fp32(mhdlib):
     """Pinned host buffers (copies truly asynchronous) in FP32, 3D, with the
-    slab count changed between steps: bitwise the state of run()."""
+    slab count changed between steps: each host-buffer step is bitwise one
+    run() step from the same float state.  (A host state has no low parts,
+    so each call starts from the float state, as set_state does.)"""
     torch = pytest.importorskip("torch")
     ini = ot_ini(dim=3, nx=24, ny=20, nz=18)
     a = gpu_solver(mhdlib, ini, precision=32)
@@ -281,7 +308,6 @@ def test_step_host_slabs_pinned_fp32(mhdlib):
     for s in (a, c):
         s.init_problem()
     c.set_host_slabs(4)
-    a.run(6)
     U0 = c.get_state()
     h_in = torch.from_numpy(U0.reshape(-1).copy()).pin_memory()
     h_out = torch.zeros_like(h_in).pin_memory()
@@ -289,10 +315,13 @@ def test_step_host_slabs_pinned_fp32(mhdlib):
         if q == 4:
             c.set_host_slabs(3)
         x, y = (h_in, h_out) if q % 2 == 0 else (h_out, h_in)
+        a.set_state(x.numpy().reshape(U0.shape))
+        a.run(1)
         c.step_host_ptr(x.data_ptr(), y.data_ptr())
-    got = h_in.numpy().reshape(U0.shape)
-    assert np.array_equal(mhdlib.interior(a.get_state()), mhdlib.interior(got))
-    assert a.time() == c.time()
+        got = y.numpy().reshape(U0.shape)
+        assert np.array_equal(mhdlib.interior(a.get_state()), mhdlib.interior(got)), q
+        assert a.time()[1] == c.time()[1]
+    assert c.time()[2] == 6
     with pytest.raises(mhdlib.MHDError):
         c.set_host_slabs(17)
 

@@ -240,7 +240,8 @@ def test_surrogate_flux_stage_against_fp64_oracle(mhdlib, oracle):
 @pytest.mark.gpu
 def test_surrogate_step_host_slabs_match_run(mhdlib):
     """The host-buffer step in slabs with the network in the flux stage (one
-    more launch before the edge stage) gives the state of run(), bitwise."""
+    more launch before the edge stage) gives the state of a run() step from
+    the same float state, bitwise."""
     from ppkmhd_gb300.surrogate import FluxMLP
 
     ini, U = _turbulence_case(24)
@@ -251,13 +252,16 @@ def test_surrogate_step_host_slabs_match_run(mhdlib):
         s.set_state(U.astype(np.float32))
         s.set_surrogate(mlp, tau=0.01)
     c.set_host_slabs(3)
-    a.run(3)
     V = c.get_state()
     out = np.zeros_like(V)
-    for _ in range(3):
+    for q in range(3):
+        # a host state starts without low parts: compare with one run() step
+        # from the same float state
+        a.set_state(V)
+        a.run(1)
         c.step_host(V, out)
+        assert np.array_equal(mhdlib.interior(a.get_state()), mhdlib.interior(out)), q
         V, out = out, V
-    assert np.array_equal(mhdlib.interior(a.get_state()), mhdlib.interior(V))
 
 
 @pytest.mark.gpu

@@ -57,10 +57,15 @@ def test_noalloc_matches_context_path_two_calls(mhdlib, dim, n, precision):
     ref.init_problem()
     U0 = ref.get_state()
     t0, _, _ = ref.time()
+    # one context step from each state the caller holds (set_state: an FP32
+    # state from outside has no low parts, as for the caller's arrays here)
     expected, dts = [], []
+    state = U0
     for _ in range(2):
+        ref.set_state(state)
         ref.run(1)
-        expected.append(m.interior(ref.get_state()))
+        state = ref.get_state()
+        expected.append(m.interior(state))
         dts.append(ref.time()[1])
     p = ref.params
     ref.close()
