@@ -301,8 +301,26 @@ const char *mhd_ensemble_last_error(mhd_ensemble *ens);
  * restarts at 0 as in the reference.  Continuing from a checkpoint is
  * bitwise equal to the uninterrupted run.
  */
+/* VTK ImageData output of a host state (save_VTK_2D / save_VTK_3D,
+ * src/utils/io/IO_VTK.cpp:24-209, :212-410 of the reference): interior cells,
+ * one cell-data array per variable named as SolverBase does (rho, energy,
+ * rho_vx, rho_vy, rho_vz, bx, by, bz), raw appended binary with a UInt64 byte
+ * count before each array (or ASCII with [output] outputVtkAscii), written to
+ * [output] outputDir/outputPrefix_NNNNNNN.vti for the mesh of ini_text.
+ * U: ghost-inclusive LayoutLeft FP64 state.  The file name is copied to path
+ * (pathlen bytes, may be NULL).  Host only: needs no device. */
+int mhd_write_vtk(const char *ini_text, const double *U, int iStep, char *path, size_t pathlen);
+
 int mhd_checkpoint_save(mhd_ctx *ctx, const char *path, int times_saved);
 int mhd_checkpoint_load(mhd_ctx *ctx, const char *path, int reset_time, int *times_saved);
+/* [run] restart_upscale (copy_buffer of the HDF5 restart reader, IO_HDF5.h:
+ * 1603-1694): load a checkpoint of half the context's resolution (nx/2,
+ * ny/2[, nz/2]; nx, ny, nz even).  Fine cell i (ghost-inclusive) takes coarse
+ * cell (i + g) / 2 along every axis; the face-centred normal field takes the
+ * coarse face value where i + g is even and the mean of the two coarse faces
+ * around it otherwise, which keeps the discrete div B at zero.  A format-2
+ * file's low parts are not carried over. */
+int mhd_checkpoint_load_upscaled(mhd_ctx *ctx, const char *path, int reset_time, int *times_saved);
 
 /*
  * HLLD flux surrogate.  The reference has no learned component; this is the

@@ -22,6 +22,7 @@ SRCS=(
   "$REF/src/utils/config/ConfigMap.cpp"
   "$REF/src/utils/config/inih/INIReader.cpp"
   "$REF/src/utils/config/inih/ini.cpp"
+  "$REF/src/utils/io/IO_VTK.cpp"
 )
 INC=(-I "$HERE/kokkos_shim" -I "$REF/src" -I "$REF/src/utils")
 # -ffp-contract=off: no FMA contraction, as a plain x86-64 g++ build of the

@@ -29,6 +29,7 @@
 #include <memory>
 #include <ostream>
 #include <iostream>
+#include <sstream>
 #include <string>
 #include <type_traits>
 #include <initializer_list>

@@ -218,6 +218,19 @@ def ref_available(bits: int = 64) -> bool:
     return os.path.exists(REF_SO[bits])
 
 
+def ref_save_vtk(ini_text: str, U_left: np.ndarray, istep: int, bits: int = 64) -> None:
+    """The reference's own VTK writer (save_VTK_2D / save_VTK_3D of
+    IO_VTK.cpp, compiled via the shim) on a LayoutLeft state; the file goes
+    where the .ini's [output] section says."""
+    L = ctypes.CDLL(REF_SO[bits])
+    L.ref_save_vtk.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int]
+    L.ref_save_vtk.restype = ctypes.c_int
+    real = np.float64 if bits == 64 else np.float32
+    UR = np.ascontiguousarray(np.asarray(U_left, dtype=real).T)  # LayoutRight (i,j[,k],var)
+    if L.ref_save_vtk(ini_text.encode(), UR.ctypes.data_as(ctypes.c_void_p), int(istep)) != 0:
+        raise ValueError("reference: unsupported solver_name")
+
+
 class RefSolver:
     """The reference's own functors (compiled via the Kokkos-API shim)."""
 

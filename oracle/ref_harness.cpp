@@ -32,6 +32,7 @@
 #include "muscl/MHDRunFunctors2D.h"
 #include "muscl/MHDRunFunctors3D.h"
 #include "utils/config/ConfigMap.h"
+#include "utils/io/IO_VTK.h"
 
 using namespace ppkMHD;
 using namespace ppkMHD::muscl;
@@ -629,6 +630,41 @@ extern "C"
     if (emf_dir == EMFY)
       return compute_emf<EMFY>(q, p);
     return compute_emf<EMFX>(q, p);
+  }
+
+  // The reference's VTK writer (save_VTK_2D / save_VTK_3D, IO_VTK.cpp) on the
+  // state u (LayoutRight, the sizes of the .ini), with SolverBase's variable
+  // names (SolverBase.cpp:48-55) and no debug name.  Returns 0, or -1 on an
+  // unknown solver.
+  int
+  ref_save_vtk(const char * ini_text, const real_t * u, int iStep)
+  {
+    std::string s(ini_text);
+    char *      buf = &s[0];
+    ConfigMap   cfg(buf, (int)s.size());
+    HydroParams params;
+    params.setup(cfg);
+    const std::map<int, std::string> names = { { ID, "rho" },    { IP, "energy" }, { IU, "rho_vx" },
+                                               { IV, "rho_vy" }, { IW, "rho_vz" }, { IA, "bx" },
+                                               { IB, "by" },     { IC, "bz" } };
+    const std::string solver = cfg.getString("run", "solver_name", "unknown");
+    if (solver == "MHD_Muscl_2D")
+    {
+      DataArray2d U("U", params.isize, params.jsize, params.nbvar);
+      std::memcpy(U.data(), u, U.size() * sizeof(real_t));
+      DataArray2d::HostMirror Uh = Kokkos::create_mirror(U);
+      ppkMHD::io::save_VTK_2D(U, Uh, params, cfg, params.nbvar, names, iStep, "");
+      return 0;
+    }
+    if (solver == "MHD_Muscl_3D")
+    {
+      DataArray3d U("U", params.isize, params.jsize, params.ksize, params.nbvar);
+      std::memcpy(U.data(), u, U.size() * sizeof(real_t));
+      DataArray3d::HostMirror Uh = Kokkos::create_mirror(U);
+      ppkMHD::io::save_VTK_3D(U, Uh, params, cfg, params.nbvar, names, iStep, "");
+      return 0;
+    }
+    return -1;
   }
 
   // Effective (float-rounded, as ConfigMap::getFloat parses) parameters:

@@ -87,6 +87,8 @@ _fp = ctypes.POINTER(ctypes.c_float)
 _i64p = ctypes.POINTER(ctypes.c_int64)
 SIGNATURES = {
     "mhd_params_default": (ctypes.c_int, [ctypes.POINTER(MHDParams)]),
+    "mhd_write_vtk": (ctypes.c_int, [ctypes.c_char_p, _vp, ctypes.c_int, ctypes.c_char_p,
+                                     ctypes.c_size_t]),
     "mhd_params_from_ini": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(MHDParams),
                                            ctypes.c_char_p, ctypes.c_size_t]),
     "mhd_create": (ctypes.c_int, [ctypes.POINTER(MHDParams), ctypes.POINTER(_vp)]),
@@ -133,6 +135,7 @@ SIGNATURES = {
     "mhd_harvest_faces": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_int64, _i64p]),
     "mhd_checkpoint_save": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int]),
     "mhd_checkpoint_load": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int, _ip]),
+    "mhd_checkpoint_load_upscaled": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int, _ip]),
     "mhd_mlp_create": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(_vp)]),
     "mhd_mlp_destroy": (ctypes.c_int, [_vp]),
     "mhd_mlp_set_params": (ctypes.c_int, [_vp, _vp, ctypes.c_int]),
@@ -189,6 +192,18 @@ def initial_state(params: MHDParams) -> np.ndarray:
     if rc != MHD_OK:
         raise MHDError(rc, "invalid parameters")
     return U
+
+
+def write_vtk(ini_text: str, U: np.ndarray, istep: int = 0) -> str:
+    """Write the LayoutLeft FP64 state U as the reference's .vti file (the
+    .ini's [output] outputDir / outputPrefix / outputVtkAscii); returns the
+    file name.  Host only."""
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    path = ctypes.create_string_buffer(4096)
+    rc = lib().mhd_write_vtk(ini_text.encode(), U.ctypes.data, int(istep), path, len(path))
+    if rc != MHD_OK:
+        raise MHDError(rc, "mhd_write_vtk failed")
+    return path.value.decode()
 
 
 def default_params() -> MHDParams:
@@ -346,6 +361,14 @@ class MHDSolver:
         ts = ctypes.c_int()
         self._check(lib().mhd_checkpoint_load(self.h, os.fsencode(path), int(reset_time),
                                               ctypes.byref(ts)))
+        return ts.value
+
+    def checkpoint_load_upscaled(self, path: str, reset_time: bool = False) -> int:
+        """Restore from a checkpoint of half the resolution ([run]
+        restart_upscale); returns its output counter."""
+        ts = ctypes.c_int()
+        self._check(lib().mhd_checkpoint_load_upscaled(self.h, os.fsencode(path), int(reset_time),
+                                                       ctypes.byref(ts)))
         return ts.value
 
     def harvest(self, stride: int = 1) -> np.ndarray:

@@ -138,6 +138,122 @@ namespace mhd
 
 } // namespace mhd
 
+namespace
+{
+
+// restart_upscale (IO_HDF5.h:1603-1694 of the reference, copy_buffer): a
+// state of half the resolution, ghost cells included (isize_c = nx/2 + 2g),
+// onto the context's grid.  Fine cell i (ghost-inclusive) takes coarse cell
+// (i + g) / 2 (integer division) along every axis; the face-centred normal
+// field takes the coarse face value where i + g is even and the mean of the
+// two coarse faces around it otherwise, so the discrete div B stays zero.
+template <class T>
+void
+upscale_state(const T * c, T * f, int dim, int isize, int jsize, int ksize, int g, int nx, int ny)
+{
+  const int64_t iL = nx / 2 + 2 * g, jL = ny / 2 + 2 * g;
+  const int64_t cv = iL * jL * (dim == 3 ? (ksize - 2 * g) / 2 + 2 * g : 1);
+  const int64_t fv = (int64_t)isize * jsize * ksize;
+  for (int v = 0; v < 8; ++v)
+    for (int k = 0; k < ksize; ++k)
+    {
+      const int kl = dim == 3 ? (k + g) / 2 : 0;
+      for (int j = 0; j < jsize; ++j)
+      {
+        const int jl = (j + g) / 2;
+        for (int i = 0; i < isize; ++i)
+        {
+          const int      il = (i + g) / 2;
+          const T *      src = c + v * cv;
+          const int64_t  a = il + iL * jl + iL * jL * kl;
+          T              x = src[a];
+          if (v == 5 && i + g - 2 * il != 0)
+            x = (src[a] + src[a + 1]) / 2;
+          else if (v == 6 && j + g - 2 * jl != 0)
+            x = (src[a] + src[a + iL]) / 2;
+          else if (dim == 3 && v == 7 && k + g - 2 * kl != 0)
+            x = (src[a] + src[a + iL * jL]) / 2;
+          f[v * fv + i + (int64_t)isize * (j + (int64_t)jsize * k)] = x;
+        }
+      }
+    }
+}
+
+int
+checkpoint_load(mhd_ctx * ctx, const char * path, int reset_time, int * times_saved, bool upscale)
+{
+  if (!ctx || !ctx->core)
+    return MHD_ERR_INVALID_ARG;
+  if (!path)
+    return fail(ctx, MHD_ERR_INVALID_ARG, "null path");
+  FILE * f = std::fopen(path, "rb");
+  if (!f)
+    return fail(ctx, MHD_ERR_INVALID_ARG, std::string("cannot open ") + path);
+  CheckpointHeader   h{};
+  const bool         got = std::fread(&h, sizeof h, 1, f) == 1;
+  const mhd_params & p = ctx->params;
+  const int          k = upscale ? 2 : 1; // file resolution = context / k
+  std::string        bad;
+  if (!got || std::memcmp(h.magic, "PPKMHDCK", 8) != 0 || (h.format != 1 && h.format != 2))
+    bad = "not a checkpoint file (format 1 or 2)";
+  else if (upscale && (p.nx % 2 || p.ny % 2 || (p.dim == 3 && p.nz % 2)))
+    bad = "restart_upscale needs even nx, ny, nz";
+  else if ((int)h.dim != p.dim || (int)h.nx * k != p.nx || (int)h.ny * k != p.ny ||
+           (p.dim == 3 && (int)h.nz * k != p.nz) || (int)h.ghost != p.ghost || h.nbvar != 8)
+    bad = upscale ? "checkpoint grid is not half the context's (restart_upscale)"
+                  : "checkpoint grid does not match the context";
+  else if ((int)h.real_bytes != ctx->core->real_bytes())
+    bad = "checkpoint precision does not match the context";
+  int sz[4];
+  ctx->core->sizes(sz);
+  const int                  g = p.ghost;
+  const size_t               nfile = (size_t)(h.nx + 2 * g) * (h.ny + 2 * g) *
+                         (p.dim == 3 ? h.nz + 2 * g : 1) * 8;
+  std::vector<unsigned char> U, lo;
+  if (bad.empty())
+  {
+    U.resize(nfile * h.real_bytes);
+    if (std::fread(U.data(), 1, U.size(), f) != U.size())
+      bad = "checkpoint file is truncated";
+    // the low parts of a compensated FP32 state carry over at the same
+    // resolution only (an upscaled state starts without them)
+    if (bad.empty() && h.format == 2 && !upscale)
+    {
+      lo.resize((size_t)ctx->core->low_part_bytes());
+      if (lo.empty())
+        bad = "checkpoint has low parts the context does not keep";
+      else if (std::fread(lo.data(), 1, lo.size(), f) != lo.size())
+        bad = "checkpoint file is truncated";
+    }
+  }
+  std::fclose(f);
+  if (!bad.empty())
+    return fail(ctx, MHD_ERR_INVALID_ARG, bad);
+  if (upscale)
+  {
+    std::vector<unsigned char> fine((size_t)sz[0] * sz[1] * sz[2] * sz[3] * h.real_bytes);
+    if (h.real_bytes == 8)
+      upscale_state((const double *)U.data(), (double *)fine.data(), p.dim, sz[0], sz[1],
+                    p.dim == 3 ? sz[2] : 1, g, p.nx, p.ny);
+    else
+      upscale_state((const float *)U.data(), (float *)fine.data(), p.dim, sz[0], sz[1],
+                    p.dim == 3 ? sz[2] : 1, g, p.nx, p.ny);
+    U.swap(fine);
+  }
+  ctx->core->set_time_origin(reset_time ? 0.0 : h.t);
+  int rc = ctx->core->set_state(U.data(), MHD_LAYOUT_LEFT);
+  ctx->core->set_time_origin(p.tCurrent);
+  if (rc == MHD_OK && !lo.empty())
+    rc = ctx->core->set_low_parts(lo.data());
+  if (rc)
+    return from_core(ctx, rc);
+  if (times_saved)
+    *times_saved = h.times_saved;
+  return MHD_OK;
+}
+
+} // namespace
+
 extern "C"
 {
 
@@ -477,53 +593,13 @@ extern "C"
   int
   mhd_checkpoint_load(mhd_ctx * ctx, const char * path, int reset_time, int * times_saved)
   {
-    NEED_CORE(ctx);
-    if (!path)
-      return fail(ctx, MHD_ERR_INVALID_ARG, "null path");
-    FILE * f = std::fopen(path, "rb");
-    if (!f)
-      return fail(ctx, MHD_ERR_INVALID_ARG, std::string("cannot open ") + path);
-    CheckpointHeader h{};
-    const bool       got = std::fread(&h, sizeof h, 1, f) == 1;
-    const mhd_params & p = ctx->params;
-    std::string      bad;
-    if (!got || std::memcmp(h.magic, "PPKMHDCK", 8) != 0 || (h.format != 1 && h.format != 2))
-      bad = "not a checkpoint file (format 1 or 2)";
-    else if ((int)h.dim != p.dim || (int)h.nx != p.nx || (int)h.ny != p.ny ||
-             (p.dim == 3 && (int)h.nz != p.nz) || (int)h.ghost != p.ghost || h.nbvar != 8)
-      bad = "checkpoint grid does not match the context";
-    else if ((int)h.real_bytes != ctx->core->real_bytes())
-      bad = "checkpoint precision does not match the context";
-    std::vector<unsigned char> U, lo;
-    if (bad.empty())
-    {
-      int sz[4];
-      ctx->core->sizes(sz);
-      U.resize((size_t)sz[0] * sz[1] * sz[2] * sz[3] * h.real_bytes);
-      if (std::fread(U.data(), 1, U.size(), f) != U.size())
-        bad = "checkpoint file is truncated";
-      if (bad.empty() && h.format == 2)
-      {
-        lo.resize((size_t)ctx->core->low_part_bytes());
-        if (lo.empty())
-          bad = "checkpoint has low parts the context does not keep";
-        else if (std::fread(lo.data(), 1, lo.size(), f) != lo.size())
-          bad = "checkpoint file is truncated";
-      }
-    }
-    std::fclose(f);
-    if (!bad.empty())
-      return fail(ctx, MHD_ERR_INVALID_ARG, bad);
-    ctx->core->set_time_origin(reset_time ? 0.0 : h.t);
-    int rc = ctx->core->set_state(U.data(), MHD_LAYOUT_LEFT);
-    ctx->core->set_time_origin(p.tCurrent);
-    if (rc == MHD_OK && !lo.empty())
-      rc = ctx->core->set_low_parts(lo.data());
-    if (rc)
-      return from_core(ctx, rc);
-    if (times_saved)
-      *times_saved = h.times_saved;
-    return MHD_OK;
+    return checkpoint_load(ctx, path, reset_time, times_saved, false);
+  }
+
+  int
+  mhd_checkpoint_load_upscaled(mhd_ctx * ctx, const char * path, int reset_time, int * times_saved)
+  {
+    return checkpoint_load(ctx, path, reset_time, times_saved, true);
   }
 
   int

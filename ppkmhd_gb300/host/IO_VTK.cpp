@@ -1,8 +1,11 @@
 #include "IO_VTK.h"
 
 #include <cstdint>
+#include <cstring>
 #include <fstream>
 #include <sstream>
+
+#include "ppkmhd_gb300.h"
 
 namespace ppkmhd_gb300
 {
@@ -86,3 +89,36 @@ save_VTK(const double * U, const HydroParams & params, const ConfigMap & configM
 }
 
 } // namespace ppkmhd_gb300
+
+extern "C"
+{
+
+  // The .ini's [output] outputDir / outputPrefix / outputVtkAscii and mesh
+  // decide the file; U is the ghost-inclusive LayoutLeft FP64 state; the
+  // variable names are SolverBase's (SolverBase.cpp:48-55 of the reference).
+  int
+  mhd_write_vtk(const char * ini_text, const double * U, int iStep, char * path, size_t pathlen)
+  {
+    if (!ini_text || !U || iStep < 0)
+      return MHD_ERR_INVALID_ARG;
+    const ConfigMap map(ini_text, (int)std::strlen(ini_text));
+    if (map.ParseError() != 0)
+      return MHD_ERR_PARSE;
+    ppkmhd_gb300::HydroParams params;
+    params.setup(map);
+    const std::map<int, std::string> names = { { 0, "rho" },    { 1, "energy" }, { 2, "rho_vx" },
+                                               { 3, "rho_vy" }, { 4, "rho_vz" }, { 5, "bx" },
+                                               { 6, "by" },     { 7, "bz" } };
+    const int         dim = params.dimType == ppkmhd_gb300::THREE_D ? 3 : 2;
+    const std::string file = ppkmhd_gb300::save_VTK(U, params, map, names, iStep, dim);
+    if (file.empty())
+      return MHD_ERR_INVALID_ARG;
+    if (path && pathlen)
+    {
+      std::strncpy(path, file.c_str(), pathlen - 1);
+      path[pathlen - 1] = '\0';
+    }
+    return MHD_OK;
+  }
+
+} // extern "C"

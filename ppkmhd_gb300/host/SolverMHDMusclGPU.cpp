@@ -23,7 +23,10 @@ SolverMHDMusclGPU<dim>::SolverMHDMusclGPU(HydroParams & p, ConfigMap & cfg)
   {
     const std::string file = cfg.getString("run", "restart_filename", "");
     const bool        reset = cfg.getBool("run", "restart_reset_totaltime", false);
-    rc = mhd_checkpoint_load(ctx, file.c_str(), reset ? 1 : 0, &m_times_saved);
+    // restart_upscale: the file holds half the resolution (IO_HDF5.h:1603-1694)
+    const bool        upscale = cfg.getBool("run", "restart_upscale", false);
+    rc = upscale ? mhd_checkpoint_load_upscaled(ctx, file.c_str(), reset ? 1 : 0, &m_times_saved)
+                 : mhd_checkpoint_load(ctx, file.c_str(), reset ? 1 : 0, &m_times_saved);
     if (rc == MHD_OK)
       std::cout << "### This is a restarted run ! ###\n";
   }

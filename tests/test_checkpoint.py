@@ -65,3 +65,58 @@ def test_checkpoint_rejects_mismatch(mhdlib, tmp_path):
     assert "truncated" in str(e.value)
     with pytest.raises(mhdlib.MHDError):
         a.checkpoint_load(str(tmp_path / "missing.ckpt"))
+
+
+def _upscale_reference(Uc, dim, g=3):
+    """copy_buffer with restart_upscale (IO_HDF5.h:1603-1694), restated:
+    fine cell i <- coarse (i + g) // 2 per axis; the face-centred normal field
+    averages the two coarse faces where i + g is odd."""
+    Uc = np.asarray(Uc)
+    fine_shape = tuple(2 * (n - 2 * g) + 2 * g for n in Uc.shape[1:])
+    idx = [(np.arange(n) + g) // 2 for n in fine_shape]
+    grids = np.meshgrid(*idx, indexing="ij")
+    par = [((np.arange(n) + g) % 2) for n in fine_shape]
+    U = np.empty((8,) + fine_shape, dtype=Uc.dtype)
+    for v in range(8):
+        U[v] = Uc[v][tuple(grids)]
+    # axes of the [var][k][j][i] arrays: x is the last one
+    axes = {5: dim, 6: dim - 1, 7: dim - 2}
+    for v, ax in axes.items():
+        if v == 7 and dim == 2:
+            continue
+        odd = par[ax - 1].astype(bool)
+        shifted = [g_.copy() for g_ in grids]
+        shifted[ax - 1] = shifted[ax - 1] + 1
+        avg = (Uc[v][tuple(grids)] + Uc[v][tuple(shifted)]) / 2
+        m = odd.reshape([-1 if a == ax - 1 else 1 for a in range(dim)])
+        U[v] = np.where(m, avg, U[v])
+    return U
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim,precision", [(2, 64), (3, 64), (3, 32)])
+def test_restart_upscale_from_half_resolution(mhdlib, tmp_path, dim, precision):
+    coarse = mhdlib.MHDSolver.from_ini(ot_ini(dim=dim, nx=16, ny=12, nz=10, precision=precision))
+    coarse.init_problem()
+    coarse.run(5)
+    path = str(tmp_path / "coarse.ckpt")
+    coarse.checkpoint_save(path, times_saved=2)
+    Uc = coarse.get_state()
+    t5 = coarse.time()[0]
+    fine = mhdlib.MHDSolver.from_ini(ot_ini(dim=dim, nx=32, ny=24, nz=20, precision=precision))
+    assert fine.checkpoint_load_upscaled(path) == 2
+    assert fine.time()[0] == t5
+    expect = _upscale_reference(Uc, dim)
+    got = fine.get_state()
+    # interior cells as the reference's copy_buffer builds them (the ghost
+    # cells are refilled by the boundary conditions)
+    assert np.array_equal(mhdlib.interior(got), mhdlib.interior(expect))
+    # the averaged face field keeps the discrete divergence at round-off
+    _, _, divb_max = fine.diagnostics()
+    assert divb_max < (1e-12 if precision == 64 else 1e-4), divb_max
+    assert fine.run(3) == 3
+    # a same-size context refuses the half-resolution file, and vice versa
+    with pytest.raises(mhdlib.MHDError):
+        fine.checkpoint_load(path)
+    with pytest.raises(mhdlib.MHDError):
+        coarse.checkpoint_load_upscaled(path)
