@@ -271,9 +271,30 @@ int mhd_ensemble_diagnostics(mhd_ensemble *ens, int prob, double sums[8], double
                              double *divb_max);
 
 /* Pick the threads per block of every batched kernel by timing candidates
- * on the current states (results unchanged); report = one line per
- * candidate (may be NULL). */
+ * on the current states, then the form (graphs or persistent, two timed
+ * iterations of each on a snapshot of the states); results unchanged;
+ * report = one line per candidate (may be NULL). */
 int mhd_ensemble_autotune(mhd_ensemble *ens, char *report, size_t report_len);
+
+/* The form mhd_ensemble_run takes (the ensemble has no counterpart in the
+ * reference).  MHD_ENSEMBLE_GRAPHS: the eight per-stage launches of an
+ * iteration, each over all problems, replayed from CUDA graphs (the
+ * default).  MHD_ENSEMBLE_PERSISTENT: the whole run in one cooperative
+ * launch of as many blocks as are resident, the stages of every iteration
+ * separated by grid-wide barriers; same kernel bodies, same states bit for
+ * bit.  mhd_ensemble_autotune times both on the current states and keeps
+ * the faster. */
+#define MHD_ENSEMBLE_GRAPHS 0
+#define MHD_ENSEMBLE_PERSISTENT 1
+int mhd_ensemble_set_mode(mhd_ensemble *ens, int mode);
+int mhd_ensemble_get_mode(mhd_ensemble *ens, int *mode);
+
+/* Bound, in clock cycles, of every grid-barrier wait of the persistent form
+ * (default 2^34).  A wait that runs out stops the launch early: the run
+ * returns MHD_ERR_CUDA, the states of that run are incomplete (set them
+ * again) and the ensemble stays usable.  0 makes every wait give up at once:
+ * the way to exercise that path. */
+int mhd_ensemble_set_wait_limit(mhd_ensemble *ens, long long cycles);
 
 /* As mhd_profile_step, for one iteration of the whole ensemble. */
 int mhd_ensemble_profile_step(mhd_ensemble *ens, const char **names, float *ms, int max,

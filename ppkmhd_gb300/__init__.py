@@ -32,6 +32,7 @@ MHD_ERR_NUMERIC = -4
 MHD_ERR_PARSE = -5
 MHD_ERR_TOO_LARGE = -6
 MHD_FINISHED = 1  # mhd_step_noalloc: t >= tEnd, nothing computed
+MHD_ENSEMBLE_GRAPHS, MHD_ENSEMBLE_PERSISTENT = 0, 1
 
 MHD_RIEMANN_LLF, MHD_RIEMANN_HLL, MHD_RIEMANN_HLLD = 1, 2, 4
 MHD_BC_REFLECTING, MHD_BC_OUTFLOW, MHD_BC_PERIODIC = 1, 2, 3
@@ -126,6 +127,9 @@ SIGNATURES = {
     "mhd_ensemble_run": (ctypes.c_int, [_vp, ctypes.c_int, _fp]),
     "mhd_ensemble_time": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _ip]),
     "mhd_ensemble_diagnostics": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp]),
+    "mhd_ensemble_set_mode": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "mhd_ensemble_get_mode": (ctypes.c_int, [_vp, _ip]),
+    "mhd_ensemble_set_wait_limit": (ctypes.c_int, [_vp, ctypes.c_longlong]),
     "mhd_ensemble_autotune": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_size_t]),
     "mhd_ensemble_profile_step": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_char_p), _fp,
                                                  ctypes.c_int, _ip]),
@@ -534,6 +538,21 @@ class MHDEnsemble:
         self._check(lib().mhd_ensemble_diagnostics(self.h, int(prob), sums, ctypes.byref(l1),
                                                    ctypes.byref(mx)))
         return np.array(list(sums)), l1.value, mx.value
+
+    def set_mode(self, mode: int):
+        """MHD_ENSEMBLE_GRAPHS or MHD_ENSEMBLE_PERSISTENT."""
+        self._check(lib().mhd_ensemble_set_mode(self.h, int(mode)))
+
+    @property
+    def mode(self) -> int:
+        m = ctypes.c_int()
+        self._check(lib().mhd_ensemble_get_mode(self.h, ctypes.byref(m)))
+        return m.value
+
+    def set_wait_limit(self, cycles: int):
+        """Clock-cycle bound of the persistent form's barrier waits (0: give
+        up at once)."""
+        self._check(lib().mhd_ensemble_set_wait_limit(self.h, int(cycles)))
 
     def autotune(self) -> str:
         buf = ctypes.create_string_buffer(8192)

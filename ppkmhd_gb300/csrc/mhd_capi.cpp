@@ -811,6 +811,30 @@ extern "C"
   }
 
   int
+  mhd_ensemble_set_mode(mhd_ensemble * e, int mode)
+  {
+    NEED_ENSEMBLE(e);
+    return from_core(e, e->core->set_mode(mode));
+  }
+
+  int
+  mhd_ensemble_get_mode(mhd_ensemble * e, int * mode)
+  {
+    NEED_ENSEMBLE(e);
+    if (!mode)
+      return fail(e, MHD_ERR_INVALID_ARG, "null output");
+    *mode = e->core->mode();
+    return MHD_OK;
+  }
+
+  int
+  mhd_ensemble_set_wait_limit(mhd_ensemble * e, long long cycles)
+  {
+    NEED_ENSEMBLE(e);
+    return from_core(e, e->core->set_wait_limit(cycles));
+  }
+
+  int
   mhd_ensemble_profile_step(mhd_ensemble * e, const char ** names, float * ms, int max, int * count)
   {
     NEED_ENSEMBLE(e);

@@ -67,6 +67,11 @@ public:
   virtual int profile_step(const char ** names, float * ms, int max, int * count) = 0;
   virtual int cells(int64_t * interior) = 0;
   virtual int launches_per_step() const = 0;
+  //! MHD_ENSEMBLE_GRAPHS or MHD_ENSEMBLE_PERSISTENT (mhd_ensemble_set_mode)
+  virtual int set_mode(int mode) = 0;
+  virtual int mode() const = 0;
+  //! clock-cycle bound of every grid-barrier wait of the persistent form
+  virtual int set_wait_limit(long long cycles) = 0;
   virtual int real_bytes() const = 0;
   virtual int bind_device() = 0;
   std::string err;

@@ -156,6 +156,168 @@ kb_update(const Grid<R> * Gs, const Buffers<R> * Bs, const BlockRef * map, int p
   update_body<R, DIM>(v.G, v.B, m.b * (int64_t)blockDim.x + threadIdx.x);
 }
 
+// ---------------------------------------------------------------- persistent form
+
+// One work item of the persistent kernel: a problem, a block of that
+// problem's box and, for the face and edge stages, the direction.
+struct PersistRef
+{
+  int p, b, d;
+};
+
+// Work lists of the six box stages (boundaries, primitives + CFL, trace,
+// faces, edges, update) for blocks of kPersistThreads threads.
+constexpr int kPersistThreads = 256;
+struct PersistWork
+{
+  const PersistRef * list[6];
+  unsigned           n[6];
+};
+
+// Grid-wide barrier state of the persistent kernel.
+struct PersistSync
+{
+  unsigned count, gen; // arrivals at the current barrier, barrier generation
+  int      status;     // non-zero: a wait gave up; every block stops
+  int      pad;
+};
+
+// Grid-wide barrier with a bounded wait.  Thread 0 of every block arrives;
+// the last arrival opens the barrier (next generation), the others spin on
+// the generation for at most `budget` clock cycles.  A wait that gives up
+// sets sync->status and returns false, and so does every wait that sees the
+// status set: the kernel then ends early and the host reports the error.
+// The launch is cooperative, so all blocks are resident and a normal
+// barrier always opens.
+__device__ __forceinline__ bool
+grid_barrier(PersistSync * s, long long budget)
+{
+  __shared__ int go;
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    volatile unsigned * vgen = &s->gen;
+    volatile int *      vst = &s->status;
+    int                 ok = 1;
+    const unsigned      g = *vgen;
+    __threadfence();
+    if (atomicAdd(&s->count, 1u) == gridDim.x - 1)
+    {
+      atomicExch(&s->count, 0u);
+      __threadfence();
+      atomicAdd(&s->gen, 1u);
+    }
+    else
+    {
+      const long long t0 = clock64();
+      while (*vgen == g)
+      {
+        if (*vst != 0 || clock64() - t0 > budget)
+        {
+          atomicExch(&s->status, 1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    if (*vst != 0)
+      ok = 0;
+    go = ok;
+  }
+  __syncthreads();
+  return go != 0;
+}
+
+// All iterations of a run in one cooperative launch: the stages of every
+// iteration follow each other with grid-wide barriers instead of separate
+// launches; each block takes work items of the current stage in turn (the
+// same bodies, indices and arithmetic as the per-stage kernels above, so the
+// states are the same bit for bit).
+template <class R, int DIM>
+__global__ void __launch_bounds__(kPersistThreads)
+kp_run(const Grid<R> * Gs, const Buffers<R> * Bs, const PersistWork W, int nprob, int parity0,
+       int niter, PersistSync * sync, long long budget)
+{
+  __shared__ ProblemView<R> v;
+  const int64_t t = threadIdx.x;
+  for (int it = 0; it < niter; ++it)
+  {
+    const int parity = (parity0 + it) & 1;
+    for (unsigned w = blockIdx.x; w < W.n[0]; w += gridDim.x)
+    {
+      const PersistRef m = W.list[0][w];
+      load_problem(v, Gs, Bs, m.p, parity);
+      boundaries_body<R, DIM>(v.G, v.B.Uin, v.B.st, 0, m.b * (int64_t)blockDim.x + t,
+                              m.b == 0 && t == 0);
+      __syncthreads();
+    }
+    if (!grid_barrier(sync, budget))
+      return;
+    for (unsigned w = blockIdx.x; w < W.n[1]; w += gridDim.x)
+    {
+      const PersistRef m = W.list[1][w];
+      load_problem(v, Gs, Bs, m.p, parity);
+      prim_dt_body<R, DIM>(v.G, v.B.Uin, v.B.Q, v.B.st, 0, m.b * (int64_t)blockDim.x + t);
+      __syncthreads();
+    }
+    if (!grid_barrier(sync, budget))
+      return;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nprob; p += gridDim.x * blockDim.x)
+      finalize_dt_body<R>(Gs[p], Bs[p].st, 0);
+    if (!grid_barrier(sync, budget))
+      return;
+    for (unsigned w = blockIdx.x; w < W.n[2]; w += gridDim.x)
+    {
+      const PersistRef m = W.list[2][w];
+      load_problem(v, Gs, Bs, m.p, parity);
+      trace_body<R, DIM>(v.G, v.B, m.b * (int64_t)blockDim.x + t);
+      __syncthreads();
+    }
+    if (!grid_barrier(sync, budget))
+      return;
+    for (unsigned w = blockIdx.x; w < W.n[3]; w += gridDim.x)
+    {
+      const PersistRef m = W.list[3][w];
+      load_problem(v, Gs, Bs, m.p, parity);
+      flux_body<R, DIM>(v.G, v.B, m.b * (int64_t)blockDim.x + t, m.d);
+      __syncthreads();
+    }
+    if (!grid_barrier(sync, budget))
+      return;
+    for (unsigned w = blockIdx.x; w < W.n[4]; w += gridDim.x)
+    {
+      const PersistRef m = W.list[4][w];
+      load_problem(v, Gs, Bs, m.p, parity);
+      emf_body<R, DIM>(v.G, v.B, m.b * (int64_t)blockDim.x + t, m.d);
+      __syncthreads();
+    }
+    if (!grid_barrier(sync, budget))
+      return;
+    for (unsigned w = blockIdx.x; w < W.n[5]; w += gridDim.x)
+    {
+      const PersistRef m = W.list[5][w];
+      load_problem(v, Gs, Bs, m.p, parity);
+      update_body<R, DIM>(v.G, v.B, m.b * (int64_t)blockDim.x + t);
+      __syncthreads();
+    }
+    if (!grid_barrier(sync, budget))
+      return;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nprob; p += gridDim.x * blockDim.x)
+    {
+      DevState * st = Bs[p].st;
+      if (!step_finished(st))
+      {
+        st->it += 1;
+        st->t += st->dt;
+      }
+    }
+    if (!grid_barrier(sync, budget))
+      return;
+  }
+}
+
 #define MHD_ECK(call)                                                                 \
   do                                                                                  \
   {                                                                                   \
@@ -200,6 +362,14 @@ public:
   cudaStream_t            stream = nullptr;
   cudaGraphExec_t         graph_pair[2] = { nullptr, nullptr };
   int64_t                 launched = 0;
+  // persistent form: work lists of the six box stages, barrier state,
+  // cooperative grid size, wait bound, and the form run() uses
+  PersistRef *  plist[6] = {};
+  unsigned      pn[6] = {};
+  PersistSync * psync = nullptr;
+  int           pgrid = 0;
+  long long     pbudget = 1LL << 34; // about 8 s at 2 GHz per barrier wait
+  int           run_mode = MHD_ENSEMBLE_GRAPHS;
 
   ~EnsembleImpl() override
   {
@@ -207,6 +377,11 @@ public:
     for (auto & m : map)
       if (m)
         cudaFree(m);
+    for (auto & m : plist)
+      if (m)
+        cudaFree(m);
+    if (psync)
+      cudaFree(psync);
     if (dG)
       cudaFree(dG);
     if (dB)
@@ -752,17 +927,27 @@ public:
     MHD_ECK(cudaEventCreate(&e0));
     MHD_ECK(cudaEventCreate(&e1));
     MHD_ECK(cudaEventRecord(e0, stream));
-    int left = nsteps;
-    while (left >= 2)
+    if (run_mode == MHD_ENSEMBLE_PERSISTENT)
     {
-      MHD_ECK(cudaGraphLaunch(graph_pair[parity], stream));
-      left -= 2;
-    }
-    if (left)
-    {
-      enqueue_step(parity);
-      if (int rc = check_launch())
+      if (int rc = build_persist())
         return rc;
+      if (int rc = enqueue_persistent(parity, nsteps))
+        return rc;
+    }
+    else
+    {
+      int left = nsteps;
+      while (left >= 2)
+      {
+        MHD_ECK(cudaGraphLaunch(graph_pair[parity], stream));
+        left -= 2;
+      }
+      if (left)
+      {
+        enqueue_step(parity);
+        if (int rc = check_launch())
+          return rc;
+      }
     }
     MHD_ECK(cudaEventRecord(e1, stream));
     MHD_ECK(cudaEventSynchronize(e1));
@@ -772,6 +957,9 @@ public:
     cudaEventDestroy(e1);
     if (ms)
       *ms = el;
+    if (run_mode == MHD_ENSEMBLE_PERSISTENT && nsteps > 0)
+      if (int rc = persistent_status())
+        return rc;
     if (int rc = read_records())
       return rc;
     for (int p = 0; p < n; ++p)
@@ -780,6 +968,129 @@ public:
         err = "problem " + std::to_string(p) + ": non-finite or non-positive state detected";
         return MHD_ERR_NUMERIC;
       }
+    return MHD_OK;
+  }
+
+  int
+  set_mode(int m) override
+  {
+    if (m != MHD_ENSEMBLE_GRAPHS && m != MHD_ENSEMBLE_PERSISTENT)
+    {
+      err = "mode must be MHD_ENSEMBLE_GRAPHS or MHD_ENSEMBLE_PERSISTENT";
+      return MHD_ERR_INVALID_ARG;
+    }
+    if (m == MHD_ENSEMBLE_PERSISTENT)
+      if (int rc = build_persist())
+        return rc;
+    run_mode = m;
+    return MHD_OK;
+  }
+
+  int
+  mode() const override
+  {
+    return run_mode;
+  }
+
+  int
+  set_wait_limit(long long cycles) override
+  {
+    if (cycles < 0)
+    {
+      err = "wait limit must be non-negative";
+      return MHD_ERR_INVALID_ARG;
+    }
+    pbudget = cycles;
+    return MHD_OK;
+  }
+
+  // Work lists of the persistent kernel (blocks of kPersistThreads threads;
+  // the face and edge stages direction-major) and its cooperative grid:
+  // as many blocks as are resident on the device at once.
+  int
+  build_persist()
+  {
+    if (psync)
+      return MHD_OK;
+    const Kind kinds[6] = { K_BC, K_PRIM, K_TRACE, K_FLUX, K_EMF, K_UPDATE };
+    for (int q = 0; q < 6; ++q)
+    {
+      std::vector<PersistRef> h;
+      const int nd = kinds[q] == K_FLUX ? dim : (kinds[q] == K_EMF ? (dim == 3 ? 3 : 1) : 1);
+      for (int d = 0; d < nd; ++d)
+        for (int p = 0; p < n; ++p)
+        {
+          const int64_t nb = (box_count(G[p], kinds[q]) + kPersistThreads - 1) / kPersistThreads;
+          for (int64_t b = 0; b < nb; ++b)
+            h.push_back(PersistRef{ p, (int)b, d });
+        }
+      MHD_ECK(cudaMalloc(&plist[q], std::max<size_t>(1, h.size()) * sizeof(PersistRef)));
+      if (!h.empty())
+        MHD_ECK(cudaMemcpy(plist[q], h.data(), h.size() * sizeof(PersistRef),
+                           cudaMemcpyHostToDevice));
+      pn[q] = (unsigned)h.size();
+    }
+    int dev = 0, sms = 0, coop = 0, bps = 0;
+    MHD_ECK(cudaGetDevice(&dev));
+    MHD_ECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    MHD_ECK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop)
+    {
+      err = "the device does not support cooperative launches (persistent ensemble form)";
+      return MHD_ERR_CUDA;
+    }
+    MHD_ECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, persist_kernel(), kPersistThreads, 0));
+    pgrid = bps * sms;
+    if (pgrid <= 0)
+    {
+      err = "persistent ensemble kernel cannot be resident";
+      return MHD_ERR_CUDA;
+    }
+    MHD_ECK(cudaMalloc(&psync, sizeof(PersistSync)));
+    return MHD_OK;
+  }
+
+  const void *
+  persist_kernel() const
+  {
+    return dim == 2 ? (const void *)kp_run<R, 2> : (const void *)kp_run<R, 3>;
+  }
+
+  // nsteps iterations in one cooperative launch (queued on the stream)
+  int
+  enqueue_persistent(int parity, int nsteps)
+  {
+    if (nsteps <= 0)
+      return MHD_OK;
+    MHD_ECK(cudaMemsetAsync(psync, 0, sizeof(PersistSync), stream));
+    PersistWork W;
+    for (int q = 0; q < 6; ++q)
+    {
+      W.list[q] = plist[q];
+      W.n[q] = pn[q];
+    }
+    const Grid<R> *    gs = dG;
+    const Buffers<R> * bs = dB;
+    int                np = n, par = parity, ni = nsteps;
+    long long          bud = pbudget;
+    void *             args[] = { &gs, &bs, &W, &np, &par, &ni, &psync, &bud };
+    MHD_ECK(cudaLaunchCooperativeKernel(persist_kernel(), dim3(pgrid), dim3(kPersistThreads), args,
+                                        0, stream));
+    return MHD_OK;
+  }
+
+  int
+  persistent_status()
+  {
+    PersistSync h{};
+    MHD_ECK(cudaMemcpyAsync(&h, psync, sizeof h, cudaMemcpyDeviceToHost, stream));
+    MHD_ECK(cudaStreamSynchronize(stream));
+    if (h.status)
+    {
+      err = "persistent ensemble: a grid-barrier wait gave up after " + std::to_string(pbudget) +
+            " clock cycles (the states of this run are incomplete)";
+      return MHD_ERR_CUDA;
+    }
     return MHD_OK;
   }
 
@@ -834,12 +1145,96 @@ public:
       std::snprintf(line, sizeof line, "-> %s uses %d threads per block\n", kKindName[k], best_t);
       report += line;
     }
+    drop_graphs();
+    // the work split: per-stage launches replayed from graphs, or one
+    // persistent launch with grid-wide barriers; two iterations of each on a
+    // snapshot of the states (restored afterwards), the faster one is kept
+    if (int rc = tune_mode(parity, e0, e1, report))
+      return rc;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    drop_graphs();
     // the tuning launches rewrote boundary cells and primitives of the
     // current states only; restore the invariant of a fresh iteration
     MHD_ECK(cudaStreamSynchronize(stream));
+    return MHD_OK;
+  }
+
+  int
+  tune_mode(int parity, cudaEvent_t e0, cudaEvent_t e1, std::string & report)
+  {
+    if (int rc = build_graphs())
+      return rc;
+    if (int rc = build_persist())
+      return rc;
+    // snapshot: both state arrays, the FP32 low parts and the records
+    std::vector<size_t> off(n + 1, 0);
+    const int           nplanes = 8 * (sizeof(R) == 4 ? 3 : 2);
+    for (int p = 0; p < n; ++p)
+      off[p + 1] = off[p] + (size_t)G[p].sv * nplanes;
+    R * snap = nullptr;
+    MHD_ECK(cudaMalloc(&snap, off[n] * sizeof(R)));
+    DevState * st_snap = nullptr;
+    MHD_ECK(cudaMalloc(&st_snap, n * sizeof(DevState)));
+    auto save = [&](bool back) -> int {
+      for (int p = 0; p < n; ++p)
+      {
+        const size_t c = (size_t)G[p].sv * 8 * sizeof(R);
+        R *          bufs[3] = { B[p].Uin, B[p].Uout, B[p].Ulo };
+        for (int q = 0; q < nplanes / 8; ++q)
+        {
+          R * s0 = snap + off[p] + (size_t)q * 8 * G[p].sv;
+          MHD_ECK(cudaMemcpyAsync(back ? bufs[q] : s0, back ? s0 : bufs[q], c,
+                                  cudaMemcpyDeviceToDevice, stream));
+        }
+      }
+      MHD_ECK(cudaMemcpyAsync(back ? st : st_snap, back ? st_snap : st, n * sizeof(DevState),
+                              cudaMemcpyDeviceToDevice, stream));
+      return MHD_OK;
+    };
+    float t[2] = { 0.f, 0.f };
+    int   rc = save(false);
+    for (int m = 0; m < 2 && rc == MHD_OK; ++m)
+    {
+      for (int rep = 0; rep < 2 && rc == MHD_OK; ++rep) // warm, then timed
+      {
+        if ((rc = save(true)) != MHD_OK)
+          break;
+        if (cudaEventRecord(e0, stream) != cudaSuccess)
+          rc = MHD_ERR_CUDA;
+        if (m == 0)
+        {
+          if (rc == MHD_OK && cudaGraphLaunch(graph_pair[parity], stream) != cudaSuccess)
+            rc = MHD_ERR_CUDA;
+        }
+        else if (rc == MHD_OK)
+          rc = enqueue_persistent(parity, 2);
+        if (cudaEventRecord(e1, stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess)
+          rc = MHD_ERR_CUDA;
+        if (rc == MHD_OK && m == 1)
+          rc = persistent_status();
+        if (rc == MHD_OK)
+          cudaEventElapsedTime(&t[m], e0, e1);
+      }
+    }
+    if (rc == MHD_OK)
+      rc = save(true);
+    cudaStreamSynchronize(stream);
+    cudaFree(snap);
+    cudaFree(st_snap);
+    if (rc != MHD_OK)
+    {
+      if (err.empty())
+        err = "autotune of the ensemble form failed";
+      return rc;
+    }
+    char line[200];
+    std::snprintf(line, sizeof line,
+                  "form graphs: %.3f ms per iteration; persistent (%d blocks x %d threads): %.3f ms "
+                  "per iteration\n",
+                  t[0] / 2, pgrid, kPersistThreads, t[1] / 2);
+    report += line;
+    run_mode = t[1] < t[0] ? MHD_ENSEMBLE_PERSISTENT : MHD_ENSEMBLE_GRAPHS;
+    report += run_mode == MHD_ENSEMBLE_PERSISTENT ? "-> form persistent\n" : "-> form graphs\n";
     return MHD_OK;
   }
 

@@ -471,45 +471,48 @@ prim_dt_body(const Grid<R> & G, const R * __restrict__ U, R * __restrict__ Q, De
     }
   }
   // block max in the working precision (max is exact in any precision), then
-  // one FP64 atomicMax per block
-  __shared__ R red[32];
+  // one FP64 atomicMax per block; FP32 also reduces the range of the
+  // positive, finite interior total pressures (bit patterns of positive
+  // floats order like the values; max and min are order-independent, so the
+  // momentum-flux shift is deterministic), in the same block step
+  __shared__ R        red[32];
+  __shared__ unsigned rhi[32], rlo[32];
   rate = warp_max(rate);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned  phi = 0u, plo = 0x7f800000u;
+  if constexpr (sizeof(R) == 4)
+  {
+    const bool ok = ptot > 0.f && ptot < INFINITY;
+    phi = __reduce_max_sync(0xffffffffu, ok ? __float_as_uint(ptot) : 0u);
+    plo = __reduce_min_sync(0xffffffffu, ok ? __float_as_uint(ptot) : 0x7f800000u);
+  }
   if (lane == 0)
+  {
     red[wid] = rate;
+    rhi[wid] = phi;
+    rlo[wid] = plo;
+  }
   if (__syncthreads_or(bad) && threadIdx.x == 0)
     atomicOr(&st->status, STATUS_NUMERIC);
   if (wid == 0)
   {
-    rate = lane < (int)(blockDim.x >> 5) ? red[lane] : R(0);
+    const bool in = lane < (int)(blockDim.x >> 5);
+    rate = in ? red[lane] : R(0);
     rate = warp_max(rate);
-    if (lane == 0 && rate > R(0))
-      atomicMax(&st->invdt_bits, (unsigned long long)__double_as_longlong((double)rate));
-  }
-  if constexpr (sizeof(R) == 4)
-  {
-    // range of the positive, finite total pressures (max and min are
-    // order-independent, so the shift is deterministic): warp, then block
-    // reductions on the bit patterns, one atomic of each kind per block
-    __shared__ unsigned rhi[32], rlo[32];
-    const bool ok = ptot > 0.f && ptot < INFINITY;
-    unsigned   hi = __reduce_max_sync(0xffffffffu, ok ? __float_as_uint(ptot) : 0u);
-    unsigned   lo = __reduce_min_sync(0xffffffffu, ok ? __float_as_uint(ptot) : 0x7f800000u);
-    if (lane == 0)
+    // one atomic per block, and none when the running maximum (minimum),
+    // read first, already covers the block's value: most blocks then skip
+    // the atomics that all target the same word (the result is the same)
+    const unsigned long long rb = (unsigned long long)__double_as_longlong((double)rate);
+    if (lane == 0 && rate > R(0) && rb > *(volatile unsigned long long *)&st->invdt_bits)
+      atomicMax(&st->invdt_bits, rb);
+    if constexpr (sizeof(R) == 4)
     {
-      rhi[wid] = hi;
-      rlo[wid] = lo;
-    }
-    __syncthreads();
-    if (wid == 0)
-    {
-      const bool in = lane < (int)(blockDim.x >> 5);
-      hi = __reduce_max_sync(0xffffffffu, in ? rhi[lane] : 0u);
-      lo = __reduce_min_sync(0xffffffffu, in ? rlo[lane] : 0x7f800000u);
-      if (lane == 0 && hi != 0u)
-        atomicMax(&st->ptmax_bits, hi);
-      if (lane == 0 && lo != 0x7f800000u)
-        atomicMin(&st->ptmin_bits, lo);
+      phi = __reduce_max_sync(0xffffffffu, in ? rhi[lane] : 0u);
+      plo = __reduce_min_sync(0xffffffffu, in ? rlo[lane] : 0x7f800000u);
+      if (lane == 0 && phi != 0u && phi > *(volatile unsigned *)&st->ptmax_bits)
+        atomicMax(&st->ptmax_bits, phi);
+      if (lane == 0 && plo != 0x7f800000u && plo < *(volatile unsigned *)&st->ptmin_bits)
+        atomicMin(&st->ptmin_bits, plo);
     }
   }
 }

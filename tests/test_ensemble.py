@@ -267,3 +267,74 @@ def test_ensemble_512_fp32_subset_against_fp64_oracle(mhdlib, oracle):
                      oracle.interior(o.get_state()))
         assert err.max() <= TOL_FP32, (q, sizes[q], err)
         assert ens.time(q)[2] == steps
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,exact", [(64, True), (32, False)])
+def test_persistent_form_equals_graph_form(mhdlib, precision, exact):
+    """One cooperative launch for the whole run (grid-wide barriers between
+    the stages) gives the states of the per-stage graph form bit for bit (the
+    same kernel bodies), and in the FMA-free build those of independent
+    single-problem runs."""
+    fp = "exact" if exact else "fast"
+    probs = [workloads.ensemble_problem(s, precision=precision, fp_mode=fp) for s in _small_specs()]
+    a = mhdlib.MHDEnsemble.from_ini([ini for ini, _ in probs])
+    b = mhdlib.MHDEnsemble.from_ini([ini for ini, _ in probs])
+    for q, (_, U) in enumerate(probs):
+        a.set_state(q, U)
+        b.set_state(q, U)
+    b.set_mode(mhdlib.MHD_ENSEMBLE_PERSISTENT)
+    assert a.mode == mhdlib.MHD_ENSEMBLE_GRAPHS and b.mode == mhdlib.MHD_ENSEMBLE_PERSISTENT
+    a.run(7)
+    b.run(4)
+    b.run(3)  # a second launch continues where the first stopped
+    for q, (ini, U) in enumerate(probs):
+        assert np.array_equal(a.get_state(q), b.get_state(q)), q
+        assert a.time(q) == b.time(q)
+        if exact:
+            s = mhdlib.MHDSolver.from_ini(ini)
+            s.set_state(U.astype(s.real))
+            s.run(7)
+            assert np.array_equal(b.get_state(q), s.get_state()), q
+
+
+@pytest.mark.gpu
+def test_persistent_barrier_wait_limit_reports_and_recovers(mhdlib):
+    """A grid-barrier wait of the persistent form that runs out (wait limit
+    0: every wait gives up at once) stops the launch early and is reported as
+    an error; the ensemble stays usable and, with the states set again, runs
+    to the graph form's result."""
+    probs = [workloads.ensemble_problem(s, precision=32) for s in _small_specs()]
+    ref = mhdlib.MHDEnsemble.from_ini([ini for ini, _ in probs])
+    ens = mhdlib.MHDEnsemble.from_ini([ini for ini, _ in probs])
+    for q, (_, U) in enumerate(probs):
+        ref.set_state(q, U)
+        ens.set_state(q, U)
+    ref.run(3)
+    ens.set_mode(mhdlib.MHD_ENSEMBLE_PERSISTENT)
+    ens.set_wait_limit(0)
+    with pytest.raises(mhdlib.MHDError) as e:
+        ens.run(3)
+    assert e.value.code == mhdlib.MHD_ERR_CUDA and "gave up" in str(e.value)
+    ens.set_wait_limit(1 << 34)
+    for q, (_, U) in enumerate(probs):
+        ens.set_state(q, U)
+    ens.run(3)
+    for q in range(len(probs)):
+        assert np.array_equal(ens.get_state(q), ref.get_state(q)), q
+
+
+@pytest.mark.gpu
+def test_autotune_times_both_forms(mhdlib):
+    probs = [workloads.ensemble_problem(s, precision=32) for s in _small_specs()]
+    ens = mhdlib.MHDEnsemble.from_ini([ini for ini, _ in probs])
+    for q, (_, U) in enumerate(probs):
+        ens.set_state(q, U)
+    before = [ens.get_state(q) for q in range(len(probs))]
+    report = ens.autotune()
+    assert "form graphs:" in report and "persistent" in report
+    assert ens.mode in (mhdlib.MHD_ENSEMBLE_GRAPHS, mhdlib.MHD_ENSEMBLE_PERSISTENT)
+    # tuning leaves the states as they were
+    for q in range(len(probs)):
+        assert np.array_equal(mhdlib.interior(ens.get_state(q)), mhdlib.interior(before[q]))
+        assert ens.time(q)[2] == 0

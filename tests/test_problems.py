@@ -83,18 +83,10 @@ def wave_ini(nx, wave_type, tend, version=2):
         "[wave]", f"type={wave_type}", "[OTHER]", f"implementationVersion={version}"]) + "\n"
 
 
-@pytest.mark.gpu
-@pytest.mark.parametrize("wave_type,tend", [(0, "0.5"), (1, "1.0")])
-def test_linear_wave_convergence(mhdlib, wave_type, tend):
-    """One period of a linear fast / Alfven wave (the reference's
-    convergence test): the L1 error against the initial state falls with
-    every doubling of the resolution.  At N = 16, 32, 64 the scheme (bitwise
-    the reference's, see the wave fixtures) converges at orders 1.2-1.7, not
-    yet at its asymptotic second order; the test requires at least first
-    order."""
+def _wave_errors(mhdlib, wave_type, tend, version, sizes):
     errs = []
-    for nx in (16, 32, 64):
-        s = mhdlib.MHDSolver.from_ini(wave_ini(nx, wave_type, tend))
+    for nx in sizes:
+        s = mhdlib.MHDSolver.from_ini(wave_ini(nx, wave_type, tend, version=version))
         s.init_problem()
         U0 = mhdlib.interior(s.get_state())
         s.run(100000)
@@ -103,9 +95,41 @@ def test_linear_wave_convergence(mhdlib, wave_type, tend):
         U1 = mhdlib.interior(s.get_state())
         # error of the perturbed quantities (amplitude 1e-6): all conserved variables
         errs.append(np.abs(U1 - U0).mean())
-    orders = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
-    print(f"\nwave type {wave_type}: L1 errors {errs}, orders {orders}")
-    assert np.all(orders > 1.0), (errs, orders)
+        s.close()
+    return errs, np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("wave_type,tend", [(0, "0.5"), (1, "1.0")])
+def test_linear_wave_convergence_second_order(mhdlib, wave_type, tend):
+    """The reference's convergence test (test/convergence/mhd_wave_3D.ini.skel:
+    implementationVersion=0, NY = NZ = NX / 2, one period of a linear fast /
+    Alfven wave; its plot draws a second-order slope): the L1 error against
+    the initial state falls at second order.  Measured with the reference
+    itself (compiled here) at N = 16, 32, 64: orders 2.46, 1.81 (fast) and
+    2.52, 2.13 (Alfven); the library is bitwise that path (version-0 wave
+    fixtures).  The finest pair must reach order 1.8."""
+    errs, orders = _wave_errors(mhdlib, wave_type, tend, 0, (16, 32, 64, 128))
+    print(f"\nversion 0 wave type {wave_type}: L1 errors {errs}, orders {orders}")
+    assert np.all(orders > 1.5), (errs, orders)
+    assert orders[-1] >= 1.8, (errs, orders)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("wave_type,tend", [(0, "0.5"), (1, "1.0")])
+def test_linear_wave_convergence_version2_first_order(mhdlib, wave_type, tend):
+    """The same waves through implementation version 2 converge at first
+    order in 3D, in the reference as here (the library is bitwise the
+    reference on this path): its edge reconstruction takes the face-centred
+    field's z slope with the minus sample at k + 1 (compute_limited_slope,
+    MHDBaseFunctor3D.h:142), so Bx and By are piecewise constant along z on x
+    and y edges, and y / x edges add transverse slopes twice
+    (MHDRunFunctors3D.h:1490-1524).  Orders 1.50, 1.16, 1.02, 1.00 (fast) from
+    N = 16 to 256; the reference's C restatement gives the same errors.  The
+    test holds the errors to falling at first order at least."""
+    errs, orders = _wave_errors(mhdlib, wave_type, tend, 2, (16, 32, 64, 128))
+    print(f"\nversion 2 wave type {wave_type}: L1 errors {errs}, orders {orders}")
+    assert np.all(orders > 0.9), (errs, orders)
 
 
 @pytest.mark.gpu
