@@ -639,7 +639,8 @@ def run_ensemble(args):
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "kernels_per_step": ens.launches_per_step(),
                        "per_kernel_ms": prof,
-                       "autotune": [ln for ln in tune.splitlines() if ln.startswith("->")]},
+                       "autotune": [ln for ln in tune.splitlines()
+                                    if ln.startswith("->") or ln.startswith("form")]},
             "e2e": {"value": e2e_value, "unit": "cell-updates/s",
                     "h2d_bytes_per_step": state_bytes / e2e_steps,
                     "d2h_bytes_per_step": state_bytes / e2e_steps, "steps": e2e_steps,

