@@ -230,15 +230,29 @@ rn_mul(float a, float b)
 }
 
 // Selection by comparison.  GB300 runs FP64 comparisons on the narrow FP64
-// pipe; the fast FP64 build compares the bit patterns as integers instead
-// (key(x) = bits ^ ((bits >> 63) & 0x7fff...) orders like the values for
-// non-NaN doubles, with -0 below +0), which runs on the integer pipes.  The
-// exact build keeps the reference's FP comparisons (mhd_utils.h:36-77).
+// pipe; the FP64 builds compare the bit patterns as integers instead, on the
+// integer pipes.  The fast build's key(x) = bits ^ ((bits >> 63) & 0x7fff...)
+// orders like the values for non-NaN doubles, with -0 below +0.  The exact
+// build must select exactly what the reference's FP comparison selects
+// (mhd_utils.h:36-77) for every input, so its key is the signed magnitude
+// (-0 and +0 equal) and a NaN operand makes the comparison false, as the FP
+// comparison is.
 __device__ __forceinline__ long long
 order_key(double x)
 {
   const long long b = __double_as_longlong(x);
   return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+// (a > r) and (a < r) of IEEE doubles, bit for bit, on integer operations
+__device__ __forceinline__ bool
+exact_gt(double a, double r)
+{
+  const long long ba = __double_as_longlong(a), br = __double_as_longlong(r);
+  const long long ma = ba & 0x7fffffffffffffffLL, mr = br & 0x7fffffffffffffffLL;
+  const long long inf = 0x7ff0000000000000LL;
+  if (ma > inf || mr > inf)
+    return false; // a NaN operand
+  return (ba < 0 ? -ma : ma) > (br < 0 ? -mr : mr);
 }
 template <class R>
 __device__ __forceinline__ R
@@ -246,6 +260,8 @@ sel_max(R r, R a)
 {
   if constexpr (sizeof(R) == 8 && !kExactOrder)
     return order_key(a) > order_key(r) ? a : r;
+  else if constexpr (sizeof(R) == 8)
+    return exact_gt(a, r) ? a : r;
   else
     return (a > r) ? a : r;
 }
@@ -255,6 +271,8 @@ sel_min(R r, R a)
 {
   if constexpr (sizeof(R) == 8 && !kExactOrder)
     return order_key(a) < order_key(r) ? a : r;
+  else if constexpr (sizeof(R) == 8)
+    return exact_gt(r, a) ? a : r;
   else
     return (a < r) ? a : r;
 }

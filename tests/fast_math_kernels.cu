@@ -8,6 +8,8 @@
 // back to.  One thread per element, every access in bounds.  Prints
 //   <name> max_ulp <m> correctly_rounded <fraction>      (normal arguments)
 //   special_<name> mismatches <count> of <n>             (fallback arguments)
+//   special_gt mismatches <count> of <n>                 (exact build's integer
+//                                                         comparison, all pairs)
 // and exits non-zero on a CUDA error.
 //
 // Build and run (GB300):
@@ -82,6 +84,18 @@ apply(int op, const double * dx, double * dy, int n)
   case OP_SQRT: return launch<OP_SQRT>(dx, dy, n);
   default: return launch<OP_RSQ>(dx, dy, n);
   }
+}
+
+// exact build's integer comparison against the FP comparison, all pairs
+__global__ void
+k_gt(const double * __restrict__ v, int n, unsigned * __restrict__ bad)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * n)
+    return;
+  const double a = v[i / n], b = v[i % n];
+  if (mhd::exact_gt(a, b) != (a > b))
+    atomicAdd(bad, 1u);
 }
 
 static bool
@@ -185,6 +199,20 @@ main()
         bad += !same_bits(hy[i], hz[i]);
     }
     std::printf("special_%s mismatches %d of %d\n", names[pr[0]], bad, ns);
+  }
+  // the exact build's integer comparison on every pair of the special values
+  {
+    unsigned * dbad = nullptr;
+    if (cudaMalloc(&dbad, sizeof(unsigned)) != cudaSuccess)
+      return 1;
+    cudaMemset(dbad, 0, sizeof(unsigned));
+    k_gt<<<(ns * ns + 255) / 256, 256>>>(dx, ns, dbad);
+    unsigned hb = 0;
+    if (cudaDeviceSynchronize() != cudaSuccess)
+      return 1;
+    cudaMemcpy(&hb, dbad, sizeof hb, cudaMemcpyDeviceToHost);
+    std::printf("special_gt mismatches %u of %d\n", hb, ns * ns);
+    cudaFree(dbad);
   }
   cudaFree(dx);
   cudaFree(dy);

@@ -9,7 +9,9 @@ tests/fast_math_kernels.cu against that header and checks their error bounds
 on 2^20 log-uniform arguments over [1e-30, 1e30] against correctly rounded
 host references, and that the arguments outside the fast ranges (zeros,
 subnormals, |x| >= 2^1021, infinities, NaN, negative square-root arguments)
-get exactly the library function's result.
+get exactly the library function's result; and that the exact build's
+integer comparison (exact_gt) answers as the FP comparison on every pair of
+those special values.
 """
 import os
 import shutil
@@ -34,7 +36,7 @@ def test_fast_fp64_reciprocal_and_sqrt_error_bounds(tmp_path):
             special[f[0][8:]] = (int(f[2]), int(f[4]))
         else:
             res[f[0]] = (float(f[2]), float(f[4]))
-    assert set(special) == {"rcp", "fsqrt"}, out
+    assert set(special) == {"rcp", "fsqrt", "gt"}, out
     for name, (bad, total) in special.items():
         assert total > 900 and bad == 0, (name, bad, total)
     # library references: correctly rounded (rsqrt within its documented bound)
