@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define MHD_ABI_VERSION 1
+#define MHD_ABI_VERSION 2
 
 /* status codes */
 #define MHD_OK 0
@@ -39,10 +39,18 @@ extern "C" {
 #define MHD_ERR_TOO_LARGE -6    /* request larger than a fixed limit */
 #define MHD_FINISHED 1          /* mhd_step_noalloc: t >= tEnd, nothing was computed */
 
-/* enums.h:94-101 (RiemannSolverType); only the MHD solvers are accepted */
+/* enums.h:136-143 (RiemannSolverType).  The MHD solver takes LLF, HLL and
+ * HLLD; the hydro solver takes APPROX, LLF, HLLC and, in 2D, HLL (the
+ * reference's 3D hydro dispatch has no HLL branch, RiemannSolvers.h:608-633) */
+#define MHD_RIEMANN_APPROX 0
 #define MHD_RIEMANN_LLF 1
 #define MHD_RIEMANN_HLL 2
+#define MHD_RIEMANN_HLLC 3
 #define MHD_RIEMANN_HLLD 4
+
+/* mhd_params::solver: [run] solver_name MHD_Muscl_2D/3D or Hydro_Muscl_2D/3D */
+#define MHD_SOLVER_MHD_MUSCL 0
+#define MHD_SOLVER_HYDRO_MUSCL 1
 
 /* enums.h:105-112 (BoundaryConditionType) */
 #define MHD_BC_REFLECTING 1 /* BC_DIRICHLET */
@@ -80,6 +88,14 @@ extern "C" {
 #define MHD_PROBLEM_WAVE 6             /* real: amplitude, V0, rev[7], d0, p0, sin_a2, cos_a2,
                                           sin_a3, cos_a3, dby, dbz, bx0, by0, bz0, k_par
                                           (WaveParams.h); int: type */
+/* hydro solver problems (SolverHydroMuscl.cpp:110-250; blast, implode and
+ * kelvin_helmholtz take the layouts above; unknown names give implode) */
+#define MHD_PROBLEM_GRESHO_VORTEX 7     /* real: rho0, Ma */
+#define MHD_PROBLEM_FOUR_QUADRANT 8     /* real: x, y; int: config_number (2D) */
+#define MHD_PROBLEM_ISENTROPIC_VORTEX 9 /* real: rho_a, T_a, u_a, v_a, center_x, center_y,
+                                           strength (2D) */
+#define MHD_PROBLEM_RAYLEIGH_TAYLOR 10  /* real: amplitude, d0, d1, gx, gy, gz */
+#define MHD_PROBLEM_RISING_BUBBLE 11    /* real: R, x0, y0, z0, din, dout, gx, gy, gz */
 
 /*
  * Run/mesh/scheme parameters.  Mirrors the fields of HydroParams /
@@ -107,12 +123,19 @@ typedef struct mhd_params
   int    device;     /* CUDA device ordinal the context binds (default 0) */
   double problem_real[24]; /* per-problem parameters, see MHD_PROBLEM_* */
   int    problem_int[4];
+  int    solver;     /* MHD_SOLVER_MHD_MUSCL (default) or MHD_SOLVER_HYDRO_MUSCL */
+  int    gravity;    /* hydro solver: [gravity] static (SolverBase.cpp:138-141) */
+  double gravity_field[3]; /* hydro solver: the uniform static field the problem's
+                              initialisation sets (zero for problems that set none) */
 } mhd_params;
 
 typedef struct mhd_ctx mhd_ctx;
 
 /* Fill defaults: HydroParams()/HydroSettings() constructors (HydroParams.h:41-58,
- * :156-204), with the MHD solver's 3 ghost cells. */
+ * :156-204), with the MHD solver's 3 ghost cells.  The hydro-only solver
+ * (solver = MHD_SOLVER_HYDRO_MUSCL, SolverHydroMuscl<dim>) uses 2 ghost cells
+ * and state arrays of dim + 2 variables (rho, E, rho u, rho v[, rho w]);
+ * every entry point below serves both solvers unless it says otherwise. */
 int mhd_params_default(mhd_params *p);
 
 /* Parse .ini text with the reference's rules: INIReader (lower-cased

@@ -18,6 +18,7 @@ OUT="$HERE/_ref"
 mkdir -p "$OUT"
 SRCS=(
   "$HERE/ref_harness.cpp"
+  "$HERE/ref_harness_hydro.cpp"
   "$REF/src/shared/HydroParams.cpp"
   "$REF/src/utils/config/ConfigMap.cpp"
   "$REF/src/utils/config/inih/INIReader.cpp"

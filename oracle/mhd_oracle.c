@@ -41,172 +41,8 @@ enum { ID = 0, IP = 1, IU = 2, IV = 3, IW = 4, IA = 5, IB = 6, IC = 7 };
 enum { STG_OTHER = 0, STG_PRIM, STG_DT, STG_SLOPES, STG_HALF, STG_EFIELD, STG_FACEB, STG_FLUX,
        STG_EMF, STG_UPDATE, STG_COUNT };
 
-/* ====================================================================== */
-/* INI parsing: inih ini.cpp:100-190 + INIReader.cpp:40-117 + ConfigMap.cpp:38-82 */
-/* ====================================================================== */
-
-typedef struct
-{
-  char key[128];
-  char val[256];
-} ini_kv;
-
-typedef struct
-{
-  ini_kv *kv;
-  int     n, cap;
-} ini_map;
-
-static void
-ini_set(ini_map *m, const char *section, const char *name, const char *value)
-{
-  char key[128];
-  snprintf(key, sizeof key, "%s.%s", section, name);
-  for (char *c = key; *c; ++c)
-    *c = (char)tolower((unsigned char)*c); /* INIReader.cpp:100-105 */
-  for (int q = 0; q < m->n; ++q)
-    if (!strcmp(m->kv[q].key, key))
-    {
-      snprintf(m->kv[q].val, sizeof m->kv[q].val, "%s", value);
-      return;
-    }
-  if (m->n == m->cap)
-  {
-    m->cap = m->cap ? 2 * m->cap : 32;
-    m->kv = (ini_kv *)realloc(m->kv, (size_t)m->cap * sizeof(ini_kv));
-  }
-  snprintf(m->kv[m->n].key, sizeof m->kv[m->n].key, "%s", key);
-  snprintf(m->kv[m->n].val, sizeof m->kv[m->n].val, "%s", value);
-  m->n++;
-}
-
-static const char *
-ini_get(const ini_map *m, const char *section, const char *name)
-{
-  char key[128];
-  snprintf(key, sizeof key, "%s.%s", section, name);
-  for (char *c = key; *c; ++c)
-    *c = (char)tolower((unsigned char)*c);
-  for (int q = 0; q < m->n; ++q)
-    if (!strcmp(m->kv[q].key, key))
-      return m->kv[q].val;
-  return NULL;
-}
-
-static char *
-str_rstrip(char *s)
-{
-  char *p = s + strlen(s);
-  while (p > s && isspace((unsigned char)p[-1]))
-    *--p = '\0';
-  return s;
-}
-
-static char *
-str_lskip(char *s)
-{
-  while (*s && isspace((unsigned char)*s))
-    s++;
-  return s;
-}
-
-/* first occurrence of c, or of a ';' that follows whitespace (inline comment) */
-static char *
-find_char_or_comment(char *s, char c)
-{
-  int ws = 0;
-  while (*s && *s != c && !(ws && *s == ';'))
-  {
-    ws = isspace((unsigned char)*s);
-    s++;
-  }
-  return s;
-}
-
-static void
-ini_parse_text(ini_map *m, const char *text)
-{
-  char        section[64] = "";
-  char        prev_name[64] = "";
-  const char *p = text;
-  while (*p)
-  {
-    char        line[512];
-    const char *nl = strchr(p, '\n');
-    size_t      len = nl ? (size_t)(nl - p) : strlen(p);
-    if (len >= sizeof line)
-      len = sizeof line - 1;
-    memcpy(line, p, len);
-    line[len] = '\0';
-    p = nl ? nl + 1 : p + strlen(p);
-
-    char *start = str_lskip(str_rstrip(line));
-    if (*prev_name && *start && start > line)
-    {
-      ini_set(m, section, prev_name, start); /* continuation line */
-    }
-    else if (*start == ';' || *start == '#')
-    {
-    }
-    else if (*start == '[')
-    {
-      char *end = find_char_or_comment(start + 1, ']');
-      if (*end == ']')
-      {
-        *end = '\0';
-        snprintf(section, sizeof section, "%s", start + 1);
-        prev_name[0] = '\0';
-      }
-    }
-    else if (*start)
-    {
-      char *end = find_char_or_comment(start, '=');
-      if (*end == '=')
-      {
-        *end = '\0';
-        char *name = str_rstrip(start);
-        char *value = str_lskip(end + 1);
-        end = find_char_or_comment(value, '\0');
-        if (*end == ';')
-          *end = '\0';
-        str_rstrip(value);
-        snprintf(prev_name, sizeof prev_name, "%s", name);
-        ini_set(m, section, name, value);
-      }
-    }
-  }
-}
-
-/* ConfigMap::getFloat: strtof, default value itself passed as float */
-static double
-ini_float(const ini_map *m, const char *s, const char *n, float def)
-{
-  const char *v = ini_get(m, s, n);
-  if (!v)
-    return (double)def;
-  char *end;
-  float f = strtof(v, &end);
-  return end > v ? (double)f : (double)def;
-}
-
-/* INIReader::getInteger: strtol base 0 */
-static long
-ini_int(const ini_map *m, const char *s, const char *n, long def)
-{
-  const char *v = ini_get(m, s, n);
-  if (!v)
-    return def;
-  char *end;
-  long  x = strtol(v, &end, 0);
-  return end > v ? x : def;
-}
-
-static const char *
-ini_str(const ini_map *m, const char *s, const char *n, const char *def)
-{
-  const char *v = ini_get(m, s, n);
-  return v ? v : def;
-}
+/* INI parsing with the reference's rules (inih + INIReader + ConfigMap) */
+#include "ini_text.h"
 
 /* HydroParams::setup (HydroParams.cpp:27-217) + init (:420-453) */
 int

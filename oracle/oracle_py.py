@@ -171,6 +171,106 @@ def compute_emf(p: OrcParams, emf_dir: int, q_edge) -> float:
     return float(lib().orc_compute_emf(ctypes.byref(p), int(emf_dir), _ptr(q)))
 
 
+# ---------------------------------------------------------------- hydro solver
+
+class HorcParams(ctypes.Structure):
+    """Mirror of ``horc_params`` in hydro_oracle.h."""
+
+    _fields_ = [
+        ("dim", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+        ("ghost", ctypes.c_int), ("nvar", ctypes.c_int),
+        ("isize", ctypes.c_int), ("jsize", ctypes.c_int), ("ksize", ctypes.c_int),
+        ("xmin", ctypes.c_double), ("xmax", ctypes.c_double), ("ymin", ctypes.c_double),
+        ("ymax", ctypes.c_double), ("zmin", ctypes.c_double), ("zmax", ctypes.c_double),
+        ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
+        ("gamma0", ctypes.c_double), ("gamma6", ctypes.c_double), ("cfl", ctypes.c_double),
+        ("slope_type", ctypes.c_double), ("smallr", ctypes.c_double), ("smallc", ctypes.c_double),
+        ("smallp", ctypes.c_double), ("smallpp", ctypes.c_double),
+        ("riemann", ctypes.c_int), ("version", ctypes.c_int), ("bc", ctypes.c_int * 6),
+        ("tEnd", ctypes.c_double), ("tCurrent", ctypes.c_double), ("nStepmax", ctypes.c_int),
+        ("gravity", ctypes.c_int), ("grav", ctypes.c_double * 3),
+    ]
+
+
+_hlib = None
+
+
+def hlib():
+    global _hlib
+    if _hlib is None:
+        L = lib()
+        L.horc_params_from_ini.argtypes = [ctypes.c_char_p, ctypes.POINTER(HorcParams)]
+        L.horc_params_from_ini.restype = ctypes.c_int
+        L.horc_nelem.argtypes = [ctypes.POINTER(HorcParams)]
+        L.horc_nelem.restype = ctypes.c_int64
+        L.horc_create.argtypes = [ctypes.POINTER(HorcParams), ctypes.c_int]
+        L.horc_create.restype = ctypes.c_void_p
+        L.horc_destroy.argtypes = [ctypes.c_void_p]
+        L.horc_set_state.argtypes = [ctypes.c_void_p, _dp]
+        L.horc_get_state.argtypes = [ctypes.c_void_p, _dp]
+        L.horc_run.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.horc_run.restype = ctypes.c_int
+        L.horc_time.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.POINTER(ctypes.c_int)]
+        L.horc_riemann.argtypes = [ctypes.POINTER(HorcParams), _dp, _dp, _dp]
+        _hlib = L
+    return _hlib
+
+
+def hydro_params_from_ini(ini_text: str) -> HorcParams:
+    p = HorcParams()
+    if hlib().horc_params_from_ini(ini_text.encode(), ctypes.byref(p)) != 0:
+        raise ValueError("hydro oracle: unsupported .ini (solver, version 2, 3D hll or point gravity)")
+    return p
+
+
+def hydro_state_shape(p: HorcParams):
+    if p.dim == 2:
+        return (p.nvar, p.jsize, p.isize)
+    return (p.nvar, p.ksize, p.jsize, p.isize)
+
+
+class HydroOracleSolver:
+    """The C restatement of SolverHydroMuscl driven like the reference."""
+
+    def __init__(self, ini_text: str, nthreads: int = 1):
+        self.p = hydro_params_from_ini(ini_text)
+        self.h = hlib().horc_create(ctypes.byref(self.p), int(nthreads))
+
+    def close(self):
+        if self.h:
+            hlib().horc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_state(self, U: np.ndarray):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        assert U.shape == hydro_state_shape(self.p)
+        hlib().horc_set_state(self.h, _ptr(U))
+
+    def get_state(self) -> np.ndarray:
+        U = np.empty(hydro_state_shape(self.p), dtype=np.float64)
+        hlib().horc_get_state(self.h, _ptr(U))
+        return U
+
+    def run(self, n: int) -> int:
+        return hlib().horc_run(self.h, int(n))
+
+    def time(self):
+        t, dt, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        hlib().horc_time(self.h, ctypes.byref(t), ctypes.byref(dt), ctypes.byref(it))
+        return t.value, dt.value, it.value
+
+
+def hydro_riemann(p: HorcParams, qL, qR) -> np.ndarray:
+    l = np.ascontiguousarray(qL, dtype=np.float64)
+    r = np.ascontiguousarray(qR, dtype=np.float64)
+    f = np.zeros(p.nvar)
+    hlib().horc_riemann(ctypes.byref(p), _ptr(l), _ptr(r), _ptr(f))
+    return f
+
+
 # ---------------------------------------------------------------- flux surrogate
 
 MLP_NPARAM = 7832
@@ -310,6 +410,7 @@ def ref_probe_lib(bits: int = 64):
     L.ref_compute_emf.argtypes = [ctypes.c_char_p, ctypes.c_int, rp]
     L.ref_compute_emf.restype = real
     L.ref_params.argtypes = [ctypes.c_char_p, _dp]
+    L.ref_hydro_riemann.argtypes = [ctypes.c_char_p, rp, rp, rp]
     return L
 
 

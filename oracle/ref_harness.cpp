@@ -34,6 +34,8 @@
 #include "utils/config/ConfigMap.h"
 #include "utils/io/IO_VTK.h"
 
+#include "ref_harness_base.h"
+
 using namespace ppkMHD;
 using namespace ppkMHD::muscl;
 
@@ -83,54 +85,6 @@ init_problem_3d(ConfigMap & cfg, HydroParams & params, DA U)
   else
     InitOrszagTangFunctor3D::apply(params, OrszagTangParams(cfg), U);
 }
-
-struct RefBase
-{
-  ConfigMap   cfg;
-  HydroParams params;
-  double      m_t = 0, m_dt = 0, m_tEnd = 0;
-  int         m_iteration = 0;
-  RefBase(char *& buf, int n)
-    : cfg(buf, n)
-  {
-    params.setup(cfg);
-    m_tEnd = cfg.getFloat("run", "tEnd", 0.0);
-    m_t = cfg.getFloat("run", "tCurrent", 0.0);
-  }
-  virtual ~RefBase() {}
-  virtual void
-  step() = 0;
-  virtual void
-  set_state(const real_t * u) = 0;
-  virtual void
-  get_state(real_t * u) const = 0;
-  virtual size_t
-  nelem() const = 0;
-  virtual double
-  compute_dt_local() = 0;
-  // SolverBase.cpp:148-179
-  void
-  compute_dt()
-  {
-    m_dt = compute_dt_local();
-    if (m_t + m_dt > m_tEnd)
-      m_dt = m_tEnd - m_t;
-  }
-  // SolverBase.cpp:195-201
-  int
-  finished() const
-  {
-    return m_t >= (m_tEnd - 1e-14) || m_iteration >= params.nStepmax;
-  }
-  // SolverBase.cpp:205-220
-  void
-  next_iteration()
-  {
-    step();
-    ++m_iteration;
-    m_t += m_dt;
-  }
-};
 
 struct Ref2D : RefBase
 {
@@ -506,6 +460,8 @@ extern "C"
       return new Ref2D(buf, (int)s.size());
     if (solver == "MHD_Muscl_3D")
       return new Ref3D(buf, (int)s.size());
+    if (solver == "Hydro_Muscl_2D" || solver == "Hydro_Muscl_3D")
+      return ref_hydro_new(buf, (int)s.size(), solver == "Hydro_Muscl_3D");
     return nullptr;
   }
 
@@ -543,6 +499,8 @@ extern "C"
         std::memcpy(out, U.data(), U.size() * sizeof(real_t));
       return (long)U.size();
     }
+    if (solver == "Hydro_Muscl_2D" || solver == "Hydro_Muscl_3D")
+      return ref_hydro_initial_state(ini_text, out);
     return 0;
   }
 

@@ -34,7 +34,8 @@ MHD_ERR_TOO_LARGE = -6
 MHD_FINISHED = 1  # mhd_step_noalloc: t >= tEnd, nothing computed
 MHD_ENSEMBLE_GRAPHS, MHD_ENSEMBLE_PERSISTENT = 0, 1
 
-MHD_RIEMANN_LLF, MHD_RIEMANN_HLL, MHD_RIEMANN_HLLD = 1, 2, 4
+MHD_RIEMANN_APPROX, MHD_RIEMANN_LLF, MHD_RIEMANN_HLL, MHD_RIEMANN_HLLC, MHD_RIEMANN_HLLD = range(5)
+MHD_SOLVER_MHD_MUSCL, MHD_SOLVER_HYDRO_MUSCL = 0, 1
 MHD_BC_REFLECTING, MHD_BC_OUTFLOW, MHD_BC_PERIODIC = 1, 2, 3
 MHD_FP64, MHD_FP32 = 64, 32
 MHD_FP_FAST, MHD_FP_EXACT = 0, 1
@@ -42,6 +43,9 @@ MHD_LAYOUT_LEFT, MHD_LAYOUT_RIGHT = 0, 1
 MHD_PROBLEM_ORSZAG_TANG = 0
 (MHD_PROBLEM_BLAST, MHD_PROBLEM_IMPLODE, MHD_PROBLEM_KELVIN_HELMHOLTZ, MHD_PROBLEM_ROTOR,
  MHD_PROBLEM_FIELD_LOOP, MHD_PROBLEM_WAVE) = range(1, 7)
+# hydro solver problems
+(MHD_PROBLEM_GRESHO_VORTEX, MHD_PROBLEM_FOUR_QUADRANT, MHD_PROBLEM_ISENTROPIC_VORTEX,
+ MHD_PROBLEM_RAYLEIGH_TAYLOR, MHD_PROBLEM_RISING_BUBBLE) = range(7, 12)
 MHD_MLP_PARAMS = 7832
 MHD_MLP_FEATURES = 40
 MHD_SAMPLE_FLOATS = 24
@@ -65,11 +69,18 @@ class MHDParams(ctypes.Structure):
         ("problem", ctypes.c_int), ("ot_kt", ctypes.c_double),
         ("precision", ctypes.c_int), ("fp_mode", ctypes.c_int), ("device", ctypes.c_int),
         ("problem_real", ctypes.c_double * 24), ("problem_int", ctypes.c_int * 4),
+        ("solver", ctypes.c_int), ("gravity", ctypes.c_int),
+        ("gravity_field", ctypes.c_double * 3),
     ]
+
+    @property
+    def nvar(self) -> int:
+        """Variables of the state arrays: 8 (MHD) or dim + 2 (hydro)."""
+        return self.dim + 2 if self.solver == MHD_SOLVER_HYDRO_MUSCL else 8
 
     def as_dict(self):
         d = {f: getattr(self, f) for f, _ in self._fields_}
-        for f in ("boundary", "problem_real", "problem_int"):
+        for f in ("boundary", "problem_real", "problem_int", "gravity_field"):
             d[f] = list(getattr(self, f))
         return d
 
@@ -188,9 +199,9 @@ def params_from_ini(ini_text: str) -> MHDParams:
 def initial_state(params: MHDParams) -> np.ndarray:
     """The initial condition of params.problem (host FP64, LayoutLeft, ghosts
     included, before any boundary fill)."""
-    g = params.ghost
-    shape = (8, params.ny + 2 * g, params.nx + 2 * g) if params.dim == 2 else \
-        (8, params.nz + 2 * g, params.ny + 2 * g, params.nx + 2 * g)
+    g, nv = params.ghost, params.nvar
+    shape = (nv, params.ny + 2 * g, params.nx + 2 * g) if params.dim == 2 else \
+        (nv, params.nz + 2 * g, params.ny + 2 * g, params.nx + 2 * g)
     U = np.empty(shape, dtype=np.float64)
     rc = lib().mhd_initial_state(ctypes.byref(params), U.ctypes.data)
     if rc != MHD_OK:
@@ -217,7 +228,9 @@ def default_params() -> MHDParams:
 
 
 class MHDSolver:
-    """One MHD problem on the GPU (an ``mhd_ctx``)."""
+    """One problem on the GPU (an ``mhd_ctx``): the MHD MUSCL solver, or the
+    hydro-only MUSCL solver when ``params.solver`` is MHD_SOLVER_HYDRO_MUSCL
+    ([run] solver_name Hydro_Muscl_2D/3D)."""
 
     def __init__(self, params: MHDParams):
         self.params = params
@@ -268,14 +281,14 @@ class MHDSolver:
     @property
     def shape_left(self):
         if self.params.dim == 2:
-            return (8, self.jsize, self.isize)
-        return (8, self.ksize, self.jsize, self.isize)
+            return (self.nbvar, self.jsize, self.isize)
+        return (self.nbvar, self.ksize, self.jsize, self.isize)
 
     @property
     def shape_right(self):
         if self.params.dim == 2:
-            return (self.isize, self.jsize, 8)
-        return (self.isize, self.jsize, self.ksize, 8)
+            return (self.isize, self.jsize, self.nbvar)
+        return (self.isize, self.jsize, self.ksize, self.nbvar)
 
     def init_problem(self):
         self._check(lib().mhd_init_problem(self.h))

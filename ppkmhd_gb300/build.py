@@ -1,7 +1,7 @@
 """Build the in-tree CUDA library ``ppkmhd_gb300/lib/libppkmhd_gb300.so``.
 
 nvcc compiles for sm_103a only (``-gencode arch=compute_103a,code=sm_103a``),
-one translation unit per arithmetic variant plus the host layer, in
+one translation unit per arithmetic variant and solver plus the host layer, in
 parallel; g++ links.  No CMake, no torch extension machinery: the library
 exposes the plain C ABI of include/ppkmhd_gb300.h.
 
@@ -94,6 +94,13 @@ def build(jobs: int | None = None, force: bool = False, verbose: bool = False) -
                      f"-DMHD_VARIANT_TAG={tag}", f"-DMHD_REAL={real}", f"-DMHD_FACTORY={factory}",
                      f"-DMHD_EXACT_BUILD={1 if fmad == 'false' else 0}",
                      "-c", os.path.join(CSRC, "mhd_variant.cu"), "-o", o])
+        o = os.path.join(OBJ, f"hydro_{tag}.o")
+        objs.append(o)
+        cmds.append([nvcc(), *GENCODE, *NVCC_COMMON, f"--fmad={fmad}", "-Xptxas", "-v",
+                     f"-DMHD_VARIANT_TAG={tag}", f"-DMHD_REAL={real}",
+                     f"-DMHD_HYDRO_FACTORY={factory.replace('create_core', 'create_hydro_core')}",
+                     f"-DMHD_EXACT_BUILD={1 if fmad == 'false' else 0}",
+                     "-c", os.path.join(CSRC, "hydro_variant.cu"), "-o", o])
         o = os.path.join(OBJ, f"mhd_ensemble_{tag}.o")
         objs.append(o)
         cmds.append([nvcc(), *GENCODE, *NVCC_COMMON, f"--fmad={fmad}", "-Xptxas", "-v",
@@ -109,7 +116,7 @@ def build(jobs: int | None = None, force: bool = False, verbose: bool = False) -
     objs.append(o)
     cmds.append([nvcc(), *GENCODE, *NVCC_COMMON, "--fmad=true", "-Xptxas", "-v",
                  "-c", os.path.join(CSRC, "mhd_noalloc.cu"), "-o", o])
-    for src in ("mhd_capi.cpp", "mhd_init.cpp"):
+    for src in ("mhd_capi.cpp", "mhd_init.cpp", "hydro_init.cpp"):
         o = os.path.join(OBJ, src.replace(".cpp", ".o"))
         objs.append(o)
         cmds.append(["g++", *CXX_COMMON, "-c", os.path.join(CSRC, src), "-o", o])

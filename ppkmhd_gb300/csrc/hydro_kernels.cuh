@@ -1,0 +1,974 @@
+// Kernels of one iteration of the hydro-only MUSCL-Hancock solver
+// (ppkMHD's SolverHydroMuscl<dim>, solver names Hydro_Muscl_2D/3D),
+// templated on the real type R and the dimension DIM (NVAR = DIM + 2
+// conservative variables: rho, E, rho u, rho v[, rho w]; ghost width 2).
+//
+// One iteration is 7 launches on one stream, every face flux computed once
+// by one thread and every cell updated by the thread that owns it (gather
+// form, no atomics except the CFL maximum, bitwise deterministic):
+//
+//   k_hbound     ghost fill of U_in (periodic / reflecting / outflow)
+//   k_hprim_dt   primitives Q over the whole array + CFL max-reduction
+//   k_hfinalize  dt = cfl / max, clipped to tEnd; dt/dx, dt/dy, dt/dz
+//   k_hslopes    limited slopes S_d of every cell the faces read
+//   k_hflux      per face: both traced states, gravity predictor, Riemann
+//                solver (approx / LLF / HLL / HLLC), flux * dt/dx stored
+//   k_hupdate    U_out = U_in + flux differences (interior), gravity source
+//                term; ghost cells copied (the reference's deep_copy)
+//   k_advance    iteration += 1, t += dt
+//
+// Implementation versions 0 (ComputeAndStoreFluxes + Update) and 1 (stored
+// slopes, per-direction trace/flux/update) compute the same face fluxes from
+// the same slopes and apply the same additions in the same order, so both
+// run these kernels; their one difference (version 1 in 3D gives the right
+// state of z faces no gravity predictor) is a flag of k_hflux.
+//
+// Device layout: SoA planes, i fastest, ghost cells included:
+//   U[i + isize*(j + jsize*(k + ksize*var))]   (Kokkos LayoutLeft)
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mhd_kernels.cuh"
+
+namespace mhd
+{
+inline namespace MHD_VARIANT_TAG
+{
+namespace hydro
+{
+
+constexpr int MAXV = 5;
+
+template <class R>
+struct HGrid
+{
+  int     dim, nx, ny, nz, g, nvar;
+  int     isize, jsize, ksize;
+  int64_t sj, sk, sv;
+  int     bc[6];
+  int     riemann;   // MHD_RIEMANN_APPROX / LLF / HLL / HLLC
+  int     gravity;   // [gravity] static
+  int     zgrav_right; // 0: version 1 in 3D (no predictor on the right state of z faces)
+  R       gamma0, gamma6, smallr, smallc, smallp, smallpp, slope_type, entho;
+  R       grav[3];   // uniform static gravity field
+  double  cfl, dx, dy, dz, dxg; // dxg = min(dx, dy[, dz]) (ComputeDtGravityFunctor)
+  double  idx, idy, idz, idxg;  // host IEEE reciprocals
+  Box     box[BOX_COUNT];
+};
+
+template <class R>
+__device__ __forceinline__ int64_t
+hcell(const HGrid<R> & G, int i, int j, int k)
+{
+  return (int64_t)i + (int64_t)j * G.sj + (int64_t)k * G.sk;
+}
+
+// Quotient of the builds: the FMA-free FP64 build divides as the reference
+// does (IEEE); the fast builds multiply by the approximate reciprocal (FP64:
+// rcp with one third-order refinement, within 0.51 ulp; FP32: rcp.approx).
+template <class R>
+__device__ __forceinline__ R
+hdiv(R a, R b)
+{
+  if constexpr (kExactOrder)
+    return a / b;
+  else
+    return a * rcp(b);
+}
+template <class R>
+__device__ __forceinline__ R
+hsqrt(R x)
+{
+  if constexpr (kExactOrder)
+    return sqrt(x);
+  else
+    return fsqrt(x);
+}
+
+// ---------------------------------------------------------------- point-wise physics
+
+// computePrimitives (HydroBaseFunctor2D.h:82-112, HydroBaseFunctor3D.h:79-117):
+// q = (rho, p, u, v[, w]) and the sound speed c
+template <class R, int DIM>
+__device__ __forceinline__ void
+hprim(const HGrid<R> & G, const R * u, R & c, R * q)
+{
+  const R d = fmax(u[ID], G.smallr);
+  R       ux, uy, uz = R(0), eken, e;
+  if constexpr (kExactOrder)
+  {
+    ux = u[IU] / d;
+    uy = u[IV] / d;
+    if constexpr (DIM == 3)
+    {
+      uz = u[IW] / d;
+      eken = R(0.5) * (ux * ux + uy * uy + uz * uz);
+    }
+    else
+      eken = R(0.5) * (ux * ux + uy * uy);
+    e = u[IP] / d - eken;
+  }
+  else
+  {
+    const R id = rcp(d);
+    ux = u[IU] * id;
+    uy = u[IV] * id;
+    if constexpr (DIM == 3)
+    {
+      uz = u[IW] * id;
+      eken = R(0.5) * (ux * ux + uy * uy + uz * uz);
+    }
+    else
+      eken = R(0.5) * (ux * ux + uy * uy);
+    e = u[IP] * id - eken;
+  }
+  const R p = fmax((G.gamma0 - R(1)) * d * e, d * G.smallp);
+  c = hsqrt(hdiv(G.gamma0 * (p), d));
+  q[ID] = d;
+  q[IP] = p;
+  q[IU] = ux;
+  q[IV] = uy;
+  if constexpr (DIM == 3)
+    q[IW] = uz;
+}
+
+// trace_unsplit_2d_along_dir (HydroBaseFunctor2D.h:225-311) /
+// trace_unsplit_3d_along_dir (HydroBaseFunctor3D.h:274-400): the state on
+// the minus (MINUS) or plus face of a cell along direction DIR.  dq[d][v]
+// are the cell's limited slopes, t = dt/dx_DIR.
+template <class R, int DIM, int DIR, bool MINUS>
+__device__ __forceinline__ void
+htrace(const HGrid<R> & G, const R * q, const R (*dq)[MAXV], R t, R * qf)
+{
+  const R r = q[ID], p = q[IP], u = q[IU], v = q[IV];
+  R       sr0, sp0, su0, sv0, sw0 = R(0), w = R(0);
+  if constexpr (DIM == 2)
+  {
+    sr0 = -u * dq[0][ID] - v * dq[1][ID] - (dq[0][IU] + dq[1][IV]) * r;
+    sp0 = -u * dq[0][IP] - v * dq[1][IP] - (dq[0][IU] + dq[1][IV]) * G.gamma0 * p;
+    if constexpr (kExactOrder)
+    {
+      su0 = -u * dq[0][IU] - v * dq[1][IU] - (dq[0][IP]) / r;
+      sv0 = -u * dq[0][IV] - v * dq[1][IV] - (dq[1][IP]) / r;
+    }
+    else
+    {
+      const R ir = rcp(r);
+      su0 = -u * dq[0][IU] - v * dq[1][IU] - dq[0][IP] * ir;
+      sv0 = -u * dq[0][IV] - v * dq[1][IV] - dq[1][IP] * ir;
+    }
+  }
+  else
+  {
+    w = q[IW];
+    sr0 = -u * dq[0][ID] - v * dq[1][ID] - w * dq[2][ID] - (dq[0][IU] + dq[1][IV] + dq[2][IW]) * r;
+    sp0 = -u * dq[0][IP] - v * dq[1][IP] - w * dq[2][IP] -
+          (dq[0][IU] + dq[1][IV] + dq[2][IW]) * G.gamma0 * p;
+    if constexpr (kExactOrder)
+    {
+      su0 = -u * dq[0][IU] - v * dq[1][IU] - w * dq[2][IU] - (dq[0][IP]) / r;
+      sv0 = -u * dq[0][IV] - v * dq[1][IV] - w * dq[2][IV] - (dq[1][IP]) / r;
+      sw0 = -u * dq[0][IW] - v * dq[1][IW] - w * dq[2][IW] - (dq[2][IP]) / r;
+    }
+    else
+    {
+      const R ir = rcp(r);
+      su0 = -u * dq[0][IU] - v * dq[1][IU] - w * dq[2][IU] - dq[0][IP] * ir;
+      sv0 = -u * dq[0][IV] - v * dq[1][IV] - w * dq[2][IV] - dq[1][IP] * ir;
+      sw0 = -u * dq[0][IW] - v * dq[1][IW] - w * dq[2][IW] - dq[2][IP] * ir;
+    }
+  }
+  const R * d = dq[DIR];
+  if constexpr (MINUS)
+  {
+    qf[ID] = r - R(0.5) * d[ID] + sr0 * t * R(0.5);
+    qf[IP] = p - R(0.5) * d[IP] + sp0 * t * R(0.5);
+    qf[IU] = u - R(0.5) * d[IU] + su0 * t * R(0.5);
+    qf[IV] = v - R(0.5) * d[IV] + sv0 * t * R(0.5);
+    if constexpr (DIM == 3)
+      qf[IW] = w - R(0.5) * d[IW] + sw0 * t * R(0.5);
+  }
+  else
+  {
+    qf[ID] = r + R(0.5) * d[ID] + sr0 * t * R(0.5);
+    qf[IP] = p + R(0.5) * d[IP] + sp0 * t * R(0.5);
+    qf[IU] = u + R(0.5) * d[IU] + su0 * t * R(0.5);
+    qf[IV] = v + R(0.5) * d[IV] + sv0 * t * R(0.5);
+    if constexpr (DIM == 3)
+      qf[IW] = w + R(0.5) * d[IW] + sw0 * t * R(0.5);
+  }
+  qf[ID] = fmax(G.smallr, qf[ID]);
+}
+
+// cmpflx (RiemannSolvers.h:19-48)
+template <class R, int DIM>
+__device__ __forceinline__ void
+hcmpflx(const HGrid<R> & G, const R * qg, R * flux)
+{
+  flux[ID] = qg[ID] * qg[IU];
+  flux[IU] = flux[ID] * qg[IU] + qg[IP];
+  flux[IV] = flux[ID] * qg[IV];
+  if constexpr (DIM == 3)
+    flux[IW] = flux[ID] * qg[IW];
+  R ekin = R(0.5) * qg[ID] * (qg[IU] * qg[IU] + qg[IV] * qg[IV]);
+  if constexpr (DIM == 3)
+    ekin += R(0.5) * qg[ID] * (qg[IW] * qg[IW]);
+  const R etot = qg[IP] * G.entho + ekin;
+  flux[IP] = qg[IU] * (etot + qg[IP]);
+}
+
+// riemann_approx (RiemannSolvers.h:50-199): two-shock approximate solver,
+// Newton iterations on the star pressure (at most 10, to |dp / p| <= 1e-6)
+template <class R, int DIM>
+__device__ __forceinline__ void
+riemann_approx(const HGrid<R> & G, const R * ql, const R * qr, R * flux)
+{
+  const R gamma0 = G.gamma0, gamma6 = G.gamma6, smallr = G.smallr, smallc = G.smallc;
+  const R rl = fmax(ql[ID], smallr);
+  const R ul = ql[IU];
+  const R pl = fmax(ql[IP], rl * G.smallp);
+  const R rr = fmax(qr[ID], smallr);
+  const R ur = qr[IU];
+  const R pr = fmax(qr[IP], rr * G.smallp);
+  const R cl = gamma0 * pl * rl;
+  const R cr = gamma0 * pr * rr;
+  R       wl = hsqrt(cl);
+  R       wr = hsqrt(cr);
+  R       pstar = fmax(hdiv((wr * pl + wl * pr) + wl * wr * (ul - ur), wl + wr), R(0));
+  R       pold = pstar;
+  R       conv = R(1);
+  // the divisions by pl and pr of every iteration: one reciprocal each in
+  // the fast builds
+  const R ipl = kExactOrder ? R(0) : rcp(pl);
+  const R ipr = kExactOrder ? R(0) : rcp(pr);
+  for (int iter = 0; (iter < 10) && (conv > R(1e-6)); ++iter)
+  {
+    R wwl, wwr, qlw, qrw, usl, usr, delp;
+    if constexpr (kExactOrder)
+    {
+      wwl = sqrt(cl * (R(1) + gamma6 * (pold - pl) / pl));
+      wwr = sqrt(cr * (R(1) + gamma6 * (pold - pr) / pr));
+      qlw = R(2) * wwl * wwl * wwl / (wwl * wwl + cl);
+      qrw = R(2) * wwr * wwr * wwr / (wwr * wwr + cr);
+      usl = ul - (pold - pl) / wwl;
+      usr = ur + (pold - pr) / wwr;
+      delp = fmax(qrw * qlw / (qrw + qlw) * (usl - usr), -pold);
+      pold = pold + delp;
+      conv = fabs(delp / (pold + G.smallpp));
+    }
+    else
+    {
+      wwl = fsqrt(cl * (R(1) + gamma6 * (pold - pl) * ipl));
+      wwr = fsqrt(cr * (R(1) + gamma6 * (pold - pr) * ipr));
+      const R iwl = rcp(wwl), iwr = rcp(wwr);
+      qlw = R(2) * wwl * wwl * wwl * rcp(wwl * wwl + cl);
+      qrw = R(2) * wwr * wwr * wwr * rcp(wwr * wwr + cr);
+      usl = ul - (pold - pl) * iwl;
+      usr = ur + (pold - pr) * iwr;
+      delp = fmax(qrw * qlw * rcp(qrw + qlw) * (usl - usr), -pold);
+      pold = pold + delp;
+      conv = fabs(delp * rcp(pold + G.smallpp));
+    }
+  }
+  pstar = pold;
+  if constexpr (kExactOrder)
+  {
+    wl = sqrt(cl * (R(1) + gamma6 * (pstar - pl) / pl));
+    wr = sqrt(cr * (R(1) + gamma6 * (pstar - pr) / pr));
+  }
+  else
+  {
+    wl = fsqrt(cl * (R(1) + gamma6 * (pstar - pl) * ipl));
+    wr = fsqrt(cr * (R(1) + gamma6 * (pstar - pr) * ipr));
+  }
+  const R ustar = R(0.5) * (ul + hdiv(pl - pstar, wl) + ur - hdiv(pr - pstar, wr));
+  const R sgnm = copysign(R(1), ustar);
+  R       ro, uo, po, wo;
+  if (sgnm > R(0))
+  {
+    ro = rl;
+    uo = ul;
+    po = pl;
+    wo = wl;
+  }
+  else
+  {
+    ro = rr;
+    uo = ur;
+    po = pr;
+    wo = wr;
+  }
+  const R co = fmax(smallc, hsqrt(fabs(hdiv(gamma0 * po, ro))));
+  const R rstar = fmax(hdiv(ro, R(1) + hdiv(ro * (po - pstar), wo * wo)), smallr);
+  const R cstar = fmax(smallc, hsqrt(fabs(hdiv(gamma0 * pstar, rstar))));
+  R       spout = co - sgnm * uo;
+  R       spin = cstar - sgnm * ustar;
+  const R ushock = hdiv(wo, ro) - sgnm * uo;
+  if (pstar >= po)
+  {
+    spin = ushock;
+    spout = ushock;
+  }
+  const R scr = fmax(spout - spin, smallc + fabs(spout + spin));
+  R       frac = R(0.5) * (R(1) + hdiv(spout + spin, scr));
+  if (frac != frac)
+    frac = R(0);
+  else
+    frac = frac >= R(1) ? R(1) : frac <= R(0) ? R(0) : frac;
+  R qg[MAXV];
+  qg[ID] = frac * rstar + (R(1) - frac) * ro;
+  qg[IU] = frac * ustar + (R(1) - frac) * uo;
+  qg[IP] = frac * pstar + (R(1) - frac) * po;
+  if (spout < R(0))
+  {
+    qg[ID] = ro;
+    qg[IU] = uo;
+    qg[IP] = po;
+  }
+  if (spin > R(0))
+  {
+    qg[ID] = rstar;
+    qg[IU] = ustar;
+    qg[IP] = pstar;
+  }
+  if (sgnm > R(0))
+  {
+    qg[IV] = ql[IV];
+    if constexpr (DIM == 3)
+      qg[IW] = ql[IW];
+  }
+  else
+  {
+    qg[IV] = qr[IV];
+    if constexpr (DIM == 3)
+      qg[IW] = qr[IW];
+  }
+  hcmpflx<R, DIM>(G, qg, flux);
+}
+
+// conservative state and physical flux of riemann_llf / riemann_hll
+// (RiemannSolvers.h:249-309, :374-425); HLL takes fleft[ID] = uleft[IU]
+template <class R, int DIM>
+__device__ __forceinline__ void
+hcons_flux(const HGrid<R> & G, const R * q, bool hll, R * u, R * f)
+{
+  u[ID] = q[ID];
+  u[IP] = q[IP] * G.entho + R(0.5) * q[ID] * q[IU] * q[IU];
+  u[IP] += R(0.5) * q[ID] * q[IV] * q[IV];
+  if constexpr (DIM == 3)
+    u[IP] += R(0.5) * q[ID] * q[IW] * q[IW];
+  u[IU] = q[ID] * q[IU];
+  u[IV] = q[ID] * q[IV];
+  if constexpr (DIM == 3)
+    u[IW] = q[ID] * q[IW];
+  f[ID] = hll ? u[IU] : u[ID] * q[IU];
+  f[IP] = q[IU] * (u[IP] + q[IP]);
+  f[IU] = q[IP] + u[IU] * q[IU];
+  f[IV] = f[ID] * q[IV];
+  if constexpr (DIM == 3)
+    f[IW] = f[ID] * q[IW];
+}
+
+// riemann_llf (RiemannSolvers.h:201-327) and riemann_hll (:329-435)
+template <class R, int DIM>
+__device__ __forceinline__ void
+riemann_llf_hll(const HGrid<R> & G, const R * ql, const R * qr, bool hll, R * flux)
+{
+  constexpr int NVAR = DIM + 2;
+  const R       rl = fmax(ql[ID], G.smallr);
+  const R       ul = ql[IU];
+  const R       pl = fmax(ql[IP], rl * G.smallp);
+  const R       rr = fmax(qr[ID], G.smallr);
+  const R       ur = qr[IU];
+  const R       pr = fmax(qr[IP], rr * G.smallp);
+  const R       cl = hsqrt(hdiv(G.gamma0 * pl, rl));
+  const R       cr = hsqrt(hdiv(G.gamma0 * pr, rr));
+  R             uleft[MAXV], uright[MAXV], fleft[MAXV], fright[MAXV];
+  hcons_flux<R, DIM>(G, ql, hll, uleft, fleft);
+  hcons_flux<R, DIM>(G, qr, hll, uright, fright);
+  if (!hll)
+  {
+    const R cmax = fmax(fabs(ul) + cl, fabs(ur) + cr);
+#pragma unroll
+    for (int v = 0; v < NVAR; ++v)
+      flux[v] = R(0.5) * (fleft[v] + fright[v] - cmax * (uright[v] - uleft[v]));
+    return;
+  }
+  const R SL = fmin(fmin(ul, ur) - fmax(cl, cr), R(0));
+  const R SR = fmax(fmax(ul, ur) + fmax(cl, cr), R(0));
+  if constexpr (kExactOrder)
+  {
+#pragma unroll
+    for (int v = 0; v < NVAR; ++v)
+      flux[v] = (SR * fleft[v] - SL * fright[v] + SR * SL * (uright[v] - uleft[v])) / (SR - SL);
+  }
+  else
+  {
+    const R is = rcp(SR - SL);
+#pragma unroll
+    for (int v = 0; v < NVAR; ++v)
+      flux[v] = (SR * fleft[v] - SL * fright[v] + SR * SL * (uright[v] - uleft[v])) * is;
+  }
+}
+
+// riemann_hllc (RiemannSolvers.h:437-568)
+template <class R, int DIM>
+__device__ __forceinline__ void
+riemann_hllc(const HGrid<R> & G, const R * ql, const R * qr, R * flux)
+{
+  const R gamma0 = G.gamma0, smallc = G.smallc;
+  const R rl = fmax(ql[ID], G.smallr);
+  const R pl = fmax(ql[IP], rl * G.smallp);
+  const R ul = ql[IU];
+  R       ecinl = R(0.5) * rl * ul * ul;
+  ecinl += R(0.5) * rl * ql[IV] * ql[IV];
+  if constexpr (DIM == 3)
+    ecinl += R(0.5) * rl * ql[IW] * ql[IW];
+  const R etotl = pl * G.entho + ecinl;
+  const R ptotl = pl;
+  const R rr = fmax(qr[ID], G.smallr);
+  const R pr = fmax(qr[IP], rr * G.smallp);
+  const R ur = qr[IU];
+  R       ecinr = R(0.5) * rr * ur * ur;
+  ecinr += R(0.5) * rr * qr[IV] * qr[IV];
+  if constexpr (DIM == 3)
+    ecinr += R(0.5) * rr * qr[IW] * qr[IW];
+  const R etotr = pr * G.entho + ecinr;
+  const R ptotr = pr;
+  const R cfastl = hsqrt(fmax(hdiv(gamma0 * pl, rl), smallc * smallc));
+  const R cfastr = hsqrt(fmax(hdiv(gamma0 * pr, rr), smallc * smallc));
+  const R SL = fmin(ul, ur) - fmax(cfastl, cfastr);
+  const R SR = fmax(ul, ur) + fmax(cfastl, cfastr);
+  const R rcl = rl * (ul - SL);
+  const R rcr = rr * (SR - ur);
+  R       ustar, ptotstar, rstarl, etotstarl, rstarr, etotstarr;
+  if constexpr (kExactOrder)
+  {
+    ustar = (rcr * ur + rcl * ul + (ptotl - ptotr)) / (rcr + rcl);
+    ptotstar = (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) / (rcr + rcl);
+    rstarl = rl * (SL - ul) / (SL - ustar);
+    etotstarl = ((SL - ul) * etotl - ptotl * ul + ptotstar * ustar) / (SL - ustar);
+    rstarr = rr * (SR - ur) / (SR - ustar);
+    etotstarr = ((SR - ur) * etotr - ptotr * ur + ptotstar * ustar) / (SR - ustar);
+  }
+  else
+  {
+    const R irc = rcp(rcr + rcl);
+    ustar = (rcr * ur + rcl * ul + (ptotl - ptotr)) * irc;
+    ptotstar = (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) * irc;
+    const R isl = rcp(SL - ustar), isr = rcp(SR - ustar);
+    rstarl = rl * (SL - ul) * isl;
+    etotstarl = ((SL - ul) * etotl - ptotl * ul + ptotstar * ustar) * isl;
+    rstarr = rr * (SR - ur) * isr;
+    etotstarr = ((SR - ur) * etotr - ptotr * ur + ptotstar * ustar) * isr;
+  }
+  R ro, uo, ptoto, etoto;
+  if (SL > R(0))
+  {
+    ro = rl;
+    uo = ul;
+    ptoto = ptotl;
+    etoto = etotl;
+  }
+  else if (ustar > R(0))
+  {
+    ro = rstarl;
+    uo = ustar;
+    ptoto = ptotstar;
+    etoto = etotstarl;
+  }
+  else if (SR > R(0))
+  {
+    ro = rstarr;
+    uo = ustar;
+    ptoto = ptotstar;
+    etoto = etotstarr;
+  }
+  else
+  {
+    ro = rr;
+    uo = ur;
+    ptoto = ptotr;
+    etoto = etotr;
+  }
+  flux[ID] = ro * uo;
+  flux[IU] = ro * uo * uo + ptoto;
+  flux[IP] = (etoto + ptoto) * uo;
+  flux[IV] = flux[ID] > R(0) ? flux[ID] * ql[IV] : flux[ID] * qr[IV];
+  if constexpr (DIM == 3)
+    flux[IW] = flux[ID] > R(0) ? flux[ID] * ql[IW] : flux[ID] * qr[IW];
+}
+
+// riemann_hydro (RiemannSolvers.h:570-633)
+template <class R, int DIM>
+__device__ __forceinline__ void
+hriemann(const HGrid<R> & G, const R * ql, const R * qr, R * flux)
+{
+  if (G.riemann == MHD_RIEMANN_HLLC)
+    riemann_hllc<R, DIM>(G, ql, qr, flux);
+  else if (G.riemann == MHD_RIEMANN_LLF)
+    riemann_llf_hll<R, DIM>(G, ql, qr, false, flux);
+  else if (G.riemann == MHD_RIEMANN_HLL)
+    riemann_llf_hll<R, DIM>(G, ql, qr, true, flux);
+  else
+    riemann_approx<R, DIM>(G, ql, qr, flux);
+}
+
+// ---------------------------------------------------------------- kernels
+
+// Ghost fill.  The reference fills the X faces (over the full j, k range),
+// then Y, then Z (MakeBoundariesFunctor2D/3D, BoundariesFunctors.h:18-530;
+// SolverBase.cpp:338-410): a ghost cell ends up with the interior value at
+// the composition of the per-axis source maps, times the reflection signs of
+// the normal velocities.  The iteration's first thread clears the CFL word.
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+k_hbound(const HGrid<R> G, R * __restrict__ U, DevState * st, int force)
+{
+  if (!force && step_finished(st))
+    return;
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx == 0)
+    st->invdt_bits = 0ull;
+  int i, j, k;
+  if (!box_cell(G.box[BOX_ALL], idx, i, j, k))
+    return;
+  const int  g = G.g;
+  const bool gx = i < g || i >= G.nx + g;
+  const bool gy = j < g || j >= G.ny + g;
+  const bool gz = DIM == 3 && (k < g || k >= G.nz + g);
+  if (!gx && !gy && !gz)
+    return;
+  bool fx = false, fy = false, fz = false;
+  int  i0 = i, j0 = j, k0 = k;
+  if (gx)
+    i0 = bc_source(i, G.nx, g, G.bc[i < g ? 0 : 1], i >= g, fx);
+  if (gy)
+    j0 = bc_source(j, G.ny, g, G.bc[j < g ? 2 : 3], j >= g, fy);
+  if (gz)
+    k0 = bc_source(k, G.nz, g, G.bc[k < g ? 4 : 5], k >= g, fz);
+  const int64_t dst = hcell(G, i, j, k), src = hcell(G, i0, j0, k0);
+#pragma unroll
+  for (int v = 0; v < DIM + 2; ++v)
+  {
+    R x = U[src + v * G.sv];
+    if (fx && v == IU)
+      x = x * R(-1);
+    if (fy && v == IV)
+      x = x * R(-1);
+    if (fz && v == IW)
+      x = x * R(-1);
+    U[dst + v * G.sv] = x;
+  }
+}
+
+// ConvertToPrimitivesFunctor2D/3D over the whole array
+// (HydroRunFunctors2D.h:184-240), fused with the CFL reduction over the
+// interior cells: ComputeDtFunctor2D/3D (2D:13-82, 3D:14-88),
+// max of sum_d (c + |v_d|) / dx_d, or with static gravity
+// ComputeDtGravityFunctor2D/3D (2D:84-175, 3D:90-190).  The max is reduced
+// in FP64 (one atomicMax per block on the bit pattern, which orders like the
+// value for non-negative doubles): order-independent, so dt is the
+// reference's bit for bit in the FMA-free build.
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+k_hprim_dt(const HGrid<R> G, const R * __restrict__ U, R * __restrict__ Q, DevState * st,
+           int force)
+{
+  if (!force && step_finished(st))
+    return;
+  constexpr int NVAR = DIM + 2;
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  R             rate = R(0);
+  bool          bad = false;
+  int           i, j, k;
+  if (box_cell(G.box[BOX_ALL], idx, i, j, k))
+  {
+    const int64_t c = hcell(G, i, j, k);
+    R             u[MAXV], q[MAXV], cs;
+#pragma unroll
+    for (int v = 0; v < NVAR; ++v)
+      u[v] = U[c + v * G.sv];
+    hprim<R, DIM>(G, u, cs, q);
+#pragma unroll
+    for (int v = 0; v < NVAR; ++v)
+      Q[c + v * G.sv] = q[v];
+    const int  g = G.g;
+    const bool interior = i >= g && i < G.nx + g && j >= g && j < G.ny + g &&
+                          (DIM == 2 || (k >= g && k < G.nz + g));
+    if (interior)
+    {
+      R val;
+      if (G.gravity)
+      {
+        R velocity = R(0);
+        velocity += cs + fabs(q[IU]);
+        velocity += cs + fabs(q[IV]);
+        if constexpr (DIM == 3)
+          velocity += cs + fabs(q[IW]);
+        R kk = fabs(G.grav[0]) + fabs(G.grav[1]);
+        if constexpr (DIM == 3)
+          kk = kk + fabs(G.grav[2]);
+        kk *= hdiv(R(G.cfl) * R(G.dxg), velocity * velocity);
+        kk = fmax(kk, R(1e-4));
+        velocity *= hdiv(kk, hsqrt(R(1) + R(2) * kk) - R(1));
+        val = qdiv(velocity, R(G.dxg), R(G.idxg));
+        if constexpr (!kExactOrder)
+          val = velocity * R(G.idxg);
+      }
+      else
+      {
+        const R vx = cs + fabs(q[IU]);
+        const R vy = cs + fabs(q[IV]);
+        if constexpr (kExactOrder)
+        {
+          if constexpr (DIM == 3)
+          {
+            const R vz = cs + fabs(q[IW]);
+            val = qdiv(vx, R(G.dx), R(G.idx)) + qdiv(vy, R(G.dy), R(G.idy)) +
+                  qdiv(vz, R(G.dz), R(G.idz));
+          }
+          else
+            val = qdiv(vx, R(G.dx), R(G.idx)) + qdiv(vy, R(G.dy), R(G.idy));
+        }
+        else
+        {
+          if constexpr (DIM == 3)
+            val = vx * R(G.idx) + vy * R(G.idy) + (cs + fabs(q[IW])) * R(G.idz);
+          else
+            val = vx * R(G.idx) + vy * R(G.idy);
+        }
+      }
+      rate = (val >= R(0)) ? val : R(0); // fmax drops a NaN operand
+      bad = !(u[ID] > R(0)) || !isfinite(u[IP]);
+    }
+  }
+  __shared__ R red[32];
+  rate = warp_max(rate);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0)
+    red[wid] = rate;
+  if (__syncthreads_or(bad) && threadIdx.x == 0)
+    atomicOr(&st->status, STATUS_NUMERIC);
+  if (wid == 0)
+  {
+    rate = lane < (int)(blockDim.x >> 5) ? red[lane] : R(0);
+    rate = warp_max(rate);
+    const unsigned long long rb = (unsigned long long)__double_as_longlong((double)rate);
+    if (lane == 0 && rate > R(0) && rb > *(volatile unsigned long long *)&st->invdt_bits)
+      atomicMax(&st->invdt_bits, rb);
+  }
+}
+
+// dt = cfl / invDt (SolverHydroMuscl.h:649-690) clipped to tEnd
+// (SolverBase.cpp:148-179); dt/dx of ComputeAndStoreFluxesFunctor
+// (HydroRunFunctors2D.h:505-507) in the working precision.
+template <class R>
+__global__ void
+k_hfinalize(const HGrid<R> G, DevState * st, int force)
+{
+  if (!force && step_finished(st))
+    return;
+  const double invDt = __longlong_as_double((long long)st->invdt_bits);
+  double       dt = G.cfl / invDt;
+  if (st->t + dt > st->tEnd)
+    dt = st->tEnd - st->t;
+  st->dt = dt;
+  st->dtdx = dt / G.dx;
+  st->dtdy = dt / G.dy;
+  st->dtdz = dt / G.dz;
+  st->fdtdx = (float)((float)dt / (float)G.dx);
+  st->fdtdy = (float)((float)dt / (float)G.dy);
+  st->fdtdz = (float)((float)dt / (float)G.dz);
+  if (!(invDt > 0.0) || !isfinite(dt))
+    st->status |= STATUS_NUMERIC;
+}
+
+// godunov_unsplit(dt) with the caller's dt
+template <class R>
+__global__ void
+k_hset_dt(const HGrid<R> G, DevState * st, double dt)
+{
+  if (step_finished(st))
+    return;
+  st->dt = dt;
+  st->dtdx = dt / G.dx;
+  st->dtdy = dt / G.dy;
+  st->dtdz = dt / G.dz;
+  st->fdtdx = (float)((float)dt / (float)G.dx);
+  st->fdtdy = (float)((float)dt / (float)G.dy);
+  st->fdtdz = (float)((float)dt / (float)G.dz);
+}
+
+// ComputeSlopesFunctor2D/3D (HydroRunFunctors2D.h:900-985, 3D:930-1040) with
+// slope_unsplit_hydro_2d/3d (HydroBaseFunctor2D.h:432-525, 3D:411-540) over
+// [g-1, size-g] per axis: S[(d * NVAR + v) * sv + cell]; slope_type 0 gives
+// zero slopes (first order).
+template <class R, int DIM>
+__global__ void __launch_bounds__(128)
+k_hslopes(const HGrid<R> G, const R * __restrict__ Q, R * __restrict__ S, const DevState * st)
+{
+  if (step_finished(st))
+    return;
+  constexpr int NVAR = DIM + 2;
+  int           i, j, k;
+  if (!box_cell(G.box[BOX_TRACE], blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
+    return;
+  const int64_t c = hcell(G, i, j, k);
+  const int64_t str[3] = { 1, G.sj, G.sk };
+#pragma unroll
+  for (int d = 0; d < DIM; ++d)
+#pragma unroll
+    for (int v = 0; v < NVAR; ++v)
+    {
+      const R * Qv = Q + v * G.sv;
+      R         s = R(0);
+      if (G.slope_type != R(0))
+      {
+        if constexpr (kExactOrder)
+          s = limited_slope(Qv[c], Qv[c + str[d]], Qv[c - str[d]], G.slope_type);
+        else
+          s = limited_slope_bits(Qv[c], Qv[c + str[d]], Qv[c - str[d]], G.slope_type);
+      }
+      S[(d * NVAR + v) * G.sv + c] = s;
+    }
+}
+
+// Face flux along direction D of the face at the minus side of every cell
+// of [g, size-g] per axis (ComputeAndStoreFluxesFunctor2D/3D,
+// HydroRunFunctors2D.h:490-755, 3D:300-705; ComputeTraceAndFluxes_Functor,
+// 2D:988-1255, 3D:1044-1420): right state = the cell traced to its minus
+// face, left state = the minus neighbour traced to its plus face, the gravity
+// predictor 0.5 dt g on both, the normal velocity swapped into IU, the
+// Riemann solver, the flux swapped back and scaled by dt/dx_D.
+template <class R, int DIM, int D>
+__device__ __forceinline__ void
+hflux_face(const HGrid<R> & G, const R * __restrict__ Q, const R * __restrict__ S,
+           R * __restrict__ F, const DevState * st, int64_t c)
+{
+  constexpr int NVAR = DIM + 2;
+  constexpr int VN = D == 0 ? IU : D == 1 ? IV : IW; // normal velocity
+  const int64_t nb = c - (D == 0 ? 1 : D == 1 ? G.sj : G.sk);
+  R             qc[MAXV], qn[MAXV], dqc[DIM][MAXV], dqn[DIM][MAXV];
+#pragma unroll
+  for (int v = 0; v < NVAR; ++v)
+  {
+    qc[v] = Q[c + v * G.sv];
+    qn[v] = Q[nb + v * G.sv];
+  }
+#pragma unroll
+  for (int e = 0; e < DIM; ++e)
+#pragma unroll
+    for (int v = 0; v < NVAR; ++v)
+    {
+      dqc[e][v] = S[(e * NVAR + v) * G.sv + c];
+      dqn[e][v] = S[(e * NVAR + v) * G.sv + nb];
+    }
+  R tx, ty, tz;
+  dt_over_dx(st, tx, ty, tz);
+  const R t = D == 0 ? tx : D == 1 ? ty : tz;
+  R       qleft[MAXV], qright[MAXV], flux[MAXV];
+  htrace<R, DIM, D, true>(G, qc, dqc, t, qright);
+  htrace<R, DIM, D, false>(G, qn, dqn, t, qleft);
+  if (G.gravity)
+  {
+    const R hdt = R(0.5 * st->dt);
+    qleft[IU] += hdt * G.grav[0];
+    qleft[IV] += hdt * G.grav[1];
+    if constexpr (DIM == 3)
+      qleft[IW] += hdt * G.grav[2];
+    if (D != 2 || G.zgrav_right)
+    {
+      qright[IU] += hdt * G.grav[0];
+      qright[IV] += hdt * G.grav[1];
+      if constexpr (DIM == 3)
+        qright[IW] += hdt * G.grav[2];
+    }
+  }
+  if constexpr (D > 0)
+  {
+    swap_vals(qleft[IU], qleft[VN]);
+    swap_vals(qright[IU], qright[VN]);
+  }
+  hriemann<R, DIM>(G, qleft, qright, flux);
+  if constexpr (D > 0)
+    swap_vals(flux[IU], flux[VN]);
+#pragma unroll
+  for (int v = 0; v < NVAR; ++v)
+    F[(D * NVAR + v) * G.sv + c] = flux[v] * t;
+}
+
+// grid (faces / 128, DIM): blockIdx.y is the direction
+template <class R, int DIM>
+__global__ void __launch_bounds__(128)
+k_hflux(const HGrid<R> G, const R * __restrict__ Q, const R * __restrict__ S, R * __restrict__ F,
+        const DevState * st)
+{
+  if (step_finished(st))
+    return;
+  int i, j, k;
+  if (!box_cell(G.box[BOX_FACE], blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
+    return;
+  const int64_t c = hcell(G, i, j, k);
+  if (blockIdx.y == 0)
+    hflux_face<R, DIM, 0>(G, Q, S, F, st, c);
+  else if (blockIdx.y == 1)
+    hflux_face<R, DIM, 1>(G, Q, S, F, st, c);
+  else if constexpr (DIM == 3)
+    hflux_face<R, DIM, 2>(G, Q, S, F, st, c);
+}
+
+// UpdateFunctor2D/3D (HydroRunFunctors2D.h:765-840, 3D:715-800) or
+// UpdateDirFunctor per direction (same additions in the same order),
+// then GravitySourceTermFunctor2D (HydroRunFunctors2D.h:1262-1340, new density
+// floored at smallr) / 3D (3D:1440-1510, not floored); ghost cells are the
+// boundary-filled input (Kokkos::deep_copy(data_out, data_in)).
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+k_hupdate(const HGrid<R> G, const R * __restrict__ Uin, R * __restrict__ Uout,
+          const R * __restrict__ F, const DevState * st)
+{
+  if (step_finished(st))
+    return;
+  constexpr int NVAR = DIM + 2;
+  int           i, j, k;
+  if (!box_cell(G.box[BOX_ALL], blockIdx.x * (int64_t)blockDim.x + threadIdx.x, i, j, k))
+    return;
+  const int64_t c = hcell(G, i, j, k);
+  const int     g = G.g;
+  const bool    interior = i >= g && i < G.nx + g && j >= g && j < G.ny + g &&
+                        (DIM == 2 || (k >= g && k < G.nz + g));
+  if (!interior)
+  {
+#pragma unroll
+    for (int v = 0; v < NVAR; ++v)
+      Uout[c + v * G.sv] = Uin[c + v * G.sv];
+    return;
+  }
+  const int64_t str[3] = { 1, G.sj, G.sk };
+  R             u[MAXV];
+#pragma unroll
+  for (int v = 0; v < NVAR; ++v)
+  {
+    R x = Uin[c + v * G.sv];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+    {
+      const R * Fd = F + (d * NVAR + v) * G.sv;
+      x = rn_add(x, Fd[c]);
+      x = rn_sub(x, Fd[c + str[d]]);
+    }
+    u[v] = x;
+  }
+  if (G.gravity)
+  {
+    const R rhoOld = Uin[c + ID * G.sv];
+    const R rhoNew = DIM == 2 ? fmax(G.smallr, u[ID]) : u[ID];
+    R       rhou = u[IU], rhov = u[IV], rhow = DIM == 3 ? u[IW] : R(0);
+    R       ekin_old, ekin_new;
+    if constexpr (DIM == 3)
+      ekin_old = hdiv(R(0.5) * (rhou * rhou + rhov * rhov + rhow * rhow), rhoNew);
+    else
+      ekin_old = hdiv(R(0.5) * (rhou * rhou + rhov * rhov), rhoNew);
+    const R hdt = R(0.5 * st->dt);
+    rhou += hdt * G.grav[0] * (rhoOld + rhoNew);
+    rhov += hdt * G.grav[1] * (rhoOld + rhoNew);
+    if constexpr (DIM == 3)
+      rhow += hdt * G.grav[2] * (rhoOld + rhoNew);
+    u[IU] = rhou;
+    u[IV] = rhov;
+    if constexpr (DIM == 3)
+      u[IW] = rhow;
+    if constexpr (DIM == 3)
+      ekin_new = hdiv(R(0.5) * (rhou * rhou + rhov * rhov + rhow * rhow), rhoNew);
+    else
+      ekin_new = hdiv(R(0.5) * (rhou * rhou + rhov * rhov), rhoNew);
+    u[IP] += (ekin_new - ekin_old);
+  }
+#pragma unroll
+  for (int v = 0; v < NVAR; ++v)
+    Uout[c + v * G.sv] = u[v];
+}
+
+// LayoutRight <-> LayoutLeft of an NVAR-variable array.  dir = 0: right ->
+// left, dir = 1: left -> right.
+template <class R>
+__global__ void
+k_htranspose(const HGrid<R> G, const R * __restrict__ src, R * __restrict__ dst, int dir)
+{
+  const int64_t n = G.sv * G.nvar;
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx >= n)
+    return;
+  const int64_t v = idx / G.sv;
+  const int64_t cell = idx - v * G.sv;
+  const int64_t k = cell / G.sk;
+  const int64_t rem = cell - k * G.sk;
+  const int64_t j = rem / G.sj;
+  const int64_t i = rem - j * G.sj;
+  const int64_t right = ((i * G.jsize + j) * G.ksize + k) * G.nvar + v;
+  if (dir == 0)
+    dst[idx] = src[right];
+  else
+    dst[right] = src[idx];
+}
+
+template <class R>
+HGrid<R>
+make_hgrid(const mhd_params & p)
+{
+  HGrid<R> G{};
+  G.dim = p.dim;
+  G.nx = p.nx;
+  G.ny = p.ny;
+  G.nz = p.dim == 3 ? p.nz : 1;
+  G.g = p.ghost;
+  G.nvar = p.dim + 2;
+  G.isize = p.nx + 2 * p.ghost;
+  G.jsize = p.ny + 2 * p.ghost;
+  G.ksize = p.dim == 3 ? p.nz + 2 * p.ghost : 1;
+  G.sj = G.isize;
+  G.sk = (int64_t)G.isize * G.jsize;
+  G.sv = G.sk * G.ksize;
+  for (int f = 0; f < 6; ++f)
+    G.bc[f] = p.boundary[f];
+  G.riemann = p.riemann;
+  G.gravity = p.gravity;
+  G.zgrav_right = !(p.dim == 3 && p.implementation_version == 1);
+  // HydroParams::init (HydroParams.cpp:436-443) in real_t
+  G.gamma0 = R(p.gamma0);
+  G.entho = R(1) / (G.gamma0 - R(1));
+  G.smallr = R(p.smallr);
+  G.smallc = R(p.smallc);
+  G.smallp = R(R(p.smallc) * R(p.smallc) / R(p.gamma0));
+  G.smallpp = R(G.smallr * G.smallp);
+  G.gamma6 = R((G.gamma0 + R(1)) / (R(2) * G.gamma0));
+  G.slope_type = R(p.slope_type);
+  for (int q = 0; q < 3; ++q)
+    G.grav[q] = R(q < p.dim ? p.gravity_field[q] : 0.0);
+  G.cfl = p.cfl;
+  G.dx = (double)R(R(p.xmax - p.xmin) / R(p.nx));
+  G.dy = (double)R(R(p.ymax - p.ymin) / R(p.ny));
+  G.dz = p.dim == 3 ? (double)R(R(p.zmax - p.zmin) / R(p.nz)) : 1.0;
+  G.dxg = std::fmin(G.dx, G.dy);
+  if (p.dim == 3)
+    G.dxg = std::fmin(G.dxg, G.dz);
+  G.idx = 1.0 / G.dx;
+  G.idy = 1.0 / G.dy;
+  G.idz = 1.0 / G.dz;
+  G.idxg = 1.0 / G.dxg;
+  const bool d3 = p.dim == 3;
+  const int  g = G.g;
+  G.box[BOX_ALL] = Box(0, 0, 0, G.isize, G.jsize, d3 ? G.ksize : 1);
+  G.box[BOX_PRIM] = G.box[BOX_ALL];
+  G.box[BOX_TRACE] = Box(g - 1, g - 1, d3 ? g - 1 : 0, G.nx + 2, G.ny + 2, d3 ? G.nz + 2 : 1);
+  G.box[BOX_FACE] = Box(g, g, d3 ? g : 0, G.nx + 1, G.ny + 1, d3 ? G.nz + 1 : 1);
+  G.box[BOX_INTERIOR] = Box(g, g, d3 ? g : 0, G.nx, G.ny, d3 ? G.nz : 1);
+  return G;
+}
+
+} // namespace hydro
+} // namespace MHD_VARIANT_TAG
+} // namespace mhd

@@ -79,9 +79,84 @@ namespace mhd
 {
 
 // Empty string when the parameters can be run.
+// The hydro-only solver's parameters (SolverHydroMuscl<dim>).
+std::string
+validate_hydro_params(const mhd_params & p)
+{
+  if (p.dim != 2 && p.dim != 3)
+    return "dim must be 2 or 3";
+  if (p.ghost != 2)
+    return "ghost width must be 2 for the hydro MUSCL scheme";
+  if (p.nx < p.ghost || p.ny < p.ghost || (p.dim == 3 && p.nz < p.ghost))
+    return "each interior extent must be at least the ghost width (2)";
+  const double cells = (double)(p.nx + 4) * (p.ny + 4) * (p.dim == 3 ? p.nz + 4 : 1);
+  if (cells * (p.dim + 2) > 4.0e9)
+    return "grid too large: ghost-inclusive cells x variables must stay below 4e9";
+  if (p.riemann != MHD_RIEMANN_APPROX && p.riemann != MHD_RIEMANN_LLF &&
+      p.riemann != MHD_RIEMANN_HLLC && p.riemann != MHD_RIEMANN_HLL)
+    return "riemann solver must be approx, llf, hll or hllc for the hydro solver";
+  // riemann_hydro's 3D dispatch has no HLL branch (RiemannSolvers.h:608-633):
+  // the reference would leave the face flux uninitialised
+  if (p.dim == 3 && p.riemann == MHD_RIEMANN_HLL)
+    return "the 3D hydro solver has no hll Riemann solver (approx, llf or hllc)";
+  // godunov_unsplit_impl has branches for versions 0 and 1 only
+  // (SolverHydroMuscl.cpp:277-319, :350-399)
+  if (p.implementation_version != 0 && p.implementation_version != 1)
+    return "implementationVersion must be 0 or 1 for the hydro solver";
+  for (int f = 0; f < (p.dim == 3 ? 6 : 4); ++f)
+    if (p.boundary[f] != MHD_BC_REFLECTING && p.boundary[f] != MHD_BC_OUTFLOW &&
+        p.boundary[f] != MHD_BC_PERIODIC)
+      return "boundary types must be 1 (reflecting), 2 (outflow) or 3 (periodic)";
+  // slope_unsplit_hydro_2d/3d: 0 = first order, 1 and 2 limited
+  // (HydroBaseFunctor2D.h:487-525); other values leave the slopes unset
+  if (p.slope_type != 0.0 && p.slope_type != 1.0 && p.slope_type != 2.0)
+    return "slope_type must be 0, 1 (minmod) or 2 (monotonized central)";
+  if (!(p.gamma0 > 1.0) || !(p.cfl > 0.0) || !(p.smallr > 0.0) || !(p.smallc > 0.0))
+    return "gamma0 must be > 1 and cfl, smallr, smallc > 0";
+  if (!(p.xmax > p.xmin) || !(p.ymax > p.ymin) || (p.dim == 3 && !(p.zmax > p.zmin)))
+    return "domain bounds must satisfy max > min";
+  if (p.precision != MHD_FP64 && p.precision != MHD_FP32)
+    return "precision must be 64 or 32";
+  if (p.fp_mode != MHD_FP_FAST && p.fp_mode != MHD_FP_EXACT)
+    return "fp_mode must be MHD_FP_FAST or MHD_FP_EXACT";
+  if (p.precision == MHD_FP32 && p.fp_mode == MHD_FP_EXACT)
+    return "MHD_FP_EXACT is only available with MHD_FP64";
+  if (p.gravity == 2)
+    return "point-source gravity (the disk problem) is not built";
+  if (p.gravity != 0 && p.gravity != 1)
+    return "gravity must be 0 or 1 (static)";
+  const int q = p.problem;
+  if (q == -1)
+    return "the disk problem needs point-source gravity, which is not built";
+  if (q != MHD_PROBLEM_BLAST && q != MHD_PROBLEM_IMPLODE && q != MHD_PROBLEM_KELVIN_HELMHOLTZ &&
+      q != MHD_PROBLEM_GRESHO_VORTEX && q != MHD_PROBLEM_FOUR_QUADRANT &&
+      q != MHD_PROBLEM_ISENTROPIC_VORTEX && q != MHD_PROBLEM_RAYLEIGH_TAYLOR &&
+      q != MHD_PROBLEM_RISING_BUBBLE)
+    return "unknown problem id for the hydro solver";
+  if (p.dim == 3 && (q == MHD_PROBLEM_FOUR_QUADRANT || q == MHD_PROBLEM_ISENTROPIC_VORTEX))
+    return "four_quadrant and isentropic_vortex are 2D problems";
+  if (q == MHD_PROBLEM_KELVIN_HELMHOLTZ && p.problem_int[3])
+    return "kelvin_helmholtz: perturbation_rand draws from Kokkos' own generator; use the sine "
+           "perturbation";
+  // the hydro functors have the random and the Robertson perturbations only
+  // (HydroInitFunctors2D.h:278-332, 3D)
+  if (q == MHD_PROBLEM_KELVIN_HELMHOLTZ && !p.problem_int[1])
+    return "kelvin_helmholtz: the hydro solver seeds with perturbation_sine_robertson only (the "
+           "reference leaves the state empty otherwise)";
+  // the init functors of these two write the gravity field, which the
+  // reference allocates only with gravity on (SolverHydroMuscl.h:242-246)
+  if ((q == MHD_PROBLEM_RAYLEIGH_TAYLOR || q == MHD_PROBLEM_RISING_BUBBLE) && !p.gravity)
+    return "rayleigh_taylor and rising_bubble need [gravity] static=true";
+  return "";
+}
+
 std::string
 validate_params(const mhd_params & p)
 {
+  if (p.solver == MHD_SOLVER_HYDRO_MUSCL)
+    return validate_hydro_params(p);
+  if (p.solver != MHD_SOLVER_MHD_MUSCL)
+    return "solver must be MHD_SOLVER_MHD_MUSCL or MHD_SOLVER_HYDRO_MUSCL";
   if (p.dim != 2 && p.dim != 3)
     return "dim must be 2 or 3";
   if (p.ghost != 3)
@@ -149,12 +224,14 @@ namespace
 // two coarse faces around it otherwise, so the discrete div B stays zero.
 template <class T>
 void
-upscale_state(const T * c, T * f, int dim, int isize, int jsize, int ksize, int g, int nx, int ny)
+upscale_state(const T * c, T * f, int dim, int isize, int jsize, int ksize, int g, int nx, int ny,
+              int nvar)
 {
   const int64_t iL = nx / 2 + 2 * g, jL = ny / 2 + 2 * g;
   const int64_t cv = iL * jL * (dim == 3 ? (ksize - 2 * g) / 2 + 2 * g : 1);
   const int64_t fv = (int64_t)isize * jsize * ksize;
-  for (int v = 0; v < 8; ++v)
+  const bool mhd = nvar == 8; // the hydro solver has no face-centred field
+  for (int v = 0; v < nvar; ++v)
     for (int k = 0; k < ksize; ++k)
     {
       const int kl = dim == 3 ? (k + g) / 2 : 0;
@@ -167,11 +244,11 @@ upscale_state(const T * c, T * f, int dim, int isize, int jsize, int ksize, int 
           const T *      src = c + v * cv;
           const int64_t  a = il + iL * jl + iL * jL * kl;
           T              x = src[a];
-          if (v == 5 && i + g - 2 * il != 0)
+          if (mhd && v == 5 && i + g - 2 * il != 0)
             x = (src[a] + src[a + 1]) / 2;
-          else if (v == 6 && j + g - 2 * jl != 0)
+          else if (mhd && v == 6 && j + g - 2 * jl != 0)
             x = (src[a] + src[a + iL]) / 2;
-          else if (dim == 3 && v == 7 && k + g - 2 * kl != 0)
+          else if (mhd && dim == 3 && v == 7 && k + g - 2 * kl != 0)
             x = (src[a] + src[a + iL * jL]) / 2;
           f[v * fv + i + (int64_t)isize * (j + (int64_t)jsize * k)] = x;
         }
@@ -191,6 +268,8 @@ checkpoint_load(mhd_ctx * ctx, const char * path, int reset_time, int * times_sa
     return fail(ctx, MHD_ERR_INVALID_ARG, std::string("cannot open ") + path);
   CheckpointHeader   h{};
   const bool         got = std::fread(&h, sizeof h, 1, f) == 1;
+  int                sz[4];
+  ctx->core->sizes(sz);
   const mhd_params & p = ctx->params;
   const int          k = upscale ? 2 : 1; // file resolution = context / k
   std::string        bad;
@@ -199,16 +278,15 @@ checkpoint_load(mhd_ctx * ctx, const char * path, int reset_time, int * times_sa
   else if (upscale && (p.nx % 2 || p.ny % 2 || (p.dim == 3 && p.nz % 2)))
     bad = "restart_upscale needs even nx, ny, nz";
   else if ((int)h.dim != p.dim || (int)h.nx * k != p.nx || (int)h.ny * k != p.ny ||
-           (p.dim == 3 && (int)h.nz * k != p.nz) || (int)h.ghost != p.ghost || h.nbvar != 8)
+           (p.dim == 3 && (int)h.nz * k != p.nz) || (int)h.ghost != p.ghost ||
+           (int)h.nbvar != sz[3])
     bad = upscale ? "checkpoint grid is not half the context's (restart_upscale)"
                   : "checkpoint grid does not match the context";
   else if ((int)h.real_bytes != ctx->core->real_bytes())
     bad = "checkpoint precision does not match the context";
-  int sz[4];
-  ctx->core->sizes(sz);
   const int                  g = p.ghost;
   const size_t               nfile = (size_t)(h.nx + 2 * g) * (h.ny + 2 * g) *
-                         (p.dim == 3 ? h.nz + 2 * g : 1) * 8;
+                         (p.dim == 3 ? h.nz + 2 * g : 1) * sz[3];
   std::vector<unsigned char> U, lo;
   if (bad.empty())
   {
@@ -234,10 +312,10 @@ checkpoint_load(mhd_ctx * ctx, const char * path, int reset_time, int * times_sa
     std::vector<unsigned char> fine((size_t)sz[0] * sz[1] * sz[2] * sz[3] * h.real_bytes);
     if (h.real_bytes == 8)
       upscale_state((const double *)U.data(), (double *)fine.data(), p.dim, sz[0], sz[1],
-                    p.dim == 3 ? sz[2] : 1, g, p.nx, p.ny);
+                    p.dim == 3 ? sz[2] : 1, g, p.nx, p.ny, sz[3]);
     else
       upscale_state((const float *)U.data(), (float *)fine.data(), p.dim, sz[0], sz[1],
-                    p.dim == 3 ? sz[2] : 1, g, p.nx, p.ny);
+                    p.dim == 3 ? sz[2] : 1, g, p.nx, p.ny, sz[3]);
     U.swap(fine);
   }
   ctx->core->set_time_origin(reset_time ? 0.0 : h.t);
@@ -311,7 +389,8 @@ extern "C"
     hp.setup(map);
     if (!hp.valid_solver)
     {
-      set_err("[run] solver_name must be MHD_Muscl_2D or MHD_Muscl_3D");
+      set_err("[run] solver_name must be MHD_Muscl_2D, MHD_Muscl_3D, Hydro_Muscl_2D or "
+              "Hydro_Muscl_3D");
       return MHD_ERR_PARSE;
     }
     // back-end options (not in the reference): [gb300] precision = 64|32,
@@ -341,12 +420,13 @@ extern "C"
       return MHD_ERR_INVALID_ARG;
     }
     std::string err;
+    const bool  hydro = p->solver == MHD_SOLVER_HYDRO_MUSCL;
     if (p->precision == MHD_FP32)
-      ctx->core = mhd::create_core_f32(*p, err);
+      ctx->core = hydro ? mhd::create_hydro_core_f32(*p, err) : mhd::create_core_f32(*p, err);
     else if (p->fp_mode == MHD_FP_EXACT)
-      ctx->core = mhd::create_core_f64x(*p, err);
+      ctx->core = hydro ? mhd::create_hydro_core_f64x(*p, err) : mhd::create_core_f64x(*p, err);
     else
-      ctx->core = mhd::create_core_f64(*p, err);
+      ctx->core = hydro ? mhd::create_hydro_core_f64(*p, err) : mhd::create_core_f64(*p, err);
     *out = ctx;
     if (!ctx->core && err.find("out of range") != std::string::npos)
     {
@@ -387,8 +467,9 @@ extern "C"
   {
     if (!p || !U || !validate_params(*p).empty())
       return MHD_ERR_INVALID_ARG;
+    const int    nvar = p->solver == MHD_SOLVER_HYDRO_MUSCL ? p->dim + 2 : 8;
     const size_t n = (size_t)(p->nx + 2 * p->ghost) * (p->ny + 2 * p->ghost) *
-                     (p->dim == 3 ? p->nz + 2 * p->ghost : 1) * 8;
+                     (p->dim == 3 ? p->nz + 2 * p->ghost : 1) * nvar;
     std::memset(U, 0, n * sizeof(double));
     mhd::init_problem_host(*p, U);
     return MHD_OK;
@@ -570,7 +651,7 @@ extern "C"
     h.ny = (uint32_t)p.ny;
     h.nz = (uint32_t)(p.dim == 3 ? p.nz : 1);
     h.ghost = (uint32_t)p.ghost;
-    h.nbvar = 8;
+    h.nbvar = (uint32_t)sz[3];
     h.real_bytes = (uint32_t)rb;
     h.t = t;
     h.dt = dt;
@@ -658,6 +739,9 @@ extern "C"
       const std::string bad = validate_params(p[q]);
       if (!bad.empty())
         return fail(e, MHD_ERR_INVALID_ARG, "problem " + std::to_string(q) + ": " + bad);
+      if (p[q].solver != MHD_SOLVER_MHD_MUSCL)
+        return fail(e, MHD_ERR_INVALID_ARG,
+                    "problem " + std::to_string(q) + ": ensembles run the MHD solver");
       if (p[q].implementation_version != 2)
         return fail(e, MHD_ERR_INVALID_ARG,
                     "problem " + std::to_string(q) + ": ensembles use implementation version 2");

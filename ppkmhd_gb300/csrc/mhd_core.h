@@ -81,6 +81,11 @@ public:
 SolverCore * create_core_f64x(const mhd_params & p, std::string & err);
 SolverCore * create_core_f64(const mhd_params & p, std::string & err);
 SolverCore * create_core_f32(const mhd_params & p, std::string & err);
+// hydro-only MUSCL solver cores (hydro_variant.cu), mhd_params::solver =
+// MHD_SOLVER_HYDRO_MUSCL
+SolverCore * create_hydro_core_f64x(const mhd_params & p, std::string & err);
+SolverCore * create_hydro_core_f64(const mhd_params & p, std::string & err);
+SolverCore * create_hydro_core_f32(const mhd_params & p, std::string & err);
 EnsembleCore * create_ensemble_f64x(const mhd_params * p, int n, std::string & err);
 EnsembleCore * create_ensemble_f64(const mhd_params * p, int n, std::string & err);
 EnsembleCore * create_ensemble_f32(const mhd_params * p, int n, std::string & err);
@@ -96,10 +101,13 @@ const float * mlp_params(const mhd_mlp * m);
 std::string validate_params(const mhd_params & p);
 
 // Initial condition of p.problem in FP64 on the host, LayoutLeft, ghosts
-// included, into a zeroed array (mhd_init.cpp).
+// included, into a zeroed array (mhd_init.cpp; hydro problems in
+// hydro_init.cpp).
 void init_problem_host(const mhd_params & p, double * U);
 // Orszag-Tang initial condition (MHDInitFunctors2D.h:241-389,
 // MHDInitFunctors3D.h:264-415).
 void init_orszag_tang_host(const mhd_params & p, double * U);
+// Initial conditions of the hydro-only solver (hydro_init.cpp).
+void init_hydro_problem_host(const mhd_params & p, double * U);
 
 } // namespace mhd

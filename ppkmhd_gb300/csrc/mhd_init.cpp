@@ -533,6 +533,8 @@ wave(const mhd_params & p, const Mesh & m, double * U)
 void
 init_problem_host(const mhd_params & p, double * U)
 {
+  if (p.solver == MHD_SOLVER_HYDRO_MUSCL)
+    return init_hydro_problem_host(p, U);
   const Mesh m(p);
   switch (p.problem)
   {

@@ -216,8 +216,8 @@ extern "C"
   {
     if (!p || !U_in || !U_out || !dt || U_in == U_out)
       return MHD_ERR_INVALID_ARG;
-    if (!mhd::validate_params(*p).empty() || p->fp_mode != MHD_FP_FAST ||
-        p->implementation_version != 2)
+    if (!mhd::validate_params(*p).empty() || p->solver != MHD_SOLVER_MHD_MUSCL ||
+        p->fp_mode != MHD_FP_FAST || p->implementation_version != 2)
       return MHD_ERR_INVALID_ARG;
     // the reference's finished() test (SolverBase.cpp:195-201): nothing to do
     if (t >= p->tEnd - 1e-14)

@@ -36,6 +36,18 @@ HydroParams::setup(const ConfigMap & map)
     ghostWidth = 3;
     mhdEnabled = true;
   }
+  else if (solver_name == "Hydro_Muscl_2D" || solver_name == "Hydro_Muscl_2D_gpu")
+  {
+    dimType = TWO_D;
+    nbvar = 4;
+    ghostWidth = 2;
+  }
+  else if (solver_name == "Hydro_Muscl_3D" || solver_name == "Hydro_Muscl_3D_gpu")
+  {
+    dimType = THREE_D;
+    nbvar = 5;
+    ghostWidth = 2;
+  }
   else
   {
     std::cerr << "Solver name not valid : " << solver_name << "\n";
@@ -67,20 +79,20 @@ HydroParams::setup(const ConfigMap & map)
   niter_riemann = (int)map.getInteger("hydro", "niter_riemann", 10);
   const std::string rs = map.getString("hydro", "riemann", "approx");
   if (rs == "approx")
-    riemannSolverType = 0;
+    riemannSolverType = MHD_RIEMANN_APPROX;
   else if (rs == "llf")
     riemannSolverType = MHD_RIEMANN_LLF;
   else if (rs == "hll")
     riemannSolverType = MHD_RIEMANN_HLL;
   else if (rs == "hllc")
-    riemannSolverType = 3;
+    riemannSolverType = MHD_RIEMANN_HLLC;
   else if (rs == "hlld")
     riemannSolverType = MHD_RIEMANN_HLLD;
   else
   {
     std::cout << "Riemann Solver specified in parameter file is invalid\n";
     std::cout << "Use the default one : approx\n";
-    riemannSolverType = 0;
+    riemannSolverType = MHD_RIEMANN_APPROX;
   }
 
   implementationVersion = (int)map.getFloat("OTHER", "implementationVersion", 0.0f);
@@ -173,8 +185,31 @@ HydroParams::to_mhd_params(const ConfigMap & map, int precision, int fp_mode) co
   p.tEnd = map.getFloat("run", "tEnd", 0.0f);
   p.tCurrent = map.getFloat("run", "tCurrent", 0.0f);
   p.nStepmax = nStepmax;
-  const std::string problem = map.getString("hydro", "problem", "unknown");
-  p.problem = MHD_PROBLEM_ORSZAG_TANG; // unknown problems default to Orszag-Tang (SolverMHDMuscl.h:700-708)
+  std::string problem = map.getString("hydro", "problem", "unknown");
+  p.solver = mhdEnabled ? MHD_SOLVER_MHD_MUSCL : MHD_SOLVER_HYDRO_MUSCL;
+  if (!mhdEnabled)
+  {
+    // the names SolverHydroMuscl<dim>::init dispatches (SolverHydroMuscl.cpp:
+    // 123-177 in 2D, :202-244 in 3D); any other name runs implode with its
+    // parameters
+    const bool two = dimType == TWO_D;
+    const bool known = problem == "implode" || problem == "blast" ||
+                       problem == "kelvin_helmholtz" || problem == "gresho_vortex" ||
+                       problem == "rayleigh_taylor" || problem == "rising_bubble" ||
+                       problem == "disk" ||
+                       (two && (problem == "four_quadrant" || problem == "isentropic_vortex"));
+    if (!known)
+      problem = "implode";
+  }
+  // unknown problems default to Orszag-Tang in the MHD solver
+  // (SolverMHDMuscl.h:700-708) and to implode in the hydro solver
+  // (SolverHydroMuscl.cpp:170-177)
+  p.problem = mhdEnabled ? MHD_PROBLEM_ORSZAG_TANG : MHD_PROBLEM_IMPLODE;
+  // SolverBase::read_config (SolverBase.cpp:138-141); point gravity (the
+  // disk problem) is marked 2 and refused by the hydro solver
+  p.gravity = map.getBool("gravity", "static", false) ? 1 : 0;
+  if (map.getBool("gravity", "point", false))
+    p.gravity = 2;
   p.ot_kt = map.getFloat("OrszagTang", "kt", 0.0f);
   double * r = p.problem_real;
   int *    n = p.problem_int;
@@ -224,7 +259,7 @@ HydroParams::to_mhd_params(const ConfigMap & map, int precision, int fp_mode) co
     n[2] = (int)map.getInteger("KH", "mode", 2);
     n[3] = map.getBool("KH", "perturbation_rand", false) ? 1 : 0;
   }
-  else if (problem == "rotor")
+  else if (mhdEnabled && problem == "rotor")
   {
     // RotorParams (src/shared/problems/RotorParams.h)
     p.problem = MHD_PROBLEM_ROTOR;
@@ -234,7 +269,7 @@ HydroParams::to_mhd_params(const ConfigMap & map, int precision, int fp_mode) co
     r[3] = map.getFloat("rotor", "p0", 1.0f);
     r[4] = map.getFloat("rotor", "b0", (float)(5.0 / std::sqrt(4 * M_PI)));
   }
-  else if (problem == "field_loop" || problem == "field loop")
+  else if (mhdEnabled && (problem == "field_loop" || problem == "field loop"))
   {
     // FieldLoopParams (src/shared/problems/FieldLoopParams.h)
     p.problem = MHD_PROBLEM_FIELD_LOOP;
@@ -243,7 +278,7 @@ HydroParams::to_mhd_params(const ConfigMap & map, int precision, int fp_mode) co
     r[2] = map.getFloat("FieldLoop", "amplitude", 1.0f);
     r[3] = map.getFloat("FieldLoop", "vflow", 1.0f);
   }
-  else if (problem == "wave")
+  else if (mhdEnabled && problem == "wave")
   {
     // WaveParams (src/shared/problems/WaveParams.h): right eigenvectors of
     // the fast, Alfven, slow and contact waves and the rotated wave vector
@@ -292,6 +327,68 @@ HydroParams::to_mhd_params(const ConfigMap & map, int precision, int fp_mode) co
       r[19] = 0.5;
     }
   }
+  else if (!mhdEnabled && problem == "gresho_vortex")
+  {
+    // GreshoParams (src/shared/problems/GreshoParams.h)
+    p.problem = MHD_PROBLEM_GRESHO_VORTEX;
+    r[0] = map.getFloat("Gresho", "rho0", 1.0f);
+    r[1] = map.getFloat("Gresho", "Ma", 0.1f);
+  }
+  else if (!mhdEnabled && problem == "four_quadrant")
+  {
+    // SolverHydroMuscl<2>::init_four_quadrant (SolverHydroMuscl.cpp:60-82)
+    p.problem = MHD_PROBLEM_FOUR_QUADRANT;
+    n[0] = (int)map.getInteger("riemann2d", "config_number", 0);
+    r[0] = map.getFloat("riemann2d", "x", 0.8f);
+    r[1] = map.getFloat("riemann2d", "y", 0.8f);
+  }
+  else if (!mhdEnabled && problem == "isentropic_vortex")
+  {
+    // IsentropicVortexParams (src/shared/problems/IsentropicVortexParams.h)
+    p.problem = MHD_PROBLEM_ISENTROPIC_VORTEX;
+    const double x0 = map.getFloat("mesh", "xmin", 0.0f), x1 = map.getFloat("mesh", "xmax", 1.0f);
+    const double y0 = map.getFloat("mesh", "ymin", 0.0f), y1 = map.getFloat("mesh", "ymax", 1.0f);
+    r[0] = map.getFloat("isentropic_vortex", "density_ambient", 1.0f);
+    r[1] = map.getFloat("isentropic_vortex", "temperature_ambient", 1.0f);
+    r[2] = map.getFloat("isentropic_vortex", "vx_ambient", 1.0f);
+    r[3] = map.getFloat("isentropic_vortex", "vy_ambient", 1.0f);
+    r[4] = map.getFloat("isentropic_vortex", "center_x", (float)((x0 + x1) / 2));
+    r[5] = map.getFloat("isentropic_vortex", "center_y", (float)((y0 + y1) / 2));
+    r[6] = map.getFloat("isentropic_vortex", "strength", 5.0f);
+  }
+  else if (!mhdEnabled && problem == "rayleigh_taylor")
+  {
+    // RayleighTaylorInstabilityParams (src/shared/problems/RayleighTaylorInstabilityParams.h)
+    p.problem = MHD_PROBLEM_RAYLEIGH_TAYLOR;
+    r[0] = map.getFloat("rayleigh_taylor", "amplitude", 0.01f);
+    r[1] = map.getFloat("rayleigh_taylor", "d0", 1.0f);
+    r[2] = map.getFloat("rayleigh_taylor", "d1", 2.0f);
+    r[3] = map.getFloat("rayleigh_taylor", "gx", 0.0f);
+    r[4] = map.getFloat("rayleigh_taylor", "gy", -0.1f);
+    r[5] = map.getFloat("rayleigh_taylor", "gz", 0.0f);
+    for (int q = 0; q < 3; ++q)
+      p.gravity_field[q] = r[3 + q];
+  }
+  else if (!mhdEnabled && problem == "rising_bubble")
+  {
+    // RisingBubbleParams (src/shared/problems/RisingBubbleParams.h)
+    p.problem = MHD_PROBLEM_RISING_BUBBLE;
+    r[0] = map.getFloat("rising_bubble", "R", 0.1f);
+    r[1] = map.getFloat("rising_bubble", "x0", 0.5f);
+    r[2] = map.getFloat("rising_bubble", "y0", 0.25f);
+    r[3] = map.getFloat("rising_bubble", "z0", 0.5f);
+    r[4] = map.getFloat("rising_bubble", "din", 1.0f);
+    r[5] = map.getFloat("rising_bubble", "dout", 2.0f);
+    r[6] = map.getFloat("rising_bubble", "gx", 0.0f);
+    r[7] = map.getFloat("rising_bubble", "gy", -0.1f);
+    r[8] = map.getFloat("rising_bubble", "gz", 0.0f);
+    for (int q = 0; q < 3; ++q)
+      p.gravity_field[q] = r[6 + q];
+  }
+  else if (!mhdEnabled && problem == "disk")
+    p.problem = -1; // the disk problem needs point-source gravity, which is not built
+  if (p.dim == 2)
+    p.gravity_field[2] = 0.0;
   p.precision = precision;
   p.fp_mode = fp_mode;
   return p;

@@ -66,3 +66,43 @@ def perturb(U, seed: int, amp: float = 0.05):
     U[2:5] += amp * rng.standard_normal(U[2:5].shape) * U[0]
     U[1] += 2 * amp * np.abs(rng.standard_normal(U[1].shape))
     return U
+
+
+def hydro_ini(dim: int = 2, nx: int = 24, ny: int | None = None, nz: int | None = None,
+              problem: str = "implode", riemann: str = "approx", slope_type: str = "2",
+              bc=(3, 3, 3, 3, 3, 3), gamma0: str = "1.4", cfl: str = "0.8", version: int = 0,
+              tend: str = "10.0", nstepmax: int = 1000, gravity: bool = False,
+              mesh: str = "", extra: str = "") -> str:
+    """A .ini for the hydro-only MUSCL solver (Hydro_Muscl_2D/3D)."""
+    ny = nx + 3 if ny is None else ny
+    nz = nx - 2 if nz is None else nz
+    names = ["xmin", "xmax", "ymin", "ymax", "zmin", "zmax"]
+    lines = ["[run]", f"solver_name=Hydro_Muscl_{dim}D", f"tEnd={tend}", f"nStepmax={nstepmax}",
+             "nOutput=0", "nlog=0", "", "[mesh]", f"nx={nx}", f"ny={ny}"]
+    if dim == 3:
+        lines.append(f"nz={nz}")
+    lines += [f"boundary_type_{names[f]}={bc[f]}" for f in range(6 if dim == 3 else 4)]
+    lines += [mesh, "", "[hydro]", f"gamma0={gamma0}", f"cfl={cfl}", f"riemann={riemann}",
+              f"problem={problem}", f"slope_type={slope_type}", "smallr=1e-8", "smallc=1e-8", "",
+              "[OTHER]", f"implementationVersion={version}", ""]
+    if gravity:
+        lines += ["[gravity]", "static=true", ""]
+    return "\n".join(lines) + "\n" + extra
+
+
+def hydro_perturbed(U0, seed: int):
+    """A smooth seeded perturbation of a hydro state: up to 5 % on density
+    and energy, 0.05 on the momenta (the state stays physical)."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    U = U0.copy()
+    grids = np.meshgrid(*[np.linspace(0, 2 * np.pi, n) for n in U.shape[1:]], indexing="ij")
+    for v in range(U.shape[0]):
+        ph = rng.uniform(0, 2 * np.pi, len(grids))
+        wave = np.prod([np.sin((q + 1) * g + p) for q, (g, p) in enumerate(zip(grids, ph))], axis=0)
+        if v in (0, 1):
+            U[v] *= 1.0 + 0.05 * wave
+        else:
+            U[v] += 0.05 * wave
+    return U
