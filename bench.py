@@ -393,6 +393,10 @@ def run_gb300(args):
             variants[tag] = v
             s32.close()
 
+    hydro = None
+    if args.workload == "ot3d_256_fp64" and not args.no_variants and world == 1:
+        hydro = hydro_companion(m, local, 10, cpu=not args.no_cpu_baseline)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
@@ -491,10 +495,129 @@ def run_gb300(args):
         }
         if accuracy is not None:
             out["accuracy"] = accuracy
+        if hydro is not None:
+            out["hydro"] = hydro
         emit(out)
     s.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+HYDRO_WORKLOAD = ("Hydro_Muscl_3D blast with the settings of the reference's "
+                  "settings/test_blast_3D.ini (HLLC, slope_type 2, reflecting walls, gamma0 "
+                  "1.666, cfl 0.8, implementation version 0) at four times its resolution: "
+                  "256 x 192 x 128 interior cells")
+
+
+def hydro_bench_ini(nx: int = 256, ny: int = 192, nz: int = 128) -> str:
+    return f"""[run]
+solver_name=Hydro_Muscl_3D
+tEnd=50.0
+nStepmax=100000
+nOutput=0
+[mesh]
+nx={nx}
+ny={ny}
+nz={nz}
+xmax=2.0
+ymax=1.5
+zmax=1.0
+boundary_type_xmin=1
+boundary_type_xmax=1
+boundary_type_ymin=1
+boundary_type_ymax=1
+boundary_type_zmin=1
+boundary_type_zmax=1
+[hydro]
+gamma0=1.666
+cfl=0.8
+niter_riemann=10
+iorder=2
+slope_type=2
+problem=blast
+riemann=hllc
+[blast]
+density_in=1.0
+density_out=1.2
+[other]
+implementationVersion=0
+"""
+
+
+def hydro_companion(m, local: int, steps: int, cpu: bool):
+    """The hydro-only MUSCL solver (row f4) on HYDRO_WORKLOAD: the three
+    builds device-resident (CUDA events), per-kernel times of the exact
+    build, the exact build against the C oracle (bitwise, 2 iterations of the
+    full grid), the other builds' relative L1 per variable against the exact
+    state after 10 iterations, and the oracle's CPU rate on the same grid."""
+    ini = hydro_bench_ini()
+    out = {"workload": HYDRO_WORKLOAD, "builds": {}}
+    states = {}
+    for tag, prec, mode in (("fp64_exact", 64, m.MHD_FP_EXACT), ("fp64_fast", 64, m.MHD_FP_FAST),
+                            ("fp32", 32, m.MHD_FP_FAST)):
+        p = m.params_from_ini(ini)
+        p.device, p.precision, p.fp_mode = local, prec, mode
+        s = m.MHDSolver(p)
+        s.init_problem()
+        cells, _ = s.cell_counts()
+        s.run(10)
+        states[tag] = m.interior(s.get_state(), ghost=2).astype(np.float64)
+        s.init_problem()
+        s.run_timed(3)
+        ms = s.run_timed(steps)
+        out["builds"][tag] = {"value": cells * steps / (ms / 1e3), "ms_per_step": ms / steps,
+                              "dtype": "f64" if prec == 64 else "f32"}
+        if tag == "fp64_exact":
+            prof = {}
+            for _ in range(3):
+                for name, kms in s.profile_step():
+                    prof.setdefault(name, []).append(kms)
+            out["per_kernel_ms"] = {k: float(np.median(v)) for k, v in prof.items()}
+            s.init_problem()
+            s.run(2)
+            exact2 = m.interior(s.get_state(), ghost=2)
+            U0 = m.initial_state(m.params_from_ini(ini))
+        s.close()
+        out["cells"] = cells
+    ref = states["fp64_exact"]
+    den = np.maximum(np.abs(ref).sum(axis=(1, 2, 3)), 1e-300)
+    for tag in ("fp64_fast", "fp32"):
+        err = np.abs(states[tag] - ref).sum(axis=(1, 2, 3)) / den
+        out["builds"][tag]["rel_l1_vs_exact_per_variable"] = [float(x) for x in err]
+        out["builds"][tag]["accuracy_steps"] = 10
+    ms_exact = out["builds"]["fp64_exact"]["ms_per_step"]
+    hbm_peak, peak_kind = load_peaks()
+    alg = 2 * 5 * 8  # read and write the 5 FP64 conservative variables per cell
+    out["roofline"] = {"bound": "fp64 alu (exact build; see the MHD alu_roofline)",
+                       "algorithmic_bytes_per_cell": alg,
+                       "step_achieved_gbs": alg * out["cells"] / (ms_exact / 1e3) / 1e9,
+                       "hbm_peak_gbs": hbm_peak, "peak_source": f"hbm_gbs of {peak_kind}"}
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+
+    oracle_py.build_oracle()
+    nthreads = os.cpu_count() or 1
+    o = oracle_py.HydroOracleSolver(ini, nthreads=nthreads)
+    o.set_state(U0)
+    t0 = time.perf_counter()
+    o.run(2)
+    el = time.perf_counter() - t0
+    out["accuracy"] = {"steps": 2, "bitwise_equal_exact_vs_oracle": bool(np.array_equal(
+        oracle_py.interior(o.get_state(), 2), exact2)),
+        "reference": "oracle/hydro_oracle.c, bitwise the reference's hydro functors compiled "
+                     "without FMA contraction (tests/test_hydro_oracle.py)"}
+    if cpu:
+        ns = int(min(50, max(2, 8.0 / max(el / 2, 1e-6))))
+        t0 = time.perf_counter()
+        o.run(ns)
+        el = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": out["cells"] * ns / el, "unit": "cell-updates/s",
+                               "cores": nthreads, "kind": "port",
+                               "sample": f"{ns} iterations of the same grid after 2, "
+                                         f"oracle/hydro_oracle.c with {nthreads} OpenMP threads "
+                                         f"({el:.1f} s timed)"}
+    o.close()
+    return out
 
 
 def ensemble_sample(specs):
@@ -587,6 +710,10 @@ def run_ensemble(args):
     alg = 16 * 4
     achieved = alg * cells / (prof[dom] / 1e3) / 1e9
     step_achieved = alg * cells / (step_ms / 1e3) / 1e9
+
+    hydro = None
+    if args.workload == "ot3d_256_fp64" and not args.no_variants and world == 1:
+        hydro = hydro_companion(m, local, 10, cpu=not args.no_cpu_baseline)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -748,6 +875,10 @@ def run_turbulence(args):
     alg = 64
     achieved = alg * cells / (prof[dom] / 1e3) / 1e9
     step_ms = sum(prof.values())
+    hydro = None
+    if args.workload == "ot3d_256_fp64" and not args.no_variants and world == 1:
+        hydro = hydro_companion(m, local, 10, cpu=not args.no_cpu_baseline)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))

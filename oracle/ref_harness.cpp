@@ -606,7 +606,7 @@ extern "C"
                                                { IV, "rho_vy" }, { IW, "rho_vz" }, { IA, "bx" },
                                                { IB, "by" },     { IC, "bz" } };
     const std::string solver = cfg.getString("run", "solver_name", "unknown");
-    if (solver == "MHD_Muscl_2D")
+    if (solver == "MHD_Muscl_2D" || solver == "Hydro_Muscl_2D")
     {
       DataArray2d U("U", params.isize, params.jsize, params.nbvar);
       std::memcpy(U.data(), u, U.size() * sizeof(real_t));
@@ -614,7 +614,7 @@ extern "C"
       ppkMHD::io::save_VTK_2D(U, Uh, params, cfg, params.nbvar, names, iStep, "");
       return 0;
     }
-    if (solver == "MHD_Muscl_3D")
+    if (solver == "MHD_Muscl_3D" || solver == "Hydro_Muscl_3D")
     {
       DataArray3d U("U", params.isize, params.jsize, params.ksize, params.nbvar);
       std::memcpy(U.data(), u, U.size() * sizeof(real_t));

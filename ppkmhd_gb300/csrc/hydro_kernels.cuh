@@ -10,7 +10,8 @@
 //   k_hbound     ghost fill of U_in (periodic / reflecting / outflow)
 //   k_hprim_dt   primitives Q over the whole array + CFL max-reduction
 //   k_hfinalize  dt = cfl / max, clipped to tEnd; dt/dx, dt/dy, dt/dz
-//   k_hslopes    limited slopes S_d of every cell the faces read
+//   k_hslopes    limited slopes S_d and trace source terms of every cell the
+//                faces read
 //   k_hflux      per face: both traced states, gravity predictor, Riemann
 //                solver (approx / LLF / HLL / HLLC), flux * dt/dx stored
 //   k_hupdate    U_out = U_in + flux differences (interior), gravity source
@@ -134,70 +135,71 @@ hprim(const HGrid<R> & G, const R * u, R & c, R * q)
     q[IW] = uz;
 }
 
-// trace_unsplit_2d_along_dir (HydroBaseFunctor2D.h:225-311) /
-// trace_unsplit_3d_along_dir (HydroBaseFunctor3D.h:274-400): the state on
-// the minus (MINUS) or plus face of a cell along direction DIR.  dq[d][v]
-// are the cell's limited slopes, t = dt/dx_DIR.
-template <class R, int DIM, int DIR, bool MINUS>
+// Source terms of the half-step prediction of trace_unsplit_2d_along_dir
+// (HydroBaseFunctor2D.h:225-311) / trace_unsplit_3d_along_dir
+// (HydroBaseFunctor3D.h:274-400): sr0, sp0, su0, sv0[, sw0] of a cell from
+// its primitives q and limited slopes dq[d][v].  They do not depend on the
+// face, so each cell's are computed once (by the slopes stage) for its 2 DIM
+// face states; the expressions are the reference's, so the values are the
+// ones every trace call of the reference recomputes.
+template <class R, int DIM>
 __device__ __forceinline__ void
-htrace(const HGrid<R> & G, const R * q, const R (*dq)[MAXV], R t, R * qf)
+hsources(const HGrid<R> & G, const R * q, const R (*dq)[MAXV], R * src)
 {
   const R r = q[ID], p = q[IP], u = q[IU], v = q[IV];
-  R       sr0, sp0, su0, sv0, sw0 = R(0), w = R(0);
   if constexpr (DIM == 2)
   {
-    sr0 = -u * dq[0][ID] - v * dq[1][ID] - (dq[0][IU] + dq[1][IV]) * r;
-    sp0 = -u * dq[0][IP] - v * dq[1][IP] - (dq[0][IU] + dq[1][IV]) * G.gamma0 * p;
+    src[ID] = -u * dq[0][ID] - v * dq[1][ID] - (dq[0][IU] + dq[1][IV]) * r;
+    src[IP] = -u * dq[0][IP] - v * dq[1][IP] - (dq[0][IU] + dq[1][IV]) * G.gamma0 * p;
     if constexpr (kExactOrder)
     {
-      su0 = -u * dq[0][IU] - v * dq[1][IU] - (dq[0][IP]) / r;
-      sv0 = -u * dq[0][IV] - v * dq[1][IV] - (dq[1][IP]) / r;
+      src[IU] = -u * dq[0][IU] - v * dq[1][IU] - (dq[0][IP]) / r;
+      src[IV] = -u * dq[0][IV] - v * dq[1][IV] - (dq[1][IP]) / r;
     }
     else
     {
       const R ir = rcp(r);
-      su0 = -u * dq[0][IU] - v * dq[1][IU] - dq[0][IP] * ir;
-      sv0 = -u * dq[0][IV] - v * dq[1][IV] - dq[1][IP] * ir;
+      src[IU] = -u * dq[0][IU] - v * dq[1][IU] - dq[0][IP] * ir;
+      src[IV] = -u * dq[0][IV] - v * dq[1][IV] - dq[1][IP] * ir;
     }
   }
   else
   {
-    w = q[IW];
-    sr0 = -u * dq[0][ID] - v * dq[1][ID] - w * dq[2][ID] - (dq[0][IU] + dq[1][IV] + dq[2][IW]) * r;
-    sp0 = -u * dq[0][IP] - v * dq[1][IP] - w * dq[2][IP] -
-          (dq[0][IU] + dq[1][IV] + dq[2][IW]) * G.gamma0 * p;
+    const R w = q[IW];
+    src[ID] =
+      -u * dq[0][ID] - v * dq[1][ID] - w * dq[2][ID] - (dq[0][IU] + dq[1][IV] + dq[2][IW]) * r;
+    src[IP] = -u * dq[0][IP] - v * dq[1][IP] - w * dq[2][IP] -
+              (dq[0][IU] + dq[1][IV] + dq[2][IW]) * G.gamma0 * p;
     if constexpr (kExactOrder)
     {
-      su0 = -u * dq[0][IU] - v * dq[1][IU] - w * dq[2][IU] - (dq[0][IP]) / r;
-      sv0 = -u * dq[0][IV] - v * dq[1][IV] - w * dq[2][IV] - (dq[1][IP]) / r;
-      sw0 = -u * dq[0][IW] - v * dq[1][IW] - w * dq[2][IW] - (dq[2][IP]) / r;
+      src[IU] = -u * dq[0][IU] - v * dq[1][IU] - w * dq[2][IU] - (dq[0][IP]) / r;
+      src[IV] = -u * dq[0][IV] - v * dq[1][IV] - w * dq[2][IV] - (dq[1][IP]) / r;
+      src[IW] = -u * dq[0][IW] - v * dq[1][IW] - w * dq[2][IW] - (dq[2][IP]) / r;
     }
     else
     {
       const R ir = rcp(r);
-      su0 = -u * dq[0][IU] - v * dq[1][IU] - w * dq[2][IU] - dq[0][IP] * ir;
-      sv0 = -u * dq[0][IV] - v * dq[1][IV] - w * dq[2][IV] - dq[1][IP] * ir;
-      sw0 = -u * dq[0][IW] - v * dq[1][IW] - w * dq[2][IW] - dq[2][IP] * ir;
+      src[IU] = -u * dq[0][IU] - v * dq[1][IU] - w * dq[2][IU] - dq[0][IP] * ir;
+      src[IV] = -u * dq[0][IV] - v * dq[1][IV] - w * dq[2][IV] - dq[1][IP] * ir;
+      src[IW] = -u * dq[0][IW] - v * dq[1][IW] - w * dq[2][IW] - dq[2][IP] * ir;
     }
   }
-  const R * d = dq[DIR];
-  if constexpr (MINUS)
+}
+
+// The face state of trace_unsplit_*_along_dir on the minus (MINUS) or plus
+// face of a cell: q -/+ dq_DIR / 2 + src * t / 2 with t = dt/dx_DIR, density
+// floored at smallr.
+template <class R, int DIM, bool MINUS>
+__device__ __forceinline__ void
+htrace(const HGrid<R> & G, const R * q, const R * d, const R * src, R t, R * qf)
+{
+#pragma unroll
+  for (int v = 0; v < DIM + 2; ++v)
   {
-    qf[ID] = r - R(0.5) * d[ID] + sr0 * t * R(0.5);
-    qf[IP] = p - R(0.5) * d[IP] + sp0 * t * R(0.5);
-    qf[IU] = u - R(0.5) * d[IU] + su0 * t * R(0.5);
-    qf[IV] = v - R(0.5) * d[IV] + sv0 * t * R(0.5);
-    if constexpr (DIM == 3)
-      qf[IW] = w - R(0.5) * d[IW] + sw0 * t * R(0.5);
-  }
-  else
-  {
-    qf[ID] = r + R(0.5) * d[ID] + sr0 * t * R(0.5);
-    qf[IP] = p + R(0.5) * d[IP] + sp0 * t * R(0.5);
-    qf[IU] = u + R(0.5) * d[IU] + su0 * t * R(0.5);
-    qf[IV] = v + R(0.5) * d[IV] + sv0 * t * R(0.5);
-    if constexpr (DIM == 3)
-      qf[IW] = w + R(0.5) * d[IW] + sw0 * t * R(0.5);
+    if constexpr (MINUS)
+      qf[v] = q[v] - R(0.5) * d[v] + src[v] * t * R(0.5);
+    else
+      qf[v] = q[v] + R(0.5) * d[v] + src[v] * t * R(0.5);
   }
   qf[ID] = fmax(G.smallr, qf[ID]);
 }
@@ -705,7 +707,8 @@ k_hset_dt(const HGrid<R> G, DevState * st, double dt)
 // ComputeSlopesFunctor2D/3D (HydroRunFunctors2D.h:900-985, 3D:930-1040) with
 // slope_unsplit_hydro_2d/3d (HydroBaseFunctor2D.h:432-525, 3D:411-540) over
 // [g-1, size-g] per axis: S[(d * NVAR + v) * sv + cell]; slope_type 0 gives
-// zero slopes (first order).
+// zero slopes (first order).  The cell's trace source terms follow in planes
+// S[(DIM * NVAR + v) * sv + cell] (hsources).
 template <class R, int DIM>
 __global__ void __launch_bounds__(128)
 k_hslopes(const HGrid<R> G, const R * __restrict__ Q, R * __restrict__ S, const DevState * st)
@@ -718,22 +721,31 @@ k_hslopes(const HGrid<R> G, const R * __restrict__ Q, R * __restrict__ S, const 
     return;
   const int64_t c = hcell(G, i, j, k);
   const int64_t str[3] = { 1, G.sj, G.sk };
+  R             q[MAXV], dq[DIM][MAXV], src[MAXV];
+#pragma unroll
+  for (int v = 0; v < NVAR; ++v)
+    q[v] = Q[c + v * G.sv];
 #pragma unroll
   for (int d = 0; d < DIM; ++d)
 #pragma unroll
     for (int v = 0; v < NVAR; ++v)
     {
       const R * Qv = Q + v * G.sv;
-      R         s = R(0);
+      R         sl = R(0);
       if (G.slope_type != R(0))
       {
         if constexpr (kExactOrder)
-          s = limited_slope(Qv[c], Qv[c + str[d]], Qv[c - str[d]], G.slope_type);
+          sl = limited_slope(q[v], Qv[c + str[d]], Qv[c - str[d]], G.slope_type);
         else
-          s = limited_slope_bits(Qv[c], Qv[c + str[d]], Qv[c - str[d]], G.slope_type);
+          sl = limited_slope_bits(q[v], Qv[c + str[d]], Qv[c - str[d]], G.slope_type);
       }
-      S[(d * NVAR + v) * G.sv + c] = s;
+      dq[d][v] = sl;
+      S[(d * NVAR + v) * G.sv + c] = sl;
     }
+  hsources<R, DIM>(G, q, dq, src);
+#pragma unroll
+  for (int v = 0; v < NVAR; ++v)
+    S[(DIM * NVAR + v) * G.sv + c] = src[v];
 }
 
 // Face flux along direction D of the face at the minus side of every cell
@@ -751,27 +763,24 @@ hflux_face(const HGrid<R> & G, const R * __restrict__ Q, const R * __restrict__ 
   constexpr int NVAR = DIM + 2;
   constexpr int VN = D == 0 ? IU : D == 1 ? IV : IW; // normal velocity
   const int64_t nb = c - (D == 0 ? 1 : D == 1 ? G.sj : G.sk);
-  R             qc[MAXV], qn[MAXV], dqc[DIM][MAXV], dqn[DIM][MAXV];
+  // the cell and its minus neighbour: primitives, slopes along D, sources
+  R qc[MAXV], qn[MAXV], dc[MAXV], dn[MAXV], sc[MAXV], sn[MAXV];
 #pragma unroll
   for (int v = 0; v < NVAR; ++v)
   {
     qc[v] = Q[c + v * G.sv];
     qn[v] = Q[nb + v * G.sv];
+    dc[v] = S[(D * NVAR + v) * G.sv + c];
+    dn[v] = S[(D * NVAR + v) * G.sv + nb];
+    sc[v] = S[(DIM * NVAR + v) * G.sv + c];
+    sn[v] = S[(DIM * NVAR + v) * G.sv + nb];
   }
-#pragma unroll
-  for (int e = 0; e < DIM; ++e)
-#pragma unroll
-    for (int v = 0; v < NVAR; ++v)
-    {
-      dqc[e][v] = S[(e * NVAR + v) * G.sv + c];
-      dqn[e][v] = S[(e * NVAR + v) * G.sv + nb];
-    }
   R tx, ty, tz;
   dt_over_dx(st, tx, ty, tz);
   const R t = D == 0 ? tx : D == 1 ? ty : tz;
   R       qleft[MAXV], qright[MAXV], flux[MAXV];
-  htrace<R, DIM, D, true>(G, qc, dqc, t, qright);
-  htrace<R, DIM, D, false>(G, qn, dqn, t, qleft);
+  htrace<R, DIM, true>(G, qc, dc, sc, t, qright);
+  htrace<R, DIM, false>(G, qn, dn, sn, t, qleft);
   if (G.gravity)
   {
     const R hdt = R(0.5 * st->dt);

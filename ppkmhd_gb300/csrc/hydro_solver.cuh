@@ -46,7 +46,7 @@ public:
   R *             U = nullptr;
   R *             U2 = nullptr;
   R *             Q = nullptr;
-  R *             S = nullptr; // slopes, DIM blocks of NVAR planes
+  R *             S = nullptr; // slopes (DIM blocks of NVAR planes), then trace sources (NVAR)
   R *             F = nullptr; // face fluxes * dt/dx, DIM blocks of NVAR planes
   double *        diag = nullptr;
   DevState *      st = nullptr;
@@ -133,7 +133,7 @@ public:
     HY_CK(cudaMalloc(&U, n * nvar * sizeof(R)));
     HY_CK(cudaMalloc(&U2, n * nvar * sizeof(R)));
     HY_CK(cudaMalloc(&Q, n * nvar * sizeof(R)));
-    HY_CK(cudaMalloc(&S, n * nvar * dim * sizeof(R)));
+    HY_CK(cudaMalloc(&S, n * nvar * (dim + 1) * sizeof(R)));
     HY_CK(cudaMalloc(&F, n * nvar * dim * sizeof(R)));
     HY_CK(cudaMalloc(&diag, (kDiagBlocks * 10 + 16) * sizeof(double)));
     HY_CK(cudaMalloc(&st, sizeof(DevState)));
@@ -141,7 +141,7 @@ public:
     R * b3[] = { U, U2, Q };
     for (R * b : b3)
       HY_CK(cudaMemsetAsync(b, 0, n * nvar * sizeof(R), stream));
-    HY_CK(cudaMemsetAsync(S, 0, n * nvar * dim * sizeof(R), stream));
+    HY_CK(cudaMemsetAsync(S, 0, n * nvar * (dim + 1) * sizeof(R), stream));
     HY_CK(cudaMemsetAsync(F, 0, n * nvar * dim * sizeof(R), stream));
     HY_CK(reset_time_state());
     HY_CK(cudaStreamSynchronize(stream));

@@ -20,6 +20,12 @@ SolverFactory::SolverFactory()
   registerSolver("MHD_Muscl_3D", &SolverMHDMusclGPU<3>::create);
   registerSolver("MHD_Muscl_2D_gpu", &SolverMHDMusclGPU<2>::create);
   registerSolver("MHD_Muscl_3D_gpu", &SolverMHDMusclGPU<3>::create);
+  // the hydro-only MUSCL solver (SolverHydroMuscl<dim> of the reference) runs
+  // through the same context: mhd_params::solver selects the scheme
+  registerSolver("Hydro_Muscl_2D", &SolverMHDMusclGPU<2>::create);
+  registerSolver("Hydro_Muscl_3D", &SolverMHDMusclGPU<3>::create);
+  registerSolver("Hydro_Muscl_2D_gpu", &SolverMHDMusclGPU<2>::create);
+  registerSolver("Hydro_Muscl_3D_gpu", &SolverMHDMusclGPU<3>::create);
 }
 
 void

@@ -40,3 +40,28 @@ def test_vti_bytes_equal_reference_writer(mhdlib, oracle, tmp_path, dim, ascii_)
     assert ref.exists()
     a, b = open(name, "rb").read(), ref.read_bytes()
     assert len(a) == len(b) and a == b
+
+
+@pytest.mark.parametrize("dim,ascii_", [(2, False), (3, True)])
+def test_vti_bytes_equal_reference_writer_hydro(mhdlib, oracle, tmp_path, dim, ascii_):
+    """The same for a hydro-only solver state (dim + 2 variables, ghost 2)."""
+    if not oracle.ref_available(64):
+        pytest.skip("oracle/_ref not built (reference sources absent)")
+    from mhd_cases import hydro_ini
+
+    nx, ny, nz = 11, 8, 6
+    g, nv = 2, dim + 2
+    shape = (nv, ny + 2 * g, nx + 2 * g) if dim == 2 else (nv, nz + 2 * g, ny + 2 * g, nx + 2 * g)
+    U = np.random.default_rng(9 + dim).standard_normal(shape)
+
+    def ini(outdir):
+        return hydro_ini(dim=dim, nx=nx, ny=ny, nz=nz) + (
+            f"\n[output]\noutputDir={outdir}\noutputPrefix=h\n"
+            f"outputVtkAscii={'true' if ascii_ else 'false'}\n")
+
+    mine_dir, ref_dir = tmp_path / "mine", tmp_path / "ref"
+    mine_dir.mkdir()
+    ref_dir.mkdir()
+    name = mhdlib.write_vtk(ini(str(mine_dir)), U, 3)
+    oracle.ref_save_vtk(ini(str(ref_dir)), U, 3)
+    assert open(name, "rb").read() == (ref_dir / "h_0000003.vti").read_bytes()
