@@ -14,6 +14,11 @@ Kelvin-Helmholtz network (gamma0 = 1.4) ``ppkmhd_gb300/data/flux_mlp_kh.npz``.
 ``python -m ppkmhd_gb300.surrogate run --n 96 --steps 3`` runs the
 turbulence state with the network (the case the flux-stage profile uses).
 
+``python -m ppkmhd_gb300.surrogate spec`` trains the specified plain
+15-64-64-7 network on about 2e8 harvested faces and compares it with the
+deployed network on held-out faces (a measurement; torch does that
+training).
+
 Record layout (MHD_SAMPLE_FLOATS = 24 floats): qL[7], qR[7] (rho, vn, vt1,
 vt2, p, Bt1, Bt2, face-normal frame), a (normal B), J (sensor), D[7] (FP64
 central flux minus FP64 HLLD flux), gamma0.
@@ -303,6 +308,175 @@ def run_turbulence(n: int = 96, steps: int = 3, tau: float = 0.01, weights: str 
     return out
 
 
+def _spec_io(records: np.ndarray):
+    """Inputs and targets of the plain 15 -> 64 -> 64 -> 7 network: the 15
+    face values (qL[7], qR[7], a) made dimensionless with the face's own
+    scales (density, velocity, pressure and field of the mean state, as in
+    ``evaluate``) and the 7 dissipation components D divided by the same
+    flux scales (times the sensor value).  Returns (x, y, scale); large sets
+    go through in chunks of 1e7 records."""
+    n = records.shape[0]
+    if n > 10_000_000:
+        x = np.empty((n, 15), np.float32)
+        y = np.empty((n, 7), np.float32)
+        sc = np.empty((n, 7), np.float32)
+        for a0 in range(0, n, 10_000_000):
+            a1 = min(n, a0 + 10_000_000)
+            x[a0:a1], y[a0:a1], sc[a0:a1] = _spec_io(records[a0:a1])
+        return x, y, sc
+    r = records.astype(np.float64)
+    ql, qr, a = r[:, 0:7], r[:, 7:14], r[:, 14]
+    rs = 0.5 * (ql[:, 0] + qr[:, 0])
+    b2l = a ** 2 + ql[:, 5] ** 2 + ql[:, 6] ** 2
+    b2r = a ** 2 + qr[:, 5] ** 2 + qr[:, 6] ** 2
+    Ps = 0.5 * (ql[:, 4] + qr[:, 4]) + 0.25 * (b2l + b2r)
+    vs = np.sqrt(Ps / rs)
+    bs = np.sqrt(Ps)
+    qs = np.stack([rs, vs, vs, vs, Ps, bs, bs], axis=1)
+    x = np.concatenate([ql / qs, qr / qs, (a / bs)[:, None]], axis=1)
+    sJ = np.maximum(r[:, REC_J], 1e-4)
+    sc = np.stack([rs * vs, Ps * vs, Ps, Ps, Ps, bs * vs, bs * vs], axis=1) * sJ[:, None]
+    y = r[:, 16:23] / sc
+    return x.astype(np.float32), y.astype(np.float32), sc
+
+
+def harvest_spec_set(n_target: float = 2e8, seed: int = 17):
+    """Inputs and targets (``_spec_io``) of about n_target smooth face records
+    (J <= 0.1) from FP32 runs of the 3D Orszag-Tang state at 256^3 with a 5 %
+    velocity perturbation, harvested from every face every 25 iterations,
+    and of the 3D turbulence state at 128^3 for the rest.  The records of
+    each harvest are converted and dropped at once (the arrays are filled in
+    place), so the host holds the float32 inputs and targets plus one
+    harvest."""
+    g = "1.6666666666666667"
+    n_target = int(n_target)
+    x = np.empty((n_target, 15), np.float32)
+    y = np.empty((n_target, 7), np.float32)
+    have = 0
+
+    def take(s):
+        nonlocal have
+        rec = smooth(s.harvest(1))
+        k = min(rec.shape[0], n_target - have)
+        x[have:have + k], y[have:have + k], _ = _spec_io(rec[:k])
+        have += k
+
+    ini3 = workloads.ot_ini(3, 256, gamma0=g, precision=32)
+    s = MHDSolver(params_from_ini(ini3))
+    s.init_problem()
+    U = workloads.perturbed_ot_3d(s.get_state().astype(np.float64), seed=seed, amp=0.05,
+                                  gamma0=GAMMA)
+    s.set_state(U.astype(np.float32))
+    del U
+    for _ in range(6):
+        take(s)
+        if have >= n_target:
+            break
+        s.run(25)
+    s.close()
+    if have < n_target:
+        U = workloads.turbulence_3d(128, seed=seed + 7)
+        s = _solver(workloads.ot_ini(3, 128, gamma0=g, precision=32), U)
+        while have < n_target:
+            take(s)
+            s.run(10)
+        s.close()
+    return x, y
+
+
+def compare_spec(n_train: float = 2e8, epochs: int = 3, batch: int = 65536, lr: float = 3e-3,
+                 seed: int = 1, weights: str = DEFAULT_WEIGHTS) -> dict:
+    """The specified surrogate (15 -> 64 -> 64 -> 7, GELU, BF16 weights and
+    activations with FP32 accumulation) trained on about 2e8 harvested face
+    samples, against the deployed 27-64-64-19 network, on held-out faces of
+    another state (the turbulence state at 64^3, another seed).  A
+    measurement only: the plain network is trained with torch on the GPU
+    (autocast BF16), the deployed one is evaluated by the library's own
+    tensor-core forward; both report the relative L1 of the dissipation and
+    of the full flux against HLLD."""
+    import torch
+
+    torch.manual_seed(seed)
+    # keep the host arrays (96 B per sample with one harvest on top) within a
+    # third of the machine's memory
+    mem = os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES")
+    n_train = min(float(n_train), mem / 3 / 96)
+    t0 = time.time()
+    x, y = harvest_spec_set(n_train)
+    t_h = time.time() - t0
+    n = x.shape[0]
+    dev = torch.device("cuda")
+    X = torch.from_numpy(x).to(dev)
+    Y = torch.from_numpy(y).to(dev)
+    del x, y
+    net = torch.nn.Sequential(torch.nn.Linear(15, 64), torch.nn.GELU(), torch.nn.Linear(64, 64),
+                              torch.nn.GELU(), torch.nn.Linear(64, 7)).to(dev)
+    opt = torch.optim.Adam(net.parameters(), lr=lr)
+    steps = epochs * (n // batch)
+    sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, steps, eta_min=lr / 20)
+    t0 = time.time()
+    losses = []
+    for ep in range(epochs):
+        perm = torch.randperm(n, device=dev)
+        tot = 0.0
+        for b in range(n // batch):
+            idx = perm[b * batch:(b + 1) * batch]
+            with torch.autocast("cuda", dtype=torch.bfloat16):
+                loss = torch.mean((net(X[idx]).float() - Y[idx]) ** 2)
+            opt.zero_grad(set_to_none=True)
+            loss.backward()
+            opt.step()
+            sched.step()
+            tot += float(loss.detach())
+        losses.append(tot / max(1, n // batch))
+    t_t = time.time() - t0
+    del X, Y
+    # held-out faces: the turbulence state, another seed
+    U = workloads.turbulence_3d(64, seed=4242)
+    s = _solver(workloads.ot_ini(3, 64, gamma0="1.6666666666666667", precision=32), U)
+    test = smooth(s.harvest(1))
+    s.run(20)
+    test = np.concatenate([test, smooth(s.harvest(1))], axis=0)
+    s.close()
+    xt, yt, sct = _spec_io(test)
+    with torch.no_grad(), torch.autocast("cuda", dtype=torch.bfloat16):
+        yp = net(torch.from_numpy(xt).to(dev)).float().cpu().numpy().astype(np.float64)
+    D = test[:, 16:23].astype(np.float64)
+    Dp = yp * sct
+    deployed = evaluate(FluxMLP.load(weights), test)
+
+    def flux_err(Dpred):
+        # the full flux error relative to HLLD: central flux minus D, as evaluate()
+        r = test.astype(np.float64)
+        ql, qr, a, g0 = r[:, 0:7], r[:, 7:14], r[:, 14], r[:, 23]
+
+        def flux(q):
+            rr, u, v, w, p, b, c = (q[:, i] for i in range(7))
+            B2 = a ** 2 + b ** 2 + c ** 2
+            Pt = p + 0.5 * B2
+            E = p / (g0 - 1) + 0.5 * rr * (u * u + v * v + w * w) + 0.5 * B2
+            vB = u * a + v * b + w * c
+            return np.stack([rr * u, (E + Pt) * u - a * vB, rr * u * u + Pt - a * a,
+                             rr * u * v - a * b, rr * u * w - a * c, b * u - a * v,
+                             c * u - a * w], axis=1)
+
+        Fc = 0.5 * (flux(ql) + flux(qr))
+        Fh = Fc - D
+        return (np.abs((Fc - Dpred) - Fh).sum(0) / np.maximum(np.abs(Fh).sum(0), 1e-300)).tolist()
+
+    return {
+        "spec_network": "15-64-64-7 GELU, BF16 autocast, FP32 accumulation (torch, measurement)",
+        "train_samples": int(n), "epochs": epochs, "batch": batch, "harvest_s": t_h,
+        "train_s": t_t, "loss_history": losses, "test_samples": int(test.shape[0]),
+        "spec": {"rel_l1_dissipation": (np.abs(Dp - D).sum(0) /
+                                        np.maximum(np.abs(D).sum(0), 1e-300)).tolist(),
+                 "rel_l1_flux": flux_err(Dp),
+                 "macs_per_face": 15 * 64 + 64 * 64 + 64 * 7},
+        "deployed": {k: deployed[k] for k in ("rel_l1_dissipation", "rel_l1_flux", "samples")},
+        "deployed_macs_per_face": 32 * 64 + 64 * 64 + 64 * 24,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -319,7 +493,19 @@ def main():
     t.add_argument("--seed", type=int, default=1)
     t.add_argument("--weight-power", type=float, default=1.0)
     t.add_argument("--workload", choices=("ot", "kh"), default="ot")
+    c = sub.add_parser("spec", help="the specified 15-64-64-7 network on ~2e8 samples vs the "
+                                    "deployed one (measurement)")
+    c.add_argument("--samples", type=float, default=2e8)
+    c.add_argument("--epochs", type=int, default=3)
+    c.add_argument("--out", default=None)
     a = ap.parse_args()
+    if a.cmd == "spec":
+        res = compare_spec(a.samples, a.epochs)
+        txt = json.dumps(res, indent=1)
+        if a.out:
+            with open(a.out, "w") as f:
+                f.write(txt)
+        print(txt)
     if a.cmd == "run":
         used, total = run_turbulence(a.n, a.steps, a.tau)
         print(json.dumps({"faces_network": used, "faces_total": total}))
