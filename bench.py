@@ -566,7 +566,8 @@ def hydro_companion(m, local: int, steps: int, cpu: bool):
         s.run_timed(3)
         ms = s.run_timed(steps)
         out["builds"][tag] = {"value": cells * steps / (ms / 1e3), "ms_per_step": ms / steps,
-                              "dtype": "f64" if prec == 64 else "f32"}
+                              "dtype": "f64" if prec == 64 else "f32",
+                              "form": "fused tile kernel" if s.fused else "stage kernels"}
         if tag == "fp64_exact":
             prof = {}
             for _ in range(3):

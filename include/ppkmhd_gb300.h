@@ -217,6 +217,20 @@ int mhd_step_host(mhd_ctx *ctx, const void *U_in, void *U_out, int layout, int r
  * No counterpart in the reference, which copies no state per step. */
 int mhd_set_host_slabs(mhd_ctx *ctx, int nslabs);
 
+/* Hydro solver: the form of an iteration.  fused = 1 (the default): the plain
+ * form fused into one tile kernel per iteration after the CFL reduction
+ * (k_hdt + k_hfused): each block loads a tile of the state with two halo
+ * layers and computes primitives, slopes, trace sources, face fluxes and the
+ * update in shared memory, writing only the new state to HBM.  fused = 0:
+ * the stage kernels, which store primitives, slopes and fluxes in HBM.  Both
+ * give the same state bit for bit in the MHD_FP_EXACT build (the FMA builds
+ * contract each kernel's expressions independently: round-off differences).
+ * Without this call the first stepping call times one iteration of each form
+ * on the current state and keeps the faster.  The MHD solver has the stage
+ * form only (fused = 1 returns MHD_ERR_INVALID_ARG). */
+int mhd_set_fused(mhd_ctx *ctx, int fused);
+int mhd_get_fused(mhd_ctx *ctx, int *fused);
+
 /* t, the dt of the last computed CFL condition, and the iteration count
  * (SolverBase m_t, m_dt, m_iteration).  Synchronises the stream. */
 int mhd_time(mhd_ctx *ctx, double *t, double *dt, int *iteration);

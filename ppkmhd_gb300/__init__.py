@@ -115,6 +115,8 @@ SIGNATURES = {
     "mhd_run": (ctypes.c_int, [_vp, ctypes.c_int, _ip]),
     "mhd_step_host": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int]),
     "mhd_set_host_slabs": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "mhd_set_fused": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "mhd_get_fused": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int)]),
     "mhd_time": (ctypes.c_int, [_vp, _dp, _dp, _ip]),
     "mhd_diagnostics": (ctypes.c_int, [_vp, _dp, _dp, _dp]),
     "mhd_run_timed": (ctypes.c_int, [_vp, ctypes.c_int, _fp]),
@@ -336,6 +338,16 @@ class MHDSolver:
     def set_host_slabs(self, n: int):
         """Slab count of step_host (0 = automatic, 1 = no copy/compute overlap)."""
         self._check(lib().mhd_set_host_slabs(self.h, int(n)))
+
+    def set_fused(self, fused: bool):
+        """Hydro solver: fused tile kernel (default) or stage kernels."""
+        self._check(lib().mhd_set_fused(self.h, int(bool(fused))))
+
+    @property
+    def fused(self) -> bool:
+        v = ctypes.c_int()
+        self._check(lib().mhd_get_fused(self.h, ctypes.byref(v)))
+        return bool(v.value)
 
     def time(self):
         t, dt, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()

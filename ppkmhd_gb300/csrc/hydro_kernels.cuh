@@ -29,6 +29,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include "mhd_kernels.cuh"
@@ -519,6 +520,108 @@ hriemann(const HGrid<R> & G, const R * ql, const R * qr, R * flux)
 }
 
 // ---------------------------------------------------------------- kernels
+// The CFL rate of one interior cell: ComputeDtFunctor2D/3D
+// (HydroRunFunctors2D.h:13-82, 3D:14-88), sum_d (c + |v_d|) / dx_d, or with
+// static gravity ComputeDtGravityFunctor2D/3D (2D:84-175, 3D:90-190); a NaN
+// rate counts as 0 (fmax ignores NaN operands).
+template <class R, int DIM>
+__device__ __forceinline__ R
+hrate(const HGrid<R> & G, const R * q, R cs)
+{
+  R val;
+  if (G.gravity)
+  {
+    R velocity = R(0);
+    velocity += cs + fabs(q[IU]);
+    velocity += cs + fabs(q[IV]);
+    if constexpr (DIM == 3)
+      velocity += cs + fabs(q[IW]);
+    R kk = fabs(G.grav[0]) + fabs(G.grav[1]);
+    if constexpr (DIM == 3)
+      kk = kk + fabs(G.grav[2]);
+    kk *= hdiv(R(G.cfl) * R(G.dxg), velocity * velocity);
+    kk = fmax(kk, R(1e-4));
+    velocity *= hdiv(kk, hsqrt(R(1) + R(2) * kk) - R(1));
+    if constexpr (kExactOrder)
+      val = qdiv(velocity, R(G.dxg), R(G.idxg));
+    else
+      val = velocity * R(G.idxg);
+  }
+  else
+  {
+    const R vx = cs + fabs(q[IU]);
+    const R vy = cs + fabs(q[IV]);
+    if constexpr (kExactOrder)
+    {
+      if constexpr (DIM == 3)
+      {
+        const R vz = cs + fabs(q[IW]);
+        val = qdiv(vx, R(G.dx), R(G.idx)) + qdiv(vy, R(G.dy), R(G.idy)) +
+              qdiv(vz, R(G.dz), R(G.idz));
+      }
+      else
+        val = qdiv(vx, R(G.dx), R(G.idx)) + qdiv(vy, R(G.dy), R(G.idy));
+    }
+    else
+    {
+      if constexpr (DIM == 3)
+        val = vx * R(G.idx) + vy * R(G.idy) + (cs + fabs(q[IW])) * R(G.idz);
+      else
+        val = vx * R(G.idx) + vy * R(G.idy);
+    }
+  }
+  return (val >= R(0)) ? val : R(0);
+}
+
+// U_out of one interior cell: the flux additions in the reference's order
+// (xf/xp: the flux * dt/dx of the cell's minus and plus faces per direction
+// and variable), then the gravity source term (GravitySourceTermFunctor2D,
+// HydroRunFunctors2D.h:1262-1340, new density floored at smallr; 3D,
+// 3D:1440-1510, not floored).
+template <class R, int DIM>
+__device__ __forceinline__ void
+hupdate_cell(const HGrid<R> & G, const DevState * st, const R * uin, const R (*fm)[MAXV],
+             const R (*fp)[MAXV], R * u)
+{
+#pragma unroll
+  for (int v = 0; v < DIM + 2; ++v)
+  {
+    R x = uin[v];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+    {
+      x = rn_add(x, fm[d][v]);
+      x = rn_sub(x, fp[d][v]);
+    }
+    u[v] = x;
+  }
+  if (G.gravity)
+  {
+    const R rhoOld = uin[ID];
+    const R rhoNew = DIM == 2 ? fmax(G.smallr, u[ID]) : u[ID];
+    R       rhou = u[IU], rhov = u[IV], rhow = DIM == 3 ? u[IW] : R(0);
+    R       ekin_old, ekin_new;
+    if constexpr (DIM == 3)
+      ekin_old = hdiv(R(0.5) * (rhou * rhou + rhov * rhov + rhow * rhow), rhoNew);
+    else
+      ekin_old = hdiv(R(0.5) * (rhou * rhou + rhov * rhov), rhoNew);
+    const R hdt = R(0.5 * st->dt);
+    rhou += hdt * G.grav[0] * (rhoOld + rhoNew);
+    rhov += hdt * G.grav[1] * (rhoOld + rhoNew);
+    if constexpr (DIM == 3)
+      rhow += hdt * G.grav[2] * (rhoOld + rhoNew);
+    u[IU] = rhou;
+    u[IV] = rhov;
+    if constexpr (DIM == 3)
+      u[IW] = rhow;
+    if constexpr (DIM == 3)
+      ekin_new = hdiv(R(0.5) * (rhou * rhou + rhov * rhov + rhow * rhow), rhoNew);
+    else
+      ekin_new = hdiv(R(0.5) * (rhou * rhou + rhov * rhov), rhoNew);
+    u[IP] += (ekin_new - ekin_old);
+  }
+}
+
 
 // Ghost fill.  The reference fills the X faces (over the full j, k range),
 // then Y, then Z (MakeBoundariesFunctor2D/3D, BoundariesFunctors.h:18-530;
@@ -602,48 +705,7 @@ k_hprim_dt(const HGrid<R> G, const R * __restrict__ U, R * __restrict__ Q, DevSt
                           (DIM == 2 || (k >= g && k < G.nz + g));
     if (interior)
     {
-      R val;
-      if (G.gravity)
-      {
-        R velocity = R(0);
-        velocity += cs + fabs(q[IU]);
-        velocity += cs + fabs(q[IV]);
-        if constexpr (DIM == 3)
-          velocity += cs + fabs(q[IW]);
-        R kk = fabs(G.grav[0]) + fabs(G.grav[1]);
-        if constexpr (DIM == 3)
-          kk = kk + fabs(G.grav[2]);
-        kk *= hdiv(R(G.cfl) * R(G.dxg), velocity * velocity);
-        kk = fmax(kk, R(1e-4));
-        velocity *= hdiv(kk, hsqrt(R(1) + R(2) * kk) - R(1));
-        val = qdiv(velocity, R(G.dxg), R(G.idxg));
-        if constexpr (!kExactOrder)
-          val = velocity * R(G.idxg);
-      }
-      else
-      {
-        const R vx = cs + fabs(q[IU]);
-        const R vy = cs + fabs(q[IV]);
-        if constexpr (kExactOrder)
-        {
-          if constexpr (DIM == 3)
-          {
-            const R vz = cs + fabs(q[IW]);
-            val = qdiv(vx, R(G.dx), R(G.idx)) + qdiv(vy, R(G.dy), R(G.idy)) +
-                  qdiv(vz, R(G.dz), R(G.idz));
-          }
-          else
-            val = qdiv(vx, R(G.dx), R(G.idx)) + qdiv(vy, R(G.dy), R(G.idy));
-        }
-        else
-        {
-          if constexpr (DIM == 3)
-            val = vx * R(G.idx) + vy * R(G.idy) + (cs + fabs(q[IW])) * R(G.idz);
-          else
-            val = vx * R(G.idx) + vy * R(G.idy);
-        }
-      }
-      rate = (val >= R(0)) ? val : R(0); // fmax drops a NaN operand
+      rate = hrate<R, DIM>(G, q, cs);
       bad = !(u[ID] > R(0)) || !isfinite(u[IP]);
     }
   }
@@ -755,27 +817,17 @@ k_hslopes(const HGrid<R> G, const R * __restrict__ Q, R * __restrict__ S, const 
 // face, left state = the minus neighbour traced to its plus face, the gravity
 // predictor 0.5 dt g on both, the normal velocity swapped into IU, the
 // Riemann solver, the flux swapped back and scaled by dt/dx_D.
+// The flux of one face along D from the register copies of its two cells:
+// right cell (primitives qc, slopes along D dc, sources sc) and its minus
+// neighbour (qn, dn, sn); returns flux * t, t = dt/dx_D.
 template <class R, int DIM, int D>
 __device__ __forceinline__ void
-hflux_face(const HGrid<R> & G, const R * __restrict__ Q, const R * __restrict__ S,
-           R * __restrict__ F, const DevState * st, int64_t c)
+hface_flux(const HGrid<R> & G, const DevState * st, const R * qc, const R * dc, const R * sc,
+           const R * qn, const R * dn, const R * sn, R * out)
 {
   constexpr int NVAR = DIM + 2;
   constexpr int VN = D == 0 ? IU : D == 1 ? IV : IW; // normal velocity
-  const int64_t nb = c - (D == 0 ? 1 : D == 1 ? G.sj : G.sk);
-  // the cell and its minus neighbour: primitives, slopes along D, sources
-  R qc[MAXV], qn[MAXV], dc[MAXV], dn[MAXV], sc[MAXV], sn[MAXV];
-#pragma unroll
-  for (int v = 0; v < NVAR; ++v)
-  {
-    qc[v] = Q[c + v * G.sv];
-    qn[v] = Q[nb + v * G.sv];
-    dc[v] = S[(D * NVAR + v) * G.sv + c];
-    dn[v] = S[(D * NVAR + v) * G.sv + nb];
-    sc[v] = S[(DIM * NVAR + v) * G.sv + c];
-    sn[v] = S[(DIM * NVAR + v) * G.sv + nb];
-  }
-  R tx, ty, tz;
+  R             tx, ty, tz;
   dt_over_dx(st, tx, ty, tz);
   const R t = D == 0 ? tx : D == 1 ? ty : tz;
   R       qleft[MAXV], qright[MAXV], flux[MAXV];
@@ -806,7 +858,32 @@ hflux_face(const HGrid<R> & G, const R * __restrict__ Q, const R * __restrict__ 
     swap_vals(flux[IU], flux[VN]);
 #pragma unroll
   for (int v = 0; v < NVAR; ++v)
-    F[(D * NVAR + v) * G.sv + c] = flux[v] * t;
+    out[v] = flux[v] * t;
+}
+
+template <class R, int DIM, int D>
+__device__ __forceinline__ void
+hflux_face(const HGrid<R> & G, const R * __restrict__ Q, const R * __restrict__ S,
+           R * __restrict__ F, const DevState * st, int64_t c)
+{
+  constexpr int NVAR = DIM + 2;
+  const int64_t nb = c - (D == 0 ? 1 : D == 1 ? G.sj : G.sk);
+  // the cell and its minus neighbour: primitives, slopes along D, sources
+  R qc[MAXV], qn[MAXV], dc[MAXV], dn[MAXV], sc[MAXV], sn[MAXV], f[MAXV];
+#pragma unroll
+  for (int v = 0; v < NVAR; ++v)
+  {
+    qc[v] = Q[c + v * G.sv];
+    qn[v] = Q[nb + v * G.sv];
+    dc[v] = S[(D * NVAR + v) * G.sv + c];
+    dn[v] = S[(D * NVAR + v) * G.sv + nb];
+    sc[v] = S[(DIM * NVAR + v) * G.sv + c];
+    sn[v] = S[(DIM * NVAR + v) * G.sv + nb];
+  }
+  hface_flux<R, DIM, D>(G, st, qc, dc, sc, qn, dn, sn, f);
+#pragma unroll
+  for (int v = 0; v < NVAR; ++v)
+    F[(D * NVAR + v) * G.sv + c] = f[v];
 }
 
 // grid (faces / 128, DIM): blockIdx.y is the direction
@@ -857,48 +934,293 @@ k_hupdate(const HGrid<R> G, const R * __restrict__ Uin, R * __restrict__ Uout,
     return;
   }
   const int64_t str[3] = { 1, G.sj, G.sk };
-  R             u[MAXV];
+  R             uin[MAXV], u[MAXV], fm[DIM][MAXV], fp[DIM][MAXV];
 #pragma unroll
   for (int v = 0; v < NVAR; ++v)
   {
-    R x = Uin[c + v * G.sv];
+    uin[v] = Uin[c + v * G.sv];
 #pragma unroll
     for (int d = 0; d < DIM; ++d)
     {
       const R * Fd = F + (d * NVAR + v) * G.sv;
-      x = rn_add(x, Fd[c]);
-      x = rn_sub(x, Fd[c + str[d]]);
+      fm[d][v] = Fd[c];
+      fp[d][v] = Fd[c + str[d]];
     }
-    u[v] = x;
   }
-  if (G.gravity)
-  {
-    const R rhoOld = Uin[c + ID * G.sv];
-    const R rhoNew = DIM == 2 ? fmax(G.smallr, u[ID]) : u[ID];
-    R       rhou = u[IU], rhov = u[IV], rhow = DIM == 3 ? u[IW] : R(0);
-    R       ekin_old, ekin_new;
-    if constexpr (DIM == 3)
-      ekin_old = hdiv(R(0.5) * (rhou * rhou + rhov * rhov + rhow * rhow), rhoNew);
-    else
-      ekin_old = hdiv(R(0.5) * (rhou * rhou + rhov * rhov), rhoNew);
-    const R hdt = R(0.5 * st->dt);
-    rhou += hdt * G.grav[0] * (rhoOld + rhoNew);
-    rhov += hdt * G.grav[1] * (rhoOld + rhoNew);
-    if constexpr (DIM == 3)
-      rhow += hdt * G.grav[2] * (rhoOld + rhoNew);
-    u[IU] = rhou;
-    u[IV] = rhov;
-    if constexpr (DIM == 3)
-      u[IW] = rhow;
-    if constexpr (DIM == 3)
-      ekin_new = hdiv(R(0.5) * (rhou * rhou + rhov * rhov + rhow * rhow), rhoNew);
-    else
-      ekin_new = hdiv(R(0.5) * (rhou * rhou + rhov * rhov), rhoNew);
-    u[IP] += (ekin_new - ekin_old);
-  }
+  hupdate_cell<R, DIM>(G, st, uin, fm, fp, u);
 #pragma unroll
   for (int v = 0; v < NVAR; ++v)
     Uout[c + v * G.sv] = u[v];
+}
+
+// ---------------------------------------------------------------- fused form
+
+// The CFL reduction of the fused form (no primitive array is written): the
+// rates of the interior cells as k_hprim_dt computes them; ghost cells of
+// U_in, just filled by k_hbound, are copied to U_out (the reference's
+// deep_copy(data_out, data_in) of the ghost layers; the tile kernel writes
+// the interior).
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+k_hdt(const HGrid<R> G, const R * __restrict__ U, R * __restrict__ Uout, DevState * st, int force)
+{
+  if (!force && step_finished(st))
+    return;
+  constexpr int NVAR = DIM + 2;
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  R             rate = R(0);
+  bool          bad = false;
+  int           i, j, k;
+  if (box_cell(G.box[BOX_ALL], idx, i, j, k))
+  {
+    const int64_t c = hcell(G, i, j, k);
+    const int     g = G.g;
+    const bool    interior = i >= g && i < G.nx + g && j >= g && j < G.ny + g &&
+                          (DIM == 2 || (k >= g && k < G.nz + g));
+    if (interior)
+    {
+      R u[MAXV], q[MAXV], cs;
+#pragma unroll
+      for (int v = 0; v < NVAR; ++v)
+        u[v] = U[c + v * G.sv];
+      hprim<R, DIM>(G, u, cs, q);
+      rate = hrate<R, DIM>(G, q, cs);
+      bad = !(u[ID] > R(0)) || !isfinite(u[IP]);
+    }
+    else if (Uout)
+    {
+#pragma unroll
+      for (int v = 0; v < NVAR; ++v)
+        Uout[c + v * G.sv] = U[c + v * G.sv];
+    }
+  }
+  __shared__ R red[32];
+  rate = warp_max(rate);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0)
+    red[wid] = rate;
+  if (__syncthreads_or(bad) && threadIdx.x == 0)
+    atomicOr(&st->status, STATUS_NUMERIC);
+  if (wid == 0)
+  {
+    rate = lane < (int)(blockDim.x >> 5) ? red[lane] : R(0);
+    rate = warp_max(rate);
+    const unsigned long long rb = (unsigned long long)__double_as_longlong((double)rate);
+    if (lane == 0 && rate > R(0) && rb > *(volatile unsigned long long *)&st->invdt_bits)
+      atomicMax(&st->invdt_bits, rb);
+  }
+}
+
+// Tile shape of the fused form: TX x TY x TZ interior cells per block (TZ = 1
+// in 2D), chosen so that the block's shared-memory working set (below) fits
+// in 227 KB.
+template <class R, int DIM>
+struct HTile
+{
+  static constexpr int TX = DIM == 2 ? 32 : (sizeof(R) == 4 ? 16 : 8);
+  static constexpr int TY = DIM == 2 ? 16 : 8;
+  static constexpr int TZ = DIM == 2 ? 1 : 4;
+  static constexpr int NVAR = DIM + 2;
+  // primitives over the tile and 2 halo layers
+  static constexpr int MX = TX + 4, MY = TY + 4, MZ = DIM == 2 ? 1 : TZ + 4;
+  static constexpr int NM = MX * MY * MZ;
+  // slopes and sources over the tile and 1 halo layer
+  static constexpr int SX = TX + 2, SY = TY + 2, SZ = DIM == 2 ? 1 : TZ + 2;
+  static constexpr int NS = SX * SY * SZ;
+  static constexpr int NSC = NVAR; // the trace sources (slopes are recomputed per face)
+  // faces along d of the tile: one extra layer along d
+  static constexpr int NF0 = (TX + 1) * TY * TZ;
+  static constexpr int NF1 = TX * (TY + 1) * TZ;
+  static constexpr int NF2 = DIM == 2 ? 0 : TX * TY * (TZ + 1);
+  static constexpr int NF = NF0 + NF1 + NF2;
+  static constexpr int THREADS = 256;
+  static constexpr size_t SMEM = sizeof(R) * ((size_t)NM * NVAR + (size_t)NS * NSC + (size_t)NF * NVAR);
+};
+
+// One whole iteration but the CFL reduction for one tile of interior cells
+// (the plain form fused: primitives, slopes, trace sources, face fluxes,
+// update), every intermediate in shared memory:
+//   1. primitives of the tile and 2 halo layers, from U_in (ghost cells
+//      filled by k_hbound) — ConvertToPrimitivesFunctor;
+//   2. trace source terms of the tile and 1 halo layer (from the limited
+//      slopes of ComputeSlopesFunctor, kept in registers);
+//   3. the flux * dt/dx of every face of the tile's cells (both faces of the
+//      boundary layer), the two cells' slopes along the face normal taken
+//      again from the primitives — ComputeAndStoreFluxes /
+//      ComputeTraceAndFluxes;
+//   4. the update of the tile's cells, gravity source included, written to
+//      U_out — UpdateFunctor / UpdateDirFunctor, GravitySourceTermFunctor.
+// Each value is computed by the same device functions from the same
+// operands as in the unfused kernels, so U_out is bitwise theirs; halo cells
+// are recomputed by neighbouring tiles instead of being written to and read
+// back from HBM.  Loads along x are coalesced (i fastest in shared memory as
+// in HBM).
+template <class R, int DIM>
+__global__ void __launch_bounds__(HTile<R, DIM>::THREADS)
+k_hfused(const HGrid<R> G, const R * __restrict__ U, R * __restrict__ Uout, const DevState * st)
+{
+  using T = HTile<R, DIM>;
+  constexpr int NVAR = T::NVAR;
+  if (step_finished(st))
+    return;
+  extern __shared__ __align__(16) unsigned char hsm_raw[];
+  R * Qs = reinterpret_cast<R *>(hsm_raw);       // [NVAR][NM]
+  R * Ss = Qs + (size_t)NVAR * T::NM;             // [NSC][NS]
+  R * Fs = Ss + (size_t)T::NSC * T::NS;           // [NVAR][NF]
+  const int g = G.g;
+  const int i0 = g + blockIdx.x * T::TX, j0 = g + blockIdx.y * T::TY;
+  const int k0 = DIM == 3 ? g + blockIdx.z * T::TZ : 0;
+  const int tid = threadIdx.x;
+
+  // 1. primitives over global [i0-2, i0+TX+2) x ... (inside the array)
+  for (int m = tid; m < T::NM; m += T::THREADS)
+  {
+    const int a = m % T::MX, b = (m / T::MX) % T::MY, cz = m / (T::MX * T::MY);
+    const int i = i0 - 2 + a, j = j0 - 2 + b, k = DIM == 3 ? k0 - 2 + cz : 0;
+    R         q[MAXV];
+    if (i < G.isize && j < G.jsize && k < G.ksize)
+    {
+      const int64_t c = hcell(G, i, j, k);
+      R             u[MAXV], cs;
+#pragma unroll
+      for (int v = 0; v < NVAR; ++v)
+        u[v] = U[c + v * G.sv];
+      hprim<R, DIM>(G, u, cs, q);
+    }
+    else
+    {
+      // beyond the array (a partial last tile): a neutral state that only
+      // cells outside the interior read
+#pragma unroll
+      for (int v = 0; v < NVAR; ++v)
+        q[v] = (v == ID || v == IP) ? R(1) : R(0);
+    }
+#pragma unroll
+    for (int v = 0; v < NVAR; ++v)
+      Qs[v * T::NM + m] = q[v];
+  }
+  __syncthreads();
+
+  // 2. slopes and sources over the tile and 1 halo layer
+  constexpr int mstr[3] = { 1, T::MX, T::MX * T::MY };
+  for (int sidx = tid; sidx < T::NS; sidx += T::THREADS)
+  {
+    const int a = sidx % T::SX, b = (sidx / T::SX) % T::SY, cz = sidx / (T::SX * T::SY);
+    const int m = (a + 1) + T::MX * ((b + 1) + T::MY * (DIM == 3 ? cz + 1 : 0));
+    R         q[MAXV], dq[DIM][MAXV], src[MAXV];
+#pragma unroll
+    for (int v = 0; v < NVAR; ++v)
+      q[v] = Qs[v * T::NM + m];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+#pragma unroll
+      for (int v = 0; v < NVAR; ++v)
+      {
+        R sl = R(0);
+        if (G.slope_type != R(0))
+        {
+          const R qp = Qs[v * T::NM + m + mstr[d]], qm = Qs[v * T::NM + m - mstr[d]];
+          if constexpr (kExactOrder)
+            sl = limited_slope(q[v], qp, qm, G.slope_type);
+          else
+            sl = limited_slope_bits(q[v], qp, qm, G.slope_type);
+        }
+        dq[d][v] = sl;
+      }
+    hsources<R, DIM>(G, q, dq, src);
+#pragma unroll
+    for (int v = 0; v < NVAR; ++v)
+      Ss[v * T::NS + sidx] = src[v];
+  }
+  __syncthreads();
+
+  // 3. face fluxes: faces of direction d of the tile's cells, one extra
+  // layer along d (the plus faces of the last cells)
+  auto face_dir = [&](auto dtag) {
+    constexpr int D = decltype(dtag)::value;
+    constexpr int FX = T::TX + (D == 0), FY = T::TY + (D == 1), FZ = T::TZ + (D == 2);
+    constexpr int NFD = FX * FY * FZ;
+    constexpr int off = D == 0 ? 0 : D == 1 ? T::NF0 : T::NF0 + T::NF1;
+    constexpr int sstr[3] = { 1, T::SX, T::SX * T::SY };
+    for (int f = tid; f < NFD; f += T::THREADS)
+    {
+      const int a = f % FX, b = (f / FX) % FY, cz = f / (FX * FY);
+      // the face's right cell in the slopes box and in the primitives box
+      const int sc_ = (a + 1) + T::SX * ((b + 1) + T::SY * (DIM == 3 ? cz + 1 : 0));
+      const int mc = (a + 2) + T::MX * ((b + 2) + T::MY * (DIM == 3 ? cz + 2 : 0));
+      const int sn_ = sc_ - sstr[D], mn = mc - mstr[D];
+      R         qc[MAXV], qn[MAXV], dc[MAXV], dn[MAXV], scv[MAXV], snv[MAXV], fl[MAXV];
+#pragma unroll
+      for (int v = 0; v < NVAR; ++v)
+      {
+        const R * Qv = Qs + v * T::NM;
+        qc[v] = Qv[mc];
+        qn[v] = Qv[mn];
+        // the slopes along D of both cells again (the same limiter on the
+        // same primitives as the slopes stage)
+        dc[v] = R(0);
+        dn[v] = R(0);
+        if (G.slope_type != R(0))
+        {
+          const R qcp = Qv[mc + mstr[D]], qnm = Qv[mn - mstr[D]];
+          if constexpr (kExactOrder)
+          {
+            dc[v] = limited_slope(qc[v], qcp, qn[v], G.slope_type);
+            dn[v] = limited_slope(qn[v], qc[v], qnm, G.slope_type);
+          }
+          else
+          {
+            dc[v] = limited_slope_bits(qc[v], qcp, qn[v], G.slope_type);
+            dn[v] = limited_slope_bits(qn[v], qc[v], qnm, G.slope_type);
+          }
+        }
+        scv[v] = Ss[v * T::NS + sc_];
+        snv[v] = Ss[v * T::NS + sn_];
+      }
+      hface_flux<R, DIM, D>(G, st, qc, dc, scv, qn, dn, snv, fl);
+#pragma unroll
+      for (int v = 0; v < NVAR; ++v)
+        Fs[v * T::NF + off + f] = fl[v];
+    }
+  };
+  face_dir(std::integral_constant<int, 0>{});
+  face_dir(std::integral_constant<int, 1>{});
+  if constexpr (DIM == 3)
+    face_dir(std::integral_constant<int, 2>{});
+  __syncthreads();
+
+  // 4. update of the tile's interior cells
+  constexpr int NT = T::TX * T::TY * T::TZ;
+  for (int o = tid; o < NT; o += T::THREADS)
+  {
+    const int a = o % T::TX, b = (o / T::TX) % T::TY, cz = o / (T::TX * T::TY);
+    const int i = i0 + a, j = j0 + b, k = DIM == 3 ? k0 + cz : 0;
+    if (i >= G.nx + g || j >= G.ny + g || (DIM == 3 && k >= G.nz + g))
+      continue;
+    const int64_t c = hcell(G, i, j, k);
+    // face index of the cell's minus face along d, and of its plus face
+    const int f0 = a + (T::TX + 1) * (b + T::TY * cz);
+    const int f1 = T::NF0 + a + T::TX * (b + (T::TY + 1) * cz);
+    const int f2 = T::NF0 + T::NF1 + a + T::TX * (b + T::TY * cz);
+    const int fm_[3] = { f0, f1, f2 };
+    const int fstep[3] = { 1, T::TX, T::TX * T::TY };
+    R         uin[MAXV], u[MAXV], fm[DIM][MAXV], fp[DIM][MAXV];
+#pragma unroll
+    for (int v = 0; v < NVAR; ++v)
+    {
+      uin[v] = U[c + v * G.sv];
+#pragma unroll
+      for (int d = 0; d < DIM; ++d)
+      {
+        fm[d][v] = Fs[v * T::NF + fm_[d]];
+        fp[d][v] = Fs[v * T::NF + fm_[d] + fstep[d]];
+      }
+    }
+    hupdate_cell<R, DIM>(G, st, uin, fm, fp, u);
+#pragma unroll
+    for (int v = 0; v < NVAR; ++v)
+      Uout[c + v * G.sv] = u[v];
+  }
 }
 
 // LayoutRight <-> LayoutLeft of an NVAR-variable array.  dir = 0: right ->

@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <string>
 #include <vector>
 
@@ -55,7 +56,15 @@ public:
   cudaGraphExec_t graph[2] = { nullptr, nullptr };
   cudaGraphExec_t graph_pair[2] = { nullptr, nullptr };
   int64_t         launched = 0;
-  static constexpr int kLaunches = 7;
+  static constexpr int kLaunches = 7;      // stage form
+  static constexpr int kFusedLaunches = 5; // fused form
+  // the fused plain form (k_hdt + k_hfused, intermediates in shared memory)
+  // or the stage kernels; same results bit for bit.  Unless mhd_set_fused
+  // fixed it, the first stepping call times one iteration of each on the
+  // current state and keeps the faster (tune_form).
+  bool fused = true;
+  bool tuned = false;
+  std::string tune_report;
 
   ~HydroImpl() override
   {
@@ -144,7 +153,89 @@ public:
     HY_CK(cudaMemsetAsync(S, 0, n * nvar * (dim + 1) * sizeof(R), stream));
     HY_CK(cudaMemsetAsync(F, 0, n * nvar * dim * sizeof(R), stream));
     HY_CK(reset_time_state());
+    if (dim == 2)
+      HY_CK(cudaFuncSetAttribute(k_hfused<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)HTile<R, 2>::SMEM));
+    else
+      HY_CK(cudaFuncSetAttribute(k_hfused<R, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)HTile<R, 3>::SMEM));
     HY_CK(cudaStreamSynchronize(stream));
+    return MHD_OK;
+  }
+
+  int
+  fused_form() const override
+  {
+    return fused ? 1 : 0;
+  }
+
+  int
+  set_fused(int on) override
+  {
+    HY_CK(cudaStreamSynchronize(stream));
+    drop_graphs();
+    fused = on != 0;
+    tuned = true;
+    return MHD_OK;
+  }
+
+  // Time one iteration of each form on a snapshot of the current state (the
+  // array the next iteration reads and the time-step record), restore the
+  // snapshot after each, keep the faster form.  Both forms produce the same
+  // state, so the choice changes only the speed.
+  int
+  tune_form()
+  {
+    if (tuned)
+      return MHD_OK;
+    tuned = true;
+    if (int rc = read_state())
+      return rc;
+    if (step_finished_host())
+      return MHD_OK;
+    const DevState saved = *st_host;
+    const int      parity = (int)(saved.it & 1);
+    R *            cur = parity ? U2 : U;
+    R *            snap = nullptr;
+    HY_CK(cudaMalloc(&snap, state_bytes()));
+    cudaEvent_t e0, e1;
+    HY_CK(cudaEventCreate(&e0));
+    HY_CK(cudaEventCreate(&e1));
+    float ms[2] = { 0.f, 0.f };
+    HY_CK(cudaMemcpyAsync(snap, cur, state_bytes(), cudaMemcpyDeviceToDevice, stream));
+    for (int pass = 0; pass < 3; ++pass) // a warm pass per form, then the timed ones
+    {
+      for (int f = 0; f < 2; ++f)
+      {
+        fused = f == 1;
+        HY_CK(cudaMemcpyAsync(cur, snap, state_bytes(), cudaMemcpyDeviceToDevice, stream));
+        *st_host = saved;
+        HY_CK(cudaMemcpyAsync(st, st_host, sizeof(DevState), cudaMemcpyHostToDevice, stream));
+        HY_CK(cudaEventRecord(e0, stream));
+        enqueue_step(parity);
+        HY_CK(cudaEventRecord(e1, stream));
+        if (int rc = check_launch())
+          return rc;
+        HY_CK(cudaEventSynchronize(e1));
+        float t = 0.f;
+        HY_CK(cudaEventElapsedTime(&t, e0, e1));
+        if (pass > 0)
+          ms[f] += t;
+      }
+    }
+    HY_CK(cudaMemcpyAsync(cur, snap, state_bytes(), cudaMemcpyDeviceToDevice, stream));
+    *st_host = saved;
+    HY_CK(cudaMemcpyAsync(st, st_host, sizeof(DevState), cudaMemcpyHostToDevice, stream));
+    HY_CK(cudaStreamSynchronize(stream));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(snap);
+    fused = ms[1] <= ms[0];
+    char buf[160];
+    std::snprintf(buf, sizeof buf, "stages %.3f ms, fused %.3f ms per iteration -> %s",
+                  ms[0] / 2, ms[1] / 2, fused ? "fused" : "stages");
+    tune_report = buf;
+    launched = saved.it;
     return MHD_OK;
   }
 
@@ -217,20 +308,61 @@ public:
       k_hupdate<R, 3><<<nblocks(ncell, 256), 256, 0, stream>>>(G, in, out, F, st);
   }
 
+  void
+  launch_dt(const R * in, R * out, int force)
+  {
+    if (dim == 2)
+      k_hdt<R, 2><<<nblocks(ncell, 256), 256, 0, stream>>>(G, in, out, st, force);
+    else
+      k_hdt<R, 3><<<nblocks(ncell, 256), 256, 0, stream>>>(G, in, out, st, force);
+  }
+  void
+  launch_fused(const R * in, R * out)
+  {
+    if (dim == 2)
+    {
+      using T = HTile<R, 2>;
+      const dim3 grid((G.nx + T::TX - 1) / T::TX, (G.ny + T::TY - 1) / T::TY, 1);
+      k_hfused<R, 2><<<grid, T::THREADS, T::SMEM, stream>>>(G, in, out, st);
+    }
+    else
+    {
+      using T = HTile<R, 3>;
+      const dim3 grid((G.nx + T::TX - 1) / T::TX, (G.ny + T::TY - 1) / T::TY,
+                      (G.nz + T::TZ - 1) / T::TZ);
+      k_hfused<R, 3><<<grid, T::THREADS, T::SMEM, stream>>>(G, in, out, st);
+    }
+  }
+
   int
   step_kernel_names(const char ** names) const
   {
     static const char * nm[kLaunches] = { "k_hbound", "k_hprim_dt", "k_hfinalize", "k_hslopes",
                                           "k_hflux",  "k_hupdate",  "k_advance" };
-    for (int q = 0; q < kLaunches; ++q)
-      names[q] = nm[q];
-    return kLaunches;
+    static const char * nf[kFusedLaunches] = { "k_hbound", "k_hdt", "k_hfinalize", "k_hfused",
+                                               "k_advance" };
+    const int n = fused ? kFusedLaunches : kLaunches;
+    for (int q = 0; q < n; ++q)
+      names[q] = fused ? nf[q] : nm[q];
+    return n;
   }
 
   // launch q of one iteration reading `in` and writing `out`
   void
   launch_stage(int q, R * in, R * out)
   {
+    if (fused)
+    {
+      switch (q)
+      {
+        case 0: return launch_bound(in, 0);
+        case 1: return launch_dt(in, out, 0);
+        case 2: return launch_finalize(0);
+        case 3: return launch_fused(in, out);
+        default: k_advance<R><<<1, 1, 0, stream>>>(st);
+      }
+      return;
+    }
     switch (q)
     {
       case 0: return launch_bound(in, 0);
@@ -248,14 +380,15 @@ public:
   {
     R * in = parity ? U2 : U;
     R * out = parity ? U : U2;
-    for (int q = 0; q < kLaunches; ++q)
+    const int n = launches_per_step();
+    for (int q = 0; q < n; ++q)
       launch_stage(q, in, out);
   }
 
   int
   launches_per_step() override
   {
-    return kLaunches;
+    return fused ? kFusedLaunches : kLaunches;
   }
 
   int
@@ -393,6 +526,12 @@ public:
     return MHD_OK;
   }
 
+  bool
+  step_finished_host() const
+  {
+    return st_host->t >= st_host->tEnd - 1e-14 || st_host->it >= st_host->nStepmax;
+  }
+
   R *
   current()
   {
@@ -428,6 +567,8 @@ public:
   int
   step() override
   {
+    if (int rc = tune_form())
+      return rc;
     enqueue_step((int)(launched & 1));
     ++launched;
     return check_launch();
@@ -460,13 +601,15 @@ public:
       err = "dt must be positive and finite";
       return MHD_ERR_INVALID_ARG;
     }
+    if (int rc = tune_form())
+      return rc;
     const int p = (int)(launched & 1);
     R *       in = p ? U2 : U;
     R *       out = p ? U : U2;
     launch_stage(0, in, out);
     launch_stage(1, in, out);
     k_hset_dt<R><<<1, 1, 0, stream>>>(G, st, dt);
-    for (int q = 3; q < kLaunches; ++q)
+    for (int q = 3; q < launches_per_step(); ++q)
       launch_stage(q, in, out);
     ++launched;
     return check_launch();
@@ -493,6 +636,8 @@ public:
   int
   run(int nsteps, int * done) override
   {
+    if (int rc = tune_form())
+      return rc;
     if (int rc = build_graphs())
       return rc;
     if (int rc = read_state())
@@ -528,6 +673,8 @@ public:
     launched = st_host->it;
     R * out = (launched & 1) ? U : U2;
     if (int rc = upload(Uin, current(), layout))
+      return rc;
+    if (int rc = tune_form()) // on the uploaded state
       return rc;
     enqueue_step((int)(launched & 1));
     ++launched;
@@ -596,6 +743,8 @@ public:
   int
   run_timed(int nsteps, float * ms) override
   {
+    if (int rc = tune_form())
+      return rc;
     if (int rc = build_graphs())
       return rc;
     if (int rc = read_state())
@@ -620,6 +769,8 @@ public:
   int
   profile_step(const char ** names, float * ms, int max, int * count) override
   {
+    if (int rc = tune_form())
+      return rc;
     if (int rc = read_state())
       return rc;
     launched = st_host->it;
@@ -627,12 +778,12 @@ public:
     R *         in = p ? U2 : U;
     R *         out = p ? U : U2;
     const char *kn[kLaunches];
-    step_kernel_names(kn);
+    const int   n = step_kernel_names(kn);
     cudaEvent_t ev[kLaunches + 1];
-    for (int q = 0; q <= kLaunches; ++q)
+    for (int q = 0; q <= n; ++q)
       HY_CK(cudaEventCreate(&ev[q]));
     HY_CK(cudaEventRecord(ev[0], stream));
-    for (int q = 0; q < kLaunches; ++q)
+    for (int q = 0; q < n; ++q)
     {
       launch_stage(q, in, out);
       HY_CK(cudaEventRecord(ev[q + 1], stream));
@@ -640,17 +791,17 @@ public:
     ++launched;
     if (int rc = check_launch())
       return rc;
-    HY_CK(cudaEventSynchronize(ev[kLaunches]));
-    for (int q = 0; q < kLaunches && q < max; ++q)
+    HY_CK(cudaEventSynchronize(ev[n]));
+    for (int q = 0; q < n && q < max; ++q)
     {
       if (names)
         names[q] = kn[q];
       HY_CK(cudaEventElapsedTime(&ms[q], ev[q], ev[q + 1]));
     }
-    for (int q = 0; q <= kLaunches; ++q)
+    for (int q = 0; q <= n; ++q)
       cudaEventDestroy(ev[q]);
     if (count)
-      *count = kLaunches;
+      *count = n;
     return MHD_OK;
   }
 

@@ -564,6 +564,23 @@ extern "C"
   }
 
   int
+  mhd_set_fused(mhd_ctx * ctx, int fused)
+  {
+    NEED_CORE(ctx);
+    return from_core(ctx, ctx->core->set_fused(fused));
+  }
+
+  int
+  mhd_get_fused(mhd_ctx * ctx, int * fused)
+  {
+    NEED_CORE(ctx);
+    if (!fused)
+      return fail(ctx, MHD_ERR_INVALID_ARG, "null pointer");
+    *fused = ctx->core->fused_form();
+    return MHD_OK;
+  }
+
+  int
   mhd_time(mhd_ctx * ctx, double * t, double * dt, int * iteration)
   {
     NEED_CORE(ctx);

@@ -9,6 +9,11 @@ oracle (SolverHydroMuscl<dim>, Hydro_Muscl_2D/3D, through the C ABI).
 * Fast FP64 build: within 1e-11 of the oracle (relative L1 per variable).
 * FP32 build: within 2e-4 of the oracle after 20 iterations (momenta
   relative to the acoustic momentum scale sum(rho c) where that is larger).
+* The fused form (one tile kernel per iteration, intermediates in shared
+  memory) and the stage kernels give the same state bit for bit in the
+  FMA-free build (and within round-off in the FMA builds, which contract
+  each kernel's expressions independently), on tiles cut by the domain edge
+  too.
 * CUDA-graph runs, single steps and host-array steps agree bit for bit;
   checkpoints restart bitwise; periodic runs conserve mass and energy to
   round-off at 1024^2.
@@ -46,11 +51,14 @@ def rel_l1(a, b, gamma0=1.4):
     return num / np.maximum(den, 1e-300)
 
 
+@pytest.mark.parametrize("fused", [True, False], ids=["fused", "stages"])
 @pytest.mark.parametrize("path", CASES, ids=IDS)
-def test_hydro_exact_build_matches_reference_bitwise(mhdlib, path):
+def test_hydro_exact_build_matches_reference_bitwise(mhdlib, path, fused):
     m = mhdlib
     z = np.load(path)
     s = m.MHDSolver.from_ini(str(z["ini"]), precision=64, fp_mode=m.MHD_FP_EXACT)
+    s.set_fused(fused)
+    assert s.fused == fused
     if bool(z["perturbed"]):
         s.set_state(z["U0"])
     else:
@@ -218,4 +226,59 @@ def test_hydro_numeric_status_on_bad_state(mhdlib):
         s.set_state(U)
         s.run(1)
     assert e.value.code == m.MHD_ERR_NUMERIC
+    s.close()
+
+
+FUSED_CASES = [
+    # partial tiles along every axis (the tile is 32 x 16 in 2D, 16 x 8 x 4 /
+    # 8 x 8 x 4 in 3D), every build, gravity, both versions, all solvers
+    ("2d_partial", dict(dim=2, nx=77, ny=41, riemann="hllc", bc=(1, 2, 3, 3))),
+    ("2d_gravity_v1", dict(dim=2, nx=40, ny=35, riemann="approx", gravity=True, version=1,
+                           problem="rayleigh_taylor", bc=(3, 3, 1, 1))),
+    ("2d_hll_slope1", dict(dim=2, nx=33, ny=17, riemann="hll", slope_type="1")),
+    ("3d_partial", dict(dim=3, nx=19, ny=13, nz=7, riemann="approx", bc=(1, 2, 3, 3, 2, 1))),
+    ("3d_gravity_v1", dict(dim=3, nx=17, ny=9, nz=10, riemann="llf", gravity=True, version=1,
+                           problem="rising_bubble", bc=(2, 2, 1, 1, 2, 2))),
+    ("3d_slope0", dict(dim=3, nx=16, ny=16, nz=8, riemann="hllc", slope_type="0")),
+]
+
+
+@pytest.mark.parametrize("prec,mode", [(64, 1), (64, 0), (32, 0)], ids=["exact", "fast", "fp32"])
+@pytest.mark.parametrize("name,kw", FUSED_CASES, ids=[c[0] for c in FUSED_CASES])
+def test_hydro_fused_form_equals_stage_form(mhdlib, name, kw, prec, mode):
+    m = mhdlib
+    ini = hydro_ini(**kw)
+    U0 = hydro_perturbed(m.initial_state(m.params_from_ini(ini)), 5)
+    out = []
+    for fused in (True, False, None):
+        s = m.MHDSolver.from_ini(ini, precision=prec, fp_mode=mode)
+        if fused is not None:
+            s.set_fused(fused)
+        s.set_state(U0.astype(s.real))
+        s.run(6)  # None: the first run times both forms on a snapshot and keeps the faster
+        out.append((s.get_state(), s.time()))
+        s.close()
+    for q in (1, 2):
+        if mode == m.MHD_FP_EXACT:
+            # no contraction: the same operations in the same order
+            assert np.array_equal(out[0][0], out[q][0])
+            assert out[0][1] == out[q][1]
+        else:
+            # the FMA builds contract the same expressions independently in
+            # each kernel: round-off level differences
+            tol = 1e-13 if prec == 64 else 1e-5
+            a, b = out[0][0].astype(np.float64), out[q][0].astype(np.float64)
+            assert rel_l1(interior(a), interior(b)).max() <= tol
+            assert out[0][1][2] == out[q][1][2]
+
+
+def test_mhd_solver_has_no_fused_form(mhdlib):
+    m = mhdlib
+    from mhd_cases import ot_ini
+
+    s = m.MHDSolver.from_ini(ot_ini(dim=2, nx=16))
+    assert not s.fused
+    s.set_fused(False)
+    with pytest.raises(m.MHDError):
+        s.set_fused(True)
     s.close()
