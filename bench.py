@@ -58,6 +58,15 @@ WORKLOADS = {
     # reduced size for ncu captures (a few GB on the device, inputs still > L2)
     "ot3d_128_fp64": (3, 128, 64, "3D Orszag-Tang 128^3, FP64 plain MUSCL-Hancock+HLLD+CT"),
     "ot3d_128_fp32": (3, 128, 32, "3D Orszag-Tang 128^3, FP32 plain MUSCL-Hancock+HLLD+CT"),
+    # the hydro-only MUSCL solver (Hydro_Muscl_3D / _2D), run_hydro
+    "hydro_blast3d_fp64": (3, 0, 64, "Hydro_Muscl_3D blast, settings/test_blast_3D.ini at 4x its "
+                                      "resolution (256 x 192 x 128), FP64"),
+    "hydro_blast3d_fp32": (3, 0, 32, "Hydro_Muscl_3D blast, settings/test_blast_3D.ini at 4x its "
+                                      "resolution (256 x 192 x 128), FP32"),
+    "hydro_kh2d_4096_fp32": (2, 4096, 32, "Hydro_Muscl_2D Kelvin-Helmholtz 4096^2 (Robertson "
+                                          "seed, HLLC, periodic), FP32"),
+    "hydro_kh2d_4096_fp64": (2, 4096, 64, "Hydro_Muscl_2D Kelvin-Helmholtz 4096^2 (Robertson "
+                                          "seed, HLLC, periodic), FP64"),
 }
 
 
@@ -621,6 +630,144 @@ def hydro_companion(m, local: int, steps: int, cpu: bool):
     return out
 
 
+def hydro_kh2d_ini(n: int = 4096) -> str:
+    return f"""[run]
+solver_name=Hydro_Muscl_2D
+tEnd=10.0
+nStepmax=100000
+nOutput=0
+[mesh]
+nx={n}
+ny={n}
+boundary_type_xmin=3
+boundary_type_xmax=3
+boundary_type_ymin=3
+boundary_type_ymax=3
+[hydro]
+gamma0=1.4
+cfl=0.8
+slope_type=2
+problem=kelvin_helmholtz
+riemann=hllc
+[other]
+implementationVersion=0
+"""
+
+
+def run_hydro(args):
+    """A hydro-only MUSCL workload as its own line: device-resident rate
+    (CUDA events), per-kernel times, the form the context chose (fused tile
+    kernel or stage kernels), the HBM roofline of the dominant kernel, the
+    host-buffer rate (mhd_step_host, pinned buffers), the FMA-free build
+    against the oracle (bitwise, 2 iterations) and the oracle on the host
+    cores."""
+    import torch
+    import ppkmhd_gb300 as m
+
+    dim, _, precision, label = WORKLOADS[args.workload]
+    ini = hydro_bench_ini() if "blast3d" in args.workload else hydro_kh2d_ini()
+    exact = precision == 64 and args.fp_mode == "exact"
+    p = m.params_from_ini(ini)
+    p.precision = precision
+    p.fp_mode = m.MHD_FP_EXACT if exact else m.MHD_FP_FAST
+    s = m.MHDSolver(p)
+    s.init_problem()
+    cells, ghost_cells = s.cell_counts()
+    U0 = s.get_state()
+    s.run_timed(max(args.warmup, 3))
+    s.init_problem()
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        ms = s.run_timed(args.steps)
+    torch.cuda.synchronize()
+    value = cells * args.steps / (ms / 1e3)
+    prof = {}
+    for _ in range(3):
+        for name, kms in s.profile_step():
+            prof.setdefault(name, []).append(kms)
+    prof = {k: float(np.median(v)) for k, v in prof.items()}
+    dom = max(prof, key=prof.get)
+    rb = 8 if precision == 64 else 4
+    alg = 2 * (dim + 2) * rb
+    hbm_peak, peak_kind = load_peaks()
+    achieved = alg * cells / (prof[dom] / 1e3) / 1e9
+    form = "fused tile kernel" if s.fused else "stage kernels"
+    # host-buffer steps
+    h_in = torch.empty(U0.size, dtype=torch.float64 if precision == 64 else torch.float32,
+                       pin_memory=True)
+    h_out = torch.empty_like(h_in, pin_memory=True)
+    h_in.numpy()[:] = U0.reshape(-1)
+    s.init_problem()
+    for _ in range(2):
+        s.step_host_ptr(h_in.data_ptr(), h_out.data_ptr())
+    n_e2e = max(2, min(args.steps, 10))
+    t0 = time.perf_counter()
+    for q in range(n_e2e):
+        a, b = (h_in, h_out) if q % 2 == 0 else (h_out, h_in)
+        s.step_host_ptr(a.data_ptr(), b.data_ptr())
+    e2e = cells * n_e2e / (time.perf_counter() - t0)
+    accuracy, cpu = None, None
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle_py
+
+        oracle_py.build_oracle()
+        nthreads = os.cpu_count() or 1
+        o = oracle_py.HydroOracleSolver(ini, nthreads=nthreads)
+        o.set_state(U0.astype(np.float64))
+        t0 = time.perf_counter()
+        o.run(2)
+        el2 = time.perf_counter() - t0
+        if precision == 64:
+            s.set_state(U0)
+            s.run(2)
+            mine = m.interior(s.get_state(), ghost=2)
+            ref = oracle_py.interior(o.get_state(), 2)
+            den = np.maximum(np.abs(ref).sum(axis=tuple(range(1, dim + 1))), 1e-300)
+            accuracy = {"steps": 2, "bitwise_equal": bool(np.array_equal(mine, ref)),
+                        "rel_l1_per_variable": [float(x) for x in np.abs(mine - ref).sum(
+                            axis=tuple(range(1, dim + 1))) / den],
+                        "reference": "oracle/hydro_oracle.c (bitwise the reference's hydro "
+                                     "functors compiled without FMA contraction)"}
+        ns = int(min(50, max(2, 8.0 / max(el2 / 2, 1e-6))))
+        t0 = time.perf_counter()
+        o.run(ns)
+        el = time.perf_counter() - t0
+        o.close()
+        cpu = {"value": cells * ns / el, "unit": "cell-updates/s", "cores": nthreads,
+               "kind": "port", "sample": f"{ns} iterations of the same grid after 2, "
+                                         f"oracle/hydro_oracle.c with {nthreads} OpenMP threads "
+                                         f"({el:.1f} s timed)"}
+    out = {
+        "metric": "hydro cell-updates/s (interior cells), MUSCL-Hancock hydro step "
+                  f"(Hydro_Muscl_{dim}D)",
+        "value": value, "unit": "cell-updates/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == 64 else "f32",
+        "fp_mode": ("exact" if exact else "fast") if precision == 64 else "fp32",
+        "data": "synthetic (the problem's own initial condition)",
+        "config": {"workload": label, "cells": cells, "cells_with_ghosts": ghost_cells,
+                   "state_bytes": U0.nbytes, "form": form, "per_kernel_ms": prof,
+                   "kernels_per_step": s.launches_per_step(),
+                   "l2": "inputs larger than L2 (state %.2f GB per array)" % (U0.nbytes / 1e9)},
+        "e2e": {"value": e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": U0.nbytes,
+                "d2h_bytes_per_step": U0.nbytes, "steps": n_e2e,
+                "call": "mhd_step_host (pinned host buffers, copies inside the timed region)"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
+                     "unit": "GB/s", "frac": achieved / hbm_peak,
+                     "traffic": load_profile_traffic(args.workload, dom),
+                     "peak_source": f"hbm_gbs of {peak_kind}",
+                     "algorithmic_bytes_per_cell": alg},
+        "clocks": clk.summary(),
+        "gpu_launches": s.launches_per_step() * args.steps,
+        "cpu_baseline": cpu,
+    }
+    if accuracy is not None:
+        out["accuracy"] = accuracy
+    s.close()
+    emit(out)
+
+
 def ensemble_sample(specs):
     """Problems the CPU legs time: the smallest, the largest and 6 seeded
     random ones."""
@@ -1011,6 +1158,43 @@ def run_reference(args):
               "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
                       "d2h_bytes_per_step": 0}})
         return
+    if args.workload.startswith("hydro"):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle_py
+
+        oracle_py.build_oracle()
+        ini = hydro_bench_ini() if "blast3d" in args.workload else hydro_kh2d_ini()
+        o = oracle_py.HydroOracleSolver(ini, nthreads=nthreads)
+        import ppkmhd_gb300 as m
+
+        o.set_state(m.initial_state(m.params_from_ini(ini)))
+        cells = o.p.nx * o.p.ny * (o.p.nz if dim == 3 else 1)
+        t0 = time.perf_counter()
+        o.run(max(args.warmup, 1))
+        t_one = (time.perf_counter() - t0) / max(args.warmup, 1)
+        ns = int(min(steps or args.steps, max(2, 150.0 / max(t_one, 1e-6))))
+        t0 = time.perf_counter()
+        o.run(ns)
+        el = time.perf_counter() - t0
+        o.close()
+        v = cells * ns / el
+        emit({"impl": "reference",
+              "metric": "hydro cell-updates/s (interior cells), MUSCL-Hancock hydro step "
+                        f"(Hydro_Muscl_{dim}D)",
+              "value": v, "unit": "cell-updates/s", "n_gpus": world, "steps": ns,
+              "warmup": args.warmup, "ms_per_step": el * 1e3 / ns, "higher_is_better": True,
+              "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+              "data": "synthetic (the problem's own initial condition)",
+              "config": {"workload": label,
+                         "implementation": "CPU port of the reference hydro step "
+                                           "(oracle/hydro_oracle.c, bitwise equal to the "
+                                           "reference functors), OpenMP"},
+              "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": nthreads,
+                               "kind": "port", "sample": f"{ns} iterations of the full grid "
+                                                         f"after {args.warmup} ({el:.1f} s)"},
+              "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                      "d2h_bytes_per_step": 0}})
+        return
     if steps is None:
         # the GPU arm's K steps after W warm-up steps, unless that exceeds a
         # few minutes of host work (then ~150 s worth, stated in "steps")
@@ -1071,6 +1255,8 @@ def main():
         run_ensemble(args)
     elif args.workload.startswith("turb"):
         run_turbulence(args)
+    elif args.workload.startswith("hydro"):
+        run_hydro(args)
     else:
         run_gb300(args)
 
