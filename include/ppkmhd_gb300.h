@@ -96,6 +96,9 @@ extern "C" {
                                            strength (2D) */
 #define MHD_PROBLEM_RAYLEIGH_TAYLOR 10  /* real: amplitude, d0, d1, gx, gy, gz */
 #define MHD_PROBLEM_RISING_BUBBLE 11    /* real: R, x0, y0, z0, din, dout, gx, gy, gz */
+#define MHD_PROBLEM_DISK 12             /* real: radius, radius_inner, xc, yc, zc, ref_density,
+                                           contrast_density, contrast_width, ref_sound_speed,
+                                           then the point source xs, ys, zs, G M, soften */
 
 /*
  * Run/mesh/scheme parameters.  Mirrors the fields of HydroParams /
@@ -124,9 +127,11 @@ typedef struct mhd_params
   double problem_real[24]; /* per-problem parameters, see MHD_PROBLEM_* */
   int    problem_int[4];
   int    solver;     /* MHD_SOLVER_MHD_MUSCL (default) or MHD_SOLVER_HYDRO_MUSCL */
-  int    gravity;    /* hydro solver: [gravity] static (SolverBase.cpp:138-141) */
+  int    gravity;    /* hydro solver: 0 off, 1 [gravity] static, 2 [gravity] point
+                        (SolverBase.cpp:138-141; either switches gravity on) */
   double gravity_field[3]; /* hydro solver: the uniform static field the problem's
-                              initialisation sets (zero for problems that set none) */
+                              initialisation sets (zero for problems that set none;
+                              the disk sets the point-source field instead) */
 } mhd_params;
 
 typedef struct mhd_ctx mhd_ctx;

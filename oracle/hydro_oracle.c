@@ -84,9 +84,26 @@ horc_params_from_ini(const char *ini_text, horc_params *p)
   p->version = (int)ini_float(&m, "OTHER", "implementationVersion", 0.0f);
   if (p->version != 0 && p->version != 1 && p->version != 2)
     p->version = 0;
-  p->gravity = ini_bool(&m, "gravity", "static", 0);
   const int point = ini_bool(&m, "gravity", "point", 0);
+  p->gravity = ini_bool(&m, "gravity", "static", 0) || point;
   const char *prob = ini_str(&m, "hydro", "problem", "unknown");
+  if (!strcmp(prob, "disk"))
+  {
+    /* PointSourceGravity.h and the disk centre of DiskParams.h (mesh
+     * defaults -0.5 .. 0.5 there) */
+    p->point = 1;
+    p->xs = ini_float(&m, "gravity", "x", 0.0f);
+    p->ys = ini_float(&m, "gravity", "y", 0.0f);
+    p->zs = ini_float(&m, "gravity", "z", 0.0f);
+    p->GM = ini_float(&m, "gravity", "G", 1.0f) * ini_float(&m, "gravity", "M", 1.0f);
+    p->eps = ini_float(&m, "gravity", "soften", 0.01f);
+    const double x0 = ini_float(&m, "mesh", "xmin", -0.5f), x1 = ini_float(&m, "mesh", "xmax", 0.5f);
+    const double y0 = ini_float(&m, "mesh", "ymin", -0.5f), y1 = ini_float(&m, "mesh", "ymax", 0.5f);
+    const double z0 = ini_float(&m, "mesh", "zmin", -0.5f), z1 = ini_float(&m, "mesh", "zmax", 0.5f);
+    p->xc = ini_float(&m, "disk", "xc", (float)((x0 + x1) / 2));
+    p->yc = ini_float(&m, "disk", "yc", (float)((y0 + y1) / 2));
+    p->zc = ini_float(&m, "disk", "zc", (float)((z0 + z1) / 2));
+  }
   if (!strcmp(prob, "rayleigh_taylor"))
   {
     p->grav[0] = ini_float(&m, "rayleigh_taylor", "gx", 0.0f);
@@ -102,8 +119,8 @@ horc_params_from_ini(const char *ini_text, horc_params *p)
   if (p->dim == 2)
     p->grav[2] = 0.0;
   free(m.kv);
-  if (point || p->version == 2 || (p->dim == 3 && p->riemann == HORC_HLL))
-    return -1; /* point gravity (disk), version 2 and 3D HLL are not restated */
+  if (p->version == 2 || (p->dim == 3 && p->riemann == HORC_HLL))
+    return -1; /* version 2 and 3D HLL are not restated */
 
   p->isize = p->nx + 2 * p->ghost;
   p->jsize = p->ny + 2 * p->ghost;
@@ -121,6 +138,43 @@ int64_t
 horc_nelem(const horc_params *p)
 {
   return (int64_t)p->isize * p->jsize * p->ksize * p->nvar;
+}
+
+/* ---------------------------------------------------------------- gravity field */
+
+/* The field the init functors write: uniform (RayleighTaylorInstabilityFunctor,
+ * RisingBubbleFunctor) or, for the disk (InitDiskFunctor2D/3D,
+ * HydroInitFunctors2D.h:907-1060), PointSourceGravity::eval at the cell centre
+ * relative to the disk centre (z = 0 in 2D). */
+void
+horc_gravity_field(const horc_params *p, double *g)
+{
+  const int64_t sk = (int64_t)p->isize * p->jsize, sv = sk * p->ksize;
+  for (int k = 0; k < p->ksize; ++k)
+    for (int j = 0; j < p->jsize; ++j)
+      for (int i = 0; i < p->isize; ++i)
+      {
+        const int64_t c = i + (int64_t)j * p->isize + k * sk;
+        double        gx = p->grav[0], gy = p->grav[1], gz = p->grav[2];
+        if (!p->gravity)
+          gx = gy = gz = 0.0;
+        else if (p->point)
+        {
+          const double x = p->xmin + p->dx / 2 + (i - p->ghost) * p->dx - p->xc;
+          const double y = p->ymin + p->dy / 2 + (j - p->ghost) * p->dy - p->yc;
+          const double z = p->dim == 3 ? p->zmin + p->dz / 2 + (k - p->ghost) * p->dz - p->zc : 0.0;
+          const double r = sqrt((x - p->xs) * (x - p->xs) + (y - p->ys) * (y - p->ys) +
+                                (z - p->zs) * (z - p->zs) + p->eps * p->eps);
+          const double GM2 = p->GM / (r * r * r);
+          gx = GM2 * (p->xs - x);
+          gy = GM2 * (p->ys - y);
+          gz = GM2 * (p->zs - z);
+        }
+        g[c] = gx;
+        g[c + sv] = gy;
+        if (p->dim == 3)
+          g[c + 2 * sv] = gz;
+      }
 }
 
 /* ---------------------------------------------------------------- indexing */
@@ -593,7 +647,7 @@ horc_riemann(const horc_params *p, const double *qL, const double *qR, double *f
 struct horc_solver
 {
   horc_params P;
-  double     *U, *U2, *Q, *F[3];
+  double     *U, *U2, *Q, *F[3], *g; /* g: gravity field, dim planes */
   double      t, dt;
   int         it, nthreads;
 };
@@ -609,6 +663,8 @@ horc_create(const horc_params *p, int nthreads)
   s->Q = (double *)calloc(n, sizeof(double));
   for (int d = 0; d < p->dim; ++d)
     s->F[d] = (double *)calloc(n, sizeof(double));
+  s->g = (double *)calloc((size_t)p->isize * p->jsize * p->ksize * p->dim, sizeof(double));
+  horc_gravity_field(p, s->g);
   s->t = p->tCurrent;
   s->nthreads = nthreads > 0 ? nthreads : 1;
   return s;
@@ -624,6 +680,7 @@ horc_destroy(horc_solver *s)
   free(s->Q);
   for (int d = 0; d < 3; ++d)
     free(s->F[d]);
+  free(s->g);
   free(s);
 }
 
@@ -661,9 +718,10 @@ compute_dt(horc_solver *s)
           velocity += cs + fabs(q[IV]);
           if (p->dim == 3)
             velocity += cs + fabs(q[IW]);
-          double kk = fabs(p->grav[0]) + fabs(p->grav[1]);
+          const double *gf = s->g;
+          double kk = fabs(gf[c]) + fabs(gf[c + L.sv]);
           if (p->dim == 3)
-            kk = kk + fabs(p->grav[2]);
+            kk = kk + fabs(gf[c + 2 * L.sv]);
           kk *= p->cfl * dxg / (velocity * velocity);
           kk = fmax(kk, 1e-4);
           velocity *= kk / (sqrt(1.0 + 2.0 * kk) - 1.0);
@@ -767,20 +825,21 @@ godunov(horc_solver *s, double *in, double *out, double dt)
           trace_face(p, qn, dqn, dtd, d, +1, qleft);
           if (p->gravity)
           {
-            /* gravity predictor (half time step); the field is uniform */
-            qleft[IU] += 0.5 * dt * p->grav[0];
-            qleft[IV] += 0.5 * dt * p->grav[1];
+            /* gravity predictor (half time step), the field at each cell */
+            const double *gf = s->g;
+            qleft[IU] += 0.5 * dt * gf[nb];
+            qleft[IV] += 0.5 * dt * gf[nb + L.sv];
             if (dim == 3)
-              qleft[IW] += 0.5 * dt * p->grav[2];
+              qleft[IW] += 0.5 * dt * gf[nb + 2 * L.sv];
             /* version 1 in 3D gives the right state of z faces no
              * predictor (HydroRunFunctors3D.h:1344-1346, where the x and y
              * faces have it at :1198-1206 and :1272-1280) */
             if (!(p->version == 1 && dim == 3 && d == 2))
             {
-              qright[IU] += 0.5 * dt * p->grav[0];
-              qright[IV] += 0.5 * dt * p->grav[1];
+              qright[IU] += 0.5 * dt * gf[c];
+              qright[IV] += 0.5 * dt * gf[c + L.sv];
               if (dim == 3)
-                qright[IW] += 0.5 * dt * p->grav[2];
+                qright[IW] += 0.5 * dt * gf[c + 2 * L.sv];
             }
           }
           /* rotate to the face-normal frame: swap the normal velocity into IU */
@@ -835,10 +894,11 @@ godunov(horc_solver *s, double *in, double *out, double dt)
             ekin_old = 0.5 * (rhou * rhou + rhov * rhov + rhow * rhow) / rhoNew;
           else
             ekin_old = 0.5 * (rhou * rhou + rhov * rhov) / rhoNew;
-          rhou += 0.5 * dt * p->grav[0] * (rhoOld + rhoNew);
-          rhov += 0.5 * dt * p->grav[1] * (rhoOld + rhoNew);
+          const double *gf = s->g;
+          rhou += 0.5 * dt * gf[c] * (rhoOld + rhoNew);
+          rhov += 0.5 * dt * gf[c + L.sv] * (rhoOld + rhoNew);
           if (dim == 3)
-            rhow += 0.5 * dt * p->grav[2] * (rhoOld + rhoNew);
+            rhow += 0.5 * dt * gf[c + 2 * L.sv] * (rhoOld + rhoNew);
           out[c + IU * L.sv] = rhou;
           out[c + IV * L.sv] = rhov;
           if (dim == 3)

@@ -42,14 +42,20 @@ typedef struct horc_params
   int    riemann, version, bc[6];
   double tEnd, tCurrent;
   int    nStepmax;
-  int    gravity;    /* [gravity] static */
+  int    gravity;    /* [gravity] static or point */
   double grav[3];    /* the uniform field the problem's init sets (0 otherwise) */
+  int    point;      /* the disk problem: the point-source field instead */
+  double xs, ys, zs, GM, eps; /* [gravity] x, y, z, G * M, soften */
+  double xc, yc, zc;          /* [disk] centre (the field is evaluated relative to it) */
 } horc_params;
 
 /* INI text -> parameters (HydroParams::setup + init, SolverBase's gravity
  * keys).  Returns 0, or -1 when the solver is not Hydro_Muscl_2D/3D. */
 int     horc_params_from_ini(const char *ini_text, horc_params *p);
 int64_t horc_nelem(const horc_params *p);
+/* The gravity field the problem's initialisation writes (dim planes,
+ * LayoutLeft, ghosts included; zero for problems that write none). */
+void horc_gravity_field(const horc_params *p, double *g);
 
 typedef struct horc_solver horc_solver;
 horc_solver *horc_create(const horc_params *p, int nthreads);

@@ -189,6 +189,9 @@ class HorcParams(ctypes.Structure):
         ("riemann", ctypes.c_int), ("version", ctypes.c_int), ("bc", ctypes.c_int * 6),
         ("tEnd", ctypes.c_double), ("tCurrent", ctypes.c_double), ("nStepmax", ctypes.c_int),
         ("gravity", ctypes.c_int), ("grav", ctypes.c_double * 3),
+        ("point", ctypes.c_int), ("xs", ctypes.c_double), ("ys", ctypes.c_double),
+        ("zs", ctypes.c_double), ("GM", ctypes.c_double), ("eps", ctypes.c_double),
+        ("xc", ctypes.c_double), ("yc", ctypes.c_double), ("zc", ctypes.c_double),
     ]
 
 
@@ -261,6 +264,31 @@ class HydroOracleSolver:
         t, dt, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
         hlib().horc_time(self.h, ctypes.byref(t), ctypes.byref(dt), ctypes.byref(it))
         return t.value, dt.value, it.value
+
+
+def hydro_gravity_field(ini_text: str) -> np.ndarray:
+    """The oracle's gravity field for the .ini (dim planes, LayoutLeft)."""
+    p = hydro_params_from_ini(ini_text)
+    hlib().horc_gravity_field.argtypes = [ctypes.POINTER(HorcParams), _dp]
+    shape = hydro_state_shape(p)
+    g = np.zeros((p.dim,) + shape[1:], dtype=np.float64)
+    hlib().horc_gravity_field(ctypes.byref(p), _ptr(g))
+    return g
+
+
+def ref_hydro_gravity_field(ini_text: str, bits: int = 64) -> np.ndarray:
+    """The gravity field the reference's hydro init functor writes (dim
+    planes, LayoutLeft float64; zeros for problems that write none)."""
+    r = RefSolver(ini_text, bits)
+    dim, shape = r.dim, r._right_shape()
+    r.close()
+    L = ctypes.CDLL(REF_SO[bits])
+    L.ref_hydro_gravity_field.argtypes = [ctypes.c_char_p, ctypes.c_void_p]
+    L.ref_hydro_gravity_field.restype = ctypes.c_long
+    g = np.empty(shape[:-1] + (dim,), dtype=np.float64 if bits == 64 else np.float32)
+    n = L.ref_hydro_gravity_field(ini_text.encode(), g.ctypes.data_as(ctypes.c_void_p))
+    assert n == g.size
+    return np.ascontiguousarray(g.T, dtype=np.float64)
 
 
 def hydro_riemann(p: HorcParams, qL, qR) -> np.ndarray:

@@ -12,7 +12,7 @@
 //     version, the gravity field when [gravity] static/point is on, init,
 //     make_boundaries, deep_copy(U2, U), compute_dt);
 //   * init dispatch: SolverHydroMuscl.cpp:110-244 (unknown problems fall
-//     back to implode);
+//     back to implode; the disk writes the point-source gravity field);
 //   * one iteration: SolverHydroMuscl.h:695-735 (compute_dt, then
 //     godunov_unsplit(m_dt) ping-ponging U/U2) -> SolverHydroMuscl.cpp:
 //     257-320 (2D) / :327-400 (3D);
@@ -79,6 +79,8 @@ init_problem_2d(ConfigMap & cfg, HydroParams & params, DataArray2d U, VectorFiel
                                               gravity);
   else if (problem == "rising_bubble")
     RisingBubbleFunctor2D::apply(params, RisingBubbleParams(cfg), U, gravity);
+  else if (problem == "disk")
+    InitDiskFunctor2D::apply(params, DiskParams(cfg), PointSourceGravity(cfg), U, gravity);
   else
     InitImplodeFunctor2D::apply(params, ImplodeParams(cfg), U);
 }
@@ -99,6 +101,8 @@ init_problem_3d(ConfigMap & cfg, HydroParams & params, DataArray3d U, VectorFiel
                                               gravity);
   else if (problem == "rising_bubble")
     RisingBubbleFunctor3D::apply(params, RisingBubbleParams(cfg), U, gravity);
+  else if (problem == "disk")
+    InitDiskFunctor3D::apply(params, DiskParams(cfg), PointSourceGravity(cfg), U, gravity);
   else
     InitImplodeFunctor3D::apply(params, ImplodeParams(cfg), U);
 }
@@ -382,6 +386,38 @@ ref_hydro_initial_state(const char * ini_text, real_t * out)
 
 extern "C"
 {
+  // The gravity field the init functor writes (dim planes, LayoutRight
+  // (i, j[, k], comp)), element count or 0
+  long
+  ref_hydro_gravity_field(const char * ini_text, real_t * out)
+  {
+    std::string s(ini_text);
+    char *      buf = &s[0];
+    ConfigMap   cfg(buf, (int)s.size());
+    HydroParams params;
+    params.setup(cfg);
+    const std::string solver = cfg.getString("run", "solver_name", "unknown");
+    if (solver == "Hydro_Muscl_2D")
+    {
+      DataArray2d   U("U", params.isize, params.jsize, params.nbvar);
+      VectorField2d g("gravity field", params.isize, params.jsize);
+      init_problem_2d(cfg, params, U, g);
+      if (out)
+        std::memcpy(out, g.data(), g.size() * sizeof(real_t));
+      return (long)g.size();
+    }
+    if (solver == "Hydro_Muscl_3D")
+    {
+      DataArray3d   U("U", params.isize, params.jsize, params.ksize, params.nbvar);
+      VectorField3d g("gravity field", params.isize, params.jsize, params.ksize);
+      init_problem_3d(cfg, params, U, g);
+      if (out)
+        std::memcpy(out, g.data(), g.size() * sizeof(real_t));
+      return (long)g.size();
+    }
+    return 0;
+  }
+
   // riemann_hydro (RiemannSolvers.h:570-633) on nvar-component primitive
   // states; dim from the .ini's solver
   void

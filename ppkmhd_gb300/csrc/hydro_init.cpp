@@ -17,6 +17,8 @@
 //   isentropic_vortex  HydroInitFunctors2D.h:570-663 (2D)
 //   rayleigh_taylor    HydroInitFunctors2D.h:668-787, 3D:520-640
 //   rising_bubble      HydroInitFunctors2D.h:795-902, 3D:645-760
+//   disk               HydroInitFunctors2D.h:907-1060, 3D (with the
+//                      point-source gravity field, init_hydro_gravity_host)
 // The problem parameters arrive in mhd_params::problem_real/problem_int in
 // the layout documented in ppkmhd_gb300.h.
 #include <cmath>
@@ -398,7 +400,98 @@ rising_bubble(const mhd_params & p, const HMesh & m, double * U)
   });
 }
 
+// PointSourceGravity::eval (PointSourceGravity.h): the softened
+// point-source field at (x, y, z)
+void
+point_source(const double * r, double x, double y, double z, double & gx, double & gy, double & gz)
+{
+  const double xs = r[9], ys = r[10], zs = r[11], GM = r[12], eps = r[13];
+  const double rr = std::sqrt((x - xs) * (x - xs) + (y - ys) * (y - ys) + (z - zs) * (z - zs) +
+                              eps * eps);
+  const double GM2 = GM / (rr * rr * rr);
+  gx = GM2 * (xs - x);
+  gy = GM2 * (ys - y);
+  gz = GM2 * (zs - z);
+}
+
+// InitDiskFunctor2D / 3D (HydroInitFunctors2D.h:907-1060, 3D): a rotating
+// disk around the point source, coordinates relative to the disk centre
+void
+disk(const mhd_params & p, const HMesh & m, double * U)
+{
+  const double * r = p.problem_real;
+  const double   radius = r[0], radius_inner = r[1], xc = r[2], yc = r[3], zc = r[4];
+  const double   rho0 = r[5], rho_contrast = r[6], contrast_width = r[7], ref_cs = r[8];
+  const double   GM = r[12], eps = r[13];
+  m.each([&](int i, int j, int k, int64_t c) {
+    const double x = m.x(i) - xc, y = m.y(j) - yc;
+    const double z = m.dim == 3 ? m.z(k) - zc : 0;
+    const double r2 = x * x + y * y;
+    const double rc = std::sqrt(r2);
+    const double r_soft = std::sqrt(r2 + eps * eps);
+    const double r_sph = std::sqrt(r2 + eps * eps + z * z);
+    const double x_soft = x * (r_soft / rc);
+    const double y_soft = y * (r_soft / rc);
+    // DiskParams::radial_speed_of_sound
+    const double csound =
+      rc < radius_inner ? ref_cs / std::sqrt(radius_inner / radius) : ref_cs / std::sqrt(rc / radius);
+    double omega2 = 0;
+    if (rc >= radius_inner)
+      omega2 = GM / (r_soft * r_soft * r_sph) - 3.5 * (csound / r_soft) * (csound / r_soft);
+    else
+      omega2 = GM / (r_soft * r_soft * r_soft) - 2.5 * (csound / r_soft) * (csound / r_soft);
+    const double omega = std::sqrt(std::fmax(omega2, 0.0));
+    double       rho = rho0 * std::pow(r_soft / radius, -2.5) *
+                 std::exp(GM / (csound * csound) * (1. / r_sph - 1. / r_soft));
+    if (rc > radius || std::fabs(z) > 0.5 * radius)
+    {
+      if (rc > radius + contrast_width || std::fabs(z) > 0.5 * radius + contrast_width)
+        rho /= rho_contrast;
+      else
+      {
+        const double cutdown = std::fmax((rc - radius) / contrast_width,
+                                         (std::fabs(z) - 0.5 * radius) / contrast_width);
+        rho *= std::pow(rho_contrast, -cutdown);
+      }
+    }
+    rho = std::fmax(rho, 1e-6);
+    U[c + ID * m.sv] = rho;
+    U[c + IU * m.sv] = -y_soft * omega * rho;
+    U[c + IV * m.sv] = x_soft * omega * rho;
+    if (m.dim == 3)
+      U[c + IW * m.sv] = 0.0;
+    const double pressure = csound * csound * rho;
+    U[c + IP * m.sv] = pressure / (m.gamma0 - 1.0) + 0.5 * rho * omega2 * (r2 + eps * eps);
+  });
+}
+
 } // namespace
+
+void
+init_hydro_gravity_host(const mhd_params & p, double * g)
+{
+  // RayleighTaylorInstabilityFunctor / RisingBubbleFunctor write the uniform
+  // (gx, gy[, gz]); InitDiskFunctor the point-source field at the cell
+  // centre relative to the disk centre (z = 0 in 2D); other problems write
+  // none (the reference's field stays zero)
+  const HMesh m(p);
+  m.each([&](int i, int j, int k, int64_t c) {
+    double gx = p.gravity_field[0], gy = p.gravity_field[1], gz = p.gravity_field[2];
+    if (p.problem == MHD_PROBLEM_DISK)
+    {
+      const double * r = p.problem_real;
+      const double   x = m.x(i) - r[2], y = m.y(j) - r[3];
+      const double   z = m.dim == 3 ? m.z(k) - r[4] : 0;
+      point_source(r, x, y, z, gx, gy, gz);
+    }
+    else if (p.problem != MHD_PROBLEM_RAYLEIGH_TAYLOR && p.problem != MHD_PROBLEM_RISING_BUBBLE)
+      gx = gy = gz = 0.0;
+    g[c] = gx;
+    g[c + m.sv] = gy;
+    if (m.dim == 3)
+      g[c + 2 * m.sv] = gz;
+  });
+}
 
 void
 init_hydro_problem_host(const mhd_params & p, double * U)
@@ -420,6 +513,8 @@ init_hydro_problem_host(const mhd_params & p, double * U)
     return rayleigh_taylor(p, m, U);
   case MHD_PROBLEM_RISING_BUBBLE:
     return rising_bubble(p, m, U);
+  case MHD_PROBLEM_DISK:
+    return disk(p, m, U);
   default:
     return implode(p, m, U);
   }

@@ -51,10 +51,10 @@ struct HGrid
   int64_t sj, sk, sv;
   int     bc[6];
   int     riemann;   // MHD_RIEMANN_APPROX / LLF / HLL / HLLC
-  int     gravity;   // [gravity] static
+  int     gravity;   // [gravity] static or point: the predictor and source terms
   int     zgrav_right; // 0: version 1 in 3D (no predictor on the right state of z faces)
   R       gamma0, gamma6, smallr, smallc, smallp, smallpp, slope_type, entho;
-  R       grav[3];   // uniform static gravity field
+  const R * gf;      // gravity field (dim planes of sv cells) when gravity is on
   double  cfl, dx, dy, dz, dxg; // dxg = min(dx, dy[, dz]) (ComputeDtGravityFunctor)
   double  idx, idy, idz, idxg;  // host IEEE reciprocals
   Box     box[BOX_COUNT];
@@ -526,7 +526,7 @@ hriemann(const HGrid<R> & G, const R * ql, const R * qr, R * flux)
 // rate counts as 0 (fmax ignores NaN operands).
 template <class R, int DIM>
 __device__ __forceinline__ R
-hrate(const HGrid<R> & G, const R * q, R cs)
+hrate(const HGrid<R> & G, const R * q, R cs, int64_t c)
 {
   R val;
   if (G.gravity)
@@ -536,9 +536,9 @@ hrate(const HGrid<R> & G, const R * q, R cs)
     velocity += cs + fabs(q[IV]);
     if constexpr (DIM == 3)
       velocity += cs + fabs(q[IW]);
-    R kk = fabs(G.grav[0]) + fabs(G.grav[1]);
+    R kk = fabs(G.gf[c]) + fabs(G.gf[c + G.sv]);
     if constexpr (DIM == 3)
-      kk = kk + fabs(G.grav[2]);
+      kk = kk + fabs(G.gf[c + 2 * G.sv]);
     kk *= hdiv(R(G.cfl) * R(G.dxg), velocity * velocity);
     kk = fmax(kk, R(1e-4));
     velocity *= hdiv(kk, hsqrt(R(1) + R(2) * kk) - R(1));
@@ -581,7 +581,7 @@ hrate(const HGrid<R> & G, const R * q, R cs)
 template <class R, int DIM>
 __device__ __forceinline__ void
 hupdate_cell(const HGrid<R> & G, const DevState * st, const R * uin, const R (*fm)[MAXV],
-             const R (*fp)[MAXV], R * u)
+             const R (*fp)[MAXV], R * u, int64_t c)
 {
 #pragma unroll
   for (int v = 0; v < DIM + 2; ++v)
@@ -606,10 +606,10 @@ hupdate_cell(const HGrid<R> & G, const DevState * st, const R * uin, const R (*f
     else
       ekin_old = hdiv(R(0.5) * (rhou * rhou + rhov * rhov), rhoNew);
     const R hdt = R(0.5 * st->dt);
-    rhou += hdt * G.grav[0] * (rhoOld + rhoNew);
-    rhov += hdt * G.grav[1] * (rhoOld + rhoNew);
+    rhou += hdt * G.gf[c] * (rhoOld + rhoNew);
+    rhov += hdt * G.gf[c + G.sv] * (rhoOld + rhoNew);
     if constexpr (DIM == 3)
-      rhow += hdt * G.grav[2] * (rhoOld + rhoNew);
+      rhow += hdt * G.gf[c + 2 * G.sv] * (rhoOld + rhoNew);
     u[IU] = rhou;
     u[IV] = rhov;
     if constexpr (DIM == 3)
@@ -705,7 +705,7 @@ k_hprim_dt(const HGrid<R> G, const R * __restrict__ U, R * __restrict__ Q, DevSt
                           (DIM == 2 || (k >= g && k < G.nz + g));
     if (interior)
     {
-      rate = hrate<R, DIM>(G, q, cs);
+      rate = hrate<R, DIM>(G, q, cs, c);
       bad = !(u[ID] > R(0)) || !isfinite(u[IP]);
     }
   }
@@ -823,7 +823,7 @@ k_hslopes(const HGrid<R> G, const R * __restrict__ Q, R * __restrict__ S, const 
 template <class R, int DIM, int D>
 __device__ __forceinline__ void
 hface_flux(const HGrid<R> & G, const DevState * st, const R * qc, const R * dc, const R * sc,
-           const R * qn, const R * dn, const R * sn, R * out)
+           const R * qn, const R * dn, const R * sn, R * out, int64_t c, int64_t nb)
 {
   constexpr int NVAR = DIM + 2;
   constexpr int VN = D == 0 ? IU : D == 1 ? IV : IW; // normal velocity
@@ -835,17 +835,20 @@ hface_flux(const HGrid<R> & G, const DevState * st, const R * qc, const R * dc, 
   htrace<R, DIM, false>(G, qn, dn, sn, t, qleft);
   if (G.gravity)
   {
+    // the gravity predictor with the field at each cell (left state: the
+    // minus neighbour nb, right state: the cell c)
     const R hdt = R(0.5 * st->dt);
-    qleft[IU] += hdt * G.grav[0];
-    qleft[IV] += hdt * G.grav[1];
+    const R * g = G.gf;
+    qleft[IU] += hdt * g[nb];
+    qleft[IV] += hdt * g[nb + G.sv];
     if constexpr (DIM == 3)
-      qleft[IW] += hdt * G.grav[2];
+      qleft[IW] += hdt * g[nb + 2 * G.sv];
     if (D != 2 || G.zgrav_right)
     {
-      qright[IU] += hdt * G.grav[0];
-      qright[IV] += hdt * G.grav[1];
+      qright[IU] += hdt * g[c];
+      qright[IV] += hdt * g[c + G.sv];
       if constexpr (DIM == 3)
-        qright[IW] += hdt * G.grav[2];
+        qright[IW] += hdt * g[c + 2 * G.sv];
     }
   }
   if constexpr (D > 0)
@@ -880,7 +883,7 @@ hflux_face(const HGrid<R> & G, const R * __restrict__ Q, const R * __restrict__ 
     sc[v] = S[(DIM * NVAR + v) * G.sv + c];
     sn[v] = S[(DIM * NVAR + v) * G.sv + nb];
   }
-  hface_flux<R, DIM, D>(G, st, qc, dc, sc, qn, dn, sn, f);
+  hface_flux<R, DIM, D>(G, st, qc, dc, sc, qn, dn, sn, f, c, nb);
 #pragma unroll
   for (int v = 0; v < NVAR; ++v)
     F[(D * NVAR + v) * G.sv + c] = f[v];
@@ -947,7 +950,7 @@ k_hupdate(const HGrid<R> G, const R * __restrict__ Uin, R * __restrict__ Uout,
       fp[d][v] = Fd[c + str[d]];
     }
   }
-  hupdate_cell<R, DIM>(G, st, uin, fm, fp, u);
+  hupdate_cell<R, DIM>(G, st, uin, fm, fp, u, c);
 #pragma unroll
   for (int v = 0; v < NVAR; ++v)
     Uout[c + v * G.sv] = u[v];
@@ -984,7 +987,7 @@ k_hdt(const HGrid<R> G, const R * __restrict__ U, R * __restrict__ Uout, DevStat
       for (int v = 0; v < NVAR; ++v)
         u[v] = U[c + v * G.sv];
       hprim<R, DIM>(G, u, cs, q);
-      rate = hrate<R, DIM>(G, q, cs);
+      rate = hrate<R, DIM>(G, q, cs, c);
       bad = !(u[ID] > R(0)) || !isfinite(u[IP]);
     }
     else if (Uout)
@@ -1177,7 +1180,14 @@ k_hfused(const HGrid<R> G, const R * __restrict__ U, R * __restrict__ Uout, cons
         scv[v] = Ss[v * T::NS + sc_];
         snv[v] = Ss[v * T::NS + sn_];
       }
-      hface_flux<R, DIM, D>(G, st, qc, dc, scv, qn, dn, snv, fl);
+      // global cells of the face for the gravity field in HBM, clamped to
+      // the array: a partial last tile's faces beyond it are computed but
+      // never used
+      const int     gi = min(i0 + a, G.isize - 1), gj = min(j0 + b, G.jsize - 1);
+      const int     gk = DIM == 3 ? min(k0 + cz, G.ksize - 1) : 0;
+      const int64_t gc = hcell(G, gi, gj, gk);
+      const int64_t gn = gc - (D == 0 ? 1 : D == 1 ? G.sj : G.sk);
+      hface_flux<R, DIM, D>(G, st, qc, dc, scv, qn, dn, snv, fl, gc, gn);
 #pragma unroll
       for (int v = 0; v < NVAR; ++v)
         Fs[v * T::NF + off + f] = fl[v];
@@ -1216,7 +1226,7 @@ k_hfused(const HGrid<R> G, const R * __restrict__ U, R * __restrict__ Uout, cons
         fp[d][v] = Fs[v * T::NF + fm_[d] + fstep[d]];
       }
     }
-    hupdate_cell<R, DIM>(G, st, uin, fm, fp, u);
+    hupdate_cell<R, DIM>(G, st, uin, fm, fp, u, c);
 #pragma unroll
     for (int v = 0; v < NVAR; ++v)
       Uout[c + v * G.sv] = u[v];
@@ -1266,7 +1276,8 @@ make_hgrid(const mhd_params & p)
   for (int f = 0; f < 6; ++f)
     G.bc[f] = p.boundary[f];
   G.riemann = p.riemann;
-  G.gravity = p.gravity;
+  G.gravity = p.gravity != 0;
+  G.gf = nullptr; // set by the solver core once the field is on the device
   G.zgrav_right = !(p.dim == 3 && p.implementation_version == 1);
   // HydroParams::init (HydroParams.cpp:436-443) in real_t
   G.gamma0 = R(p.gamma0);
@@ -1277,8 +1288,6 @@ make_hgrid(const mhd_params & p)
   G.smallpp = R(G.smallr * G.smallp);
   G.gamma6 = R((G.gamma0 + R(1)) / (R(2) * G.gamma0));
   G.slope_type = R(p.slope_type);
-  for (int q = 0; q < 3; ++q)
-    G.grav[q] = R(q < p.dim ? p.gravity_field[q] : 0.0);
   G.cfl = p.cfl;
   G.dx = (double)R(R(p.xmax - p.xmin) / R(p.nx));
   G.dy = (double)R(R(p.ymax - p.ymin) / R(p.ny));

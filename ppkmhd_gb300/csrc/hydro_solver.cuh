@@ -49,6 +49,7 @@ public:
   R *             Q = nullptr;
   R *             S = nullptr; // slopes (DIM blocks of NVAR planes), then trace sources (NVAR)
   R *             F = nullptr; // face fluxes * dt/dx, DIM blocks of NVAR planes
+  R *             Gf = nullptr; // gravity field, DIM planes (gravity on only)
   double *        diag = nullptr;
   DevState *      st = nullptr;
   DevState *      st_host = nullptr;
@@ -69,7 +70,7 @@ public:
   ~HydroImpl() override
   {
     drop_graphs();
-    R * bufs[] = { U, U2, Q, S, F };
+    R * bufs[] = { U, U2, Q, S, F, Gf };
     for (R * b : bufs)
       if (b)
         cudaFree(b);
@@ -152,6 +153,16 @@ public:
       HY_CK(cudaMemsetAsync(b, 0, n * nvar * sizeof(R), stream));
     HY_CK(cudaMemsetAsync(S, 0, n * nvar * (dim + 1) * sizeof(R), stream));
     HY_CK(cudaMemsetAsync(F, 0, n * nvar * dim * sizeof(R), stream));
+    if (p.gravity)
+    {
+      // the field the problem's initialisation writes (constant in time)
+      std::vector<double> gh(n * dim, 0.0);
+      init_hydro_gravity_host(P, gh.data());
+      std::vector<R> gr(gh.begin(), gh.end());
+      HY_CK(cudaMalloc(&Gf, n * dim * sizeof(R)));
+      HY_CK(cudaMemcpy(Gf, gr.data(), n * dim * sizeof(R), cudaMemcpyHostToDevice));
+      G.gf = Gf;
+    }
     HY_CK(reset_time_state());
     if (dim == 2)
       HY_CK(cudaFuncSetAttribute(k_hfused<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -121,17 +121,13 @@ validate_hydro_params(const mhd_params & p)
     return "fp_mode must be MHD_FP_FAST or MHD_FP_EXACT";
   if (p.precision == MHD_FP32 && p.fp_mode == MHD_FP_EXACT)
     return "MHD_FP_EXACT is only available with MHD_FP64";
-  if (p.gravity == 2)
-    return "point-source gravity (the disk problem) is not built";
-  if (p.gravity != 0 && p.gravity != 1)
-    return "gravity must be 0 or 1 (static)";
+  if (p.gravity < 0 || p.gravity > 2)
+    return "gravity must be 0, 1 (static) or 2 (point)";
   const int q = p.problem;
-  if (q == -1)
-    return "the disk problem needs point-source gravity, which is not built";
   if (q != MHD_PROBLEM_BLAST && q != MHD_PROBLEM_IMPLODE && q != MHD_PROBLEM_KELVIN_HELMHOLTZ &&
       q != MHD_PROBLEM_GRESHO_VORTEX && q != MHD_PROBLEM_FOUR_QUADRANT &&
       q != MHD_PROBLEM_ISENTROPIC_VORTEX && q != MHD_PROBLEM_RAYLEIGH_TAYLOR &&
-      q != MHD_PROBLEM_RISING_BUBBLE)
+      q != MHD_PROBLEM_RISING_BUBBLE && q != MHD_PROBLEM_DISK)
     return "unknown problem id for the hydro solver";
   if (p.dim == 3 && (q == MHD_PROBLEM_FOUR_QUADRANT || q == MHD_PROBLEM_ISENTROPIC_VORTEX))
     return "four_quadrant and isentropic_vortex are 2D problems";
@@ -145,8 +141,9 @@ validate_hydro_params(const mhd_params & p)
            "reference leaves the state empty otherwise)";
   // the init functors of these two write the gravity field, which the
   // reference allocates only with gravity on (SolverHydroMuscl.h:242-246)
-  if ((q == MHD_PROBLEM_RAYLEIGH_TAYLOR || q == MHD_PROBLEM_RISING_BUBBLE) && !p.gravity)
-    return "rayleigh_taylor and rising_bubble need [gravity] static=true";
+  if ((q == MHD_PROBLEM_RAYLEIGH_TAYLOR || q == MHD_PROBLEM_RISING_BUBBLE ||
+       q == MHD_PROBLEM_DISK) && !p.gravity)
+    return "rayleigh_taylor, rising_bubble and disk need [gravity] static=true or point=true";
   return "";
 }
 

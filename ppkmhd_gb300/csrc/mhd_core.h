@@ -120,5 +120,8 @@ void init_problem_host(const mhd_params & p, double * U);
 void init_orszag_tang_host(const mhd_params & p, double * U);
 // Initial conditions of the hydro-only solver (hydro_init.cpp).
 void init_hydro_problem_host(const mhd_params & p, double * U);
+// The gravity field the hydro problem's initialisation writes, dim planes
+// over the ghost-inclusive cells, LayoutLeft (hydro_init.cpp).
+void init_hydro_gravity_host(const mhd_params & p, double * g);
 
 } // namespace mhd

@@ -205,8 +205,8 @@ HydroParams::to_mhd_params(const ConfigMap & map, int precision, int fp_mode) co
   // (SolverMHDMuscl.h:700-708) and to implode in the hydro solver
   // (SolverHydroMuscl.cpp:170-177)
   p.problem = mhdEnabled ? MHD_PROBLEM_ORSZAG_TANG : MHD_PROBLEM_IMPLODE;
-  // SolverBase::read_config (SolverBase.cpp:138-141); point gravity (the
-  // disk problem) is marked 2 and refused by the hydro solver
+  // SolverBase::read_config (SolverBase.cpp:138-141): static or point
+  // gravity switches gravity on (2 marks point)
   p.gravity = map.getBool("gravity", "static", false) ? 1 : 0;
   if (map.getBool("gravity", "point", false))
     p.gravity = 2;
@@ -386,7 +386,28 @@ HydroParams::to_mhd_params(const ConfigMap & map, int precision, int fp_mode) co
       p.gravity_field[q] = r[6 + q];
   }
   else if (!mhdEnabled && problem == "disk")
-    p.problem = -1; // the disk problem needs point-source gravity, which is not built
+  {
+    // DiskParams (src/shared/problems/DiskParams.h; its mesh defaults are
+    // -0.5 .. 0.5) and PointSourceGravity (PointSourceGravity.h)
+    p.problem = MHD_PROBLEM_DISK;
+    const double x0 = map.getFloat("mesh", "xmin", -0.5f), y0 = map.getFloat("mesh", "ymin", -0.5f);
+    const double z0 = map.getFloat("mesh", "zmin", -0.5f), x1 = map.getFloat("mesh", "xmax", 0.5f);
+    const double y1 = map.getFloat("mesh", "ymax", 0.5f), z1 = map.getFloat("mesh", "zmax", 0.5f);
+    r[0] = map.getFloat("disk", "radius", (float)((x1 - x0) * 0.125));
+    r[1] = map.getFloat("disk", "radius_inner", (float)(r[0] / 10));
+    r[2] = map.getFloat("disk", "xc", (float)((x0 + x1) / 2));
+    r[3] = map.getFloat("disk", "yc", (float)((y0 + y1) / 2));
+    r[4] = map.getFloat("disk", "zc", (float)((z0 + z1) / 2));
+    r[5] = map.getFloat("disk", "ref_density", 1.0f);
+    r[6] = map.getFloat("disk", "contrast_density", 100.0f);
+    r[7] = map.getFloat("disk", "contrast_width", 0.01f);
+    r[8] = map.getFloat("disk", "ref_sound_speed", 0.2f);
+    r[9] = map.getFloat("gravity", "x", 0.0f);
+    r[10] = map.getFloat("gravity", "y", 0.0f);
+    r[11] = map.getFloat("gravity", "z", 0.0f);
+    r[12] = (double)map.getFloat("gravity", "G", 1.0f) * (double)map.getFloat("gravity", "M", 1.0f);
+    r[13] = map.getFloat("gravity", "soften", 0.01f);
+  }
   if (p.dim == 2)
     p.gravity_field[2] = 0.0;
   p.precision = precision;

@@ -7,9 +7,10 @@ Kokkos-API shim into oracle/_ref/libppkmhd_ref64.so (oracle/build_ref.sh,
 oracle/ref_harness_hydro.cpp), serially, on small cases:
 
   hydro_<case>.npz   the init functor's output (ghost cells included, before
-                     the boundary fill), the interior after 1 and after n
-                     iterations, t and dt along the way; perturbed cases add
-                     a seeded smooth perturbation to the initial state
+                     the boundary fill) and the gravity field it writes, the
+                     interior after 1 and after n iterations, t and dt along
+                     the way; perturbed cases add a seeded smooth
+                     perturbation to the initial state
   hydro_riemann.npz  riemann_hydro fluxes (approx, llf, hll, hllc; 2D and 3D
                      states) for random and edge-case face states
 
@@ -71,6 +72,16 @@ CASES = [
                              riemann="llf", bc=(2, 2, 1, 1, 2, 2)), 5, None),
     ("rb3d_gravity_v0", dict(dim=3, nx=10, problem="rising_bubble", gravity=True, version=0,
                              riemann="llf", bc=(2, 2, 1, 1, 2, 2)), 5, None),
+    # the disk: point-source gravity field written by the init functor
+    ("disk2d_point", dict(dim=2, nx=32, ny=32, problem="disk", mesh=SQUARE, bc=(2, 2, 2, 2),
+                          extra="[gravity]\npoint=true\n"), 8, None),
+    ("disk2d_static_v1", dict(dim=2, nx=30, ny=34, problem="disk", mesh=SQUARE, riemann="hllc",
+                              version=1, bc=(2, 2, 2, 2),
+                              extra="[gravity]\nstatic=true\nG=2.0\nsoften=0.05\nx=0.01\n"
+                                    "[disk]\nradius=0.2\n"), 8, None),
+    ("disk3d_point_v1", dict(dim=3, nx=14, ny=16, nz=12, problem="disk", mesh=SQUARE,
+                             version=1, riemann="llf", bc=(2, 2, 2, 2, 2, 2),
+                             extra="[gravity]\npoint=true\nz=0.05\n"), 5, None),
 ]
 
 
@@ -98,7 +109,8 @@ def make_case(name, kw, nsteps, seed):
     Un = op.interior(r.get_state(), g)
     stamp()
     np.savez_compressed(os.path.join(HERE, f"hydro_{name}.npz"), ini=ini, U0=U0, U1=U1, Un=Un,
-                        nsteps=nsteps, t=np.array(t), dt=np.array(dt), perturbed=seed is not None)
+                        nsteps=nsteps, t=np.array(t), dt=np.array(dt), perturbed=seed is not None,
+                        gravity=op.ref_hydro_gravity_field(ini))
     return dict(case=name, nsteps=nsteps, shape=list(U0.shape))
 
 

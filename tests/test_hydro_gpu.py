@@ -84,6 +84,14 @@ ORACLE_CASES = [
     ("3d_hllc_v1_gravity", dict(dim=3, nx=20, riemann="hllc", version=1, gravity=True,
                                 problem="rising_bubble", bc=(2, 2, 1, 1, 2, 2)), 6),
     ("3d_llf_blast", dict(dim=3, nx=22, riemann="llf", problem="blast"), 6),
+    ("2d_disk_point_gravity", dict(dim=2, nx=64, ny=64, problem="disk", bc=(2, 2, 2, 2),
+                                   mesh="xmin=-0.5\nxmax=0.5\nymin=-0.5\nymax=0.5",
+                                   extra="[gravity]\npoint=true\n"), 20),
+    ("3d_disk_point_gravity_v1", dict(dim=3, nx=24, ny=20, nz=16, problem="disk", version=1,
+                                      riemann="hllc", bc=(2, 2, 2, 2, 2, 2),
+                                      mesh="xmin=-0.5\nxmax=0.5\nymin=-0.5\nymax=0.5\n"
+                                           "zmin=-0.5\nzmax=0.5",
+                                      extra="[gravity]\npoint=true\n"), 6),
 ]
 
 

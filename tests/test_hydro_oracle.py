@@ -42,6 +42,15 @@ def test_hydro_oracle_matches_reference(oracle, path):
     assert (t, dt, it) == (z["t"][2], z["dt"][2], int(z["nsteps"]))
 
 
+@pytest.mark.parametrize("path", CASES, ids=IDS)
+def test_hydro_oracle_gravity_field_matches_reference(oracle, path):
+    """The gravity field the init functors write (uniform for Rayleigh-Taylor
+    and the rising bubble, the softened point source around the disk centre,
+    zero otherwise)."""
+    z = np.load(path)
+    assert np.array_equal(oracle.hydro_gravity_field(str(z["ini"])), z["gravity"])
+
+
 @pytest.mark.parametrize("path", [p for p in CASES if not np.load(p)["perturbed"]],
                          ids=[i for p, i in zip(CASES, IDS) if not np.load(p)["perturbed"]])
 def test_hydro_host_initial_state_matches_reference(mhdlib, path):
@@ -98,6 +107,8 @@ def test_hydro_oracle_against_compiled_reference(oracle, dim, kw):
         s.run(1)
         assert np.array_equal(r.get_state(), s.get_state())
         assert r.time() == s.time()
+    r.close()
+    s.close()
 
 
 def test_hydro_params_parse_like_reference(mhdlib):
@@ -123,8 +134,7 @@ def test_hydro_params_parse_like_reference(mhdlib):
     (dict(dim=2, riemann="hlld"), "", "approx, llf, hll or hllc"),
     (dict(dim=2, version=2), "", "0 or 1"),
     (dict(dim=2, problem="rayleigh_taylor"), "", "[gravity] static"),
-    (dict(dim=2, problem="disk"), "", "disk"),
-    (dict(dim=2), "[gravity]\npoint=true\n", "point-source"),
+    (dict(dim=2, problem="disk"), "", "point=true"),
     (dict(dim=2, slope_type="3"), "", "slope_type"),
     (dict(dim=2, problem="kelvin_helmholtz"), "[KH]\nperturbation_sine_robertson=false\n",
      "robertson"),
