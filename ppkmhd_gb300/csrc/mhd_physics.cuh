@@ -294,6 +294,69 @@ max5(R a0, R a1, R a2, R a3, R a4)
 {
   return sel_max(sel_max(sel_max(sel_max(a0, a1), a2), a3), a4);
 }
+// max5(|n0|/sqrt(r0), ..., |n3|/sqrt(r3), smallc) of IEEE quotients and
+// square roots, bit for bit, with one quotient and one square root instead
+// of four of each.  Approximate ratios t_i = |n_i| rsqrt(r_i) (the library
+// rsqrt, within 1 ulp: |t_i / (|n_i| / sqrt(r_i)) - 1| <= 3.4e-16) bracket
+// the rounded ratios q_i = RN(|n_i| / RN(sqrt(r_i))) (|q_i / (|n_i| /
+// sqrt(r_i)) - 1| <= 2.3e-16), so when the largest t_j exceeds every other
+// t_i by more than the relative margin 4e-15, q_j is the largest q and is
+// the only one computed; a contender within the margin with the same
+// operands (the same bits) is the same value.  Other contenders, and
+// operands outside the ranges where those bounds hold (r not a positive
+// double in [2^-900, 2^900], |n| not 0 or in [2^-500, 2^500)), take the four
+// IEEE quotients.  The result is the max5 chain of sel_max on the q_i.
+__device__ __forceinline__ bool
+alfven_operands_ok(double n, double r)
+{
+  const unsigned hr = (unsigned)__double2hiint(r), hn = (unsigned)__double2hiint(n) & 0x7fffffffu;
+  const unsigned er = hr >> 20, en = hn >> 20;
+  return er - 0x07bu <= 0x708u && (en - 0x20bu <= 0x3e7u || (hn | (unsigned)__double2loint(n)) == 0u);
+}
+__device__ __forceinline__ double
+alfven_max5_exact(double n0, double r0, double n1, double r1, double n2, double r2, double n3,
+                  double r3, double smallc)
+{
+  const double n[4] = { fabs(n0), fabs(n1), fabs(n2), fabs(n3) };
+  const double r[4] = { r0, r1, r2, r3 };
+  bool         ok = true;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    ok = ok && alfven_operands_ok(n[i], r[i]);
+  if (ok)
+  {
+    double t[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      t[i] = n[i] * rsqrt(r[i]);
+    int j = 0;
+#pragma unroll
+    for (int i = 1; i < 4; ++i)
+      j = t[i] > t[j] ? i : j;
+    const double lim = t[j] * (1.0 - 4e-15);
+    bool         amb = false;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      amb = amb || (i != j && t[i] >= lim &&
+                    (__double_as_longlong(n[i]) != __double_as_longlong(n[j]) ||
+                     __double_as_longlong(r[i]) != __double_as_longlong(r[j])));
+    if (!amb)
+    {
+      const double q = n[j] / sqrt(r[j]);
+      return exact_gt(smallc, q) ? smallc : q;
+    }
+  }
+  // the chain of the exact build's sel_max (exact_gt): max5 of the quotients
+  double m = n[0] / sqrt(r[0]);
+#pragma unroll
+  for (int i = 1; i < 4; ++i)
+  {
+    const double q = n[i] / sqrt(r[i]);
+    m = exact_gt(q, m) ? q : m;
+  }
+  return exact_gt(smallc, m) ? smallc : m;
+}
+
 // Sign tests and |d| <= t (t >= 0) of the fast FP64 build on bit patterns
 // (integer pipe).  They agree with the FP comparisons for every non-NaN
 // argument, -0 included.
@@ -1057,14 +1120,16 @@ mag_riemann2d_hlld(const State<R> (&q)[4], const R (&e)[4], R gamma0, R smallc)
   const R EstarRRy = uRR * bRR - vstar * AstarRR;
   const R EstarRR = ustar * BstarRR - vstar * AstarRR;
 
-  const R calfvenL = max5(fabs(aLR) / sqrt(rstarLRx), fabs(AstarLR) / sqrt(rstarLR),
-                          fabs(aLL) / sqrt(rstarLLx), fabs(AstarLL) / sqrt(rstarLL), smallc);
-  const R calfvenR = max5(fabs(aRR) / sqrt(rstarRRx), fabs(AstarRR) / sqrt(rstarRR),
-                          fabs(aRL) / sqrt(rstarRLx), fabs(AstarRL) / sqrt(rstarRL), smallc);
-  const R calfvenB = max5(fabs(bLL) / sqrt(rstarLLy), fabs(BstarLL) / sqrt(rstarLL),
-                          fabs(bRL) / sqrt(rstarRLy), fabs(BstarRL) / sqrt(rstarRL), smallc);
-  const R calfvenT = max5(fabs(bLR) / sqrt(rstarLRy), fabs(BstarLR) / sqrt(rstarLR),
-                          fabs(bRR) / sqrt(rstarRRy), fabs(BstarRR) / sqrt(rstarRR), smallc);
+  // FMAX5 of |B| / sqrt(rho) over the corner states (RiemannSolvers_MHD.h:
+  // 529-548), one IEEE quotient and square root per maximum
+  const R calfvenL = alfven_max5_exact(aLR, rstarLRx, AstarLR, rstarLR, aLL, rstarLLx, AstarLL,
+                                       rstarLL, smallc);
+  const R calfvenR = alfven_max5_exact(aRR, rstarRRx, AstarRR, rstarRR, aRL, rstarRLx, AstarRL,
+                                       rstarRL, smallc);
+  const R calfvenB = alfven_max5_exact(bLL, rstarLLy, BstarLL, rstarLL, bRL, rstarRLy, BstarRL,
+                                       rstarRL, smallc);
+  const R calfvenT = alfven_max5_exact(bLR, rstarLRy, BstarLR, rstarLR, bRR, rstarRRy, BstarRR,
+                                       rstarRR, smallc);
 
   const R SAL = fmin(ustar - calfvenL, R(0));
   const R SAR = fmax(ustar + calfvenR, R(0));

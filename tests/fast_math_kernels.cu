@@ -10,6 +10,9 @@
 //   special_<name> mismatches <count> of <n>             (fallback arguments)
 //   special_gt mismatches <count> of <n>                 (exact build's integer
 //                                                         comparison, all pairs)
+//   special_alfven mismatches <count> of <n>             (exact build's Alfven-speed
+//                                                         maximum with one quotient,
+//                                                         ties, near ties, specials)
 // and exits non-zero on a CUDA error.
 //
 // Build and run (GB300):
@@ -107,6 +110,109 @@ same_bits(double a, double b)
   std::memcpy(&x, &a, 8);
   std::memcpy(&y, &b, 8);
   return x == y;
+}
+
+// The exact build's Alfven-speed maximum (one quotient and square root)
+// against the four IEEE quotients and the exact sel_max chain, bit for bit.
+__global__ void
+k_alfven(const double * __restrict__ in, double * __restrict__ out, int n)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  const double * a = in + 9 * (size_t)i;
+  out[2 * i] = mhd::alfven_max5_exact(a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8]);
+  double m = fabs(a[0]) / sqrt(a[1]);
+  for (int q = 1; q < 4; ++q)
+  {
+    const double v = fabs(a[2 * q]) / sqrt(a[2 * q + 1]);
+    m = mhd::exact_gt(v, m) ? v : m;
+  }
+  out[2 * i + 1] = mhd::exact_gt(a[8], m) ? a[8] : m;
+}
+
+static int
+check_alfven()
+{
+  const int           n = 1 << 20;
+  std::vector<double> h(9 * (size_t)n);
+  uint64_t            s = 0x9e3779b97f4a7c15ull;
+  auto rnd = [&]() {
+    s ^= s << 13;
+    s ^= s >> 7;
+    s ^= s << 17;
+    return s;
+  };
+  auto uni = [&]() { return (double)(rnd() >> 11) * (1.0 / 9007199254740992.0); };
+  auto logu = [&](double lo, double hi) { return std::exp(std::log(lo) + uni() * std::log(hi / lo)); };
+  const double specials[] = { 0.0, -0.0, 1e-310, -1e-310, INFINITY, -INFINITY, NAN, 1e300, 1e-300,
+                              -1.0, 2.2250738585072014e-308 };
+  for (int i = 0; i < n; ++i)
+  {
+    double * a = &h[9 * (size_t)i];
+    const int kind = (int)(rnd() % 8);
+    for (int q = 0; q < 4; ++q)
+    {
+      a[2 * q] = logu(1e-20, 1e20) * ((rnd() & 1) ? 1.0 : -1.0);
+      a[2 * q + 1] = logu(1e-20, 1e20);
+    }
+    a[8] = logu(1e-12, 1e2);
+    if (kind == 1) // identical operands (exact ties)
+      for (int q = 1; q < 4; ++q)
+      {
+        a[2 * q] = a[0];
+        a[2 * q + 1] = a[1];
+      }
+    else if (kind == 2) // equal ratios from different operands: n 2^k, r 4^k
+    {
+      const int q = 1 + (int)(rnd() % 3);
+      a[2 * q] = a[0] * 4.0;
+      a[2 * q + 1] = a[1] * 16.0;
+    }
+    else if (kind == 3) // near ties: one ulp apart
+    {
+      const int q = 1 + (int)(rnd() % 3);
+      a[2 * q] = a[0];
+      a[2 * q + 1] = std::nextafter(a[1], (rnd() & 1) ? 0.0 : INFINITY);
+    }
+    else if (kind == 4) // ratios within 1e-15 of each other
+    {
+      const int q = 1 + (int)(rnd() % 3);
+      a[2 * q] = a[0] * (1.0 + (uni() - 0.5) * 4e-15);
+      a[2 * q + 1] = a[1];
+    }
+    else if (kind == 5) // special operands
+    {
+      const int q = (int)(rnd() % 9);
+      a[q] = specials[rnd() % (sizeof specials / sizeof specials[0])];
+    }
+    else if (kind == 6) // zero numerators and large smallc
+    {
+      a[2 * (rnd() % 4)] = 0.0;
+      a[8] = logu(1e-3, 1e12);
+    }
+  }
+  double *d_in = nullptr, *d_out = nullptr;
+  if (cudaMalloc(&d_in, h.size() * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&d_out, 2 * (size_t)n * sizeof(double)) != cudaSuccess)
+    return 1;
+  cudaMemcpy(d_in, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice);
+  k_alfven<<<(n + 255) / 256, 256>>>(d_in, d_out, n);
+  std::vector<double> o(2 * (size_t)n);
+  if (cudaMemcpy(o.data(), d_out, o.size() * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return 1;
+  int bad = 0;
+  for (int i = 0; i < n; ++i)
+  {
+    uint64_t x, y;
+    std::memcpy(&x, &o[2 * (size_t)i], 8);
+    std::memcpy(&y, &o[2 * (size_t)i + 1], 8);
+    bad += x != y;
+  }
+  std::printf("special_alfven mismatches %d of %d\n", bad, n);
+  cudaFree(d_in);
+  cudaFree(d_out);
+  return 0;
 }
 
 int
@@ -216,5 +322,7 @@ main()
   }
   cudaFree(dx);
   cudaFree(dy);
-  return 0;
+  if (check_alfven())
+    return 1;
+  return cudaDeviceSynchronize() == cudaSuccess ? 0 : 1;
 }

@@ -11,7 +11,9 @@ host references, and that the arguments outside the fast ranges (zeros,
 subnormals, |x| >= 2^1021, infinities, NaN, negative square-root arguments)
 get exactly the library function's result; and that the exact build's
 integer comparison (exact_gt) answers as the FP comparison on every pair of
-those special values.
+those special values, and that its Alfven-speed maximum with one quotient
+(alfven_max5_exact) equals the four-quotient maximum bit for bit on 2^20
+random, tied, nearly tied and special operand sets.
 """
 import os
 import shutil
@@ -36,7 +38,7 @@ def test_fast_fp64_reciprocal_and_sqrt_error_bounds(tmp_path):
             special[f[0][8:]] = (int(f[2]), int(f[4]))
         else:
             res[f[0]] = (float(f[2]), float(f[4]))
-    assert set(special) == {"rcp", "fsqrt", "gt"}, out
+    assert set(special) == {"rcp", "fsqrt", "gt", "alfven"}, out
     for name, (bad, total) in special.items():
         assert total > 900 and bad == 0, (name, bad, total)
     # library references: correctly rounded (rsqrt within its documented bound)

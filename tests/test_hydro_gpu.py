@@ -110,7 +110,11 @@ def test_hydro_builds_against_oracle(mhdlib, oracle, name, kw, n):
     variable) against the C oracle on a seeded perturbed state."""
     m = mhdlib
     ini = hydro_ini(**kw)
-    U0 = hydro_perturbed(m.initial_state(m.params_from_ini(ini)), 7)
+    U0 = m.initial_state(m.params_from_ini(ini))
+    if kw.get("problem") != "disk":
+        # (the disk's 1e-6 density floor outside the disk leaves no room for
+        # the momentum perturbation)
+        U0 = hydro_perturbed(U0, 7)
     ref, (t, dt, it) = _oracle_run(oracle, ini, U0, n)
     for prec, mode, tol in ((64, m.MHD_FP_EXACT, 0.0), (64, m.MHD_FP_FAST, 1e-11),
                             (32, m.MHD_FP_FAST, 2e-4)):
