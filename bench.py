@@ -12,7 +12,8 @@ cell-updates per second.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                   [--fp-mode exact|fast]
                   [--workload ot3d_256_fp64|ot3d_256_fp32|ot2d_256_fp64|
-                              ensemble512_fp32|kh2d_4096_fp32|ot3d_128_fp64|ot3d_128_fp32]
+                              ensemble512_fp32|kh2d_4096_fp32|ot3d_128_fp64|ot3d_128_fp32|
+                              kh2d_2048_fp32|turb3d_512_fp32_mlp|hydro_*]
 
 Other workloads: the 512-problem 2D Orszag-Tang ensemble in FP32 (one
 ensemble context, autotuned launch shapes) and the 2D magnetised
@@ -58,6 +59,9 @@ WORKLOADS = {
     # reduced size for ncu captures (a few GB on the device, inputs still > L2)
     "ot3d_128_fp64": (3, 128, 64, "3D Orszag-Tang 128^3, FP64 plain MUSCL-Hancock+HLLD+CT"),
     "ot3d_128_fp32": (3, 128, 32, "3D Orszag-Tang 128^3, FP32 plain MUSCL-Hancock+HLLD+CT"),
+    "kh2d_2048_fp32": (2, 2048, 32, "2D magnetised Kelvin-Helmholtz 2048^2 (periodic x, "
+                                    "reflecting y, gamma 1.4, Bx 0.1), FP32 plain "
+                                    "MUSCL-Hancock+HLLD+CT"),
     # the hydro-only MUSCL solver (Hydro_Muscl_3D / _2D), run_hydro
     "hydro_blast3d_fp64": (3, 0, 64, "Hydro_Muscl_3D blast, settings/test_blast_3D.ini at 4x its "
                                       "resolution (256 x 192 x 128), FP64"),
@@ -480,6 +484,8 @@ def run_gb300(args):
                        "l2": "inputs larger than L2 (state %.2f GB per array)" % (state_bytes / 1e9),
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "kernels_per_step": s.launches_per_step(),
+                       "form": ("fused tile kernel (k_mfused2d)" if s.fused
+                                else "stage kernels"),
                        "per_kernel_ms": prof},
             "e2e": {"value": e2e_value, "unit": "cell-updates/s",
                     "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes,

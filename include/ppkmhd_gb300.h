@@ -222,17 +222,26 @@ int mhd_step_host(mhd_ctx *ctx, const void *U_in, void *U_out, int layout, int r
  * No counterpart in the reference, which copies no state per step. */
 int mhd_set_host_slabs(mhd_ctx *ctx, int nslabs);
 
-/* Hydro solver: the form of an iteration.  fused = 1 (the default): the plain
- * form fused into one tile kernel per iteration after the CFL reduction
- * (k_hdt + k_hfused): each block loads a tile of the state with two halo
- * layers and computes primitives, slopes, trace sources, face fluxes and the
- * update in shared memory, writing only the new state to HBM.  fused = 0:
- * the stage kernels, which store primitives, slopes and fluxes in HBM.  Both
- * give the same state bit for bit in the MHD_FP_EXACT build (the FMA builds
- * contract each kernel's expressions independently: round-off differences).
- * Without this call the first stepping call times one iteration of each form
- * on the current state and keeps the faster.  The MHD solver has the stage
- * form only (fused = 1 returns MHD_ERR_INVALID_ARG). */
+/* The form of an iteration.  MHD_FORM_FUSED: the plain form fused into one
+ * tile kernel per iteration after the CFL reduction: each block loads a tile
+ * of the state with two halo layers and computes primitives, slopes (and
+ * half step, edge field), face fluxes (and edge EMFs) and the update in
+ * shared memory, writing only the new state to HBM (hydro solver: k_hdt +
+ * k_hfused; MHD solver, 2D implementation version 2 without the flux
+ * surrogate: k_dt_only + k_mfused2d).  MHD_FORM_STAGES: the stage kernels,
+ * which keep the intermediates in HBM.  Both give the same state bit for bit
+ * in the MHD_FP_EXACT build; the FMA builds contract each kernel's
+ * expressions independently (round-off differences).  Without this call a
+ * context runs the form its configuration maps to (the faster one on GB300
+ * for that configuration: fused for 2D FP32, stages otherwise), so the same
+ * configuration always runs the same kernels.  MHD_FORM_TIMED: the next
+ * stepping call times one iteration of each form on the current state and
+ * keeps the faster.  MHD_FORM_FUSED where the configuration has no fused
+ * form returns MHD_ERR_INVALID_ARG.  mhd_get_fused: 1 when the fused form
+ * runs. */
+#define MHD_FORM_STAGES 0
+#define MHD_FORM_FUSED 1
+#define MHD_FORM_TIMED 2
 int mhd_set_fused(mhd_ctx *ctx, int fused);
 int mhd_get_fused(mhd_ctx *ctx, int *fused);
 

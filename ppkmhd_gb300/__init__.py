@@ -36,6 +36,7 @@ MHD_ENSEMBLE_GRAPHS, MHD_ENSEMBLE_PERSISTENT = 0, 1
 
 MHD_RIEMANN_APPROX, MHD_RIEMANN_LLF, MHD_RIEMANN_HLL, MHD_RIEMANN_HLLC, MHD_RIEMANN_HLLD = range(5)
 MHD_SOLVER_MHD_MUSCL, MHD_SOLVER_HYDRO_MUSCL = 0, 1
+MHD_FORM_STAGES, MHD_FORM_FUSED, MHD_FORM_TIMED = 0, 1, 2
 MHD_BC_REFLECTING, MHD_BC_OUTFLOW, MHD_BC_PERIODIC = 1, 2, 3
 MHD_FP64, MHD_FP32 = 64, 32
 MHD_FP_FAST, MHD_FP_EXACT = 0, 1
@@ -339,9 +340,13 @@ class MHDSolver:
         """Slab count of step_host (0 = automatic, 1 = no copy/compute overlap)."""
         self._check(lib().mhd_set_host_slabs(self.h, int(n)))
 
-    def set_fused(self, fused: bool):
-        """Hydro solver: fused tile kernel (default) or stage kernels."""
-        self._check(lib().mhd_set_fused(self.h, int(bool(fused))))
+    def set_fused(self, fused):
+        """True: the fused tile form (hydro solver; 2D MHD solver, version 2);
+        False: the stage kernels; "timed": the next stepping call times one
+        iteration of each and keeps the faster.  Without a call the context
+        runs the form its configuration maps to."""
+        form = MHD_FORM_TIMED if fused == "timed" else int(bool(fused))
+        self._check(lib().mhd_set_fused(self.h, form))
 
     @property
     def fused(self) -> bool:

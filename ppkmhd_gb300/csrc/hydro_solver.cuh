@@ -60,11 +60,13 @@ public:
   static constexpr int kLaunches = 7;      // stage form
   static constexpr int kFusedLaunches = 5; // fused form
   // the fused plain form (k_hdt + k_hfused, intermediates in shared memory)
-  // or the stage kernels; same results bit for bit.  Unless mhd_set_fused
-  // fixed it, the first stepping call times one iteration of each on the
-  // current state and keeps the faster (tune_form).
-  bool fused = true;
-  bool tuned = false;
+  // or the stage kernels; the same state bit for bit in the FMA-free build,
+  // round-off apart in the FMA builds.  The default is a fixed function of
+  // the configuration (default_form), so a configuration always runs the
+  // same kernels; mhd_set_fused fixes either form or has the next stepping
+  // call time one iteration of each and keep the faster (tune_form).
+  bool fused = false;
+  bool tuned = true;
   std::string tune_report;
 
   ~HydroImpl() override
@@ -164,6 +166,7 @@ public:
       G.gf = Gf;
     }
     HY_CK(reset_time_state());
+    fused = default_form();
     if (dim == 2)
       HY_CK(cudaFuncSetAttribute(k_hfused<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)HTile<R, 2>::SMEM));
@@ -180,12 +183,32 @@ public:
     return fused ? 1 : 0;
   }
 
+  // The form measured faster on GB300 for the configuration: fused for 2D
+  // FP32 (2D KH 4096^2: 0.92 vs 1.01 ms), stages otherwise (the halo
+  // recomputation costs more than the HBM traffic it saves in 3D and in
+  // FP64).
+  bool
+  default_form() const
+  {
+    return dim == 2 && sizeof(R) == 4;
+  }
+
   int
   set_fused(int on) override
   {
+    if (on < MHD_FORM_STAGES || on > MHD_FORM_TIMED)
+    {
+      err = "form must be MHD_FORM_STAGES, MHD_FORM_FUSED or MHD_FORM_TIMED";
+      return MHD_ERR_INVALID_ARG;
+    }
     HY_CK(cudaStreamSynchronize(stream));
     drop_graphs();
-    fused = on != 0;
+    if (on == MHD_FORM_TIMED)
+    {
+      tuned = false; // timed by the next stepping call
+      return MHD_OK;
+    }
+    fused = on == MHD_FORM_FUSED;
     tuned = true;
     return MHD_OK;
   }

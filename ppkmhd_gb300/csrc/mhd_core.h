@@ -41,19 +41,19 @@ public:
   virtual int harvest(int stride, float * host, int64_t capacity, int64_t * count) = 0;
   //! time that set_state / init_problem start from (tCurrent)
   virtual void set_time_origin(double t) = 0;
-  //! FP32 version-2 contexts keep the low parts of the state (Buffers::Ulo):
-  //! their size in bytes (0: none), and host copies for checkpoints
-  //! the fused plain form (hydro solver) or the stage kernels
+  //! the fused plain form (hydro solver; 2D MHD solver) or the stage kernels
   virtual int set_fused(int on)
   {
     if (on)
     {
-      err = "the fused form is built for the hydro solver only";
+      err = "no fused form for this configuration";
       return MHD_ERR_INVALID_ARG;
     }
     return MHD_OK;
   }
   virtual int fused_form() const { return 0; }
+  //! FP32 version-2 contexts keep the low parts of the state (Buffers::Ulo):
+  //! their size in bytes (0: none), and host copies for checkpoints
   virtual int64_t low_part_bytes() = 0;
   virtual int     get_low_parts(void * host) = 0;
   virtual int     set_low_parts(const void * host) = 0;

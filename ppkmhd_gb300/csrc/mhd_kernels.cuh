@@ -373,14 +373,63 @@ warp_max(T v)
 // (warp shuffles, then one atomicMax per block on the bit pattern, which
 // orders like the value for non-negative doubles) and is order-independent,
 // so dt is bitwise the reference's.
+// constoprim_mhd (MHDBaseFunctor2D.h:194-242, MHDBaseFunctor3D.h:194-242)
+// of cell c: the cell-centred field is the mean of the cell's two faces per
+// direction (the +1 neighbour's face field is read), the density floored at
+// smallr, the pressure at d * smallp.  Shared by the stage kernels and the
+// fused tile kernel, so both evaluate the same expressions.
+template <class R>
+struct CellPrim
+{
+  R d, p, vu, vv, vw, a, bb, cc;
+  R emag, invd; // 0.5 |B|^2 and the reciprocal of d the quotients used
+};
+
 template <class R, int DIM>
+__device__ __forceinline__ CellPrim<R>
+cell_prim(const Grid<R> & G, const R * __restrict__ U, int64_t c)
+{
+  const int64_t sv = G.sv;
+  const R       nbx = U[c + 1 + IA * sv];
+  const R       nby = U[c + G.sj + IB * sv];
+  const R       nbz = DIM == 3 ? U[c + G.sk + IC * sv] : R(0);
+  const R       d = fmax(U[c + ID * sv], G.smallr);
+  R             vu, vv, vw;
+  // exact build: the nine quotients over d share its correctly rounded
+  // reciprocal (qdiv: bit for bit the IEEE quotients); fast builds multiply
+  // by an approximate reciprocal
+  const R       invd = kExactOrder ? qrcp(d) : rcp(d);
+  if constexpr (kExactOrder)
+  {
+    vu = qdiv(U[c + IU * sv], d, invd);
+    vv = qdiv(U[c + IV * sv], d, invd);
+    vw = qdiv(U[c + IW * sv], d, invd);
+  }
+  else
+  {
+    vu = U[c + IU * sv] * invd;
+    vv = U[c + IV * sv] * invd;
+    vw = U[c + IW * sv] * invd;
+  }
+  const R       a = R(0.5) * (U[c + IA * sv] + nbx);
+  const R       bb = R(0.5) * (U[c + IB * sv] + nby);
+  const R       cc = R(0.5) * (U[c + IC * sv] + nbz);
+  const R       eken = R(0.5) * (vu * vu + vv * vv + vw * vw);
+  const R       emag = R(0.5) * (a * a + bb * bb + cc * cc);
+  const R       eint = kExactOrder ? qdiv(U[c + IP * sv] - emag, d, invd) - eken
+                                   : (U[c + IP * sv] - emag) * invd - eken;
+  const R       p = fmax((G.gamma0 - R(1)) * d * eint, d * G.smallp);
+  return CellPrim<R>{ d, p, vu, vv, vw, a, bb, cc, emag, invd };
+}
+
+template <class R, int DIM, bool STORE_Q = true>
 __device__ __forceinline__ void
 prim_dt_body(const Grid<R> & G, const R * __restrict__ U, R * __restrict__ Q, DevState * st,
              int force, int64_t idx, int64_t end = INT64_MAX)
 {
   if (!force && step_finished(st))
     return;
-  const Box & b = G.box[BOX_PRIM];
+  const Box & b = G.box[STORE_Q ? BOX_PRIM : BOX_INTERIOR];
   int       i, j, k;
   R         rate = R(0);
   R         ptot = R(-1); // FP32: interior total pressure, -1 elsewhere
@@ -389,43 +438,20 @@ prim_dt_body(const Grid<R> & G, const R * __restrict__ U, R * __restrict__ Q, De
   {
     const int64_t c = cell_at(G, i, j, k);
     const int64_t sv = G.sv;
-    const R       nbx = U[c + 1 + IA * sv];
-    const R       nby = U[c + G.sj + IB * sv];
-    const R       nbz = DIM == 3 ? U[c + G.sk + IC * sv] : R(0);
-    const R       d = fmax(U[c + ID * sv], G.smallr);
-    R             vu, vv, vw;
-    // exact build: the nine quotients over d share its correctly rounded
-    // reciprocal (qdiv: bit for bit the IEEE quotients); fast builds multiply
-    // by an approximate reciprocal
-    const R       invd = kExactOrder ? qrcp(d) : rcp(d);
-    if constexpr (kExactOrder)
+    const CellPrim<R> P = cell_prim<R, DIM>(G, U, c);
+    const R d = P.d, p = P.p, vu = P.vu, vv = P.vv, vw = P.vw, a = P.a, bb = P.bb, cc = P.cc;
+    const R emag = P.emag, invd = P.invd;
+    if constexpr (STORE_Q)
     {
-      vu = qdiv(U[c + IU * sv], d, invd);
-      vv = qdiv(U[c + IV * sv], d, invd);
-      vw = qdiv(U[c + IW * sv], d, invd);
+      Q[c + ID * sv] = d;
+      Q[c + IP * sv] = p;
+      Q[c + IU * sv] = vu;
+      Q[c + IV * sv] = vv;
+      Q[c + IW * sv] = vw;
+      Q[c + IA * sv] = a;
+      Q[c + IB * sv] = bb;
+      Q[c + IC * sv] = cc;
     }
-    else
-    {
-      vu = U[c + IU * sv] * invd;
-      vv = U[c + IV * sv] * invd;
-      vw = U[c + IW * sv] * invd;
-    }
-    const R       a = R(0.5) * (U[c + IA * sv] + nbx);
-    const R       bb = R(0.5) * (U[c + IB * sv] + nby);
-    const R       cc = R(0.5) * (U[c + IC * sv] + nbz);
-    const R       eken = R(0.5) * (vu * vu + vv * vv + vw * vw);
-    const R       emag = R(0.5) * (a * a + bb * bb + cc * cc);
-    const R       eint = kExactOrder ? qdiv(U[c + IP * sv] - emag, d, invd) - eken
-                                     : (U[c + IP * sv] - emag) * invd - eken;
-    const R       p = fmax((G.gamma0 - R(1)) * d * eint, d * G.smallp);
-    Q[c + ID * sv] = d;
-    Q[c + IP * sv] = p;
-    Q[c + IU * sv] = vu;
-    Q[c + IV * sv] = vv;
-    Q[c + IW * sv] = vw;
-    Q[c + IA * sv] = a;
-    Q[c + IB * sv] = bb;
-    Q[c + IC * sv] = cc;
     const int g = G.g;
     const bool interior = i >= g && i < G.isize - g && j >= g && j < G.jsize - g &&
                           (DIM == 2 || (k >= g && k < G.ksize - g));
@@ -628,6 +654,99 @@ face_field_slope(const Grid<R> & G, const R * __restrict__ U, uint32_t c, int co
 }
 
 
+// Hancock half step of one cell (ComputeUpdatedPrimVarFunctor,
+// MHDRunFunctors2D.h:920-1051, 3D:865-1022): q2 = q + (dt/2) times the
+// primitive MHD source terms built from the limited slopes s.  Shared by the
+// trace stage and the fused tile kernel.
+template <class R, int DIM>
+__device__ __forceinline__ void
+hancock(const R (&q)[NV], const R (&s)[DIM][NV], R gamma, R dtdx, R dtdy, R dtdz, R (&q2)[NV])
+{
+  (void)dtdz;
+  const R r = q[ID], p = q[IP], u = q[IU], v = q[IV], w = q[IW], A = q[IA], Bc = q[IB], C = q[IC];
+  const R drx = s[0][ID], dpx = s[0][IP], dux = s[0][IU], dvx = s[0][IV], dwx = s[0][IW],
+          dBx = s[0][IB], dCx = s[0][IC];
+  const R dry = s[1][ID], dpy = s[1][IP], duy = s[1][IU], dvy = s[1][IV], dwy = s[1][IW],
+          dAy = s[1][IA], dCy = s[1][IC];
+  const R dAx = s[0][IA], dBy = s[1][IB];
+  R       sr0, su0, sv0, sw0, sp0, sA0, sB0, sC0;
+  if constexpr (!kExactOrder)
+  {
+    // same source terms with one reciprocal of the density
+    const R ir = rcp(r);
+    if constexpr (DIM == 2)
+    {
+      sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy;
+      su0 = (-u * dux - (dpx + Bc * dBx + C * dCx) * ir) * dtdx + (-v * duy + Bc * dAy * ir) * dtdy;
+      sv0 = (-u * dvx + A * dBx * ir) * dtdx + (-v * dvy - (dpy + A * dAy + C * dCy) * ir) * dtdy;
+      sw0 = (-u * dwx + A * dCx * ir) * dtdx + (-v * dwy + Bc * dCy * ir) * dtdy;
+      sp0 = (-u * dpx - dux * gamma * p) * dtdx + (-v * dpy - dvy * gamma * p) * dtdy;
+      sA0 = (u * dBy + Bc * duy - v * dAy - A * dvy) * dtdy;
+      sB0 = (-u * dBx - Bc * dux + v * dAx + A * dvx) * dtdx;
+      sC0 = (w * dAx + A * dwx - u * dCx - C * dux) * dtdx +
+            (-v * dCy - C * dvy + w * dBy + Bc * dwy) * dtdy;
+    }
+    else
+    {
+      const R drz = s[DIM - 1][ID], dpz = s[DIM - 1][IP], duz = s[DIM - 1][IU],
+              dvz = s[DIM - 1][IV], dwz = s[DIM - 1][IW], dAz = s[DIM - 1][IA],
+              dBz = s[DIM - 1][IB], dCz = s[DIM - 1][IC];
+      sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy + (-w * drz - dwz * r) * dtdz;
+      su0 = (-u * dux - (dpx + Bc * dBx + C * dCx) * ir) * dtdx + (-v * duy + Bc * dAy * ir) * dtdy +
+            (-w * duz + C * dAz * ir) * dtdz;
+      sv0 = (-u * dvx + A * dBx * ir) * dtdx + (-v * dvy - (dpy + A * dAy + C * dCy) * ir) * dtdy +
+            (-w * dvz + C * dBz * ir) * dtdz;
+      sw0 = (-u * dwx + A * dCx * ir) * dtdx + (-v * dwy + Bc * dCy * ir) * dtdy +
+            (-w * dwz - (dpz + A * dAz + Bc * dBz) * ir) * dtdz;
+      sp0 = (-u * dpx - dux * gamma * p) * dtdx + (-v * dpy - dvy * gamma * p) * dtdy +
+            (-w * dpz - dwz * gamma * p) * dtdz;
+      sA0 = (u * dBy + Bc * duy - v * dAy - A * dvy) * dtdy + (u * dCz + C * duz - w * dAz - A * dwz) * dtdz;
+      sB0 = (v * dAx + A * dvx - u * dBx - Bc * dux) * dtdx + (v * dCz + C * dvz - w * dBz - Bc * dwz) * dtdz;
+      sC0 = (w * dAx + A * dwx - u * dCx - C * dux) * dtdx + (w * dBy + Bc * dwy - v * dCy - C * dvy) * dtdy;
+    }
+  }
+  else if constexpr (DIM == 2)
+  {
+    sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy;
+    su0 = (-u * dux - dpx / r - Bc * dBx / r - C * dCx / r) * dtdx + (-v * duy + Bc * dAy / r) * dtdy;
+    sv0 = (-u * dvx + A * dBx / r) * dtdx + (-v * dvy - dpy / r - A * dAy / r - C * dCy / r) * dtdy;
+    sw0 = (-u * dwx + A * dCx / r) * dtdx + (-v * dwy + Bc * dCy / r) * dtdy;
+    sp0 = (-u * dpx - dux * gamma * p) * dtdx + (-v * dpy - dvy * gamma * p) * dtdy;
+    sA0 = (u * dBy + Bc * duy - v * dAy - A * dvy) * dtdy;
+    sB0 = (-u * dBx - Bc * dux + v * dAx + A * dvx) * dtdx;
+    sC0 = (w * dAx + A * dwx - u * dCx - C * dux) * dtdx +
+          (-v * dCy - C * dvy + w * dBy + Bc * dwy) * dtdy;
+  }
+  else
+  {
+    const R drz = s[DIM - 1][ID], dpz = s[DIM - 1][IP], duz = s[DIM - 1][IU],
+            dvz = s[DIM - 1][IV], dwz = s[DIM - 1][IW], dAz = s[DIM - 1][IA],
+            dBz = s[DIM - 1][IB], dCz = s[DIM - 1][IC];
+    // (IEEE quotients here: in this register-heavy stage the shared
+    // reciprocal form measured 5 % slower)
+    sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy + (-w * drz - dwz * r) * dtdz;
+    su0 = (-u * dux - (dpx + Bc * dBx + C * dCx) / r) * dtdx + (-v * duy + Bc * dAy / r) * dtdy +
+          (-w * duz + C * dAz / r) * dtdz;
+    sv0 = (-u * dvx + A * dBx / r) * dtdx + (-v * dvy - (dpy + A * dAy + C * dCy) / r) * dtdy +
+          (-w * dvz + C * dBz / r) * dtdz;
+    sw0 = (-u * dwx + A * dCx / r) * dtdx + (-v * dwy + Bc * dCy / r) * dtdy +
+          (-w * dwz - (dpz + A * dAz + Bc * dBz) / r) * dtdz;
+    sp0 = (-u * dpx - dux * gamma * p) * dtdx + (-v * dpy - dvy * gamma * p) * dtdy +
+          (-w * dpz - dwz * gamma * p) * dtdz;
+    sA0 = (u * dBy + Bc * duy - v * dAy - A * dvy) * dtdy + (u * dCz + C * duz - w * dAz - A * dwz) * dtdz;
+    sB0 = (v * dAx + A * dvx - u * dBx - Bc * dux) * dtdx + (v * dCz + C * dvz - w * dBz - Bc * dwz) * dtdz;
+    sC0 = (w * dAx + A * dwx - u * dCx - C * dux) * dtdx + (w * dBy + Bc * dwy - v * dCy - C * dvy) * dtdy;
+  }
+  q2[ID] = r + R(0.5) * sr0;
+  q2[IU] = u + R(0.5) * su0;
+  q2[IV] = v + R(0.5) * sv0;
+  q2[IW] = w + R(0.5) * sw0;
+  q2[IP] = p + R(0.5) * sp0;
+  q2[IA] = A + R(0.5) * sA0;
+  q2[IB] = Bc + R(0.5) * sB0;
+  q2[IC] = C + R(0.5) * sC0;
+}
+
 // Slopes, half step and edge field over the box [g-1, size-g+1]^DIM:
 //  * ComputeSlopesFunctor (MHDRunFunctors2D.h:164-248, 3D:168-273): MC-type
 //    limited slopes per direction; the face-normal field slope is the
@@ -783,90 +902,12 @@ trace_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
   }
 
   // Hancock half step
-  const R r = q[ID], p = q[IP], u = q[IU], v = q[IV], w = q[IW], A = q[IA], Bc = q[IB], C = q[IC];
-  const R gamma = G.gamma0;
-  const R drx = s[0][ID], dpx = s[0][IP], dux = s[0][IU], dvx = s[0][IV], dwx = s[0][IW],
-          dBx = s[0][IB], dCx = s[0][IC];
-  const R dry = s[1][ID], dpy = s[1][IP], duy = s[1][IU], dvy = s[1][IV], dwy = s[1][IW],
-          dAy = s[1][IA], dCy = s[1][IC];
-  const R dAx = s[0][IA], dBy = s[1][IB];
-  R       sr0, su0, sv0, sw0, sp0, sA0, sB0, sC0;
-  if constexpr (!kExactOrder)
-  {
-    // same source terms with one reciprocal of the density
-    const R ir = rcp(r);
-    if constexpr (DIM == 2)
-    {
-      sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy;
-      su0 = (-u * dux - (dpx + Bc * dBx + C * dCx) * ir) * dtdx + (-v * duy + Bc * dAy * ir) * dtdy;
-      sv0 = (-u * dvx + A * dBx * ir) * dtdx + (-v * dvy - (dpy + A * dAy + C * dCy) * ir) * dtdy;
-      sw0 = (-u * dwx + A * dCx * ir) * dtdx + (-v * dwy + Bc * dCy * ir) * dtdy;
-      sp0 = (-u * dpx - dux * gamma * p) * dtdx + (-v * dpy - dvy * gamma * p) * dtdy;
-      sA0 = (u * dBy + Bc * duy - v * dAy - A * dvy) * dtdy;
-      sB0 = (-u * dBx - Bc * dux + v * dAx + A * dvx) * dtdx;
-      sC0 = (w * dAx + A * dwx - u * dCx - C * dux) * dtdx +
-            (-v * dCy - C * dvy + w * dBy + Bc * dwy) * dtdy;
-    }
-    else
-    {
-      const R drz = s[DIM - 1][ID], dpz = s[DIM - 1][IP], duz = s[DIM - 1][IU],
-              dvz = s[DIM - 1][IV], dwz = s[DIM - 1][IW], dAz = s[DIM - 1][IA],
-              dBz = s[DIM - 1][IB], dCz = s[DIM - 1][IC];
-      sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy + (-w * drz - dwz * r) * dtdz;
-      su0 = (-u * dux - (dpx + Bc * dBx + C * dCx) * ir) * dtdx + (-v * duy + Bc * dAy * ir) * dtdy +
-            (-w * duz + C * dAz * ir) * dtdz;
-      sv0 = (-u * dvx + A * dBx * ir) * dtdx + (-v * dvy - (dpy + A * dAy + C * dCy) * ir) * dtdy +
-            (-w * dvz + C * dBz * ir) * dtdz;
-      sw0 = (-u * dwx + A * dCx * ir) * dtdx + (-v * dwy + Bc * dCy * ir) * dtdy +
-            (-w * dwz - (dpz + A * dAz + Bc * dBz) * ir) * dtdz;
-      sp0 = (-u * dpx - dux * gamma * p) * dtdx + (-v * dpy - dvy * gamma * p) * dtdy +
-            (-w * dpz - dwz * gamma * p) * dtdz;
-      sA0 = (u * dBy + Bc * duy - v * dAy - A * dvy) * dtdy + (u * dCz + C * duz - w * dAz - A * dwz) * dtdz;
-      sB0 = (v * dAx + A * dvx - u * dBx - Bc * dux) * dtdx + (v * dCz + C * dvz - w * dBz - Bc * dwz) * dtdz;
-      sC0 = (w * dAx + A * dwx - u * dCx - C * dux) * dtdx + (w * dBy + Bc * dwy - v * dCy - C * dvy) * dtdy;
-    }
-  }
-  else if constexpr (DIM == 2)
-  {
-    sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy;
-    su0 = (-u * dux - dpx / r - Bc * dBx / r - C * dCx / r) * dtdx + (-v * duy + Bc * dAy / r) * dtdy;
-    sv0 = (-u * dvx + A * dBx / r) * dtdx + (-v * dvy - dpy / r - A * dAy / r - C * dCy / r) * dtdy;
-    sw0 = (-u * dwx + A * dCx / r) * dtdx + (-v * dwy + Bc * dCy / r) * dtdy;
-    sp0 = (-u * dpx - dux * gamma * p) * dtdx + (-v * dpy - dvy * gamma * p) * dtdy;
-    sA0 = (u * dBy + Bc * duy - v * dAy - A * dvy) * dtdy;
-    sB0 = (-u * dBx - Bc * dux + v * dAx + A * dvx) * dtdx;
-    sC0 = (w * dAx + A * dwx - u * dCx - C * dux) * dtdx +
-          (-v * dCy - C * dvy + w * dBy + Bc * dwy) * dtdy;
-  }
-  else
-  {
-    const R drz = s[DIM - 1][ID], dpz = s[DIM - 1][IP], duz = s[DIM - 1][IU],
-            dvz = s[DIM - 1][IV], dwz = s[DIM - 1][IW], dAz = s[DIM - 1][IA],
-            dBz = s[DIM - 1][IB], dCz = s[DIM - 1][IC];
-    // (IEEE quotients here: in this register-heavy stage the shared
-    // reciprocal form measured 5 % slower)
-    sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy + (-w * drz - dwz * r) * dtdz;
-    su0 = (-u * dux - (dpx + Bc * dBx + C * dCx) / r) * dtdx + (-v * duy + Bc * dAy / r) * dtdy +
-          (-w * duz + C * dAz / r) * dtdz;
-    sv0 = (-u * dvx + A * dBx / r) * dtdx + (-v * dvy - (dpy + A * dAy + C * dCy) / r) * dtdy +
-          (-w * dvz + C * dBz / r) * dtdz;
-    sw0 = (-u * dwx + A * dCx / r) * dtdx + (-v * dwy + Bc * dCy / r) * dtdy +
-          (-w * dwz - (dpz + A * dAz + Bc * dBz) / r) * dtdz;
-    sp0 = (-u * dpx - dux * gamma * p) * dtdx + (-v * dpy - dvy * gamma * p) * dtdy +
-          (-w * dpz - dwz * gamma * p) * dtdz;
-    sA0 = (u * dBy + Bc * duy - v * dAy - A * dvy) * dtdy + (u * dCz + C * duz - w * dAz - A * dwz) * dtdz;
-    sB0 = (v * dAx + A * dvx - u * dBx - Bc * dux) * dtdx + (v * dCz + C * dvz - w * dBz - Bc * dwz) * dtdz;
-    sC0 = (w * dAx + A * dwx - u * dCx - C * dux) * dtdx + (w * dBy + Bc * dwy - v * dCy - C * dvy) * dtdy;
-  }
+  R q2[NV];
+  hancock<R, DIM>(q, s, G.gamma0, dtdx, dtdy, dtdz, q2);
   R * Q2 = B.Q2;
-  Q2[c + ID * sv] = r + R(0.5) * sr0;
-  Q2[c + IU * sv] = u + R(0.5) * su0;
-  Q2[c + IV * sv] = v + R(0.5) * sv0;
-  Q2[c + IW * sv] = w + R(0.5) * sw0;
-  Q2[c + IP * sv] = p + R(0.5) * sp0;
-  Q2[c + IA * sv] = A + R(0.5) * sA0;
-  Q2[c + IB * sv] = Bc + R(0.5) * sB0;
-  Q2[c + IC * sv] = C + R(0.5) * sC0;
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+    Q2[c + v * sv] = q2[v];
 }
 
 template <class R, int DIM>

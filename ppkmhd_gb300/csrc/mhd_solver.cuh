@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include "mhd_core.h"
+#include "mhd_fused.cuh"
 #include "mhd_kernels.cuh"
 #include "mhd_surrogate.cuh"
 #include "mhd_kernels_v0.cuh"
@@ -169,6 +170,18 @@ public:
   bool                 sur_on = false;
   int                  sm_count = 0;
   int                  sur_blocks_per_sm = 1;
+  // 2D version 2: the fused tile form (k_dt_only + k_mfused2d, every
+  // intermediate in shared memory) or the stage kernels; the same state bit
+  // for bit in the FMA-free build, round-off apart in the FMA builds.  The
+  // default is a fixed function of the configuration (default_form), so a
+  // configuration always runs the same kernels; mhd_set_fused fixes either
+  // form or has the next stepping call time both (tune_form).
+  static constexpr int kFusedTY = 8;
+  using FusedTile = MTile<R, kFusedTY>;
+  bool                 fused = false;
+  bool                 tuned = true;
+  int                  form_req = -1; // -1: default_form; else the mhd_set_fused request
+  std::string          tune_report;
 
   ~SolverImpl() override
   {
@@ -290,7 +303,146 @@ public:
     MHD_CK(cudaMemsetAsync(F, 0, n * nf * dim * sizeof(R), stream));
     MHD_CK(cudaMemsetAsync(Em, 0, n * nplanes_e * sizeof(R), stream));
     MHD_CK(reset_time_state());
+    fused = default_form();
+    if (fused_ok())
+    {
+      MHD_CK(cudaFuncSetAttribute(k_mfused2d<R, kFusedTY, RIEMANN_HLLD>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)FusedTile::SMEM));
+      MHD_CK(cudaFuncSetAttribute(k_mfused2d<R, kFusedTY, 0>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)FusedTile::SMEM));
+    }
     MHD_CK(cudaStreamSynchronize(stream));
+    return MHD_OK;
+  }
+
+  // the fused form exists for 2D implementation version 2 without the
+  // flux surrogate (its tile reads 2 halo layers: ghost >= 2)
+  bool
+  fused_ok() const
+  {
+    return dim == 2 && version == 2 && !sur_on && G.g >= 2;
+  }
+
+  int
+  fused_form() const override
+  {
+    return fused ? 1 : 0;
+  }
+
+  // The form measured faster on GB300 for the configuration.
+  bool
+  default_form() const
+  {
+    return fused_ok() && sizeof(R) == 4;
+  }
+
+  int
+  set_fused(int on) override
+  {
+    if (on < MHD_FORM_STAGES || on > MHD_FORM_TIMED)
+    {
+      err = "form must be MHD_FORM_STAGES, MHD_FORM_FUSED or MHD_FORM_TIMED";
+      return MHD_ERR_INVALID_ARG;
+    }
+    if (on == MHD_FORM_FUSED && !fused_ok())
+    {
+      err = "the fused form is built for 2D implementation version 2 without the flux surrogate";
+      return MHD_ERR_INVALID_ARG;
+    }
+    MHD_CK(cudaStreamSynchronize(stream));
+    drop_graphs();
+    form_req = on;
+    if (on == MHD_FORM_TIMED)
+    {
+      tuned = false; // timed by the next stepping call
+      return MHD_OK;
+    }
+    fused = on == MHD_FORM_FUSED;
+    tuned = true;
+    return MHD_OK;
+  }
+
+  size_t
+  state_bytes() const
+  {
+    return (size_t)ncell * NV * sizeof(R);
+  }
+
+  // Time one iteration of each form on a snapshot of the current state (the
+  // array the next iteration reads, the low parts of an FP32 state and the
+  // time-step record), restore the snapshot after each, keep the faster.
+  // The FMA-free build gives the same state in both forms bit for bit, the
+  // FMA builds to round-off, so the choice changes the speed only.
+  int
+  tune_form()
+  {
+    if (tuned)
+      return MHD_OK;
+    tuned = true;
+    if (!fused_ok())
+    {
+      fused = false;
+      return MHD_OK;
+    }
+    if (int rc = read_state())
+      return rc;
+    if (step_finished_host())
+      return MHD_OK;
+    const DevState saved = *st_host;
+    const int      parity = (int)(saved.it & 1);
+    R *            cur = parity ? U2 : U;
+    R *            snap = nullptr;
+    const size_t   nb = state_bytes() * (Ulo ? 2 : 1);
+    MHD_CK(cudaMalloc(&snap, nb));
+    auto restore = [&]() -> cudaError_t {
+      cudaError_t e = cudaMemcpyAsync(cur, snap, state_bytes(), cudaMemcpyDeviceToDevice, stream);
+      if (e == cudaSuccess && Ulo)
+        e = cudaMemcpyAsync(Ulo, snap + ncell * NV, state_bytes(), cudaMemcpyDeviceToDevice,
+                            stream);
+      *st_host = saved;
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(st, st_host, sizeof(DevState), cudaMemcpyHostToDevice, stream);
+      return e;
+    };
+    cudaEvent_t e0, e1;
+    MHD_CK(cudaEventCreate(&e0));
+    MHD_CK(cudaEventCreate(&e1));
+    float ms[2] = { 0.f, 0.f };
+    MHD_CK(cudaMemcpyAsync(snap, cur, state_bytes(), cudaMemcpyDeviceToDevice, stream));
+    if (Ulo)
+      MHD_CK(cudaMemcpyAsync(snap + ncell * NV, Ulo, state_bytes(), cudaMemcpyDeviceToDevice,
+                             stream));
+    for (int pass = 0; pass < 3; ++pass) // a warm pass per form, then the timed ones
+    {
+      for (int f = 0; f < 2; ++f)
+      {
+        fused = f == 1;
+        MHD_CK(restore());
+        MHD_CK(cudaEventRecord(e0, stream));
+        enqueue_step(parity);
+        MHD_CK(cudaEventRecord(e1, stream));
+        if (int rc = check_launch())
+          return rc;
+        MHD_CK(cudaEventSynchronize(e1));
+        float t = 0.f;
+        MHD_CK(cudaEventElapsedTime(&t, e0, e1));
+        if (pass > 0)
+          ms[f] += t;
+      }
+    }
+    MHD_CK(restore());
+    MHD_CK(cudaStreamSynchronize(stream));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(snap);
+    fused = ms[1] <= ms[0];
+    char buf[160];
+    std::snprintf(buf, sizeof buf, "stages %.3f ms, fused %.3f ms per iteration -> %s",
+                  ms[0] / 2, ms[1] / 2, fused ? "fused" : "stages");
+    tune_report = buf;
+    launched = saved.it;
     return MHD_OK;
   }
 
@@ -507,6 +659,36 @@ public:
     k_advance<R><<<1, 1, 0, stream>>>(st);
   }
 
+  // ---- fused form (2D) ----
+  void
+  launch_dt_only(const R * arr, int force)
+  {
+    const int64_t n = (int64_t)G.nx * G.ny;
+    k_dt_only<R, 2><<<nblocks(n, 256), 256, 0, stream>>>(G, arr, st, force);
+  }
+  int
+  fused_tile_rows() const
+  {
+    return (G.ny + FusedTile::TY - 1) / FusedTile::TY;
+  }
+  // tile rows r0 <= row < r1 (default: all)
+  void
+  launch_fused(const Buffers<R> & B, int r0 = 0, int r1 = -1)
+  {
+    using T = FusedTile;
+    if (r1 < 0)
+      r1 = fused_tile_rows();
+    if (r1 <= r0)
+      return;
+    const dim3 grid((unsigned)((G.nx + T::TX - 1) / T::TX), (unsigned)(r1 - r0));
+    if (G.riemann == RIEMANN_HLLD)
+      k_mfused2d<R, kFusedTY, RIEMANN_HLLD>
+        <<<grid, T::THREADS, T::SMEM, stream>>>(G, B.Uin, B.Uout, B.Ulo, st, r0);
+    else
+      k_mfused2d<R, kFusedTY, 0>
+        <<<grid, T::THREADS, T::SMEM, stream>>>(G, B.Uin, B.Uout, B.Ulo, st, r0);
+  }
+
   static constexpr int kMaxLaunches = 9;
 
   // Names of the launches of one iteration, in order.
@@ -523,16 +705,39 @@ public:
     static const char * v2s[] = { "k_boundaries", "k_prim_dt",       "k_finalize_dt",
                                   "k_trace",      "k_flux_mlp",      "k_flux_fallback",
                                   "k_emf",        "k_update",        "k_advance" };
-    const char ** src = version == 2 ? (sur_on ? v2s : v2) : (dim == 3 ? v0_3d : v0_2d);
-    const int     n = version == 2 ? (sur_on ? 9 : 8) : (dim == 3 ? 9 : 8);
+    static const char * v2f[] = { "k_boundaries", "k_dt_only", "k_finalize_dt", "k_mfused2d",
+                                  "k_advance" };
+    const bool    fz = fused && fused_ok();
+    const char ** src =
+      fz ? v2f : version == 2 ? (sur_on ? v2s : v2) : (dim == 3 ? v0_3d : v0_2d);
+    const int n = fz ? 5 : version == 2 ? (sur_on ? 9 : 8) : (dim == 3 ? 9 : 8);
     for (int q = 0; q < n; ++q)
       names[q] = src[q];
     return n;
   }
 
-  // Launch number q of one iteration.
+  // Launch number q of one iteration in the context's form.
   void
   launch_stage(int q, const Buffers<R> & B)
+  {
+    if (fused && fused_ok())
+    {
+      if (q == 0)
+        return launch_boundaries(B.Uin, 0);
+      if (q == 1)
+        return launch_dt_only(B.Uin, 0);
+      if (q == 2)
+        return launch_finalize(0);
+      if (q == 3)
+        return launch_fused(B);
+      return launch_advance();
+    }
+    launch_stage_plain(q, B);
+  }
+
+  // Launch number q of one iteration of the stage kernels.
+  void
+  launch_stage_plain(int q, const Buffers<R> & B)
   {
     if (q == 0)
       return launch_boundaries(B.Uin, 0);
@@ -804,6 +1009,8 @@ public:
   int
   step() override
   {
+    if (int rc = tune_form())
+      return rc;
     enqueue_step((int)(launched & 1));
     ++launched;
     return check_launch();
@@ -840,6 +1047,8 @@ public:
       err = "dt must be positive and finite";
       return MHD_ERR_INVALID_ARG;
     }
+    if (int rc = tune_form())
+      return rc;
     const Buffers<R> B = buffers((int)(launched & 1));
     const char *     names[kMaxLaunches];
     const int        n = step_kernel_names(names);
@@ -855,6 +1064,8 @@ public:
   int
   run(int nsteps, int * done) override
   {
+    if (int rc = tune_form())
+      return rc;
     if (int rc = build_graphs())
       return rc;
     if (int rc = read_state())
@@ -920,7 +1131,7 @@ public:
   // bitwise the same; only the order of the CFL atomics differs, and their
   // maximum is order-independent.
   int
-  enqueue_step_host(int parity, const void * in_host, void * out_host, int nslab)
+  make_copy_stream()
   {
     if (!copy_stream)
     {
@@ -931,6 +1142,98 @@ public:
       for (cudaEvent_t & e : up_ev)
         MHD_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
+    return MHD_OK;
+  }
+
+  // The host-buffer step of the fused form (2D), in nslab slabs of tile rows:
+  //  in:  slab s of U_in goes up on the second stream; the main stream fills
+  //       the ghost cells of its rows along x and reduces the CFL rates of
+  //       every interior row whose next row has arrived; after the last slab
+  //       the ghost rows, the remaining rates and dt;
+  //  out: the tile kernel runs slab by slab, each finished slab of U_out
+  //       going down while the next one computes.
+  // The same kernels on the same cells as enqueue_step: bitwise its result.
+  int
+  enqueue_step_host_fused(int parity, const void * in_host, void * out_host, int nslab)
+  {
+    if (int rc = make_copy_stream())
+      return rc;
+    const Buffers<R> B = buffers(parity);
+    const int        ns = G.ny, g = G.g, nplanes = G.jsize, ntr = fused_tile_rows();
+    const int64_t    plane = G.sj;
+    nslab = std::max(1, std::min(nslab, ntr));
+    auto t_lo = [&](int s) { return (int)((int64_t)s * ntr / nslab); }; // tile rows
+    auto u_lo = [&](int s) { return std::min(ns, t_lo(s) * FusedTile::TY); };
+    auto a_lo = [&](int s) { return s == 0 ? 0 : g + u_lo(s); };
+    auto a_hi = [&](int s) { return s == nslab - 1 ? nplanes : g + u_lo(s + 1); };
+    auto copy = [&](void * dst, const void * src, int s, cudaMemcpyKind kind) -> int {
+      for (int v = 0; v < NV; ++v)
+      {
+        const int64_t off = v * G.sv + (int64_t)a_lo(s) * plane;
+        const size_t  bytes = (size_t)(a_hi(s) - a_lo(s)) * plane * sizeof(R);
+        MHD_CK(cudaMemcpyAsync(static_cast<R *>(dst) + off, static_cast<const R *>(src) + off,
+                               bytes, kind, copy_stream));
+      }
+      return MHD_OK;
+    };
+    auto bound = [&](int p0, int p1, int reset) {
+      const int64_t n = (int64_t)(p1 - p0) * plane;
+      if (n > 0)
+        k_boundaries_range<R, 2>
+          <<<nblocks(n, 256), 256, 0, stream>>>(G, B.Uin, st, p0 * plane, p1 * plane, reset);
+    };
+    auto rates = [&](int r0, int r1) { // interior rows r0 <= row < r1 (0-based)
+      const int64_t n = (int64_t)(r1 - r0) * G.nx;
+      if (n > 0)
+        k_dt_only_range<R, 2><<<nblocks(n, 256), 256, 0, stream>>>(
+          G, B.Uin, st, (int64_t)r0 * G.nx, (int64_t)r1 * G.nx);
+    };
+    MHD_CK(cudaEventRecord(copy_ev, stream));
+    MHD_CK(cudaStreamWaitEvent(copy_stream, copy_ev, 0));
+    for (int s = 0; s < nslab; ++s)
+    {
+      if (int rc = copy(B.Uin, in_host, s, cudaMemcpyHostToDevice))
+        return rc;
+      MHD_CK(cudaEventRecord(up_ev[s], copy_stream));
+    }
+    int rdone = 0; // interior rows whose rates are reduced
+    for (int s = 0; s < nslab; ++s)
+    {
+      MHD_CK(cudaStreamWaitEvent(stream, up_ev[s], 0));
+      bound(g + u_lo(s), g + u_lo(s + 1), s == 0);
+      // a row's rate reads the face field of the next row
+      const int r1 = s == nslab - 1 ? rdone : std::max(rdone, u_lo(s + 1) - 1);
+      rates(rdone, r1);
+      rdone = r1;
+    }
+    bound(0, g, 0);
+    bound(g + ns, nplanes, 0);
+    rates(rdone, ns);
+    launch_finalize(0);
+    for (int s = 0; s < nslab; ++s)
+    {
+      launch_fused(B, t_lo(s), t_lo(s + 1));
+      MHD_CK(cudaEventRecord(slab_ev[s], stream));
+    }
+    launch_advance();
+    if (int rc = check_launch())
+      return rc;
+    for (int s = 0; s < nslab; ++s)
+    {
+      MHD_CK(cudaStreamWaitEvent(copy_stream, slab_ev[s], 0));
+      if (int rc = copy(out_host, B.Uout, s, cudaMemcpyDeviceToHost))
+        return rc;
+    }
+    MHD_CK(cudaEventRecord(copy_ev, copy_stream));
+    MHD_CK(cudaStreamWaitEvent(stream, copy_ev, 0));
+    return MHD_OK;
+  }
+
+  int
+  enqueue_step_host(int parity, const void * in_host, void * out_host, int nslab)
+  {
+    if (int rc = make_copy_stream())
+      return rc;
     const Buffers<R> B = buffers(parity);
     const int        ns = slow_cells(), g = G.g;
     const int        nplanes = dim == 3 ? G.ksize : G.jsize;
@@ -1057,6 +1360,8 @@ public:
     if (int rc = read_state())
       return rc;
     launched = st_host->it;
+    if (int rc = tune_form())
+      return rc;
     const int  nslab = host_slabs();
     const bool overlap = layout == MHD_LAYOUT_LEFT && version == 2 && nslab > 1;
     R *        out = (launched & 1) ? U : U2; // the buffer this iteration writes
@@ -1065,7 +1370,9 @@ public:
       return rc;
     if (overlap)
     {
-      if (int rc = enqueue_step_host((int)(launched & 1), Uin, Uout, nslab))
+      const int par = (int)(launched & 1);
+      if (int rc = fused ? enqueue_step_host_fused(par, Uin, Uout, nslab)
+                         : enqueue_step_host(par, Uin, Uout, nslab))
         return rc;
       ++launched;
     }
@@ -1129,6 +1436,8 @@ public:
   int
   run_timed(int nsteps, float * ms) override
   {
+    if (int rc = tune_form())
+      return rc;
     if (int rc = build_graphs())
       return rc;
     if (int rc = read_state())
@@ -1163,6 +1472,8 @@ public:
   int
   profile_step(const char ** names, float * ms, int max, int * count) override
   {
+    if (int rc = tune_form())
+      return rc;
     if (int rc = read_state())
       return rc;
     launched = st_host->it;
@@ -1224,9 +1535,18 @@ public:
     {
       MHD_CK(cudaStreamSynchronize(stream));
       drop_graphs();
+      fused = false; // the fused form has no surrogate
+      tuned = true;
       if (!wpack)
       {
         sur_on = false;
+        // the form the context had: the requested one, else the default
+        if (form_req == MHD_FORM_FUSED)
+          fused = true;
+        else if (form_req == MHD_FORM_TIMED)
+          tuned = false;
+        else if (form_req != MHD_FORM_STAGES)
+          fused = default_form();
         return MHD_OK;
       }
       if (version != 2 || G.riemann != MHD_RIEMANN_HLLD)
@@ -1328,10 +1648,10 @@ public:
     const Buffers<R> B = buffers((int)(launched & 1));
     float *          d_out = nullptr;
     MHD_CK(cudaMalloc(&d_out, nrec * mlp::kRecord * sizeof(float)));
-    launch_stage(0, B);
-    launch_stage(1, B);
-    launch_stage(2, B);
-    launch_stage(3, B);
+    launch_stage_plain(0, B);
+    launch_stage_plain(1, B);
+    launch_stage_plain(2, B);
+    launch_stage_plain(3, B);
     if (dim == 2)
       k_harvest<R, 2><<<dim3(nblocks(nslot, 128), 2), 128, 0, stream>>>(G, B, d_out, stride, nslot);
     else

@@ -262,15 +262,18 @@ def test_hydro_fused_form_equals_stage_form(mhdlib, name, kw, prec, mode):
     ini = hydro_ini(**kw)
     U0 = hydro_perturbed(m.initial_state(m.params_from_ini(ini)), 5)
     out = []
-    for fused in (True, False, None):
+    for fused in (True, False, None, "timed"):
         s = m.MHDSolver.from_ini(ini, precision=prec, fp_mode=mode)
         if fused is not None:
             s.set_fused(fused)
+        else:
+            # the configuration's default form: fused for 2D FP32
+            assert s.fused == (kw["dim"] == 2 and prec == 32)
         s.set_state(U0.astype(s.real))
-        s.run(6)  # None: the first run times both forms on a snapshot and keeps the faster
+        s.run(6)  # "timed": the first run times both forms on a snapshot and keeps the faster
         out.append((s.get_state(), s.time()))
         s.close()
-    for q in (1, 2):
+    for q in (1, 2, 3):
         if mode == m.MHD_FP_EXACT:
             # no contraction: the same operations in the same order
             assert np.array_equal(out[0][0], out[q][0])
@@ -284,13 +287,24 @@ def test_hydro_fused_form_equals_stage_form(mhdlib, name, kw, prec, mode):
             assert out[0][1][2] == out[q][1][2]
 
 
-def test_mhd_solver_has_no_fused_form(mhdlib):
+def test_form_requests(mhdlib):
+    """The 3D MHD solver has the stage form only; form values outside
+    stages / fused / timed are refused."""
     m = mhdlib
     from mhd_cases import ot_ini
 
-    s = m.MHDSolver.from_ini(ot_ini(dim=2, nx=16))
+    s = m.MHDSolver.from_ini(ot_ini(dim=3, nx=8))
     assert not s.fused
     s.set_fused(False)
     with pytest.raises(m.MHDError):
         s.set_fused(True)
+    s.set_fused("timed")
+    s.init_problem()
+    s.run(1)
+    assert not s.fused
     s.close()
+    h = m.MHDSolver.from_ini(hydro_ini(dim=2, nx=16))
+    for bad in (3, -1):
+        with pytest.raises(m.MHDError):
+            h._check(m.lib().mhd_set_fused(h.h, bad))
+    h.close()
