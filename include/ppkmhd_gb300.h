@@ -322,21 +322,26 @@ int mhd_ensemble_diagnostics(mhd_ensemble *ens, int prob, double sums[8], double
                              double *divb_max);
 
 /* Pick the threads per block of every batched kernel by timing candidates
- * on the current states, then the form (graphs or persistent, two timed
- * iterations of each on a snapshot of the states); results unchanged;
- * report = one line per candidate (may be NULL). */
+ * on the current states, then the form (graphs, persistent and, in 2D,
+ * fused: two timed iterations of each); every trial starts from a snapshot
+ * of the states taken first and restored at the end, so results are
+ * unchanged; report = one line per candidate (may be NULL). */
 int mhd_ensemble_autotune(mhd_ensemble *ens, char *report, size_t report_len);
 
 /* The form mhd_ensemble_run takes (the ensemble has no counterpart in the
  * reference).  MHD_ENSEMBLE_GRAPHS: the eight per-stage launches of an
  * iteration, each over all problems, replayed from CUDA graphs (the
- * default).  MHD_ENSEMBLE_PERSISTENT: the whole run in one cooperative
- * launch of as many blocks as are resident, the stages of every iteration
- * separated by grid-wide barriers; same kernel bodies, same states bit for
- * bit.  mhd_ensemble_autotune times both on the current states and keeps
- * the faster. */
+ * default, except for 2D FP32 ensembles).  MHD_ENSEMBLE_PERSISTENT: the
+ * whole run in one cooperative launch of as many blocks as are resident,
+ * the stages of every iteration separated by grid-wide barriers; same kernel
+ * bodies, same states bit for bit.  MHD_ENSEMBLE_FUSED (2D only; the default
+ * of 2D FP32 ensembles): the fused tile form of mhd_set_fused over all
+ * problems, five launches per iteration replayed from CUDA graphs, the same
+ * states bit for bit in the MHD_FP_EXACT build.  mhd_ensemble_autotune times
+ * the forms on the current states and keeps the fastest. */
 #define MHD_ENSEMBLE_GRAPHS 0
 #define MHD_ENSEMBLE_PERSISTENT 1
+#define MHD_ENSEMBLE_FUSED 2
 int mhd_ensemble_set_mode(mhd_ensemble *ens, int mode);
 int mhd_ensemble_get_mode(mhd_ensemble *ens, int *mode);
 

@@ -32,7 +32,7 @@ MHD_ERR_NUMERIC = -4
 MHD_ERR_PARSE = -5
 MHD_ERR_TOO_LARGE = -6
 MHD_FINISHED = 1  # mhd_step_noalloc: t >= tEnd, nothing computed
-MHD_ENSEMBLE_GRAPHS, MHD_ENSEMBLE_PERSISTENT = 0, 1
+MHD_ENSEMBLE_GRAPHS, MHD_ENSEMBLE_PERSISTENT, MHD_ENSEMBLE_FUSED = 0, 1, 2
 
 MHD_RIEMANN_APPROX, MHD_RIEMANN_LLF, MHD_RIEMANN_HLL, MHD_RIEMANN_HLLC, MHD_RIEMANN_HLLD = range(5)
 MHD_SOLVER_MHD_MUSCL, MHD_SOLVER_HYDRO_MUSCL = 0, 1
@@ -570,7 +570,7 @@ class MHDEnsemble:
         return np.array(list(sums)), l1.value, mx.value
 
     def set_mode(self, mode: int):
-        """MHD_ENSEMBLE_GRAPHS or MHD_ENSEMBLE_PERSISTENT."""
+        """MHD_ENSEMBLE_GRAPHS, MHD_ENSEMBLE_PERSISTENT or (2D) MHD_ENSEMBLE_FUSED."""
         self._check(lib().mhd_ensemble_set_mode(self.h, int(mode)))
 
     @property

@@ -2,9 +2,10 @@
 //
 // Every launch of an iteration covers all problems at once: a block map
 // assigns each CUDA block to one problem and to a block of that problem's
-// box, so one set of 8 launches advances the whole ensemble by one
-// iteration, each problem with its own CFL dt, time and stopping rule
-// (SolverBase::finished per problem).  Whole runs replay from CUDA graphs
+// box, so one set of 8 launches (5 in the fused 2D form: one block per
+// problem tile) advances the whole ensemble by one iteration, each problem
+// with its own CFL dt, time and stopping rule (SolverBase::finished per
+// problem).  Whole runs replay from CUDA graphs
 // without host synchronisation.  The launch shape (threads per block) of
 // every kernel is picked by a small autotuner that times the candidates on
 // the ensemble itself.
@@ -154,6 +155,37 @@ kb_update(const Grid<R> * Gs, const Buffers<R> * Bs, const BlockRef * map, int p
   const BlockRef            m = map[blockIdx.x];
   load_problem(v, Gs, Bs, m.p, parity);
   update_body<R, DIM>(v.G, v.B, m.b * (int64_t)blockDim.x + threadIdx.x);
+}
+
+// ---------------------------------------------------------------- fused form (2D)
+
+// The CFL reduction of the fused form over all problems: interior cells,
+// primitives computed but not stored (each tile computes its own).
+template <class R, int DIM>
+__global__ void __launch_bounds__(256)
+kb_dt_only(const Grid<R> * Gs, const Buffers<R> * Bs, const BlockRef * map, int parity)
+{
+  __shared__ ProblemView<R> v;
+  const BlockRef            m = map[blockIdx.x];
+  load_problem(v, Gs, Bs, m.p, parity);
+  prim_dt_body<R, DIM, false>(v.G, v.B.Uin, nullptr, v.B.st, 0,
+                              m.b * (int64_t)blockDim.x + threadIdx.x);
+}
+
+// One iteration of one tile of one problem per block (the block map holds
+// (problem, tile) with the tiles of a problem row by row): the
+// single-problem tile kernel's body on the problem's grid and arrays.
+template <class R, int TY, int RS>
+__global__ void __launch_bounds__(MTile<R, TY>::THREADS, MTile<R, TY>::MIN_BLOCKS)
+kb_mfused2d(const Grid<R> * Gs, const Buffers<R> * Bs, const BlockRef * map, int parity)
+{
+  __shared__ ProblemView<R>                   v;
+  extern __shared__ __align__(16) unsigned char msm_raw[];
+  const BlockRef                              m = map[blockIdx.x];
+  load_problem(v, Gs, Bs, m.p, parity);
+  const int ntx = (v.G.nx + MTile<R, TY>::TX - 1) / MTile<R, TY>::TX;
+  mfused2d_tile<R, TY, RS>(v.G, v.B.Uin, v.B.Uout, v.B.Ulo, v.B.st, m.b % ntx, m.b / ntx,
+                           msm_raw);
 }
 
 // ---------------------------------------------------------------- persistent form
@@ -342,10 +374,15 @@ public:
     K_FLUX,
     K_EMF,
     K_UPDATE,
+    K_DT,    // fused form: CFL reduction without stored primitives
+    K_FUSED, // fused form: one block per (problem, tile), 256 threads
     K_COUNT
   };
-  static constexpr const char * kKindName[K_COUNT] = { "boundaries", "prim_dt", "trace",
-                                                       "flux",       "emf",     "update" };
+  static constexpr const char * kKindName[K_COUNT] = { "boundaries", "prim_dt", "trace", "flux",
+                                                       "emf",        "update",  "dt_only",
+                                                       "fused" };
+  static constexpr int kFusedTY = sizeof(R) == 4 ? MFUSED_TILE_ROWS : 8;
+  using FusedTile = MTile<R, kFusedTY>;
 
   std::vector<mhd_params> P;
   std::vector<Grid<R>>    G;     // host copies
@@ -356,7 +393,8 @@ public:
   DevState *              st = nullptr;
   DevState *              st_host = nullptr;
   int                     dim = 2, n = 0;
-  int                     threads[K_COUNT] = { 256, 256, 128, 128, 128, 256 };
+  int                     threads[K_COUNT] = { 256, 256, 128, 128, 128, 256, 256, 256 };
+  int                     fused_rs = 0; // RIEMANN_HLLD when every problem uses it
   BlockRef *              map[K_COUNT] = {};
   unsigned                nblk[K_COUNT] = {};
   cudaStream_t            stream = nullptr;
@@ -374,6 +412,7 @@ public:
   ~EnsembleImpl() override
   {
     drop_graphs();
+    snapshot_free();
     for (auto & m : map)
       if (m)
         cudaFree(m);
@@ -434,9 +473,19 @@ public:
     case K_FLUX:
     case K_EMF:
       return g.box[BOX_FACE].count();
+    case K_FUSED: // tiles, one block of FusedTile::THREADS (= threads[K_FUSED]) each
+      return (int64_t)((g.nx + FusedTile::TX - 1) / FusedTile::TX) *
+             ((g.ny + FusedTile::TY - 1) / FusedTile::TY) * FusedTile::THREADS;
     default:
       return g.box[BOX_INTERIOR].count();
     }
+  }
+
+  // the fused form exists for 2D ensembles (every problem is version 2)
+  bool
+  fused_ok() const
+  {
+    return dim == 2;
   }
 
   int
@@ -525,8 +574,26 @@ public:
       reset_record(p);
     MHD_ECK(cudaMemcpyAsync(st, st_host, n * sizeof(DevState), cudaMemcpyHostToDevice, stream));
     for (int k = 0; k < K_COUNT; ++k)
-      if (int rc = build_map((Kind)k))
-        return rc;
+      if ((k != K_DT && k != K_FUSED) || fused_ok())
+        if (int rc = build_map((Kind)k))
+          return rc;
+    if (fused_ok())
+    {
+      fused_rs = RIEMANN_HLLD;
+      for (int p = 0; p < n; ++p)
+        if (G[p].riemann != RIEMANN_HLLD)
+          fused_rs = 0;
+      MHD_ECK(cudaFuncSetAttribute(kb_mfused2d<R, kFusedTY, RIEMANN_HLLD>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)FusedTile::SMEM));
+      MHD_ECK(cudaFuncSetAttribute(kb_mfused2d<R, kFusedTY, 0>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)FusedTile::SMEM));
+      // the default form of a 2D FP32 ensemble is the fused one (the single
+      // problem's rule); mhd_ensemble_set_mode / _autotune change it
+      if (sizeof(R) == 4)
+        run_mode = MHD_ENSEMBLE_FUSED;
+    }
     MHD_ECK(cudaStreamSynchronize(stream));
     return MHD_OK;
   }
@@ -565,6 +632,17 @@ public:
       case K_EMF:
         kb_emf<R, 2><<<dim3(nb, 1), th, 0, stream>>>(dG, dB, map[k], parity);
         break;
+      case K_DT:
+        kb_dt_only<R, 2><<<nb, th, 0, stream>>>(dG, dB, map[k], parity);
+        break;
+      case K_FUSED:
+        if (fused_rs == RIEMANN_HLLD)
+          kb_mfused2d<R, kFusedTY, RIEMANN_HLLD>
+            <<<nb, FusedTile::THREADS, FusedTile::SMEM, stream>>>(dG, dB, map[k], parity);
+        else
+          kb_mfused2d<R, kFusedTY, 0>
+            <<<nb, FusedTile::THREADS, FusedTile::SMEM, stream>>>(dG, dB, map[k], parity);
+        break;
       default:
         kb_update<R, 2><<<nb, th, 0, stream>>>(dG, dB, map[k], parity);
       }
@@ -597,6 +675,15 @@ public:
   void
   enqueue_step(int parity)
   {
+    if (run_mode == MHD_ENSEMBLE_FUSED)
+    {
+      launch_kind(K_BC, parity);
+      launch_kind(K_DT, parity);
+      kb_finalize_dt<R><<<(n + 127) / 128, 128, 0, stream>>>(dG, dB, n);
+      launch_kind(K_FUSED, parity);
+      kb_advance<R><<<(n + 127) / 128, 128, 0, stream>>>(dB, n);
+      return;
+    }
     launch_kind(K_BC, parity);
     launch_kind(K_PRIM, parity);
     kb_finalize_dt<R><<<(n + 127) / 128, 128, 0, stream>>>(dG, dB, n);
@@ -610,7 +697,7 @@ public:
   int
   launches_per_step() const override
   {
-    return 8;
+    return run_mode == MHD_ENSEMBLE_FUSED ? 5 : 8;
   }
 
   int
@@ -974,14 +1061,24 @@ public:
   int
   set_mode(int m) override
   {
-    if (m != MHD_ENSEMBLE_GRAPHS && m != MHD_ENSEMBLE_PERSISTENT)
+    if (m != MHD_ENSEMBLE_GRAPHS && m != MHD_ENSEMBLE_PERSISTENT && m != MHD_ENSEMBLE_FUSED)
     {
-      err = "mode must be MHD_ENSEMBLE_GRAPHS or MHD_ENSEMBLE_PERSISTENT";
+      err = "mode must be MHD_ENSEMBLE_GRAPHS, MHD_ENSEMBLE_PERSISTENT or MHD_ENSEMBLE_FUSED";
+      return MHD_ERR_INVALID_ARG;
+    }
+    if (m == MHD_ENSEMBLE_FUSED && !fused_ok())
+    {
+      err = "the fused ensemble form is built for 2D ensembles";
       return MHD_ERR_INVALID_ARG;
     }
     if (m == MHD_ENSEMBLE_PERSISTENT)
       if (int rc = build_persist())
         return rc;
+    if (m != run_mode)
+    {
+      MHD_ECK(cudaStreamSynchronize(stream));
+      drop_graphs(); // the graphs hold the form's launches
+    }
     run_mode = m;
     return MHD_OK;
   }
@@ -1094,9 +1191,57 @@ public:
     return MHD_OK;
   }
 
+  // Snapshot of every problem's two state arrays, FP32 low parts and
+  // record, for the autotuner's trials.
+  R *                 snap = nullptr;
+  DevState *          st_snap = nullptr;
+  std::vector<size_t> snap_off;
+
+  int
+  snapshot(bool back)
+  {
+    const int nplanes = 8 * (sizeof(R) == 4 ? 3 : 2);
+    if (!snap)
+    {
+      snap_off.assign(n + 1, 0);
+      for (int p = 0; p < n; ++p)
+        snap_off[p + 1] = snap_off[p] + (size_t)G[p].sv * nplanes;
+      MHD_ECK(cudaMalloc(&snap, snap_off[n] * sizeof(R)));
+      MHD_ECK(cudaMalloc(&st_snap, n * sizeof(DevState)));
+    }
+    for (int p = 0; p < n; ++p)
+    {
+      const size_t c = (size_t)G[p].sv * 8 * sizeof(R);
+      R *          bufs[3] = { B[p].Uin, B[p].Uout, B[p].Ulo };
+      for (int q = 0; q < nplanes / 8; ++q)
+      {
+        R * s0 = snap + snap_off[p] + (size_t)q * 8 * G[p].sv;
+        MHD_ECK(cudaMemcpyAsync(back ? bufs[q] : s0, back ? s0 : bufs[q], c,
+                                cudaMemcpyDeviceToDevice, stream));
+      }
+    }
+    MHD_ECK(cudaMemcpyAsync(back ? st : st_snap, back ? st_snap : st, n * sizeof(DevState),
+                            cudaMemcpyDeviceToDevice, stream));
+    return MHD_OK;
+  }
+
+  void
+  snapshot_free()
+  {
+    cudaStreamSynchronize(stream);
+    if (snap)
+      cudaFree(snap);
+    if (st_snap)
+      cudaFree(st_snap);
+    snap = nullptr;
+    st_snap = nullptr;
+  }
+
   // Time each launch kind with every candidate block size on the current
-  // states (kernels other than the dt bookkeeping are idempotent for a
-  // fixed input), keep the fastest, rebuild the block maps and graphs.
+  // states, keep the fastest, rebuild the block maps; then the form.  The
+  // trials rerun the update (which adds into the FP32 low parts) and advance
+  // the states, so everything is taken from a snapshot made first and
+  // restored at the end: results unchanged.
   int
   autotune(std::string & report) override
   {
@@ -1107,20 +1252,23 @@ public:
     cudaEvent_t e0, e1;
     MHD_ECK(cudaEventCreate(&e0));
     MHD_ECK(cudaEventCreate(&e1));
+    int rc = snapshot(false);
     char line[160];
     // primitives and dt are needed by the kernels downstream of them
     launch_kind(K_BC, parity);
     launch_kind(K_PRIM, parity);
     kb_finalize_dt<R><<<(n + 127) / 128, 128, 0, stream>>>(dG, dB, n);
-    for (int k = 0; k < K_COUNT; ++k)
+    for (int k = 0; k < K_COUNT && rc == MHD_OK; ++k)
     {
+      if (k == K_FUSED || (k == K_DT && !fused_ok()))
+        continue; // the tile kernel's shape is fixed
       float best = 1e30f;
       int   best_t = threads[k];
       for (int c : cand)
       {
         threads[k] = c;
-        if (int rc = build_map((Kind)k))
-          return rc;
+        if ((rc = build_map((Kind)k)) != MHD_OK)
+          break;
         launch_kind((Kind)k, parity); // warm
         MHD_ECK(cudaEventRecord(e0, stream));
         for (int r = 0; r < 3; ++r)
@@ -1129,8 +1277,8 @@ public:
         MHD_ECK(cudaEventSynchronize(e1));
         float el = 0.f;
         MHD_ECK(cudaEventElapsedTime(&el, e0, e1));
-        if (int rc = check_launch())
-          return rc;
+        if ((rc = check_launch()) != MHD_OK)
+          break;
         std::snprintf(line, sizeof line, "%s threads=%d: %.3f ms\n", kKindName[k], c, el / 3);
         report += line;
         if (el < best)
@@ -1140,68 +1288,46 @@ public:
         }
       }
       threads[k] = best_t;
-      if (int rc = build_map((Kind)k))
-        return rc;
+      if (rc == MHD_OK)
+        rc = build_map((Kind)k);
       std::snprintf(line, sizeof line, "-> %s uses %d threads per block\n", kKindName[k], best_t);
       report += line;
     }
-    drop_graphs();
-    // the work split: per-stage launches replayed from graphs, or one
-    // persistent launch with grid-wide barriers; two iterations of each on a
-    // snapshot of the states (restored afterwards), the faster one is kept
-    if (int rc = tune_mode(parity, e0, e1, report))
-      return rc;
+    // the form: per-stage launches replayed from graphs, one persistent
+    // launch with grid-wide barriers, or (2D) the fused tile form replayed
+    // from graphs; two iterations of each from the snapshot
+    if (rc == MHD_OK)
+      rc = tune_mode(parity, e0, e1, report);
+    if (rc == MHD_OK)
+      rc = snapshot(true);
+    snapshot_free();
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    // the tuning launches rewrote boundary cells and primitives of the
-    // current states only; restore the invariant of a fresh iteration
-    MHD_ECK(cudaStreamSynchronize(stream));
-    return MHD_OK;
+    if (rc != MHD_OK && err.empty())
+      err = "ensemble autotune failed";
+    return rc;
   }
 
   int
   tune_mode(int parity, cudaEvent_t e0, cudaEvent_t e1, std::string & report)
   {
-    if (int rc = build_graphs())
-      return rc;
-    if (int rc = build_persist())
-      return rc;
-    // snapshot: both state arrays, the FP32 low parts and the records
-    std::vector<size_t> off(n + 1, 0);
-    const int           nplanes = 8 * (sizeof(R) == 4 ? 3 : 2);
-    for (int p = 0; p < n; ++p)
-      off[p + 1] = off[p] + (size_t)G[p].sv * nplanes;
-    R * snap = nullptr;
-    MHD_ECK(cudaMalloc(&snap, off[n] * sizeof(R)));
-    DevState * st_snap = nullptr;
-    MHD_ECK(cudaMalloc(&st_snap, n * sizeof(DevState)));
-    auto save = [&](bool back) -> int {
-      for (int p = 0; p < n; ++p)
-      {
-        const size_t c = (size_t)G[p].sv * 8 * sizeof(R);
-        R *          bufs[3] = { B[p].Uin, B[p].Uout, B[p].Ulo };
-        for (int q = 0; q < nplanes / 8; ++q)
-        {
-          R * s0 = snap + off[p] + (size_t)q * 8 * G[p].sv;
-          MHD_ECK(cudaMemcpyAsync(back ? bufs[q] : s0, back ? s0 : bufs[q], c,
-                                  cudaMemcpyDeviceToDevice, stream));
-        }
-      }
-      MHD_ECK(cudaMemcpyAsync(back ? st : st_snap, back ? st_snap : st, n * sizeof(DevState),
-                              cudaMemcpyDeviceToDevice, stream));
-      return MHD_OK;
-    };
-    float t[2] = { 0.f, 0.f };
-    int   rc = save(false);
-    for (int m = 0; m < 2 && rc == MHD_OK; ++m)
+    const int modes[3] = { MHD_ENSEMBLE_GRAPHS, MHD_ENSEMBLE_PERSISTENT, MHD_ENSEMBLE_FUSED };
+    const int nmodes = fused_ok() ? 3 : 2;
+    float     t[3] = { 0.f, 0.f, 0.f };
+    int       rc = build_persist();
+    for (int q = 0; q < nmodes && rc == MHD_OK; ++q)
     {
+      run_mode = modes[q];
+      drop_graphs();
+      if (run_mode != MHD_ENSEMBLE_PERSISTENT && (rc = build_graphs()) != MHD_OK)
+        break;
       for (int rep = 0; rep < 2 && rc == MHD_OK; ++rep) // warm, then timed
       {
-        if ((rc = save(true)) != MHD_OK)
+        if ((rc = snapshot(true)) != MHD_OK)
           break;
         if (cudaEventRecord(e0, stream) != cudaSuccess)
           rc = MHD_ERR_CUDA;
-        if (m == 0)
+        if (run_mode != MHD_ENSEMBLE_PERSISTENT)
         {
           if (rc == MHD_OK && cudaGraphLaunch(graph_pair[parity], stream) != cudaSuccess)
             rc = MHD_ERR_CUDA;
@@ -1210,31 +1336,37 @@ public:
           rc = enqueue_persistent(parity, 2);
         if (cudaEventRecord(e1, stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess)
           rc = MHD_ERR_CUDA;
-        if (rc == MHD_OK && m == 1)
+        if (rc == MHD_OK && run_mode == MHD_ENSEMBLE_PERSISTENT)
           rc = persistent_status();
         if (rc == MHD_OK)
-          cudaEventElapsedTime(&t[m], e0, e1);
+          cudaEventElapsedTime(&t[q], e0, e1);
       }
     }
-    if (rc == MHD_OK)
-      rc = save(true);
-    cudaStreamSynchronize(stream);
-    cudaFree(snap);
-    cudaFree(st_snap);
+    drop_graphs();
     if (rc != MHD_OK)
     {
-      if (err.empty())
-        err = "autotune of the ensemble form failed";
+      run_mode = MHD_ENSEMBLE_GRAPHS;
       return rc;
     }
-    char line[200];
+    char line[240];
     std::snprintf(line, sizeof line,
                   "form graphs: %.3f ms per iteration; persistent (%d blocks x %d threads): %.3f ms "
-                  "per iteration\n",
+                  "per iteration",
                   t[0] / 2, pgrid, kPersistThreads, t[1] / 2);
     report += line;
-    run_mode = t[1] < t[0] ? MHD_ENSEMBLE_PERSISTENT : MHD_ENSEMBLE_GRAPHS;
-    report += run_mode == MHD_ENSEMBLE_PERSISTENT ? "-> form persistent\n" : "-> form graphs\n";
+    int best = 0;
+    for (int q = 1; q < nmodes; ++q)
+      if (t[q] < t[best])
+        best = q;
+    if (nmodes == 3)
+    {
+      std::snprintf(line, sizeof line, "; fused tiles: %.3f ms per iteration", t[2] / 2);
+      report += line;
+    }
+    run_mode = modes[best];
+    report += run_mode == MHD_ENSEMBLE_PERSISTENT ? "\n-> form persistent\n"
+              : run_mode == MHD_ENSEMBLE_FUSED    ? "\n-> form fused\n"
+                                                  : "\n-> form graphs\n";
     return MHD_OK;
   }
 
@@ -1251,6 +1383,36 @@ public:
       MHD_ECK(cudaEventCreate(&e));
     static const char * kNames[8] = { "kb_boundaries", "kb_prim_dt", "kb_finalize_dt", "kb_trace",
                                       "kb_flux",       "kb_emf",     "kb_update",      "kb_advance" };
+    if (run_mode == MHD_ENSEMBLE_FUSED)
+    {
+      static const char * kf[5] = { "kb_boundaries", "kb_dt_only", "kb_finalize_dt",
+                                    "kb_mfused2d", "kb_advance" };
+      MHD_ECK(cudaEventRecord(ev[0], stream));
+      launch_kind(K_BC, parity);
+      MHD_ECK(cudaEventRecord(ev[1], stream));
+      launch_kind(K_DT, parity);
+      MHD_ECK(cudaEventRecord(ev[2], stream));
+      kb_finalize_dt<R><<<(n + 127) / 128, 128, 0, stream>>>(dG, dB, n);
+      MHD_ECK(cudaEventRecord(ev[3], stream));
+      launch_kind(K_FUSED, parity);
+      MHD_ECK(cudaEventRecord(ev[4], stream));
+      kb_advance<R><<<(n + 127) / 128, 128, 0, stream>>>(dB, n);
+      MHD_ECK(cudaEventRecord(ev[5], stream));
+      if (int rc = check_launch())
+        return rc;
+      MHD_ECK(cudaEventSynchronize(ev[5]));
+      for (int q = 0; q < 5 && q < max; ++q)
+      {
+        MHD_ECK(cudaEventElapsedTime(&ms[q], ev[q], ev[q + 1]));
+        if (names)
+          names[q] = kf[q];
+      }
+      for (auto & e : ev)
+        cudaEventDestroy(e);
+      if (count)
+        *count = 5;
+      return MHD_OK;
+    }
     MHD_ECK(cudaEventRecord(ev[0], stream));
     launch_kind(K_BC, parity);
     MHD_ECK(cudaEventRecord(ev[1], stream));

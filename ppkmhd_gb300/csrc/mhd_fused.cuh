@@ -29,8 +29,16 @@
 
 #include "mhd_kernels.cuh"
 
+// FP32 tiles are 32 x MFUSED_TILE_ROWS cells with one thread per cell;
+// MFUSED_MIN_BLOCKS blocks of 32 x 8 per SM (the register bound the compiler
+// keeps to: 64 per thread), fewer of the taller tiles for the same warps.
+// 32 x 16 tiles of 512 threads recompute less halo but measured 3.6 %
+// slower on GB300 (Kelvin-Helmholtz 4096^2: 1.776 against 1.714 ms).
 #ifndef MFUSED_MIN_BLOCKS
 #  define MFUSED_MIN_BLOCKS 4
+#endif
+#ifndef MFUSED_TILE_ROWS
+#  define MFUSED_TILE_ROWS 8
 #endif
 
 namespace mhd
@@ -42,7 +50,9 @@ template <class R, int TY_>
 struct MTile
 {
   static constexpr int TX = 32, TY = TY_;
-  static constexpr int THREADS = 256;
+  static constexpr int THREADS = TX * TY; // one thread per tile cell
+  // blocks per SM the FP32 kernels are compiled for (the same 32 warps)
+  static constexpr int MIN_BLOCKS = sizeof(R) == 4 ? MFUSED_MIN_BLOCKS * 8 / TY : 1;
   // primitives and face fields: tile + 2 halo layers
   static constexpr int MX = TX + 4, MY = TY + 4, NM = MX * MY;
   // slopes and half-step primitives: tile + 1 halo layer
@@ -114,18 +124,19 @@ face_field_y2(R b, R e_lo, R e_hi, R dtdx)
     return rn_add(b, rn_mul(rn_sub(e_lo, e_hi), R(0.5) * dtdx));
 }
 
-// RS: the Riemann solver fixed at compile time (RIEMANN_HLLD, the common
-// case: the other solvers' code is left out of the kernel), or 0 for the
-// run-time choice of G.riemann
+// One iteration of tile (tx, ty) of a problem (the block's whole work; smem:
+// MTile::SMEM bytes of dynamic shared memory).  RS: the Riemann solver fixed
+// at compile time (RIEMANN_HLLD, the common case: the other solvers' code is
+// left out of the kernel), or 0 for the run-time choice of G.riemann.
 template <class R, int TY, int RS>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? MFUSED_MIN_BLOCKS : 1)
-k_mfused2d(const Grid<R> G, const R * __restrict__ Uin, R * __restrict__ Uout,
-           R * __restrict__ Ulo, const DevState * __restrict__ st, int row0)
+__device__ __forceinline__ void
+mfused2d_tile(const Grid<R> & G, const R * __restrict__ Uin, R * __restrict__ Uout,
+              R * __restrict__ Ulo, const DevState * __restrict__ st, int tx, int ty,
+              unsigned char * msm_raw)
 {
   using T = MTile<R, TY>;
   if (step_finished(st))
     return;
-  extern __shared__ __align__(16) unsigned char msm_raw[];
   R * As = reinterpret_cast<R *>(msm_raw); // primitives [NV][NM], later the fluxes
   R * Ua = As + T::NA;                      // face field B_x [NM]
   R * Ub = Ua + T::NM;                      // face field B_y [NM]
@@ -134,8 +145,7 @@ k_mfused2d(const Grid<R> G, const R * __restrict__ Uin, R * __restrict__ Uout,
   R * S1s = S0s + NV * T::NT;               // slopes along y [NV][NT]
   R * Es = S1s + NV * T::NT;                // edge field [NE]
   const int g = G.g;
-  // tile row row0 + blockIdx.y (a launch may cover a range of tile rows)
-  const int i0 = g + blockIdx.x * T::TX, j0 = g + (row0 + (int)blockIdx.y) * T::TY;
+  const int i0 = g + tx * T::TX, j0 = g + ty * T::TY;
   const int tid = threadIdx.x;
   const int64_t sv = G.sv, sj = G.sj;
   R dtdx, dtdy, dtdz;
@@ -441,6 +451,18 @@ k_mfused2d(const Grid<R> G, const R * __restrict__ Uin, R * __restrict__ Uout,
     }
   }
   (void)sj;
+}
+
+// Tile (blockIdx.x, row0 + blockIdx.y) of the problem (a launch may cover a
+// range of tile rows)
+template <class R, int TY, int RS>
+__global__ void __launch_bounds__(MTile<R, TY>::THREADS, MTile<R, TY>::MIN_BLOCKS)
+k_mfused2d(const Grid<R> G, const R * __restrict__ Uin, R * __restrict__ Uout,
+           R * __restrict__ Ulo, const DevState * __restrict__ st, int row0)
+{
+  extern __shared__ __align__(16) unsigned char msm_raw[];
+  mfused2d_tile<R, TY, RS>(G, Uin, Uout, Ulo, st, (int)blockIdx.x, row0 + (int)blockIdx.y,
+                           msm_raw);
 }
 
 // The CFL reduction of the fused form: k_prim_dt over the interior cells

@@ -176,7 +176,7 @@ public:
   // default is a fixed function of the configuration (default_form), so a
   // configuration always runs the same kernels; mhd_set_fused fixes either
   // form or has the next stepping call time both (tune_form).
-  static constexpr int kFusedTY = 8;
+  static constexpr int kFusedTY = sizeof(R) == 4 ? MFUSED_TILE_ROWS : 8;
   using FusedTile = MTile<R, kFusedTY>;
   bool                 fused = false;
   bool                 tuned = true;

@@ -124,7 +124,8 @@ def test_ensemble_equals_independent_runs(mhdlib, precision, exact):
     ens = mhdlib.MHDEnsemble.from_ini([ini for ini, _ in probs])
     for q, (_, U) in enumerate(probs):
         ens.set_state(q, U)
-    assert ens.launches_per_step() == 8
+    # 2D FP32 ensembles run the fused tile form by default (5 launches)
+    assert ens.launches_per_step() == (5 if precision == 32 else 8)
     ens.run(9)
     for q, (ini, U) in enumerate(probs):
         s = mhdlib.MHDSolver.from_ini(ini)
@@ -208,8 +209,13 @@ def test_ensemble_batched_state_calls_match_per_problem_calls(mhdlib, layout):
 
 
 @pytest.mark.gpu
-def test_ensemble_autotune_keeps_results(mhdlib):
-    probs = [workloads.ensemble_problem(s, precision=64, fp_mode="exact") for s in _small_specs()]
+@pytest.mark.parametrize("precision,fp", [(64, "exact"), (32, "fast")])
+def test_ensemble_autotune_keeps_results(mhdlib, precision, fp):
+    """Autotuning (block sizes, then the form) leaves the states, the FP32
+    low parts and the records as they were: afterwards the run continues
+    exactly as in an ensemble that was not tuned and takes the same form."""
+    probs = [workloads.ensemble_problem(s, precision=precision, fp_mode=fp)
+             for s in _small_specs()]
     a = mhdlib.MHDEnsemble.from_ini([ini for ini, _ in probs])
     b = mhdlib.MHDEnsemble.from_ini([ini for ini, _ in probs])
     for q, (_, U) in enumerate(probs):
@@ -219,6 +225,7 @@ def test_ensemble_autotune_keeps_results(mhdlib):
     b.run(2)
     report = a.autotune()
     assert "uses" in report and "emf" in report
+    b.set_mode(a.mode)
     a.run(5)
     b.run(5)
     for q in range(len(probs)):
@@ -283,6 +290,7 @@ def test_persistent_form_equals_graph_form(mhdlib, precision, exact):
     for q, (_, U) in enumerate(probs):
         a.set_state(q, U)
         b.set_state(q, U)
+    a.set_mode(mhdlib.MHD_ENSEMBLE_GRAPHS)
     b.set_mode(mhdlib.MHD_ENSEMBLE_PERSISTENT)
     assert a.mode == mhdlib.MHD_ENSEMBLE_GRAPHS and b.mode == mhdlib.MHD_ENSEMBLE_PERSISTENT
     a.run(7)
@@ -310,6 +318,7 @@ def test_persistent_barrier_wait_limit_reports_and_recovers(mhdlib):
     for q, (_, U) in enumerate(probs):
         ref.set_state(q, U)
         ens.set_state(q, U)
+    ref.set_mode(mhdlib.MHD_ENSEMBLE_GRAPHS)
     ref.run(3)
     ens.set_mode(mhdlib.MHD_ENSEMBLE_PERSISTENT)
     ens.set_wait_limit(0)
@@ -332,9 +341,60 @@ def test_autotune_times_both_forms(mhdlib):
         ens.set_state(q, U)
     before = [ens.get_state(q) for q in range(len(probs))]
     report = ens.autotune()
-    assert "form graphs:" in report and "persistent" in report
-    assert ens.mode in (mhdlib.MHD_ENSEMBLE_GRAPHS, mhdlib.MHD_ENSEMBLE_PERSISTENT)
+    assert "form graphs:" in report and "persistent" in report and "fused tiles" in report
+    assert ens.mode in (mhdlib.MHD_ENSEMBLE_GRAPHS, mhdlib.MHD_ENSEMBLE_PERSISTENT,
+                        mhdlib.MHD_ENSEMBLE_FUSED)
     # tuning leaves the states as they were
     for q in range(len(probs)):
         assert np.array_equal(mhdlib.interior(ens.get_state(q)), mhdlib.interior(before[q]))
         assert ens.time(q)[2] == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,exact", [(64, True), (64, False), (32, False)])
+def test_fused_ensemble_form(mhdlib, precision, exact):
+    """The fused tile form over all problems: the FMA-free build gives the
+    per-stage graph form's states bit for bit and those of independent
+    single-problem runs in the fused form; the FMA builds agree to
+    round-off."""
+    fp = "exact" if exact else "fast"
+    probs = [workloads.ensemble_problem(s, precision=precision, fp_mode=fp) for s in _small_specs()]
+    a = mhdlib.MHDEnsemble.from_ini([ini for ini, _ in probs])
+    b = mhdlib.MHDEnsemble.from_ini([ini for ini, _ in probs])
+    for q, (_, U) in enumerate(probs):
+        a.set_state(q, U)
+        b.set_state(q, U)
+    a.set_mode(mhdlib.MHD_ENSEMBLE_GRAPHS)
+    b.set_mode(mhdlib.MHD_ENSEMBLE_FUSED)
+    assert b.launches_per_step() == 5 and a.launches_per_step() == 8
+    a.run(7)
+    b.run(4)
+    b.run(3)
+    for q, (ini, U) in enumerate(probs):
+        s = mhdlib.MHDSolver.from_ini(ini)
+        s.set_fused(True)
+        s.set_state(U.astype(s.real))
+        s.run(7)
+        ga, gb = a.get_state(q), b.get_state(q)
+        if exact:
+            assert np.array_equal(ga, gb), q
+            assert a.time(q) == b.time(q)
+            assert np.array_equal(gb, s.get_state()), q
+        else:
+            tol = 1e-13 if precision == 64 else 2e-6
+            assert rel_l1(ga.astype(np.float64), gb.astype(np.float64)).max() <= tol, q
+            assert rel_l1(gb.astype(np.float64), s.get_state().astype(np.float64)).max() <= tol
+            assert a.time(q)[2] == b.time(q)[2]
+        s.close()
+    # (profile_step runs a real iteration)
+    names = [k for k, _ in b.profile_step()]
+    assert names == ["kb_boundaries", "kb_dt_only", "kb_finalize_dt", "kb_mfused2d", "kb_advance"]
+
+
+@pytest.mark.gpu
+def test_fused_ensemble_form_is_2d_only(mhdlib):
+    ini = ot_ini(dim=3, nx=8)
+    ens = mhdlib.MHDEnsemble.from_ini([ini, ini])
+    with pytest.raises(mhdlib.MHDError):
+        ens.set_mode(mhdlib.MHD_ENSEMBLE_FUSED)
+    assert ens.mode == mhdlib.MHD_ENSEMBLE_GRAPHS
