@@ -637,8 +637,8 @@ k_hbound(const HGrid<R> G, R * __restrict__ U, DevState * st, int force)
   const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (idx == 0)
     st->invdt_bits = 0ull;
-  int i, j, k;
-  if (!box_cell(G.box[BOX_ALL], idx, i, j, k))
+  int i, j, k; // idx enumerates the ghost cells only
+  if (!ghost_cell<R, DIM>(G, idx, i, j, k))
     return;
   const int  g = G.g;
   const bool gx = i < g || i >= G.nx + g;
@@ -959,42 +959,53 @@ k_hupdate(const HGrid<R> G, const R * __restrict__ Uin, R * __restrict__ Uout,
 // ---------------------------------------------------------------- fused form
 
 // The CFL reduction of the fused form (no primitive array is written): the
-// rates of the interior cells as k_hprim_dt computes them; ghost cells of
-// U_in, just filled by k_hbound, are copied to U_out (the reference's
-// deep_copy(data_out, data_in) of the ghost layers; the tile kernel writes
-// the interior).
+// rates of the interior cells as k_hprim_dt computes them, kHdtCells cells
+// per thread in the first nrate blocks; the ghost cells of U_in, just
+// filled by k_hbound, are copied to U_out by the blocks after them (the
+// reference's deep_copy(data_out, data_in) of the ghost layers; the tile
+// kernel writes the interior).
+constexpr int kHdtCells = 4;
+
 template <class R, int DIM>
 __global__ void __launch_bounds__(256)
-k_hdt(const HGrid<R> G, const R * __restrict__ U, R * __restrict__ Uout, DevState * st, int force)
+k_hdt(const HGrid<R> G, const R * __restrict__ U, R * __restrict__ Uout, DevState * st, int force,
+      unsigned nrate)
 {
   if (!force && step_finished(st))
     return;
   constexpr int NVAR = DIM + 2;
-  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  R             rate = R(0);
-  bool          bad = false;
-  int           i, j, k;
-  if (box_cell(G.box[BOX_ALL], idx, i, j, k))
+  if (blockIdx.x >= nrate)
   {
+    // the ghost layers copied to U_out (blocks nrate.. of the launch)
+    int i, j, k;
+    if (!Uout ||
+        !ghost_cell<R, DIM>(G, (blockIdx.x - nrate) * (int64_t)blockDim.x + threadIdx.x, i, j, k))
+      return;
     const int64_t c = hcell(G, i, j, k);
-    const int     g = G.g;
-    const bool    interior = i >= g && i < G.nx + g && j >= g && j < G.ny + g &&
-                          (DIM == 2 || (k >= g && k < G.nz + g));
-    if (interior)
+#pragma unroll
+    for (int v = 0; v < NVAR; ++v)
+      Uout[c + v * G.sv] = U[c + v * G.sv];
+    return;
+  }
+  // the rates of kHdtCells interior cells per thread (blocks 0..nrate-1)
+  R    rate = R(0);
+  bool bad = false;
+#pragma unroll
+  for (int q = 0; q < kHdtCells; ++q)
+  {
+    int i, j, k;
+    if (box_cell(G.box[BOX_INTERIOR], (blockIdx.x * (int64_t)kHdtCells + q) * blockDim.x +
+                                        threadIdx.x, i, j, k))
     {
-      R u[MAXV], q[MAXV], cs;
+      const int64_t c = hcell(G, i, j, k);
+      R             u[MAXV], qv[MAXV], cs;
 #pragma unroll
       for (int v = 0; v < NVAR; ++v)
         u[v] = U[c + v * G.sv];
-      hprim<R, DIM>(G, u, cs, q);
-      rate = hrate<R, DIM>(G, q, cs, c);
-      bad = !(u[ID] > R(0)) || !isfinite(u[IP]);
-    }
-    else if (Uout)
-    {
-#pragma unroll
-      for (int v = 0; v < NVAR; ++v)
-        Uout[c + v * G.sv] = U[c + v * G.sv];
+      hprim<R, DIM>(G, u, cs, qv);
+      const R r = hrate<R, DIM>(G, qv, cs, c);
+      rate = r > rate ? r : rate;
+      bad = bad || !(u[ID] > R(0)) || !isfinite(u[IP]);
     }
   }
   __shared__ R red[32];
@@ -1106,9 +1117,25 @@ k_hfused(const HGrid<R> G, const R * __restrict__ U, R * __restrict__ Uout, cons
 
   // 2. slopes and sources over the tile and 1 halo layer
   constexpr int mstr[3] = { 1, T::MX, T::MX * T::MY };
-  for (int sidx = tid; sidx < T::NS; sidx += T::THREADS)
+  // (2D: warps on 32-column rows of the item grid, contiguous shared-memory
+  // reads whatever the row pitch; ItemGrid)
+  using IS = ItemGrid<T::SX, T::SY>;
+  for (int w = tid; w < (DIM == 2 ? IS::COUNT : T::NS); w += T::THREADS)
   {
-    const int a = sidx % T::SX, b = (sidx / T::SX) % T::SY, cz = sidx / (T::SX * T::SY);
+    int a, b, cz = 0, sidx;
+    if constexpr (DIM == 2)
+    {
+      if (!IS::at(w, a, b))
+        continue;
+      sidx = a + T::SX * b;
+    }
+    else
+    {
+      sidx = w;
+      a = sidx % T::SX;
+      b = (sidx / T::SX) % T::SY;
+      cz = sidx / (T::SX * T::SY);
+    }
     const int m = (a + 1) + T::MX * ((b + 1) + T::MY * (DIM == 3 ? cz + 1 : 0));
     R         q[MAXV], dq[DIM][MAXV], src[MAXV];
 #pragma unroll
@@ -1145,9 +1172,23 @@ k_hfused(const HGrid<R> G, const R * __restrict__ U, R * __restrict__ Uout, cons
     constexpr int NFD = FX * FY * FZ;
     constexpr int off = D == 0 ? 0 : D == 1 ? T::NF0 : T::NF0 + T::NF1;
     constexpr int sstr[3] = { 1, T::SX, T::SX * T::SY };
-    for (int f = tid; f < NFD; f += T::THREADS)
+    using IF = ItemGrid<FX, FY>;
+    for (int w = tid; w < (DIM == 2 ? IF::COUNT : NFD); w += T::THREADS)
     {
-      const int a = f % FX, b = (f / FX) % FY, cz = f / (FX * FY);
+      int a, b, cz = 0, f;
+      if constexpr (DIM == 2)
+      {
+        if (!IF::at(w, a, b))
+          continue;
+        f = a + FX * b;
+      }
+      else
+      {
+        f = w;
+        a = f % FX;
+        b = (f / FX) % FY;
+        cz = f / (FX * FY);
+      }
       // the face's right cell in the slopes box and in the primitives box
       const int sc_ = (a + 1) + T::SX * ((b + 1) + T::SY * (DIM == 3 ? cz + 1 : 0));
       const int mc = (a + 2) + T::MX * ((b + 2) + T::MY * (DIM == 3 ? cz + 2 : 0));

@@ -298,9 +298,9 @@ public:
   launch_bound(R * arr, int force)
   {
     if (dim == 2)
-      k_hbound<R, 2><<<nblocks(ncell, 256), 256, 0, stream>>>(G, arr, st, force);
+      k_hbound<R, 2><<<nblocks(ghost_count<R, 2>(G), 256), 256, 0, stream>>>(G, arr, st, force);
     else
-      k_hbound<R, 3><<<nblocks(ncell, 256), 256, 0, stream>>>(G, arr, st, force);
+      k_hbound<R, 3><<<nblocks(ghost_count<R, 3>(G), 256), 256, 0, stream>>>(G, arr, st, force);
   }
   void
   launch_prim_dt(const R * arr, int force)
@@ -345,10 +345,13 @@ public:
   void
   launch_dt(const R * in, R * out, int force)
   {
+    const unsigned nr = nblocks(G.box[BOX_INTERIOR].count(), 256 * kHdtCells);
     if (dim == 2)
-      k_hdt<R, 2><<<nblocks(ncell, 256), 256, 0, stream>>>(G, in, out, st, force);
+      k_hdt<R, 2><<<nr + nblocks(ghost_count<R, 2>(G), 256), 256, 0, stream>>>(G, in, out, st,
+                                                                                force, nr);
     else
-      k_hdt<R, 3><<<nblocks(ncell, 256), 256, 0, stream>>>(G, in, out, st, force);
+      k_hdt<R, 3><<<nr + nblocks(ghost_count<R, 3>(G), 256), 256, 0, stream>>>(G, in, out, st,
+                                                                                force, nr);
   }
   void
   launch_fused(const R * in, R * out)

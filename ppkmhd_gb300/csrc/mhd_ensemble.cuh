@@ -160,7 +160,8 @@ kb_update(const Grid<R> * Gs, const Buffers<R> * Bs, const BlockRef * map, int p
 // ---------------------------------------------------------------- fused form (2D)
 
 // The CFL reduction of the fused form over all problems: interior cells,
-// primitives computed but not stored (each tile computes its own).
+// primitives computed but not stored (each tile computes its own), kDtCells
+// cells per thread.
 template <class R, int DIM>
 __global__ void __launch_bounds__(256)
 kb_dt_only(const Grid<R> * Gs, const Buffers<R> * Bs, const BlockRef * map, int parity)
@@ -168,8 +169,7 @@ kb_dt_only(const Grid<R> * Gs, const Buffers<R> * Bs, const BlockRef * map, int 
   __shared__ ProblemView<R> v;
   const BlockRef            m = map[blockIdx.x];
   load_problem(v, Gs, Bs, m.p, parity);
-  prim_dt_body<R, DIM, false>(v.G, v.B.Uin, nullptr, v.B.st, 0,
-                              m.b * (int64_t)blockDim.x + threadIdx.x);
+  dt_cells_body<R, DIM, kDtCells>(v.G, v.B.Uin, v.B.st, 0, m.b);
 }
 
 // One iteration of one tile of one problem per block (the block map holds
@@ -465,7 +465,7 @@ public:
     switch (k)
     {
     case K_BC:
-      return g.box[BOX_ALL].count();
+      return g.dim == 3 ? ghost_count<R, 3>(g) : ghost_count<R, 2>(g);
     case K_PRIM:
       return g.box[BOX_PRIM].count();
     case K_TRACE:
@@ -473,6 +473,8 @@ public:
     case K_FLUX:
     case K_EMF:
       return g.box[BOX_FACE].count();
+    case K_DT: // kDtCells cells per thread
+      return (g.box[BOX_INTERIOR].count() + kDtCells - 1) / kDtCells;
     case K_FUSED: // tiles, one block of FusedTile::THREADS (= threads[K_FUSED]) each
       return (int64_t)((g.nx + FusedTile::TX - 1) / FusedTile::TX) *
              ((g.ny + FusedTile::TY - 1) / FusedTile::TY) * FusedTile::THREADS;
@@ -754,7 +756,8 @@ public:
     // a state from the host has zero low parts
     if (B[p].Ulo)
       MHD_ECK(cudaMemsetAsync(B[p].Ulo, 0, (size_t)g.sv * NV * sizeof(R), stream));
-    const int64_t   nall = g.box[BOX_ALL].count(), nprim = g.box[BOX_PRIM].count();
+    const int64_t   nall = dim == 3 ? ghost_count<R, 3>(g) : ghost_count<R, 2>(g),
+                    nprim = g.box[BOX_PRIM].count();
     if (dim == 2)
     {
       k_boundaries<R, 2><<<(unsigned)((nall + 255) / 256), 256, 0, stream>>>(g, B[p].Uin, B[p].st, 1);
@@ -897,7 +900,7 @@ public:
       return rc;
     R *             cur = current(p);
     const Grid<R> & g = G[p];
-    const int64_t   nall = g.box[BOX_ALL].count();
+    const int64_t   nall = dim == 3 ? ghost_count<R, 3>(g) : ghost_count<R, 2>(g);
     // ghost refresh from the interior: the next iteration starts with the same fill
     if (dim == 2)
       k_boundaries<R, 2><<<blocks_for(nall, 256), 256, 0, stream>>>(g, cur, B[p].st, 1);
@@ -921,7 +924,7 @@ public:
     {
       R *             cur = current(p);
       const Grid<R> & g = G[p];
-      const int64_t   nall = g.box[BOX_ALL].count();
+      const int64_t   nall = dim == 3 ? ghost_count<R, 3>(g) : ghost_count<R, 2>(g);
       if (dim == 2)
         k_boundaries<R, 2><<<blocks_for(nall, 256), 256, 0, stream>>>(g, cur, B[p].st, 1);
       else
@@ -951,7 +954,7 @@ public:
     const unsigned  nb = std::min(1024u, blocks_for(g.box[BOX_INTERIOR].count(), 256));
     double *        partial = reinterpret_cast<double *>(B[p].S);
     double *        out = partial + (size_t)nb * 10;
-    const int64_t   nall = g.box[BOX_ALL].count();
+    const int64_t   nall = dim == 3 ? ghost_count<R, 3>(g) : ghost_count<R, 2>(g);
     if (dim == 2)
     {
       k_boundaries<R, 2><<<blocks_for(nall, 256), 256, 0, stream>>>(g, current(p), B[p].st, 1);

@@ -69,39 +69,6 @@ struct MTile
   static constexpr size_t SMEM = sizeof(R) * (size_t)NREAL;
 };
 
-// The items of a W x H grid (W >= 32) in warp order: the first 32 columns
-// row by row, one row per warp, so that a warp reads a contiguous run of a
-// shared-memory row (no bank conflicts whatever the row pitch), then the
-// W - 32 remaining columns; the count is rounded up to whole warps, so that
-// consecutive item ranges start on a warp boundary.
-template <int W, int H>
-struct ItemGrid
-{
-  static constexpr int MAIN = 32 * H, XW = W - 32;
-  static constexpr int COUNT = MAIN + (XW * H + 31) / 32 * 32;
-  __device__ __forceinline__ static bool
-  at(int w, int & a, int & b)
-  {
-    if (w < MAIN)
-    {
-      a = w & 31;
-      b = w >> 5;
-      return true;
-    }
-    if constexpr (XW == 0)
-      return false;
-    else
-    {
-      w -= MAIN;
-      if (w >= XW * H)
-        return false;
-      a = 32 + w % XW;
-      b = w / XW;
-      return true;
-    }
-  }
-};
-
 // half-step normal field of an x face (B_x + (E(j+1) - E(j)) dt/(2 dy)) and
 // of a y face (B_y - (E(i+1) - E(i)) dt/(2 dx)) from the values; the same
 // expressions as face_field
@@ -465,14 +432,16 @@ k_mfused2d(const Grid<R> G, const R * __restrict__ Uin, R * __restrict__ Uout,
                            msm_raw);
 }
 
-// The CFL reduction of the fused form: k_prim_dt over the interior cells
-// without storing the primitives (the tile kernel computes its own).
+// The CFL reduction of the fused form: the rates of the interior cells
+// without storing the primitives (the tile kernel computes its own),
+// kDtCells cells per thread.
+constexpr int kDtCells = 4;
+
 template <class R, int DIM>
 __global__ void __launch_bounds__(256)
 k_dt_only(const Grid<R> G, const R * __restrict__ U, DevState * st, int force)
 {
-  prim_dt_body<R, DIM, false>(G, U, nullptr, st, force,
-                              blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+  dt_cells_body<R, DIM, kDtCells>(G, U, st, force, blockIdx.x);
 }
 
 // interior cells base <= index < end (threads past end still join the block

@@ -233,6 +233,39 @@ box_cell(const Box & b, int64_t idx, int & i, int & j, int & k)
   return true;
 }
 
+// The items of a W x H grid (W >= 32) in warp order: the first 32 columns
+// row by row, one row per warp, so that a warp reads a contiguous run of a
+// shared-memory row (no bank conflicts whatever the row pitch), then the
+// W - 32 remaining columns; the count is rounded up to whole warps, so that
+// consecutive item ranges start on a warp boundary.
+template <int W, int H>
+struct ItemGrid
+{
+  static constexpr int MAIN = 32 * H, XW = W - 32;
+  static constexpr int COUNT = MAIN + (XW * H + 31) / 32 * 32;
+  __device__ __forceinline__ static bool
+  at(int w, int & a, int & b)
+  {
+    if (w < MAIN)
+    {
+      a = w & 31;
+      b = w >> 5;
+      return true;
+    }
+    if constexpr (XW == 0)
+      return false;
+    else
+    {
+      w -= MAIN;
+      if (w >= XW * H)
+        return false;
+      a = 32 + w % XW;
+      b = w / XW;
+      return true;
+    }
+  }
+};
+
 template <class R>
 struct Grid
 {
@@ -287,23 +320,11 @@ bc_source(int c, int n, int g, int type, bool hi, bool & flip)
 // the full extent of the other axes; a ghost cell therefore ends up with the
 // interior value at the composition of the per-axis source maps, multiplied
 // by the per-axis reflection signs (normal velocity and normal field).
+// Interior cells are left alone.
 template <class R, int DIM>
 __device__ __forceinline__ void
-boundaries_body(const Grid<R> & G, R * __restrict__ U, DevState * st, int force, int64_t idx,
-                bool first)
+fill_ghost(const Grid<R> & G, R * __restrict__ U, int i, int j, int k)
 {
-  if (!force && step_finished(st))
-    return;
-  if (first)
-  {
-    st->invdt_bits = 0ull; // reset the CFL reduction of this iteration
-    st->ptmax_bits = 0u;
-    st->ptmin_bits = 0x7f800000u; // +inf
-  }
-  const Box & b = G.box[BOX_ALL];
-  int       i, j, k;
-  if (!box_cell(b, idx, i, j, k))
-    return;
   const int g = G.g;
   const bool gx = i < g || i >= G.nx + g;
   const bool gy = j < g || j >= G.ny + g;
@@ -333,6 +354,98 @@ boundaries_body(const Grid<R> & G, R * __restrict__ U, DevState * st, int force,
   }
 }
 
+// The ghost cells of the array, enumerated without the interior: the
+// ghost layers of the slowest axis whole, then the ghost rows of the
+// interior planes (3D), then the ghost columns of the interior rows.  GR:
+// any grid description with nx, ny, nz, g, isize, jsize, ksize (the MHD and
+// the hydro solvers').
+template <class R, int DIM, class GR>
+__host__ __device__ __forceinline__ int64_t
+ghost_count(const GR & G)
+{
+  const int64_t all = (int64_t)G.isize * G.jsize * (DIM == 3 ? G.ksize : 1);
+  return all - (int64_t)G.nx * G.ny * (DIM == 3 ? G.nz : 1);
+}
+
+template <class R, int DIM, class GR>
+__device__ __forceinline__ bool
+ghost_cell(const GR & G, int64_t idx, int & i, int & j, int & k)
+{
+  if (idx >= ghost_count<R, DIM>(G))
+    return false;
+  const int g = G.g, g2 = 2 * G.g;
+  // counts stay below 2^31 (grids are limited to 4e9 values)
+  unsigned x = (unsigned)idx;
+  k = 0;
+  if constexpr (DIM == 3)
+  {
+    const unsigned plane = (unsigned)(G.isize * G.jsize);
+    const unsigned nA = (unsigned)g2 * plane;
+    if (x < nA)
+    {
+      const unsigned r = x / plane, rem = x - r * plane;
+      k = (int)r < g ? (int)r : G.nz + (int)r;
+      j = (int)(rem / (unsigned)G.isize);
+      i = (int)(rem - (unsigned)j * (unsigned)G.isize);
+      return true;
+    }
+    x -= nA;
+    const unsigned nB = (unsigned)G.nz * (unsigned)g2 * (unsigned)G.isize;
+    if (x < nB)
+    {
+      const unsigned t = x / (unsigned)G.isize;
+      i = (int)(x - t * (unsigned)G.isize);
+      const unsigned kk = t / (unsigned)g2, r = t - kk * (unsigned)g2;
+      k = g + (int)kk;
+      j = (int)r < g ? (int)r : G.ny + (int)r;
+      return true;
+    }
+    x -= nB;
+    const unsigned t = x / (unsigned)g2, c = x - t * (unsigned)g2;
+    i = (int)c < g ? (int)c : G.nx + (int)c;
+    const unsigned kk = t / (unsigned)G.ny;
+    j = g + (int)(t - kk * (unsigned)G.ny);
+    k = g + (int)kk;
+    return true;
+  }
+  else
+  {
+    const unsigned nA = (unsigned)g2 * (unsigned)G.isize;
+    if (x < nA)
+    {
+      const unsigned r = x / (unsigned)G.isize;
+      i = (int)(x - r * (unsigned)G.isize);
+      j = (int)r < g ? (int)r : G.ny + (int)r;
+      return true;
+    }
+    x -= nA;
+    const unsigned t = x / (unsigned)g2, c = x - t * (unsigned)g2;
+    i = (int)c < g ? (int)c : G.nx + (int)c;
+    j = g + (int)t;
+    return true;
+  }
+}
+
+// Ghost cell number idx (0 <= idx < ghost_count) of U; first: the launch's
+// first thread, which also clears the iteration's CFL reduction.
+template <class R, int DIM>
+__device__ __forceinline__ void
+boundaries_body(const Grid<R> & G, R * __restrict__ U, DevState * st, int force, int64_t idx,
+                bool first)
+{
+  if (!force && step_finished(st))
+    return;
+  if (first)
+  {
+    st->invdt_bits = 0ull; // reset the CFL reduction of this iteration
+    st->ptmax_bits = 0u;
+    st->ptmin_bits = 0x7f800000u; // +inf
+  }
+  int i, j, k;
+  if (ghost_cell<R, DIM>(G, idx, i, j, k))
+    fill_ghost<R, DIM>(G, U, i, j, k);
+}
+
 template <class R, int DIM>
 __global__ void __launch_bounds__(256)
 k_boundaries(const Grid<R> G, R * __restrict__ U, DevState * st, int force)
@@ -350,8 +463,17 @@ k_boundaries_range(const Grid<R> G, R * __restrict__ U, DevState * st, int64_t b
                    int reset)
 {
   const int64_t idx = base + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (idx < end)
-    boundaries_body<R, DIM>(G, U, st, 0, idx, reset && blockIdx.x == 0 && threadIdx.x == 0);
+  if (idx >= end || step_finished(st))
+    return;
+  if (reset && blockIdx.x == 0 && threadIdx.x == 0)
+  {
+    st->invdt_bits = 0ull;
+    st->ptmax_bits = 0u;
+    st->ptmin_bits = 0x7f800000u;
+  }
+  int i, j, k;
+  if (box_cell(G.box[BOX_ALL], idx, i, j, k))
+    fill_ghost<R, DIM>(G, U, i, j, k);
 }
 
 // ---------------------------------------------------------------- primitives + CFL
@@ -422,85 +544,71 @@ cell_prim(const Grid<R> & G, const R * __restrict__ U, int64_t c)
   return CellPrim<R>{ d, p, vu, vv, vw, a, bb, cc, emag, invd };
 }
 
-template <class R, int DIM, bool STORE_Q = true>
+// find_speed_info<NDIM> (mhd_utils.h:319-366) of an interior cell from its
+// primitives: the CFL rate sum_d (c_fast,d + |v_d|)/dx_d (0 for NaN), the
+// FP32 total pressure p + B^2/2 (the momentum-flux shift), and whether the
+// conservative state is non-positive or non-finite.
+template <class R, int DIM>
 __device__ __forceinline__ void
-prim_dt_body(const Grid<R> & G, const R * __restrict__ U, R * __restrict__ Q, DevState * st,
-             int force, int64_t idx, int64_t end = INT64_MAX)
+cell_rate(const Grid<R> & G, const R * __restrict__ U, int64_t c, const CellPrim<R> & P,
+          R & rate, R & ptot, bool & bad)
 {
-  if (!force && step_finished(st))
-    return;
-  const Box & b = G.box[STORE_Q ? BOX_PRIM : BOX_INTERIOR];
-  int       i, j, k;
-  R         rate = R(0);
-  R         ptot = R(-1); // FP32: interior total pressure, -1 elsewhere
-  bool      bad = false;
-  if (idx < end && box_cell(b, idx, i, j, k))
+  const int64_t sv = G.sv;
+  const R d = P.d, p = P.p, vu = P.vu, vv = P.vv, vw = P.vw, a = P.a, bb = P.bb, cc = P.cc;
+  const R emag = P.emag, invd = P.invd;
+  (void)vw;
+  (void)emag;
+  const R b2 = a * a + bb * bb + cc * cc;
+  R       val;
+  if constexpr (kExactOrder)
   {
-    const int64_t c = cell_at(G, i, j, k);
-    const int64_t sv = G.sv;
-    const CellPrim<R> P = cell_prim<R, DIM>(G, U, c);
-    const R d = P.d, p = P.p, vu = P.vu, vv = P.vv, vw = P.vw, a = P.a, bb = P.bb, cc = P.cc;
-    const R emag = P.emag, invd = P.invd;
-    if constexpr (STORE_Q)
+    // 1/dx.. are the host's IEEE reciprocals (correctly rounded)
+    const R c2 = qdiv(G.gamma0 * p, d, invd);
+    const R d2 = R(0.5) * (qdiv(b2, d, invd) + c2);
+    const R sx = sqrt(d2 + sqrt(d2 * d2 - qdiv(c2 * a * a, d, invd))) + fabs(vu);
+    const R sy = sqrt(d2 + sqrt(d2 * d2 - qdiv(c2 * bb * bb, d, invd))) + fabs(vv);
+    if constexpr (DIM == 3)
     {
-      Q[c + ID * sv] = d;
-      Q[c + IP * sv] = p;
-      Q[c + IU * sv] = vu;
-      Q[c + IV * sv] = vv;
-      Q[c + IW * sv] = vw;
-      Q[c + IA * sv] = a;
-      Q[c + IB * sv] = bb;
-      Q[c + IC * sv] = cc;
+      const R sz = sqrt(d2 + sqrt(d2 * d2 - qdiv(c2 * cc * cc, d, invd))) + fabs(vw);
+      val = qdiv(sx, R(G.dx), R(G.idx)) + qdiv(sy, R(G.dy), R(G.idy)) +
+            qdiv(sz, R(G.dz), R(G.idz));
     }
-    const int g = G.g;
-    const bool interior = i >= g && i < G.isize - g && j >= g && j < G.jsize - g &&
-                          (DIM == 2 || (k >= g && k < G.ksize - g));
-    if (interior)
-    {
-      // find_speed_info<NDIM> (mhd_utils.h:319-366)
-      const R b2 = a * a + bb * bb + cc * cc;
-      R       val;
-      if constexpr (kExactOrder)
-      {
-        // 1/dx.. are the host's IEEE reciprocals (correctly rounded)
-        const R c2 = qdiv(G.gamma0 * p, d, invd);
-        const R d2 = R(0.5) * (qdiv(b2, d, invd) + c2);
-        const R sx = sqrt(d2 + sqrt(d2 * d2 - qdiv(c2 * a * a, d, invd))) + fabs(vu);
-        const R sy = sqrt(d2 + sqrt(d2 * d2 - qdiv(c2 * bb * bb, d, invd))) + fabs(vv);
-        if constexpr (DIM == 3)
-        {
-          const R sz = sqrt(d2 + sqrt(d2 * d2 - qdiv(c2 * cc * cc, d, invd))) + fabs(vw);
-          val = qdiv(sx, R(G.dx), R(G.idx)) + qdiv(sy, R(G.dy), R(G.idy)) +
-                qdiv(sz, R(G.dz), R(G.idz));
-        }
-        else
-          val = qdiv(sx, R(G.dx), R(G.idx)) + qdiv(sy, R(G.dy), R(G.idy));
-      }
-      else
-      {
-        const R c2 = G.gamma0 * p * invd;
-        const R d2 = R(0.5) * (b2 * invd + c2);
-        const R cd = c2 * invd;
-        const R sx = fsqrt(d2 + fsqrt(d2 * d2 - cd * a * a)) + fabs(vu);
-        const R sy = fsqrt(d2 + fsqrt(d2 * d2 - cd * bb * bb)) + fabs(vv);
-        if constexpr (DIM == 3)
-        {
-          const R sz = fsqrt(d2 + fsqrt(d2 * d2 - cd * cc * cc)) + fabs(vw);
-          val = sx * R(G.idx) + sy * R(G.idy) + sz * R(G.idz);
-        }
-        else
-          val = sx * R(G.idx) + sy * R(G.idy);
-      }
-      // fmax in the reference ignores NaN operands; a NaN rate is dropped
-      // (it arises legitimately when round-off makes the inner root of the
-      // fast speed slightly negative, e.g. for a field along one axis)
-      rate = (val >= R(0)) ? val : R(0);
-      if constexpr (sizeof(R) == 4)
-        ptot = p + emag;
-      const R Ein = U[c + IP * sv];
-      bad = !(U[c + ID * sv] > R(0)) || !isfinite(Ein);
-    }
+    else
+      val = qdiv(sx, R(G.dx), R(G.idx)) + qdiv(sy, R(G.dy), R(G.idy));
   }
+  else
+  {
+    const R c2 = G.gamma0 * p * invd;
+    const R d2 = R(0.5) * (b2 * invd + c2);
+    const R cd = c2 * invd;
+    const R sx = fsqrt(d2 + fsqrt(d2 * d2 - cd * a * a)) + fabs(vu);
+    const R sy = fsqrt(d2 + fsqrt(d2 * d2 - cd * bb * bb)) + fabs(vv);
+    if constexpr (DIM == 3)
+    {
+      const R sz = fsqrt(d2 + fsqrt(d2 * d2 - cd * cc * cc)) + fabs(vw);
+      val = sx * R(G.idx) + sy * R(G.idy) + sz * R(G.idz);
+    }
+    else
+      val = sx * R(G.idx) + sy * R(G.idy);
+  }
+  // fmax in the reference ignores NaN operands; a NaN rate is dropped
+  // (it arises legitimately when round-off makes the inner root of the
+  // fast speed slightly negative, e.g. for a field along one axis)
+  rate = (val >= R(0)) ? val : R(0);
+  if constexpr (sizeof(R) == 4)
+    ptot = p + emag;
+  const R Ein = U[c + IP * sv];
+  bad = !(U[c + ID * sv] > R(0)) || !isfinite(Ein);
+}
+
+// The block's part of the CFL reduction (every thread of the block calls
+// it): rate, the thread's maximum rate; thi / tlo, the bit patterns of the
+// largest / smallest positive finite FP32 total pressure it saw (0 / +inf
+// for none); bad, a non-positive or non-finite state seen.
+template <class R>
+__device__ __forceinline__ void
+reduce_dt(DevState * st, R rate, unsigned thi, unsigned tlo, bool bad)
+{
   // block max in the working precision (max is exact in any precision), then
   // one FP64 atomicMax per block; FP32 also reduces the range of the
   // positive, finite interior total pressures (bit patterns of positive
@@ -513,9 +621,8 @@ prim_dt_body(const Grid<R> & G, const R * __restrict__ U, R * __restrict__ Q, De
   unsigned  phi = 0u, plo = 0x7f800000u;
   if constexpr (sizeof(R) == 4)
   {
-    const bool ok = ptot > 0.f && ptot < INFINITY;
-    phi = __reduce_max_sync(0xffffffffu, ok ? __float_as_uint(ptot) : 0u);
-    plo = __reduce_min_sync(0xffffffffu, ok ? __float_as_uint(ptot) : 0x7f800000u);
+    phi = __reduce_max_sync(0xffffffffu, thi);
+    plo = __reduce_min_sync(0xffffffffu, tlo);
   }
   if (lane == 0)
   {
@@ -546,6 +653,92 @@ prim_dt_body(const Grid<R> & G, const R * __restrict__ U, R * __restrict__ Q, De
         atomicMin(&st->ptmin_bits, plo);
     }
   }
+}
+
+// positive finite FP32 total pressures as ordered bit patterns
+__device__ __forceinline__ void
+ptot_range(float ptot, unsigned & thi, unsigned & tlo)
+{
+  if (ptot > 0.f && ptot < INFINITY)
+  {
+    thi = max(thi, __float_as_uint(ptot));
+    tlo = min(tlo, __float_as_uint(ptot));
+  }
+}
+__device__ __forceinline__ void
+ptot_range(double, unsigned &, unsigned &)
+{
+}
+
+template <class R, int DIM, bool STORE_Q = true>
+__device__ __forceinline__ void
+prim_dt_body(const Grid<R> & G, const R * __restrict__ U, R * __restrict__ Q, DevState * st,
+             int force, int64_t idx, int64_t end = INT64_MAX)
+{
+  if (!force && step_finished(st))
+    return;
+  const Box & b = G.box[STORE_Q ? BOX_PRIM : BOX_INTERIOR];
+  int       i, j, k;
+  R         rate = R(0);
+  R         ptot = R(-1); // FP32: interior total pressure, -1 elsewhere
+  bool      bad = false;
+  if (idx < end && box_cell(b, idx, i, j, k))
+  {
+    const int64_t c = cell_at(G, i, j, k);
+    const int64_t sv = G.sv;
+    const CellPrim<R> P = cell_prim<R, DIM>(G, U, c);
+    if constexpr (STORE_Q)
+    {
+      Q[c + ID * sv] = P.d;
+      Q[c + IP * sv] = P.p;
+      Q[c + IU * sv] = P.vu;
+      Q[c + IV * sv] = P.vv;
+      Q[c + IW * sv] = P.vw;
+      Q[c + IA * sv] = P.a;
+      Q[c + IB * sv] = P.bb;
+      Q[c + IC * sv] = P.cc;
+    }
+    const int g = G.g;
+    const bool interior = i >= g && i < G.isize - g && j >= g && j < G.jsize - g &&
+                          (DIM == 2 || (k >= g && k < G.ksize - g));
+    if (interior)
+      cell_rate<R, DIM>(G, U, c, P, rate, ptot, bad);
+  }
+  unsigned thi = 0u, tlo = 0x7f800000u;
+  ptot_range(ptot, thi, tlo);
+  reduce_dt<R>(st, rate, thi, tlo, bad);
+}
+
+// The CFL reduction alone over CPT cells per thread (the cells of block blk
+// of BOX_INTERIOR, CPT consecutive runs of blockDim.x cells): more loads in
+// flight per thread and one block reduction per CPT x blockDim.x cells.
+template <class R, int DIM, int CPT>
+__device__ __forceinline__ void
+dt_cells_body(const Grid<R> & G, const R * __restrict__ U, DevState * st, int force, int64_t blk)
+{
+  if (!force && step_finished(st))
+    return;
+  const Box & b = G.box[BOX_INTERIOR];
+  R           rate = R(0);
+  unsigned    thi = 0u, tlo = 0x7f800000u;
+  bool        bad = false;
+#pragma unroll
+  for (int q = 0; q < CPT; ++q)
+  {
+    int i, j, k;
+    if (box_cell(b, (blk * CPT + q) * (int64_t)blockDim.x + threadIdx.x, i, j, k))
+    {
+      const int64_t     c = cell_at(G, i, j, k);
+      const CellPrim<R> P = cell_prim<R, DIM>(G, U, c);
+      R                 r = R(0), pt = R(-1);
+      bool              bd = false;
+      cell_rate<R, DIM>(G, U, c, P, r, pt, bd);
+      rate = r > rate ? r : rate;
+      ptot_range(pt, thi, tlo);
+      bad = bad || bd;
+    }
+  }
+  reduce_dt<R>(st, rate, thi, tlo, bad);
 }
 
 template <class R, int DIM>

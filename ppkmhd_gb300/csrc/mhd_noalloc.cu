@@ -155,14 +155,13 @@ step(const mhd_params & p, void * U_in, void * U_out, double t, double * dt, cud
     return MHD_ERR_CUDA;
   }
   k_noalloc_reset<<<1, 1, 0, s>>>(B.st, t, p.tEnd);
-  const int64_t nall = (int64_t)n;
   const int64_t nprim = (int64_t)(G.isize - 1) * (G.jsize - 1) * (dim == 3 ? G.ksize - 1 : 1);
   const int64_t ntrace = (int64_t)(G.nx + 3) * (G.ny + 3) * (dim == 3 ? G.nz + 3 : 1);
   const int64_t nface = (int64_t)(G.nx + 1) * (G.ny + 1) * (dim == 3 ? G.nz + 1 : 1);
   const int64_t ncell = (int64_t)G.nx * G.ny * (dim == 3 ? G.nz : 1);
   if (dim == 2)
   {
-    k_boundaries<R, 2><<<nb(nall, 256), 256, 0, s>>>(G, B.Uin, B.st, 0);
+    k_boundaries<R, 2><<<nb(ghost_count<R, 2>(G), 256), 256, 0, s>>>(G, B.Uin, B.st, 0);
     k_prim_dt<R, 2><<<nb(nprim, 256), 256, 0, s>>>(G, B.Uin, B.Q, B.st, 0);
     k_finalize_dt<R><<<1, 1, 0, s>>>(G, B.st, 0);
     k_trace<R, 2><<<nb(ntrace, 128), 128, 0, s>>>(G, B);
@@ -172,7 +171,7 @@ step(const mhd_params & p, void * U_in, void * U_out, double t, double * dt, cud
   }
   else
   {
-    k_boundaries<R, 3><<<nb(nall, 256), 256, 0, s>>>(G, B.Uin, B.st, 0);
+    k_boundaries<R, 3><<<nb(ghost_count<R, 3>(G), 256), 256, 0, s>>>(G, B.Uin, B.st, 0);
     k_prim_dt<R, 3><<<nb(nprim, 256), 256, 0, s>>>(G, B.Uin, B.Q, B.st, 0);
     k_finalize_dt<R><<<1, 1, 0, s>>>(G, B.st, 0);
     k_trace<R, 3><<<nb(ntrace, 128), 128, 0, s>>>(G, B);

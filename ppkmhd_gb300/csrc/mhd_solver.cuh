@@ -489,11 +489,10 @@ public:
   void
   launch_boundaries(R * arr, int force)
   {
-    const int64_t n = ncell;
     if (dim == 2)
-      k_boundaries<R, 2><<<nblocks(n, 256), 256, 0, stream>>>(G, arr, st, force);
+      k_boundaries<R, 2><<<nblocks(ghost_count<R, 2>(G), 256), 256, 0, stream>>>(G, arr, st, force);
     else
-      k_boundaries<R, 3><<<nblocks(n, 256), 256, 0, stream>>>(G, arr, st, force);
+      k_boundaries<R, 3><<<nblocks(ghost_count<R, 3>(G), 256), 256, 0, stream>>>(G, arr, st, force);
   }
   void
   launch_prim_dt(const R * arr, int force)
@@ -664,7 +663,7 @@ public:
   launch_dt_only(const R * arr, int force)
   {
     const int64_t n = (int64_t)G.nx * G.ny;
-    k_dt_only<R, 2><<<nblocks(n, 256), 256, 0, stream>>>(G, arr, st, force);
+    k_dt_only<R, 2><<<nblocks(n, 256 * kDtCells), 256, 0, stream>>>(G, arr, st, force);
   }
   int
   fused_tile_rows() const
