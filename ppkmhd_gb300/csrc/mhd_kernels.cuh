@@ -1103,8 +1103,14 @@ trace_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
     Q2[c + v * sv] = q2[v];
 }
 
+// FP32 3D: blocks of 128 threads per SM the register allocation is bounded
+// for (80 registers without a bound leave 24 warps per SM for a kernel that
+// waits on its loads)
+#ifndef MTRACE_MIN_BLOCKS
+#  define MTRACE_MIN_BLOCKS 8
+#endif
 template <class R, int DIM>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, sizeof(R) == 4 && DIM == 3 ? MTRACE_MIN_BLOCKS : 1)
 k_trace(const Grid<R> G, Buffers<R> B)
 {
   trace_body<R, DIM>(G, B, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
