@@ -318,11 +318,13 @@ public:
   }
 
   // the fused form exists for 2D implementation version 2 without the
-  // flux surrogate (its tile reads 2 halo layers: ghost >= 2)
+  // flux surrogate (its tile reads 2 halo layers: ghost >= 2; the tile rows
+  // are the launch's grid.y, at most 65535)
   bool
   fused_ok() const
   {
-    return dim == 2 && version == 2 && !sur_on && G.g >= 2;
+    return dim == 2 && version == 2 && !sur_on && G.g >= 2 &&
+           (G.ny + FusedTile::TY - 1) / FusedTile::TY <= 65535;
   }
 
   int
