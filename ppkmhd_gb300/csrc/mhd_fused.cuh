@@ -380,19 +380,42 @@ mfused2d_tile(const Grid<R> & G, const R * __restrict__ Uin, R * __restrict__ Uo
     const R       dtd[2] = { dtdx, dtdy };
     if constexpr (sizeof(R) == 4)
     {
+      // (update_fp32's arithmetic; every load before the first store)
+      int   var[NV];
+      float d[NV], h[NV], l[NV];
 #pragma unroll
       for (int q = 0; q < T::NF; ++q)
       {
-        const int v = FluxComps<2>::var(q);
-        float     d = 0.f;
-        d = d + (Fx[q * T::NFX + fx] - Fx[q * T::NFX + fx + 1]) * dtd[0];
-        d = d + (Fy[q * T::NFY + fy] - Fy[q * T::NFY + fy + T::TX]) * dtd[1];
-        add_compensated(Uout + v * sv, Ulo ? Ulo + v * sv : nullptr, c, Uin[c + v * sv], d);
+        var[q] = FluxComps<2>::var(q);
+        float x = 0.f;
+        x = x + (Fx[q * T::NFX + fx] - Fx[q * T::NFX + fx + 1]) * dtd[0];
+        x = x + (Fy[q * T::NFY + fy] - Fy[q * T::NFY + fy + T::TX]) * dtd[1];
+        d[q] = x;
       }
-      const float da = (Ems[fx + T::TX + 1] - Ems[fx]) * dtd[1];
-      const float db = (Ems[fx] - Ems[fx + 1]) * dtd[0];
-      add_compensated(Uout + IA * sv, Ulo ? Ulo + IA * sv : nullptr, c, Uin[c + IA * sv], da);
-      add_compensated(Uout + IB * sv, Ulo ? Ulo + IB * sv : nullptr, c, Uin[c + IB * sv], db);
+      var[T::NF] = IA;
+      var[T::NF + 1] = IB;
+      d[T::NF] = (Ems[fx + T::TX + 1] - Ems[fx]) * dtd[1];
+      d[T::NF + 1] = (Ems[fx] - Ems[fx + 1]) * dtd[0];
+#pragma unroll
+      for (int k = 0; k < NV; ++k)
+      {
+        h[k] = Uin[c + var[k] * sv];
+        l[k] = Ulo ? Ulo[c + var[k] * sv] : 0.f;
+      }
+#pragma unroll
+      for (int k = 0; k < NV; ++k)
+      {
+        const int64_t cv = c + var[k] * sv;
+        if (!Ulo)
+        {
+          Uout[cv] = __fadd_rn(h[k], d[k]);
+          continue;
+        }
+        float hn, ln;
+        compensated_sum(h[k], d[k], l[k], hn, ln);
+        Uout[cv] = hn;
+        Ulo[cv] = ln;
+      }
     }
     else
     {

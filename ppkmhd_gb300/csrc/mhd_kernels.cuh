@@ -1505,25 +1505,24 @@ k_emf(const Grid<R> G, Buffers<R> B, int64_t base, int64_t end)
 // is added with an error-free two-sum and the pair renormalised, so the
 // state's own rounding no longer accumulates over the iterations.  Without
 // an Ulo array (the no-allocation path) U_out = U_in + d.
+//
+// compensated_sum: h + d into the pair (hn, ln) given the low part l.
 __device__ __forceinline__ void
-add_compensated(float * hi_out, float * lo, int64_t c, float h, float d)
+compensated_sum(float h, float d, float l, float & hn, float & ln)
 {
-  if (!lo)
-  {
-    hi_out[c] = __fadd_rn(h, d);
-    return;
-  }
   // two-sum h + d = s + e exactly (Knuth), then the low parts
   const float s = __fadd_rn(h, d);
   const float bb = __fsub_rn(s, h);
   const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(d, bb));
-  const float t = __fadd_rn(e, lo[c]);
+  const float t = __fadd_rn(e, l);
   // fast two-sum renormalisation (|s| >= |t|)
-  const float hn = __fadd_rn(s, t);
-  hi_out[c] = hn;
-  lo[c] = __fsub_rn(t, __fsub_rn(hn, s));
+  hn = __fadd_rn(s, t);
+  ln = __fsub_rn(t, __fsub_rn(hn, s));
 }
 
+// Every load of the cell (fluxes, EMFs, state, low parts) is issued before
+// its first store, through restrict-qualified pointers, so that the loads
+// overlap instead of waiting for each variable's stores.
 template <int DIM>
 __device__ __forceinline__ void
 update_fp32(const Grid<float> & G, const Buffers<float> & B, int64_t c)
@@ -1533,37 +1532,65 @@ update_fp32(const Grid<float> & G, const Buffers<float> & B, int64_t c)
   dt_over_dx(B.st, dtd[0], dtd[1], dtd[2]);
   const int64_t off[3] = { 1, sj, sk };
   constexpr int NF = FluxComps<DIM>::NF;
+  constexpr int NB = DIM == 2 ? 2 : 3; // face-field components the EMFs update
+  constexpr int NU = NF + NB;          // = NV
+  const float * __restrict__ F = B.F;
+  const float * __restrict__ Em = B.Em;
+  const float * __restrict__ Uin = B.Uin;
+  float * __restrict__       Uout = B.Uout;
+  float * __restrict__       lo = B.Ulo;
+  int   var[NU];
+  float d[NU];
 #pragma unroll
   for (int q = 0; q < NF; ++q)
   {
-    const int v = FluxComps<DIM>::var(q);
-    float     d = 0.f;
+    var[q] = FluxComps<DIM>::var(q);
+    float x = 0.f;
 #pragma unroll
     for (int dd = 0; dd < DIM; ++dd)
     {
-      const float * F = B.F + ((int64_t)dd * NF + q) * sv;
-      d = d + (F[c] - F[c + off[dd]]) * dtd[dd];
+      const float * Fq = F + ((int64_t)dd * NF + q) * sv;
+      x = x + (Fq[c] - Fq[c + off[dd]]) * dtd[dd];
     }
-    add_compensated(B.Uout + v * sv, B.Ulo ? B.Ulo + v * sv : nullptr, c, B.Uin[c + v * sv], d);
+    d[q] = x;
   }
-  const float * Em = B.Em;
-  float *       lo = B.Ulo;
   if constexpr (DIM == 2)
   {
-    const float da = (Em[c + sj] - Em[c]) * dtd[1];
-    const float db = (Em[c] - Em[c + 1]) * dtd[0];
-    add_compensated(B.Uout + IA * sv, lo ? lo + IA * sv : nullptr, c, B.Uin[c + IA * sv], da);
-    add_compensated(B.Uout + IB * sv, lo ? lo + IB * sv : nullptr, c, B.Uin[c + IB * sv], db);
+    var[NF] = IA;
+    var[NF + 1] = IB;
+    d[NF] = (Em[c + sj] - Em[c]) * dtd[1];
+    d[NF + 1] = (Em[c] - Em[c + 1]) * dtd[0];
   }
   else
   {
     const float *eX = Em, *eY = Em + sv, *eZ = Em + 2 * sv;
-    const float  da = (eY[c] - eY[c + sk]) * dtd[2] + (eZ[c + sj] - eZ[c]) * dtd[1];
-    const float  db = (eX[c + sk] - eX[c]) * dtd[2] + (eZ[c] - eZ[c + 1]) * dtd[0];
-    const float  dc = (eX[c] - eX[c + sj]) * dtd[1] + (eY[c + 1] - eY[c]) * dtd[0];
-    add_compensated(B.Uout + IA * sv, lo ? lo + IA * sv : nullptr, c, B.Uin[c + IA * sv], da);
-    add_compensated(B.Uout + IB * sv, lo ? lo + IB * sv : nullptr, c, B.Uin[c + IB * sv], db);
-    add_compensated(B.Uout + IC * sv, lo ? lo + IC * sv : nullptr, c, B.Uin[c + IC * sv], dc);
+    var[NF] = IA;
+    var[NF + 1] = IB;
+    var[NF + 2] = IC;
+    d[NF] = (eY[c] - eY[c + sk]) * dtd[2] + (eZ[c + sj] - eZ[c]) * dtd[1];
+    d[NF + 1] = (eX[c + sk] - eX[c]) * dtd[2] + (eZ[c] - eZ[c + 1]) * dtd[0];
+    d[NF + 2] = (eX[c] - eX[c + sj]) * dtd[1] + (eY[c + 1] - eY[c]) * dtd[0];
+  }
+  float h[NU], l[NU];
+#pragma unroll
+  for (int k = 0; k < NU; ++k)
+  {
+    h[k] = Uin[c + var[k] * sv];
+    l[k] = lo ? lo[c + var[k] * sv] : 0.f;
+  }
+#pragma unroll
+  for (int k = 0; k < NU; ++k)
+  {
+    const int64_t cv = c + var[k] * sv;
+    if (!lo)
+    {
+      Uout[cv] = __fadd_rn(h[k], d[k]);
+      continue;
+    }
+    float hn, ln;
+    compensated_sum(h[k], d[k], l[k], hn, ln);
+    Uout[cv] = hn;
+    lo[cv] = ln;
   }
 }
 
@@ -1588,31 +1615,36 @@ update_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
   dt_over_dx(B.st, dtd[0], dtd[1], dtd[2]);
   const int64_t off[3] = { 1, sj, sk };
   constexpr int NF = FluxComps<DIM>::NF;
+  // restrict-qualified: the stores of one variable do not hold back the
+  // loads of the next
+  const R * __restrict__ Uin = B.Uin;
+  const R * __restrict__ Fl = B.F;
+  R * __restrict__       Uout = B.Uout;
 #pragma unroll
   for (int q = 0; q < NF; ++q)
   {
     const int v = FluxComps<DIM>::var(q);
-    R         x = B.Uin[c + v * sv];
+    R         x = Uin[c + v * sv];
 #pragma unroll
     for (int d = 0; d < DIM; ++d)
     {
-      const R * F = B.F + ((int64_t)d * NF + q) * sv;
+      const R * F = Fl + ((int64_t)d * NF + q) * sv;
       x += F[c] * dtd[d];
       x -= F[c + off[d]] * dtd[d];
     }
-    B.Uout[c + v * sv] = x;
+    Uout[c + v * sv] = x;
   }
-  const R *Em = B.Em;
+  const R * __restrict__ Em = B.Em;
   if constexpr (DIM == 2)
   {
-    R x = B.Uin[c + IA * sv];
+    R x = Uin[c + IA * sv];
     x -= Em[c] * dtd[1];
     x += Em[c + sj] * dtd[1];
-    B.Uout[c + IA * sv] = x;
-    x = B.Uin[c + IB * sv];
+    Uout[c + IA * sv] = x;
+    x = Uin[c + IB * sv];
     x += Em[c] * dtd[0];
     x -= Em[c + 1] * dtd[0];
-    B.Uout[c + IB * sv] = x;
+    Uout[c + IB * sv] = x;
     if constexpr (NF == 6)
     {
     }
@@ -1620,24 +1652,24 @@ update_body(const Grid<R> & G, const Buffers<R> & B, int64_t idx)
   else
   {
     const R *eX = Em, *eY = Em + sv, *eZ = Em + 2 * sv;
-    R        x = B.Uin[c + IA * sv];
+    R        x = Uin[c + IA * sv];
     x += eY[c] * dtd[2];
     x -= eY[c + sk] * dtd[2];
     x -= eZ[c] * dtd[1];
     x += eZ[c + sj] * dtd[1];
-    B.Uout[c + IA * sv] = x;
-    x = B.Uin[c + IB * sv];
+    Uout[c + IA * sv] = x;
+    x = Uin[c + IB * sv];
     x -= eX[c] * dtd[2];
     x += eX[c + sk] * dtd[2];
     x += eZ[c] * dtd[0];
     x -= eZ[c + 1] * dtd[0];
-    B.Uout[c + IB * sv] = x;
-    x = B.Uin[c + IC * sv];
+    Uout[c + IB * sv] = x;
+    x = Uin[c + IC * sv];
     x += eX[c] * dtd[1];
     x -= eX[c + sj] * dtd[1];
     x -= eY[c] * dtd[0];
     x += eY[c + 1] * dtd[0];
-    B.Uout[c + IC * sv] = x;
+    Uout[c + IC * sv] = x;
   }
 }
 

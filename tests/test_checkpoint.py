@@ -14,7 +14,7 @@ HEADER = struct.Struct("<8s8I2dq2i7d")
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("dim,precision", [(2, 64), (3, 32)])
+@pytest.mark.parametrize("dim,precision", [(2, 64), (3, 32), (2, 32)])
 def test_restart_continues_bitwise(mhdlib, tmp_path, dim, precision):
     ini = ot_ini(dim=dim, nx=32, ny=24, nz=16, precision=precision)
     a = mhdlib.MHDSolver.from_ini(ini)
