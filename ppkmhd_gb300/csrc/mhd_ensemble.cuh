@@ -538,7 +538,9 @@ public:
       const size_t cells = (size_t)G[p].sv;
       total += ((cells * planes + 63) / 64) * 64; // 256-byte aligned problems (FP32)
     }
-    MHD_ECK(cudaMalloc(&arena, total * sizeof(R)));
+    // (256 bytes of padding: the fused form's optional bulk copies of a
+    // problem's last rows, MFUSED_BULK_STAGING, may run past its last value)
+    MHD_ECK(cudaMalloc(&arena, total * sizeof(R) + 256));
     MHD_ECK(cudaMemsetAsync(arena, 0, total * sizeof(R), stream));
     MHD_ECK(cudaMalloc(&st, n * sizeof(DevState)));
     MHD_ECK(cudaMallocHost(&st_host, n * sizeof(DevState)));
@@ -1052,6 +1054,13 @@ public:
         return rc;
     if (int rc = read_records())
       return rc;
+    for (int p = 0; p < n; ++p)
+      if (st_host[p].status & STATUS_STAGING)
+      {
+        err = "problem " + std::to_string(p) +
+              ": a tile's bulk copies into shared memory did not complete within the wait bound";
+        return MHD_ERR_CUDA;
+      }
     for (int p = 0; p < n; ++p)
       if (st_host[p].status & STATUS_NUMERIC)
       {

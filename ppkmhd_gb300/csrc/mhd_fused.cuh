@@ -40,6 +40,17 @@
 #ifndef MFUSED_TILE_ROWS
 #  define MFUSED_TILE_ROWS 8
 #endif
+// 1: the tile's state rows reach shared memory by bulk copies (the TMA
+// engine, cp.async.bulk: one per variable and row, issued by a warp and
+// completed on an mbarrier) before the primitives are computed; 0 (the
+// default): each thread loads its cells' values itself.  Both give the same
+// state bit for bit; the bulk copies measured 20 % slower on GB300
+// (Kelvin-Helmholtz 4096^2 FP32: 2.05 against 1.72 ms), the block waiting
+// for its whole tile where the loads of the plain form overlap with the
+// other warps' arithmetic.
+#ifndef MFUSED_BULK_STAGING
+#  define MFUSED_BULK_STAGING 0
+#endif
 
 namespace mhd
 {
@@ -68,6 +79,55 @@ struct MTile
   static constexpr int NREAL = NA + 2 * NM + 3 * NV * NT + NE;
   static constexpr size_t SMEM = sizeof(R) * (size_t)NREAL;
 };
+
+// ---- bulk copies into shared memory (cp.async.bulk, completed on an mbarrier)
+
+__device__ __forceinline__ uint32_t
+smem_u32(const void * p)
+{
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void
+stage_bar_init(uint32_t bar)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void
+stage_expect(uint32_t bar, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+// bytes (a multiple of 16) from a 16-byte aligned global address to a
+// 16-byte aligned shared address
+__device__ __forceinline__ void
+stage_copy(uint32_t dst, const void * src, uint32_t bytes, uint32_t bar)
+{
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+               "[%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+// at most `limit` polls of the phase-0 completion; false when it ran out
+__device__ __forceinline__ bool
+stage_wait(uint32_t bar, int limit)
+{
+  uint32_t done = 0;
+  for (int it = 0; it < limit && !done; ++it)
+    asm volatile("{\n\t.reg .pred q;\n\tmbarrier.try_wait.parity.shared::cta.b64 q, [%1], 0;\n\t"
+                 "selp.u32 %0, 1, 0, q;\n\t}\n"
+                 : "=r"(done)
+                 : "r"(bar)
+                 : "memory");
+  return done != 0;
+}
+
+constexpr int kStageWaitPolls = 1 << 22;
 
 // half-step normal field of an x face (B_x + (E(j+1) - E(j)) dt/(2 dy)) and
 // of a y face (B_y - (E(i+1) - E(i)) dt/(2 dx)) from the values; the same
@@ -98,7 +158,7 @@ face_field_y2(R b, R e_lo, R e_hi, R dtdx)
 template <class R, int TY, int RS>
 __device__ __forceinline__ void
 mfused2d_tile(const Grid<R> & G, const R * __restrict__ Uin, R * __restrict__ Uout,
-              R * __restrict__ Ulo, const DevState * __restrict__ st, int tx, int ty,
+              R * __restrict__ Ulo, DevState * __restrict__ st, int tx, int ty,
               unsigned char * msm_raw)
 {
   using T = MTile<R, TY>;
@@ -121,19 +181,85 @@ mfused2d_tile(const Grid<R> & G, const R * __restrict__ Uin, R * __restrict__ Uo
   // 1. primitives and face fields of cells [i0-2, i0+TX+2) x [j0-2, j0+TY+2);
   // cells whose +1 neighbour lies beyond the array (only in a partial last
   // tile, and read by nothing the tile's interior cells need) get a neutral
-  // state
+  // state.
+#if MFUSED_BULK_STAGING
+  // The state rows arrive first by bulk copies: per variable, rows j0-2 ..
+  // j0+TY+1 (and row j0+TY+2 of B_y, the +1 neighbours' face field), each a
+  // run of SW values from the 16-byte boundary at or before column i0-2, so
+  // that it holds columns i0-2 .. i0+TX+2; rows beyond the array are not
+  // copied.  They land in the half-step region, unused until phase 2.  A
+  // copy may run past the last row of the last variable: the arrays carry
+  // 256 bytes of padding.
+  constexpr int VPC = 16 / (int)sizeof(R);                     // values per 16 bytes
+  constexpr int SW = (T::MX + 1 + VPC - 1 + VPC - 1) / VPC * VPC; // staged row width
+  constexpr int SR = T::MY + 1;                                // staged rows per variable
+  __shared__ alignas(8) unsigned long long stg_bar;
+  R * stg = reinterpret_cast<R *>((reinterpret_cast<uintptr_t>(Q2s) + 15) & ~uintptr_t(15));
+  static_assert(NV * SR * SW + VPC <= 3 * NV * T::NT, "staging fits the half-step region");
+  const int jlo = j0 - 2;
+  const int nrows = min(SR, G.jsize - jlo); // rows that exist in the array
+  auto      row_src = [&](int v, int b) { return Uin + (int64_t)(jlo + b) * sj + (i0 - 2) + v * sv; };
+  if (tid < 32)
+  {
+    // warp 0: lane 0 sets up the barrier, then the lanes issue the copies
+    const int nmain = min(nrows, T::MY);
+    const int ncopy = NV * nmain + (nrows > T::MY ? 1 : 0);
+    if (tid == 0)
+    {
+      stage_bar_init(smem_u32(&stg_bar));
+      stage_expect(smem_u32(&stg_bar), (uint32_t)ncopy * (uint32_t)(SW * sizeof(R)));
+    }
+    __syncwarp();
+    for (int k = tid; k < ncopy; k += 32)
+    {
+      const int       v = k < NV * nmain ? k / nmain : IB;
+      const int       b = k < NV * nmain ? k - v * nmain : T::MY;
+      const uintptr_t src = reinterpret_cast<uintptr_t>(row_src(v, b));
+      stage_copy(smem_u32(stg + (v * SR + b) * SW),
+                 reinterpret_cast<const void *>(src & ~uintptr_t(15)), (uint32_t)(SW * sizeof(R)),
+                 smem_u32(&stg_bar));
+    }
+  }
+  __syncthreads();
+  if (!__syncthreads_and(stage_wait(smem_u32(&stg_bar), kStageWaitPolls)))
+  {
+    // the copies did not complete within the bound: report it, give them a
+    // second bound to land, and leave the tile
+    if (tid == 0)
+      atomicOr(&st->status, STATUS_STAGING);
+    stage_wait(smem_u32(&stg_bar), kStageWaitPolls);
+    return;
+  }
+  // the first staged value of row b of variable v
+  auto staged = [&](int v, int b) {
+    const uintptr_t src = reinterpret_cast<uintptr_t>(row_src(v, b));
+    return stg + (v * SR + b) * SW + (int)((src & 15u) / sizeof(R));
+  };
+#endif
   for (int m = tid; m < T::NM; m += T::THREADS)
   {
     const int i = i0 - 2 + m % T::MX, j = j0 - 2 + m / T::MX;
     R         q[NV], fa = R(0), fb = R(0);
     if (i < G.isize - 1 && j < G.jsize - 1)
     {
+#if MFUSED_BULK_STAGING
+      const int a = m % T::MX, b = m / T::MX;
+      R         u[NV];
+#  pragma unroll
+      for (int v = 0; v < NV; ++v)
+        u[v] = staged(v, b)[a];
+      const CellPrim<R> P =
+        cell_prim_v<R, 2>(G, u, staged(IA, b)[a + 1], staged(IB, b + 1)[a], R(0));
+      fa = u[IA];
+      fb = u[IB];
+#else
       const int64_t     c = cell_at(G, i, j, 0);
       const CellPrim<R> P = cell_prim<R, 2>(G, Uin, c);
-      q[ID] = P.d; q[IP] = P.p; q[IU] = P.vu; q[IV] = P.vv; q[IW] = P.vw;
-      q[IA] = P.a; q[IB] = P.bb; q[IC] = P.cc;
       fa = Uin[c + IA * sv];
       fb = Uin[c + IB * sv];
+#endif
+      q[ID] = P.d; q[IP] = P.p; q[IU] = P.vu; q[IV] = P.vv; q[IW] = P.vw;
+      q[IA] = P.a; q[IB] = P.bb; q[IC] = P.cc;
     }
     else
     {
@@ -448,7 +574,7 @@ mfused2d_tile(const Grid<R> & G, const R * __restrict__ Uin, R * __restrict__ Uo
 template <class R, int TY, int RS>
 __global__ void __launch_bounds__(MTile<R, TY>::THREADS, MTile<R, TY>::MIN_BLOCKS)
 k_mfused2d(const Grid<R> G, const R * __restrict__ Uin, R * __restrict__ Uout,
-           R * __restrict__ Ulo, const DevState * __restrict__ st, int row0)
+           R * __restrict__ Ulo, DevState * __restrict__ st, int row0)
 {
   extern __shared__ __align__(16) unsigned char msm_raw[];
   mfused2d_tile<R, TY, RS>(G, Uin, Uout, Ulo, st, (int)blockIdx.x, row0 + (int)blockIdx.y,

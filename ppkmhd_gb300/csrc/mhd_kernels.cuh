@@ -88,7 +88,8 @@ dt_over_dx(const DevState * st, float & x, float & y, float & z)
 
 enum : int
 {
-  STATUS_NUMERIC = 1
+  STATUS_NUMERIC = 1,
+  STATUS_STAGING = 2 // a tile's bulk copies did not complete within the wait bound
 };
 
 
@@ -499,7 +500,8 @@ warp_max(T v)
 // of cell c: the cell-centred field is the mean of the cell's two faces per
 // direction (the +1 neighbour's face field is read), the density floored at
 // smallr, the pressure at d * smallp.  Shared by the stage kernels and the
-// fused tile kernel, so both evaluate the same expressions.
+// fused tile kernel, so both evaluate the same expressions (cell_prim_v: on
+// the cell's values u and the +1 neighbours' face fields nbx, nby, nbz).
 template <class R>
 struct CellPrim
 {
@@ -509,13 +511,9 @@ struct CellPrim
 
 template <class R, int DIM>
 __device__ __forceinline__ CellPrim<R>
-cell_prim(const Grid<R> & G, const R * __restrict__ U, int64_t c)
+cell_prim_v(const Grid<R> & G, const R (&u)[NV], R nbx, R nby, R nbz)
 {
-  const int64_t sv = G.sv;
-  const R       nbx = U[c + 1 + IA * sv];
-  const R       nby = U[c + G.sj + IB * sv];
-  const R       nbz = DIM == 3 ? U[c + G.sk + IC * sv] : R(0);
-  const R       d = fmax(U[c + ID * sv], G.smallr);
+  const R       d = fmax(u[ID], G.smallr);
   R             vu, vv, vw;
   // exact build: the nine quotients over d share its correctly rounded
   // reciprocal (qdiv: bit for bit the IEEE quotients); fast builds multiply
@@ -523,25 +521,40 @@ cell_prim(const Grid<R> & G, const R * __restrict__ U, int64_t c)
   const R       invd = kExactOrder ? qrcp(d) : rcp(d);
   if constexpr (kExactOrder)
   {
-    vu = qdiv(U[c + IU * sv], d, invd);
-    vv = qdiv(U[c + IV * sv], d, invd);
-    vw = qdiv(U[c + IW * sv], d, invd);
+    vu = qdiv(u[IU], d, invd);
+    vv = qdiv(u[IV], d, invd);
+    vw = qdiv(u[IW], d, invd);
   }
   else
   {
-    vu = U[c + IU * sv] * invd;
-    vv = U[c + IV * sv] * invd;
-    vw = U[c + IW * sv] * invd;
+    vu = u[IU] * invd;
+    vv = u[IV] * invd;
+    vw = u[IW] * invd;
   }
-  const R       a = R(0.5) * (U[c + IA * sv] + nbx);
-  const R       bb = R(0.5) * (U[c + IB * sv] + nby);
-  const R       cc = R(0.5) * (U[c + IC * sv] + nbz);
+  const R       a = R(0.5) * (u[IA] + nbx);
+  const R       bb = R(0.5) * (u[IB] + nby);
+  const R       cc = R(0.5) * (u[IC] + nbz);
   const R       eken = R(0.5) * (vu * vu + vv * vv + vw * vw);
   const R       emag = R(0.5) * (a * a + bb * bb + cc * cc);
-  const R       eint = kExactOrder ? qdiv(U[c + IP * sv] - emag, d, invd) - eken
-                                   : (U[c + IP * sv] - emag) * invd - eken;
+  const R       eint = kExactOrder ? qdiv(u[IP] - emag, d, invd) - eken
+                                   : (u[IP] - emag) * invd - eken;
   const R       p = fmax((G.gamma0 - R(1)) * d * eint, d * G.smallp);
   return CellPrim<R>{ d, p, vu, vv, vw, a, bb, cc, emag, invd };
+}
+
+template <class R, int DIM>
+__device__ __forceinline__ CellPrim<R>
+cell_prim(const Grid<R> & G, const R * __restrict__ U, int64_t c)
+{
+  const int64_t sv = G.sv;
+  R             u[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+    u[v] = U[c + v * sv];
+  const R nbx = U[c + 1 + IA * sv];
+  const R nby = U[c + G.sj + IB * sv];
+  const R nbz = DIM == 3 ? U[c + G.sk + IC * sv] : R(0);
+  return cell_prim_v<R, DIM>(G, u, nbx, nby, nbz);
 }
 
 // find_speed_info<NDIM> (mhd_utils.h:319-366) of an interior cell from its

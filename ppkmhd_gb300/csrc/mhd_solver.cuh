@@ -262,8 +262,10 @@ public:
     const int    nplanes_e = dim == 3 ? 3 : 1;
     const int    nf = dim == 3 ? 5 : 6;
     version = p.implementation_version;
-    MHD_CK(cudaMalloc(&U, n * NV * sizeof(R)));
-    MHD_CK(cudaMalloc(&U2, n * NV * sizeof(R)));
+    // (256 bytes of padding: the fused form's optional bulk copies of the
+    // last rows, MFUSED_BULK_STAGING, may run past the last value)
+    MHD_CK(cudaMalloc(&U, n * NV * sizeof(R) + 256));
+    MHD_CK(cudaMalloc(&U2, n * NV * sizeof(R) + 256));
     MHD_CK(cudaMalloc(&Q, n * NV * sizeof(R)));
     if (version == 2)
     {
@@ -999,6 +1001,11 @@ public:
   int
   status_check()
   {
+    if (st_host->status & STATUS_STAGING)
+    {
+      err = "a tile's bulk copies into shared memory did not complete within the wait bound";
+      return MHD_ERR_CUDA;
+    }
     if (st_host->status & STATUS_NUMERIC)
     {
       err = "non-finite or non-positive state detected (density, energy or CFL rate)";
