@@ -53,7 +53,7 @@ harvest_face(const Grid<R> & G, const Buffers<R> & B, int64_t c, float * rec)
     dr[v] = double(qR[v]);
     fl[v] = 0.0;
   }
-  riemann_hlld(dl, dr, fl, double(G.gamma0));
+  riemann_hlld(dl, dr, fl, double(G.gamma0), 1.0 / (double(G.gamma0) - 1.0));
   const double Fh[7] = { fl[ID], fl[IP], fl[IU], fl[IV], fl[IW], fl[IB], fl[IC] };
 #pragma unroll
   for (int q = 0; q < 7; ++q)
