@@ -470,6 +470,18 @@ int mhd_mlp_forward(mhd_mlp *mlp, const float *features, int64_t n, float *out);
  * wait give up at once: the way to exercise that error path. */
 #define MHD_MLP_WAIT_POLLS (1 << 20)
 int mhd_mlp_set_wait_limit(mhd_mlp *mlp, int polls);
+
+/* Kernel form of mhd_mlp_forward (both give bitwise the same outputs):
+ * MHD_MLP_FORWARD_PERSISTENT (the default) keeps SMs x resident blocks of
+ * two 128-row pipelines each, the network staged once per block, one
+ * pipeline's MMAs running while the other's rows go through the epilogue;
+ * MHD_MLP_FORWARD_TILES launches one 128-thread block per 128-row tile. */
+#define MHD_MLP_FORWARD_TILES 0
+#define MHD_MLP_FORWARD_PERSISTENT 1
+int mhd_mlp_set_forward_form(mhd_mlp *mlp, int form);
+/* Device time (CUDA events around the launch, ms) of the last
+ * mhd_mlp_forward kernel; -1 before the first. */
+int mhd_mlp_last_forward_ms(mhd_mlp *mlp, double *ms);
 const char *mhd_mlp_last_error(mhd_mlp *mlp);
 
 /* Use the network in the flux stage of an FP32, version-2, HLLD context

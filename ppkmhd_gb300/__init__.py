@@ -52,6 +52,8 @@ MHD_MLP_FEATURES = 40
 MHD_SAMPLE_FLOATS = 24
 MHD_MLP_TRAIN, MHD_MLP_CHECK = 0, 1
 MHD_MLP_WAIT_POLLS = 1 << 20
+MHD_MLP_FORWARD_TILES = 0
+MHD_MLP_FORWARD_PERSISTENT = 1
 
 
 class MHDParams(ctypes.Structure):
@@ -165,6 +167,8 @@ SIGNATURES = {
                                      ctypes.c_float, ctypes.c_float, ctypes.c_uint64, _vp]),
     "mhd_mlp_forward": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp]),
     "mhd_mlp_set_wait_limit": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "mhd_mlp_set_forward_form": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "mhd_mlp_last_forward_ms": (ctypes.c_int, [_vp, _dp]),
     "mhd_mlp_last_error": (ctypes.c_char_p, [_vp]),
     "mhd_set_surrogate": (ctypes.c_int, [_vp, _vp, ctypes.c_double]),
     "mhd_surrogate_stats": (ctypes.c_int, [_vp, _i64p, _i64p, ctypes.c_int]),

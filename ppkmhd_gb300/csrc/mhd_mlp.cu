@@ -30,6 +30,8 @@ static_assert(kParams == MHD_MLP_PARAMS, "surrogate parameter count");
 static_assert(kRecord == MHD_SAMPLE_FLOATS, "face record size");
 static_assert(kFeat == MHD_MLP_FEATURES, "face feature count");
 static_assert(kTcWaitPolls == MHD_MLP_WAIT_POLLS, "default tensor-core wait bound");
+static_assert(kFeat % 4 == 0 && kIn % 4 == 0 && kBasis % 4 == 0 && kOutUsed == 7,
+              "16-byte feature and output groups");
 
 struct mhd_mlp
 {
@@ -37,6 +39,8 @@ struct mhd_mlp
   double       gamma0 = 5.0 / 3.0;
   std::vector<float> params; // host copy of the master weights (kept in sync)
   int          wait_polls = kTcWaitPolls; // bound of the tensor-core completion waits
+  int          forward_form = MHD_MLP_FORWARD_PERSISTENT;
+  double       last_forward_ms = -1.0; // device time of the last batch forward kernel
   float *      d_params = nullptr;
   float *      d_m = nullptr;
   float *      d_v = nullptr;
@@ -333,7 +337,8 @@ k_forward_tc(const uint32_t * __restrict__ pack, const float * __restrict__ feat
   for (int q = 0; q < kBasis; ++q)
     u[q] = s < n ? feat[s * kFeat + kIn + q] : 0.f;
   uint32_t   parity = 0;
-  const bool ok = block_forward(smem, tmem, parity, f, y, polls);
+  const bool ok = block_forward<0>(smem, smem + kTcAct, mhd::umma::smem_addr(smem + kTcBar),
+                                   threadIdx.x, tmem, parity, f, y, polls);
   if (ok && s < n)
   {
     combine(y, u, Dn);
@@ -350,6 +355,97 @@ k_forward_tc(const uint32_t * __restrict__ pack, const float * __restrict__ feat
   {
     mhd::umma::fence_after_sync();
     mhd::umma::tmem_dealloc(tmem, kTcCols);
+  }
+}
+
+// The same batch forward as a persistent kernel: each 256-thread block stages
+// the network once and runs two 128-row pipelines (threads 0-127 and
+// 128-255) over the tiles 2 b + g, 2 b + g + 2 gridDim.x, ...  The pipelines
+// synchronise on their own named barriers and wait on their own mbarriers,
+// so one pipeline's MMAs run while the other moves its rows through the
+// epilogue.  Per row the arithmetic is block_forward's: the outputs are
+// bitwise those of k_forward_tc.  status[0] is set when a wait reached its
+// limit; that pipeline stops, the other finishes its tiles.
+__global__ void __launch_bounds__(kTc2Threads, 3)
+k_forward_tc2(const uint32_t * __restrict__ pack, const float * __restrict__ feat, int64_t n,
+              float * __restrict__ out, int * __restrict__ status, int polls)
+{
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int  g = threadIdx.x >> 7, r = threadIdx.x & (kTcRows - 1);
+  uint32_t * slot = reinterpret_cast<uint32_t *>(smem + kTc2Bar + 16);
+  stage_network_tc(pack, smem);
+  if (threadIdx.x == 0)
+  {
+    mhd::umma::mbar_init(mhd::umma::smem_addr(smem + kTc2Bar), 1);
+    mhd::umma::mbar_init(mhd::umma::smem_addr(smem + kTc2Bar + 8), 1);
+  }
+  if (threadIdx.x < 32)
+    mhd::umma::tmem_alloc(mhd::umma::smem_addr(slot), kTc2Cols);
+  mhd::umma::fence_before_sync();
+  __syncthreads();
+  mhd::umma::fence_after_sync();
+  const uint32_t  tmem_base = *slot;
+  const uint32_t  tmem = tmem_base + kTcCols * g;
+  unsigned char * act = smem + kTc2Act + g * kTc2ActBytes;
+  const uint32_t  mbar = mhd::umma::smem_addr(smem + kTc2Bar + 8 * g);
+  uint32_t        parity = 0;
+  bool            ok = true;
+  for (int64_t tile = 2 * (int64_t)blockIdx.x + g; tile * kTcRows < n;
+       tile += 2 * (int64_t)gridDim.x)
+  {
+    const int64_t s = tile * kTcRows + r;
+    float         f[kIn], u[kBasis], y[kOut], Dn[kOutUsed];
+    // the pipeline's next tile (its rows are one contiguous block of
+    // 128 x 160 bytes, 16-byte aligned) prefetched into L2 while this one
+    // computes
+    const int64_t next = tile + 2 * (int64_t)gridDim.x;
+    if (r == 0 && next * kTcRows < n)
+      mhd::umma::bulk_prefetch_l2(
+        feat + next * kTcRows * kFeat,
+        (uint32_t)(min((int64_t)kTcRows, n - next * kTcRows) * kFeat * sizeof(float)));
+    // the row's 40 features as ten 16-byte loads (rows are 160 bytes)
+    const float4 * f4 = reinterpret_cast<const float4 *>(feat + (s < n ? s : 0) * kFeat);
+#pragma unroll
+    for (int q4 = 0; q4 < kIn / 4; ++q4)
+    {
+      const float4 a = s < n ? __ldg(f4 + q4) : make_float4(0.f, 0.f, 0.f, 0.f);
+      f[4 * q4] = a.x;
+      f[4 * q4 + 1] = a.y;
+      f[4 * q4 + 2] = a.z;
+      f[4 * q4 + 3] = a.w;
+    }
+    ok = g == 0 ? block_forward<1>(smem, act, mbar, r, tmem, parity, f, y, polls)
+                : block_forward<2>(smem, act, mbar, r, tmem, parity, f, y, polls);
+    if (!ok)
+      break;
+    if (s < n)
+    {
+      // the odd bases (the row's last 32 bytes) only now: fewer live
+      // registers across the forward pass
+#pragma unroll
+      for (int q4 = 0; q4 < kBasis / 4; ++q4)
+      {
+        const float4 a = __ldg(f4 + kIn / 4 + q4);
+        u[4 * q4] = a.x;
+        u[4 * q4 + 1] = a.y;
+        u[4 * q4 + 2] = a.z;
+        u[4 * q4 + 3] = a.w;
+      }
+      combine(y, u, Dn);
+      float4 * o4 = reinterpret_cast<float4 *>(out + s * kTgt);
+      o4[0] = make_float4(Dn[0], Dn[1], Dn[2], Dn[3]);
+      o4[1] = make_float4(Dn[4], Dn[5], Dn[6], 0.f);
+    }
+  }
+  if (!ok && r == 0)
+    atomicOr(status, 1);
+  // both pipelines' TMEM accesses are complete before warp 0 frees it
+  mhd::umma::fence_before_sync();
+  __syncthreads();
+  if (threadIdx.x < 32)
+  {
+    mhd::umma::fence_after_sync();
+    mhd::umma::tmem_dealloc(tmem_base, kTc2Cols);
   }
 }
 
@@ -590,6 +686,24 @@ extern "C"
   }
 
   int
+  mhd_mlp_set_forward_form(mhd_mlp * m, int form)
+  {
+    if (!m || (form != MHD_MLP_FORWARD_TILES && form != MHD_MLP_FORWARD_PERSISTENT))
+      return MHD_ERR_INVALID_ARG;
+    m->forward_form = form;
+    return MHD_OK;
+  }
+
+  int
+  mhd_mlp_last_forward_ms(mhd_mlp * m, double * ms)
+  {
+    if (!m || !ms)
+      return MHD_ERR_INVALID_ARG;
+    *ms = m->last_forward_ms;
+    return MHD_OK;
+  }
+
+  int
   mhd_mlp_set_wait_limit(mhd_mlp * m, int polls)
   {
     if (!m || polls < 0)
@@ -773,10 +887,58 @@ extern "C"
     MLP_CK(cudaMemcpy(dp.p, pack.data(), pack.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     MLP_CK(cudaMemcpy(feat.p, features, (size_t)n * kFeat * sizeof(float), cudaMemcpyHostToDevice));
     MLP_CK(cudaMemset(status.p, 0, sizeof(int)));
-    k_forward_tc<<<(unsigned)((n + kTcRows - 1) / kTcRows), kTcRows, kTcSmemBytes, m->stream>>>(
-      dp.p, feat.p, n, o.p, status.p, m->wait_polls);
-    MLP_CK(cudaGetLastError());
+    const int64_t tiles = (n + kTcRows - 1) / kTcRows;
+    unsigned      grid = 0;
+    if (m->forward_form == MHD_MLP_FORWARD_PERSISTENT)
+    {
+      // every block resident at once: SMs x blocks per SM, at most one
+      // block per two tiles.  Blocks per SM from the kernel's registers, its
+      // shared memory and the SM's 512 TMEM columns (cudaOccupancy... gave 1
+      // for this kernel on GB300 where 3 fit, and a grid of one block per
+      // SM ran 8 warps per SM)
+      int                sms = 0, sm_regs = 0, sm_smem = 0, reserved = 0, sm_threads = 0;
+      cudaFuncAttributes fa{};
+      MLP_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device));
+      MLP_CK(cudaDeviceGetAttribute(&sm_regs, cudaDevAttrMaxRegistersPerMultiprocessor, m->device));
+      MLP_CK(cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor,
+                                    m->device));
+      MLP_CK(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, m->device));
+      MLP_CK(cudaDeviceGetAttribute(&sm_threads, cudaDevAttrMaxThreadsPerMultiProcessor,
+                                    m->device));
+      MLP_CK(cudaFuncSetAttribute(k_forward_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kTc2SmemBytes));
+      // the whole unified L1 as shared memory
+      MLP_CK(cudaFuncSetAttribute(k_forward_tc2, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  (int)cudaSharedmemCarveoutMaxShared));
+      MLP_CK(cudaFuncGetAttributes(&fa, k_forward_tc2));
+      const int warp_regs = ((fa.numRegs * 32 + 255) / 256) * 256; // 256-register granules
+      const int by_regs = warp_regs > 0 ? (sm_regs / warp_regs) / (kTc2Threads / 32) : 0;
+      const int by_smem = sm_smem / (kTc2SmemBytes + (int)fa.sharedSizeBytes + reserved);
+      const int per_sm = std::min({by_regs, by_smem, sm_threads / kTc2Threads, (int)(512 / kTc2Cols)});
+      if (per_sm < 1)
+        return fail(m, MHD_ERR_CUDA, "the persistent forward does not fit an SM");
+      grid = (unsigned)std::min<int64_t>((tiles + 1) / 2, (int64_t)sms * per_sm);
+    }
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    MLP_CK(cudaEventCreate(&ev[0]));
+    MLP_CK(cudaEventCreate(&ev[1]));
+    MLP_CK(cudaEventRecord(ev[0], m->stream));
+    if (m->forward_form == MHD_MLP_FORWARD_PERSISTENT)
+      k_forward_tc2<<<grid, kTc2Threads, kTc2SmemBytes, m->stream>>>(dp.p, feat.p, n, o.p,
+                                                                      status.p, m->wait_polls);
+    else
+      k_forward_tc<<<(unsigned)tiles, kTcRows, kTcSmemBytes, m->stream>>>(dp.p, feat.p, n, o.p,
+                                                                          status.p, m->wait_polls);
+    const cudaError_t launch = cudaGetLastError();
+    MLP_CK(cudaEventRecord(ev[1], m->stream));
     MLP_CK(cudaStreamSynchronize(m->stream));
+    float ms = -1.f;
+    if (launch == cudaSuccess)
+      MLP_CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    MLP_CK(launch);
+    m->last_forward_ms = ms;
     int st = 0;
     MLP_CK(cudaMemcpy(&st, status.p, sizeof(int), cudaMemcpyDeviceToHost));
     if (st)

@@ -86,6 +86,7 @@ constexpr int kTcW2 = kTcW1 + kHid * kIn * 2;    // 4096
 constexpr int kTcW3 = kTcW2 + kHid * kHid * 2;   // 12288
 constexpr int kTcWBytes = kTcW3 + kN3 * kHid * 2; // 16384
 constexpr int kTcPackWords = kTcWBytes / 4 + kBiasFloats;
+static_assert(kTcWBytes % 16 == 0 && kHid % 4 == 0 && kOut % 4 == 0, "16-byte bias groups");
 
 constexpr double kJFloor = 1e-4;
 constexpr double kTauRef = 0.1;
@@ -423,6 +424,21 @@ constexpr int      kTcSmemBytes = kTcBar + 16;
 constexpr uint32_t kTcCols = 64; // TMEM columns per block (FP32 accumulators)
 constexpr int      kTcWaitPolls = 1 << 20;
 
+// The persistent form: 256-thread blocks of two independent 128-row
+// pipelines, each with its own activation tile, mbarrier, named barrier
+// (1 + pipeline) and kTcCols TMEM columns, sharing one copy of the network
+// image.  Shared memory: image, activation tiles 0 and 1, mbarriers 0 and
+// 1, the TMEM address slot.  At most 4 blocks fit an SM by shared memory,
+// which keeps 4 x kTc2Cols within the SM's 512 TMEM columns.
+constexpr int      kTc2Threads = 2 * kTcRows;
+constexpr int      kTc2Act = kTcAct;
+constexpr int      kTc2ActBytes = kTcRows * kHid * 2;
+constexpr int      kTc2Bar = kTc2Act + 2 * kTc2ActBytes;
+constexpr int      kTc2SmemBytes = kTc2Bar + 24;
+constexpr uint32_t kTc2Cols = 2 * kTcCols;
+// (an SM has 228 KB of shared memory, of which each block reserves 1 KB)
+static_assert(5 * (kTc2SmemBytes + 1024) > 228 * 1024, "at most 4 blocks of the persistent form per SM");
+
 __device__ __forceinline__ void
 stage_network_tc(const uint32_t * __restrict__ pack, unsigned char * smem)
 {
@@ -446,11 +462,19 @@ hidden_epilogue(uint32_t trow, const float * bias, unsigned char * act, int r)
   {
     uint32_t v[32];
     umma::ld32(trow + 32 * half, v);
-    uint32_t w[16];
+    // the biases as 16-byte shared loads (the image's bias block is
+    // 16-byte aligned): a quarter of the load instructions
+    const float4 * b4 = reinterpret_cast<const float4 *>(bias + 32 * half);
+    uint32_t       w[16];
 #pragma unroll
-    for (int q = 0; q < 16; ++q)
-      w[q] = gelu_bf16x2(pack_bf16x2(__uint_as_float(v[2 * q]) + bias[32 * half + 2 * q],
-                                     __uint_as_float(v[2 * q + 1]) + bias[32 * half + 2 * q + 1]));
+    for (int q4 = 0; q4 < 8; ++q4)
+    {
+      const float4 b = b4[q4];
+      w[2 * q4] = gelu_bf16x2(pack_bf16x2(__uint_as_float(v[4 * q4]) + b.x,
+                                          __uint_as_float(v[4 * q4 + 1]) + b.y));
+      w[2 * q4 + 1] = gelu_bf16x2(pack_bf16x2(__uint_as_float(v[4 * q4 + 2]) + b.z,
+                                              __uint_as_float(v[4 * q4 + 3]) + b.w));
+    }
 #pragma unroll
     for (int kc = 0; kc < 4; ++kc)
       *reinterpret_cast<uint4 *>(act + umma::canon_offset(r, 32 * half + 8 * kc, kHid)) =
@@ -458,27 +482,47 @@ hidden_epilogue(uint32_t trow, const float * bias, unsigned char * act, int r)
   }
 }
 
-// Forward pass of 128 rows on the tensor cores, one row per thread of the
-// block (row = threadIdx.x = TMEM lane); every thread of the block must call
-// it.  x: this row's inputs; y: its raw outputs (biases included).  tmem: the
-// block's kTcCols TMEM columns; parity: the mbarrier phase to wait for next
-// (advanced by three on success).  Thread 0 issues each layer's MMAs
-// (M = 128, K = 16 per instruction) and commits them to the mbarrier; every
-// thread then moves its row from TMEM through bias and activation into the
-// next A tile.  Numerics are those of warp_forward: BF16 operands, FP32
-// accumulation, bias added in FP32, BF16 GELU.  Returns false, for every
-// thread, when a wait reached its limit: the outputs are then invalid, the
-// pending phase has been waited for once more (bounded) and the caller must
-// stop using the tile and free TMEM.  polls bounds each layer's wait (the
-// drain always allows kTcWaitPolls).
+// OR of pred over the 128 threads of one pipeline, which synchronise on the
+// named barrier kBarId (0 with a 128-thread block is __syncthreads_or).  The
+// id is a compile-time constant so that a kernel reserves only the barriers
+// it names.
+template <int kBarId>
 __device__ __forceinline__ bool
-block_forward(unsigned char * smem, uint32_t tmem, uint32_t & parity, const float (&x)[kIn],
-              float (&y)[kOut], int polls = kTcWaitPolls)
+group_sync_or(bool pred)
 {
-  const int       r = threadIdx.x;
-  unsigned char * act = smem + kTcAct;
+  uint32_t out;
+  asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\t"
+               "bar.red.or.pred q, %2, 128, p;\n\tselp.u32 %0, 1, 0, q;\n\t}\n"
+               : "=r"(out)
+               : "r"((uint32_t)pred), "n"(kBarId)
+               : "memory");
+  return out != 0;
+}
+
+// Forward pass of 128 rows on the tensor cores, one row per thread of a
+// 128-thread pipeline (row r = TMEM lane r; the pipeline's warps are four
+// consecutive warps of the block, so warp w reads lanes 32 (w % 4) ..).
+// Every thread of the pipeline must call it.  smem: the network image
+// (weights, then biases); act: the pipeline's activation tile; mbar: its
+// mbarrier; kBarId: its named barrier.  x: this row's inputs; y: its raw
+// outputs (biases included).  tmem: the pipeline's kTcCols TMEM columns;
+// parity: the mbarrier phase to wait for next (advanced by three on
+// success).  Row 0 issues each layer's MMAs (M = 128, K = 16 per
+// instruction) and commits them to the mbarrier; every thread then moves its
+// row from TMEM through bias and activation into the next A tile.  Numerics
+// are those of warp_forward: BF16 operands, FP32 accumulation, bias added in
+// FP32, BF16 GELU.  Returns false, for every thread, when a wait reached its
+// limit: the outputs are then invalid, the pending phase has been waited for
+// once more (bounded) and the caller must stop using the pipeline and free
+// TMEM.  polls bounds each layer's wait (the drain always allows
+// kTcWaitPolls).
+template <int kBarId>
+__device__ __forceinline__ bool
+block_forward(unsigned char * smem, unsigned char * act, uint32_t mbar, int r, uint32_t tmem,
+              uint32_t & parity, const float (&x)[kIn], float (&y)[kOut],
+              int polls = kTcWaitPolls)
+{
   const float *   bias = reinterpret_cast<const float *>(smem + kTcWBytes);
-  const uint32_t  mbar = umma::smem_addr(smem + kTcBar);
   const uint32_t  trow = tmem + ((uint32_t)(r & ~31) << 16); // the warp's lane quarter
   const uint32_t  a0 = umma::smem_addr(act), w0 = umma::smem_addr(smem);
 #pragma unroll
@@ -494,7 +538,7 @@ block_forward(unsigned char * smem, uint32_t tmem, uint32_t & parity, const floa
     // TMEM loads of the previous layer -> this layer's accumulator writes
     umma::fence_proxy_async();
     umma::fence_before_sync();
-    const bool failed = __syncthreads_or(!ok);
+    const bool failed = group_sync_or<kBarId>(!ok);
     umma::fence_after_sync();
     if (failed)
     {
@@ -525,14 +569,21 @@ block_forward(unsigned char * smem, uint32_t tmem, uint32_t & parity, const floa
       {
         uint32_t v[32];
         umma::ld32(trow, v);
+        const float4 * b4 = reinterpret_cast<const float4 *>(bias + 2 * kHid);
 #pragma unroll
-        for (int o = 0; o < kOut; ++o)
-          y[o] = __uint_as_float(v[o]) + bias[2 * kHid + o];
+        for (int o4 = 0; o4 < kOut / 4; ++o4)
+        {
+          const float4 b = b4[o4];
+          y[4 * o4] = __uint_as_float(v[4 * o4]) + b.x;
+          y[4 * o4 + 1] = __uint_as_float(v[4 * o4 + 1]) + b.y;
+          y[4 * o4 + 2] = __uint_as_float(v[4 * o4 + 2]) + b.z;
+          y[4 * o4 + 3] = __uint_as_float(v[4 * o4 + 3]) + b.w;
+        }
       }
     }
   }
   umma::fence_before_sync();
-  const bool failed = __syncthreads_or(!ok);
+  const bool failed = group_sync_or<kBarId>(!ok);
   umma::fence_after_sync();
   if (failed && !ok)
     umma::mbar_wait(mbar, parity, kTcWaitPolls);

@@ -136,6 +136,15 @@ fence_proxy_async()
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+// Bulk prefetch of [p, p + bytes) from global memory into L2 by the TMA
+// engine (one instruction, no completion to wait for).  p 16-byte aligned,
+// bytes a multiple of 16, the range inside one allocation.
+__device__ __forceinline__ void
+bulk_prefetch_l2(const void * p, uint32_t bytes)
+{
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 // 32 consecutive FP32 columns of this thread's TMEM lane (shape 32x32b);
 // the warp's lane quarter is in bits 16-31 of taddr.
 __device__ __forceinline__ void

@@ -126,6 +126,17 @@ class FluxMLP:
         self._check(lib().mhd_mlp_forward(self.h, f.ctypes.data, f.shape[0], out.ctypes.data))
         return out
 
+    def set_forward_form(self, form: int):
+        """Kernel of forward(): MHD_MLP_FORWARD_PERSISTENT (default) or
+        MHD_MLP_FORWARD_TILES; both give bitwise the same outputs."""
+        self._check(lib().mhd_mlp_set_forward_form(self.h, int(form)))
+
+    def last_forward_ms(self) -> float:
+        """Device time of the last forward() kernel in ms (-1 before the first)."""
+        ms = ctypes.c_double()
+        self._check(lib().mhd_mlp_last_forward_ms(self.h, ctypes.byref(ms)))
+        return ms.value
+
     def set_wait_limit(self, polls: int = MHD_MLP_WAIT_POLLS):
         """Bound of the tensor-core completion waits of forward() (0: give up
         at once, which makes forward() report the failure)."""

@@ -265,12 +265,40 @@ def test_surrogate_step_host_slabs_match_run(mhdlib):
 
 
 @pytest.mark.gpu
-def test_tensor_core_wait_limit_reports_and_recovers(mhdlib):
+@pytest.mark.parametrize("n", [1, 127, 128, 257, 1000, (1 << 20) + 77])
+def test_tensor_core_forward_forms_bitwise(mhdlib, n):
+    """The persistent two-pipeline forward and the one-tile-per-block forward
+    give bitwise the same outputs, on ragged sizes and on more tiles than
+    the persistent grid holds (each pipeline then loops over tiles)."""
+    from ppkmhd_gb300.surrogate import FluxMLP
+
+    rng = np.random.default_rng(n)
+    m = FluxMLP(seed=7)
+    P = m.params.copy()
+    P[P != 0] += rng.normal(0, 0.05, (P != 0).sum()).astype(np.float32)
+    m.params = P
+    X = rng.normal(0, 1, (n, 40)).astype(np.float32)
+    X[:, 27:32] = 0
+    m.set_forward_form(mhdlib.MHD_MLP_FORWARD_TILES)
+    y_tiles = m.forward(X)
+    assert m.last_forward_ms() > 0
+    m.set_forward_form(mhdlib.MHD_MLP_FORWARD_PERSISTENT)
+    y_pers = m.forward(X)
+    assert m.last_forward_ms() > 0
+    assert np.isfinite(y_pers).all()
+    assert np.array_equal(y_pers, y_tiles)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", [0, 1])
+def test_tensor_core_wait_limit_reports_and_recovers(mhdlib, form):
     """A tensor-core completion wait that gives up is reported as an error
-    (after the pending work drained), and the next call works again."""
+    (after the pending work drained), and the next call works again; in
+    both kernel forms."""
     from ppkmhd_gb300.surrogate import FluxMLP
 
     m = FluxMLP(seed=3)
+    m.set_forward_form(form)
     X = np.random.default_rng(1).normal(0, 1, (300, 40)).astype(np.float32)
     X[:, 27:32] = 0
     y0 = m.forward(X)
