@@ -235,7 +235,7 @@ def turbulence_3d(n: int, seed: int = 11, kmin: float = 1.0, kmax: float = 8.0,
     vx, vy, vz = random_vector(-2.0)
     kdotv = (kx * vx + ky * vy + kz * vz) / kk_safe ** 2
     vhat = [vx - kx * kdotv, vy - ky * kdotv, vz - kz * kdotv]
-    v = [irfftn(c, s=(n, n, n)) for c in vhat]
+    v = [irfftn(c, s=(n, n, n), axes=(0, 1, 2)) for c in vhat]
     del vx, vy, vz, kdotv, vhat
     norm = vrms / np.sqrt(np.mean(v[0] ** 2 + v[1] ** 2 + v[2] ** 2))
     v = [c * norm for c in v]
@@ -244,9 +244,9 @@ def turbulence_3d(n: int, seed: int = 11, kmin: float = 1.0, kmax: float = 8.0,
     # (x, y+h/2, z), Az at (x, y, z+h/2), grid points x = i / n
     ax, ay, az = random_vector(-3.0)
     half = np.pi / n  # 2 pi k * (h/2) with h = 1/n
-    A = [irfftn(ax * np.exp(1j * half * kx), s=(n, n, n)),
-         irfftn(ay * np.exp(1j * half * ky), s=(n, n, n)),
-         irfftn(az * np.exp(1j * half * kz), s=(n, n, n))]
+    A = [irfftn(ax * np.exp(1j * half * kx), s=(n, n, n), axes=(0, 1, 2)),
+         irfftn(ay * np.exp(1j * half * ky), s=(n, n, n), axes=(0, 1, 2)),
+         irfftn(az * np.exp(1j * half * kz), s=(n, n, n), axes=(0, 1, 2))]
     del ax, ay, az
     h = 1.0 / n
 
